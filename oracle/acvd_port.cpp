@@ -1,0 +1,942 @@
+// ORACLE / TEST INFRASTRUCTURE ONLY -- never linked into the product library.
+//
+// CPU restatement of ACVD's discrete Voronoi clustering path (sequential, FP64),
+// written from the behaviour of the reference files cited at each function:
+//   engine    Common/vtkUniformClustering.h            (MinimizeEnergy, ProcessOneLoop, ...)
+//   adapter   DiscreteRemeshing/vtkVerticesProcessing.h (items = vertices, edges = mesh edges)
+//   metrics   DiscreteRemeshing/vtkIsotropicMetricForClustering.h,
+//             DiscreteRemeshing/vtkQEMetricForClustering.h,
+//             DiscreteRemeshing/vtkQuadricAnisotropicMetricForClustering.h
+//   quadrics  Common/vtkQuadricTools.cxx
+//   mesh      Common/vtkSurfaceBase.cxx (edge table, vertex rings), Common/vtkSurface.cxx (areas)
+//   dual mesh DiscreteRemeshing/vtkDiscreteRemeshing.h:956-1152
+// The arithmetic follows the reference expression by expression so that, given the
+// same VTK math (oracle/restated_math.h), its results match the reference's own
+// headers compiled against oracle/shim bit for bit (tests/test_oracle_pin.py).
+// It is the checker for the CUDA path and the CPU baseline timed by bench.py.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <queue>
+#include <random>
+#include <vector>
+
+#include "restated_math.h"
+#include "port_mesh.h"
+
+namespace port {
+
+// vtkQuadricTools::ComputeDisplacement (.cxx:83-163), threshold 1e-3 (.h:36)
+static int compute_displacement(const double* Q, const double* p, double* disp, int maxUsed,
+                                double thr = 0.001) {
+    double A[3][3], U[3][3], VT[3][3], b[3], w[3], T[3][3], T2[3][3];
+    int rank_def = 0;
+    b[0] = -Q[3]; b[1] = -Q[6]; b[2] = -Q[8];
+    A[0][0] = Q[0]; A[0][1] = A[1][0] = Q[1]; A[0][2] = A[2][0] = Q[2];
+    A[1][1] = Q[4]; A[1][2] = A[2][1] = Q[5]; A[2][2] = Q[7];
+    rmath::svd3(A, U, w, VT);
+    double absw[3], maxW = -1.0;
+    for (int j = 0; j < 3; j++) { absw[j] = std::fabs(w[j]); if (absw[j] > maxW) maxW = absw[j]; }
+    const double invmaxW = 1.0 / maxW;
+    for (int i = 0; i < 3; i++) {
+        double lmax = -1; int im = -1;
+        for (int j = 0; j < 3; j++) if (lmax < absw[j]) { lmax = absw[j]; im = j; }
+        if ((absw[im] * invmaxW > thr) && (maxUsed > 0)) {
+            const double inv = 1.0 / w[im];
+            T[im][0] = U[0][im] * inv; T[im][1] = U[1][im] * inv; T[im][2] = U[2][im] * inv;
+        } else {
+            T[im][0] = T[im][1] = T[im][2] = 0; rank_def++;
+        }
+        absw[im] = -2; maxUsed--;
+    }
+    rmath::transpose33(VT, VT);
+    rmath::mul33(VT, T, T2);
+    rmath::mul33v(A, p, disp);
+    for (int i = 0; i < 3; i++) disp[i] = b[i] - disp[i];
+    rmath::mul33v(T2, disp, disp);
+    return rank_def;
+}
+
+// vtkQuadricTools::ComputeRepresentativePoint (.cxx:168-177)
+static int representative_point(const double* Q, double* p, int maxUsed) {
+    double d[3];
+    const int r = compute_displacement(Q, p, d, maxUsed);
+    for (int i = 0; i < 3; i++) p[i] += d[i];
+    return r;
+}
+
+// ClampWeights (vtkIsotropicMetricForClustering.h:273-291 and siblings)
+template <class ItemT>
+static void clamp_weights(std::vector<ItemT>& it, double ratio) {
+    double avg = 0;
+    for (auto& x : it) avg += x.w;
+    avg /= (double)it.size();
+    const double mn = avg / ratio, mx = avg * ratio;
+    for (auto& x : it) { if (x.w > mx) x.w = mx; if (x.w < mn) x.w = mn; }
+}
+
+// ---------------------------------------------------------------------------
+// Metrics (the plugin concept of the reference: Item, Cluster, Add/Sub,
+// ComputeClusterCentroid, ComputeClusterEnergy)
+// ---------------------------------------------------------------------------
+struct IsoMetric {   // vtkIsotropicMetricForClustering.h
+    struct Item { double v[3]; double w; };
+    struct Cluster { double S[3]; double W; double E; };
+    std::vector<Item> items;
+    const Mesh* mesh = nullptr;
+    double gradation = 0; const double* indicator = nullptr;
+    void set_constrained(int) {}
+    void reset(Cluster* c) const { c->S[0] = c->S[1] = c->S[2] = 0; c->W = 0; c->E = 0; }
+    double weight(idt i) const { return items[i].w; }
+    void add(idt i, Cluster* c) const {
+        const Item& I = items[i];
+        c->S[0] += I.v[0]; c->S[1] += I.v[1]; c->S[2] += I.v[2]; c->W += I.w;
+    }
+    void sub(idt i, Cluster* c) const {
+        const Item& I = items[i];
+        c->S[0] -= I.v[0]; c->S[1] -= I.v[1]; c->S[2] -= I.v[2]; c->W -= I.w;
+    }
+    void centroid(Cluster*) const {}
+    void energy(Cluster* c) const {
+        c->E = (-c->S[0] * c->S[0] - c->S[1] * c->S[1] - c->S[2] * c->S[2]) / c->W;
+    }
+    void get_centroid(const Cluster* c, double* p) const {
+        p[0] = c->S[0] / c->W; p[1] = c->S[1] / c->W; p[2] = c->S[2] / c->W;
+    }
+    void build(const Mesh& m) {   // BuildMetric, vertex items (:244-266)
+        mesh = &m;
+        items.resize(m.nV);
+        for (idt i = 0; i < m.nV; i++) {
+            const double a = m.vertex_area(i);
+            items[i].w = indicator ? a * std::pow(indicator[i], gradation) : a;
+            m.point(i, items[i].v);
+        }
+        clamp_weights(items, 100000);
+        for (auto& I : items) { I.v[0] *= I.w; I.v[1] *= I.w; I.v[2] *= I.w; }
+    }
+    void accum(const Cluster* c, double* S, double* W, double* Q) const {
+        for (int k = 0; k < 3; k++) S[k] = c->S[k];
+        *W = c->W;
+        for (int k = 0; k < 9; k++) Q[k] = 0;
+    }
+};
+
+struct QEMMetric {   // vtkQEMetricForClustering.h
+    struct Item { double Q[9]; double v[3]; double w; };
+    struct Cluster {
+        double E; double SQ[9]; double c[3]; double S[3]; double W; char rank; idt anchor;
+        Cluster() : E(0), W(0), rank(0), anchor(-1) {
+            for (double& x : SQ) x = 0; for (double& x : c) x = 0; for (double& x : S) x = 0;
+        }
+    };
+    std::vector<Item> items;
+    const Mesh* mesh = nullptr;
+    double gradation = 0; const double* indicator = nullptr;
+    int active = 1, level = 3;
+    void set_constrained(int c) { active = c; }
+    void reset(Cluster* c) const {
+        for (double& x : c->SQ) x = 0; for (double& x : c->S) x = 0; for (double& x : c->c) x = 0;
+        c->W = 0; c->E = 0;
+    }
+    double weight(idt i) const { return items[i].w; }
+    void add(idt i, Cluster* c) const {
+        const Item& I = items[i];
+        for (int k = 0; k < 3; k++) c->S[k] += I.v[k];
+        for (int k = 0; k < 9; k++) c->SQ[k] += I.Q[k];
+        c->W += I.w;
+    }
+    void sub(idt i, Cluster* c) const {
+        const Item& I = items[i];
+        for (int k = 0; k < 3; k++) c->S[k] -= I.v[k];
+        for (int k = 0; k < 9; k++) c->SQ[k] -= I.Q[k];
+        c->W -= I.w;
+        if (c->anchor == i) c->anchor = -2;
+    }
+    void centroid(Cluster* c) const {   // :268-285
+        if (c->anchor >= 0) { mesh->point(c->anchor, c->c); return; }
+        for (int k = 0; k < 3; k++) c->c[k] = c->S[k] / c->W;
+        if (!active || !level) return;
+        c->rank = (char)representative_point(c->SQ, c->c, level);
+    }
+    void energy(Cluster* c) const {     // :194-208
+        if (c->anchor == -2) { c->E = 1e100; return; }
+        c->E = (c->c[0] * c->c[0] + c->c[1] * c->c[1] + c->c[2] * c->c[2]) * c->W
+               - 2.0 * (c->c[0] * c->S[0] + c->c[1] * c->S[1] + c->c[2] * c->S[2]);
+    }
+    void get_centroid(const Cluster* c, double* p) const { for (int k = 0; k < 3; k++) p[k] = c->c[k]; }
+    void build(const Mesh& m) {   // BuildMetric, vertex items (:325-342)
+        mesh = &m;
+        items.resize(m.nV);
+        for (idt i = 0; i < m.nV; i++) {
+            items[i].w = m.vertex_area(i);
+            if (gradation > 0) items[i].w *= std::pow(indicator[i], gradation);
+        }
+        clamp_weights(items, 10000);
+        std::vector<idt> fl;
+        for (idt i = 0; i < m.nV; i++) {   // ComputeVertexQuadric (:151-167)
+            Item& I = items[i];
+            const double w = I.w;
+            for (double& x : I.Q) x = 0;
+            m.vertex_faces(i, fl);
+            for (idt f : fl) m.add_triangle_quadric(I.Q, f);
+            m.point(i, I.v);
+            for (int k = 0; k < 3; k++) I.v[k] = I.v[k] * w;
+            I.w = w;
+        }
+    }
+    void accum(const Cluster* c, double* S, double* W, double* Q) const {
+        for (int k = 0; k < 3; k++) S[k] = c->S[k];
+        *W = c->W;
+        for (int k = 0; k < 9; k++) Q[k] = c->SQ[k];
+    }
+};
+
+struct AnisoMetric {   // vtkQuadricAnisotropicMetricForClustering.h
+    struct Item { float v[3]; float w; float T[6]; float TX[3]; double Q[9]; };
+    struct Cluster {
+        double S[3]; double W; double E; double ST[6]; double STX[3]; double c[3]; double SQ[9];
+    };
+    std::vector<Item> items;
+    const Mesh* mesh = nullptr;
+    double gradation = 0; const double* indicator = nullptr; const float* pdirs = nullptr;
+    int level = 3;
+    void set_constrained(int) {}   // :61, no-op
+    void reset(Cluster* c) const { std::memset(c, 0, sizeof(Cluster)); }
+    double weight(idt i) const { return items[i].w; }
+    void add(idt i, Cluster* c) const {
+        const Item& I = items[i];
+        for (int k = 0; k < 3; k++) { c->S[k] += (double)I.v[k]; c->STX[k] += (double)I.TX[k]; }
+        for (int k = 0; k < 6; k++) c->ST[k] += (double)I.T[k];
+        for (int k = 0; k < 9; k++) c->SQ[k] += (double)I.Q[k];
+        c->W += (double)I.w;
+    }
+    void sub(idt i, Cluster* c) const {
+        const Item& I = items[i];
+        for (int k = 0; k < 3; k++) { c->S[k] -= (double)I.v[k]; c->STX[k] -= (double)I.TX[k]; }
+        for (int k = 0; k < 6; k++) c->ST[k] -= (double)I.T[k];
+        for (int k = 0; k < 9; k++) c->SQ[k] -= (double)I.Q[k];
+        c->W -= (double)I.w;
+    }
+    void centroid(Cluster* c) const {   // :282-288
+        c->c[0] = c->S[0] / c->W; c->c[1] = c->S[1] / c->W; c->c[2] = c->S[2] / c->W;
+        representative_point(c->SQ, c->c, level);
+    }
+    void energy(Cluster* c) const {     // :168-184
+        const double x = c->c[0], y = c->c[1], z = c->c[2];
+        const double* T = c->ST;
+        c->E = T[0] * x * x + T[3] * y * y + T[5] * z * z
+               + 2.0 * T[1] * x * y + 2.0 * T[2] * x * z + 2.0 * T[4] * y * z;
+        const double* U = c->STX;
+        c->E -= 2.0 * (x * U[0] + y * U[1] + z * U[2]);
+    }
+    void get_centroid(const Cluster* c, double* p) const { for (int k = 0; k < 3; k++) p[k] = c->c[k]; }
+    void build(const Mesh& m) {   // BuildMetric, vertex items (:374-487)
+        mesh = &m;
+        items.resize(m.nV);
+        std::vector<idt> fl;
+        for (idt i = 0; i < m.nV; i++) {
+            Item& I = items[i];
+            for (double& x : I.Q) x = 0;                      // ComputeVertexQuadric (:524-539)
+            m.vertex_faces(i, fl);
+            for (idt f : fl) m.add_triangle_quadric(I.Q, f);
+            if (gradation == 0) I.w = (float)m.vertex_area(i);
+            else I.w = (float)(m.vertex_area(i) * std::pow(indicator[i], gradation));
+            double p[3]; m.point(i, p);
+            I.v[0] = (float)p[0]; I.v[1] = (float)p[1]; I.v[2] = (float)p[2];
+        }
+        {   // ClampWeights, ratio 1e5 (:401, :489-508)
+            double avg = 0;
+            for (auto& I : items) avg += I.w;
+            avg = avg / (double)items.size();
+            const double mn = avg / 100000, mx = avg * 100000;
+            for (auto& I : items) {
+                if (I.w > mx) I.w = (float)mx;
+                if (I.w < mn) I.w = (float)mn;
+            }
+        }
+        for (idt i = 0; i < m.nV; i++) {
+            Item& I = items[i];
+            const double area = m.vertex_area(i);
+            double PD[6];
+            for (int j = 0; j < 6; j++) PD[j] = (double)pdirs[i * 6 + j];
+            // Area*(d1 d1^T + d2 d2^T) in compact form; entry 3 uses PD[5]^2 in place of
+            // PD[4]^2 exactly as the reference does (:442-446)
+            I.T[0] = (float)(area * PD[0] * PD[0] + area * PD[3] * PD[3]);
+            I.T[1] = (float)(area * PD[0] * PD[1] + area * PD[3] * PD[4]);
+            I.T[2] = (float)(area * PD[0] * PD[2] + area * PD[3] * PD[5]);
+            I.T[3] = (float)(area * PD[1] * PD[1] + area * PD[5] * PD[5]);
+            I.T[4] = (float)(area * PD[1] * PD[2] + area * PD[4] * PD[5]);
+            I.T[5] = (float)(area * PD[2] * PD[2] + area * PD[5] * PD[5]);
+            I.TX[0] = I.T[0] * I.v[0] + I.T[1] * I.v[1] + I.T[2] * I.v[2];
+            I.TX[1] = I.T[1] * I.v[0] + I.T[3] * I.v[1] + I.T[4] * I.v[2];
+            I.TX[2] = I.T[2] * I.v[0] + I.T[4] * I.v[1] + I.T[5] * I.v[2];
+            I.v[0] *= I.w; I.v[1] *= I.w; I.v[2] *= I.w;
+        }
+    }
+    void accum(const Cluster* c, double* S, double* W, double* Q) const {
+        for (int k = 0; k < 3; k++) S[k] = c->S[k];
+        *W = c->W;
+        for (int k = 0; k < 9; k++) Q[k] = c->SQ[k];
+    }
+};
+
+// ---------------------------------------------------------------------------
+// Engine (Common/vtkUniformClustering.h) + vertex adapter (vtkVerticesProcessing.h)
+// ---------------------------------------------------------------------------
+struct EngineBase {
+    virtual ~EngineBase() {}
+    Mesh mesh;
+    int K = 0;
+    std::vector<int> labels;       // Clustering
+    std::vector<int> initial;      // InitialClustering
+    std::vector<int> sizes;        // ClustersSizes
+    std::vector<int> last_mod;     // ClustersLastModification
+    std::vector<unsigned char> frozen;
+    std::vector<unsigned char> edges_last_loop;
+    unsigned char rel_loops = 1;
+    int n_loops = 0;
+    int connexity = 0;
+    int unconstrained_init = 0;
+    int sampling_type = 1;
+    int max_convergences = 1000000000;
+    int max_loops = 5000000;
+    std::queue<idt> queue;
+    // statistics of the last MinimizeEnergy
+    int stat_convergences = 0;
+    long long stat_moves = 0;
+    double stat_seconds = 0;
+
+    virtual void build_metric() = 0;
+    virtual void set_constrained(int c) = 0;
+    virtual void recompute_statistics() = 0;
+    virtual int process_one_loop() = 0;
+    virtual double item_weight(idt i) const = 0;
+    virtual double cluster_energy(int k) const = 0;
+    virtual void cluster_accum(int k, double* S, double* W, double* Q, double* c) const = 0;
+
+    idt n_items() const { return mesh.nV; }
+
+    // vtkVerticesProcessing::ConnexityConstraintProblemLocal (:168-237)
+    int connexity_problem(idt item, int cluster) const {
+        if (!connexity) return 0;
+        std::vector<idt> vl;
+        for (idt e : mesh.ring[item]) {
+            const idt v1 = mesh.ev1[e], v2 = mesh.ev2[e];
+            if (v1 != item && labels[v1] == cluster) vl.push_back(v1);
+            if (v2 != item && labels[v2] == cluster) vl.push_back(v2);
+        }
+        if (vl.empty()) return 0;
+        const size_t total = vl.size();
+        size_t visited = 1;
+        std::queue<idt> q;
+        idt v = vl[0];
+        vl.erase(vl.begin());
+        q.push(v);
+        while (!q.empty()) {
+            const idt a = q.front(); q.pop();
+            for (idt e : mesh.ring[a]) {
+                const idt b = mesh.ev1[e], c = mesh.ev2[e];
+                for (size_t j = 0; j < vl.size(); j++) {
+                    if (vl[j] == b || vl[j] == c) {
+                        q.push(vl[j]); visited++;
+                        vl.erase(vl.begin() + j);
+                        break;
+                    }
+                }
+            }
+        }
+        return visited == total ? 0 : 1;
+    }
+
+    void add_ring_to_queue(idt item) { for (idt e : mesh.ring[item]) queue.push(e); }
+
+    // ReComputeClustersSize (:353-373)
+    void recompute_sizes() {
+        std::fill(sizes.begin(), sizes.end(), 0);
+        for (idt i = 0; i < n_items(); i++) {
+            const int c = labels[i];
+            if (c >= 0 && c < K) sizes[c]++;
+        }
+    }
+
+    // CleanClustering (:406-549); returns the number of clusters that had several components
+    int clean_clustering() {
+        const idt n = n_items();
+        std::vector<char> visited(n, 0);
+        std::vector<std::vector<std::pair<idt, int>>> extra(K);
+        std::vector<idt> first(K, 0);
+        std::vector<int> first_size(K, 0);
+        std::vector<idt> nb;
+        std::queue<idt> q;
+        for (idt i = 0; i < n; i++) {
+            if (visited[i] || labels[i] == K) continue;
+            while (!q.empty()) q.pop();
+            int size = 0;
+            q.push(i);
+            const int type = labels[i];
+            while (!q.empty()) {
+                const idt a = q.front(); q.pop();
+                if (visited[a]) continue;
+                size += 1;
+                visited[a] = 1;
+                mesh.vertex_neighbours(a, nb);
+                for (idt b : nb) if (!visited[b] && labels[b] == type) q.push(b);
+            }
+            if (first[type] == 0) { first[type] = i; first_size[type] = size; }
+            else {
+                if (extra[type].empty()) extra[type].push_back({first[type], first_size[type]});
+                extra[type].push_back({i, size});
+            }
+        }
+        std::fill(visited.begin(), visited.end(), 0);
+        int number = 0;
+        for (int k = 0; k < K; k++) {
+            if (extra[k].empty()) continue;
+            number++;
+            int smax = 0, imax = 0;
+            for (size_t j = 0; j < extra[k].size(); j++) {
+                if (smax >= extra[k][j].second) continue;
+                smax = extra[k][j].second; imax = (int)j;
+            }
+            for (size_t j = 0; j < extra[k].size(); j++) {
+                if ((int)j == imax) continue;
+                while (!q.empty()) q.pop();
+                q.push(extra[k][j].first);
+                const int type = labels[extra[k][j].first];
+                while (!q.empty()) {
+                    const idt a = q.front(); q.pop();
+                    if (visited[a]) continue;
+                    visited[a] = 1;
+                    labels[a] = K;
+                    mesh.vertex_neighbours(a, nb);
+                    for (idt b : nb) if (labels[b] == type) q.push(b);
+                }
+            }
+        }
+        return number;
+    }
+
+    // FillHolesInClustering (:552-633); returns the number of items left unassigned
+    int fill_holes() {
+        std::queue<idt> q;
+        for (idt e = 0; e < mesh.n_edges(); e++) {
+            const idt i1 = mesh.ev1[e], i2 = mesh.ev2[e];
+            const int c1 = labels[i1], c2 = labels[i2];
+            const bool bad1 = (c1 < 0) || (c1 >= K), bad2 = (c2 < 0) || (c2 >= K);
+            if (bad1 != bad2) q.push(e);
+        }
+        while (!q.empty()) {
+            const idt e = q.front(); q.pop();
+            idt i1 = mesh.ev1[e], i2 = mesh.ev2[e];
+            int c1 = labels[i1], c2 = labels[i2];
+            if (c1 == K) { std::swap(i1, i2); c1 = c2; c2 = K; }
+            if (c1 != K && c2 == K && connexity_problem(i2, c2) == 0) {
+                labels[i2] = c1;
+                add_ring_to(q, i2);
+            }
+        }
+        int problems = 0;
+        for (idt i = 0; i < n_items(); i++) if (labels[i] < 0 || labels[i] >= K) problems++;
+        return problems;
+    }
+    void add_ring_to(std::queue<idt>& q, idt item) { for (idt e : mesh.ring[item]) q.push(e); }
+
+    // FillQueuesFromClustering (:636-652)
+    void fill_queue() {
+        while (!queue.empty()) queue.pop();
+        for (idt e = 0; e < mesh.n_edges(); e++)
+            if (labels[mesh.ev1[e]] != labels[mesh.ev2[e]]) queue.push(e);
+        queue.push(-1);
+    }
+
+    void set_all_modified() { for (int k = 0; k < K; k++) last_mod[k] = n_loops; }
+
+    // Init (:1363-1381) + Allocate (:1349-1360)
+    void init() {
+        sizes.assign(K, 0);
+        labels.assign(n_items(), K);
+        last_mod.assign(K, 0);
+        edges_last_loop.assign(mesh.n_edges(), 0);
+        frozen.assign(K, 0);
+        build_metric();
+        rel_loops = 1;
+        n_loops = 0;
+        while (!queue.empty()) queue.pop();
+    }
+
+    // ComputeInitialRandomSampling (:1178-1316), no fixed clusters
+    void initial_random_sampling() {
+        const idt n = n_items();
+        for (idt i = 0; i < n; i++) labels[i] = K;
+        std::vector<int> itm(n);
+        idt remaining_items = n;
+        int remaining_regions = K;
+        for (idt i = 0; i < n; i++) itm[i] = (int)i;
+        std::mt19937 rng;
+        rng.seed(0);
+        for (idt i = n - 1; i > 0; --i) std::swap(itm[i], itm[rng() % n]);
+        double sw = 0;
+        for (idt i = 0; i < n; i++) sw += item_weight(i);
+        const double target = sw / (double)K;
+        idt first = 0;
+        std::queue<int> q;
+        std::vector<idt> nb;
+        while (remaining_items > 0 && remaining_regions > 0) {
+            bool found = false;
+            int item = 0;
+            while (!found && first < n) {
+                item = itm[first];
+                if (labels[item] == K) found = true; else first++;
+            }
+            if (!found) continue;
+            while (!q.empty()) q.pop();
+            q.push(item);
+            sw = 0;
+            remaining_regions--;
+            while (!q.empty()) {
+                item = q.front(); q.pop();
+                if (labels[item] != K) continue;
+                labels[item] = remaining_regions;
+                sw += item_weight(item);
+                remaining_items--;
+                mesh.vertex_neighbours(item, nb);
+                for (idt b : nb) q.push((int)b);
+                if (sw > target) break;
+            }
+        }
+        if (remaining_regions == 0) return;
+        std::fill(sizes.begin(), sizes.end(), 0);
+        for (idt i = 0; i < n; i++) {
+            itm[i] = (int)i;
+            if (labels[i] == K) continue;
+            sizes[labels[i]]++;
+        }
+        for (idt i = n - 1; i > 0; --i) std::swap(itm[i], itm[rng() % n]);
+        first = 0;
+        while (remaining_regions) {
+            idt item;
+            while (true) {
+                item = itm[first];
+                first++;
+                const int cl = labels[item];
+                if (cl == K) break;
+                if (sizes[cl] == 1) continue;
+                labels[item] = remaining_regions;
+                sizes[cl]--;
+                sizes[remaining_regions]++;
+                break;
+            }
+            remaining_regions--;
+            labels[item] = remaining_regions;
+        }
+    }
+
+    // InitSamples (:1124-1175), types 1 and 2
+    void init_samples() {
+        for (idt i = 0; i < n_items(); i++) labels[i] = K;
+        if (sampling_type == 2) {
+            for (idt i = 0; i < n_items(); i++) labels[i] = initial[i];
+        } else {
+            initial_random_sampling();
+        }
+    }
+
+    // MinimizeEnergy (:725-830)
+    void minimize_energy() {
+        auto t0 = std::chrono::steady_clock::now();
+        fill_holes();
+        fill_queue();
+        recompute_statistics();
+        set_all_modified();
+        int convergences = 0;
+        int early = 0;
+        for (int k = 0; k < K; k++) if (!frozen[k]) early += sizes[k];
+        stat_moves = 0;
+        while (true) {
+            const int mods = process_one_loop();
+            stat_moves += mods;
+            n_loops++;
+            if (rel_loops == 255) {
+                std::fill(edges_last_loop.begin(), edges_last_loop.end(), 0);
+                rel_loops = 1;
+            } else rel_loops++;
+            if (mods == 0 || n_loops > max_loops || (mods <= early / 1000 && convergences <= 1)) {
+                if (unconstrained_init && convergences == 0) set_constrained(1);
+                if (convergences >= 1) connexity = 1;
+                convergences++;
+                const int disconnected = clean_clustering();
+                fill_holes();
+                recompute_sizes();
+                if (disconnected == 0 && mods == 0) break;
+                if (n_loops >= max_loops) break;
+                if (convergences >= max_convergences) break;
+                recompute_statistics();
+                fill_queue();
+                set_all_modified();
+            }
+        }
+        stat_convergences = convergences;
+        stat_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    }
+
+    // ProcessClustering (:655-714) from the point where Init and InitSamples are done
+    void process_clustering() {
+        if (unconstrained_init) set_constrained(0);
+        minimize_energy();
+    }
+
+    // ComputeGlobalEnergy (:1319-1346), bins as in the reference
+    long double global_energy() const {
+        long double energy = 0;
+        const int nb = (int)std::sqrt((double)K);
+        std::vector<long double> bins(nb, 0.0L);
+        int bin = 0, count = 0;
+        for (int k = 0; k < K; k++) {
+            bins[bin] += (long double)cluster_energy(k);
+            count++;
+            if (count == nb && bin < nb - 1) bin++;
+        }
+        for (int i = 0; i < nb; i++) energy += bins[i];
+        return energy;
+    }
+};
+
+template <class M>
+struct Engine : EngineBase {
+    M metric;
+    std::vector<typename M::Cluster> clusters;
+
+    void build_metric() override { metric.build(mesh); }
+    void set_constrained(int c) override { metric.set_constrained(c); }
+    double item_weight(idt i) const override { return metric.weight(i); }
+    double cluster_energy(int k) const override { return clusters[k].E; }
+    void cluster_accum(int k, double* S, double* W, double* Q, double* c) const override {
+        metric.accum(&clusters[k], S, W, Q);
+        metric.get_centroid(&clusters[k], c);
+    }
+
+    void set_k(int k) {   // SetNumberOfClusters (:62-69)
+        K = k;
+        clusters.resize(k);
+        for (auto& c : clusters) metric.reset(&c);
+    }
+
+    void recompute_statistics() override {   // (:376-403)
+        recompute_sizes();
+        for (auto& c : clusters) metric.reset(&c);
+        for (idt i = 0; i < n_items(); i++) {
+            const int c = labels[i];
+            if (c >= 0 && c < K) metric.add(i, &clusters[c]);
+        }
+        for (auto& c : clusters) { metric.centroid(&c); metric.energy(&c); }
+    }
+
+    int process_one_loop() override {   // (:833-995)
+        typename M::Cluster c21, c22, c31, c32;
+        int mods = 0;
+        while (true) {
+            const idt edge = queue.front();
+            queue.pop();
+            if (edge == -1) { queue.push(-1); return mods; }
+            const idt i1 = mesh.ev1[edge], i2 = mesh.ev2[edge];
+            if (edges_last_loop[edge] == rel_loops || i2 < 0) continue;
+            edges_last_loop[edge] = rel_loops;
+            const int v1 = labels[i1], v2 = labels[i2];
+            if (v1 == v2) continue;
+            if (v1 == K) {
+                typename M::Cluster* c2 = &clusters[v2];
+                metric.add(i1, c2); metric.centroid(c2); metric.energy(c2);
+                sizes[v2]++;
+                add_ring_to_queue(i1);
+                mods++;
+                labels[i1] = v2;
+                last_mod[v2] = n_loops;
+                continue;
+            } else if (v2 == K) {
+                typename M::Cluster* c1 = &clusters[v1];
+                metric.add(i2, c1); metric.centroid(c1); metric.energy(c1);
+                sizes[v1]++;
+                add_ring_to_queue(i2);
+                mods++;
+                labels[i2] = v1;
+                last_mod[v1] = n_loops;
+                continue;
+            }
+            if ((last_mod[v1] < n_loops - 1 && last_mod[v2] < n_loops - 1) || frozen[v1] || frozen[v2]) {
+                queue.push(edge);
+                continue;
+            }
+            typename M::Cluster* c1 = &clusters[v1];
+            typename M::Cluster* c2 = &clusters[v2];
+            double try1, try2, try3;
+            try1 = c1->E + c2->E;
+            if (sizes[v1] == 1 || connexity_problem(i1, v1) == 1) try2 = 100000000.0;
+            else {
+                c21 = *c1; metric.sub(i1, &c21);
+                c22 = *c2; metric.add(i1, &c22);
+                metric.centroid(&c21); metric.centroid(&c22);
+                metric.energy(&c21); metric.energy(&c22);
+                try2 = c21.E + c22.E;
+            }
+            if (sizes[v2] == 1 || connexity_problem(i2, v2) == 1) try3 = 1000000000.0;
+            else {
+                c32 = *c2; metric.sub(i2, &c32);
+                c31 = *c1; metric.add(i2, &c31);
+                metric.centroid(&c31); metric.centroid(&c32);
+                metric.energy(&c31); metric.energy(&c32);
+                try3 = c31.E + c32.E;
+            }
+            if (try1 <= try2 && try1 <= try3) {
+                queue.push(edge);
+            } else if (try2 < try1 && try2 < try3) {
+                labels[i1] = v2;
+                sizes[v2]++; sizes[v1]--;
+                *c1 = c21; *c2 = c22;
+                add_ring_to_queue(i1);
+                mods++;
+                last_mod[v1] = n_loops; last_mod[v2] = n_loops;
+            } else {
+                labels[i2] = v1;
+                sizes[v1]++; sizes[v2]--;
+                *c1 = c31; *c2 = c32;
+                add_ring_to_queue(i2);
+                mods++;
+                last_mod[v1] = n_loops; last_mod[v2] = n_loops;
+            }
+        }
+    }
+};
+
+}  // namespace port
+
+// ---------------------------------------------------------------------------
+// C ABI for the tests and the CPU baseline (ctypes)
+// ---------------------------------------------------------------------------
+using namespace port;
+
+struct PortHandle {
+    EngineBase* eng = nullptr;
+    int metric = 0;
+    std::vector<double> indicator;
+    std::vector<float> pdirs;
+};
+
+extern "C" {
+
+// metric: 0 isotropic, 1 QEM, 2 quadric-anisotropic.  indicator/pdirs may be null.
+void* port_create(int metric, long long nV, const double* pts, long long nF, const int* tri,
+                  const double* indicator, const float* pdirs, double gradation, int K) {
+    PortHandle* h = new PortHandle;
+    h->metric = metric;
+    if (indicator) h->indicator.assign(indicator, indicator + nV);
+    if (pdirs) h->pdirs.assign(pdirs, pdirs + 6 * nV);
+    EngineBase* e = nullptr;
+    if (metric == 0) {
+        auto* x = new Engine<IsoMetric>;
+        x->metric.gradation = gradation;
+        x->metric.indicator = indicator ? h->indicator.data() : nullptr;
+        e = x; x->mesh.build(nV, pts, nF, tri); x->set_k(K);
+    } else if (metric == 1) {
+        auto* x = new Engine<QEMMetric>;
+        x->metric.gradation = gradation;
+        x->metric.indicator = indicator ? h->indicator.data() : nullptr;
+        e = x; x->mesh.build(nV, pts, nF, tri); x->set_k(K);
+    } else {
+        auto* x = new Engine<AnisoMetric>;
+        x->metric.gradation = gradation;
+        x->metric.indicator = indicator ? h->indicator.data() : nullptr;
+        x->metric.pdirs = h->pdirs.data();
+        e = x; x->mesh.build(nV, pts, nF, tri); x->set_k(K);
+    }
+    h->eng = e;
+    return h;
+}
+
+void port_destroy(void* hp) {
+    PortHandle* h = (PortHandle*)hp;
+    delete h->eng;
+    delete h;
+}
+
+// name in {"level", "unconstrained_init", "max_loops", "max_convergences", "connexity"}
+int port_set_option(void* hp, const char* name, double value) {
+    PortHandle* h = (PortHandle*)hp;
+    EngineBase* e = h->eng;
+    if (!std::strcmp(name, "unconstrained_init")) e->unconstrained_init = (int)value;
+    else if (!std::strcmp(name, "max_loops")) e->max_loops = (int)value;
+    else if (!std::strcmp(name, "max_convergences")) e->max_convergences = (int)value;
+    else if (!std::strcmp(name, "connexity")) e->connexity = (int)value;
+    else if (!std::strcmp(name, "level")) {
+        if (h->metric == 1) static_cast<Engine<QEMMetric>*>(e)->metric.level = (int)value;
+        else if (h->metric == 2) static_cast<Engine<AnisoMetric>*>(e)->metric.level = (int)value;
+    } else if (!std::strcmp(name, "constrained")) e->set_constrained((int)value);
+    else return -1;
+    return 0;
+}
+
+// Init + InitSamples.  initial may be null (random sampling, type 1) or N labels (type 2).
+void port_init(void* hp, const int* initial) {
+    EngineBase* e = ((PortHandle*)hp)->eng;
+    e->init();
+    if (initial) { e->sampling_type = 2; e->initial.assign(initial, initial + e->n_items()); }
+    else e->sampling_type = 1;
+    e->init_samples();
+}
+
+// The remainder of ProcessClustering: unconstrained switch + MinimizeEnergy.
+double port_run(void* hp) {
+    EngineBase* e = ((PortHandle*)hp)->eng;
+    e->process_clustering();
+    return e->stat_seconds;
+}
+
+void port_get_labels(void* hp, int* out) {
+    EngineBase* e = ((PortHandle*)hp)->eng;
+    std::memcpy(out, e->labels.data(), sizeof(int) * e->n_items());
+}
+
+void port_set_labels(void* hp, const int* in) {
+    EngineBase* e = ((PortHandle*)hp)->eng;
+    std::memcpy(e->labels.data(), in, sizeof(int) * e->n_items());
+}
+
+// Init() then load the labels and ReComputeStatistics -- the reference's own load path
+// (vtkDiscreteRemeshing.h:915-932).  constrained sets the metric's placement switch.
+void port_evaluate(void* hp, const int* lab, int constrained) {
+    EngineBase* e = ((PortHandle*)hp)->eng;
+    e->init();
+    e->set_constrained(constrained);
+    std::memcpy(e->labels.data(), lab, sizeof(int) * e->n_items());
+    e->recompute_statistics();
+}
+
+void port_recompute(void* hp) { ((PortHandle*)hp)->eng->recompute_statistics(); }
+
+double port_global_energy(void* hp) { return (double)((PortHandle*)hp)->eng->global_energy(); }
+
+// Per-cluster S (3K), W (K), Q (9K; zeros for the isotropic metric), centroid (3K),
+// energy (K) and size (K).
+void port_get_clusters(void* hp, double* S, double* W, double* Q, double* C, double* E, int* sizes) {
+    EngineBase* e = ((PortHandle*)hp)->eng;
+    for (int k = 0; k < e->K; k++) {
+        e->cluster_accum(k, S + 3 * k, W + k, Q + 9 * k, C + 3 * k);
+        E[k] = e->cluster_energy(k);
+        sizes[k] = e->sizes[k];
+    }
+}
+
+// Items as the metric stores them: value (3, weight-multiplied), weight, quadric (9).
+void port_get_items(void* hp, double* V, double* W, double* Q) {
+    PortHandle* h = (PortHandle*)hp;
+    EngineBase* e = h->eng;
+    for (idt i = 0; i < e->n_items(); i++) {
+        if (h->metric == 0) {
+            auto& I = static_cast<Engine<IsoMetric>*>(e)->metric.items[i];
+            for (int k = 0; k < 3; k++) V[3 * i + k] = I.v[k];
+            W[i] = I.w;
+            for (int k = 0; k < 9; k++) Q[9 * i + k] = 0;
+        } else if (h->metric == 1) {
+            auto& I = static_cast<Engine<QEMMetric>*>(e)->metric.items[i];
+            for (int k = 0; k < 3; k++) V[3 * i + k] = I.v[k];
+            W[i] = I.w;
+            for (int k = 0; k < 9; k++) Q[9 * i + k] = I.Q[k];
+        } else {
+            auto& I = static_cast<Engine<AnisoMetric>*>(e)->metric.items[i];
+            for (int k = 0; k < 3; k++) V[3 * i + k] = I.v[k];
+            W[i] = I.w;
+            for (int k = 0; k < 9; k++) Q[9 * i + k] = I.Q[k];
+        }
+    }
+}
+
+// Anisotropic items' tensor (6) and tensor x position (3), float as stored.
+void port_get_aniso_items(void* hp, float* T, float* TX) {
+    PortHandle* h = (PortHandle*)hp;
+    if (h->metric != 2) return;
+    auto* x = static_cast<Engine<AnisoMetric>*>(h->eng);
+    for (idt i = 0; i < x->n_items(); i++) {
+        for (int k = 0; k < 6; k++) T[6 * i + k] = x->metric.items[i].T[k];
+        for (int k = 0; k < 3; k++) TX[3 * i + k] = x->metric.items[i].TX[k];
+    }
+}
+
+int port_clean(void* hp) { return ((PortHandle*)hp)->eng->clean_clustering(); }
+int port_fill_holes(void* hp) { return ((PortHandle*)hp)->eng->fill_holes(); }
+int port_connexity_problem(void* hp, long long item, int cluster) {
+    EngineBase* e = ((PortHandle*)hp)->eng;
+    const int save = e->connexity;
+    e->connexity = 1;
+    const int r = e->connexity_problem(item, cluster);
+    e->connexity = save;
+    return r;
+}
+
+// Topology in the reference's numbering: number of edges; fills edge endpoints
+// (2E, may be null) and the CSR of vertex rings (row N+1, col 2E; may be null).
+long long port_topology(void* hp, int* edge_v, int* row, int* col) {
+    EngineBase* e = ((PortHandle*)hp)->eng;
+    const Mesh& m = e->mesh;
+    if (edge_v)
+        for (idt i = 0; i < m.n_edges(); i++) { edge_v[2 * i] = (int)m.ev1[i]; edge_v[2 * i + 1] = (int)m.ev2[i]; }
+    if (row && col) {
+        idt p = 0;
+        for (idt v = 0; v < m.nV; v++) {
+            row[v] = (int)p;
+            for (idt ed : m.ring[v]) col[p++] = (int)(m.ev1[ed] == v ? m.ev2[ed] : m.ev1[ed]);
+        }
+        row[m.nV] = (int)p;
+    }
+    return m.n_edges();
+}
+
+// Statistics of the last run: loops, convergences, total moves.
+void port_stats(void* hp, int* loops, int* convergences, long long* moves) {
+    EngineBase* e = ((PortHandle*)hp)->eng;
+    *loops = e->n_loops; *convergences = e->stat_convergences; *moves = e->stat_moves;
+}
+
+// BuildDelaunayTriangulation for vertex clustering (vtkDiscreteRemeshing.h:1003-1152
+// without display and manifold repair): output vertex k = cluster centroid (empty
+// clusters take the first non-empty cluster's), one triangle per input face whose
+// three labels are distinct and valid, duplicates (same vertex set) rejected.
+// Returns the triangle count; tris (3F) and verts (3K) may be null.
+long long port_dual_mesh(void* hp, int* tris, double* verts) {
+    EngineBase* e = ((PortHandle*)hp)->eng;
+    const Mesh& m = e->mesh;
+    if (verts) {
+        int valid = 0;
+        for (int k = 0; k < e->K; k++) if (e->sizes[k] > 0) { valid = k; break; }
+        for (int k = 0; k < e->K; k++) {
+            double S[3], W, Q[9], c[3];
+            e->cluster_accum(e->sizes[k] == 0 ? valid : k, S, &W, Q, c);
+            verts[3 * k] = c[0]; verts[3 * k + 1] = c[1]; verts[3 * k + 2] = c[2];
+        }
+    }
+    std::vector<std::vector<std::pair<int, int>>> adj(e->K);  // face lookup by smallest vertex
+    long long count = 0;
+    for (idt f = 0; f < m.nF; f++) {
+        int cl[3]; int n = 0;
+        for (int j = 0; j < 3; j++) {
+            const int c = e->labels[m.F[3 * f + j]];
+            if (c >= e->K) continue;
+            bool dup = false;
+            for (int t = 0; t < n; t++) if (cl[t] == c) dup = true;
+            if (!dup) cl[n++] = c;
+        }
+        if (n != 3) continue;
+        int s[3] = {cl[0], cl[1], cl[2]};
+        std::sort(s, s + 3);
+        bool exists = false;
+        for (auto& pr : adj[s[0]]) if (pr.first == s[1] && pr.second == s[2]) { exists = true; break; }
+        if (exists) continue;
+        adj[s[0]].push_back({s[1], s[2]});
+        if (tris) { tris[3 * count] = cl[0]; tris[3 * count + 1] = cl[1]; tris[3 * count + 2] = cl[2]; }
+        count++;
+    }
+    return count;
+}
+
+}  // extern "C"

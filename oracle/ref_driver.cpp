@@ -1,0 +1,188 @@
+// ORACLE / TEST INFRASTRUCTURE ONLY.
+//
+// Drives the reference's own clustering code -- Common/vtkUniformClustering.h,
+// DiscreteRemeshing/vtkSurfaceClustering.h, DiscreteRemeshing/vtkVerticesProcessing.h
+// and the three metric headers, compiled unmodified from the reference tree
+// against oracle/shim (see oracle/Makefile) -- behind the same C ABI as the C++
+// restatement in acvd_port.cpp (prefix ref_ instead of port_).  The build exists
+// only where the reference sources are present; its outputs pin the restatement
+// (tests/test_oracle_pin.py) and generate tests/golden/.
+#include "vtkSurfaceClustering.h"
+#include "vtkVerticesProcessing.h"
+#include "vtkIsotropicMetricForClustering.h"
+#include "vtkQEMetricForClustering.h"
+#include "vtkQuadricAnisotropicMetricForClustering.h"
+
+#include <chrono>
+#include <type_traits>
+
+// Exposes the protected members of the reference engine; nothing is overridden.
+template <class M>
+class Probe : public vtkVerticesProcessing<vtkSurfaceClustering<M>> {
+public:
+    typedef vtkVerticesProcessing<vtkSurfaceClustering<M>> Base;
+    Probe() {}
+    using Base::Init;
+    using Base::InitSamples;
+    using Base::MinimizeEnergy;
+    using Base::ReComputeStatistics;
+    using Base::ComputeGlobalEnergy;
+    using Base::CleanClustering;
+    using Base::FillHolesInClustering;
+    using Base::Clusters;
+    using Base::Clustering;
+    using Base::ClustersSizes;
+    using Base::ConnexityConstraint;
+    using Base::NumberOfLoops;
+    using Base::UnconstrainedInitialization;
+    using Base::MetricContext;
+};
+
+struct RefBase {
+    virtual ~RefBase() {}
+    virtual void set_option(const char* name, double v) = 0;
+    virtual void init(const int* initial) = 0;
+    virtual double run() = 0;
+    virtual double process(const int* initial) = 0;
+    virtual void get_labels(int* out) = 0;
+    virtual void evaluate(const int* lab, int constrained) = 0;
+    virtual double global_energy() = 0;
+    virtual void get_clusters(double* S, double* W, double* Q, double* C, double* E, int* sz) = 0;
+    virtual int clean() = 0;
+    virtual int fill() = 0;
+    virtual void set_labels(const int* lab) = 0;
+    virtual int loops() = 0;
+};
+
+template <class M>
+struct Ref : RefBase {
+    Probe<M>* p = nullptr;
+    long long n = 0;
+    int K = 0;
+
+    Ref(long long nV, const double* pts, long long nF, const int* tri,
+        const double* indicator, const float* pdirs, double gradation, int k) {
+        n = nV; K = k;
+        vtkSurface* mesh = vtkSurface::New();
+        mesh->CreateFromArrays(nV, pts, nF, tri);
+        p = new Probe<M>;
+        p->SetInput(mesh);
+        mesh->Delete();
+        p->SetNumberOfClusters(k);
+        p->SetConsoleOutput(0);
+        p->SetDisplay(0);
+        p->GetMetric()->SetGradation(gradation);
+        if (indicator) {
+            vtkDataArrayCollection* coll = vtkDataArrayCollection::New();
+            vtkDoubleArray* ind = vtkDoubleArray::New();
+            ind->SetNumberOfValues(nV);
+            for (long long i = 0; i < nV; i++) ind->SetValue(i, indicator[i]);
+            coll->AddItem(ind);
+            ind->Delete();
+            if (pdirs) {
+                vtkFloatArray* pd = vtkFloatArray::New();
+                pd->SetNumberOfValues(6 * nV);
+                for (long long i = 0; i < 6 * nV; i++) pd->SetValue(i, pdirs[i]);
+                coll->AddItem(pd);
+                pd->Delete();
+            }
+            p->GetMetric()->SetCurvatureInfo(coll);
+            coll->Delete();
+        }
+    }
+    ~Ref() override { p->Delete(); }
+
+    void set_option(const char* name, double v) override {
+        if (!std::strcmp(name, "unconstrained_init")) p->SetUnconstrainedInitialization((int)v);
+        else if (!std::strcmp(name, "max_loops")) p->SetMaxNumberOfLoops((int)v);
+        else if (!std::strcmp(name, "max_convergences")) p->SetMaxNumberOfConvergences((int)v);
+        else if (!std::strcmp(name, "connexity")) p->ConnexityConstraint = (int)v;
+        else if (!std::strcmp(name, "constrained")) p->GetMetric()->SetConstrainedClustering((int)v);
+        else if (!std::strcmp(name, "level")) {
+            if constexpr (!std::is_same<M, vtkIsotropicMetricForClustering>::value)
+                p->GetMetric()->SetQuadricsOptimizationLevel((int)v);
+        }
+    }
+    void set_initial(const int* initial) {
+        vtkIntArray* a = vtkIntArray::New();
+        a->SetNumberOfValues(n);
+        for (long long i = 0; i < n; i++) a->SetValue(i, initial[i]);
+        p->SetInitialClustering(a);
+        a->Delete();
+    }
+    void init(const int* initial) override {
+        if (initial) set_initial(initial);
+        p->Init();
+        p->InitSamples(0);
+    }
+    double run() override {
+        auto t0 = std::chrono::steady_clock::now();
+        if (p->UnconstrainedInitialization) p->MetricContext.SetConstrainedClustering(0);
+        p->MinimizeEnergy();
+        return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    }
+    double process(const int* initial) override {
+        if (initial) set_initial(initial);
+        auto t0 = std::chrono::steady_clock::now();
+        p->ProcessClustering();
+        return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    }
+    void get_labels(int* out) override { for (long long i = 0; i < n; i++) out[i] = p->Clustering->GetValue(i); }
+    void set_labels(const int* lab) override { for (long long i = 0; i < n; i++) p->Clustering->SetValue(i, lab[i]); }
+    void evaluate(const int* lab, int constrained) override {
+        p->Init();
+        p->GetMetric()->SetConstrainedClustering(constrained);
+        set_labels(lab);
+        p->ReComputeStatistics();
+    }
+    double global_energy() override { return (double)p->ComputeGlobalEnergy(); }
+    void get_clusters(double* S, double* W, double* Q, double* C, double* E, int* sz) override {
+        for (int k = 0; k < K; k++) {
+            auto* c = p->GetCluster(k);
+            for (int j = 0; j < 3; j++) S[3 * k + j] = c->SValue[j];
+            W[k] = c->SWeight;
+            if constexpr (std::is_same<M, vtkIsotropicMetricForClustering>::value) {
+                for (int j = 0; j < 9; j++) Q[9 * k + j] = 0;
+            } else {
+                for (int j = 0; j < 9; j++) Q[9 * k + j] = c->SQuadric[j];
+            }
+            p->GetMetric()->GetClusterCentroid(c, C + 3 * k);
+            E[k] = p->GetMetric()->GetClusterEnergy(c);
+            sz[k] = p->GetClusterSize(k);
+        }
+    }
+    int clean() override { return p->CleanClustering(); }
+    int fill() override {
+        p->FillHolesInClustering(p->Clustering);
+        int bad = 0;
+        for (long long i = 0; i < n; i++) { const int c = p->Clustering->GetValue(i); if (c < 0 || c >= K) bad++; }
+        return bad;
+    }
+    int loops() override { return p->NumberOfLoops; }
+};
+
+extern "C" {
+
+void* ref_create(int metric, long long nV, const double* pts, long long nF, const int* tri,
+                 const double* indicator, const float* pdirs, double gradation, int K) {
+    if (metric == 0) return new Ref<vtkIsotropicMetricForClustering>(nV, pts, nF, tri, indicator, pdirs, gradation, K);
+    if (metric == 1) return new Ref<vtkQEMetricForClustering>(nV, pts, nF, tri, indicator, pdirs, gradation, K);
+    return new Ref<vtkQuadricAnisotropicMetricForClustering>(nV, pts, nF, tri, indicator, pdirs, gradation, K);
+}
+void ref_destroy(void* h) { delete (RefBase*)h; }
+int ref_set_option(void* h, const char* name, double v) { ((RefBase*)h)->set_option(name, v); return 0; }
+void ref_init(void* h, const int* initial) { ((RefBase*)h)->init(initial); }
+double ref_run(void* h) { return ((RefBase*)h)->run(); }
+double ref_process(void* h, const int* initial) { return ((RefBase*)h)->process(initial); }
+void ref_get_labels(void* h, int* out) { ((RefBase*)h)->get_labels(out); }
+void ref_set_labels(void* h, const int* lab) { ((RefBase*)h)->set_labels(lab); }
+void ref_evaluate(void* h, const int* lab, int constrained) { ((RefBase*)h)->evaluate(lab, constrained); }
+double ref_global_energy(void* h) { return ((RefBase*)h)->global_energy(); }
+void ref_get_clusters(void* h, double* S, double* W, double* Q, double* C, double* E, int* sz) {
+    ((RefBase*)h)->get_clusters(S, W, Q, C, E, sz);
+}
+int ref_clean(void* h) { return ((RefBase*)h)->clean(); }
+int ref_fill_holes(void* h) { return ((RefBase*)h)->fill(); }
+int ref_loops(void* h) { return ((RefBase*)h)->loops(); }
+
+}  // extern "C"

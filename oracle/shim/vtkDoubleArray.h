@@ -1,0 +1,3 @@
+// ORACLE shim: forwards to vtk_shim.h
+#pragma once
+#include "vtk_shim.h"
