@@ -1,0 +1,75 @@
+"""Builds the CUDA library libacvd_gb300.so in-tree (acvd_gb300/_build/) for sm_103a.
+
+    python -m acvd_gb300.build        # or acvd_gb300.build.build()
+
+Each translation unit is compiled by nvcc in parallel; the link is a plain
+`nvcc -shared`.  No CMake, no torch extension machinery: the library exposes a
+C ABI (include/acvd_gpu.h) and is loaded with ctypes.
+"""
+from __future__ import annotations
+
+import concurrent.futures
+import os
+import shutil
+import subprocess
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SRC = os.path.join(HERE, "csrc")
+OUT = os.path.join(HERE, "_build")
+LIB = os.path.join(OUT, "libacvd_gb300.so")
+ARCH = "-gencode=arch=compute_103a,code=sm_103a"
+CU_SOURCES = ["primitives.cu", "topology.cu", "cluster.cu", "engine.cu"]
+CXX_SOURCES = ["host.cpp"]
+
+
+def _nvcc() -> str:
+    for cand in (shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found")
+
+
+def _stale(obj: str, deps: list[str]) -> bool:
+    if not os.path.exists(obj):
+        return True
+    t = os.path.getmtime(obj)
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def build(verbose: bool = False, force: bool = False) -> str:
+    os.makedirs(OUT, exist_ok=True)
+    nvcc = _nvcc()
+    headers = [os.path.join(SRC, f) for f in os.listdir(SRC) if f.endswith((".cuh", ".h"))]
+    headers.append(os.path.join(os.path.dirname(HERE), "include", "acvd_gpu.h"))
+    jobs = []
+    objs = []
+    for f in CU_SOURCES:
+        src = os.path.join(SRC, f)
+        obj = os.path.join(OUT, f + ".o")
+        objs.append(obj)
+        if force or _stale(obj, [src] + headers):
+            jobs.append([nvcc, ARCH, "-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
+                         "-diag-suppress", "128", "-c", src, "-o", obj])
+    for f in CXX_SOURCES:
+        src = os.path.join(SRC, f)
+        obj = os.path.join(OUT, f + ".o")
+        objs.append(obj)
+        if force or _stale(obj, [src] + headers):
+            jobs.append(["g++", "-O3", "-std=c++17", "-fPIC", "-c", src, "-o", obj])
+
+    def run(cmd):
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"compile failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+        if verbose and (r.stdout or r.stderr):
+            print(r.stdout + r.stderr)
+
+    with concurrent.futures.ThreadPoolExecutor(max_workers=max(1, len(jobs))) as ex:
+        list(ex.map(run, jobs))
+    if force or jobs or not os.path.exists(LIB):
+        run([nvcc, ARCH, "-shared", "-o", LIB] + objs + ["-lcudart"])
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(verbose=True))

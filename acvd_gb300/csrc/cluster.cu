@@ -1,0 +1,785 @@
+// Clustering kernels: the deterministic parallel form of the reference's
+// boundary-swap loop (Common/vtkUniformClustering.h:833-995), the per-cluster
+// statistics (ReComputeStatistics :376-403), connectivity cleaning
+// (CleanClustering :406-549), hole filling (FillHolesInClustering :552-633) and
+// the dual mesh (DiscreteRemeshing/vtkDiscreteRemeshing.h:1003-1152).
+//
+// Schedule: the items are coloured once (no two adjacent items share a colour).
+// One step handles one colour class: `eval` proposes, for every boundary item of
+// the class, the move to a neighbouring cluster with the most negative energy
+// change; each proposal claims its source and destination clusters with a
+// 64-bit atomicMin; `apply` commits the proposals that hold both claims.  No
+// cluster takes part in two commits of one step, so every committed energy
+// change is exact and the result does not depend on thread timing.
+#include "primitives.cuh"
+#include "state.cuh"
+
+namespace acvd {
+
+// ---------------------------------------------------------------------------
+// item and cluster records
+// ---------------------------------------------------------------------------
+struct ItemRec {
+    float x[3];
+    float w;
+    float A[6];
+    float T[6];
+};
+
+template <int M>
+ACVD_DEV void load_item(const DevState& st, int i, ItemRec& it) {
+    const float4 a = st.xw[i];
+    it.x[0] = a.x; it.x[1] = a.y; it.x[2] = a.z; it.w = a.w;
+    if (M != kIso) {
+        const float4 q = st.qa[i];
+        const float2 r = st.qb[i];
+        it.A[0] = q.x; it.A[1] = q.y; it.A[2] = q.z; it.A[3] = q.w; it.A[4] = r.x; it.A[5] = r.y;
+    }
+    if (M == kAniso) {
+        const float4 t = st.ta[i];
+        const float2 u = st.tb[i];
+        it.T[0] = t.x; it.T[1] = t.y; it.T[2] = t.z; it.T[3] = t.w; it.T[4] = u.x; it.T[5] = u.y;
+    }
+}
+
+struct EvalRec {
+    float m[3], W;
+    float d[3], P;
+    float r[3];
+    float A[6];
+    float T[6];
+    float g[3];
+};
+
+template <int M>
+ACVD_DEV void load_eval(const DevState& st, int k, EvalRec& e) {
+    const float4* p = st.ev + (int64_t)k * Layout<M>::ev;
+    const float4 e0 = p[0];
+    e.m[0] = e0.x; e.m[1] = e0.y; e.m[2] = e0.z; e.W = e0.w;
+    if (M != kIso) {
+        const float4 e1 = p[1], e2 = p[2], e3 = p[3], e4 = p[4];
+        e.d[0] = e1.x; e.d[1] = e1.y; e.d[2] = e1.z; e.P = e1.w;
+        e.r[0] = e2.x; e.r[1] = e2.y; e.r[2] = e2.z;
+        e.A[0] = e3.x; e.A[1] = e3.y; e.A[2] = e3.z; e.A[3] = e3.w; e.A[4] = e4.x; e.A[5] = e4.y;
+    }
+    if (M == kAniso) {
+        const float4 e5 = p[5], e6 = p[6], e7 = p[7];
+        e.T[0] = e5.x; e.T[1] = e5.y; e.T[2] = e5.z; e.T[3] = e5.w; e.T[4] = e6.x; e.T[5] = e6.y;
+        e.g[0] = e6.z; e.g[1] = e6.w; e.g[2] = e7.x;
+    }
+}
+
+// symmetric 3x3 (compact) times vector
+template <typename T>
+ACVD_DEV void sym_mul(const T a[6], const T v[3], T o[3]) {
+    o[0] = a[0] * v[0] + a[1] * v[1] + a[2] * v[2];
+    o[1] = a[1] * v[0] + a[3] * v[1] + a[4] * v[2];
+    o[2] = a[2] * v[0] + a[4] * v[1] + a[5] * v[2];
+}
+
+// ---------------------------------------------------------------------------
+// Energy changes in float32, in forms built from local differences only
+// (x - m, m' - m, the residual r = b - A m) so that no large cancelling terms
+// appear.  E_iso = -|S|^2 / W; the QEM energy with the placed vertex c = m + delta
+// is W |delta|^2 - |S|^2 / W; the anisotropic energy is c^T T c - 2 c.u.
+// ---------------------------------------------------------------------------
+
+// Cluster X after removing (sgn = -1) or adding (sgn = +1) the item: weight,
+// centroid shift dm = m' - m and placement delta' (relative to m').
+template <int M>
+ACVD_DEV void modified_cluster(const EvalRec& c, const ItemRec& it, float sgn, int level, float thr,
+                               float& Wn, float dm[3], float dn[3]) {
+    Wn = c.W + sgn * it.w;
+    const float xm[3] = {it.x[0] - c.m[0], it.x[1] - c.m[1], it.x[2] - c.m[2]};
+    const float f = sgn * it.w / Wn;
+    dm[0] = f * xm[0]; dm[1] = f * xm[1]; dm[2] = f * xm[2];
+    float An[6];
+#pragma unroll
+    for (int j = 0; j < 6; j++) An[j] = c.A[j] + sgn * it.A[j];
+    float Aix[3], And[3];
+    sym_mul<float>(it.A, xm, Aix);
+    sym_mul<float>(An, dm, And);
+    const float rn[3] = {c.r[0] + sgn * Aix[0] - And[0], c.r[1] + sgn * Aix[1] - And[1],
+                         c.r[2] + sgn * Aix[2] - And[2]};
+    pinv_apply<float>(An, rn, dn, level, thr, 8);
+}
+
+// Energy change of cluster X (anisotropic metric) when its placed vertex moves by
+// e, ignoring the item's own term: -2 e.g + e^T T e.
+ACVD_DEV float aniso_shift(const EvalRec& c, const float e[3]) {
+    float Te[3];
+    sym_mul<float>(c.T, e, Te);
+    return -2.0f * (e[0] * c.g[0] + e[1] * c.g[1] + e[2] * c.g[2]) + (e[0] * Te[0] + e[1] * Te[1] + e[2] * Te[2]);
+}
+
+ACVD_DEV float item_quad(const float T[6], const float v[3]) {
+    float Tv[3];
+    sym_mul<float>(T, v, Tv);
+    return v[0] * Tv[0] + v[1] * Tv[1] + v[2] * Tv[2];
+}
+
+// Part of the energy change that depends on the source cluster L only.
+template <int M>
+ACVD_DEV float remove_part(const EvalRec& eL, const ItemRec& it, const RunFlags& fl, float cprime[3]) {
+    const float xm[3] = {it.x[0] - eL.m[0], it.x[1] - eL.m[1], it.x[2] - eL.m[2]};
+    const float d2 = xm[0] * xm[0] + xm[1] * xm[1] + xm[2] * xm[2];
+    if (M == kIso) return -it.w * eL.W / (eL.W - it.w) * d2;
+    if (M == kQEM) {
+        float v = -it.w * eL.W / (eL.W - it.w) * d2;
+        if (fl.constrained && fl.level > 0) {
+            float Wn, dm[3], dn[3];
+            modified_cluster<M>(eL, it, -1.0f, fl.level, fl.thr, Wn, dm, dn);
+            v += Wn * (dn[0] * dn[0] + dn[1] * dn[1] + dn[2] * dn[2]) - eL.P;
+        }
+        return v;
+    }
+    // anisotropic: shift of L's placed vertex, minus the item's own term at L'
+    float Wn, dm[3], dn[3];
+    modified_cluster<M>(eL, it, -1.0f, fl.level, fl.thr, Wn, dm, dn);
+    const float e[3] = {dm[0] + dn[0] - eL.d[0], dm[1] + dn[1] - eL.d[1], dm[2] + dn[2] - eL.d[2]};
+    const float xc[3] = {xm[0] - dm[0] - dn[0], xm[1] - dm[1] - dn[1], xm[2] - dm[2] - dn[2]};
+    cprime[0] = xc[0]; cprime[1] = xc[1]; cprime[2] = xc[2];
+    return aniso_shift(eL, e) - item_quad(it.T, xc);
+}
+
+template <int M>
+ACVD_DEV float add_part(const EvalRec& eB, const ItemRec& it, const RunFlags& fl) {
+    const float xm[3] = {it.x[0] - eB.m[0], it.x[1] - eB.m[1], it.x[2] - eB.m[2]};
+    const float d2 = xm[0] * xm[0] + xm[1] * xm[1] + xm[2] * xm[2];
+    if (M == kIso) return it.w * eB.W / (eB.W + it.w) * d2;
+    if (M == kQEM) {
+        float v = it.w * eB.W / (eB.W + it.w) * d2;
+        if (fl.constrained && fl.level > 0) {
+            float Wn, dm[3], dn[3];
+            modified_cluster<M>(eB, it, 1.0f, fl.level, fl.thr, Wn, dm, dn);
+            v += Wn * (dn[0] * dn[0] + dn[1] * dn[1] + dn[2] * dn[2]) - eB.P;
+        }
+        return v;
+    }
+    float Wn, dm[3], dn[3];
+    modified_cluster<M>(eB, it, 1.0f, fl.level, fl.thr, Wn, dm, dn);
+    const float e[3] = {dm[0] + dn[0] - eB.d[0], dm[1] + dn[1] - eB.d[1], dm[2] + dn[2] - eB.d[2]};
+    const float xc[3] = {xm[0] - dm[0] - dn[0], xm[1] - dm[1] - dn[1], xm[2] - dm[2] - dn[2]};
+    return aniso_shift(eB, e) + item_quad(it.T, xc);
+}
+
+// ---------------------------------------------------------------------------
+// local connectivity (vtkVerticesProcessing.h:168-237): the ring members of the
+// item that carry label L must stay connected through edges among themselves.
+// ---------------------------------------------------------------------------
+ACVD_DEV bool ring_connected(const DevState& st, int p0, int p1, int L) {
+    const int d = p1 - p0;
+    if (d > 32) return false;
+    unsigned msk = 0u;
+    for (int q = 0; q < d; q++)
+        if (st.label[st.col[p0 + q]] == L) msk |= 1u << q;
+    if (msk == 0u) return true;
+    unsigned vis = msk & (0u - msk);
+    unsigned front = vis;
+    while (front) {
+        unsigned nxt = 0u;
+        unsigned f = front;
+        while (f) {
+            const int q = __ffs(f) - 1;
+            f &= f - 1u;
+            nxt |= st.adj[p0 + q];
+        }
+        nxt &= msk & ~vis;
+        vis |= nxt;
+        front = nxt;
+    }
+    return vis == msk;
+}
+
+ACVD_DEV void warp_count(unsigned long long* ctr, unsigned v) {
+    const unsigned tot = __reduce_add_sync(kFull, v);
+    if ((threadIdx.x & 31) == 0 && tot) atomicAdd(ctr, (unsigned long long)tot);
+}
+
+// ---------------------------------------------------------------------------
+// eval: proposals for one colour class
+// ---------------------------------------------------------------------------
+template <int M>
+__global__ void __launch_bounds__(256) eval_kernel(DevState st, const int* __restrict__ items, int64_t count,
+                                                   int epoch, int* __restrict__ cand_dest,
+                                                   unsigned* __restrict__ cand_prio) {
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool in = idx < count;
+    unsigned n_slots = 0, n_bnd = 0, n_tgt = 0, n_cand = 0;
+    if (in) {
+        const int i = items[idx];
+        const int L = st.label[i];
+        const int p0 = st.row[i], p1 = st.row[i + 1];
+        n_slots = (unsigned)(p1 - p0);
+        bool boundary = false;
+        for (int p = p0; p < p1; p++) boundary |= (st.label[st.col[p]] != L);
+        if (boundary) {
+            n_bnd = 1;
+            const RunFlags fl = *st.flags;
+            ItemRec it;
+            load_item<M>(st, i, it);
+            if (L >= st.k) {
+                // unassigned item: joins the neighbouring cluster it is cheapest to join
+                int best = -1;
+                float bv = 0.0f;
+                for (int p = p0; p < p1; p++) {
+                    const int B = st.label[st.col[p]];
+                    if (B >= st.k) continue;
+                    const float4 e0 = st.ev[(int64_t)B * Layout<M>::ev];
+                    const float dx = it.x[0] - e0.x, dy = it.x[1] - e0.y, dz = it.x[2] - e0.z;
+                    const float v = it.w * e0.w / (e0.w + it.w) * (dx * dx + dy * dy + dz * dz);
+                    n_tgt++;
+                    if (best < 0 || v < bv || (v == bv && B < best)) { best = B; bv = v; }
+                }
+                if (best >= 0) {
+                    cand_dest[idx] = best;
+                    cand_prio[idx] = 0u;
+                    atomicMin(&st.claim[best], make_claim((unsigned)epoch, 0u, (unsigned)idx));
+                    n_cand = 1;
+                }
+            } else if (st.size[L] > 1 && (!fl.connexity || ring_connected(st, p0, p1, L))) {
+                EvalRec eL;
+                load_eval<M>(st, L, eL);
+                float xc[3];
+                const float rem = remove_part<M>(eL, it, fl, xc);
+                int best = -1;
+                float bde = 0.0f;
+                for (int p = p0; p < p1; p++) {
+                    const int B = st.label[st.col[p]];
+                    if (B == L || B >= st.k) continue;
+                    bool dup = false;
+                    for (int q = p0; q < p; q++) dup |= (st.label[st.col[q]] == B);
+                    if (dup) continue;
+                    EvalRec eB;
+                    load_eval<M>(st, B, eB);
+                    const float de = rem + add_part<M>(eB, it, fl);
+                    n_tgt++;
+                    if (de < bde || (de == bde && best >= 0 && B < best)) { best = B; bde = de; }
+                }
+                if (best >= 0 && bde < 0.0f) {
+                    const unsigned pr = prio_of_delta(bde);
+                    cand_dest[idx] = best;
+                    cand_prio[idx] = pr;
+                    const unsigned long long c = make_claim((unsigned)epoch, pr, (unsigned)idx);
+                    atomicMin(&st.claim[L], c);
+                    atomicMin(&st.claim[best], c);
+                    n_cand = 1;
+                }
+            }
+        }
+    }
+    warp_count(&st.counters[kCntVisited], in ? 1u : 0u);
+    warp_count(&st.counters[kCntSlots], n_slots);
+    warp_count(&st.counters[kCntBoundary], n_bnd);
+    warp_count(&st.counters[kCntTargets], n_tgt);
+    warp_count(&st.counters[kCntCand], n_cand);
+}
+
+// ---------------------------------------------------------------------------
+// accumulators
+// ---------------------------------------------------------------------------
+// Adds sgn * (contribution of item i) to a cluster accumulator (double-float):
+// S += w x, W += w, A += A_i, b += A_i x, T += T_i, u += T_i x, with the
+// products formed exactly (TwoProd) so that b and u stay consistent with A, T, x.
+template <int M>
+ACVD_DEV void accumulate_item(df* acc, const ItemRec& it, float sgn) {
+    auto addp = [&](int j, float a, float b) {
+        const df p = two_prod(a, b);
+        acc[j] = df_add(acc[j], sgn > 0 ? p : df_neg(p));
+    };
+    auto addf = [&](int j, float a) { acc[j] = df_add_f(acc[j], sgn * a); };
+    addp(0, it.w, it.x[0]);
+    addp(1, it.w, it.x[1]);
+    addp(2, it.w, it.x[2]);
+    addf(3, it.w);
+    if (M == kIso) return;
+#pragma unroll
+    for (int j = 0; j < 6; j++) addf(4 + j, it.A[j]);
+    const int rowi[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        addp(10 + c, it.A[rowi[c][0]], it.x[0]);
+        addp(10 + c, it.A[rowi[c][1]], it.x[1]);
+        addp(10 + c, it.A[rowi[c][2]], it.x[2]);
+    }
+    if (M == kQEM) return;
+#pragma unroll
+    for (int j = 0; j < 6; j++) addf(13 + j, it.T[j]);
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        addp(19 + c, it.T[rowi[c][0]], it.x[0]);
+        addp(19 + c, it.T[rowi[c][1]], it.x[1]);
+        addp(19 + c, it.T[rowi[c][2]], it.x[2]);
+    }
+}
+
+// Per-cluster evaluation record and FP64 energy from the accumulators
+// (ComputeClusterCentroid + ComputeClusterEnergy of the metric plugins; the
+// quadric placement with the reference's thresholded pseudo-inverse in FP64).
+template <int M>
+ACVD_DEV void update_cluster(const DevState& st, int k) {
+    const df* a = st.acc + (int64_t)k * Layout<M>::acc;
+    float4* ev = st.ev + (int64_t)k * Layout<M>::ev;
+    const double W = df_to_d(a[3]);
+    const double S[3] = {df_to_d(a[0]), df_to_d(a[1]), df_to_d(a[2])};
+    if (!(W > 0.0)) {
+        ev[0] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (M != kIso) for (int j = 1; j < Layout<M>::ev; j++) ev[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+        st.energy[k] = 0.0;
+        return;
+    }
+    const double m[3] = {S[0] / W, S[1] / W, S[2] / W};
+    ev[0] = make_float4((float)m[0], (float)m[1], (float)m[2], (float)W);
+    const double S2W = (S[0] * S[0] + S[1] * S[1] + S[2] * S[2]) / W;
+    if (M == kIso) {
+        st.energy[k] = -S2W;
+        return;
+    }
+    const RunFlags fl = *st.flags;
+    double A[6], b[3];
+    for (int j = 0; j < 6; j++) A[j] = df_to_d(a[4 + j]);
+    for (int j = 0; j < 3; j++) b[j] = df_to_d(a[10 + j]);
+    double Am[3];
+    sym_mul<double>(A, m, Am);
+    const double r[3] = {b[0] - Am[0], b[1] - Am[1], b[2] - Am[2]};
+    double d[3] = {0.0, 0.0, 0.0};
+    const bool place = (M == kAniso) || (fl.constrained && fl.level > 0);
+    if (place) pinv_apply<double>(A, r, d, fl.level, (double)fl.thr, 32);
+    const double P = W * (d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+    ev[1] = make_float4((float)d[0], (float)d[1], (float)d[2], (float)P);
+    ev[2] = make_float4((float)r[0], (float)r[1], (float)r[2], 0.f);
+    ev[3] = make_float4((float)A[0], (float)A[1], (float)A[2], (float)A[3]);
+    if (M == kQEM) {
+        ev[4] = make_float4((float)A[4], (float)A[5], 0.f, 0.f);
+        st.energy[k] = P - S2W;
+        return;
+    }
+    double T[6], u[3];
+    for (int j = 0; j < 6; j++) T[j] = df_to_d(a[13 + j]);
+    for (int j = 0; j < 3; j++) u[j] = df_to_d(a[19 + j]);
+    const double c[3] = {m[0] + d[0], m[1] + d[1], m[2] + d[2]};
+    double Tc[3];
+    sym_mul<double>(T, c, Tc);
+    const double g[3] = {u[0] - Tc[0], u[1] - Tc[1], u[2] - Tc[2]};
+    ev[4] = make_float4((float)A[4], (float)A[5], 0.f, 0.f);
+    ev[5] = make_float4((float)T[0], (float)T[1], (float)T[2], (float)T[3]);
+    ev[6] = make_float4((float)T[4], (float)T[5], (float)g[0], (float)g[1]);
+    ev[7] = make_float4((float)g[2], 0.f, 0.f, 0.f);
+    st.energy[k] = (c[0] * Tc[0] + c[1] * Tc[1] + c[2] * Tc[2]) - 2.0 * (c[0] * u[0] + c[1] * u[1] + c[2] * u[2]);
+}
+
+// ---------------------------------------------------------------------------
+// apply: commit the proposals that hold both claims
+// ---------------------------------------------------------------------------
+template <int M>
+__global__ void __launch_bounds__(256) apply_kernel(DevState st, const int* __restrict__ items, int64_t count,
+                                                    int epoch, int* __restrict__ cand_dest,
+                                                    const unsigned* __restrict__ cand_prio) {
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned won = 0;
+    if (idx < count) {
+        const int B = cand_dest[idx];
+        if (B >= 0) {
+            cand_dest[idx] = -1;
+            const int i = items[idx];
+            const int L = st.label[i];
+            const unsigned long long key = make_claim((unsigned)epoch, cand_prio[idx], (unsigned)idx);
+            if (st.claim[B] == key && (L >= st.k || st.claim[L] == key)) {
+                won = 1;
+                ItemRec it;
+                load_item<M>(st, i, it);
+                st.label[i] = B;
+                st.size[B] += 1;
+                df* aB = st.acc + (int64_t)B * Layout<M>::acc;
+                accumulate_item<M>(aB, it, 1.0f);
+                update_cluster<M>(st, B);
+                if (L < st.k) {
+                    st.size[L] -= 1;
+                    df* aL = st.acc + (int64_t)L * Layout<M>::acc;
+                    accumulate_item<M>(aL, it, -1.0f);
+                    update_cluster<M>(st, L);
+                }
+            }
+        }
+    }
+    warp_count(&st.counters[kCntMoves], won);
+}
+
+// ---------------------------------------------------------------------------
+// full recompute of the accumulators: items sorted by cluster, one warp per
+// cluster, fixed-order butterfly reduction (deterministic)
+// ---------------------------------------------------------------------------
+__global__ void cluster_keys_kernel(DevState st, uint32_t* __restrict__ keys, uint32_t* __restrict__ vals,
+                                    uint32_t* __restrict__ counts) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= st.n) return;
+    int L = st.label[i];
+    if (L < 0 || L > st.k) L = st.k;
+    keys[i] = (uint32_t)L;
+    vals[i] = (uint32_t)i;
+    if (L < st.k) atomicAdd(&counts[L], 1u);
+}
+
+template <int M>
+__global__ void __launch_bounds__(256) reduce_clusters_kernel(DevState st, const uint32_t* __restrict__ sorted,
+                                                              const uint32_t* __restrict__ seg_off,
+                                                              const uint32_t* __restrict__ seg_cnt) {
+    constexpr int NA = Layout<M>::acc;
+    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (w >= st.k) return;
+    const uint32_t off = seg_off[w], cnt = seg_cnt[w];
+    df acc[NA];
+#pragma unroll
+    for (int j = 0; j < NA; j++) acc[j] = {0.f, 0.f};
+    for (uint32_t j = lane; j < cnt; j += 32) {
+        ItemRec it;
+        load_item<M>(st, (int)sorted[off + j], it);
+        accumulate_item<M>(acc, it, 1.0f);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+        for (int j = 0; j < NA; j++) {
+            df t;
+            t.hi = __shfl_xor_sync(kFull, acc[j].hi, o);
+            t.lo = __shfl_xor_sync(kFull, acc[j].lo, o);
+            // same operand order on both partners -> identical results
+            acc[j] = (lane & o) ? df_add(t, acc[j]) : df_add(acc[j], t);
+        }
+    }
+    if (lane == 0) {
+        df* dst = st.acc + w * NA;
+#pragma unroll
+        for (int j = 0; j < NA; j++) dst[j] = acc[j];
+        st.size[w] = (int)cnt;
+    }
+}
+
+template <int M>
+__global__ void update_all_kernel(DevState st) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < st.k) update_cluster<M>(st, (int)k);
+}
+
+// ---------------------------------------------------------------------------
+// connectivity cleaning: min-id label propagation over same-cluster edges with
+// pointer jumping; each cluster keeps its largest component (ties -> the one
+// containing the smallest item id), the rest become unassigned
+// ---------------------------------------------------------------------------
+__global__ void comp_init_kernel(DevState st, int* __restrict__ comp) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= st.n) return;
+    comp[i] = st.label[i] < st.k ? (int)i : -1;
+}
+
+__global__ void comp_step_kernel(DevState st, int* __restrict__ comp) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= st.n) return;
+    const int L = st.label[i];
+    if (L >= st.k) return;
+    const int cur = comp[i];
+    int m = cur;
+    for (int p = st.row[i]; p < st.row[i + 1]; p++) {
+        const int j = st.col[p];
+        if (st.label[j] == L) m = min(m, comp[j]);
+    }
+    for (int hop = 0; hop < 64; hop++) {
+        const int mm = comp[m];
+        if (mm >= m) break;
+        m = mm;
+    }
+    if (m < cur) {
+        comp[i] = m;
+        atomicAdd(&st.counters[kCntChanged], 1ull);
+    }
+}
+
+__global__ void comp_size_kernel(DevState st, const int* __restrict__ comp, int* __restrict__ csize) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= st.n) return;
+    if (st.label[i] < st.k) atomicAdd(&csize[comp[i]], 1);
+}
+
+__global__ void comp_best_kernel(DevState st, const int* __restrict__ comp, const int* __restrict__ csize,
+                                 unsigned long long* __restrict__ best) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= st.n) return;
+    const int L = st.label[i];
+    if (L >= st.k || comp[i] != (int)i) return;
+    const unsigned long long key = ((unsigned long long)(unsigned)csize[i] << 32) | (0xffffffffull - (uint32_t)i);
+    atomicMax(&best[L], key);
+}
+
+__global__ void comp_reset_kernel(DevState st, const int* __restrict__ comp,
+                                  const unsigned long long* __restrict__ best, int* __restrict__ multi) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= st.n) return;
+    const int L = st.label[i];
+    if (L >= st.k) return;
+    const uint32_t root = 0xffffffffu - (uint32_t)(best[L] & 0xffffffffull);
+    if ((uint32_t)comp[i] != root) {
+        st.label[i] = st.k;
+        if (atomicExch(&multi[L], 1) == 0) atomicAdd(&st.counters[kCntDisconnected], 1ull);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// hole filling, one colour class at a time: an unassigned item joins the
+// cluster of its first assigned ring neighbour (ring order); with the
+// connectivity constraint on, only if the unassigned ring members stay
+// connected without it (the reference applies the same local test to the null
+// cluster, Common/vtkUniformClustering.h:606-607)
+// ---------------------------------------------------------------------------
+__global__ void fill_color_kernel(DevState st, const int* __restrict__ items, int64_t count) {
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned done = 0;
+    if (idx < count) {
+        const int i = items[idx];
+        if (st.label[i] >= st.k) {
+            const int p0 = st.row[i], p1 = st.row[i + 1];
+            int B = -1;
+            for (int p = p0; p < p1 && B < 0; p++) {
+                const int l = st.label[st.col[p]];
+                if (l < st.k) B = l;
+            }
+            if (B >= 0 && (!st.flags->connexity || ring_connected(st, p0, p1, st.k))) {
+                st.label[i] = B;
+                done = 1;
+            }
+        }
+    }
+    warp_count(&st.counters[kCntAssigned], done);
+}
+
+// ---------------------------------------------------------------------------
+// boundary edges, compaction, dual mesh
+// ---------------------------------------------------------------------------
+__global__ void boundary_edges_kernel(const int* __restrict__ ev, int64_t ne, const int* __restrict__ label,
+                                      uint32_t* __restrict__ flags) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= ne) return;
+    flags[e] = label[ev[2 * e]] != label[ev[2 * e + 1]] ? 1u : 0u;
+}
+
+__global__ void compact_kernel(const uint32_t* __restrict__ flags, const uint32_t* __restrict__ pos, int64_t n,
+                               int* __restrict__ out) {
+    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < n && flags[j]) out[pos[j]] = (int)j;
+}
+
+__global__ void dual_faces_kernel(const int* __restrict__ tri, int64_t nf, const int* __restrict__ label, int k,
+                                  uint32_t* __restrict__ flags) {
+    const int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= nf) return;
+    const int a = label[tri[3 * f]], b = label[tri[3 * f + 1]], c = label[tri[3 * f + 2]];
+    flags[f] = (a < k && b < k && c < k && a >= 0 && b >= 0 && c >= 0 && a != b && b != c && a != c) ? 1u : 0u;
+}
+
+// canonical key of the sorted label triple s0 < s1 < s2 (21 bits each), split in
+// a low and a high 32-bit word
+__global__ void dual_keys_kernel(const int* __restrict__ tri, const int* __restrict__ faces, int64_t m,
+                                 const int* __restrict__ label, uint32_t* __restrict__ klo,
+                                 uint32_t* __restrict__ khi, uint32_t* __restrict__ order) {
+    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= m) return;
+    const int f = faces[j];
+    int a = label[tri[3 * f]], b = label[tri[3 * f + 1]], c = label[tri[3 * f + 2]];
+    if (a > b) { const int t = a; a = b; b = t; }
+    if (b > c) { const int t = b; b = c; c = t; }
+    if (a > b) { const int t = a; a = b; b = t; }
+    const unsigned long long key = ((unsigned long long)a << 42) | ((unsigned long long)b << 21) | (unsigned long long)c;
+    klo[j] = (uint32_t)(key & 0xffffffffull);
+    khi[j] = (uint32_t)(key >> 32);
+    order[j] = (uint32_t)j;
+}
+
+__global__ void gather_u32_kernel(const uint32_t* __restrict__ src, const uint32_t* __restrict__ idx, int64_t m,
+                                  uint32_t* __restrict__ dst) {
+    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < m) dst[j] = src[idx[j]];
+}
+
+// after the stable sort by (khi, klo): keep the first face of every distinct triple
+__global__ void dual_unique_kernel(const uint32_t* __restrict__ klo_sorted, const uint32_t* __restrict__ khi_sorted,
+                                   const uint32_t* __restrict__ order, int64_t m, uint32_t* __restrict__ keep) {
+    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= m) return;
+    const bool first = (j == 0) || klo_sorted[j] != klo_sorted[j - 1] || khi_sorted[j] != khi_sorted[j - 1];
+    keep[order[j]] = first ? 1u : 0u;
+}
+
+__global__ void dual_write_kernel(const int* __restrict__ tri, const int* __restrict__ faces,
+                                  const int* __restrict__ sel, int64_t t, const int* __restrict__ label,
+                                  int* __restrict__ out) {
+    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= t) return;
+    const int f = faces[sel[j]];
+    out[3 * j] = label[tri[3 * f]];
+    out[3 * j + 1] = label[tri[3 * f + 1]];
+    out[3 * j + 2] = label[tri[3 * f + 2]];
+}
+
+// FP64 placed vertex of every cluster (output vertices of the coarse mesh)
+template <int M>
+__global__ void centroids_kernel(DevState st, double* __restrict__ out) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= st.k) return;
+    const df* a = st.acc + k * Layout<M>::acc;
+    const double W = df_to_d(a[3]);
+    double m[3] = {df_to_d(a[0]) / W, df_to_d(a[1]) / W, df_to_d(a[2]) / W};
+    if (M != kIso) {
+        const RunFlags fl = *st.flags;
+        if (M == kAniso || (fl.constrained && fl.level > 0)) {
+            double A[6], b[3], Am[3], d[3];
+            for (int j = 0; j < 6; j++) A[j] = df_to_d(a[4 + j]);
+            for (int j = 0; j < 3; j++) b[j] = df_to_d(a[10 + j]);
+            sym_mul<double>(A, m, Am);
+            const double r[3] = {b[0] - Am[0], b[1] - Am[1], b[2] - Am[2]};
+            pinv_apply<double>(A, r, d, fl.level, (double)fl.thr, 32);
+            m[0] += d[0]; m[1] += d[1]; m[2] += d[2];
+        }
+    }
+    out[3 * k] = m[0]; out[3 * k + 1] = m[1]; out[3 * k + 2] = m[2];
+}
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+static inline unsigned nblk(int64_t n, int b = 256) { return (unsigned)((n + b - 1) / b); }
+
+#define ACVD_DISPATCH(metric, KERNEL, grid, block, stream, ...)                         \
+    do {                                                                                \
+        ++g_launches;                                                                   \
+        if ((metric) == kIso) KERNEL<kIso><<<grid, block, 0, stream>>>(__VA_ARGS__);     \
+        else if ((metric) == kQEM) KERNEL<kQEM><<<grid, block, 0, stream>>>(__VA_ARGS__); \
+        else KERNEL<kAniso><<<grid, block, 0, stream>>>(__VA_ARGS__);                     \
+    } while (0)
+
+cudaError_t launch_eval(int metric, const DevState& st, const int* items, int64_t count, int epoch,
+                        int* cand_dest, unsigned* cand_prio, cudaStream_t s) {
+    if (count == 0) return cudaSuccess;
+    ACVD_DISPATCH(metric, eval_kernel, nblk(count), 256, s, st, items, count, epoch, cand_dest, cand_prio);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_apply(int metric, const DevState& st, const int* items, int64_t count, int epoch,
+                         int* cand_dest, const unsigned* cand_prio, cudaStream_t s) {
+    if (count == 0) return cudaSuccess;
+    ACVD_DISPATCH(metric, apply_kernel, nblk(count), 256, s, st, items, count, epoch, cand_dest, cand_prio);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_update_all(int metric, const DevState& st, cudaStream_t s) {
+    if (st.k == 0) return cudaSuccess;
+    ACVD_DISPATCH(metric, update_all_kernel, nblk(st.k, 128), 128, s, st);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_cluster_keys(const DevState& st, uint32_t* keys, uint32_t* vals, uint32_t* counts,
+                                cudaStream_t s) {
+    if (st.n == 0) return cudaSuccess;
+    ++g_launches;
+    cluster_keys_kernel<<<nblk(st.n), 256, 0, s>>>(st, keys, vals, counts);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_reduce_clusters(int metric, const DevState& st, const uint32_t* sorted_items,
+                                   const uint32_t* seg_off, const uint32_t* seg_cnt, cudaStream_t s) {
+    if (st.k == 0) return cudaSuccess;
+    ACVD_DISPATCH(metric, reduce_clusters_kernel, nblk((int64_t)st.k * 32), 256, s, st, sorted_items, seg_off,
+                  seg_cnt);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_comp_init(const DevState& st, int* comp, cudaStream_t s) {
+    ++g_launches;
+    comp_init_kernel<<<nblk(st.n), 256, 0, s>>>(st, comp);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_comp_step(const DevState& st, int* comp, cudaStream_t s) {
+    ++g_launches;
+    comp_step_kernel<<<nblk(st.n), 256, 0, s>>>(st, comp);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_comp_finish(const DevState& st, const int* comp, int* csize, unsigned long long* best,
+                               int* multi, cudaStream_t s) {
+    ++g_launches;
+    comp_size_kernel<<<nblk(st.n), 256, 0, s>>>(st, comp, csize);
+    ++g_launches;
+    comp_best_kernel<<<nblk(st.n), 256, 0, s>>>(st, comp, csize, best);
+    ++g_launches;
+    comp_reset_kernel<<<nblk(st.n), 256, 0, s>>>(st, comp, best, multi);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fill_color(const DevState& st, const int* items, int64_t count, cudaStream_t s) {
+    if (count == 0) return cudaSuccess;
+    ++g_launches;
+    fill_color_kernel<<<nblk(count), 256, 0, s>>>(st, items, count);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_boundary_edges(const int* edge_v, int64_t ne, const int* label, uint32_t* flags,
+                                  cudaStream_t s) {
+    if (ne == 0) return cudaSuccess;
+    ++g_launches;
+    boundary_edges_kernel<<<nblk(ne), 256, 0, s>>>(edge_v, ne, label, flags);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_compact(const uint32_t* flags, const uint32_t* pos, int64_t n, int* out, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    ++g_launches;
+    compact_kernel<<<nblk(n), 256, 0, s>>>(flags, pos, n, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_dual_faces(const int* tri, int64_t nf, const int* label, int k, uint32_t* flags,
+                              cudaStream_t s) {
+    if (nf == 0) return cudaSuccess;
+    ++g_launches;
+    dual_faces_kernel<<<nblk(nf), 256, 0, s>>>(tri, nf, label, k, flags);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_dual_keys(const int* tri, const int* faces, int64_t m, const int* label, uint32_t* klo,
+                             uint32_t* khi, uint32_t* order, cudaStream_t s) {
+    if (m == 0) return cudaSuccess;
+    ++g_launches;
+    dual_keys_kernel<<<nblk(m), 256, 0, s>>>(tri, faces, m, label, klo, khi, order);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gather_u32(const uint32_t* src, const uint32_t* idx, int64_t m, uint32_t* dst, cudaStream_t s) {
+    if (m == 0) return cudaSuccess;
+    ++g_launches;
+    gather_u32_kernel<<<nblk(m), 256, 0, s>>>(src, idx, m, dst);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_dual_unique(const uint32_t* klo, const uint32_t* khi, const uint32_t* order, int64_t m,
+                               uint32_t* keep, cudaStream_t s) {
+    if (m == 0) return cudaSuccess;
+    ++g_launches;
+    dual_unique_kernel<<<nblk(m), 256, 0, s>>>(klo, khi, order, m, keep);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_dual_write(const int* tri, const int* faces, const int* sel, int64_t t, const int* label,
+                              int* out, cudaStream_t s) {
+    if (t == 0) return cudaSuccess;
+    ++g_launches;
+    dual_write_kernel<<<nblk(t), 256, 0, s>>>(tri, faces, sel, t, label, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_centroids(int metric, const DevState& st, double* out, cudaStream_t s) {
+    if (st.k == 0) return cudaSuccess;
+    ACVD_DISPATCH(metric, centroids_kernel, nblk(st.k), 256, s, st, out);
+    return cudaGetLastError();
+}
+
+}  // namespace acvd

@@ -1,0 +1,185 @@
+// Shared device helpers for the ACVD clustering kernels (sm_103a).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#define ACVD_DEV __device__ __forceinline__
+#define ACVD_HD __host__ __device__ __forceinline__
+
+namespace acvd {
+
+constexpr int kWarp = 32;
+constexpr unsigned kFull = 0xffffffffu;
+
+// ---------------------------------------------------------------------------
+// Compensated float32 accumulation ("double-float"): value = hi + lo with
+// |lo| <= ulp(hi)/2.  Additions use Knuth's TwoSum; products of two floats are
+// split exactly with an FMA (TwoProd).  About 48 significant bits, float ALUs only.
+// ---------------------------------------------------------------------------
+struct df { float hi, lo; };
+
+ACVD_DEV df df_make(float x) { return {x, 0.0f}; }
+
+ACVD_DEV void two_sum(float a, float b, float& s, float& e) {
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+ACVD_DEV void fast_two_sum(float a, float b, float& s, float& e) {
+    s = __fadd_rn(a, b);
+    e = __fsub_rn(b, __fsub_rn(s, a));
+}
+
+// x += y (both double-float)
+ACVD_DEV df df_add(df x, df y) {
+    float s, e;
+    two_sum(x.hi, y.hi, s, e);
+    e = __fadd_rn(e, __fadd_rn(x.lo, y.lo));
+    float h, l;
+    fast_two_sum(s, e, h, l);
+    return {h, l};
+}
+
+ACVD_DEV df df_add_f(df x, float y) {
+    float s, e;
+    two_sum(x.hi, y, s, e);
+    e = __fadd_rn(e, x.lo);
+    float h, l;
+    fast_two_sum(s, e, h, l);
+    return {h, l};
+}
+
+ACVD_DEV df df_neg(df x) { return {-x.hi, -x.lo}; }
+
+// exact product of two floats as a double-float
+ACVD_DEV df two_prod(float a, float b) {
+    const float p = __fmul_rn(a, b);
+    const float e = __fmaf_rn(a, b, -p);
+    return {p, e};
+}
+
+ACVD_DEV double df_to_d(df x) { return (double)x.hi + (double)x.lo; }
+
+ACVD_DEV df df_from_d(double v) {
+    const float h = __double2float_rn(v);
+    const float l = __double2float_rn(v - (double)h);
+    return {h, l};
+}
+
+// ---------------------------------------------------------------------------
+// Claim words: [8-bit epoch (descending)][30-bit priority][26-bit item slot].
+// Smaller is better, so atomicMin keeps the best candidate of the newest step
+// without a reset pass between steps.
+// ---------------------------------------------------------------------------
+constexpr int kEpochBits = 8;
+constexpr int kPrioBits = 30;
+constexpr int kSlotBits = 26;
+constexpr unsigned long long kClaimEmpty = ~0ull;
+
+ACVD_HD unsigned long long make_claim(unsigned epoch, unsigned prio, unsigned slot) {
+    const unsigned long long e = (unsigned long long)(255u - (epoch & 255u));
+    return (e << (kPrioBits + kSlotBits)) |
+           ((unsigned long long)(prio & ((1u << kPrioBits) - 1u)) << kSlotBits) |
+           (unsigned long long)(slot & ((1u << kSlotBits) - 1u));
+}
+
+// Priority of an energy decrease dE < 0: larger |dE| gives a smaller priority.
+ACVD_DEV unsigned prio_of_delta(float dE) {
+    const unsigned mag = __float_as_uint(dE) & 0x7fffffffu;   // |dE| bits, monotone in |dE|
+    const unsigned q = mag >> 1;                               // 30 bits
+    return ((1u << kPrioBits) - 1u) - q;
+}
+
+// ---------------------------------------------------------------------------
+// Small symmetric 3x3 eigen-solver by cyclic Jacobi rotations (Jacobi 1846;
+// Golub & Van Loan, Matrix Computations, sec. 8.5).  a = {a00,a01,a02,a11,a12,a22}.
+// On return w holds the eigenvalues and V (columns) the eigenvectors.
+// ---------------------------------------------------------------------------
+template <typename T>
+ACVD_DEV void jacobi_eig3(const T a6[6], T w[3], T V[3][3], int max_sweeps) {
+    T A[3][3] = {{a6[0], a6[1], a6[2]}, {a6[1], a6[3], a6[4]}, {a6[2], a6[4], a6[5]}};
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) V[i][j] = (i == j) ? T(1) : T(0);
+    const T tiny = sizeof(T) == 4 ? T(1e-14) : T(1e-30);
+    for (int s = 0; s < max_sweeps; s++) {
+        const T off = A[0][1] * A[0][1] + A[0][2] * A[0][2] + A[1][2] * A[1][2];
+        const T dg = A[0][0] * A[0][0] + A[1][1] * A[1][1] + A[2][2] * A[2][2];
+        if (!(off > tiny * dg)) break;
+#pragma unroll
+        for (int pq = 0; pq < 3; pq++) {
+            const int p = pq == 2 ? 1 : 0;
+            const int q = pq == 0 ? 1 : 2;
+            const T apq = A[p][q];
+            if (apq == T(0)) continue;
+            const T theta = (A[q][q] - A[p][p]) / (T(2) * apq);
+            const T t = (theta >= T(0) ? T(1) : T(-1)) / (fabs(theta) + sqrt(theta * theta + T(1)));
+            const T c = T(1) / sqrt(t * t + T(1));
+            const T sn = t * c;
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                const T akp = A[k][p], akq = A[k][q];
+                A[k][p] = c * akp - sn * akq;
+                A[k][q] = sn * akp + c * akq;
+            }
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                const T apk = A[p][k], aqk = A[q][k];
+                A[p][k] = c * apk - sn * aqk;
+                A[q][k] = sn * apk + c * aqk;
+            }
+            A[p][q] = A[q][p] = T(0);
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                const T vkp = V[k][p], vkq = V[k][q];
+                V[k][p] = c * vkp - sn * vkq;
+                V[k][q] = sn * vkp + c * vkq;
+            }
+        }
+    }
+    w[0] = A[0][0]; w[1] = A[1][1]; w[2] = A[2][2];
+}
+
+// Thresholded pseudo-inverse applied to r, as the reference's quadric vertex
+// placement does (Common/vtkQuadricTools.cxx:83-163): eigenvalues are taken in
+// decreasing |lambda|; at most `level` of them, and only those with
+// |lambda| / max|lambda| > thr, are inverted.  Returns pinv(A) r in d and the
+// rank deficiency.
+template <typename T>
+ACVD_DEV int pinv_apply(const T a6[6], const T r[3], T d[3], int level, T thr, int max_sweeps) {
+    T w[3], V[3][3];
+    jacobi_eig3<T>(a6, w, V, max_sweeps);
+    T aw[3] = {fabs(w[0]), fabs(w[1]), fabs(w[2])};
+    const T mx = fmax(aw[0], fmax(aw[1], aw[2]));
+    d[0] = d[1] = d[2] = T(0);
+    int used = 0, rank_def = 0;
+#pragma unroll
+    for (int it = 0; it < 3; it++) {
+        int im = 0;
+        if (aw[1] > aw[im]) im = 1;
+        if (aw[2] > aw[im]) im = 2;
+        const T lam = w[im];
+        const bool keep = (mx > T(0)) && (aw[im] > thr * mx) && (used < level);
+        if (keep) {
+            const T proj = (V[0][im] * r[0] + V[1][im] * r[1] + V[2][im] * r[2]) / lam;
+            d[0] += proj * V[0][im];
+            d[1] += proj * V[1][im];
+            d[2] += proj * V[2][im];
+            used++;
+        } else {
+            rank_def++;
+        }
+        aw[im] = T(-1);
+    }
+    return rank_def;
+}
+
+ACVD_DEV float warp_sum(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+    return v;
+}
+
+}  // namespace acvd

@@ -1,0 +1,781 @@
+// Host orchestration of the GPU clustering (the MinimizeEnergy() seam) and the
+// C ABI declared in include/acvd_gpu.h.
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/acvd_gpu.h"
+#include "primitives.cuh"
+#include "state.cuh"
+
+using namespace acvd;
+
+namespace {
+
+template <class T>
+struct DBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    cudaError_t resize(size_t m) {
+        if (m <= n && p) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+        cudaError_t e = cudaMalloc((void**)&p, std::max<size_t>(m, 1) * sizeof(T));
+        if (e == cudaSuccess) n = m;
+        return e;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    ~DBuf() { release(); }
+};
+
+}  // namespace
+
+struct acvd_ctx {
+    acvd_opts opts;
+    std::string err;
+    cudaStream_t s = nullptr;
+    bool ready_mesh = false, ready_metric = false, ready_labels = false;
+
+    // mesh
+    int64_t nV = 0, nF = 0, nE = 0;
+    int max_deg = 0;
+    DBuf<double> xyz;
+    DBuf<int> tri, row, col, edge_v;
+    DBuf<unsigned> adj;
+    int ncolors = 0;
+    std::vector<int64_t> color_off;
+    DBuf<int> color_items, cand_dest;
+    DBuf<unsigned> cand_prio;
+
+    // items
+    int metric = -1;
+    DBuf<float4> xw, qa, ta;
+    DBuf<float2> qb, tb;
+
+    // clusters
+    int K = 0;
+    DBuf<int> label, size;
+    DBuf<unsigned long long> claim;
+    DBuf<df> acc;
+    DBuf<float4> ev;
+    DBuf<double> energy;
+    DBuf<unsigned long long> counters;
+    unsigned long long* h_counters = nullptr;
+    DBuf<RunFlags> dflags;
+    RunFlags flags{1, 0, 3, 1e-3f};
+    int level = 3;
+    int unconstrained = 0;
+
+    // work
+    DBuf<uint32_t> wk_a, wk_b, wk_c, wk_d, wk_cnt, wk_off;
+    DBuf<int> comp, csize, multi, wk_int;
+    DBuf<unsigned long long> best;
+    DBuf<double> dtmp;
+    Scratch scratch;
+
+    // sweep graph; one event pair per colour class brackets its evaluation kernel
+    cudaGraphExec_t sweep_exec = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    std::vector<cudaEvent_t> ev_eval;
+    int64_t launches = 0;          // kernels launched by acvd_minimize
+    int64_t sweep_kernels = 0;     // kernels in one sweep
+    DBuf<int> label_init;          // the assignment given to acvd_set_labels (for acvd_rewind)
+
+    DevState state() {
+        DevState st;
+        st.n = nV;
+        st.k = K;
+        st.row = row.p;
+        st.col = col.p;
+        st.adj = adj.p;
+        st.xw = xw.p;
+        st.qa = qa.p;
+        st.qb = qb.p;
+        st.ta = ta.p;
+        st.tb = tb.p;
+        st.label = label.p;
+        st.size = size.p;
+        st.claim = claim.p;
+        st.acc = acc.p;
+        st.ev = ev.p;
+        st.energy = energy.p;
+        st.counters = counters.p;
+        st.flags = dflags.p;
+        return st;
+    }
+    void drop_graph() {
+        if (sweep_exec) cudaGraphExecDestroy(sweep_exec);
+        sweep_exec = nullptr;
+    }
+    void drop_events() {
+        for (cudaEvent_t e : ev_eval) cudaEventDestroy(e);
+        ev_eval.clear();
+    }
+};
+
+#define CK(call)                                                              \
+    do {                                                                      \
+        cudaError_t _e = (call);                                              \
+        if (_e != cudaSuccess) return fail_cuda(ctx, _e, #call, __LINE__);   \
+    } while (0)
+
+static int fail(acvd_ctx* ctx, int code, const std::string& msg) {
+    if (ctx) ctx->err = msg;
+    return code;
+}
+
+static int fail_cuda(acvd_ctx* ctx, cudaError_t e, const char* what, int line) {
+    char buf[512];
+    std::snprintf(buf, sizeof buf, "CUDA error %d (%s) at engine.cu:%d: %s", (int)e, cudaGetErrorString(e), line,
+                  what);
+    return fail(ctx, ACVD_ERR_CUDA, buf);
+}
+
+static int sync_counters(acvd_ctx* ctx) {
+    CK(cudaMemcpyAsync(ctx->h_counters, ctx->counters.p, kNumCounters * sizeof(unsigned long long),
+                       cudaMemcpyDeviceToHost, ctx->s));
+    CK(cudaStreamSynchronize(ctx->s));
+    return ACVD_OK;
+}
+
+static int upload_flags(acvd_ctx* ctx) {
+    CK(cudaMemcpyAsync(ctx->dflags.p, &ctx->flags, sizeof(RunFlags), cudaMemcpyHostToDevice, ctx->s));
+    CK(cudaStreamSynchronize(ctx->s));
+    return ACVD_OK;
+}
+
+static cudaError_t zero_counter(acvd_ctx* ctx, int which) {
+    return cudaMemsetAsync(ctx->counters.p + which, 0, sizeof(unsigned long long), ctx->s);
+}
+
+// ---------------------------------------------------------------------------
+// setup
+// ---------------------------------------------------------------------------
+static int setup_colors(acvd_ctx* ctx) {
+    const int64_t n = ctx->nV;
+    CK(ctx->wk_int.resize(n));
+    CK(cudaMemsetAsync(ctx->wk_int.p, 0xff, n * sizeof(int), ctx->s));   // color = -1
+    CK(ctx->dtmp.resize(2));
+    int* d_maxc = (int*)ctx->dtmp.p;
+    CK(cudaMemsetAsync(d_maxc, 0, sizeof(int), ctx->s));
+    int rounds = 0;
+    for (;;) {
+        CK(zero_counter(ctx, kCntChanged));
+        CK(launch_color_round(ctx->row.p, ctx->col.p, n, ctx->wk_int.p, ctx->counters.p + kCntChanged, d_maxc,
+                              ctx->s));
+        int r = sync_counters(ctx);
+        if (r) return r;
+        if (ctx->h_counters[kCntChanged] == 0) break;
+        if (++rounds > 100000) return fail(ctx, ACVD_ERR_ITER_LIMIT, "graph colouring did not finish");
+    }
+    int maxc = 0;
+    CK(cudaMemcpy(&maxc, d_maxc, sizeof(int), cudaMemcpyDeviceToHost));
+    if (maxc >= 64) return fail(ctx, ACVD_ERR_UNSUPPORTED, "more than 64 colours needed (vertex valence too high)");
+    ctx->ncolors = maxc + 1;
+    // colour classes: stable sort of items by colour (items ascending inside a class)
+    CK(ctx->wk_a.resize(n));
+    CK(ctx->wk_b.resize(n));
+    CK(ctx->wk_c.resize(n));
+    CK(ctx->wk_d.resize(n));
+    CK(cudaMemcpyAsync(ctx->wk_a.p, ctx->wk_int.p, n * sizeof(int), cudaMemcpyDeviceToDevice, ctx->s));
+    CK(ctx->color_items.resize(n));
+    std::vector<uint32_t> iota(n);
+    for (int64_t i = 0; i < n; i++) iota[i] = (uint32_t)i;
+    CK(cudaMemcpyAsync(ctx->wk_b.p, iota.data(), n * sizeof(uint32_t), cudaMemcpyHostToDevice, ctx->s));
+    CK(radix_sort_pairs(ctx->wk_a.p, ctx->wk_b.p, ctx->wk_c.p, ctx->wk_d.p, n, 8, ctx->scratch, ctx->s));
+    CK(cudaMemcpyAsync(ctx->color_items.p, ctx->wk_b.p, n * sizeof(int), cudaMemcpyDeviceToDevice, ctx->s));
+    CK(ctx->wk_cnt.resize(64));
+    CK(cudaMemsetAsync(ctx->wk_cnt.p, 0, 64 * sizeof(uint32_t), ctx->s));
+    CK(launch_count_keys(ctx->wk_a.p, n, ctx->wk_cnt.p, ctx->s));
+    std::vector<uint32_t> cnt(64);
+    CK(cudaMemcpyAsync(cnt.data(), ctx->wk_cnt.p, 64 * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->s));
+    CK(cudaStreamSynchronize(ctx->s));
+    ctx->color_off.assign(ctx->ncolors + 1, 0);
+    int64_t mx = 0;
+    for (int c = 0; c < ctx->ncolors; c++) {
+        ctx->color_off[c + 1] = ctx->color_off[c] + cnt[c];
+        mx = std::max<int64_t>(mx, cnt[c]);
+    }
+    CK(ctx->cand_dest.resize(mx));
+    CK(ctx->cand_prio.resize(mx));
+    CK(cudaMemsetAsync(ctx->cand_dest.p, 0xff, mx * sizeof(int), ctx->s));
+    return ACVD_OK;
+}
+
+extern "C" {
+
+void acvd_default_opts(acvd_opts* o) {
+    o->device = 0;
+    o->use_graphs = 1;
+    o->max_loops = 5000000;
+    o->max_convergences = 1000000000;
+    o->kernel_timing = 0;
+}
+
+acvd_ctx* acvd_create(const acvd_opts* opts) {
+    acvd_ctx* ctx = new acvd_ctx;
+    if (opts) ctx->opts = *opts;
+    else acvd_default_opts(&ctx->opts);
+    if (cudaSetDevice(ctx->opts.device) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&ctx->s, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaMallocHost((void**)&ctx->h_counters, kNumCounters * sizeof(unsigned long long)) != cudaSuccess ||
+        ctx->counters.resize(kNumCounters) != cudaSuccess || ctx->dflags.resize(1) != cudaSuccess ||
+        cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess) {
+        cudaGetLastError();
+        delete ctx;
+        return nullptr;
+    }
+    cudaMemset(ctx->counters.p, 0, kNumCounters * sizeof(unsigned long long));
+    return ctx;
+}
+
+void acvd_destroy(acvd_ctx* ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->opts.device);
+    if (ctx->s) cudaStreamSynchronize(ctx->s);
+    ctx->drop_graph();
+    ctx->drop_events();
+    if (ctx->h_counters) cudaFreeHost(ctx->h_counters);
+    if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+    if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+    if (ctx->s) cudaStreamDestroy(ctx->s);
+    delete ctx;
+}
+
+const char* acvd_last_error(const acvd_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+void* acvd_stream(acvd_ctx* ctx) { return ctx ? (void*)ctx->s : nullptr; }
+
+int acvd_set_mesh(acvd_ctx* ctx, int64_t n_vertices, const double* xyz, int64_t n_faces, const int32_t* tri,
+                  const int32_t* csr_row, const int32_t* csr_col, int64_t n_edges, const int32_t* edge_v) {
+    if (!ctx) return ACVD_ERR_ARG;
+    if (n_vertices <= 0 || n_faces <= 0 || n_edges <= 0 || !xyz || !tri || !csr_row || !csr_col || !edge_v)
+        return fail(ctx, ACVD_ERR_ARG, "acvd_set_mesh: empty mesh or null array");
+    if (n_vertices >= (1ll << 26)) return fail(ctx, ACVD_ERR_UNSUPPORTED, "more than 2^26 vertices");
+    if (csr_row[0] != 0 || csr_row[n_vertices] != 2 * n_edges)
+        return fail(ctx, ACVD_ERR_ARG, "acvd_set_mesh: ring CSR does not hold 2 * n_edges entries");
+    CK(cudaSetDevice(ctx->opts.device));
+    ctx->drop_graph();
+    ctx->ready_mesh = ctx->ready_metric = ctx->ready_labels = false;
+    ctx->nV = n_vertices;
+    ctx->nF = n_faces;
+    ctx->nE = n_edges;
+    CK(ctx->xyz.resize(3 * n_vertices));
+    CK(ctx->tri.resize(3 * n_faces));
+    CK(ctx->row.resize(n_vertices + 1));
+    CK(ctx->col.resize(2 * n_edges));
+    CK(ctx->edge_v.resize(2 * n_edges));
+    CK(ctx->adj.resize(2 * n_edges));
+    CK(cudaMemcpyAsync(ctx->xyz.p, xyz, 3 * n_vertices * sizeof(double), cudaMemcpyHostToDevice, ctx->s));
+    CK(cudaMemcpyAsync(ctx->tri.p, tri, 3 * n_faces * sizeof(int), cudaMemcpyHostToDevice, ctx->s));
+    CK(cudaMemcpyAsync(ctx->row.p, csr_row, (n_vertices + 1) * sizeof(int), cudaMemcpyHostToDevice, ctx->s));
+    CK(cudaMemcpyAsync(ctx->col.p, csr_col, 2 * n_edges * sizeof(int), cudaMemcpyHostToDevice, ctx->s));
+    CK(cudaMemcpyAsync(ctx->edge_v.p, edge_v, 2 * n_edges * sizeof(int), cudaMemcpyHostToDevice, ctx->s));
+    int* d_maxdeg = nullptr;
+    CK(ctx->dtmp.resize(2));
+    d_maxdeg = (int*)ctx->dtmp.p;
+    CK(cudaMemsetAsync(d_maxdeg, 0, sizeof(int), ctx->s));
+    CK(launch_ring_adjacency(ctx->row.p, ctx->col.p, n_vertices, ctx->adj.p, d_maxdeg, ctx->s));
+    CK(cudaMemcpyAsync(&ctx->max_deg, d_maxdeg, sizeof(int), cudaMemcpyDeviceToHost, ctx->s));
+    CK(cudaStreamSynchronize(ctx->s));
+    int r = setup_colors(ctx);
+    if (r) return r;
+    ctx->ready_mesh = true;
+    return ACVD_OK;
+}
+
+int acvd_set_metric(acvd_ctx* ctx, int metric, const double* indicator, const float* principal_dirs,
+                    double gradation) {
+    if (!ctx) return ACVD_ERR_ARG;
+    if (!ctx->ready_mesh) return fail(ctx, ACVD_ERR_ARG, "acvd_set_metric before acvd_set_mesh");
+    if (metric < 0 || metric > 2) return fail(ctx, ACVD_ERR_ARG, "unknown metric");
+    const bool use_ind = metric == kAniso ? gradation != 0.0 : gradation > 0.0;
+    if (use_ind && !indicator) return fail(ctx, ACVD_ERR_ARG, "gradation set but no indicator given");
+    if (metric == kAniso && !principal_dirs)
+        return fail(ctx, ACVD_ERR_ARG, "the quadric-anisotropic metric needs principal directions");
+    CK(cudaSetDevice(ctx->opts.device));
+    ctx->drop_graph();
+    ctx->metric = metric;
+    const int64_t nv = ctx->nV, nf = ctx->nF;
+    DBuf<double> ind, farea, fnorm, wd, varea, wsum;
+    DBuf<float> pd;
+    if (use_ind) {
+        CK(ind.resize(nv));
+        CK(cudaMemcpyAsync(ind.p, indicator, nv * sizeof(double), cudaMemcpyHostToDevice, ctx->s));
+    }
+    if (metric == kAniso) {
+        CK(pd.resize(6 * nv));
+        CK(cudaMemcpyAsync(pd.p, principal_dirs, 6 * nv * sizeof(float), cudaMemcpyHostToDevice, ctx->s));
+    }
+    CK(farea.resize(nf));
+    CK(fnorm.resize(3 * nf));
+    CK(wd.resize(nv));
+    CK(varea.resize(nv));
+    CK(wsum.resize(1));
+    CK(launch_face_geometry(ctx->xyz.p, ctx->tri.p, nf, farea.p, fnorm.p, ctx->s));
+    // vertex -> faces in increasing face id
+    DBuf<uint32_t> k1, v1, k2, v2, vrow;
+    CK(k1.resize(3 * nf));
+    CK(v1.resize(3 * nf));
+    CK(k2.resize(3 * nf));
+    CK(v2.resize(3 * nf));
+    CK(vrow.resize(nv + 1));
+    CK(launch_vertex_keys(ctx->tri.p, nf, k1.p, v1.p, ctx->s));
+    CK(cudaMemsetAsync(vrow.p, 0, (nv + 1) * sizeof(uint32_t), ctx->s));
+    CK(launch_count_keys(k1.p, 3 * nf, vrow.p, ctx->s));
+    CK(radix_sort_pairs(k1.p, v1.p, k2.p, v2.p, 3 * nf, bits_for((uint64_t)nv), ctx->scratch, ctx->s));
+    CK(exclusive_scan_u32(vrow.p, vrow.p, nv + 1, nullptr, ctx->scratch, ctx->s));
+    CK(ctx->xw.resize(nv));
+    if (metric != kIso) {
+        CK(ctx->qa.resize(nv));
+        CK(ctx->qb.resize(nv));
+    }
+    if (metric == kAniso) {
+        CK(ctx->ta.resize(nv));
+        CK(ctx->tb.resize(nv));
+    }
+    CK(launch_vertex_items(metric, nv, ctx->xyz.p, vrow.p, v1.p, farea.p, fnorm.p, use_ind ? ind.p : nullptr,
+                           gradation, wd.p, varea.p, ctx->qa.p, ctx->qb.p, ctx->s));
+    CK(sum_f64(wd.p, nv, wsum.p, ctx->scratch, ctx->s));
+    const double ratio = metric == kQEM ? 10000.0 : 100000.0;
+    CK(launch_finish_items(metric, nv, ctx->xyz.p, wd.p, varea.p, wsum.p, ratio, pd.p, ctx->xw.p, ctx->ta.p,
+                           ctx->tb.p, ctx->s));
+    CK(cudaStreamSynchronize(ctx->s));
+    ctx->ready_metric = true;
+    return ACVD_OK;
+}
+
+int acvd_set_quadrics_optimization_level(acvd_ctx* ctx, int level) {
+    if (!ctx || level < 0 || level > 3) return fail(ctx, ACVD_ERR_ARG, "level must be 0..3");
+    ctx->level = level;
+    return ACVD_OK;
+}
+
+int acvd_set_unconstrained_initialization(acvd_ctx* ctx, int on) {
+    if (!ctx) return ACVD_ERR_ARG;
+    ctx->unconstrained = on ? 1 : 0;
+    return ACVD_OK;
+}
+
+int acvd_set_labels(acvd_ctx* ctx, int32_t k, const int32_t* labels) {
+    if (!ctx) return ACVD_ERR_ARG;
+    if (!ctx->ready_mesh) return fail(ctx, ACVD_ERR_ARG, "acvd_set_labels before acvd_set_mesh");
+    if (k <= 0 || !labels) return fail(ctx, ACVD_ERR_ARG, "acvd_set_labels: K must be positive");
+    if (k >= (1 << 21)) return fail(ctx, ACVD_ERR_UNSUPPORTED, "more than 2^21 clusters");
+    for (int64_t i = 0; i < ctx->nV; i++)
+        if (labels[i] < 0 || labels[i] > k) return fail(ctx, ACVD_ERR_ARG, "label outside [0, K]");
+    CK(cudaSetDevice(ctx->opts.device));
+    if (ctx->K != k) ctx->drop_graph();
+    ctx->K = k;
+    const int ms = ctx->metric >= 0 ? ctx->metric : kAniso;
+    CK(ctx->label.resize(ctx->nV));
+    CK(ctx->size.resize(k + 1));
+    CK(ctx->claim.resize(k + 1));
+    CK(ctx->acc.resize((size_t)(k + 1) * acc_stride(kAniso)));
+    CK(ctx->ev.resize((size_t)(k + 1) * ev_stride(kAniso)));
+    CK(ctx->energy.resize(k + 1));
+    (void)ms;
+    CK(ctx->label_init.resize(ctx->nV));
+    CK(cudaMemcpyAsync(ctx->label.p, labels, ctx->nV * sizeof(int), cudaMemcpyHostToDevice, ctx->s));
+    CK(cudaMemcpyAsync(ctx->label_init.p, ctx->label.p, ctx->nV * sizeof(int), cudaMemcpyDeviceToDevice, ctx->s));
+    CK(cudaStreamSynchronize(ctx->s));
+    ctx->ready_labels = true;
+    return ACVD_OK;
+}
+
+int acvd_rewind(acvd_ctx* ctx) {
+    if (!ctx) return ACVD_ERR_ARG;
+    if (!ctx->ready_labels) return fail(ctx, ACVD_ERR_ARG, "acvd_rewind before acvd_set_labels");
+    CK(cudaSetDevice(ctx->opts.device));
+    CK(cudaMemcpyAsync(ctx->label.p, ctx->label_init.p, ctx->nV * sizeof(int), cudaMemcpyDeviceToDevice, ctx->s));
+    return ACVD_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// MinimizeEnergy building blocks
+// ---------------------------------------------------------------------------
+static int recompute(acvd_ctx* ctx) {
+    DevState st = ctx->state();
+    const int64_t n = ctx->nV;
+    const int K = ctx->K;
+    CK(ctx->wk_a.resize(n));
+    CK(ctx->wk_b.resize(n));
+    CK(ctx->wk_c.resize(n));
+    CK(ctx->wk_d.resize(n));
+    CK(ctx->wk_cnt.resize(K + 1));
+    CK(ctx->wk_off.resize(K + 1));
+    CK(cudaMemsetAsync(ctx->wk_cnt.p, 0, (K + 1) * sizeof(uint32_t), ctx->s));
+    CK(launch_cluster_keys(st, ctx->wk_a.p, ctx->wk_b.p, ctx->wk_cnt.p, ctx->s));
+    CK(radix_sort_pairs(ctx->wk_a.p, ctx->wk_b.p, ctx->wk_c.p, ctx->wk_d.p, n, bits_for((uint64_t)K), ctx->scratch,
+                        ctx->s));
+    CK(exclusive_scan_u32(ctx->wk_cnt.p, ctx->wk_off.p, K + 1, nullptr, ctx->scratch, ctx->s));
+    CK(launch_reduce_clusters(ctx->metric, st, ctx->wk_b.p, ctx->wk_off.p, ctx->wk_cnt.p, ctx->s));
+    CK(launch_update_all(ctx->metric, st, ctx->s));
+    return ACVD_OK;
+}
+
+static int fill_holes(acvd_ctx* ctx, int* unassigned) {
+    DevState st = ctx->state();
+    for (int round = 0;; round++) {
+        if (round > 1000000) return fail(ctx, ACVD_ERR_ITER_LIMIT, "hole filling did not finish");
+        CK(zero_counter(ctx, kCntAssigned));
+        for (int c = 0; c < ctx->ncolors; c++)
+            CK(launch_fill_color(st, ctx->color_items.p + ctx->color_off[c], ctx->color_off[c + 1] - ctx->color_off[c],
+                                 ctx->s));
+        int r = sync_counters(ctx);
+        if (r) return r;
+        if (ctx->h_counters[kCntAssigned] == 0) break;
+    }
+    if (unassigned) {
+        // items still unassigned: count them with the boundary/compaction helpers' flag kernel
+        CK(ctx->wk_cnt.resize(ctx->K + 1));
+        CK(cudaMemsetAsync(ctx->wk_cnt.p, 0, (ctx->K + 1) * sizeof(uint32_t), ctx->s));
+        CK(ctx->wk_a.resize(ctx->nV));
+        CK(ctx->wk_b.resize(ctx->nV));
+        CK(launch_cluster_keys(st, ctx->wk_a.p, ctx->wk_b.p, ctx->wk_cnt.p, ctx->s));
+        std::vector<uint32_t> cnt(ctx->K);
+        CK(cudaMemcpyAsync(cnt.data(), ctx->wk_cnt.p, ctx->K * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->s));
+        CK(cudaStreamSynchronize(ctx->s));
+        int64_t assigned = 0;
+        for (int k = 0; k < ctx->K; k++) assigned += cnt[k];
+        *unassigned = (int)(ctx->nV - assigned);
+    }
+    return ACVD_OK;
+}
+
+static int clean(acvd_ctx* ctx, int* n_disconnected) {
+    DevState st = ctx->state();
+    const int64_t n = ctx->nV;
+    CK(ctx->comp.resize(n));
+    CK(ctx->csize.resize(n));
+    CK(ctx->multi.resize(ctx->K + 1));
+    CK(ctx->best.resize(ctx->K + 1));
+    CK(launch_comp_init(st, ctx->comp.p, ctx->s));
+    for (int it = 0;; it++) {
+        if (it > 100000) return fail(ctx, ACVD_ERR_ITER_LIMIT, "connected-component labelling did not converge");
+        CK(zero_counter(ctx, kCntChanged));
+        // several propagation steps between host checks
+        for (int j = 0; j < 4; j++) CK(launch_comp_step(st, ctx->comp.p, ctx->s));
+        int r = sync_counters(ctx);
+        if (r) return r;
+        if (ctx->h_counters[kCntChanged] == 0) break;
+    }
+    CK(cudaMemsetAsync(ctx->csize.p, 0, n * sizeof(int), ctx->s));
+    CK(cudaMemsetAsync(ctx->best.p, 0, (ctx->K + 1) * sizeof(unsigned long long), ctx->s));
+    CK(cudaMemsetAsync(ctx->multi.p, 0, (ctx->K + 1) * sizeof(int), ctx->s));
+    CK(zero_counter(ctx, kCntDisconnected));
+    CK(launch_comp_finish(st, ctx->comp.p, ctx->csize.p, ctx->best.p, ctx->multi.p, ctx->s));
+    int r = sync_counters(ctx);
+    if (r) return r;
+    *n_disconnected = (int)ctx->h_counters[kCntDisconnected];
+    return ACVD_OK;
+}
+
+// one sweep: every colour class once (eval + apply per class).  With kernel
+// timing on, an event pair per colour brackets the evaluation kernel; the pairs
+// are recorded inside the captured graph and read after the sweep's sync.
+static int enqueue_sweep(acvd_ctx* ctx, bool timing) {
+    DevState st = ctx->state();
+    CK(cudaMemsetAsync(ctx->claim.p, 0xff, (ctx->K + 1) * sizeof(unsigned long long), ctx->s));
+    CK(cudaMemsetAsync(ctx->counters.p + kCntMoves, 0, sizeof(unsigned long long), ctx->s));
+    int64_t kernels = 0;
+    for (int c = 0; c < ctx->ncolors; c++) {
+        const int* items = ctx->color_items.p + ctx->color_off[c];
+        const int64_t cnt = ctx->color_off[c + 1] - ctx->color_off[c];
+        if (cnt == 0) continue;
+        if (timing) CK(cudaEventRecord(ctx->ev_eval[2 * c], ctx->s));
+        CK(launch_eval(ctx->metric, st, items, cnt, c, ctx->cand_dest.p, ctx->cand_prio.p, ctx->s));
+        if (timing) CK(cudaEventRecord(ctx->ev_eval[2 * c + 1], ctx->s));
+        CK(launch_apply(ctx->metric, st, items, cnt, c, ctx->cand_dest.p, ctx->cand_prio.p, ctx->s));
+        kernels += 2;
+    }
+    ctx->sweep_kernels = kernels;
+    return ACVD_OK;
+}
+
+static int run_sweep(acvd_ctx* ctx, bool timing, double* eval_ms, int* eval_launches, int64_t* moves) {
+    if (timing && (int)ctx->ev_eval.size() != 2 * ctx->ncolors) {
+        ctx->drop_graph();
+        ctx->drop_events();
+        ctx->ev_eval.resize(2 * ctx->ncolors);
+        for (auto& e : ctx->ev_eval) CK(cudaEventCreate(&e));
+    }
+    if (ctx->opts.use_graphs) {
+        if (!ctx->sweep_exec) {
+            cudaGraph_t g;
+            const long long before = g_launches;
+            CK(cudaStreamBeginCapture(ctx->s, cudaStreamCaptureModeThreadLocal));
+            int r = enqueue_sweep(ctx, timing);
+            cudaError_t e = cudaStreamEndCapture(ctx->s, &g);
+            g_launches = before;
+            if (r) return r;
+            CK(e);
+            CK(cudaGraphInstantiate(&ctx->sweep_exec, g, 0));
+            cudaGraphDestroy(g);
+        }
+        CK(cudaGraphLaunch(ctx->sweep_exec, ctx->s));
+        g_launches += ctx->sweep_kernels;
+    } else {
+        int r = enqueue_sweep(ctx, timing);
+        if (r) return r;
+    }
+    int r = sync_counters(ctx);
+    if (r) return r;
+    *moves = (int64_t)ctx->h_counters[kCntMoves];
+    if (timing) {
+        for (int c = 0; c < ctx->ncolors; c++) {
+            if (ctx->color_off[c + 1] == ctx->color_off[c]) continue;
+            float ms = 0.f;
+            CK(cudaEventElapsedTime(&ms, ctx->ev_eval[2 * c], ctx->ev_eval[2 * c + 1]));
+            *eval_ms += ms;
+            (*eval_launches)++;
+        }
+    }
+    return ACVD_OK;
+}
+
+extern "C" int acvd_minimize(acvd_ctx* ctx, acvd_stats* stats) {
+    if (!ctx) return ACVD_ERR_ARG;
+    if (!ctx->ready_mesh || !ctx->ready_metric || !ctx->ready_labels)
+        return fail(ctx, ACVD_ERR_ARG, "acvd_minimize needs acvd_set_mesh, acvd_set_metric and acvd_set_labels");
+    CK(cudaSetDevice(ctx->opts.device));
+    acvd_stats local;
+    std::memset(&local, 0, sizeof local);
+    const bool timing = ctx->opts.kernel_timing != 0;
+    // ProcessClustering: the unconstrained first phase of the QEM metric (:683-688)
+    ctx->flags.constrained = (ctx->metric == kQEM && ctx->unconstrained) ? 0 : 1;
+    ctx->flags.connexity = 0;
+    ctx->flags.level = ctx->level;
+    ctx->flags.thr = 1e-3f;
+    int r = upload_flags(ctx);
+    if (r) return r;
+    CK(cudaMemsetAsync(ctx->counters.p, 0, kNumCounters * sizeof(unsigned long long), ctx->s));
+    const long long launches0 = g_launches;
+    cudaEvent_t t0, t1;
+    CK(cudaEventCreate(&t0));
+    CK(cudaEventCreate(&t1));
+    CK(cudaEventRecord(t0, ctx->s));
+    int status = ACVD_OK;
+    do {
+        // FillHolesInClustering, FillQueuesFromClustering, ReComputeStatistics (:727-730)
+        int unassigned = 0;
+        if ((r = fill_holes(ctx, &unassigned))) { status = r; break; }
+        if ((r = recompute(ctx))) { status = r; break; }
+        // items of non-frozen clusters, the base of the early-convergence test (:733-736)
+        const int64_t early = ctx->nV - unassigned;
+        int convergences = 0;
+        int sweeps = 0;
+        for (;;) {
+            int64_t mods = 0;
+            if ((r = run_sweep(ctx, timing, &local.eval_ms, &local.eval_launches, &mods))) { status = r; break; }
+            sweeps++;
+            local.moves += mods;
+            if (mods == 0 || sweeps > ctx->opts.max_loops || (mods <= early / 1000 && convergences <= 1)) {
+                bool flags_changed = false;
+                if (ctx->unconstrained && convergences == 0 && ctx->metric == kQEM) {
+                    ctx->flags.constrained = 1;
+                    flags_changed = true;
+                }
+                if (convergences >= 1 && !ctx->flags.connexity) {
+                    ctx->flags.connexity = 1;
+                    flags_changed = true;
+                }
+                if (flags_changed && (r = upload_flags(ctx))) { status = r; break; }
+                convergences++;
+                int disc = 0;
+                if ((r = clean(ctx, &disc))) { status = r; break; }
+                int un = 0;
+                if ((r = fill_holes(ctx, &un))) { status = r; break; }
+                local.disconnected = disc;
+                local.unassigned = un;
+                if ((r = recompute(ctx))) { status = r; break; }
+                if (disc == 0 && mods == 0) break;
+                if (sweeps >= ctx->opts.max_loops) { status = fail(ctx, ACVD_ERR_ITER_LIMIT, "sweep cap reached"); break; }
+                if (convergences >= ctx->opts.max_convergences) break;
+            }
+        }
+        local.sweeps = sweeps;
+        local.convergences = convergences;
+    } while (0);
+    CK(cudaEventRecord(t1, ctx->s));
+    CK(cudaEventSynchronize(t1));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, t0, t1));
+    cudaEventDestroy(t0);
+    cudaEventDestroy(t1);
+    local.device_ms = ms;
+    r = sync_counters(ctx);
+    if (r) return r;
+    local.candidates = (int64_t)ctx->h_counters[kCntCand];
+    local.boundary_items = (int64_t)ctx->h_counters[kCntBoundary];
+    local.targets = (int64_t)ctx->h_counters[kCntTargets];
+    local.visited = (int64_t)ctx->h_counters[kCntVisited];
+    local.slots = (int64_t)ctx->h_counters[kCntSlots];
+    local.kernel_launches = g_launches - launches0;
+    {
+        // algorithmic bytes of the evaluation kernels: per visited item its colour-list
+        // entry, ring bounds and label; per ring slot the neighbour id and label; per
+        // boundary item its record, its cluster's record and size; per destination
+        // cluster its record; per proposal the candidate slots and two claim words
+        const int64_t R = ctx->metric == kIso ? 16 : (ctx->metric == kQEM ? 40 : 64);
+        const int64_t C = 16 * (int64_t)ev_stride(ctx->metric);
+        local.eval_bytes = 16 * local.visited + 8 * local.slots + (R + C + 4) * local.boundary_items +
+                           C * local.targets + 24 * local.candidates;
+    }
+    if (status == ACVD_OK) {
+        double et = 0.0;
+        int rr = acvd_get_clusters(ctx, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, &et);
+        if (rr) return rr;
+        local.energy = et;
+    }
+    if (stats) *stats = local;
+    return status;
+}
+
+extern "C" int acvd_get_labels(acvd_ctx* ctx, int32_t* labels) {
+    if (!ctx || !labels) return ACVD_ERR_ARG;
+    if (!ctx->ready_labels) return fail(ctx, ACVD_ERR_ARG, "no labels");
+    CK(cudaSetDevice(ctx->opts.device));
+    CK(cudaMemcpyAsync(labels, ctx->label.p, ctx->nV * sizeof(int), cudaMemcpyDeviceToHost, ctx->s));
+    CK(cudaStreamSynchronize(ctx->s));
+    return ACVD_OK;
+}
+
+// Accumulators and evaluation records for the current labels (recomputed).
+extern "C" int acvd_get_clusters(acvd_ctx* ctx, int32_t* sizes, double* S, double* W, double* quadric,
+                                 double* centroid, double* energy, double* energy_total) {
+    if (!ctx) return ACVD_ERR_ARG;
+    if (!ctx->ready_metric || !ctx->ready_labels) return fail(ctx, ACVD_ERR_ARG, "no metric or labels");
+    CK(cudaSetDevice(ctx->opts.device));
+    ctx->flags.level = ctx->level;
+    int r = upload_flags(ctx);
+    if (r) return r;
+    r = recompute(ctx);
+    if (r) return r;
+    const int K = ctx->K;
+    const int as = acc_stride(ctx->metric);
+    std::vector<df> acc((size_t)K * as);
+    CK(cudaMemcpyAsync(acc.data(), ctx->acc.p, acc.size() * sizeof(df), cudaMemcpyDeviceToHost, ctx->s));
+    if (sizes) CK(cudaMemcpyAsync(sizes, ctx->size.p, K * sizeof(int), cudaMemcpyDeviceToHost, ctx->s));
+    if (energy) CK(cudaMemcpyAsync(energy, ctx->energy.p, K * sizeof(double), cudaMemcpyDeviceToHost, ctx->s));
+    if (energy_total) {
+        CK(ctx->dtmp.resize(2));
+        CK(sum_f64(ctx->energy.p, K, ctx->dtmp.p, ctx->scratch, ctx->s));
+        CK(cudaMemcpyAsync(energy_total, ctx->dtmp.p, sizeof(double), cudaMemcpyDeviceToHost, ctx->s));
+    }
+    if (centroid) {
+        DBuf<double> c;
+        CK(c.resize(3 * (size_t)K));
+        CK(launch_centroids(ctx->metric, ctx->state(), c.p, ctx->s));
+        CK(cudaMemcpyAsync(centroid, c.p, 3 * (size_t)K * sizeof(double), cudaMemcpyDeviceToHost, ctx->s));
+        CK(cudaStreamSynchronize(ctx->s));
+    }
+    CK(cudaStreamSynchronize(ctx->s));
+    for (int k = 0; k < K; k++) {
+        const df* a = acc.data() + (size_t)k * as;
+        auto d = [](df x) { return (double)x.hi + (double)x.lo; };
+        if (S) for (int j = 0; j < 3; j++) S[3 * k + j] = d(a[j]);
+        if (W) W[k] = d(a[3]);
+        if (quadric) {
+            double* q = quadric + 9 * (size_t)k;
+            if (ctx->metric == kIso) {
+                for (int j = 0; j < 9; j++) q[j] = 0.0;
+            } else {
+                // the reference's compact quadric: A entries and -b in slots 3, 6, 8
+                q[0] = d(a[4]); q[1] = d(a[5]); q[2] = d(a[6]); q[3] = -d(a[10]);
+                q[4] = d(a[7]); q[5] = d(a[8]); q[6] = -d(a[11]); q[7] = d(a[9]); q[8] = -d(a[12]);
+            }
+        }
+    }
+    return ACVD_OK;
+}
+
+extern "C" int acvd_get_boundary_edges(acvd_ctx* ctx, int32_t* ids, int64_t* count) {
+    if (!ctx || !count) return ACVD_ERR_ARG;
+    if (!ctx->ready_labels) return fail(ctx, ACVD_ERR_ARG, "no labels");
+    CK(cudaSetDevice(ctx->opts.device));
+    const int64_t ne = ctx->nE;
+    DBuf<uint32_t> flags, pos;
+    DBuf<int> out;
+    CK(flags.resize(ne + 1));
+    CK(pos.resize(ne + 1));
+    CK(ctx->dtmp.resize(2));
+    uint32_t* total = (uint32_t*)ctx->dtmp.p;
+    CK(launch_boundary_edges(ctx->edge_v.p, ne, ctx->label.p, flags.p, ctx->s));
+    CK(exclusive_scan_u32(flags.p, pos.p, ne, total, ctx->scratch, ctx->s));
+    uint32_t t = 0;
+    CK(cudaMemcpyAsync(&t, total, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->s));
+    CK(cudaStreamSynchronize(ctx->s));
+    *count = t;
+    if (ids && t) {
+        CK(out.resize(t));
+        CK(launch_compact(flags.p, pos.p, ne, out.p, ctx->s));
+        CK(cudaMemcpyAsync(ids, out.p, t * sizeof(int), cudaMemcpyDeviceToHost, ctx->s));
+        CK(cudaStreamSynchronize(ctx->s));
+    }
+    return ACVD_OK;
+}
+
+extern "C" int acvd_get_dual_mesh(acvd_ctx* ctx, int32_t* tris, int64_t* n_tris) {
+    if (!ctx || !n_tris) return ACVD_ERR_ARG;
+    if (!ctx->ready_labels) return fail(ctx, ACVD_ERR_ARG, "no labels");
+    CK(cudaSetDevice(ctx->opts.device));
+    const int64_t nf = ctx->nF;
+    DBuf<uint32_t> flags, pos, klo, khi, order, t1, t2, keep, kpos;
+    DBuf<int> faces, sel, out;
+    CK(flags.resize(nf + 1));
+    CK(pos.resize(nf + 1));
+    CK(ctx->dtmp.resize(2));
+    uint32_t* total = (uint32_t*)ctx->dtmp.p;
+    CK(launch_dual_faces(ctx->tri.p, nf, ctx->label.p, ctx->K, flags.p, ctx->s));
+    CK(exclusive_scan_u32(flags.p, pos.p, nf, total, ctx->scratch, ctx->s));
+    uint32_t m = 0;
+    CK(cudaMemcpyAsync(&m, total, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->s));
+    CK(cudaStreamSynchronize(ctx->s));
+    if (m == 0) { *n_tris = 0; return ACVD_OK; }
+    CK(faces.resize(m));
+    CK(launch_compact(flags.p, pos.p, nf, faces.p, ctx->s));
+    CK(klo.resize(m)); CK(khi.resize(m)); CK(order.resize(m)); CK(t1.resize(m)); CK(t2.resize(m));
+    CK(keep.resize(m + 1)); CK(kpos.resize(m + 1));
+    CK(launch_dual_keys(ctx->tri.p, faces.p, m, ctx->label.p, klo.p, khi.p, order.p, ctx->s));
+    // stable LSD sort on (khi, klo): by klo first, then by khi
+    CK(radix_sort_pairs(klo.p, order.p, t1.p, t2.p, m, 32, ctx->scratch, ctx->s));
+    CK(launch_gather_u32(khi.p, order.p, m, t1.p, ctx->s));           // khi in klo-sorted order
+    CK(cudaMemcpyAsync(khi.p, t1.p, m * sizeof(uint32_t), cudaMemcpyDeviceToDevice, ctx->s));
+    // carry klo along the second pass through a permutation index
+    DBuf<uint32_t> perm, klo2;
+    CK(perm.resize(m)); CK(klo2.resize(m));
+    {
+        std::vector<uint32_t> io(m);
+        for (uint32_t j = 0; j < m; j++) io[j] = j;
+        CK(cudaMemcpyAsync(perm.p, io.data(), m * sizeof(uint32_t), cudaMemcpyHostToDevice, ctx->s));
+        CK(cudaStreamSynchronize(ctx->s));
+    }
+    CK(radix_sort_pairs(khi.p, perm.p, t1.p, t2.p, m, 31, ctx->scratch, ctx->s));
+    CK(launch_gather_u32(klo.p, perm.p, m, klo2.p, ctx->s));
+    CK(launch_gather_u32(order.p, perm.p, m, t1.p, ctx->s));
+    CK(launch_dual_unique(klo2.p, khi.p, t1.p, m, keep.p, ctx->s));
+    CK(exclusive_scan_u32(keep.p, kpos.p, m, total, ctx->scratch, ctx->s));
+    uint32_t t = 0;
+    CK(cudaMemcpyAsync(&t, total, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->s));
+    CK(cudaStreamSynchronize(ctx->s));
+    *n_tris = t;
+    if (tris && t) {
+        CK(sel.resize(t));
+        CK(out.resize(3 * (size_t)t));
+        CK(launch_compact(keep.p, kpos.p, m, sel.p, ctx->s));
+        CK(launch_dual_write(ctx->tri.p, faces.p, sel.p, t, ctx->label.p, out.p, ctx->s));
+        CK(cudaMemcpyAsync(tris, out.p, 3 * (size_t)t * sizeof(int), cudaMemcpyDeviceToHost, ctx->s));
+        CK(cudaStreamSynchronize(ctx->s));
+    }
+    return ACVD_OK;
+}

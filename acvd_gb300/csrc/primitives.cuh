@@ -1,0 +1,39 @@
+// Device-wide primitives used by the clustering pipeline: exclusive scan,
+// deterministic FP64 sums and a stable LSD radix sort of (key, value) pairs.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace acvd {
+
+// Number of kernels launched by this library (host-side count of <<<>>> sites).
+extern long long g_launches;
+
+// Scratch for the primitives; grown on demand, owned by the caller's context.
+struct Scratch {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+    cudaError_t reserve(size_t need);
+    ~Scratch();
+};
+
+// out[i] = sum_{j<i} in[j] for n uint32 values (in == out allowed).  total may be null.
+cudaError_t exclusive_scan_u32(const uint32_t* in, uint32_t* out, int64_t n, uint32_t* total_dev,
+                               Scratch& scratch, cudaStream_t s);
+
+// Stable sort of (keys, vals) by the low `key_bits` bits of keys.  Results land in
+// keys/vals; tmp_keys/tmp_vals are same-sized work buffers.
+cudaError_t radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* tmp_keys, uint32_t* tmp_vals,
+                             int64_t n, int key_bits, Scratch& scratch, cudaStream_t s);
+
+// Deterministic sum of n doubles (fixed reduction tree) into *out_dev.
+cudaError_t sum_f64(const double* in, int64_t n, double* out_dev, Scratch& scratch, cudaStream_t s);
+
+// Number of bits needed to represent values in [0, v].
+inline int bits_for(uint64_t v) {
+    int b = 1;
+    while ((1ull << b) <= v && b < 63) b++;
+    return b;
+}
+
+}  // namespace acvd

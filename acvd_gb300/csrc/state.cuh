@@ -1,0 +1,131 @@
+// Device-side data layout of one clustering context and the launchers of the
+// kernels that operate on it.  All arrays live in HBM; kernels get raw pointers.
+//
+// Items (one per mesh vertex), float32:
+//   xw[i] = (x, y, z, w)                      all metrics
+//   qa[i] = (A00, A01, A02, A11), qb[i] = (A12, A22)
+//                                             quadric metrics: A = sum over the
+//                                             adjacent faces of n n^T (unit normals);
+//                                             the linear part of the reference's
+//                                             quadric is b_i = A_i x_i exactly, since
+//                                             x_i lies on every adjacent face plane
+//   ta[i] = (T00, T01, T02, T11), tb[i] = (T12, T22)   anisotropic tensor
+//
+// Clusters: compensated (double-float) accumulators, acc[k * acc_stride + j]:
+//   j = 0..2 S = sum w x, 3 W = sum w, 4..9 A, 10..12 b = sum A_i x_i,
+//   13..18 T = sum T_i, 19..21 u = sum T_i x_i
+// and a float32 evaluation record derived from them in FP64 (update_cluster),
+// ev[k * ev_stride + j] (float4):
+//   0 (m, W)  m = S / W          1 (delta, P)  placed vertex c = m + delta, P = W |delta|^2
+//   2 (r, 0)  r = b - A m        3 (A00 A01 A02 A11)   4 (A12 A22 0 0)
+//   5 (T00 T01 T02 T11)          6 (T12 T22 g0 g1)     7 (g2 0 0 0)   g = u - T c
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "common.cuh"
+
+namespace acvd {
+
+enum Metric { kIso = 0, kQEM = 1, kAniso = 2 };
+
+template <int M> struct Layout;
+template <> struct Layout<kIso> { static constexpr int acc = 4, ev = 1; };
+template <> struct Layout<kQEM> { static constexpr int acc = 13, ev = 5; };
+template <> struct Layout<kAniso> { static constexpr int acc = 22, ev = 8; };
+
+inline int acc_stride(int m) { return m == kIso ? 4 : (m == kQEM ? 13 : 22); }
+inline int ev_stride(int m) { return m == kIso ? 1 : (m == kQEM ? 5 : 8); }
+
+// Mutable run flags read by the kernels from device memory, so that one captured
+// sweep graph serves every phase of the minimisation.
+struct RunFlags {
+    int constrained;   // quadric placement active (QEM after the unconstrained phase; always for aniso)
+    int connexity;     // local connectivity constraint active
+    int level;         // number of eigenvalues the placement may invert (0..3)
+    float thr;         // relative eigenvalue threshold (1e-3)
+};
+
+// Counters written by the kernels.
+enum Counter {
+    kCntMoves = 0,       // accepted moves in the current sweep
+    kCntCand = 1,        // candidate moves proposed
+    kCntBoundary = 2,    // boundary items evaluated
+    kCntTargets = 3,     // (item, destination cluster) energy evaluations
+    kCntVisited = 4,     // items visited by the evaluation kernels
+    kCntSlots = 5,       // ring slots read by the evaluation kernels
+    kCntChanged = 6,     // generic "something changed" flag / count
+    kCntError = 7,       // device-side check failures
+    kCntDisconnected = 8,
+    kCntAssigned = 9,
+    kNumCounters = 16
+};
+
+struct DevState {
+    int64_t n;        // items
+    int k;            // clusters; label k = null (unassigned)
+    const int* row;   // CSR of vertex rings (reference ring order)
+    const int* col;
+    const unsigned* adj;        // per CSR slot: which ring slots are adjacent to this neighbour
+    const float4* xw;
+    const float4* qa;
+    const float2* qb;
+    const float4* ta;
+    const float2* tb;
+    int* label;
+    int* size;
+    unsigned long long* claim;
+    df* acc;
+    float4* ev;
+    double* energy;
+    unsigned long long* counters;
+    const RunFlags* flags;
+};
+
+// ---- items / topology (topology.cu) ----
+cudaError_t launch_ring_adjacency(const int* row, const int* col, int64_t n, unsigned* adj, int* max_deg,
+                                  cudaStream_t s);
+cudaError_t launch_color_round(const int* row, const int* col, int64_t n, int* color,
+                               unsigned long long* remaining, int* max_color, cudaStream_t s);
+cudaError_t launch_face_geometry(const double* xyz, const int* tri, int64_t nf, double* farea, double* fnorm,
+                                 cudaStream_t s);
+cudaError_t launch_vertex_keys(const int* tri, int64_t nf, uint32_t* keys, uint32_t* vals, cudaStream_t s);
+cudaError_t launch_count_keys(const uint32_t* keys, int64_t n, uint32_t* counts, cudaStream_t s);
+cudaError_t launch_vertex_items(int metric, int64_t nv, const double* xyz, const uint32_t* vf_row,
+                                const uint32_t* vf_face, const double* farea, const double* fnorm,
+                                const double* indicator, double gradation, double* wd, double* varea,
+                                float4* qa, float2* qb, cudaStream_t s);
+cudaError_t launch_finish_items(int metric, int64_t nv, const double* xyz, const double* wd, const double* vrea,
+                                const double* wsum, double ratio, const float* pdirs, float4* xw, float4* ta,
+                                float2* tb, cudaStream_t s);
+
+// ---- clustering (cluster.cu) ----
+cudaError_t launch_eval(int metric, const DevState& st, const int* items, int64_t count, int epoch,
+                        int* cand_dest, unsigned* cand_prio, cudaStream_t s);
+cudaError_t launch_apply(int metric, const DevState& st, const int* items, int64_t count, int epoch,
+                         int* cand_dest, const unsigned* cand_prio, cudaStream_t s);
+cudaError_t launch_update_all(int metric, const DevState& st, cudaStream_t s);
+cudaError_t launch_cluster_keys(const DevState& st, uint32_t* keys, uint32_t* vals, uint32_t* counts,
+                                cudaStream_t s);
+cudaError_t launch_reduce_clusters(int metric, const DevState& st, const uint32_t* sorted_items,
+                                   const uint32_t* seg_off, const uint32_t* seg_cnt, cudaStream_t s);
+cudaError_t launch_comp_init(const DevState& st, int* comp, cudaStream_t s);
+cudaError_t launch_comp_step(const DevState& st, int* comp, cudaStream_t s);
+cudaError_t launch_comp_finish(const DevState& st, const int* comp, int* csize, unsigned long long* best,
+                               int* multi, cudaStream_t s);
+cudaError_t launch_fill_color(const DevState& st, const int* items, int64_t count, cudaStream_t s);
+cudaError_t launch_boundary_edges(const int* edge_v, int64_t ne, const int* label, uint32_t* flags,
+                                  cudaStream_t s);
+cudaError_t launch_compact(const uint32_t* flags, const uint32_t* pos, int64_t n, int* out, cudaStream_t s);
+cudaError_t launch_dual_faces(const int* tri, int64_t nf, const int* label, int k, uint32_t* flags,
+                              cudaStream_t s);
+cudaError_t launch_dual_keys(const int* tri, const int* faces, int64_t m, const int* label, uint32_t* klo,
+                             uint32_t* khi, uint32_t* order, cudaStream_t s);
+cudaError_t launch_gather_u32(const uint32_t* src, const uint32_t* idx, int64_t m, uint32_t* dst, cudaStream_t s);
+cudaError_t launch_dual_unique(const uint32_t* klo, const uint32_t* khi, const uint32_t* order, int64_t m,
+                               uint32_t* keep, cudaStream_t s);
+cudaError_t launch_dual_write(const int* tri, const int* faces, const int* sel, int64_t t, const int* label,
+                              int* out, cudaStream_t s);
+cudaError_t launch_centroids(int metric, const DevState& st, double* out, cudaStream_t s);
+
+}  // namespace acvd

@@ -1,0 +1,263 @@
+"""ctypes binding of the C ABI in include/acvd_gpu.h (libacvd_gb300.so).
+
+`Engine` wraps one device context; the functions at module level are the
+host-side set-up helpers (topology, weights, initial sampling).  There is no
+fallback: if the CUDA library is missing or the device is unusable, the calls
+raise.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+ACVD_OK = 0
+ERRORS = {1: "ACVD_ERR_ARG", 2: "ACVD_ERR_CUDA", 3: "ACVD_ERR_ITER_LIMIT", 4: "ACVD_ERR_DEVICE_CHECK",
+          5: "ACVD_ERR_UNSUPPORTED"}
+METRICS = {"iso": 0, "isotropic": 0, "qem": 1, "aniso": 2, "quadric_anisotropic": 2}
+
+
+class AcvdError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class Opts(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int), ("use_graphs", ctypes.c_int), ("max_loops", ctypes.c_int),
+                ("max_convergences", ctypes.c_int), ("kernel_timing", ctypes.c_int)]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("sweeps", ctypes.c_int), ("convergences", ctypes.c_int), ("moves", ctypes.c_int64),
+                ("candidates", ctypes.c_int64), ("boundary_items", ctypes.c_int64),
+                ("targets", ctypes.c_int64), ("visited", ctypes.c_int64), ("slots", ctypes.c_int64),
+                ("disconnected", ctypes.c_int), ("unassigned", ctypes.c_int), ("device_ms", ctypes.c_double),
+                ("eval_ms", ctypes.c_double), ("eval_launches", ctypes.c_int), ("energy", ctypes.c_double),
+                ("eval_bytes", ctypes.c_int64), ("kernel_launches", ctypes.c_int64)]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+_LIB = None
+_P = ctypes.c_void_p
+_i64 = ctypes.c_int64
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def lib_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = True) -> ctypes.CDLL:
+    """Loads libacvd_gb300.so (building it first when it is absent)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    if not os.path.exists(_build.LIB):
+        if not build_if_missing:
+            raise RuntimeError(f"CUDA library not built: {_build.LIB}")
+        _build.build()
+    lib = ctypes.CDLL(_build.LIB)
+    sig = {
+        "acvd_default_opts": (None, [ctypes.POINTER(Opts)]),
+        "acvd_create": (_P, [ctypes.POINTER(Opts)]),
+        "acvd_destroy": (None, [_P]),
+        "acvd_last_error": (ctypes.c_char_p, [_P]),
+        "acvd_stream": (_P, [_P]),
+        "acvd_build_topology": (ctypes.c_int, [_i64, _i64, _P, _P, _P, _P, ctypes.POINTER(_i64)]),
+        "acvd_vertex_weights": (ctypes.c_int, [ctypes.c_int, _i64, _P, _i64, _P, _P, _P, _P, _P, ctypes.c_double, _P]),
+        "acvd_initial_sampling": (ctypes.c_int, [_i64, _P, _P, _P, ctypes.c_int32, _P]),
+        "acvd_set_mesh": (ctypes.c_int, [_P, _i64, _P, _i64, _P, _P, _P, _i64, _P]),
+        "acvd_set_metric": (ctypes.c_int, [_P, ctypes.c_int, _P, _P, ctypes.c_double]),
+        "acvd_set_quadrics_optimization_level": (ctypes.c_int, [_P, ctypes.c_int]),
+        "acvd_set_unconstrained_initialization": (ctypes.c_int, [_P, ctypes.c_int]),
+        "acvd_set_labels": (ctypes.c_int, [_P, ctypes.c_int32, _P]),
+        "acvd_minimize": (ctypes.c_int, [_P, ctypes.POINTER(Stats)]),
+        "acvd_rewind": (ctypes.c_int, [_P]),
+        "acvd_get_labels": (ctypes.c_int, [_P, _P]),
+        "acvd_get_clusters": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P, _P]),
+        "acvd_get_boundary_edges": (ctypes.c_int, [_P, _P, ctypes.POINTER(_i64)]),
+        "acvd_get_dual_mesh": (ctypes.c_int, [_P, _P, ctypes.POINTER(_i64)]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _LIB = lib
+    return lib
+
+
+def exported_symbols() -> list[str]:
+    """Entry points declared in include/acvd_gpu.h."""
+    hdr = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "acvd_gpu.h")
+    import re
+    return sorted(set(re.findall(r"\b(acvd_[a-z_0-9]+)\s*\(", open(hdr).read())))
+
+
+def _check(code: int, ctx=None, what: str = ""):
+    if code != ACVD_OK:
+        msg = what
+        if ctx:
+            msg = (load().acvd_last_error(ctx) or b"").decode() or what
+        raise AcvdError(code, msg)
+
+
+# ---------------------------------------------------------------------------
+# host-side set-up helpers
+# ---------------------------------------------------------------------------
+
+def build_topology(n_vertices: int, faces: np.ndarray):
+    """Ring CSR (row, col) and edge endpoints in the reference's numbering."""
+    lib = load()
+    tri = np.ascontiguousarray(faces, dtype=np.int32)
+    ne = _i64()
+    _check(lib.acvd_build_topology(n_vertices, tri.shape[0], _ptr(tri), None, None, None, ctypes.byref(ne)),
+           what="acvd_build_topology")
+    row = np.empty(n_vertices + 1, dtype=np.int32)
+    col = np.empty(2 * ne.value, dtype=np.int32)
+    ev = np.empty(2 * ne.value, dtype=np.int32)
+    _check(lib.acvd_build_topology(n_vertices, tri.shape[0], _ptr(tri), _ptr(row), _ptr(col), _ptr(ev),
+                                   ctypes.byref(ne)), what="acvd_build_topology")
+    return row, col, ev.reshape(-1, 2)
+
+
+def vertex_weights(metric: str, points: np.ndarray, faces: np.ndarray, indicator=None, gradation: float = 0.0):
+    lib = load()
+    pts = np.ascontiguousarray(points, dtype=np.float64)
+    tri = np.ascontiguousarray(faces, dtype=np.int32)
+    ind = None if indicator is None else np.ascontiguousarray(indicator, dtype=np.float64)
+    w = np.empty(pts.shape[0], dtype=np.float64)
+    _check(lib.acvd_vertex_weights(METRICS[metric], pts.shape[0], _ptr(pts), tri.shape[0], _ptr(tri), None, None,
+                                   None, _ptr(ind), float(gradation), _ptr(w)), what="acvd_vertex_weights")
+    return w
+
+
+def initial_sampling(row: np.ndarray, col: np.ndarray, weights: np.ndarray, k: int) -> np.ndarray:
+    lib = load()
+    row = np.ascontiguousarray(row, dtype=np.int32)
+    col = np.ascontiguousarray(col, dtype=np.int32)
+    w = np.ascontiguousarray(weights, dtype=np.float64)
+    lab = np.empty(row.shape[0] - 1, dtype=np.int32)
+    _check(lib.acvd_initial_sampling(row.shape[0] - 1, _ptr(row), _ptr(col), _ptr(w), int(k), _ptr(lab)),
+           what="acvd_initial_sampling")
+    return lab
+
+
+# ---------------------------------------------------------------------------
+# device context
+# ---------------------------------------------------------------------------
+
+class Engine:
+    """One GPU clustering context (acvd_ctx)."""
+
+    def __init__(self, device: int = 0, use_graphs: bool = True, kernel_timing: bool = False,
+                 max_loops: int | None = None):
+        lib = load()
+        o = Opts()
+        lib.acvd_default_opts(ctypes.byref(o))
+        o.device = device
+        o.use_graphs = 1 if use_graphs else 0
+        o.kernel_timing = 1 if kernel_timing else 0
+        if max_loops is not None:
+            o.max_loops = int(max_loops)
+        self._lib = lib
+        self.ctx = lib.acvd_create(ctypes.byref(o))
+        if not self.ctx:
+            raise AcvdError(2, "acvd_create failed (no usable CUDA device?)")
+        self.n = 0
+        self.k = 0
+        self.n_edges = 0
+
+    def close(self):
+        if getattr(self, "ctx", None):
+            self._lib.acvd_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _ck(self, code, what=""):
+        _check(code, self.ctx, what)
+
+    def stream(self) -> int:
+        return int(self._lib.acvd_stream(self.ctx) or 0)
+
+    def set_mesh(self, points, faces, row, col, edge_v):
+        self._pts = np.ascontiguousarray(points, dtype=np.float64)
+        self._tri = np.ascontiguousarray(faces, dtype=np.int32)
+        row = np.ascontiguousarray(row, dtype=np.int32)
+        col = np.ascontiguousarray(col, dtype=np.int32)
+        ev = np.ascontiguousarray(edge_v, dtype=np.int32)
+        self.n = self._pts.shape[0]
+        self.n_edges = ev.size // 2
+        self._ck(self._lib.acvd_set_mesh(self.ctx, self.n, _ptr(self._pts), self._tri.shape[0], _ptr(self._tri),
+                                         _ptr(row), _ptr(col), self.n_edges, _ptr(ev)), "acvd_set_mesh")
+
+    def set_metric(self, metric: str, indicator=None, principal_dirs=None, gradation: float = 0.0):
+        ind = None if indicator is None else np.ascontiguousarray(indicator, dtype=np.float64)
+        pd = None if principal_dirs is None else np.ascontiguousarray(principal_dirs, dtype=np.float32)
+        self.metric = metric
+        self._ck(self._lib.acvd_set_metric(self.ctx, METRICS[metric], _ptr(ind), _ptr(pd), float(gradation)),
+                 "acvd_set_metric")
+
+    def set_level(self, level: int):
+        self._ck(self._lib.acvd_set_quadrics_optimization_level(self.ctx, int(level)))
+
+    def set_unconstrained_initialization(self, on: int):
+        self._ck(self._lib.acvd_set_unconstrained_initialization(self.ctx, int(on)))
+
+    def set_labels(self, k: int, labels):
+        lab = np.ascontiguousarray(labels, dtype=np.int32)
+        self.k = int(k)
+        self._ck(self._lib.acvd_set_labels(self.ctx, self.k, _ptr(lab)), "acvd_set_labels")
+
+    def rewind(self):
+        self._ck(self._lib.acvd_rewind(self.ctx), "acvd_rewind")
+
+    def minimize(self) -> dict:
+        st = Stats()
+        self._ck(self._lib.acvd_minimize(self.ctx, ctypes.byref(st)), "acvd_minimize")
+        return st.as_dict()
+
+    def labels(self) -> np.ndarray:
+        out = np.empty(self.n, dtype=np.int32)
+        self._ck(self._lib.acvd_get_labels(self.ctx, _ptr(out)), "acvd_get_labels")
+        return out
+
+    def clusters(self) -> dict:
+        k = self.k
+        sz = np.empty(k, dtype=np.int32)
+        S = np.empty(3 * k); W = np.empty(k); Q = np.empty(9 * k); C = np.empty(3 * k); E = np.empty(k)
+        tot = ctypes.c_double()
+        self._ck(self._lib.acvd_get_clusters(self.ctx, _ptr(sz), _ptr(S), _ptr(W), _ptr(Q), _ptr(C), _ptr(E),
+                                             ctypes.byref(tot)), "acvd_get_clusters")
+        return {"size": sz, "S": S.reshape(k, 3), "W": W, "Q": Q.reshape(k, 9), "centroid": C.reshape(k, 3),
+                "energy": E, "energy_total": tot.value}
+
+    def boundary_edges(self) -> np.ndarray:
+        n = _i64()
+        self._ck(self._lib.acvd_get_boundary_edges(self.ctx, None, ctypes.byref(n)))
+        out = np.empty(max(n.value, 1), dtype=np.int32)
+        self._ck(self._lib.acvd_get_boundary_edges(self.ctx, _ptr(out), ctypes.byref(n)))
+        return out[:n.value]
+
+    def dual_mesh(self) -> np.ndarray:
+        n = _i64()
+        self._ck(self._lib.acvd_get_dual_mesh(self.ctx, None, ctypes.byref(n)))
+        out = np.empty(3 * max(n.value, 1), dtype=np.int32)
+        self._ck(self._lib.acvd_get_dual_mesh(self.ctx, _ptr(out), ctypes.byref(n)))
+        return out[:3 * n.value].reshape(-1, 3)

@@ -1,0 +1,347 @@
+"""Benchmark: time to a converged ACVDQ clustering on one GB300.
+
+Workload (default): ACVDQ -- QEM metric, curvature gradation 1.5, unconstrained
+initialisation -- on the seeded synthetic torus R=1, r=0.3, 1024 x 512 vertices
+(524,288 items, 1,048,576 triangles), 20,000 clusters, the reference's default
+initial sampling.  One "step" is one full minimisation (MinimizeEnergy) from the
+same initial clustering, inputs resident in HBM.  The metric is items/s =
+items / time-to-converge.  The GPU clustering's energy, evaluated with the
+reference arithmetic (oracle), must be within 0.1 % of the CPU run's converged
+energy.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Under torchrun (N > 1) every rank solves its own replica (a single mesh does not
+shard); rank 0 prints one JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "time to converged ACVDQ energy (<=0.1% of ref), items/s, batched meshes/s"
+L2_BYTES = 129 * 1024 * 1024
+
+WORKLOADS = {
+    "torus_1024x512_qem": dict(kind="torus", mesh=dict(nu=1024, nv=512, seed=0), metric="qem", k=20000,
+                               gradation=1.5, uinit=1,
+                               desc="ACVDQ torus R=1 r=0.3 1024x512 (524,288 items), K=20,000, gradation 1.5"),
+    "icosphere_l5_iso": dict(kind="icosphere", mesh=dict(level=5, seed=0), metric="iso", k=1000,
+                             gradation=0.0, uinit=0,
+                             desc="ACVD icosphere level 5 (10,242 items), K=1,000, isotropic"),
+    "torus_512x512_qem": dict(kind="torus", mesh=dict(nu=512, nv=512, seed=0), metric="qem", k=10000,
+                              gradation=1.0, uinit=1, density=True,
+                              desc="ACVDQ torus 512x512 (262,144 items), K=10,000, densities U[0.5,2], gradation 1"),
+    "heightfield_4096_aniso": dict(kind="heightfield", mesh=dict(n=4096, seed=0), metric="aniso", k=200000,
+                                   gradation=1.5, uinit=0,
+                                   desc="quadric-anisotropic heightfield 4096^2 (16,777,216 items), K=200,000"),
+}
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def make_workload(name):
+    from acvd_gb300 import synth
+    w = WORKLOADS[name]
+    m = synth.make(w["kind"], **w["mesh"])
+    ind = m.indicator
+    if w.get("density"):
+        ind = np.random.default_rng(1).uniform(0.5, 2.0, size=m.n_points)
+    use_ind = w["gradation"] != 0.0 if w["metric"] == "aniso" else w["gradation"] > 0.0
+    return m, (ind if use_ind else None), (m.principal_dirs if w["metric"] == "aniso" else None), w
+
+
+def initial_labels(m, metric, ind, grad, k):
+    import acvd_gb300
+    row, col, ev = acvd_gb300.build_topology(m.n_points, m.faces)
+    w = acvd_gb300.vertex_weights(metric, m.points, m.faces, ind, grad)
+    return acvd_gb300.initial_sampling(row, col, w, k), (row, col, ev)
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples during the timed region."""
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device),
+                 "--query-gpu=clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,"
+                 "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_power_cap,utilization.gpu",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.out = ""
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                self.out, _ = self.proc.communicate()
+
+    def summary(self):
+        rows = []
+        for line in (self.out or "").strip().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                rows.append((float(parts[0]), float(parts[1]), parts[2:6], float(parts[6])))
+            except ValueError:
+                continue
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        loaded = [r for r in rows if r[3] > 0] or rows
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in loaded for i, v in enumerate(r[2]) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(r[0] for r in loaded), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": reasons, "samples": len(rows), "samples_under_load": len(loaded)}
+
+
+def cpu_reference_run(m, ind, pd, w, lab0):
+    """The oracle's restatement of the reference's sequential MinimizeEnergy."""
+    from oracle import oracle
+    oracle.build(ref=False)
+    p = oracle.Port(w["metric"], m.points, m.faces, w["k"], w["gradation"], ind, pd, unconstrained_init=w["uinit"])
+    p.init(lab0)
+    secs = p.run()
+    return p, secs
+
+
+def _port_job(args):
+    name, = args
+    m, ind, pd, w = make_workload(name)
+    lab0, _ = initial_labels(m, w["metric"], ind, w["gradation"], w["k"])
+    p, secs = cpu_reference_run(m, ind, pd, w, lab0)
+    return m.n_points, secs, p.global_energy()
+
+
+def run_reference_arm(args):
+    """CPU arm: the reference algorithm (oracle restatement, sequential per mesh);
+    every host core solves its own copy of the workload, so the whole CPU is used."""
+    ws, rank, _ = _dist()
+    if rank != 0:
+        return
+    import multiprocessing as mp
+    cores = os.cpu_count() or 1
+    ctx = mp.get_context("spawn")
+    m, ind, pd, w = make_workload(args.workload)
+    # build once before forking workers
+    from oracle import oracle
+    oracle.build(ref=False)
+    times = []
+    energies = []
+    with ctx.Pool(cores) as pool:
+        for step in range(args.warmup + args.steps):
+            # every worker builds its copy, then times only its MinimizeEnergy; the
+            # copies run concurrently, so a step lasts as long as the slowest solve
+            res = pool.map(_port_job, [(args.workload,)] * cores)
+            if step >= args.warmup:
+                times.append(max(r[1] for r in res))
+                energies.append(res[0][2])
+    n = m.n_points
+    ms = 1000.0 * statistics.mean(times)
+    value = cores * n / (ms / 1000.0)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "items/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": args.workload, "description": w["desc"], "items": n, "clusters": w["k"],
+                       "copies_per_step": cores},
+            "cpu_baseline": {"value": value, "unit": "items/s", "cores": cores, "kind": "port",
+                             "sample": f"{cores} concurrent full solves of the workload (one per core), "
+                                       f"sequential reference algorithm restated in C++"},
+            "e2e": {"value": value, "unit": "items/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "energy": energies[-1] if energies else None}
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu_arm(args):
+    import torch
+    import acvd_gb300
+    from acvd_gb300 import engine as E
+
+    ws, rank, local = _dist()
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    device = local
+    torch.cuda.set_device(device)
+
+    m, ind, pd, w = make_workload(args.workload)
+    lab0, (row, col, ev) = initial_labels(m, w["metric"], ind, w["gradation"], w["k"])
+    n = m.n_points
+
+    eng = E.Engine(device=device, kernel_timing=True)
+    eng.set_mesh(m.points, m.faces, row, col, ev)
+    eng.set_metric(w["metric"], ind, pd, w["gradation"])
+    eng.set_unconstrained_initialization(w["uinit"])
+    eng.set_labels(w["k"], lab0)
+    stream = torch.cuda.ExternalStream(eng.stream(), device=device)
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=f"cuda:{device}")
+
+    def step():
+        eng.rewind()
+        return eng.minimize()
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+
+    step_ms = []
+    tot = {"eval_ms": 0.0, "eval_bytes": 0, "eval_launches": 0, "kernel_launches": 0, "sweeps": 0, "moves": 0}
+    with ClockSampler(device) as clk:
+        for _ in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()          # L2 flush between timed iterations (outside the events)
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            st = step()
+            e1.record(stream)
+            e1.synchronize()
+            step_ms.append(e0.elapsed_time(e1))
+            for k in tot:
+                tot[k] += st[k]
+    torch.cuda.synchronize()
+    ms = statistics.mean(step_ms)
+    if ws > 1:
+        t = torch.tensor([ms], device=f"cuda:{device}")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = ws * n / (ms / 1000.0)
+    lab = eng.labels()
+    gpu_energy_fp64 = st["energy"]
+
+    # end to end through the C ABI with host buffers (copies inside the timed region)
+    e2e = None
+    if not args.no_e2e:
+        h2d = (m.points.nbytes + m.faces.astype(np.int32).nbytes + row.nbytes + col.nbytes + ev.nbytes +
+               (ind.nbytes if ind is not None else 0) + (pd.nbytes if pd is not None else 0) + lab0.nbytes)
+        d2h = lab0.nbytes
+        e2e_ms = []
+        eng2 = E.Engine(device=device)
+        for it in range(max(1, args.steps)):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            eng2.set_mesh(m.points, m.faces, row, col, ev)
+            eng2.set_metric(w["metric"], ind, pd, w["gradation"])
+            eng2.set_unconstrained_initialization(w["uinit"])
+            eng2.set_labels(w["k"], lab0)
+            eng2.minimize()
+            out = eng2.labels()
+            torch.cuda.synchronize()
+            e2e_ms.append(1000.0 * (time.perf_counter() - t0))
+        eng2.close()
+        assert np.array_equal(out, lab), "end-to-end run differs from the resident run"
+        e2e_val = ws * n / (statistics.mean(e2e_ms) / 1000.0)
+        e2e = {"value": e2e_val, "unit": "items/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+               "ms_per_step": statistics.mean(e2e_ms)}
+
+    if ws > 1:
+        torch.distributed.barrier()
+    if rank != 0:
+        return
+
+    # CPU reference run (same workload, same initial clustering) and energy check
+    cpu = None
+    energy = {}
+    if not args.no_cpu_baseline:
+        p, secs = cpu_reference_run(m, ind, pd, w, lab0)
+        e_ref = p.global_energy()
+        from oracle import oracle
+        chk = oracle.Port(w["metric"], m.points, m.faces, w["k"], w["gradation"], ind, pd)
+        chk.evaluate(lab, 1)
+        e_gpu = chk.global_energy()
+        connected = chk.clean() == 0
+        cpu = {"value": n / secs, "unit": "items/s", "cores": 1, "kind": "port",
+               "sample": f"full workload, one sequential converged solve ({secs:.2f} s)"}
+        energy = {"reference_energy": e_ref, "gpu_energy_reference_arithmetic": e_gpu,
+                  "gpu_energy_fp64_device": gpu_energy_fp64,
+                  "rel_diff": (e_gpu - e_ref) / abs(e_ref), "within_0.1pct": bool(e_gpu <= e_ref + 1e-3 * abs(e_ref)),
+                  "all_clusters_connected": bool(connected)}
+
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    peak = peaks.get("hbm_gbs", 6800.0)
+    achieved = (tot["eval_bytes"] / 1e9) / (tot["eval_ms"] / 1000.0) if tot["eval_ms"] > 0 else None
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "eval_traffic.json")
+    if os.path.exists(tpath):
+        try:
+            traffic = json.load(open(tpath)).get(args.workload)
+        except ValueError:
+            traffic = None
+    line = {
+        "metric": METRIC, "value": value, "unit": "items/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": args.workload, "description": w["desc"], "items": n, "clusters": w["k"],
+                   "faces": m.n_faces, "parallelism": "replicas" if ws > 1 else "single",
+                   "l2": "flushed between timed steps (256 MB write)"},
+        "roofline": {"bound": "hbm", "kernel": "eval_kernel", "achieved": achieved,
+                     "peak": peak, "unit": "GB/s", "frac": (achieved / peak) if achieved else None,
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if "hbm_gbs" in peaks else "fallback",
+                     "traffic": traffic, "launches": tot["eval_launches"],
+                     "algorithmic_bytes_per_launch": tot["eval_bytes"] / max(1, tot["eval_launches"]),
+                     "avg_launch_us": 1000.0 * tot["eval_ms"] / max(1, tot["eval_launches"])},
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "gpu_launches": int(tot["kernel_launches"]),
+        "sweeps_per_step": tot["sweeps"] / max(1, args.steps),
+        "moves_per_step": tot["moves"] / max(1, args.steps),
+        "energy": energy,
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="torus_1024x512_qem", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference_arm(args)
+    else:
+        run_gpu_arm(args)
+
+
+if __name__ == "__main__":
+    main()

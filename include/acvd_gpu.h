@@ -1,0 +1,180 @@
+/*
+ * acvd_gpu.h -- C ABI of the GB300 (sm_103a) discrete Voronoi clustering engine.
+ *
+ * Drop-in for the energy-minimisation seam of ACVD's clustering path: the
+ * reference calls vtkUniformClustering<Metric>::MinimizeEnergy()
+ * (Common/vtkUniformClustering.h:264,725-830) from ProcessClustering()
+ * (:655-714), itself called by vtkDiscreteRemeshing<Metric>::Remesh()
+ * (DiscreteRemeshing/vtkDiscreteRemeshing.h:877-954).  These entry points take
+ * the same inputs that seam reads -- the mesh, the per-vertex weights /
+ * curvature data of the metric plugin, the initial clustering -- as plain host
+ * arrays, run the minimisation on the GPU and hand back the clustering, the
+ * cluster vertices and the dual (coarse) mesh.
+ *
+ * Conventions: ids are int32, vertex coordinates float64 xyz triples, triangles
+ * int32 triples.  Labels lie in [0, K); K itself marks an unassigned item (the
+ * reference's "null cluster", vtkUniformClustering.h:881-907).  The caller owns
+ * every host buffer (copied in/out during the call); the context owns all device
+ * memory.  A context is bound to one device and one CUDA stream and is not
+ * thread-safe; separate contexts may run concurrently.  No function aborts:
+ * each returns an ACVD_* status, with text from acvd_last_error().
+ */
+#ifndef ACVD_GPU_H
+#define ACVD_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define ACVD_OK 0
+#define ACVD_ERR_ARG 1          /* invalid argument or call order */
+#define ACVD_ERR_CUDA 2         /* CUDA runtime error */
+#define ACVD_ERR_ITER_LIMIT 3   /* an iteration cap was reached (MaxNumberOfLoops analogue) */
+#define ACVD_ERR_DEVICE_CHECK 4 /* a device-side consistency check failed */
+#define ACVD_ERR_UNSUPPORTED 5  /* input outside what this build handles */
+
+/* metric plugins (DiscreteRemeshing/vtk*MetricForClustering.h) */
+#define ACVD_METRIC_ISOTROPIC 0 /* vtkIsotropicMetricForClustering */
+#define ACVD_METRIC_QEM 1       /* vtkQEMetricForClustering */
+#define ACVD_METRIC_QUADRIC_ANISOTROPIC 2 /* vtkQuadricAnisotropicMetricForClustering */
+
+typedef struct acvd_ctx acvd_ctx;
+
+typedef struct acvd_opts {
+    int device;              /* CUDA device ordinal */
+    int use_graphs;          /* capture one sweep as a CUDA graph (1, default) */
+    int max_loops;           /* sweep cap; reference MaxNumberOfLoops = 5,000,000 (:1407) */
+    int max_convergences;    /* reference MaxNumberOfConvergences = 1e9 (:1406) */
+    int kernel_timing;       /* record CUDA events around every evaluation kernel */
+} acvd_opts;
+
+typedef struct acvd_stats {
+    int sweeps;               /* colour sweeps run (the reference's NumberOfLoops analogue) */
+    int convergences;         /* convergence events (reference :773-824) */
+    int64_t moves;            /* committed moves */
+    int64_t candidates;       /* proposed moves */
+    int64_t boundary_items;   /* boundary items evaluated */
+    int64_t targets;          /* (item, destination) energy evaluations */
+    int64_t visited;          /* items visited by the evaluation kernels */
+    int64_t slots;            /* ring slots read by the evaluation kernels */
+    int disconnected;         /* clusters split at the last convergence */
+    int unassigned;           /* items left unassigned after hole filling */
+    double device_ms;         /* MinimizeEnergy on the device (CUDA events) */
+    double eval_ms;           /* sum of evaluation-kernel times (kernel_timing only) */
+    int eval_launches;        /* evaluation kernels timed */
+    double energy;            /* global energy (FP64) of the final clustering */
+    int64_t eval_bytes;       /* algorithmic bytes of all evaluation kernels (counted on device) */
+    int64_t kernel_launches;  /* kernels launched by this call */
+} acvd_stats;
+
+/* Defaults: device 0, graphs on, the reference's loop caps. */
+void acvd_default_opts(acvd_opts* opts);
+
+acvd_ctx* acvd_create(const acvd_opts* opts);
+void acvd_destroy(acvd_ctx* ctx);
+const char* acvd_last_error(const acvd_ctx* ctx);
+
+/*
+ * Edge table and vertex rings in the reference's numbering
+ * (vtkSurfaceBase::CreateFromPolyData, Common/vtkSurfaceBase.cxx:1407-1468,
+ * AddEdge :1166-1221): faces are scanned in order and every new (v_j, v_j+1)
+ * pair becomes the next edge; a vertex ring lists its edges in creation order.
+ * Outputs: csr_row[nV+1], csr_col[2E] (ring neighbours), edge_v[2E].  Call with
+ * NULL outputs first to get *n_edges.
+ */
+int acvd_build_topology(int64_t n_vertices, int64_t n_faces, const int32_t* tri, int32_t* csr_row,
+                        int32_t* csr_col, int32_t* edge_v, int64_t* n_edges);
+
+/*
+ * Vertex weights of a metric plugin's BuildMetric, FP64 on the host:
+ * dual area (Common/vtkSurface.cxx:1342-1359) times indicator^gradation, clamped
+ * to [mean/ratio, mean*ratio] (ratio 1e5 isotropic / anisotropic, 1e4 QEM).
+ * indicator may be NULL.  Used for the initial sampling below.
+ */
+int acvd_vertex_weights(int metric, int64_t n_vertices, const double* xyz, int64_t n_faces, const int32_t* tri,
+                        const int32_t* csr_row, const int32_t* csr_col, const int32_t* edge_v,
+                        const double* indicator, double gradation, double* weights);
+
+/*
+ * The reference's default initial sampling (InitSamples type 1 ->
+ * ComputeInitialRandomSampling, Common/vtkUniformClustering.h:1178-1316):
+ * std::mt19937 seeded 0 shuffles the items, regions grow breadth-first to the
+ * average weight.  Writes labels[n_vertices] in [0, K] (K = unassigned).
+ */
+int acvd_initial_sampling(int64_t n_vertices, const int32_t* csr_row, const int32_t* csr_col,
+                          const double* weights, int32_t k, int32_t* labels);
+
+/*
+ * Mesh upload (SetInput, vtkSurfaceClustering.h:179-211): coordinates, triangles
+ * and the ring CSR / edge list from acvd_build_topology (or the caller's own
+ * vtkSurface, exported in the same order).
+ */
+int acvd_set_mesh(acvd_ctx* ctx, int64_t n_vertices, const double* xyz, int64_t n_faces, const int32_t* tri,
+                  const int32_t* csr_row, const int32_t* csr_col, int64_t n_edges, const int32_t* edge_v);
+
+/*
+ * Metric and its per-vertex inputs (Metric::BuildMetric, SetCurvatureInfo,
+ * SetGradation): builds the float32 item records on the device.  indicator
+ * (nV doubles) may be NULL when gradation is 0; principal_dirs (nV x 6 floats,
+ * direction 1 then direction 2, scaled by sqrt|curvature|) is required by the
+ * quadric-anisotropic metric only.
+ */
+int acvd_set_metric(acvd_ctx* ctx, int metric, const double* indicator, const float* principal_dirs,
+                    double gradation);
+
+/* Options of the reference API: SetQuadricsOptimizationLevel (default 3),
+ * SetUnconstrainedInitialization (default 0). */
+int acvd_set_quadrics_optimization_level(acvd_ctx* ctx, int level);
+int acvd_set_unconstrained_initialization(acvd_ctx* ctx, int on);
+
+/* SetNumberOfClusters + SetInitialClustering: K clusters, labels[nV] in [0, K]. */
+int acvd_set_labels(acvd_ctx* ctx, int32_t k, const int32_t* labels);
+
+/*
+ * MinimizeEnergy(): hole filling, statistics, colour sweeps until the
+ * reference's stopping rule holds (0 moves in a sweep and 0 disconnected
+ * clusters), with its early-convergence, unconstrained->constrained and
+ * connectivity phases.  stats may be NULL.
+ */
+int acvd_minimize(acvd_ctx* ctx, acvd_stats* stats);
+
+/* Restores, on the device, the assignment last given to acvd_set_labels (no
+ * host transfer), so that acvd_minimize can be repeated on resident inputs. */
+int acvd_rewind(acvd_ctx* ctx);
+
+/* GetClustering(): labels[nV]. */
+int acvd_get_labels(acvd_ctx* ctx, int32_t* labels);
+
+/*
+ * Per-cluster results: sizes[K], FP64 accumulators S[3K] (sum w x), W[K]
+ * (sum w), quadric[9K] (the reference's compact 9-coefficient quadric sum,
+ * zeros for the isotropic metric), placed vertex centroid[3K] and energy[K].
+ * Any output may be NULL.  Also returns the global energy in *energy_total.
+ */
+int acvd_get_clusters(acvd_ctx* ctx, int32_t* sizes, double* S, double* W, double* quadric, double* centroid,
+                      double* energy, double* energy_total);
+
+/* Edges whose endpoints carry different labels, in the reference's edge ids,
+ * increasing.  Call with ids = NULL to get *count first. */
+int acvd_get_boundary_edges(acvd_ctx* ctx, int32_t* ids, int64_t* count);
+
+/*
+ * Dual mesh (BuildDelaunayTriangulation, DiscreteRemeshing/vtkDiscreteRemeshing.h:1003-1152,
+ * vertex clustering, without manifold repair): one triangle per input face whose
+ * three labels are valid and distinct, in face order, duplicates (same label set)
+ * dropped; corners in the face's vertex order.  Call with tris = NULL to get
+ * *n_tris first.
+ */
+int acvd_get_dual_mesh(acvd_ctx* ctx, int32_t* tris, int64_t* n_tris);
+
+/* The CUDA stream (cudaStream_t) the context launches on. */
+void* acvd_stream(acvd_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ACVD_GPU_H */

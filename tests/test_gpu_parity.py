@@ -1,0 +1,177 @@
+"""CUDA path against the oracle (needs a GB300).
+
+(a) identical assignment: cluster sizes, boundary-edge set and dual-mesh
+    triangles bit-exact; accumulators and energies within 1e-6 relative of the
+    FP64 evaluation;
+(b) full runs from the same initial clustering: the reference arithmetic's
+    energy of the GPU clustering is within 0.1 % of the reference CPU run's
+    converged energy, every cluster connected, nothing unassigned;
+plus determinism (two runs bitwise identical) and the error paths.
+"""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+import acvd_gb300
+from acvd_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
+REL_ACC = 1e-6      # accumulators / energies vs FP64
+REL_ENERGY = 1e-3   # converged energy vs the reference run
+
+
+def _load(path):
+    z = np.load(path)
+    return {k: z[k] for k in z.files}
+
+
+def _engine(points, faces, metric, ind, pd, grad, level=3, uinit=0):
+    row, col, ev = acvd_gb300.build_topology(points.shape[0], faces)
+    e = acvd_gb300.Engine()
+    e.set_mesh(points, faces, row, col, ev)
+    e.set_metric(metric, ind, pd, grad)
+    e.set_level(level)
+    e.set_unconstrained_initialization(uinit)
+    return e, (row, col, ev)
+
+
+def _rel(a, b, scale):
+    return np.max(np.abs(np.asarray(a) - np.asarray(b)) / scale)
+
+
+@pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p)[:-4] for p in GOLDEN])
+def test_identical_assignment(oracle_lib, path):
+    g = _load(path)
+    metric = str(g["metric"])
+    k = int(g["k"])
+    grad = float(g["gradation"])
+    ind = g.get("indicator")
+    pd = g.get("principal_dirs")
+    e, (row, col, ev) = _engine(g["points"], g["faces"], metric, ind if (grad > 0 or metric == "aniso") else None,
+                                pd, grad)
+    lab = g["fixed_labels"]
+    e.set_labels(k, lab)
+    cl = e.clusters()
+    sizes = np.bincount(lab[lab < k], minlength=k)
+    np.testing.assert_array_equal(cl["size"], sizes)
+    # accumulators vs the reference's FP64 sums
+    assert _rel(cl["W"], g["fixed_W"], np.abs(g["fixed_W"])) < REL_ACC
+    sc = np.linalg.norm(g["fixed_S"], axis=1, keepdims=True)
+    assert _rel(cl["S"], g["fixed_S"], sc) < REL_ACC
+    if metric != "iso":
+        qs = np.max(np.abs(g["fixed_Q"]), axis=1, keepdims=True)
+        assert _rel(cl["Q"], g["fixed_Q"], qs) < REL_ACC
+    # energies (per cluster, and the total)
+    assert _rel(cl["energy"], g["fixed_cluster_energy"], np.abs(g["fixed_cluster_energy"])) < REL_ACC
+    assert abs(cl["energy_total"] - float(g["fixed_energy"])) < REL_ACC * abs(float(g["fixed_energy"]))
+    # boundary edges: exact set, reference edge ids
+    want = np.nonzero(lab[ev[:, 0]] != lab[ev[:, 1]])[0]
+    np.testing.assert_array_equal(e.boundary_edges(), want)
+    # dual mesh: exact triangles, order and corner order of the reference rule
+    p = oracle_lib.Port(metric, g["points"], g["faces"], k, grad, ind if (grad > 0 or metric == "aniso") else None, pd)
+    p.evaluate(lab, 1)
+    tris, _ = p.dual_mesh()
+    np.testing.assert_array_equal(e.dual_mesh(), tris)
+    e.close()
+
+
+RUNS = [
+    # name, metric, mesh, K, gradation, unconstrained init, seeds-init
+    ("iso_icosphere5_k1000_seeds", "iso", lambda: synth.icosphere(5, seed=0), 1000, 0.0, 0, True),
+    ("iso_icosphere4_k200", "iso", lambda: synth.icosphere(4, seed=1), 200, 0.0, 0, False),
+    ("qem_torus128x64_k600_g15", "qem", lambda: synth.torus(128, 64, seed=0), 600, 1.5, 1, False),
+    ("qem_torus96x48_k300_g0", "qem", lambda: synth.torus(96, 48, seed=2), 300, 0.0, 0, False),
+    ("aniso_heightfield64_k300_g15", "aniso", lambda: synth.heightfield(64, seed=0), 300, 1.5, 0, False),
+]
+
+
+def _run_case(oracle_lib, case):
+    name, metric, mk, k, grad, uinit, seeds = case
+    m = mk()
+    ind = m.indicator if (grad > 0 or metric == "aniso") else None
+    pd = m.principal_dirs if metric == "aniso" else None
+    init = synth.seed_labels(m.n_points, k, seed=11) if seeds else None
+    ref = oracle_lib.Port(metric, m.points, m.faces, k, grad, ind, pd, unconstrained_init=uinit)
+    ref.init(init)
+    lab0 = ref.labels()
+    ref.run()
+    e_ref = ref.global_energy()
+    e, topo = _engine(m.points, m.faces, metric, ind, pd, grad, uinit=uinit)
+    e.set_labels(k, lab0)
+    stats = e.minimize()
+    lab = e.labels()
+    return m, ind, pd, lab, stats, e_ref, e
+
+
+@pytest.mark.parametrize("case", RUNS, ids=[c[0] for c in RUNS])
+def test_full_run_energy_and_connectivity(oracle_lib, case):
+    name, metric, mk, k, grad, uinit, seeds = case
+    m, ind, pd, lab, stats, e_ref, e = _run_case(oracle_lib, case)
+    assert np.all(lab < k), "unassigned items left"
+    ev = oracle_lib.Port(metric, m.points, m.faces, k, grad, ind, pd)
+    ev.evaluate(lab, 1)
+    e_gpu = ev.global_energy()
+    # lower is better; within 0.1 % of the reference's converged energy
+    assert e_gpu <= e_ref + REL_ENERGY * abs(e_ref), (e_gpu, e_ref, stats)
+    # every cluster connected (the reference's CleanClustering finds nothing to split)
+    assert ev.clean() == 0
+    assert np.all(ev.clusters()["size"] > 0)
+    # the GPU's own FP64 energy of its clustering agrees with the reference arithmetic
+    assert abs(stats["energy"] - e_gpu) < REL_ACC * abs(e_gpu)
+    e.close()
+
+
+def test_determinism(oracle_lib):
+    case = RUNS[2]
+    out = []
+    for _ in range(2):
+        m, ind, pd, lab, stats, e_ref, e = _run_case(oracle_lib, case)
+        out.append((lab, stats["energy"], stats["moves"], stats["sweeps"]))
+        e.close()
+    np.testing.assert_array_equal(out[0][0], out[1][0])
+    assert out[0][1:] == out[1][1:]
+
+
+def test_remesh_api_end_to_end():
+    m = synth.torus(96, 48, seed=4)
+    mesh = acvd_gb300.Surface(m.points, m.faces)
+    r = acvd_gb300.QIsotropicDiscreteRemeshing()
+    r.SetInput(mesh)
+    r.SetNumberOfClusters(300)
+    r.SetSubsamplingThreshold(10)
+    r.GetMetric().SetGradation(1.5)
+    r.SetCurvatureInfo(m.indicator)
+    r.SetUnconstrainedInitialization(1)
+    r.Remesh()
+    out = r.GetOutput()
+    assert out.GetNumberOfPoints() == 300
+    # closed torus: the coarse mesh is a closed surface of genus 1 when it is clean
+    assert out.GetNumberOfCells() > 500
+    lab = r.GetClustering()
+    assert lab.shape == (m.n_points,) and lab.max() < 300
+
+
+def test_error_paths():
+    m = synth.icosphere(3)
+    e = acvd_gb300.Engine()
+    with pytest.raises(acvd_gb300.AcvdError):
+        e.minimize()                       # nothing set
+    row, col, ev = acvd_gb300.build_topology(m.n_points, m.faces)
+    e.set_mesh(m.points, m.faces, row, col, ev)
+    with pytest.raises(acvd_gb300.AcvdError):
+        e.set_metric("qem", None, None, 1.5)   # gradation without indicator
+    with pytest.raises(acvd_gb300.AcvdError):
+        e.set_metric("aniso", m.points[:, 0].copy(), None, 1.0)  # no principal directions
+    e.set_metric("iso")
+    with pytest.raises(acvd_gb300.AcvdError):
+        e.set_labels(10, np.full(m.n_points, 11, dtype=np.int32))  # label > K
+    r = acvd_gb300.IsotropicDiscreteRemeshing()
+    r.SetInput(acvd_gb300.Surface(m.points, m.faces))
+    r.SetNumberOfClusters(500)                 # 642 < 10 * 500: would need subdivision
+    with pytest.raises(acvd_gb300.AcvdError):
+        r.Remesh()
+    e.close()
