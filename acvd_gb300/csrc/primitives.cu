@@ -67,9 +67,10 @@ __global__ void scan_add_kernel(uint32_t* __restrict__ out, int64_t n, const uin
     if (i < n) out[i] += offs[i / kScanTile];
 }
 
-__global__ void scan_total_kernel(const uint32_t* in, const uint32_t* out, int64_t n, uint32_t* total) {
+// total = last exclusive prefix + last input (saved before an in-place scan)
+__global__ void scan_total_kernel(const uint32_t* last_in, const uint32_t* out, int64_t n, uint32_t* total) {
     if (n == 0) { *total = 0; return; }
-    *total = out[n - 1] + in[n - 1];
+    *total = out[n - 1] + last_in[0];
 }
 
 static size_t scan_scratch_words(int64_t n) {
