@@ -84,7 +84,7 @@ struct acvd_ctx {
     cudaGraphExec_t sweep_exec = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     std::vector<cudaEvent_t> ev_eval;
-    int64_t launches = 0;          // kernels launched by acvd_minimize
+    bool timing_broken = false;    // event timing unavailable on this device / driver
     int64_t sweep_kernels = 0;     // kernels in one sweep
     DBuf<int> label_init;          // the assignment given to acvd_set_labels (for acvd_rewind)
 
@@ -492,9 +492,10 @@ static int enqueue_sweep(acvd_ctx* ctx, bool timing) {
         const int* items = ctx->color_items.p + ctx->color_off[c];
         const int64_t cnt = ctx->color_off[c + 1] - ctx->color_off[c];
         if (cnt == 0) continue;
-        if (timing) CK(cudaEventRecord(ctx->ev_eval[2 * c], ctx->s));
+        // cudaEventRecordExternal makes the records real graph nodes when captured
+        if (timing) CK(cudaEventRecordWithFlags(ctx->ev_eval[2 * c], ctx->s, cudaEventRecordExternal));
         CK(launch_eval(ctx->metric, st, items, cnt, c, ctx->cand_dest.p, ctx->cand_prio.p, ctx->s));
-        if (timing) CK(cudaEventRecord(ctx->ev_eval[2 * c + 1], ctx->s));
+        if (timing) CK(cudaEventRecordWithFlags(ctx->ev_eval[2 * c + 1], ctx->s, cudaEventRecordExternal));
         CK(launch_apply(ctx->metric, st, items, cnt, c, ctx->cand_dest.p, ctx->cand_prio.p, ctx->s));
         kernels += 2;
     }
@@ -531,11 +532,17 @@ static int run_sweep(acvd_ctx* ctx, bool timing, double* eval_ms, int* eval_laun
     int r = sync_counters(ctx);
     if (r) return r;
     *moves = (int64_t)ctx->h_counters[kCntMoves];
-    if (timing) {
+    if (timing && !ctx->timing_broken) {
         for (int c = 0; c < ctx->ncolors; c++) {
             if (ctx->color_off[c + 1] == ctx->color_off[c]) continue;
             float ms = 0.f;
-            CK(cudaEventElapsedTime(&ms, ctx->ev_eval[2 * c], ctx->ev_eval[2 * c + 1]));
+            if (cudaEventElapsedTime(&ms, ctx->ev_eval[2 * c], ctx->ev_eval[2 * c + 1]) != cudaSuccess) {
+                // timing is instrumentation only: report it as unavailable, keep running
+                cudaGetLastError();
+                ctx->timing_broken = true;
+                *eval_ms = -1.0;
+                break;
+            }
             *eval_ms += ms;
             (*eval_launches)++;
         }
