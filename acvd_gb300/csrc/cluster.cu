@@ -11,6 +11,8 @@
 // 64-bit atomicMin; `apply` commits the proposals that hold both claims.  No
 // cluster takes part in two commits of one step, so every committed energy
 // change is exact and the result does not depend on thread timing.
+#include <algorithm>
+
 #include "primitives.cuh"
 #include "state.cuh"
 
@@ -198,6 +200,11 @@ ACVD_DEV void warp_count(unsigned long long* ctr, unsigned v) {
 
 // ---------------------------------------------------------------------------
 // eval: proposals for one colour class
+//
+// An item is skipped when neither its own cluster nor any cluster around it
+// changed since it was last evaluated without result (the reference skips an
+// edge when neither cluster was modified in the previous loop,
+// vtkUniformClustering.h:912-920).  Proposals go to a compact per-step list.
 // ---------------------------------------------------------------------------
 template <int M>
 __global__ void __launch_bounds__(256) eval_kernel(DevState st, const int* __restrict__ items, int64_t count,
@@ -206,21 +213,32 @@ __global__ void __launch_bounds__(256) eval_kernel(DevState st, const int* __res
     const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const bool in = idx < count;
     unsigned n_slots = 0, n_bnd = 0, n_tgt = 0, n_cand = 0;
+    int my_slot_cand = 0;
     if (in) {
         const int i = items[idx];
         const int L = st.label[i];
         const int p0 = st.row[i], p1 = st.row[i + 1];
+        const SweepState sw = *st.sweep;
+        const int ev_i = st.evald[i];
+        bool fresh = ev_i <= sw.floor || (L < st.k && st.stamp[L] >= ev_i);
         n_slots = (unsigned)(p1 - p0);
         bool boundary = false;
-        for (int p = p0; p < p1; p++) boundary |= (st.label[st.col[p]] != L);
-        if (boundary) {
+        for (int p = p0; p < p1; p++) {
+            const int B = st.label[st.col[p]];
+            if (B != L) {
+                boundary = true;
+                if (B < st.k && st.stamp[B] >= ev_i) fresh = true;
+            }
+        }
+        if (boundary && fresh) {
             n_bnd = 1;
             const RunFlags fl = *st.flags;
             ItemRec it;
             load_item<M>(st, i, it);
+            int best = -1;
+            unsigned pr = 0u;
             if (L >= st.k) {
                 // unassigned item: joins the neighbouring cluster it is cheapest to join
-                int best = -1;
                 float bv = 0.0f;
                 for (int p = p0; p < p1; p++) {
                     const int B = st.label[st.col[p]];
@@ -231,18 +249,12 @@ __global__ void __launch_bounds__(256) eval_kernel(DevState st, const int* __res
                     n_tgt++;
                     if (best < 0 || v < bv || (v == bv && B < best)) { best = B; bv = v; }
                 }
-                if (best >= 0) {
-                    cand_dest[idx] = best;
-                    cand_prio[idx] = 0u;
-                    atomicMin(&st.claim[best], make_claim((unsigned)epoch, 0u, (unsigned)idx));
-                    n_cand = 1;
-                }
+                pr = 0u;
             } else if (st.size[L] > 1 && (!fl.connexity || ring_connected(st, p0, p1, L))) {
                 EvalRec eL;
                 load_eval<M>(st, L, eL);
                 float xc[3];
                 const float rem = remove_part<M>(eL, it, fl, xc);
-                int best = -1;
                 float bde = 0.0f;
                 for (int p = p0; p < p1; p++) {
                     const int B = st.label[st.col[p]];
@@ -256,17 +268,31 @@ __global__ void __launch_bounds__(256) eval_kernel(DevState st, const int* __res
                     n_tgt++;
                     if (de < bde || (de == bde && best >= 0 && B < best)) { best = B; bde = de; }
                 }
-                if (best >= 0 && bde < 0.0f) {
-                    const unsigned pr = prio_of_delta(bde);
-                    cand_dest[idx] = best;
-                    cand_prio[idx] = pr;
-                    const unsigned long long c = make_claim((unsigned)epoch, pr, (unsigned)idx);
-                    atomicMin(&st.claim[L], c);
-                    atomicMin(&st.claim[best], c);
-                    n_cand = 1;
-                }
+                if (best >= 0 && !(bde < 0.0f)) best = -1;
+                if (best >= 0) pr = prio_of_delta(bde);
+            }
+            if (best >= 0) {
+                cand_dest[idx] = best;
+                cand_prio[idx] = pr;
+                const unsigned long long c = make_claim((unsigned)epoch, pr, (unsigned)idx);
+                if (L < st.k) atomicMin(&st.claim[L], c);
+                atomicMin(&st.claim[best], c);
+                n_cand = 1;
+                st.evald[i] = -1;
+            } else {
+                st.evald[i] = sw.sweep;
             }
         }
+        my_slot_cand = n_cand;
+    }
+    // warp-aggregated append to the compact proposal list
+    const unsigned bal = __ballot_sync(kFull, my_slot_cand != 0);
+    if (bal) {
+        const int lane = threadIdx.x & 31;
+        unsigned base = 0;
+        if (lane == 0) base = atomicAdd(&st.cand_count[epoch], (unsigned)__popc(bal));
+        base = __shfl_sync(kFull, base, 0);
+        if (my_slot_cand) st.cand_list[base + __popc(bal & ((1u << lane) - 1u))] = (int)idx;
     }
     warp_count(&st.counters[kCntVisited], in ? 1u : 0u);
     warp_count(&st.counters[kCntSlots], n_slots);
@@ -313,10 +339,14 @@ ACVD_DEV void accumulate_item(df* acc, const ItemRec& it, float sgn) {
     }
 }
 
-// Per-cluster evaluation record and FP64 energy from the accumulators
-// (ComputeClusterCentroid + ComputeClusterEnergy of the metric plugins; the
-// quadric placement with the reference's thresholded pseudo-inverse in FP64).
-template <int M>
+// Per-cluster evaluation record from the accumulators (ComputeClusterCentroid +
+// ComputeClusterEnergy of the metric plugins).  FULL: the quadric placement with
+// the reference's thresholded pseudo-inverse in FP64 and the cluster's FP64
+// energy (full recompute, final results).  Otherwise (a committed move): m and
+// the residual r = b - A m in FP64 from the compensated sums, the 3x3
+// pseudo-inverse in FP32 like the evaluation kernel's; energies are left for the
+// next FULL pass.
+template <int M, bool FULL>
 ACVD_DEV void update_cluster(const DevState& st, int k) {
     const df* a = st.acc + (int64_t)k * Layout<M>::acc;
     float4* ev = st.ev + (int64_t)k * Layout<M>::ev;
@@ -325,14 +355,14 @@ ACVD_DEV void update_cluster(const DevState& st, int k) {
     if (!(W > 0.0)) {
         ev[0] = make_float4(0.f, 0.f, 0.f, 0.f);
         if (M != kIso) for (int j = 1; j < Layout<M>::ev; j++) ev[j] = make_float4(0.f, 0.f, 0.f, 0.f);
-        st.energy[k] = 0.0;
+        if (FULL) st.energy[k] = 0.0;
         return;
     }
     const double m[3] = {S[0] / W, S[1] / W, S[2] / W};
     ev[0] = make_float4((float)m[0], (float)m[1], (float)m[2], (float)W);
     const double S2W = (S[0] * S[0] + S[1] * S[1] + S[2] * S[2]) / W;
     if (M == kIso) {
-        st.energy[k] = -S2W;
+        if (FULL) st.energy[k] = -S2W;
         return;
     }
     const RunFlags fl = *st.flags;
@@ -344,14 +374,24 @@ ACVD_DEV void update_cluster(const DevState& st, int k) {
     const double r[3] = {b[0] - Am[0], b[1] - Am[1], b[2] - Am[2]};
     double d[3] = {0.0, 0.0, 0.0};
     const bool place = (M == kAniso) || (fl.constrained && fl.level > 0);
-    if (place) pinv_apply<double>(A, r, d, fl.level, (double)fl.thr, 32);
+    if (place) {
+        if (FULL) {
+            pinv_apply<double>(A, r, d, fl.level, (double)fl.thr, 32);
+        } else {
+            const float Af[6] = {(float)A[0], (float)A[1], (float)A[2], (float)A[3], (float)A[4], (float)A[5]};
+            const float rf[3] = {(float)r[0], (float)r[1], (float)r[2]};
+            float dfl[3];
+            pinv_apply<float>(Af, rf, dfl, fl.level, fl.thr, 8);
+            d[0] = dfl[0]; d[1] = dfl[1]; d[2] = dfl[2];
+        }
+    }
     const double P = W * (d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
     ev[1] = make_float4((float)d[0], (float)d[1], (float)d[2], (float)P);
     ev[2] = make_float4((float)r[0], (float)r[1], (float)r[2], 0.f);
     ev[3] = make_float4((float)A[0], (float)A[1], (float)A[2], (float)A[3]);
     if (M == kQEM) {
         ev[4] = make_float4((float)A[4], (float)A[5], 0.f, 0.f);
-        st.energy[k] = P - S2W;
+        if (FULL) st.energy[k] = P - S2W;
         return;
     }
     double T[6], u[3];
@@ -365,44 +405,51 @@ ACVD_DEV void update_cluster(const DevState& st, int k) {
     ev[5] = make_float4((float)T[0], (float)T[1], (float)T[2], (float)T[3]);
     ev[6] = make_float4((float)T[4], (float)T[5], (float)g[0], (float)g[1]);
     ev[7] = make_float4((float)g[2], 0.f, 0.f, 0.f);
-    st.energy[k] = (c[0] * Tc[0] + c[1] * Tc[1] + c[2] * Tc[2]) - 2.0 * (c[0] * u[0] + c[1] * u[1] + c[2] * u[2]);
+    if (FULL)
+        st.energy[k] = (c[0] * Tc[0] + c[1] * Tc[1] + c[2] * Tc[2]) - 2.0 * (c[0] * u[0] + c[1] * u[1] + c[2] * u[2]);
 }
 
 // ---------------------------------------------------------------------------
-// apply: commit the proposals that hold both claims
+// apply: commit the proposals that hold both claims (grid-stride over the
+// step's compact proposal list)
 // ---------------------------------------------------------------------------
 template <int M>
-__global__ void __launch_bounds__(256) apply_kernel(DevState st, const int* __restrict__ items, int64_t count,
-                                                    int epoch, int* __restrict__ cand_dest,
+__global__ void __launch_bounds__(256) apply_kernel(DevState st, const int* __restrict__ items, int epoch,
+                                                    const int* __restrict__ cand_dest,
                                                     const unsigned* __restrict__ cand_prio) {
-    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    unsigned won = 0;
-    if (idx < count) {
+    const unsigned n = st.cand_count[epoch];
+    unsigned won_total = 0;
+    for (unsigned j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        const int idx = st.cand_list[j];
         const int B = cand_dest[idx];
-        if (B >= 0) {
-            cand_dest[idx] = -1;
-            const int i = items[idx];
-            const int L = st.label[i];
-            const unsigned long long key = make_claim((unsigned)epoch, cand_prio[idx], (unsigned)idx);
-            if (st.claim[B] == key && (L >= st.k || st.claim[L] == key)) {
-                won = 1;
-                ItemRec it;
-                load_item<M>(st, i, it);
-                st.label[i] = B;
-                st.size[B] += 1;
-                df* aB = st.acc + (int64_t)B * Layout<M>::acc;
-                accumulate_item<M>(aB, it, 1.0f);
-                update_cluster<M>(st, B);
-                if (L < st.k) {
-                    st.size[L] -= 1;
-                    df* aL = st.acc + (int64_t)L * Layout<M>::acc;
-                    accumulate_item<M>(aL, it, -1.0f);
-                    update_cluster<M>(st, L);
-                }
-            }
+        const int i = items[idx];
+        const int L = st.label[i];
+        const unsigned long long key = make_claim((unsigned)epoch, cand_prio[idx], (unsigned)idx);
+        if (st.claim[B] != key || (L < st.k && st.claim[L] != key)) continue;
+        won_total++;
+        ItemRec it;
+        load_item<M>(st, i, it);
+        const int now = st.sweep->sweep;
+        st.label[i] = B;
+        st.size[B] += 1;
+        st.stamp[B] = now;
+        accumulate_item<M>(st.acc + (int64_t)B * Layout<M>::acc, it, 1.0f);
+        update_cluster<M, false>(st, B);
+        if (L < st.k) {
+            st.size[L] -= 1;
+            st.stamp[L] = now;
+            accumulate_item<M>(st.acc + (int64_t)L * Layout<M>::acc, it, -1.0f);
+            update_cluster<M, false>(st, L);
         }
     }
-    warp_count(&st.counters[kCntMoves], won);
+    // every thread of the grid reaches this point: warp-aggregated count
+    warp_count(&st.counters[kCntMoves], won_total);
+}
+
+__global__ void begin_sweep_kernel(DevState st, int ncolors) {
+    const int t = threadIdx.x;
+    if (t == 0) st.sweep->sweep += 1;
+    if (t < ncolors) st.cand_count[t] = 0u;
 }
 
 // ---------------------------------------------------------------------------
@@ -459,7 +506,7 @@ __global__ void __launch_bounds__(256) reduce_clusters_kernel(DevState st, const
 template <int M>
 __global__ void update_all_kernel(DevState st) {
     const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (k < st.k) update_cluster<M>(st, (int)k);
+    if (k < st.k) update_cluster<M, true>(st, (int)k);
 }
 
 // ---------------------------------------------------------------------------
@@ -666,7 +713,20 @@ cudaError_t launch_eval(int metric, const DevState& st, const int* items, int64_
 cudaError_t launch_apply(int metric, const DevState& st, const int* items, int64_t count, int epoch,
                          int* cand_dest, const unsigned* cand_prio, cudaStream_t s) {
     if (count == 0) return cudaSuccess;
-    ACVD_DISPATCH(metric, apply_kernel, nblk(count), 256, s, st, items, count, epoch, cand_dest, cand_prio);
+    // the proposal count is only known on the device: a grid of 2 blocks per SM
+    // strides over the list
+    int dev = 0, sms = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int64_t want = nblk(count);
+    const unsigned grid = (unsigned)std::min<int64_t>(want, 2 * (int64_t)sms);
+    ACVD_DISPATCH(metric, apply_kernel, grid, 256, s, st, items, epoch, cand_dest, cand_prio);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_begin_sweep(const DevState& st, int ncolors, cudaStream_t s) {
+    ++g_launches;
+    begin_sweep_kernel<<<1, 64, 0, s>>>(st, ncolors);
     return cudaGetLastError();
 }
 

@@ -2,6 +2,7 @@
 // C ABI declared in include/acvd_gpu.h.
 #include <algorithm>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -51,8 +52,8 @@ struct acvd_ctx {
     DBuf<unsigned> adj;
     int ncolors = 0;
     std::vector<int64_t> color_off;
-    DBuf<int> color_items, cand_dest;
-    DBuf<unsigned> cand_prio;
+    DBuf<int> color_items, cand_dest, cand_list;
+    DBuf<unsigned> cand_prio, cand_count;
 
     // items
     int metric = -1;
@@ -61,8 +62,9 @@ struct acvd_ctx {
 
     // clusters
     int K = 0;
-    DBuf<int> label, size;
+    DBuf<int> label, size, stamp, evald;
     DBuf<unsigned long long> claim;
+    DBuf<SweepState> dsweep;
     DBuf<df> acc;
     DBuf<float4> ev;
     DBuf<double> energy;
@@ -108,6 +110,11 @@ struct acvd_ctx {
         st.energy = energy.p;
         st.counters = counters.p;
         st.flags = dflags.p;
+        st.sweep = dsweep.p;
+        st.stamp = stamp.p;
+        st.evald = evald.p;
+        st.cand_list = cand_list.p;
+        st.cand_count = cand_count.p;
         return st;
     }
     void drop_graph() {
@@ -147,6 +154,14 @@ static int sync_counters(acvd_ctx* ctx) {
 
 static int upload_flags(acvd_ctx* ctx) {
     CK(cudaMemcpyAsync(ctx->dflags.p, &ctx->flags, sizeof(RunFlags), cudaMemcpyHostToDevice, ctx->s));
+    CK(cudaStreamSynchronize(ctx->s));
+    return ACVD_OK;
+}
+
+// sweep counter and invalidation floor (every cluster counts as modified after `floor`)
+static int set_sweep_state(acvd_ctx* ctx, int sweep, int floor) {
+    SweepState h{sweep, floor};
+    CK(cudaMemcpyAsync(ctx->dsweep.p, &h, sizeof h, cudaMemcpyHostToDevice, ctx->s));
     CK(cudaStreamSynchronize(ctx->s));
     return ACVD_OK;
 }
@@ -205,7 +220,11 @@ static int setup_colors(acvd_ctx* ctx) {
     }
     CK(ctx->cand_dest.resize(mx));
     CK(ctx->cand_prio.resize(mx));
+    CK(ctx->cand_list.resize(mx));
+    CK(ctx->cand_count.resize(64));
+    CK(ctx->evald.resize(n));
     CK(cudaMemsetAsync(ctx->cand_dest.p, 0xff, mx * sizeof(int), ctx->s));
+    CK(cudaMemsetAsync(ctx->cand_count.p, 0, 64 * sizeof(unsigned), ctx->s));
     return ACVD_OK;
 }
 
@@ -227,6 +246,7 @@ acvd_ctx* acvd_create(const acvd_opts* opts) {
         cudaStreamCreateWithFlags(&ctx->s, cudaStreamNonBlocking) != cudaSuccess ||
         cudaMallocHost((void**)&ctx->h_counters, kNumCounters * sizeof(unsigned long long)) != cudaSuccess ||
         ctx->counters.resize(kNumCounters) != cudaSuccess || ctx->dflags.resize(1) != cudaSuccess ||
+        ctx->dsweep.resize(1) != cudaSuccess ||
         cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess) {
         cudaGetLastError();
         delete ctx;
@@ -377,6 +397,7 @@ int acvd_set_labels(acvd_ctx* ctx, int32_t k, const int32_t* labels) {
     const int ms = ctx->metric >= 0 ? ctx->metric : kAniso;
     CK(ctx->label.resize(ctx->nV));
     CK(ctx->size.resize(k + 1));
+    CK(ctx->stamp.resize(k + 1));
     CK(ctx->claim.resize(k + 1));
     CK(ctx->acc.resize((size_t)(k + 1) * acc_stride(kAniso)));
     CK(ctx->ev.resize((size_t)(k + 1) * ev_stride(kAniso)));
@@ -487,7 +508,8 @@ static int enqueue_sweep(acvd_ctx* ctx, bool timing) {
     DevState st = ctx->state();
     CK(cudaMemsetAsync(ctx->claim.p, 0xff, (ctx->K + 1) * sizeof(unsigned long long), ctx->s));
     CK(cudaMemsetAsync(ctx->counters.p + kCntMoves, 0, sizeof(unsigned long long), ctx->s));
-    int64_t kernels = 0;
+    CK(launch_begin_sweep(st, ctx->ncolors, ctx->s));
+    int64_t kernels = 1;
     for (int c = 0; c < ctx->ncolors; c++) {
         const int* items = ctx->color_items.p + ctx->color_off[c];
         const int64_t cnt = ctx->color_off[c + 1] - ctx->color_off[c];
@@ -574,6 +596,12 @@ extern "C" int acvd_minimize(acvd_ctx* ctx, acvd_stats* stats) {
     int status = ACVD_OK;
     do {
         // FillHolesInClustering, FillQueuesFromClustering, ReComputeStatistics (:727-730)
+        if (cudaMemsetAsync(ctx->evald.p, 0xff, ctx->nV * sizeof(int), ctx->s) != cudaSuccess ||
+            cudaMemsetAsync(ctx->stamp.p, 0, (ctx->K + 1) * sizeof(int), ctx->s) != cudaSuccess) {
+            status = fail(ctx, ACVD_ERR_CUDA, "memset of the activity arrays failed");
+            break;
+        }
+        if ((r = set_sweep_state(ctx, 0, 0))) { status = r; break; }
         int unassigned = 0;
         if ((r = fill_holes(ctx, &unassigned))) { status = r; break; }
         if ((r = recompute(ctx))) { status = r; break; }
@@ -586,6 +614,10 @@ extern "C" int acvd_minimize(acvd_ctx* ctx, acvd_stats* stats) {
             if ((r = run_sweep(ctx, timing, &local.eval_ms, &local.eval_launches, &mods))) { status = r; break; }
             sweeps++;
             local.moves += mods;
+            if (std::getenv("ACVD_TRACE"))
+                std::fprintf(stderr, "acvd sweep %d moves %lld cand %llu boundary %llu targets %llu conv %d flags %d%d\n",
+                             sweeps, (long long)mods, ctx->h_counters[kCntCand], ctx->h_counters[kCntBoundary],
+                             ctx->h_counters[kCntTargets], convergences, ctx->flags.constrained, ctx->flags.connexity);
             if (mods == 0 || sweeps > ctx->opts.max_loops || (mods <= early / 1000 && convergences <= 1)) {
                 bool flags_changed = false;
                 if (ctx->unconstrained && convergences == 0 && ctx->metric == kQEM) {
@@ -605,6 +637,8 @@ extern "C" int acvd_minimize(acvd_ctx* ctx, acvd_stats* stats) {
                 local.disconnected = disc;
                 local.unassigned = un;
                 if ((r = recompute(ctx))) { status = r; break; }
+                // SetAllClustersToModified (:822): every item is evaluated again
+                if ((r = set_sweep_state(ctx, sweeps, sweeps))) { status = r; break; }
                 if (disc == 0 && mods == 0) break;
                 if (sweeps >= ctx->opts.max_loops) { status = fail(ctx, ACVD_ERR_ITER_LIMIT, "sweep cap reached"); break; }
                 if (convergences >= ctx->opts.max_convergences) break;

@@ -61,6 +61,14 @@ enum Counter {
     kNumCounters = 16
 };
 
+// Sweep bookkeeping on the device (one captured graph serves every sweep):
+// `sweep` counts sweeps, `floor` is the sweep after which every cluster counts as
+// modified (the reference's SetAllClustersToModified, vtkUniformClustering.h:717-722).
+struct SweepState {
+    int sweep;
+    int floor;
+};
+
 struct DevState {
     int64_t n;        // items
     int k;            // clusters; label k = null (unassigned)
@@ -80,6 +88,11 @@ struct DevState {
     double* energy;
     unsigned long long* counters;
     const RunFlags* flags;
+    SweepState* sweep;     // sweep counter / invalidation floor
+    int* stamp;            // per cluster: sweep of its last modification
+    int* evald;            // per item: sweep of its last evaluation without a proposal (-1: none)
+    int* cand_list;        // compact list of proposals (colour-list positions) of the current step
+    unsigned* cand_count;  // per colour: number of proposals
 };
 
 // ---- items / topology (topology.cu) ----
@@ -100,6 +113,7 @@ cudaError_t launch_finish_items(int metric, int64_t nv, const double* xyz, const
                                 float2* tb, cudaStream_t s);
 
 // ---- clustering (cluster.cu) ----
+cudaError_t launch_begin_sweep(const DevState& st, int ncolors, cudaStream_t s);
 cudaError_t launch_eval(int metric, const DevState& st, const int* items, int64_t count, int epoch,
                         int* cand_dest, unsigned* cand_prio, cudaStream_t s);
 cudaError_t launch_apply(int metric, const DevState& st, const int* items, int64_t count, int epoch,

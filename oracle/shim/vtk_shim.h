@@ -114,6 +114,7 @@ class vtkShimArray : public vtkDataArray {
 public:
     void SetNumberOfValues(vtkIdType n) { V.resize(n); }
     void SetNumberOfComponents(int c) { NumComp = c; }
+    int GetNumberOfComponents() const { return NumComp; }
     void SetNumberOfTuples(vtkIdType n) { V.resize(n * NumComp); }
     vtkIdType GetNumberOfTuples() const { return (vtkIdType)V.size() / NumComp; }
     vtkIdType GetNumberOfValues() const { return (vtkIdType)V.size(); }
