@@ -21,6 +21,9 @@ namespace acvd {
 // ---------------------------------------------------------------------------
 // item and cluster records
 // ---------------------------------------------------------------------------
+// relative margin an energy decrease must exceed to be proposed (about 100 float32 ulps)
+constexpr float kAcceptTol = 1e-5f;
+
 struct ItemRec {
     float x[3];
     float w;
@@ -208,8 +211,9 @@ ACVD_DEV void warp_count(unsigned long long* ctr, unsigned v) {
 // ---------------------------------------------------------------------------
 template <int M>
 __global__ void __launch_bounds__(256) eval_kernel(DevState st, const int* __restrict__ items, int64_t count,
-                                                   int epoch, int* __restrict__ cand_dest,
+                                                   int color, int* __restrict__ cand_dest,
                                                    unsigned* __restrict__ cand_prio) {
+    const int epoch = color * kRounds;   // claim epoch of this step's first matching round
     const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const bool in = idx < count;
     unsigned n_slots = 0, n_bnd = 0, n_tgt = 0, n_cand = 0;
@@ -255,7 +259,7 @@ __global__ void __launch_bounds__(256) eval_kernel(DevState st, const int* __res
                 load_eval<M>(st, L, eL);
                 float xc[3];
                 const float rem = remove_part<M>(eL, it, fl, xc);
-                float bde = 0.0f;
+                float bde = 0.0f, badd = 0.0f;
                 for (int p = p0; p < p1; p++) {
                     const int B = st.label[st.col[p]];
                     if (B == L || B >= st.k) continue;
@@ -264,11 +268,15 @@ __global__ void __launch_bounds__(256) eval_kernel(DevState st, const int* __res
                     if (dup) continue;
                     EvalRec eB;
                     load_eval<M>(st, B, eB);
-                    const float de = rem + add_part<M>(eB, it, fl);
+                    const float add = add_part<M>(eB, it, fl);
+                    const float de = rem + add;
                     n_tgt++;
-                    if (de < bde || (de == bde && best >= 0 && B < best)) { best = B; bde = de; }
+                    if (de < bde || (de == bde && best >= 0 && B < best)) { best = B; bde = de; badd = add; }
                 }
-                if (best >= 0 && !(bde < 0.0f)) best = -1;
+                // a move must gain more than the float32 error of its own test
+                // (two near-tie moves could otherwise both test negative and
+                // alternate); the reference keeps an item on ties (:960)
+                if (best >= 0 && !(bde < -kAcceptTol * (fabsf(rem) + fabsf(badd)))) best = -1;
                 if (best >= 0) pr = prio_of_delta(bde);
             }
             if (best >= 0) {
@@ -290,7 +298,7 @@ __global__ void __launch_bounds__(256) eval_kernel(DevState st, const int* __res
     if (bal) {
         const int lane = threadIdx.x & 31;
         unsigned base = 0;
-        if (lane == 0) base = atomicAdd(&st.cand_count[epoch], (unsigned)__popc(bal));
+        if (lane == 0) base = atomicAdd(&st.cand_count[color], (unsigned)__popc(bal));
         base = __shfl_sync(kFull, base, 0);
         if (my_slot_cand) st.cand_list[base + __popc(bal & ((1u << lane) - 1u))] = (int)idx;
     }
@@ -414,17 +422,19 @@ ACVD_DEV void update_cluster(const DevState& st, int k) {
 // step's compact proposal list)
 // ---------------------------------------------------------------------------
 template <int M>
-__global__ void __launch_bounds__(256) apply_kernel(DevState st, const int* __restrict__ items, int epoch,
-                                                    const int* __restrict__ cand_dest,
+__global__ void __launch_bounds__(256) apply_kernel(DevState st, const int* __restrict__ items, int color,
+                                                    int round, int* __restrict__ cand_dest,
                                                     const unsigned* __restrict__ cand_prio) {
-    const unsigned n = st.cand_count[epoch];
+    const unsigned n = st.cand_count[color];
+    const unsigned epoch = (unsigned)(color * kRounds + round);
     unsigned won_total = 0;
     for (unsigned j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
         const int idx = st.cand_list[j];
         const int B = cand_dest[idx];
+        if (B < 0) continue;                     // committed or dropped in an earlier round
         const int i = items[idx];
         const int L = st.label[i];
-        const unsigned long long key = make_claim((unsigned)epoch, cand_prio[idx], (unsigned)idx);
+        const unsigned long long key = make_claim(epoch, cand_prio[idx], (unsigned)idx);
         if (st.claim[B] != key || (L < st.k && st.claim[L] != key)) continue;
         won_total++;
         ItemRec it;
@@ -433,17 +443,43 @@ __global__ void __launch_bounds__(256) apply_kernel(DevState st, const int* __re
         st.label[i] = B;
         st.size[B] += 1;
         st.stamp[B] = now;
+        st.claim[B] = 0ull;                      // taken for the rest of this step
+        cand_dest[idx] = -1;
         accumulate_item<M>(st.acc + (int64_t)B * Layout<M>::acc, it, 1.0f);
         update_cluster<M, false>(st, B);
         if (L < st.k) {
             st.size[L] -= 1;
             st.stamp[L] = now;
+            st.claim[L] = 0ull;
             accumulate_item<M>(st.acc + (int64_t)L * Layout<M>::acc, it, -1.0f);
             update_cluster<M, false>(st, L);
         }
     }
     // every thread of the grid reaches this point: warp-aggregated count
     warp_count(&st.counters[kCntMoves], won_total);
+}
+
+// Next matching round of a step: a proposal whose two clusters were not touched
+// by this step's commits still carries an exact energy change and claims again
+// with a newer epoch; one that lost a cluster to a commit is dropped (its item
+// is evaluated again next sweep).
+__global__ void reclaim_kernel(DevState st, const int* __restrict__ items, int color, int round,
+                               int* __restrict__ cand_dest, const unsigned* __restrict__ cand_prio) {
+    const unsigned n = st.cand_count[color];
+    const unsigned epoch = (unsigned)(color * kRounds + round);
+    for (unsigned j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        const int idx = st.cand_list[j];
+        const int B = cand_dest[idx];
+        if (B < 0) continue;
+        const int L = st.label[items[idx]];
+        if (st.claim[B] == 0ull || (L < st.k && st.claim[L] == 0ull)) {
+            cand_dest[idx] = -1;
+            continue;
+        }
+        const unsigned long long key = make_claim(epoch, cand_prio[idx], (unsigned)idx);
+        if (L < st.k) atomicMin(&st.claim[L], key);
+        atomicMin(&st.claim[B], key);
+    }
 }
 
 __global__ void begin_sweep_kernel(DevState st, int ncolors) {
@@ -703,24 +739,34 @@ static inline unsigned nblk(int64_t n, int b = 256) { return (unsigned)((n + b -
         else KERNEL<kAniso><<<grid, block, 0, stream>>>(__VA_ARGS__);                     \
     } while (0)
 
-cudaError_t launch_eval(int metric, const DevState& st, const int* items, int64_t count, int epoch,
+cudaError_t launch_eval(int metric, const DevState& st, const int* items, int64_t count, int color,
                         int* cand_dest, unsigned* cand_prio, cudaStream_t s) {
     if (count == 0) return cudaSuccess;
-    ACVD_DISPATCH(metric, eval_kernel, nblk(count), 256, s, st, items, count, epoch, cand_dest, cand_prio);
+    ACVD_DISPATCH(metric, eval_kernel, nblk(count), 256, s, st, items, count, color, cand_dest, cand_prio);
     return cudaGetLastError();
 }
 
-cudaError_t launch_apply(int metric, const DevState& st, const int* items, int64_t count, int epoch,
-                         int* cand_dest, const unsigned* cand_prio, cudaStream_t s) {
-    if (count == 0) return cudaSuccess;
+static unsigned list_grid(int64_t count) {
     // the proposal count is only known on the device: a grid of 2 blocks per SM
     // strides over the list
     int dev = 0, sms = 152;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int64_t want = nblk(count);
-    const unsigned grid = (unsigned)std::min<int64_t>(want, 2 * (int64_t)sms);
-    ACVD_DISPATCH(metric, apply_kernel, grid, 256, s, st, items, epoch, cand_dest, cand_prio);
+    return (unsigned)std::min<int64_t>(nblk(count), 2 * (int64_t)sms);
+}
+
+cudaError_t launch_apply(int metric, const DevState& st, const int* items, int64_t count, int color, int round,
+                         int* cand_dest, const unsigned* cand_prio, cudaStream_t s) {
+    if (count == 0) return cudaSuccess;
+    ACVD_DISPATCH(metric, apply_kernel, list_grid(count), 256, s, st, items, color, round, cand_dest, cand_prio);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_reclaim(const DevState& st, const int* items, int64_t count, int color, int round,
+                           int* cand_dest, const unsigned* cand_prio, cudaStream_t s) {
+    if (count == 0) return cudaSuccess;
+    ++g_launches;
+    reclaim_kernel<<<list_grid(count), 256, 0, s>>>(st, items, color, round, cand_dest, cand_prio);
     return cudaGetLastError();
 }
 

@@ -53,6 +53,14 @@ struct acvd_ctx {
     int ncolors = 0;
     std::vector<int64_t> color_off;
     DBuf<int> color_items, cand_dest, cand_list;
+    // sweep classes: either the colour classes, or one class holding every item
+    // (claims alone keep committed moves on disjoint clusters; colours are kept
+    // for hole filling)
+    bool sweep_by_color = true;
+    DBuf<int> all_items;
+    std::vector<int64_t> sweep_off;
+    const int* sweep_items = nullptr;
+    int nclasses = 0;
     DBuf<unsigned> cand_prio, cand_count;
 
     // items
@@ -87,6 +95,7 @@ struct acvd_ctx {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     std::vector<cudaEvent_t> ev_eval;
     bool timing_broken = false;    // event timing unavailable on this device / driver
+    int match_rounds = 1;          // claim/commit rounds per colour step (ACVD_MATCH_ROUNDS, up to kRounds)
     int64_t sweep_kernels = 0;     // kernels in one sweep
     DBuf<int> label_init;          // the assignment given to acvd_set_labels (for acvd_rewind)
 
@@ -218,6 +227,18 @@ static int setup_colors(acvd_ctx* ctx) {
         ctx->color_off[c + 1] = ctx->color_off[c] + cnt[c];
         mx = std::max<int64_t>(mx, cnt[c]);
     }
+    CK(ctx->all_items.resize(n));
+    CK(cudaMemcpyAsync(ctx->all_items.p, iota.data(), n * sizeof(int), cudaMemcpyHostToDevice, ctx->s));
+    if (ctx->sweep_by_color) {
+        ctx->sweep_off = ctx->color_off;
+        ctx->sweep_items = ctx->color_items.p;
+    } else {
+        ctx->sweep_off = {0, n};
+        ctx->sweep_items = ctx->all_items.p;
+        mx = n;
+    }
+    ctx->nclasses = (int)ctx->sweep_off.size() - 1;
+    CK(cudaStreamSynchronize(ctx->s));
     CK(ctx->cand_dest.resize(mx));
     CK(ctx->cand_prio.resize(mx));
     CK(ctx->cand_list.resize(mx));
@@ -242,6 +263,11 @@ acvd_ctx* acvd_create(const acvd_opts* opts) {
     acvd_ctx* ctx = new acvd_ctx;
     if (opts) ctx->opts = *opts;
     else acvd_default_opts(&ctx->opts);
+    if (const char* c = std::getenv("ACVD_SWEEP_COLORS")) ctx->sweep_by_color = std::atoi(c) != 0;
+    if (const char* r = std::getenv("ACVD_MATCH_ROUNDS")) {
+        const int v = std::atoi(r);
+        if (v >= 1 && v <= kRounds) ctx->match_rounds = v;
+    }
     if (cudaSetDevice(ctx->opts.device) != cudaSuccess ||
         cudaStreamCreateWithFlags(&ctx->s, cudaStreamNonBlocking) != cudaSuccess ||
         cudaMallocHost((void**)&ctx->h_counters, kNumCounters * sizeof(unsigned long long)) != cudaSuccess ||
@@ -506,30 +532,35 @@ static int clean(acvd_ctx* ctx, int* n_disconnected) {
 // are recorded inside the captured graph and read after the sweep's sync.
 static int enqueue_sweep(acvd_ctx* ctx, bool timing) {
     DevState st = ctx->state();
-    CK(cudaMemsetAsync(ctx->claim.p, 0xff, (ctx->K + 1) * sizeof(unsigned long long), ctx->s));
     CK(cudaMemsetAsync(ctx->counters.p + kCntMoves, 0, sizeof(unsigned long long), ctx->s));
-    CK(launch_begin_sweep(st, ctx->ncolors, ctx->s));
+    CK(launch_begin_sweep(st, ctx->nclasses, ctx->s));
     int64_t kernels = 1;
-    for (int c = 0; c < ctx->ncolors; c++) {
-        const int* items = ctx->color_items.p + ctx->color_off[c];
-        const int64_t cnt = ctx->color_off[c + 1] - ctx->color_off[c];
+    for (int c = 0; c < ctx->nclasses; c++) {
+        const int* items = ctx->sweep_items + ctx->sweep_off[c];
+        const int64_t cnt = ctx->sweep_off[c + 1] - ctx->sweep_off[c];
         if (cnt == 0) continue;
+        CK(cudaMemsetAsync(ctx->claim.p, 0xff, (ctx->K + 1) * sizeof(unsigned long long), ctx->s));
         // cudaEventRecordExternal makes the records real graph nodes when captured
         if (timing) CK(cudaEventRecordWithFlags(ctx->ev_eval[2 * c], ctx->s, cudaEventRecordExternal));
         CK(launch_eval(ctx->metric, st, items, cnt, c, ctx->cand_dest.p, ctx->cand_prio.p, ctx->s));
         if (timing) CK(cudaEventRecordWithFlags(ctx->ev_eval[2 * c + 1], ctx->s, cudaEventRecordExternal));
-        CK(launch_apply(ctx->metric, st, items, cnt, c, ctx->cand_dest.p, ctx->cand_prio.p, ctx->s));
+        CK(launch_apply(ctx->metric, st, items, cnt, c, 0, ctx->cand_dest.p, ctx->cand_prio.p, ctx->s));
         kernels += 2;
+        for (int r = 1; r < ctx->match_rounds; r++) {
+            CK(launch_reclaim(st, items, cnt, c, r, ctx->cand_dest.p, ctx->cand_prio.p, ctx->s));
+            CK(launch_apply(ctx->metric, st, items, cnt, c, r, ctx->cand_dest.p, ctx->cand_prio.p, ctx->s));
+            kernels += 2;
+        }
     }
     ctx->sweep_kernels = kernels;
     return ACVD_OK;
 }
 
 static int run_sweep(acvd_ctx* ctx, bool timing, double* eval_ms, int* eval_launches, int64_t* moves) {
-    if (timing && (int)ctx->ev_eval.size() != 2 * ctx->ncolors) {
+    if (timing && (int)ctx->ev_eval.size() != 2 * ctx->nclasses) {
         ctx->drop_graph();
         ctx->drop_events();
-        ctx->ev_eval.resize(2 * ctx->ncolors);
+        ctx->ev_eval.resize(2 * ctx->nclasses);
         for (auto& e : ctx->ev_eval) CK(cudaEventCreate(&e));
     }
     if (ctx->opts.use_graphs) {
@@ -555,8 +586,8 @@ static int run_sweep(acvd_ctx* ctx, bool timing, double* eval_ms, int* eval_laun
     if (r) return r;
     *moves = (int64_t)ctx->h_counters[kCntMoves];
     if (timing && !ctx->timing_broken) {
-        for (int c = 0; c < ctx->ncolors; c++) {
-            if (ctx->color_off[c + 1] == ctx->color_off[c]) continue;
+        for (int c = 0; c < ctx->nclasses; c++) {
+            if (ctx->sweep_off[c + 1] == ctx->sweep_off[c]) continue;
             float ms = 0.f;
             if (cudaEventElapsedTime(&ms, ctx->ev_eval[2 * c], ctx->ev_eval[2 * c + 1]) != cudaSuccess) {
                 // timing is instrumentation only: report it as unavailable, keep running
@@ -640,7 +671,8 @@ extern "C" int acvd_minimize(acvd_ctx* ctx, acvd_stats* stats) {
                 // SetAllClustersToModified (:822): every item is evaluated again
                 if ((r = set_sweep_state(ctx, sweeps, sweeps))) { status = r; break; }
                 if (disc == 0 && mods == 0) break;
-                if (sweeps >= ctx->opts.max_loops) { status = fail(ctx, ACVD_ERR_ITER_LIMIT, "sweep cap reached"); break; }
+                // MaxNumberOfLoops ends the minimisation like a convergence (:803-810)
+                if (sweeps >= ctx->opts.max_loops) { local.hit_loop_cap = 1; break; }
                 if (convergences >= ctx->opts.max_convergences) break;
             }
         }

@@ -29,6 +29,10 @@ namespace acvd {
 
 enum Metric { kIso = 0, kQEM = 1, kAniso = 2 };
 
+// Matching rounds per colour step (claim epochs: colour * kRounds + round, at
+// most 64 colours, so epochs fit the claim word's 8-bit field).
+constexpr int kRounds = 4;
+
 template <int M> struct Layout;
 template <> struct Layout<kIso> { static constexpr int acc = 4, ev = 1; };
 template <> struct Layout<kQEM> { static constexpr int acc = 13, ev = 5; };
@@ -114,10 +118,12 @@ cudaError_t launch_finish_items(int metric, int64_t nv, const double* xyz, const
 
 // ---- clustering (cluster.cu) ----
 cudaError_t launch_begin_sweep(const DevState& st, int ncolors, cudaStream_t s);
-cudaError_t launch_eval(int metric, const DevState& st, const int* items, int64_t count, int epoch,
+cudaError_t launch_eval(int metric, const DevState& st, const int* items, int64_t count, int color,
                         int* cand_dest, unsigned* cand_prio, cudaStream_t s);
-cudaError_t launch_apply(int metric, const DevState& st, const int* items, int64_t count, int epoch,
+cudaError_t launch_apply(int metric, const DevState& st, const int* items, int64_t count, int color, int round,
                          int* cand_dest, const unsigned* cand_prio, cudaStream_t s);
+cudaError_t launch_reclaim(const DevState& st, const int* items, int64_t count, int color, int round,
+                           int* cand_dest, const unsigned* cand_prio, cudaStream_t s);
 cudaError_t launch_update_all(int metric, const DevState& st, cudaStream_t s);
 cudaError_t launch_cluster_keys(const DevState& st, uint32_t* keys, uint32_t* vals, uint32_t* counts,
                                 cudaStream_t s);

@@ -37,7 +37,7 @@ class Stats(ctypes.Structure):
                 ("targets", ctypes.c_int64), ("visited", ctypes.c_int64), ("slots", ctypes.c_int64),
                 ("disconnected", ctypes.c_int), ("unassigned", ctypes.c_int), ("device_ms", ctypes.c_double),
                 ("eval_ms", ctypes.c_double), ("eval_launches", ctypes.c_int), ("energy", ctypes.c_double),
-                ("eval_bytes", ctypes.c_int64), ("kernel_launches", ctypes.c_int64)]
+                ("eval_bytes", ctypes.c_int64), ("kernel_launches", ctypes.c_int64), ("hit_loop_cap", ctypes.c_int)]
 
     def as_dict(self) -> dict:
         return {name: getattr(self, name) for name, _ in self._fields_}
@@ -158,8 +158,12 @@ def initial_sampling(row: np.ndarray, col: np.ndarray, weights: np.ndarray, k: i
 class Engine:
     """One GPU clustering context (acvd_ctx)."""
 
+    # sweep cap used unless the caller asks otherwise (the reference's own cap,
+    # 5,000,000 loops, is for a sequential loop; a GPU sweep does far more work)
+    DEFAULT_MAX_LOOPS = 20000
+
     def __init__(self, device: int = 0, use_graphs: bool = True, kernel_timing: bool = False,
-                 max_loops: int | None = None):
+                 max_loops: int | None = DEFAULT_MAX_LOOPS):
         lib = load()
         o = Opts()
         lib.acvd_default_opts(ctypes.byref(o))

@@ -68,6 +68,7 @@ typedef struct acvd_stats {
     double energy;            /* global energy (FP64) of the final clustering */
     int64_t eval_bytes;       /* algorithmic bytes of all evaluation kernels (counted on device) */
     int64_t kernel_launches;  /* kernels launched by this call */
+    int hit_loop_cap;         /* 1 if max_loops ended the minimisation (the reference just stops there too) */
 } acvd_stats;
 
 /* Defaults: device 0, graphs on, the reference's loop caps. */
