@@ -212,7 +212,7 @@ ACVD_DEV void warp_count(unsigned long long* ctr, unsigned v) {
 template <int M>
 __global__ void __launch_bounds__(256) eval_kernel(DevState st, const int* __restrict__ items, int64_t count,
                                                    int color, int* __restrict__ cand_dest,
-                                                   unsigned* __restrict__ cand_prio) {
+                                                   unsigned* __restrict__ cand_prio, int claims) {
     const int epoch = color * kRounds;   // claim epoch of this step's first matching round
     const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const bool in = idx < count;
@@ -282,9 +282,11 @@ __global__ void __launch_bounds__(256) eval_kernel(DevState st, const int* __res
             if (best >= 0) {
                 cand_dest[idx] = best;
                 cand_prio[idx] = pr;
-                const unsigned long long c = make_claim((unsigned)epoch, pr, (unsigned)idx);
-                if (L < st.k) atomicMin(&st.claim[L], c);
-                atomicMin(&st.claim[best], c);
+                if (claims) {
+                    const unsigned long long c = make_claim((unsigned)epoch, pr, (unsigned)idx);
+                    if (L < st.k) atomicMin(&st.claim[L], c);
+                    atomicMin(&st.claim[best], c);
+                }
                 n_cand = 1;
                 st.evald[i] = -1;
             } else {
@@ -347,13 +349,12 @@ ACVD_DEV void accumulate_item(df* acc, const ItemRec& it, float sgn) {
     }
 }
 
-// Per-cluster evaluation record from the accumulators (ComputeClusterCentroid +
-// ComputeClusterEnergy of the metric plugins).  FULL: the quadric placement with
-// the reference's thresholded pseudo-inverse in FP64 and the cluster's FP64
-// energy (full recompute, final results).  Otherwise (a committed move): m and
-// the residual r = b - A m in FP64 from the compensated sums, the 3x3
-// pseudo-inverse in FP32 like the evaluation kernel's; energies are left for the
-// next FULL pass.
+// Per-cluster evaluation record and FP64 energy from the accumulators
+// (ComputeClusterCentroid + ComputeClusterEnergy of the metric plugins).  FULL:
+// the quadric placement with the reference's thresholded pseudo-inverse in FP64
+// (full recompute, final results).  Otherwise (a committed move): m and the
+// residual r = b - A m in FP64 from the compensated sums, the 3x3
+// pseudo-inverse in FP32 like the evaluation kernel's.
 template <int M, bool FULL>
 ACVD_DEV void update_cluster(const DevState& st, int k) {
     const df* a = st.acc + (int64_t)k * Layout<M>::acc;
@@ -363,14 +364,14 @@ ACVD_DEV void update_cluster(const DevState& st, int k) {
     if (!(W > 0.0)) {
         ev[0] = make_float4(0.f, 0.f, 0.f, 0.f);
         if (M != kIso) for (int j = 1; j < Layout<M>::ev; j++) ev[j] = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (FULL) st.energy[k] = 0.0;
+        st.energy[k] = 0.0;
         return;
     }
     const double m[3] = {S[0] / W, S[1] / W, S[2] / W};
     ev[0] = make_float4((float)m[0], (float)m[1], (float)m[2], (float)W);
     const double S2W = (S[0] * S[0] + S[1] * S[1] + S[2] * S[2]) / W;
     if (M == kIso) {
-        if (FULL) st.energy[k] = -S2W;
+        st.energy[k] = -S2W;
         return;
     }
     const RunFlags fl = *st.flags;
@@ -399,7 +400,7 @@ ACVD_DEV void update_cluster(const DevState& st, int k) {
     ev[3] = make_float4((float)A[0], (float)A[1], (float)A[2], (float)A[3]);
     if (M == kQEM) {
         ev[4] = make_float4((float)A[4], (float)A[5], 0.f, 0.f);
-        if (FULL) st.energy[k] = P - S2W;
+        st.energy[k] = P - S2W;
         return;
     }
     double T[6], u[3];
@@ -413,8 +414,7 @@ ACVD_DEV void update_cluster(const DevState& st, int k) {
     ev[5] = make_float4((float)T[0], (float)T[1], (float)T[2], (float)T[3]);
     ev[6] = make_float4((float)T[4], (float)T[5], (float)g[0], (float)g[1]);
     ev[7] = make_float4((float)g[2], 0.f, 0.f, 0.f);
-    if (FULL)
-        st.energy[k] = (c[0] * Tc[0] + c[1] * Tc[1] + c[2] * Tc[2]) - 2.0 * (c[0] * u[0] + c[1] * u[1] + c[2] * u[2]);
+    st.energy[k] = (c[0] * Tc[0] + c[1] * Tc[1] + c[2] * Tc[2]) - 2.0 * (c[0] * u[0] + c[1] * u[1] + c[2] * u[2]);
 }
 
 // ---------------------------------------------------------------------------
@@ -436,23 +436,58 @@ __global__ void __launch_bounds__(256) apply_kernel(DevState st, const int* __re
         const int L = st.label[i];
         const unsigned long long key = make_claim(epoch, cand_prio[idx], (unsigned)idx);
         if (st.claim[B] != key || (L < st.k && st.claim[L] != key)) continue;
-        won_total++;
         ItemRec it;
         load_item<M>(st, i, it);
         const int now = st.sweep->sweep;
-        st.label[i] = B;
-        st.size[B] += 1;
-        st.stamp[B] = now;
         st.claim[B] = 0ull;                      // taken for the rest of this step
         cand_dest[idx] = -1;
-        accumulate_item<M>(st.acc + (int64_t)B * Layout<M>::acc, it, 1.0f);
+        df* aB = st.acc + (int64_t)B * Layout<M>::acc;
+        float4* eB = st.ev + (int64_t)B * Layout<M>::ev;
+        if (L >= st.k) {
+            // unassigned item joining a cluster: always committed
+            won_total++;
+            st.label[i] = B;
+            st.size[B] += 1;
+            st.stamp[B] = now;
+            accumulate_item<M>(aB, it, 1.0f);
+            update_cluster<M, false>(st, B);
+            continue;
+        }
+        st.claim[L] = 0ull;
+        df* aL = st.acc + (int64_t)L * Layout<M>::acc;
+        float4* eL = st.ev + (int64_t)L * Layout<M>::ev;
+        // keep the two clusters' records: the commit is undone unless the tracked
+        // energy of the pair strictly decreases (the float32 test can disagree with
+        // the updated records, e.g. when a pseudo-inverse eigenvalue sits at the
+        // threshold), so the minimisation descends monotonically and terminates
+        df saveB[Layout<M>::acc], saveL[Layout<M>::acc];
+        float4 sevB[Layout<M>::ev], sevL[Layout<M>::ev];
+#pragma unroll
+        for (int q = 0; q < Layout<M>::acc; q++) { saveB[q] = aB[q]; saveL[q] = aL[q]; }
+#pragma unroll
+        for (int q = 0; q < Layout<M>::ev; q++) { sevB[q] = eB[q]; sevL[q] = eL[q]; }
+        const double eB_old = st.energy[B], eL_old = st.energy[L];
+        const double e_old = eB_old + eL_old;
+        accumulate_item<M>(aB, it, 1.0f);
+        accumulate_item<M>(aL, it, -1.0f);
         update_cluster<M, false>(st, B);
-        if (L < st.k) {
+        update_cluster<M, false>(st, L);
+        const double e_new = st.energy[B] + st.energy[L];
+        if (e_new < e_old) {
+            won_total++;
+            st.label[i] = B;
+            st.size[B] += 1;
             st.size[L] -= 1;
+            st.stamp[B] = now;
             st.stamp[L] = now;
-            st.claim[L] = 0ull;
-            accumulate_item<M>(st.acc + (int64_t)L * Layout<M>::acc, it, -1.0f);
-            update_cluster<M, false>(st, L);
+        } else {
+#pragma unroll
+            for (int q = 0; q < Layout<M>::acc; q++) { aB[q] = saveB[q]; aL[q] = saveL[q]; }
+#pragma unroll
+            for (int q = 0; q < Layout<M>::ev; q++) { eB[q] = sevB[q]; eL[q] = sevL[q]; }
+            st.energy[B] = eB_old;
+            st.energy[L] = eL_old;
+            atomicAdd(&st.counters[kCntReverted], 1ull);
         }
     }
     // every thread of the grid reaches this point: warp-aggregated count
@@ -479,6 +514,127 @@ __global__ void reclaim_kernel(DevState st, const int* __restrict__ items, int c
         const unsigned long long key = make_claim(epoch, cand_prio[idx], (unsigned)idx);
         if (L < st.k) atomicMin(&st.claim[L], key);
         atomicMin(&st.claim[B], key);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// relaxed step (phases without the connectivity constraint): every proposal of
+// the colour class commits at once, except that a cluster is never emptied.
+// Items of one colour are never adjacent.  The committed moves' contributions are
+// summed per cluster in 64-bit fixed point -- exact, so the atomics' order does
+// not matter -- and folded into the compensated accumulators by fx_finalize.
+// ---------------------------------------------------------------------------
+
+// item contribution j (the accumulate_item components) in FP64
+template <int M>
+ACVD_DEV double contrib(const ItemRec& it, int j) {
+    const int rowi[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
+    if (j < 3) return (double)it.w * (double)it.x[j];
+    if (j == 3) return (double)it.w;
+    if (j < 10) return (double)it.A[j - 4];
+    if (j < 13) {
+        const int c = j - 10;
+        return (double)it.A[rowi[c][0]] * it.x[0] + (double)it.A[rowi[c][1]] * it.x[1] +
+               (double)it.A[rowi[c][2]] * it.x[2];
+    }
+    if (j < 19) return (double)it.T[j - 13];
+    const int c = j - 19;
+    return (double)it.T[rowi[c][0]] * it.x[0] + (double)it.T[rowi[c][1]] * it.x[1] + (double)it.T[rowi[c][2]] * it.x[2];
+}
+
+__global__ void relaxed_count_kernel(DevState st, const int* __restrict__ items, int color,
+                                     const int* __restrict__ cand_dest) {
+    const unsigned n = st.cand_count[color];
+    for (unsigned j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        const int L = st.label[items[st.cand_list[j]]];
+        if (L < st.k) atomicAdd(&st.out_cnt[L], 1);
+    }
+}
+
+template <int M>
+__global__ void relaxed_commit_kernel(DevState st, const int* __restrict__ items, int color,
+                                      const int* __restrict__ cand_dest) {
+    constexpr int NA = Layout<M>::acc;
+    const unsigned n = st.cand_count[color];
+    unsigned won = 0;
+    const int now = st.sweep->sweep;
+    for (unsigned j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        const int idx = st.cand_list[j];
+        const int i = items[idx];
+        const int B = cand_dest[idx];
+        const int L = st.label[i];
+        // sizes are untouched until fx_finalize: a cluster whose every member would
+        // leave keeps them all
+        if (L < st.k && st.size[L] - st.out_cnt[L] < 1) continue;
+        won++;
+        ItemRec it;
+        load_item<M>(st, i, it);
+        st.label[i] = B;
+        atomicAdd(&st.in_done[B], 1);
+        st.stamp[B] = now;
+        long long* dB = st.fx_delta + (int64_t)B * NA;
+#pragma unroll
+        for (int q = 0; q < NA; q++) {
+            const long long v = __double2ll_rn(contrib<M>(it, q) * st.fx_scale[q]);
+            atomicAdd((unsigned long long*)&dB[q], (unsigned long long)v);
+        }
+        if (L < st.k) {
+            atomicAdd(&st.out_done[L], 1);
+            st.stamp[L] = now;
+            long long* dL = st.fx_delta + (int64_t)L * NA;
+#pragma unroll
+            for (int q = 0; q < NA; q++) {
+                const long long v = __double2ll_rn(contrib<M>(it, q) * st.fx_scale[q]);
+                atomicAdd((unsigned long long*)&dL[q], (unsigned long long)(-v));
+            }
+        }
+    }
+    warp_count(&st.counters[kCntMoves], won);
+}
+
+template <int M>
+__global__ void fx_finalize_kernel(DevState st) {
+    constexpr int NA = Layout<M>::acc;
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= st.k) return;
+    const int in = st.in_done[k], out = st.out_done[k];
+    st.out_cnt[k] = 0;
+    if (in == 0 && out == 0) return;
+    st.in_done[k] = 0;
+    st.out_done[k] = 0;
+    st.size[k] += in - out;
+    df* a = st.acc + k * NA;
+    long long* d = st.fx_delta + k * NA;
+#pragma unroll
+    for (int q = 0; q < NA; q++) {
+        const double v = (double)d[q] / st.fx_scale[q];
+        d[q] = 0;
+        a[q] = df_add(a[q], df_from_d(v));
+    }
+    update_cluster<M, false>(st, (int)k);
+}
+
+// per accumulator component: the largest |contribution| over the items (as float
+// bits, monotone for non-negative values), from which the fixed-point scales follow
+template <int M>
+__global__ void fx_maxabs_kernel(DevState st, unsigned* __restrict__ maxbits) {
+    constexpr int NA = Layout<M>::acc;
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    float mx[NA];
+#pragma unroll
+    for (int q = 0; q < NA; q++) mx[q] = 0.f;
+    if (i < st.n) {
+        ItemRec it;
+        load_item<M>(st, (int)i, it);
+#pragma unroll
+        for (int q = 0; q < NA; q++) mx[q] = (float)fabs(contrib<M>(it, q));
+    }
+#pragma unroll
+    for (int q = 0; q < NA; q++) {
+        float v = mx[q];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(kFull, v, o));
+        if ((threadIdx.x & 31) == 0) atomicMax(&maxbits[q], __float_as_uint(v));
     }
 }
 
@@ -740,9 +896,10 @@ static inline unsigned nblk(int64_t n, int b = 256) { return (unsigned)((n + b -
     } while (0)
 
 cudaError_t launch_eval(int metric, const DevState& st, const int* items, int64_t count, int color,
-                        int* cand_dest, unsigned* cand_prio, cudaStream_t s) {
+                        int* cand_dest, unsigned* cand_prio, bool claims, cudaStream_t s) {
     if (count == 0) return cudaSuccess;
-    ACVD_DISPATCH(metric, eval_kernel, nblk(count), 256, s, st, items, count, color, cand_dest, cand_prio);
+    ACVD_DISPATCH(metric, eval_kernel, nblk(count), 256, s, st, items, count, color, cand_dest, cand_prio,
+                  claims ? 1 : 0);
     return cudaGetLastError();
 }
 
@@ -767,6 +924,22 @@ cudaError_t launch_reclaim(const DevState& st, const int* items, int64_t count, 
     if (count == 0) return cudaSuccess;
     ++g_launches;
     reclaim_kernel<<<list_grid(count), 256, 0, s>>>(st, items, color, round, cand_dest, cand_prio);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_relaxed_step(int metric, const DevState& st, const int* items, int64_t count, int color,
+                                const int* cand_dest, cudaStream_t s) {
+    if (count == 0) return cudaSuccess;
+    ++g_launches;
+    relaxed_count_kernel<<<list_grid(count), 256, 0, s>>>(st, items, color, cand_dest);
+    ACVD_DISPATCH(metric, relaxed_commit_kernel, list_grid(count), 256, s, st, items, color, cand_dest);
+    ACVD_DISPATCH(metric, fx_finalize_kernel, nblk(st.k), 256, s, st);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fx_scale(int metric, const DevState& st, unsigned* maxbits, cudaStream_t s) {
+    if (st.n == 0) return cudaSuccess;
+    ACVD_DISPATCH(metric, fx_maxabs_kernel, nblk(st.n), 256, s, st, maxbits);
     return cudaGetLastError();
 }
 

@@ -73,6 +73,11 @@ struct acvd_ctx {
     DBuf<int> label, size, stamp, evald;
     DBuf<unsigned long long> claim;
     DBuf<SweepState> dsweep;
+    // relaxed steps
+    DBuf<long long> fx_delta;
+    DBuf<double> fx_scale;
+    DBuf<int> out_cnt, in_done, out_done;
+    bool use_relaxed = true;       // ACVD_RELAXED=0 turns relaxed steps off
     DBuf<df> acc;
     DBuf<float4> ev;
     DBuf<double> energy;
@@ -96,7 +101,8 @@ struct acvd_ctx {
     std::vector<cudaEvent_t> ev_eval;
     bool timing_broken = false;    // event timing unavailable on this device / driver
     int match_rounds = 1;          // claim/commit rounds per colour step (ACVD_MATCH_ROUNDS, up to kRounds)
-    int64_t sweep_kernels = 0;     // kernels in one sweep
+    int64_t sweep_kernels = 0;     // kernels in the sweep last enqueued
+    int64_t exact_kernels = 0, relaxed_kernels = 0;
     DBuf<int> label_init;          // the assignment given to acvd_set_labels (for acvd_rewind)
 
     DevState state() {
@@ -124,11 +130,19 @@ struct acvd_ctx {
         st.evald = evald.p;
         st.cand_list = cand_list.p;
         st.cand_count = cand_count.p;
+        st.fx_delta = fx_delta.p;
+        st.fx_scale = fx_scale.p;
+        st.out_cnt = out_cnt.p;
+        st.in_done = in_done.p;
+        st.out_done = out_done.p;
         return st;
     }
+    cudaGraphExec_t relaxed_exec = nullptr;
     void drop_graph() {
         if (sweep_exec) cudaGraphExecDestroy(sweep_exec);
         sweep_exec = nullptr;
+        if (relaxed_exec) cudaGraphExecDestroy(relaxed_exec);
+        relaxed_exec = nullptr;
     }
     void drop_events() {
         for (cudaEvent_t e : ev_eval) cudaEventDestroy(e);
@@ -264,6 +278,7 @@ acvd_ctx* acvd_create(const acvd_opts* opts) {
     if (opts) ctx->opts = *opts;
     else acvd_default_opts(&ctx->opts);
     if (const char* c = std::getenv("ACVD_SWEEP_COLORS")) ctx->sweep_by_color = std::atoi(c) != 0;
+    if (const char* c = std::getenv("ACVD_RELAXED")) ctx->use_relaxed = std::atoi(c) != 0;
     if (const char* r = std::getenv("ACVD_MATCH_ROUNDS")) {
         const int v = std::atoi(r);
         if (v >= 1 && v <= kRounds) ctx->match_rounds = v;
@@ -393,6 +408,26 @@ int acvd_set_metric(acvd_ctx* ctx, int metric, const double* indicator, const fl
     const double ratio = metric == kQEM ? 10000.0 : 100000.0;
     CK(launch_finish_items(metric, nv, ctx->xyz.p, wd.p, varea.p, wsum.p, ratio, pd.p, ctx->xw.p, ctx->ta.p,
                            ctx->tb.p, ctx->s));
+    // fixed-point scales of the relaxed steps: any sum of up to N contributions of
+    // component j stays below 2^62 units
+    {
+        DBuf<unsigned> maxbits;
+        CK(maxbits.resize(32));
+        CK(cudaMemsetAsync(maxbits.p, 0, 32 * sizeof(unsigned), ctx->s));
+        DevState st = ctx->state();
+        CK(launch_fx_scale(metric, st, maxbits.p, ctx->s));
+        unsigned hb[32];
+        CK(cudaMemcpyAsync(hb, maxbits.p, sizeof hb, cudaMemcpyDeviceToHost, ctx->s));
+        CK(cudaStreamSynchronize(ctx->s));
+        double sc[32];
+        for (int q = 0; q < 32; q++) {
+            float mx;
+            std::memcpy(&mx, &hb[q], sizeof mx);
+            sc[q] = mx > 0.f ? std::ldexp(1.0, 62) / ((double)nv * (double)mx * 1.0000001) : 1.0;
+        }
+        CK(ctx->fx_scale.resize(32));
+        CK(cudaMemcpyAsync(ctx->fx_scale.p, sc, sizeof sc, cudaMemcpyHostToDevice, ctx->s));
+    }
     CK(cudaStreamSynchronize(ctx->s));
     ctx->ready_metric = true;
     return ACVD_OK;
@@ -424,6 +459,10 @@ int acvd_set_labels(acvd_ctx* ctx, int32_t k, const int32_t* labels) {
     CK(ctx->label.resize(ctx->nV));
     CK(ctx->size.resize(k + 1));
     CK(ctx->stamp.resize(k + 1));
+    CK(ctx->fx_delta.resize((size_t)(k + 1) * acc_stride(kAniso)));
+    CK(ctx->out_cnt.resize(k + 1));
+    CK(ctx->in_done.resize(k + 1));
+    CK(ctx->out_done.resize(k + 1));
     CK(ctx->claim.resize(k + 1));
     CK(ctx->acc.resize((size_t)(k + 1) * acc_stride(kAniso)));
     CK(ctx->ev.resize((size_t)(k + 1) * ev_stride(kAniso)));
@@ -530,7 +569,7 @@ static int clean(acvd_ctx* ctx, int* n_disconnected) {
 // one sweep: every colour class once (eval + apply per class).  With kernel
 // timing on, an event pair per colour brackets the evaluation kernel; the pairs
 // are recorded inside the captured graph and read after the sweep's sync.
-static int enqueue_sweep(acvd_ctx* ctx, bool timing) {
+static int enqueue_sweep(acvd_ctx* ctx, bool timing, bool relaxed) {
     DevState st = ctx->state();
     CK(cudaMemsetAsync(ctx->counters.p + kCntMoves, 0, sizeof(unsigned long long), ctx->s));
     CK(launch_begin_sweep(st, ctx->nclasses, ctx->s));
@@ -539,11 +578,16 @@ static int enqueue_sweep(acvd_ctx* ctx, bool timing) {
         const int* items = ctx->sweep_items + ctx->sweep_off[c];
         const int64_t cnt = ctx->sweep_off[c + 1] - ctx->sweep_off[c];
         if (cnt == 0) continue;
-        CK(cudaMemsetAsync(ctx->claim.p, 0xff, (ctx->K + 1) * sizeof(unsigned long long), ctx->s));
+        if (!relaxed) CK(cudaMemsetAsync(ctx->claim.p, 0xff, (ctx->K + 1) * sizeof(unsigned long long), ctx->s));
         // cudaEventRecordExternal makes the records real graph nodes when captured
         if (timing) CK(cudaEventRecordWithFlags(ctx->ev_eval[2 * c], ctx->s, cudaEventRecordExternal));
-        CK(launch_eval(ctx->metric, st, items, cnt, c, ctx->cand_dest.p, ctx->cand_prio.p, ctx->s));
+        CK(launch_eval(ctx->metric, st, items, cnt, c, ctx->cand_dest.p, ctx->cand_prio.p, !relaxed, ctx->s));
         if (timing) CK(cudaEventRecordWithFlags(ctx->ev_eval[2 * c + 1], ctx->s, cudaEventRecordExternal));
+        if (relaxed) {
+            CK(launch_relaxed_step(ctx->metric, st, items, cnt, c, ctx->cand_dest.p, ctx->s));
+            kernels += 4;
+            continue;
+        }
         CK(launch_apply(ctx->metric, st, items, cnt, c, 0, ctx->cand_dest.p, ctx->cand_prio.p, ctx->s));
         kernels += 2;
         for (int r = 1; r < ctx->match_rounds; r++) {
@@ -556,7 +600,8 @@ static int enqueue_sweep(acvd_ctx* ctx, bool timing) {
     return ACVD_OK;
 }
 
-static int run_sweep(acvd_ctx* ctx, bool timing, double* eval_ms, int* eval_launches, int64_t* moves) {
+static int run_sweep(acvd_ctx* ctx, bool timing, bool relaxed, double* eval_ms, int* eval_launches,
+                     int64_t* moves) {
     if (timing && (int)ctx->ev_eval.size() != 2 * ctx->nclasses) {
         ctx->drop_graph();
         ctx->drop_events();
@@ -564,22 +609,25 @@ static int run_sweep(acvd_ctx* ctx, bool timing, double* eval_ms, int* eval_laun
         for (auto& e : ctx->ev_eval) CK(cudaEventCreate(&e));
     }
     if (ctx->opts.use_graphs) {
-        if (!ctx->sweep_exec) {
+        cudaGraphExec_t& exec = relaxed ? ctx->relaxed_exec : ctx->sweep_exec;
+        int64_t& kern = relaxed ? ctx->relaxed_kernels : ctx->exact_kernels;
+        if (!exec) {
             cudaGraph_t g;
             const long long before = g_launches;
             CK(cudaStreamBeginCapture(ctx->s, cudaStreamCaptureModeThreadLocal));
-            int r = enqueue_sweep(ctx, timing);
+            int r = enqueue_sweep(ctx, timing, relaxed);
             cudaError_t e = cudaStreamEndCapture(ctx->s, &g);
             g_launches = before;
             if (r) return r;
             CK(e);
-            CK(cudaGraphInstantiate(&ctx->sweep_exec, g, 0));
+            CK(cudaGraphInstantiate(&exec, g, 0));
             cudaGraphDestroy(g);
+            kern = ctx->sweep_kernels;
         }
-        CK(cudaGraphLaunch(ctx->sweep_exec, ctx->s));
-        g_launches += ctx->sweep_kernels;
+        CK(cudaGraphLaunch(exec, ctx->s));
+        g_launches += kern;
     } else {
-        int r = enqueue_sweep(ctx, timing);
+        int r = enqueue_sweep(ctx, timing, relaxed);
         if (r) return r;
     }
     int r = sync_counters(ctx);
@@ -600,6 +648,15 @@ static int run_sweep(acvd_ctx* ctx, bool timing, double* eval_ms, int* eval_laun
             (*eval_launches)++;
         }
     }
+    return ACVD_OK;
+}
+
+// sum of the tracked per-cluster energies (fixed-order FP64 tree)
+static int energy_total(acvd_ctx* ctx, double* out) {
+    CK(ctx->dtmp.resize(2));
+    CK(sum_f64(ctx->energy.p, ctx->K, ctx->dtmp.p, ctx->scratch, ctx->s));
+    CK(cudaMemcpyAsync(out, ctx->dtmp.p, sizeof(double), cudaMemcpyDeviceToHost, ctx->s));
+    CK(cudaStreamSynchronize(ctx->s));
     return ACVD_OK;
 }
 
@@ -633,6 +690,13 @@ extern "C" int acvd_minimize(acvd_ctx* ctx, acvd_stats* stats) {
             break;
         }
         if ((r = set_sweep_state(ctx, 0, 0))) { status = r; break; }
+        if (cudaMemsetAsync(ctx->fx_delta.p, 0, (size_t)(ctx->K + 1) * acc_stride(kAniso) * sizeof(long long), ctx->s) ||
+            cudaMemsetAsync(ctx->out_cnt.p, 0, (ctx->K + 1) * sizeof(int), ctx->s) ||
+            cudaMemsetAsync(ctx->in_done.p, 0, (ctx->K + 1) * sizeof(int), ctx->s) ||
+            cudaMemsetAsync(ctx->out_done.p, 0, (ctx->K + 1) * sizeof(int), ctx->s)) {
+            status = fail(ctx, ACVD_ERR_CUDA, "memset of the relaxed-step arrays failed");
+            break;
+        }
         int unassigned = 0;
         if ((r = fill_holes(ctx, &unassigned))) { status = r; break; }
         if ((r = recompute(ctx))) { status = r; break; }
@@ -640,15 +704,33 @@ extern "C" int acvd_minimize(acvd_ctx* ctx, acvd_stats* stats) {
         const int64_t early = ctx->nV - unassigned;
         int convergences = 0;
         int sweeps = 0;
+        // relaxed sweeps while the connectivity constraint is off; back to exact
+        // claims for the rest of a phase as soon as a relaxed sweep raises the energy
+        bool relaxed_ok = ctx->use_relaxed;
+        double e_prev = 0.0;
+        bool have_prev = false;
+        if (relaxed_ok && (r = energy_total(ctx, &e_prev))) { status = r; break; }
+        have_prev = relaxed_ok;
         for (;;) {
             int64_t mods = 0;
-            if ((r = run_sweep(ctx, timing, &local.eval_ms, &local.eval_launches, &mods))) { status = r; break; }
+            const bool relaxed = relaxed_ok && !ctx->flags.connexity;
+            if ((r = run_sweep(ctx, timing, relaxed, &local.eval_ms, &local.eval_launches, &mods))) { status = r; break; }
+            if (relaxed) {
+                local.relaxed_sweeps++;
+                double e_now = 0.0;
+                if ((r = energy_total(ctx, &e_now))) { status = r; break; }
+                if (have_prev && !(e_now < e_prev)) relaxed_ok = false;
+                e_prev = e_now;
+                have_prev = true;
+            }
             sweeps++;
             local.moves += mods;
             if (std::getenv("ACVD_TRACE"))
-                std::fprintf(stderr, "acvd sweep %d moves %lld cand %llu boundary %llu targets %llu conv %d flags %d%d\n",
+                std::fprintf(stderr,
+                             "acvd sweep %d moves %lld cand %llu boundary %llu targets %llu reverted %llu conv %d flags %d%d\n",
                              sweeps, (long long)mods, ctx->h_counters[kCntCand], ctx->h_counters[kCntBoundary],
-                             ctx->h_counters[kCntTargets], convergences, ctx->flags.constrained, ctx->flags.connexity);
+                             ctx->h_counters[kCntTargets], ctx->h_counters[kCntReverted], convergences,
+                             ctx->flags.constrained, ctx->flags.connexity);
             if (mods == 0 || sweeps > ctx->opts.max_loops || (mods <= early / 1000 && convergences <= 1)) {
                 bool flags_changed = false;
                 if (ctx->unconstrained && convergences == 0 && ctx->metric == kQEM) {
@@ -670,6 +752,12 @@ extern "C" int acvd_minimize(acvd_ctx* ctx, acvd_stats* stats) {
                 if ((r = recompute(ctx))) { status = r; break; }
                 // SetAllClustersToModified (:822): every item is evaluated again
                 if ((r = set_sweep_state(ctx, sweeps, sweeps))) { status = r; break; }
+                relaxed_ok = ctx->use_relaxed;
+                have_prev = false;
+                if (relaxed_ok && !ctx->flags.connexity) {
+                    if ((r = energy_total(ctx, &e_prev))) { status = r; break; }
+                    have_prev = true;
+                }
                 if (disc == 0 && mods == 0) break;
                 // MaxNumberOfLoops ends the minimisation like a convergence (:803-810)
                 if (sweeps >= ctx->opts.max_loops) { local.hit_loop_cap = 1; break; }
@@ -694,6 +782,7 @@ extern "C" int acvd_minimize(acvd_ctx* ctx, acvd_stats* stats) {
     local.visited = (int64_t)ctx->h_counters[kCntVisited];
     local.slots = (int64_t)ctx->h_counters[kCntSlots];
     local.kernel_launches = g_launches - launches0;
+    local.reverted = (int64_t)ctx->h_counters[kCntReverted];
     {
         // algorithmic bytes of the evaluation kernels: per visited item its colour-list
         // entry, ring bounds and label; per ring slot the neighbour id and label; per

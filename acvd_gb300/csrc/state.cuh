@@ -62,6 +62,7 @@ enum Counter {
     kCntError = 7,       // device-side check failures
     kCntDisconnected = 8,
     kCntAssigned = 9,
+    kCntReverted = 10,   // commits undone because the pair's energy did not decrease
     kNumCounters = 16
 };
 
@@ -97,6 +98,13 @@ struct DevState {
     int* evald;            // per item: sweep of its last evaluation without a proposal (-1: none)
     int* cand_list;        // compact list of proposals (colour-list positions) of the current step
     unsigned* cand_count;  // per colour: number of proposals
+    // relaxed steps: per cluster, exact fixed-point sums of the committed moves'
+    // contributions (order-independent, hence deterministic with atomics)
+    long long* fx_delta;   // K x acc stride
+    const double* fx_scale;  // per accumulator component: fixed-point units per unit
+    int* out_cnt;          // proposals leaving the cluster in this step
+    int* in_done;          // committed moves into the cluster
+    int* out_done;         // committed moves out of the cluster
 };
 
 // ---- items / topology (topology.cu) ----
@@ -118,8 +126,11 @@ cudaError_t launch_finish_items(int metric, int64_t nv, const double* xyz, const
 
 // ---- clustering (cluster.cu) ----
 cudaError_t launch_begin_sweep(const DevState& st, int ncolors, cudaStream_t s);
+cudaError_t launch_relaxed_step(int metric, const DevState& st, const int* items, int64_t count, int color,
+                                const int* cand_dest, cudaStream_t s);
+cudaError_t launch_fx_scale(int metric, const DevState& st, unsigned* maxbits, cudaStream_t s);
 cudaError_t launch_eval(int metric, const DevState& st, const int* items, int64_t count, int color,
-                        int* cand_dest, unsigned* cand_prio, cudaStream_t s);
+                        int* cand_dest, unsigned* cand_prio, bool claims, cudaStream_t s);
 cudaError_t launch_apply(int metric, const DevState& st, const int* items, int64_t count, int color, int round,
                          int* cand_dest, const unsigned* cand_prio, cudaStream_t s);
 cudaError_t launch_reclaim(const DevState& st, const int* items, int64_t count, int color, int round,

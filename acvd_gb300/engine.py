@@ -37,7 +37,8 @@ class Stats(ctypes.Structure):
                 ("targets", ctypes.c_int64), ("visited", ctypes.c_int64), ("slots", ctypes.c_int64),
                 ("disconnected", ctypes.c_int), ("unassigned", ctypes.c_int), ("device_ms", ctypes.c_double),
                 ("eval_ms", ctypes.c_double), ("eval_launches", ctypes.c_int), ("energy", ctypes.c_double),
-                ("eval_bytes", ctypes.c_int64), ("kernel_launches", ctypes.c_int64), ("hit_loop_cap", ctypes.c_int)]
+                ("eval_bytes", ctypes.c_int64), ("kernel_launches", ctypes.c_int64), ("hit_loop_cap", ctypes.c_int),
+                ("reverted", ctypes.c_int64), ("relaxed_sweeps", ctypes.c_int)]
 
     def as_dict(self) -> dict:
         return {name: getattr(self, name) for name, _ in self._fields_}

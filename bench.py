@@ -220,7 +220,7 @@ def run_gpu_arm(args):
 
     step_ms = []
     tot = {"eval_ms": 0.0, "eval_bytes": 0, "eval_launches": 0, "kernel_launches": 0, "sweeps": 0, "moves": 0,
-           "hit_loop_cap": 0}
+           "hit_loop_cap": 0, "reverted": 0, "relaxed_sweeps": 0}
     with ClockSampler(device) as clk:
         for _ in range(args.steps):
             with torch.cuda.stream(stream):
@@ -342,6 +342,8 @@ def run_gpu_arm(args):
         "sweeps_per_step": tot["sweeps"] / max(1, args.steps),
         "moves_per_step": tot["moves"] / max(1, args.steps),
         "hit_loop_cap": bool(tot["hit_loop_cap"]),
+        "reverted_per_step": tot["reverted"] / max(1, args.steps),
+        "relaxed_sweeps_per_step": tot["relaxed_sweeps"] / max(1, args.steps),
         "energy": energy,
         "clocks": clk.summary(),
     }

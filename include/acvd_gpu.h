@@ -69,6 +69,8 @@ typedef struct acvd_stats {
     int64_t eval_bytes;       /* algorithmic bytes of all evaluation kernels (counted on device) */
     int64_t kernel_launches;  /* kernels launched by this call */
     int hit_loop_cap;         /* 1 if max_loops ended the minimisation (the reference just stops there too) */
+    int64_t reverted;         /* commits undone because the pair's tracked energy did not decrease */
+    int relaxed_sweeps;       /* sweeps run in relaxed (multi-move) mode */
 } acvd_stats;
 
 /* Defaults: device 0, graphs on, the reference's loop caps. */
