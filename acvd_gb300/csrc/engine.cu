@@ -63,6 +63,11 @@ struct acvd_ctx {
     int nclasses = 0;
     DBuf<unsigned> cand_prio, cand_count;
 
+    // batch of meshes packed in one CSR (vertex and cluster offsets per mesh)
+    int nmesh = 0;
+    std::vector<int64_t> h_voff, h_koff;
+    DBuf<int64_t> v_off, k_off;
+
     // items
     int metric = -1;
     DBuf<float4> xw, qa, ta;
@@ -325,6 +330,7 @@ int acvd_set_mesh(acvd_ctx* ctx, int64_t n_vertices, const double* xyz, int64_t 
     CK(cudaSetDevice(ctx->opts.device));
     ctx->drop_graph();
     ctx->ready_mesh = ctx->ready_metric = ctx->ready_labels = false;
+    ctx->nmesh = 0;
     ctx->nV = n_vertices;
     ctx->nF = n_faces;
     ctx->nE = n_edges;
@@ -404,10 +410,17 @@ int acvd_set_metric(acvd_ctx* ctx, int metric, const double* indicator, const fl
     }
     CK(launch_vertex_items(metric, nv, ctx->xyz.p, vrow.p, v1.p, farea.p, fnorm.p, use_ind ? ind.p : nullptr,
                            gradation, wd.p, varea.p, ctx->qa.p, ctx->qb.p, ctx->s));
-    CK(sum_f64(wd.p, nv, wsum.p, ctx->scratch, ctx->s));
     const double ratio = metric == kQEM ? 10000.0 : 100000.0;
-    CK(launch_finish_items(metric, nv, ctx->xyz.p, wd.p, varea.p, wsum.p, ratio, pd.p, ctx->xw.p, ctx->ta.p,
-                           ctx->tb.p, ctx->s));
+    if (ctx->nmesh > 0) {
+        CK(wsum.resize(ctx->nmesh));
+        CK(launch_mesh_sums(wd.p, ctx->v_off.p, ctx->nmesh, wsum.p, ctx->s));
+        CK(launch_finish_items(metric, nv, ctx->xyz.p, wd.p, varea.p, wsum.p, ctx->v_off.p, ctx->nmesh, ratio, pd.p,
+                               ctx->xw.p, ctx->ta.p, ctx->tb.p, ctx->s));
+    } else {
+        CK(sum_f64(wd.p, nv, wsum.p, ctx->scratch, ctx->s));
+        CK(launch_finish_items(metric, nv, ctx->xyz.p, wd.p, varea.p, wsum.p, nullptr, 0, ratio, pd.p, ctx->xw.p,
+                               ctx->ta.p, ctx->tb.p, ctx->s));
+    }
     // fixed-point scales of the relaxed steps: any sum of up to N contributions of
     // component j stays below 2^62 units
     {
@@ -430,6 +443,34 @@ int acvd_set_metric(acvd_ctx* ctx, int metric, const double* indicator, const fl
     }
     CK(cudaStreamSynchronize(ctx->s));
     ctx->ready_metric = true;
+    return ACVD_OK;
+}
+
+int acvd_set_batch(acvd_ctx* ctx, int n_mesh, const int64_t* vertex_offsets, const int32_t* cluster_offsets) {
+    if (!ctx) return ACVD_ERR_ARG;
+    if (!ctx->ready_mesh) return fail(ctx, ACVD_ERR_ARG, "acvd_set_batch before acvd_set_mesh");
+    if (n_mesh < 0 || (n_mesh > 0 && (!vertex_offsets || !cluster_offsets)))
+        return fail(ctx, ACVD_ERR_ARG, "acvd_set_batch: bad offsets");
+    CK(cudaSetDevice(ctx->opts.device));
+    ctx->drop_graph();
+    ctx->ready_metric = ctx->ready_labels = false;
+    ctx->nmesh = n_mesh;
+    ctx->h_voff.assign(vertex_offsets, vertex_offsets + (n_mesh ? n_mesh + 1 : 0));
+    ctx->h_koff.clear();
+    for (int m = 0; m <= n_mesh && n_mesh > 0; m++) ctx->h_koff.push_back(cluster_offsets[m]);
+    if (n_mesh == 0) return ACVD_OK;
+    if (ctx->h_voff[0] != 0 || ctx->h_voff[n_mesh] != ctx->nV)
+        return fail(ctx, ACVD_ERR_ARG, "acvd_set_batch: vertex offsets must run from 0 to n_vertices");
+    for (int m = 0; m < n_mesh; m++)
+        if (ctx->h_voff[m + 1] <= ctx->h_voff[m] || ctx->h_koff[m + 1] <= ctx->h_koff[m] || ctx->h_koff[0] != 0)
+            return fail(ctx, ACVD_ERR_ARG, "acvd_set_batch: offsets must increase from 0");
+    CK(ctx->v_off.resize(n_mesh + 1));
+    CK(ctx->k_off.resize(n_mesh + 1));
+    CK(cudaMemcpyAsync(ctx->v_off.p, ctx->h_voff.data(), (n_mesh + 1) * sizeof(int64_t), cudaMemcpyHostToDevice,
+                       ctx->s));
+    CK(cudaMemcpyAsync(ctx->k_off.p, ctx->h_koff.data(), (n_mesh + 1) * sizeof(int64_t), cudaMemcpyHostToDevice,
+                       ctx->s));
+    CK(cudaStreamSynchronize(ctx->s));
     return ACVD_OK;
 }
 
@@ -857,6 +898,23 @@ extern "C" int acvd_get_clusters(acvd_ctx* ctx, int32_t* sizes, double* S, doubl
                 q[4] = d(a[7]); q[5] = d(a[8]); q[6] = -d(a[11]); q[7] = d(a[9]); q[8] = -d(a[12]);
             }
         }
+    }
+    return ACVD_OK;
+}
+
+extern "C" int acvd_get_mesh_energies(acvd_ctx* ctx, double* energies) {
+    if (!ctx || !energies) return ACVD_ERR_ARG;
+    if (ctx->nmesh == 0) return fail(ctx, ACVD_ERR_ARG, "no batch set");
+    double tot = 0.0;
+    int r = acvd_get_clusters(ctx, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, &tot);
+    if (r) return r;
+    // per-mesh totals in the same fixed order as the global one
+    for (int m = 0; m < ctx->nmesh; m++) {
+        const int64_t a = ctx->h_koff[m], b = ctx->h_koff[m + 1];
+        CK(ctx->dtmp.resize(2));
+        CK(sum_f64(ctx->energy.p + a, b - a, ctx->dtmp.p, ctx->scratch, ctx->s));
+        CK(cudaMemcpyAsync(&energies[m], ctx->dtmp.p, sizeof(double), cudaMemcpyDeviceToHost, ctx->s));
+        CK(cudaStreamSynchronize(ctx->s));
     }
     return ACVD_OK;
 }

@@ -120,9 +120,10 @@ cudaError_t launch_vertex_items(int metric, int64_t nv, const double* xyz, const
                                 const uint32_t* vf_face, const double* farea, const double* fnorm,
                                 const double* indicator, double gradation, double* wd, double* varea,
                                 float4* qa, float2* qb, cudaStream_t s);
+cudaError_t launch_mesh_sums(const double* wd, const int64_t* v_off, int nmesh, double* out, cudaStream_t s);
 cudaError_t launch_finish_items(int metric, int64_t nv, const double* xyz, const double* wd, const double* vrea,
-                                const double* wsum, double ratio, const float* pdirs, float4* xw, float4* ta,
-                                float2* tb, cudaStream_t s);
+                                const double* wsum, const int64_t* v_off, int nmesh, double ratio, const float* pdirs,
+                                float4* xw, float4* ta, float2* tb, cudaStream_t s);
 
 // ---- clustering (cluster.cu) ----
 cudaError_t launch_begin_sweep(const DevState& st, int ncolors, cudaStream_t s);

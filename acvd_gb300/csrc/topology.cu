@@ -210,13 +210,56 @@ cudaError_t launch_vertex_items(int metric, int64_t nv, const double* xyz, const
 // area * (d1 d1^T + d2 d2^T) from the principal directions d1 = pd[0..2],
 // d2 = pd[3..5], with entry (1,1) built from pd[1]^2 + pd[5]^2 as the reference
 // builds it (vtkQuadricAnisotropicMetricForClustering.h:442-446).
+// Batched meshes: the mesh of vertex v (vertex offsets v_off[0..nmesh]).
+__device__ __forceinline__ int mesh_of(const int64_t* v_off, int nmesh, int64_t v) {
+    int lo = 0, hi = nmesh - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (v_off[mid] <= v) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+// one block per mesh: fixed-order FP64 sum of the weights of its vertex range
+__global__ void mesh_sums_kernel(const double* __restrict__ wd, const int64_t* __restrict__ v_off,
+                                 double* __restrict__ out) {
+    __shared__ double sh[256];
+    const int m = blockIdx.x;
+    const int64_t a = v_off[m], b = v_off[m + 1];
+    double acc = 0.0;
+    for (int64_t v = a + threadIdx.x; v < b; v += 256) acc += wd[v];
+    sh[threadIdx.x] = acc;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[m] = sh[0];
+}
+
+cudaError_t launch_mesh_sums(const double* wd, const int64_t* v_off, int nmesh, double* out, cudaStream_t s) {
+    if (nmesh == 0) return cudaSuccess;
+    ++g_launches;
+    mesh_sums_kernel<<<nmesh, 256, 0, s>>>(wd, v_off, out);
+    return cudaGetLastError();
+}
+
 __global__ void finish_items_kernel(int metric, int64_t nv, const double* __restrict__ xyz,
                                     const double* __restrict__ wd, const double* __restrict__ varea,
-                                    const double* __restrict__ wsum, double ratio, const float* __restrict__ pd,
+                                    const double* __restrict__ wsum, const int64_t* __restrict__ v_off, int nmesh,
+                                    double ratio, const float* __restrict__ pd,
                                     float4* __restrict__ xw, float4* __restrict__ ta, float2* __restrict__ tb) {
     const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= nv) return;
-    const double mean = *wsum / (double)nv;
+    // the mean is taken over the vertex's own mesh (every mesh of a batch is clamped
+    // as if it were clustered alone)
+    double mean;
+    if (v_off) {
+        const int m = mesh_of(v_off, nmesh, v);
+        mean = wsum[m] / (double)(v_off[m + 1] - v_off[m]);
+    } else {
+        mean = *wsum / (double)nv;
+    }
     const double lo = mean / ratio, hi = mean * ratio;
     double w = wd[v];
     if (w > hi) w = hi;
@@ -238,12 +281,12 @@ __global__ void finish_items_kernel(int metric, int64_t nv, const double* __rest
 }
 
 cudaError_t launch_finish_items(int metric, int64_t nv, const double* xyz, const double* wd, const double* varea,
-                                const double* wsum, double ratio, const float* pdirs, float4* xw, float4* ta,
-                                float2* tb, cudaStream_t s) {
+                                const double* wsum, const int64_t* v_off, int nmesh, double ratio, const float* pdirs,
+                                float4* xw, float4* ta, float2* tb, cudaStream_t s) {
     if (nv == 0) return cudaSuccess;
     ++g_launches;
-    finish_items_kernel<<<(unsigned)((nv + 255) / 256), 256, 0, s>>>(metric, nv, xyz, wd, varea, wsum, ratio,
-                                                                      pdirs, xw, ta, tb);
+    finish_items_kernel<<<(unsigned)((nv + 255) / 256), 256, 0, s>>>(metric, nv, xyz, wd, varea, wsum, v_off, nmesh,
+                                                                      ratio, pdirs, xw, ta, tb);
     return cudaGetLastError();
 }
 

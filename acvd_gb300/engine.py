@@ -83,6 +83,8 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         "acvd_set_labels": (ctypes.c_int, [_P, ctypes.c_int32, _P]),
         "acvd_minimize": (ctypes.c_int, [_P, ctypes.POINTER(Stats)]),
         "acvd_rewind": (ctypes.c_int, [_P]),
+        "acvd_set_batch": (ctypes.c_int, [_P, ctypes.c_int, _P, _P]),
+        "acvd_get_mesh_energies": (ctypes.c_int, [_P, _P]),
         "acvd_get_labels": (ctypes.c_int, [_P, _P]),
         "acvd_get_clusters": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P, _P]),
         "acvd_get_boundary_edges": (ctypes.c_int, [_P, _P, ctypes.POINTER(_i64)]),
@@ -218,6 +220,17 @@ class Engine:
         self.metric = metric
         self._ck(self._lib.acvd_set_metric(self.ctx, METRICS[metric], _ptr(ind), _ptr(pd), float(gradation)),
                  "acvd_set_metric")
+
+    def set_batch(self, vertex_offsets, cluster_offsets):
+        vo = np.ascontiguousarray(vertex_offsets, dtype=np.int64)
+        ko = np.ascontiguousarray(cluster_offsets, dtype=np.int32)
+        self.nmesh = vo.shape[0] - 1
+        self._ck(self._lib.acvd_set_batch(self.ctx, self.nmesh, _ptr(vo), _ptr(ko)), "acvd_set_batch")
+
+    def mesh_energies(self) -> np.ndarray:
+        out = np.empty(self.nmesh, dtype=np.float64)
+        self._ck(self._lib.acvd_get_mesh_energies(self.ctx, _ptr(out)), "acvd_get_mesh_energies")
+        return out
 
     def set_level(self, level: int):
         self._ck(self._lib.acvd_set_quadrics_optimization_level(self.ctx, int(level)))

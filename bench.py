@@ -52,6 +52,14 @@ WORKLOADS = {
 }
 
 
+BATCH_WORKLOADS = {
+    "batch_256_qem": dict(n_meshes=256, seed=0, metric="qem", gradation=0.0, uinit=1,
+                          desc="256 meshes (icosphere / torus / heightfield, type uniform, vertices "
+                               "log-uniform in [2,000, 500,000]), ACVDQ, K = vertices / 20 per mesh",
+                          cpu_every=16),
+}
+
+
 def _dist():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -136,6 +144,15 @@ def cpu_reference_run(m, ind, pd, w, lab0):
     return p, secs
 
 
+def evaluated_energy(w, points, faces, k, ind, pd, labels):
+    """The reference's evaluation of a final clustering (Init, labels, ReComputeStatistics
+    with the placement on); CPU and GPU clusterings are both compared through it."""
+    from oracle import oracle
+    ev = oracle.Port(w["metric"], points, faces, k, w["gradation"], ind, pd)
+    ev.evaluate(labels, 1)
+    return ev.global_energy(), ev
+
+
 def _port_job(args):
     name, = args
     m, ind, pd, w = make_workload(name)
@@ -180,6 +197,144 @@ def run_reference_arm(args):
                                        f"sequential reference algorithm restated in C++"},
             "e2e": {"value": value, "unit": "items/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "energy": energies[-1] if energies else None}
+    print(json.dumps(line), flush=True)
+
+
+def run_batch_arm(args):
+    """Batched workload: every mesh of the batch in one packed CSR, one minimisation."""
+    import torch
+    from acvd_gb300 import batch as B
+    from acvd_gb300 import engine as E
+
+    ws, rank, local = _dist()
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    device = local
+    torch.cuda.set_device(device)
+    w = BATCH_WORKLOADS[args.workload]
+    t0 = time.perf_counter()
+    b = B.synthetic_batch(w["n_meshes"], w["seed"], metric=w["metric"], gradation=w["gradation"])
+    gen_s = time.perf_counter() - t0
+    eng = E.Engine(device=device, kernel_timing=True)
+    row, col, ev = E.build_topology(b.n_points, b.faces)
+    eng.set_mesh(b.points, b.faces, row, col, ev)
+    eng.set_batch(b.v_off, b.k_off)
+    eng.set_metric(w["metric"], b.indicator, None, w["gradation"])
+    eng.set_unconstrained_initialization(w["uinit"])
+    eng.set_labels(b.k_total, b.labels0)
+    stream = torch.cuda.ExternalStream(eng.stream(), device=device)
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=f"cuda:{device}")
+    for _ in range(args.warmup):
+        eng.rewind()
+        eng.minimize()
+    torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    step_ms = []
+    tot = {"eval_ms": 0.0, "eval_bytes": 0, "eval_launches": 0, "kernel_launches": 0, "sweeps": 0, "moves": 0,
+           "relaxed_sweeps": 0}
+    with ClockSampler(device) as clk:
+        for _ in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            eng.rewind()
+            st = eng.minimize()
+            e1.record(stream)
+            e1.synchronize()
+            step_ms.append(e0.elapsed_time(e1))
+            for k in tot:
+                tot[k] += st[k]
+    ms = statistics.mean(step_ms)
+    if ws > 1:
+        t = torch.tensor([ms], device=f"cuda:{device}")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = ws * b.n_mesh / (ms / 1000.0)
+    packed = eng.labels()
+    mesh_e = eng.mesh_energies()
+    e2e = None
+    if not args.no_e2e:
+        h2d = (b.points.nbytes + b.faces.nbytes + row.nbytes + col.nbytes + ev.nbytes + b.labels0.nbytes +
+               (b.indicator.nbytes if b.indicator is not None else 0))
+        e2e_ms = []
+        eng2 = E.Engine(device=device)
+        for _ in range(max(1, args.steps)):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            eng2.set_mesh(b.points, b.faces, row, col, ev)
+            eng2.set_batch(b.v_off, b.k_off)
+            eng2.set_metric(w["metric"], b.indicator, None, w["gradation"])
+            eng2.set_unconstrained_initialization(w["uinit"])
+            eng2.set_labels(b.k_total, b.labels0)
+            eng2.minimize()
+            out = eng2.labels()
+            torch.cuda.synchronize()
+            e2e_ms.append(1000.0 * (time.perf_counter() - t0))
+        eng2.close()
+        assert np.array_equal(out, packed), "end-to-end batch run differs from the resident run"
+        e2e = {"value": ws * b.n_mesh / (statistics.mean(e2e_ms) / 1000.0), "unit": "meshes/s",
+               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(b.labels0.nbytes),
+               "ms_per_step": statistics.mean(e2e_ms)}
+    if ws > 1:
+        torch.distributed.barrier()
+    if rank != 0:
+        return
+    cpu = None
+    energy = {}
+    if not args.no_cpu_baseline:
+        from oracle import oracle
+        oracle.build(ref=False)
+        secs = 0.0
+        worst = -1e300
+        n_items = 0
+        sample = list(range(0, b.n_mesh, w["cpu_every"]))
+        for m in sample:
+            mesh = b.meshes[m]
+            k = int(b.ks[m])
+            p = oracle.Port(w["metric"], mesh.points, mesh.faces, k, w["gradation"], unconstrained_init=w["uinit"])
+            p.init(b.mesh_labels(b.labels0, m))
+            secs += p.run()
+            e_ref, _ = evaluated_energy(w, mesh.points, mesh.faces, k, None, None, p.labels())
+            e_gpu, _ = evaluated_energy(w, mesh.points, mesh.faces, k, None, None, b.mesh_labels(packed, m))
+            worst = max(worst, (e_gpu - e_ref) / abs(e_ref))
+            n_items += mesh.n_points
+        cpu = {"value": len(sample) / secs, "unit": "meshes/s", "cores": 1, "kind": "port",
+               "sample": f"every {w['cpu_every']}th mesh of the batch ({len(sample)} meshes, {n_items} vertices), "
+                         f"sequential converged solves ({secs:.2f} s)"}
+        energy = {"meshes_checked": len(sample), "worst_rel_diff_vs_reference": worst,
+                  "within_0.1pct": bool(worst <= 1e-3)}
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    peak = peaks.get("hbm_gbs", 6800.0)
+    achieved = (tot["eval_bytes"] / 1e9) / (tot["eval_ms"] / 1000.0) if tot["eval_ms"] > 0 else None
+    line = {
+        "metric": METRIC, "value": value, "unit": "meshes/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": args.workload, "description": w["desc"], "meshes": b.n_mesh, "items": b.n_points,
+                   "clusters": b.k_total, "faces": int(b.faces.shape[0]), "generation_s": gen_s,
+                   "parallelism": "replicas" if ws > 1 else "single", "l2": "flushed between timed steps (256 MB write)"},
+        "roofline": {"bound": "hbm", "kernel": "eval_kernel", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": (achieved / peak) if achieved else None,
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if "hbm_gbs" in peaks else "fallback",
+                     "traffic": None, "launches": tot["eval_launches"],
+                     "algorithmic_bytes_per_launch": tot["eval_bytes"] / max(1, tot["eval_launches"]),
+                     "avg_launch_us": 1000.0 * tot["eval_ms"] / max(1, tot["eval_launches"])},
+        "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(tot["kernel_launches"]),
+        "sweeps_per_step": tot["sweeps"] / max(1, args.steps),
+        "relaxed_sweeps_per_step": tot["relaxed_sweeps"] / max(1, args.steps),
+        "items_per_s": ws * b.n_points / (ms / 1000.0),
+        "energy": energy, "mesh_energy_total": float(np.sum(mesh_e)), "clocks": clk.summary(),
+    }
     print(json.dumps(line), flush=True)
 
 
@@ -296,11 +451,8 @@ def run_gpu_arm(args):
                   "gpu_energy_fp64_device": gpu_energy_fp64}
     elif not args.no_cpu_baseline:
         p, secs = cpu_reference_run(m, ind, pd, w, lab0)
-        e_ref = p.global_energy()
-        from oracle import oracle
-        chk = oracle.Port(w["metric"], m.points, m.faces, w["k"], w["gradation"], ind, pd)
-        chk.evaluate(lab, 1)
-        e_gpu = chk.global_energy()
+        e_ref, _ = evaluated_energy(w, m.points, m.faces, w["k"], ind, pd, p.labels())
+        e_gpu, chk = evaluated_energy(w, m.points, m.faces, w["k"], ind, pd, lab)
         connected = chk.clean() == 0
         cpu = {"value": n / secs, "unit": "items/s", "cores": 1, "kind": "port",
                "sample": f"full workload, one sequential converged solve ({secs:.2f} s)"}
@@ -356,12 +508,14 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="torus_1024x512_qem", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="torus_1024x512_qem", choices=sorted(WORKLOADS) + sorted(BATCH_WORKLOADS))
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference_arm(args)
+    elif args.workload in BATCH_WORKLOADS:
+        run_batch_arm(args)
     else:
         run_gpu_arm(args)
 

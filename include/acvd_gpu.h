@@ -128,6 +128,22 @@ int acvd_set_mesh(acvd_ctx* ctx, int64_t n_vertices, const double* xyz, int64_t 
 int acvd_set_metric(acvd_ctx* ctx, int metric, const double* indicator, const float* principal_dirs,
                     double gradation);
 
+/*
+ * Batched meshes: n_mesh independent meshes packed into the arrays given to
+ * acvd_set_mesh (vertex, face and edge ranges one after the other, ids global).
+ * vertex_offsets[n_mesh+1] delimit each mesh's vertices; cluster_offsets[n_mesh+1]
+ * each mesh's label range in [0, K).  Each mesh's weights are clamped against its
+ * own mean, as when it is clustered alone; the minimisation runs all meshes in
+ * the same sweeps (one CSR, one sweep graph).  Call after acvd_set_mesh and before
+ * acvd_set_metric; n_mesh = 0 returns to a single mesh.  Batch of
+ * DiscreteRemeshing/Examples/VolumeAnalysis.cxx:153-240, which runs one remesher
+ * per mesh on CPU threads.
+ */
+int acvd_set_batch(acvd_ctx* ctx, int n_mesh, const int64_t* vertex_offsets, const int32_t* cluster_offsets);
+
+/* Per-mesh global energies of a batch (energies[n_mesh]). */
+int acvd_get_mesh_energies(acvd_ctx* ctx, double* energies);
+
 /* Options of the reference API: SetQuadricsOptimizationLevel (default 3),
  * SetUnconstrainedInitialization (default 0). */
 int acvd_set_quadrics_optimization_level(acvd_ctx* ctx, int level);

@@ -89,6 +89,17 @@ RUNS = [
 ]
 
 
+def _evaluated(oracle_lib, metric, points, faces, k, grad, ind, pd, labels):
+    """The reference's evaluation of a final clustering: Init, load the labels,
+    ReComputeStatistics with the placement on (vtkDiscreteRemeshing.h:915-932).
+    Both the CPU run's and the GPU run's clusterings are compared through it: the
+    reference may stop at its first convergence, right after switching the
+    placement on, with cluster records still computed without it."""
+    ev = oracle_lib.Port(metric, points, faces, k, grad, ind, pd)
+    ev.evaluate(labels, 1)
+    return ev.global_energy()
+
+
 def _run_case(oracle_lib, case):
     name, metric, mk, k, grad, uinit, seeds = case
     m = mk()
@@ -99,7 +110,7 @@ def _run_case(oracle_lib, case):
     ref.init(init)
     lab0 = ref.labels()
     ref.run()
-    e_ref = ref.global_energy()
+    e_ref = _evaluated(oracle_lib, metric, m.points, m.faces, k, grad, ind, pd, ref.labels())
     e, topo = _engine(m.points, m.faces, metric, ind, pd, grad, uinit=uinit)
     e.set_labels(k, lab0)
     stats = e.minimize()
@@ -174,4 +185,31 @@ def test_error_paths():
     r.SetNumberOfClusters(500)                 # 642 < 10 * 500: would need subdivision
     with pytest.raises(acvd_gb300.AcvdError):
         r.Remesh()
+    e.close()
+
+
+def test_batched_meshes_match_individual_runs(oracle_lib):
+    """Several meshes packed in one CSR: each converges like its own CPU run."""
+    from acvd_gb300 import batch as B
+    meshes = [synth.icosphere(3, seed=1), synth.torus(40, 24, seed=2), synth.heightfield(30, seed=3),
+              synth.torus(64, 30, seed=4), synth.icosphere(4, seed=5)]
+    ks = [m.n_points // 20 for m in meshes]
+    b = B.build_batch(meshes, ks, "qem", 0.0)
+    e, stats = B.run_on_gpu(b, unconstrained_init=1)
+    packed = e.labels()
+    mesh_e = e.mesh_energies()
+    for m, mesh in enumerate(meshes):
+        lab = b.mesh_labels(packed, m)
+        k = int(ks[m])
+        assert np.all(lab < k)
+        ref = oracle_lib.Port("qem", mesh.points, mesh.faces, k, 0.0, unconstrained_init=1)
+        ref.init(b.mesh_labels(b.labels0, m))
+        ref.run()
+        e_ref = _evaluated(oracle_lib, "qem", mesh.points, mesh.faces, k, 0.0, None, None, ref.labels())
+        chk = oracle_lib.Port("qem", mesh.points, mesh.faces, k, 0.0)
+        chk.evaluate(lab, 1)
+        e_gpu = chk.global_energy()
+        assert e_gpu <= e_ref + REL_ENERGY * abs(e_ref), (m, e_gpu, e_ref)
+        assert chk.clean() == 0
+        assert abs(mesh_e[m] - e_gpu) < REL_ACC * abs(e_gpu)
     e.close()
