@@ -68,6 +68,10 @@ struct acvd_ctx {
     std::vector<int64_t> h_voff, h_koff;
     DBuf<int64_t> v_off, k_off;
 
+    // vertex -> faces (increasing face id), kept for the adjoint
+    DBuf<uint32_t> vf_row, vf_face;
+    DBuf<char> adj_work;
+
     // items
     int metric = -1;
     DBuf<float4> xw, qa, ta;
@@ -92,6 +96,7 @@ struct acvd_ctx {
     RunFlags flags{1, 0, 3, 1e-3f};
     int level = 3;
     int unconstrained = 0;
+    double gradation = 0.0;
 
     // work
     DBuf<uint32_t> wk_a, wk_b, wk_c, wk_d, wk_cnt, wk_off;
@@ -410,6 +415,11 @@ int acvd_set_metric(acvd_ctx* ctx, int metric, const double* indicator, const fl
     }
     CK(launch_vertex_items(metric, nv, ctx->xyz.p, vrow.p, v1.p, farea.p, fnorm.p, use_ind ? ind.p : nullptr,
                            gradation, wd.p, varea.p, ctx->qa.p, ctx->qb.p, ctx->s));
+    CK(ctx->vf_row.resize(nv + 1));
+    CK(ctx->vf_face.resize(3 * nf));
+    CK(cudaMemcpyAsync(ctx->vf_row.p, vrow.p, (nv + 1) * sizeof(uint32_t), cudaMemcpyDeviceToDevice, ctx->s));
+    CK(cudaMemcpyAsync(ctx->vf_face.p, v1.p, 3 * nf * sizeof(uint32_t), cudaMemcpyDeviceToDevice, ctx->s));
+    ctx->gradation = gradation;
     const double ratio = metric == kQEM ? 10000.0 : 100000.0;
     if (ctx->nmesh > 0) {
         CK(wsum.resize(ctx->nmesh));
@@ -997,5 +1007,56 @@ extern "C" int acvd_get_dual_mesh(acvd_ctx* ctx, int32_t* tris, int64_t* n_tris)
         CK(cudaMemcpyAsync(tris, out.p, 3 * (size_t)t * sizeof(int), cudaMemcpyDeviceToHost, ctx->s));
         CK(cudaStreamSynchronize(ctx->s));
     }
+    return ACVD_OK;
+}
+
+// ---------------------------------------------------------------------------
+// adjoint (fixed clustering)
+// ---------------------------------------------------------------------------
+namespace acvd {
+cudaError_t adjoint_run(const AdjState& a, int metric, int level, double thr, double ratio, double gE,
+                        const double* gC, const uint32_t* sorted, const uint32_t* off, const uint32_t* cnt,
+                        double* wsum, double* cent, double* gx, double* grho, cudaStream_t s, Scratch& scratch);
+}  // namespace acvd
+
+extern "C" int acvd_adjoint(acvd_ctx* ctx, const double* xyz, const double* rho, double gradation, double g_energy,
+                            const double* g_centroids, double* energy, double* cluster_energies, double* centroids,
+                            double* grad_xyz, double* grad_rho) {
+    if (!ctx) return ACVD_ERR_ARG;
+    if (!ctx->ready_metric || !ctx->ready_labels) return fail(ctx, ACVD_ERR_ARG, "acvd_adjoint needs metric and labels");
+    if (!xyz) return fail(ctx, ACVD_ERR_ARG, "acvd_adjoint: positions required");
+    if (ctx->metric == kAniso) return fail(ctx, ACVD_ERR_UNSUPPORTED, "adjoint of the anisotropic metric not built");
+    CK(cudaSetDevice(ctx->opts.device));
+    const int64_t nv = ctx->nV, nf = ctx->nF;
+    const int K = ctx->K;
+    // items sorted by cluster (fixed clustering)
+    DevState st = ctx->state();
+    CK(ctx->wk_a.resize(nv)); CK(ctx->wk_b.resize(nv)); CK(ctx->wk_c.resize(nv)); CK(ctx->wk_d.resize(nv));
+    CK(ctx->wk_cnt.resize(K + 1)); CK(ctx->wk_off.resize(K + 1));
+    CK(cudaMemsetAsync(ctx->wk_cnt.p, 0, (K + 1) * sizeof(uint32_t), ctx->s));
+    CK(launch_cluster_keys(st, ctx->wk_a.p, ctx->wk_b.p, ctx->wk_cnt.p, ctx->s));
+    CK(radix_sort_pairs(ctx->wk_a.p, ctx->wk_b.p, ctx->wk_c.p, ctx->wk_d.p, nv, bits_for((uint64_t)K), ctx->scratch,
+                        ctx->s));
+    CK(exclusive_scan_u32(ctx->wk_cnt.p, ctx->wk_off.p, K + 1, nullptr, ctx->scratch, ctx->s));
+    CK(ctx->adj_work.resize(adjoint_bytes(nv, nf, K) + 64));
+    AdjState a = adjoint_state(ctx->adj_work.p, nv, nf, K);
+    a.x = xyz;
+    a.rho = rho;
+    a.grad = gradation;
+    a.tri = ctx->tri.p;
+    a.label = ctx->label.p;
+    a.vf_row = ctx->vf_row.p;
+    a.vf_face = ctx->vf_face.p;
+    CK(ctx->dtmp.resize(4));
+    const double ratio = ctx->metric == kQEM ? 10000.0 : 100000.0;
+    CK(adjoint_run(a, ctx->metric, ctx->level, 1e-3, ratio, g_energy, g_centroids, ctx->wk_b.p, ctx->wk_off.p,
+                   ctx->wk_cnt.p, ctx->dtmp.p, centroids, grad_xyz, grad_rho, ctx->s, ctx->scratch));
+    if (energy) {
+        CK(sum_f64(a.ek, K, ctx->dtmp.p + 1, ctx->scratch, ctx->s));
+        CK(cudaMemcpyAsync(energy, ctx->dtmp.p + 1, sizeof(double), cudaMemcpyDeviceToHost, ctx->s));
+    }
+    if (cluster_energies)
+        CK(cudaMemcpyAsync(cluster_energies, a.ek, K * sizeof(double), cudaMemcpyDeviceToDevice, ctx->s));
+    CK(cudaStreamSynchronize(ctx->s));
     return ACVD_OK;
 }

@@ -160,4 +160,31 @@ cudaError_t launch_dual_write(const int* tri, const int* faces, const int* sel, 
                               int* out, cudaStream_t s);
 cudaError_t launch_centroids(int metric, const DevState& st, double* out, cudaStream_t s);
 
+// ---- adjoint (adjoint.cu) ----
+// Work arrays and inputs of the fixed-clustering adjoint (FP64).
+struct AdjState {
+    int64_t nv, nf;
+    int k;
+    const double* x;      // 3 nv
+    const double* rho;    // nv or null
+    double grad;          // gradation g
+    const int* tri;
+    const int* label;
+    const uint32_t* vf_row;
+    const uint32_t* vf_face;
+    double* fn;           // 3 nf unit normals
+    double* flen;         // nf |cr|
+    double* farea;        // nf
+    double* va;           // nv dual areas
+    double* vA;           // 6 nv quadrics
+    double* vw;           // nv weights (clamped)
+    unsigned char* vclamp;
+    double* cl;           // per cluster: S(3) W A(6) b(3) | E | c(3) | GS(3) GW GA(6) Gb(3)
+    double* corner;       // 9 nf corner gradients
+    double* ek;           // k per-cluster energies
+};
+
+size_t adjoint_bytes(int64_t nv, int64_t nf, int k);
+AdjState adjoint_state(void* base, int64_t nv, int64_t nf, int k);
+
 }  // namespace acvd

@@ -84,6 +84,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         "acvd_minimize": (ctypes.c_int, [_P, ctypes.POINTER(Stats)]),
         "acvd_rewind": (ctypes.c_int, [_P]),
         "acvd_set_batch": (ctypes.c_int, [_P, ctypes.c_int, _P, _P]),
+        "acvd_adjoint": (ctypes.c_int, [_P, _P, _P, ctypes.c_double, ctypes.c_double, _P, _P, _P, _P, _P, _P]),
         "acvd_get_mesh_energies": (ctypes.c_int, [_P, _P]),
         "acvd_get_labels": (ctypes.c_int, [_P, _P]),
         "acvd_get_clusters": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P, _P]),
@@ -231,6 +232,16 @@ class Engine:
         out = np.empty(self.nmesh, dtype=np.float64)
         self._ck(self._lib.acvd_get_mesh_energies(self.ctx, _ptr(out)), "acvd_get_mesh_energies")
         return out
+
+    def adjoint_raw(self, xyz_ptr: int, rho_ptr: int | None, gradation: float, g_energy: float,
+                    g_centroids_ptr: int | None, centroids_ptr: int | None, grad_xyz_ptr: int | None,
+                    grad_rho_ptr: int | None, cluster_energies_ptr: int | None = None) -> float:
+        """acvd_adjoint on DEVICE pointers (float64); returns the energy."""
+        e = ctypes.c_double()
+        self._ck(self._lib.acvd_adjoint(self.ctx, xyz_ptr, rho_ptr, float(gradation), float(g_energy),
+                                        g_centroids_ptr, ctypes.byref(e), cluster_energies_ptr, centroids_ptr,
+                                        grad_xyz_ptr, grad_rho_ptr), "acvd_adjoint")
+        return e.value
 
     def set_level(self, level: int):
         self._ck(self._lib.acvd_set_quadrics_optimization_level(self.ctx, int(level)))

@@ -189,6 +189,24 @@ int acvd_get_boundary_edges(acvd_ctx* ctx, int32_t* ids, int64_t* count);
  */
 int acvd_get_dual_mesh(acvd_ctx* ctx, int32_t* tris, int64_t* n_tris);
 
+/*
+ * Adjoint for a fixed clustering (the labels last set or computed), FP64.
+ * Inputs are DEVICE arrays: positions xyz[3 nV] and densities rho[nV] (the
+ * per-vertex indicator, weight = area * rho^gradation; NULL for area weights).
+ * Computes the metric energy sum_k E_k (host *energy), the per-cluster energies
+ * cluster_energies[K] and the quadric-placed cluster vertices centroids[3K]
+ * (device, either may be NULL), and, when grad_xyz is
+ * given, the vector-Jacobian product of  g_energy * sum_k E_k + sum_k
+ * g_centroids_k . c_k  with respect to xyz (grad_xyz[3 nV]) and rho
+ * (grad_rho[nV], may be NULL).  The pseudo-inverse keeps the eigenvalues of its
+ * forward evaluation (rank held fixed); clamped weights are constants.  Cluster
+ * sums are recomputed on every call, nothing per item is stored.  Isotropic and
+ * QEM metrics.
+ */
+int acvd_adjoint(acvd_ctx* ctx, const double* xyz, const double* rho, double gradation, double g_energy,
+                 const double* g_centroids, double* energy, double* cluster_energies, double* centroids,
+                 double* grad_xyz, double* grad_rho);
+
 /* The CUDA stream (cudaStream_t) the context launches on. */
 void* acvd_stream(acvd_ctx* ctx);
 
