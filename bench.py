@@ -38,8 +38,9 @@ WORKLOADS = {
                                gradation=1.5, uinit=1,
                                desc="ACVDQ torus R=1 r=0.3 1024x512 (524,288 items), K=20,000, gradation 1.5"),
     "icosphere_l5_iso": dict(kind="icosphere", mesh=dict(level=5, seed=0), metric="iso", k=1000,
-                             gradation=0.0, uinit=0,
-                             desc="ACVD icosphere level 5 (10,242 items), K=1,000, isotropic"),
+                             gradation=0.0, uinit=0, init="seeds",
+                             desc="ACVD icosphere level 5 (10,242 items), K=1,000 single-item seeds from a "
+                                  "seeded shuffle (others unassigned), isotropic"),
     "torus_512x512_qem": dict(kind="torus", mesh=dict(nu=512, nv=512, seed=0), metric="qem", k=10000,
                               gradation=1.0, uinit=1, density=True,
                               desc="ACVDQ torus 512x512 (262,144 items), K=10,000, densities U[0.5,2], gradation 1"),
@@ -60,6 +61,102 @@ BATCH_WORKLOADS = {
 }
 
 
+ADJOINT_WORKLOADS = {
+    "torus_512x512_adjoint": dict(mesh=dict(nu=512, nv=512, seed=0), k=10000, gradation=1.0,
+                                  desc="adjoint of ACVDQ on the torus 512x512 (262,144 items), densities "
+                                       "U[0.5, 2] with gradation 1, K=10,000 converged then fixed: gradients "
+                                       "of the energy and of the placed vertices w.r.t. positions and densities"),
+}
+
+
+def run_adjoint_arm(args):
+    """Adjoint workload: converge, fix the clustering, time forward + backward of
+    E + sum_k G_k . c_k, and check 64 random coordinates against FP64 central
+    differences (step 1e-6) and the whole gradient against the FP64 torch reference."""
+    import torch
+    import acvd_gb300
+    from acvd_gb300 import engine as E
+    from acvd_gb300 import synth
+    from acvd_gb300.adjoint import ClusteringEnergy, cluster_energies, reference_energy
+
+    ws, rank, local = _dist()
+    device = local
+    torch.cuda.set_device(device)
+    w = ADJOINT_WORKLOADS[args.workload]
+    m = synth.torus(**w["mesh"], with_curvature=False)
+    rho = np.random.default_rng(1).uniform(0.5, 2.0, m.n_points)
+    row, col, ev = acvd_gb300.build_topology(m.n_points, m.faces)
+    wts = acvd_gb300.vertex_weights("qem", m.points, m.faces, rho, w["gradation"])
+    lab0 = acvd_gb300.initial_sampling(row, col, wts, w["k"])
+    eng = E.Engine(device=device)
+    eng.set_mesh(m.points, m.faces, row, col, ev)
+    eng.set_metric("qem", rho, None, w["gradation"])
+    eng.set_unconstrained_initialization(1)
+    eng.set_labels(w["k"], lab0)
+    conv = eng.minimize()
+    lab = eng.labels()
+    eng.set_labels(w["k"], lab)            # the converged clustering, held fixed
+    G = torch.tensor(np.random.default_rng(7).normal(size=(w["k"], 3)), dtype=torch.float64, device="cuda")
+    x = torch.tensor(m.points, dtype=torch.float32, device="cuda", requires_grad=True)   # fp32 input positions
+    r = torch.tensor(rho, dtype=torch.float32, device="cuda", requires_grad=True)
+
+    def step():
+        x.grad = None
+        r.grad = None
+        En, C = ClusteringEnergy.apply(x, r, eng, w["gradation"])
+        (En + (C * G).sum()).backward()
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    times = []
+    with ClockSampler(device) as clk:
+        for _ in range(args.steps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            step()
+            torch.cuda.synchronize()
+            times.append(1000.0 * (time.perf_counter() - t0))
+    ms = statistics.mean(times)
+    # checks at full size
+    x64 = torch.tensor(m.points, dtype=torch.float64, device="cuda", requires_grad=True)
+    r64 = torch.tensor(rho, dtype=torch.float64, device="cuda", requires_grad=True)
+    En, C = ClusteringEnergy.apply(x64, r64, eng, w["gradation"])
+    En.backward()
+    gx, gr = x64.grad.cpu().numpy(), r64.grad.cpu().numpy()
+    rng = np.random.default_rng(11)
+    h = 1e-6
+    xb = torch.tensor(m.points, dtype=torch.float64, device="cuda")
+    rb = torch.tensor(rho, dtype=torch.float64, device="cuda")
+    worst_fd = 0.0
+    for _ in range(64):
+        i, d = int(rng.integers(m.n_points)), int(rng.integers(3))
+        xp, xm = xb.clone(), xb.clone()
+        xp[i, d] += h
+        xm[i, d] -= h
+        fd = float((cluster_energies(eng, xp, rb, w["gradation"]) - cluster_energies(eng, xm, rb, w["gradation"])).sum()) / (2 * h)
+        worst_fd = max(worst_fd, abs(fd - gx[i, d]) / max(abs(fd), 1e-3 * np.abs(gx).max()))
+    xr = torch.tensor(m.points, dtype=torch.float64, requires_grad=True)
+    rr = torch.tensor(rho, dtype=torch.float64, requires_grad=True)
+    Er, _ = reference_energy(xr, m.faces, lab, w["k"], rr, w["gradation"])
+    Er.backward()
+    ref_x = float(np.max(np.abs(gx - xr.grad.numpy())) / np.max(np.abs(xr.grad.numpy())))
+    ref_r = float(np.max(np.abs(gr - rr.grad.numpy())) / np.max(np.abs(rr.grad.numpy())))
+    if rank != 0:
+        return
+    line = {"metric": METRIC, "value": 1000.0 / ms, "unit": "gradient evaluations/s (forward + backward)",
+            "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": args.workload, "description": w["desc"], "items": m.n_points, "clusters": w["k"]},
+            "convergence": {"sweeps": conv["sweeps"], "device_ms": conv["device_ms"]},
+            "checks": {"fd_coordinates": 64, "fd_step": h, "worst_fd_rel_err": worst_fd,
+                       "ref_grad_rel_err_xyz": ref_x, "ref_grad_rel_err_rho": ref_r,
+                       "within_1e-4": bool(worst_fd <= 1e-4 and ref_x <= 1e-4 and ref_r <= 1e-4),
+                       "energy": float(En)},
+            "cpu_baseline": None, "e2e": None, "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+
+
 def _dist():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -78,9 +175,12 @@ def make_workload(name):
     return m, (ind if use_ind else None), (m.principal_dirs if w["metric"] == "aniso" else None), w
 
 
-def initial_labels(m, metric, ind, grad, k):
+def initial_labels(m, metric, ind, grad, k, init=None):
     import acvd_gb300
+    from acvd_gb300 import synth
     row, col, ev = acvd_gb300.build_topology(m.n_points, m.faces)
+    if init == "seeds":
+        return synth.seed_labels(m.n_points, k, seed=0), (row, col, ev)
     w = acvd_gb300.vertex_weights(metric, m.points, m.faces, ind, grad)
     return acvd_gb300.initial_sampling(row, col, w, k), (row, col, ev)
 
@@ -156,7 +256,7 @@ def evaluated_energy(w, points, faces, k, ind, pd, labels):
 def _port_job(args):
     name, = args
     m, ind, pd, w = make_workload(name)
-    lab0, _ = initial_labels(m, w["metric"], ind, w["gradation"], w["k"])
+    lab0, _ = initial_labels(m, w["metric"], ind, w["gradation"], w["k"], w.get("init"))
     p, secs = cpu_reference_run(m, ind, pd, w, lab0)
     return m.n_points, secs, p.global_energy()
 
@@ -352,7 +452,7 @@ def run_gpu_arm(args):
     torch.cuda.set_device(device)
 
     m, ind, pd, w = make_workload(args.workload)
-    lab0, (row, col, ev) = initial_labels(m, w["metric"], ind, w["gradation"], w["k"])
+    lab0, (row, col, ev) = initial_labels(m, w["metric"], ind, w["gradation"], w["k"], w.get("init"))
     n = m.n_points
 
     eng = E.Engine(device=device, kernel_timing=True)
@@ -508,7 +608,8 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="torus_1024x512_qem", choices=sorted(WORKLOADS) + sorted(BATCH_WORKLOADS))
+    ap.add_argument("--workload", default="torus_1024x512_qem",
+                    choices=sorted(WORKLOADS) + sorted(BATCH_WORKLOADS) + sorted(ADJOINT_WORKLOADS))
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
@@ -516,6 +617,8 @@ def main():
         run_reference_arm(args)
     elif args.workload in BATCH_WORKLOADS:
         run_batch_arm(args)
+    elif args.workload in ADJOINT_WORKLOADS:
+        run_adjoint_arm(args)
     else:
         run_gpu_arm(args)
 
