@@ -210,19 +210,28 @@ ACVD_DEV void warp_count(unsigned long long* ctr, unsigned v) {
 // vtkUniformClustering.h:912-920).  Proposals go to a compact per-step list.
 // ---------------------------------------------------------------------------
 template <int M>
-__global__ void __launch_bounds__(256) eval_kernel(DevState st, const int* __restrict__ items, int64_t count,
-                                                   int color, int* __restrict__ cand_dest,
-                                                   unsigned* __restrict__ cand_prio, int claims) {
+__global__ void __launch_bounds__(256, 3) eval_kernel(DevState st, const int* __restrict__ items, int64_t count,
+                                                      int color, int* __restrict__ cand_dest,
+                                                      unsigned* __restrict__ cand_prio, int claims) {
+    // Two phases per block.  A: every thread screens its item (boundary, any
+    // cluster around it changed, size guard, local connectivity) and the items
+    // that need energy tests are packed into shared memory.  B: the first
+    // threads of the block run those tests, so the expensive part runs on full
+    // warps and the rest of the block retires early.
+    __shared__ int s_work[256];
+    __shared__ unsigned s_nwork;
+    if (threadIdx.x == 0) s_nwork = 0u;
+    __syncthreads();
     const int epoch = color * kRounds;   // claim epoch of this step's first matching round
     const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const bool in = idx < count;
+    const SweepState sw = *st.sweep;
+    const RunFlags fl = *st.flags;
     unsigned n_slots = 0, n_bnd = 0, n_tgt = 0, n_cand = 0;
-    int my_slot_cand = 0;
     if (in) {
         const int i = items[idx];
         const int L = st.label[i];
         const int p0 = st.row[i], p1 = st.row[i + 1];
-        const SweepState sw = *st.sweep;
         const int ev_i = st.evald[i];
         bool fresh = ev_i <= sw.floor || (L < st.k && st.stamp[L] >= ev_i);
         n_slots = (unsigned)(p1 - p0);
@@ -236,73 +245,83 @@ __global__ void __launch_bounds__(256) eval_kernel(DevState st, const int* __res
         }
         if (boundary && fresh) {
             n_bnd = 1;
-            const RunFlags fl = *st.flags;
-            ItemRec it;
-            load_item<M>(st, i, it);
-            int best = -1;
-            unsigned pr = 0u;
-            if (L >= st.k) {
-                // unassigned item: joins the neighbouring cluster it is cheapest to join
-                float bv = 0.0f;
-                for (int p = p0; p < p1; p++) {
-                    const int B = st.label[st.col[p]];
-                    if (B >= st.k) continue;
-                    const float4 e0 = st.ev[(int64_t)B * Layout<M>::ev];
-                    const float dx = it.x[0] - e0.x, dy = it.x[1] - e0.y, dz = it.x[2] - e0.z;
-                    const float v = it.w * e0.w / (e0.w + it.w) * (dx * dx + dy * dy + dz * dz);
-                    n_tgt++;
-                    if (best < 0 || v < bv || (v == bv && B < best)) { best = B; bv = v; }
-                }
-                pr = 0u;
-            } else if (st.size[L] > 1 && (!fl.connexity || ring_connected(st, p0, p1, L))) {
-                EvalRec eL;
-                load_eval<M>(st, L, eL);
-                float xc[3];
-                const float rem = remove_part<M>(eL, it, fl, xc);
-                float bde = 0.0f, badd = 0.0f;
-                for (int p = p0; p < p1; p++) {
-                    const int B = st.label[st.col[p]];
-                    if (B == L || B >= st.k) continue;
-                    bool dup = false;
-                    for (int q = p0; q < p; q++) dup |= (st.label[st.col[q]] == B);
-                    if (dup) continue;
-                    EvalRec eB;
-                    load_eval<M>(st, B, eB);
-                    const float add = add_part<M>(eB, it, fl);
-                    const float de = rem + add;
-                    n_tgt++;
-                    if (de < bde || (de == bde && best >= 0 && B < best)) { best = B; bde = de; badd = add; }
-                }
-                // a move must gain more than the float32 error of its own test
-                // (two near-tie moves could otherwise both test negative and
-                // alternate); the reference keeps an item on ties (:960)
-                if (best >= 0 && !(bde < -kAcceptTol * (fabsf(rem) + fabsf(badd)))) best = -1;
-                if (best >= 0) pr = prio_of_delta(bde);
-            }
-            if (best >= 0) {
-                cand_dest[idx] = best;
-                cand_prio[idx] = pr;
-                if (claims) {
-                    const unsigned long long c = make_claim((unsigned)epoch, pr, (unsigned)idx);
-                    if (L < st.k) atomicMin(&st.claim[L], c);
-                    atomicMin(&st.claim[best], c);
-                }
-                n_cand = 1;
-                st.evald[i] = -1;
-            } else {
-                st.evald[i] = sw.sweep;
-            }
+            const bool movable =
+                L >= st.k || (st.size[L] > 1 && (!fl.connexity || ring_connected(st, p0, p1, L)));
+            if (movable) s_work[atomicAdd(&s_nwork, 1u)] = (int)idx;
+            else st.evald[i] = sw.sweep;   // evaluated: nothing it may do
         }
-        my_slot_cand = n_cand;
+    }
+    __syncthreads();
+    int my_cand = -1;
+    if (threadIdx.x < s_nwork) {
+        const int widx = s_work[threadIdx.x];
+        const int i = items[widx];
+        const int L = st.label[i];
+        const int p0 = st.row[i], p1 = st.row[i + 1];
+        ItemRec it;
+        load_item<M>(st, i, it);
+        int best = -1;
+        unsigned pr = 0u;
+        if (L >= st.k) {
+            // unassigned item: joins the neighbouring cluster it is cheapest to join
+            float bv = 0.0f;
+            for (int p = p0; p < p1; p++) {
+                const int B = st.label[st.col[p]];
+                if (B >= st.k) continue;
+                const float4 e0 = st.ev[(int64_t)B * Layout<M>::ev];
+                const float dx = it.x[0] - e0.x, dy = it.x[1] - e0.y, dz = it.x[2] - e0.z;
+                const float v = it.w * e0.w / (e0.w + it.w) * (dx * dx + dy * dy + dz * dz);
+                n_tgt++;
+                if (best < 0 || v < bv || (v == bv && B < best)) { best = B; bv = v; }
+            }
+        } else {
+            EvalRec eL;
+            load_eval<M>(st, L, eL);
+            float xc[3];
+            const float rem = remove_part<M>(eL, it, fl, xc);
+            float bde = 0.0f, badd = 0.0f;
+            for (int p = p0; p < p1; p++) {
+                const int B = st.label[st.col[p]];
+                if (B == L || B >= st.k) continue;
+                bool dup = false;
+                for (int q = p0; q < p; q++) dup |= (st.label[st.col[q]] == B);
+                if (dup) continue;
+                EvalRec eB;
+                load_eval<M>(st, B, eB);
+                const float add = add_part<M>(eB, it, fl);
+                const float de = rem + add;
+                n_tgt++;
+                if (de < bde || (de == bde && best >= 0 && B < best)) { best = B; bde = de; badd = add; }
+            }
+            // a move must gain more than the float32 error of its own test
+            // (two near-tie moves could otherwise both test negative and
+            // alternate); the reference keeps an item on ties (:960)
+            if (best >= 0 && !(bde < -kAcceptTol * (fabsf(rem) + fabsf(badd)))) best = -1;
+            if (best >= 0) pr = prio_of_delta(bde);
+        }
+        if (best >= 0) {
+            cand_dest[widx] = best;
+            cand_prio[widx] = pr;
+            if (claims) {
+                const unsigned long long c = make_claim((unsigned)epoch, pr, (unsigned)widx);
+                if (L < st.k) atomicMin(&st.claim[L], c);
+                atomicMin(&st.claim[best], c);
+            }
+            n_cand = 1;
+            my_cand = widx;
+            st.evald[i] = -1;
+        } else {
+            st.evald[i] = sw.sweep;
+        }
     }
     // warp-aggregated append to the compact proposal list
-    const unsigned bal = __ballot_sync(kFull, my_slot_cand != 0);
+    const unsigned bal = __ballot_sync(kFull, my_cand >= 0);
     if (bal) {
         const int lane = threadIdx.x & 31;
         unsigned base = 0;
         if (lane == 0) base = atomicAdd(&st.cand_count[color], (unsigned)__popc(bal));
         base = __shfl_sync(kFull, base, 0);
-        if (my_slot_cand) st.cand_list[base + __popc(bal & ((1u << lane) - 1u))] = (int)idx;
+        if (my_cand >= 0) st.cand_list[base + __popc(bal & ((1u << lane) - 1u))] = my_cand;
     }
     warp_count(&st.counters[kCntVisited], in ? 1u : 0u);
     warp_count(&st.counters[kCntSlots], n_slots);
