@@ -18,7 +18,7 @@ SRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libacvd_gb300.so")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
-CU_SOURCES = ["primitives.cu", "topology.cu", "cluster.cu", "adjoint.cu", "engine.cu"]
+CU_SOURCES = ["primitives.cu", "topology.cu", "cluster.cu", "adjoint.cu", "engine.cu", "noalloc.cu"]
 CXX_SOURCES = ["host.cpp"]
 
 

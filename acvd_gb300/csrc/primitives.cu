@@ -122,6 +122,14 @@ cudaError_t exclusive_scan_u32(const uint32_t* in, uint32_t* out, int64_t n, uin
     return e;
 }
 
+size_t scan_scratch_need(int64_t n) { return scan_scratch_words(n); }
+
+cudaError_t exclusive_scan_u32_raw(const uint32_t* in, uint32_t* out, int64_t n, uint32_t* scratch,
+                                   size_t scratch_words, cudaStream_t s) {
+    if (scratch_words < scan_scratch_words(n)) return cudaErrorInvalidValue;
+    return scan_rec(in, out, n, scratch, s);
+}
+
 // ---------------------------------------------------------------------------
 // deterministic FP64 sum: fixed-shape tree (256-thread blocks, 8 values/thread)
 // ---------------------------------------------------------------------------

@@ -26,6 +26,14 @@ cudaError_t exclusive_scan_u32(const uint32_t* in, uint32_t* out, int64_t n, uin
 cudaError_t radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* tmp_keys, uint32_t* tmp_vals,
                              int64_t n, int key_bits, Scratch& scratch, cudaStream_t s);
 
+// Scratch words exclusive_scan_u32_raw needs for n values.
+size_t scan_scratch_need(int64_t n);
+
+// exclusive_scan_u32 without a total, on caller-provided scratch of
+// scratch_words uint32 words (at least scan_scratch_need(n)); allocates nothing.
+cudaError_t exclusive_scan_u32_raw(const uint32_t* in, uint32_t* out, int64_t n, uint32_t* scratch,
+                                   size_t scratch_words, cudaStream_t s);
+
 // Deterministic sum of n doubles (fixed reduction tree) into *out_dev.
 cudaError_t sum_f64(const double* in, int64_t n, double* out_dev, Scratch& scratch, cudaStream_t s);
 

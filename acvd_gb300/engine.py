@@ -90,6 +90,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         "acvd_get_clusters": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P, _P]),
         "acvd_get_boundary_edges": (ctypes.c_int, [_P, _P, ctypes.POINTER(_i64)]),
         "acvd_get_dual_mesh": (ctypes.c_int, [_P, _P, ctypes.POINTER(_i64)]),
+        "acvd_boundary_edges_noalloc": (ctypes.c_int, [_P, _i64, _P, _P, _P, _P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

@@ -181,6 +181,25 @@ int acvd_get_clusters(acvd_ctx* ctx, int32_t* sizes, double* S, double* W, doubl
 int acvd_get_boundary_edges(acvd_ctx* ctx, int32_t* ids, int64_t* count);
 
 /*
+ * The boundary edges of acvd_get_boundary_edges with no device allocation.  It
+ * has no counterpart in the reference; it serves callers that hold the edge
+ * table and the labels on the device already and must not allocate.
+ * Inputs are DEVICE arrays on the current device: d_edge_v[2 n_edges] (edge
+ * endpoints, reference edge numbering), d_labels[nV]; outputs d_ids[n_edges]
+ * (boundary edge ids, increasing) and d_count[1].  Enqueued on `stream` (a
+ * cudaStream_t; NULL = the default stream) and returns without waiting.
+ * Scratch is a fixed 256 KiB device array per device: no cudaMalloc, no
+ * cudaFree.  The first call on a device looks that array up (set-up); make it
+ * before any stream capture.  Calls on one device share the array, so calls
+ * that overlap in time (other streams, other threads) race: serialise them.
+ * n_edges above ACVD_NOALLOC_MAX_EDGES returns ACVD_ERR_UNSUPPORTED with
+ * nothing enqueued.
+ */
+#define ACVD_NOALLOC_MAX_EDGES 67108864LL /* 2^26 edges */
+int acvd_boundary_edges_noalloc(const int32_t* d_edge_v, int64_t n_edges, const int32_t* d_labels,
+                                int32_t* d_ids, uint32_t* d_count, void* stream);
+
+/*
  * Dual mesh (BuildDelaunayTriangulation, DiscreteRemeshing/vtkDiscreteRemeshing.h:1003-1152,
  * vertex clustering, without manifold repair): one triangle per input face whose
  * three labels are valid and distinct, in face order, duplicates (same label set)
