@@ -209,21 +209,67 @@ ACVD_DEV void warp_count(unsigned long long* ctr, unsigned v) {
 // edge when neither cluster was modified in the previous loop,
 // vtkUniformClustering.h:912-920).  Proposals go to a compact per-step list.
 // ---------------------------------------------------------------------------
+constexpr int kRingPref = 8;   // ring slots whose labels phase A loads up front
+constexpr int kMaxTgt = 8;     // destination clusters per item on the task path
+constexpr int kTaskRemove = 15;  // task code of an item's remove part
+
+// Local connectivity with the first kRingPref ring labels already loaded.
+ACVD_DEV bool ring_connected_pref(const DevState& st, int p0, int p1, int L, const int* lb) {
+    const int d = p1 - p0;
+    if (d > 32) return false;
+    unsigned msk = 0u;
+#pragma unroll
+    for (int q = 0; q < kRingPref; q++)
+        if (q < d && lb[q] == L) msk |= 1u << q;
+    for (int q = kRingPref; q < d; q++)
+        if (st.label[st.col[p0 + q]] == L) msk |= 1u << q;
+    if (msk == 0u) return true;
+    unsigned vis = msk & (0u - msk);
+    unsigned front = vis;
+    while (front) {
+        unsigned nxt = 0u;
+        unsigned f = front;
+        while (f) {
+            const int q = __ffs(f) - 1;
+            f &= f - 1u;
+            nxt |= st.adj[p0 + q];
+        }
+        nxt &= msk & ~vis;
+        vis |= nxt;
+        front = nxt;
+    }
+    return vis == msk;
+}
+
+// One tile of 256 items of a colour class (blockDim.x == 256; every thread of the
+// block calls it).  Arrays written during a sweep are read through plain
+// pointers: the persistent sweep kernel reads them after other blocks wrote them.
+//
+// Phase A (one item per thread): skip test, boundary test, size guard and local
+// connectivity, with the ring's labels loaded up front; a movable item joins the
+// block's work list with its distinct destination clusters.  Phase B1: the energy
+// tests -- one task per (item, destination) plus one per item for the part that
+// depends on its own cluster -- spread over all threads of the block.  Phase B2
+// (one work item per thread): the best destination, the acceptance margin, the
+// proposal and its claims.  Unassigned items and items with more than kMaxTgt
+// destinations run the whole test in B2.
 template <int M>
-__global__ void __launch_bounds__(256, 3) eval_kernel(DevState st, const int* __restrict__ items, int64_t count,
-                                                      int color, int* __restrict__ cand_dest,
-                                                      unsigned* __restrict__ cand_prio, int claims) {
-    // Two phases per block.  A: every thread screens its item (boundary, any
-    // cluster around it changed, size guard, local connectivity) and the items
-    // that need energy tests are packed into shared memory.  B: the first
-    // threads of the block run those tests, so the expensive part runs on full
-    // warps and the rest of the block retires early.
-    __shared__ int s_work[256];
-    __shared__ unsigned s_nwork;
-    if (threadIdx.x == 0) s_nwork = 0u;
+ACVD_DEV void eval_tile(const DevState& st, const int* __restrict__ items, int64_t count, int color,
+                        int* cand_dest, unsigned* cand_prio, int claims, int64_t tile) {
+    __shared__ int s_idx[256];                 // work item -> colour-list position
+    __shared__ int s_tgt[256][kMaxTgt];        // work item -> destination clusters (ring order)
+    __shared__ float s_val[256][kMaxTgt + 1];  // energy parts: [j] add to s_tgt[j], [kMaxTgt] remove
+    __shared__ signed char s_nt[256];          // destinations; -1: the whole test runs in B2
+    __shared__ unsigned short s_task[256 * (kMaxTgt + 1)];
+    __shared__ unsigned s_nwork, s_ntask;
+    __syncthreads();                     // the previous tile is done with the shared arrays
+    if (threadIdx.x == 0) {
+        s_nwork = 0u;
+        s_ntask = 0u;
+    }
     __syncthreads();
     const int epoch = color * kRounds;   // claim epoch of this step's first matching round
-    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t idx = tile * 256 + threadIdx.x;
     const bool in = idx < count;
     const SweepState sw = *st.sweep;
     const RunFlags fl = *st.flags;
@@ -233,11 +279,25 @@ __global__ void __launch_bounds__(256, 3) eval_kernel(DevState st, const int* __
         const int L = st.label[i];
         const int p0 = st.row[i], p1 = st.row[i + 1];
         const int ev_i = st.evald[i];
+        const int deg = p1 - p0;
+        int lb[kRingPref];
+#pragma unroll
+        for (int q = 0; q < kRingPref; q++) lb[q] = q < deg ? st.col[p0 + q] : -1;
+#pragma unroll
+        for (int q = 0; q < kRingPref; q++) lb[q] = lb[q] >= 0 ? st.label[lb[q]] : L;
         bool fresh = ev_i <= sw.floor || (L < st.k && st.stamp[L] >= ev_i);
-        n_slots = (unsigned)(p1 - p0);
+        n_slots = (unsigned)deg;
         bool boundary = false;
-        for (int p = p0; p < p1; p++) {
-            const int B = st.label[st.col[p]];
+#pragma unroll
+        for (int q = 0; q < kRingPref; q++) {
+            const int B = lb[q];
+            if (B != L) {
+                boundary = true;
+                if (B < st.k && st.stamp[B] >= ev_i) fresh = true;
+            }
+        }
+        for (int q = kRingPref; q < deg; q++) {
+            const int B = st.label[st.col[p0 + q]];
             if (B != L) {
                 boundary = true;
                 if (B < st.k && st.stamp[B] >= ev_i) fresh = true;
@@ -246,58 +306,127 @@ __global__ void __launch_bounds__(256, 3) eval_kernel(DevState st, const int* __
         if (boundary && fresh) {
             n_bnd = 1;
             const bool movable =
-                L >= st.k || (st.size[L] > 1 && (!fl.connexity || ring_connected(st, p0, p1, L)));
-            if (movable) s_work[atomicAdd(&s_nwork, 1u)] = (int)idx;
-            else st.evald[i] = sw.sweep;   // evaluated: nothing it may do
+                L >= st.k || (st.size[L] > 1 && (!fl.connexity || ring_connected_pref(st, p0, p1, L, lb)));
+            if (movable) {
+                const int w = (int)atomicAdd(&s_nwork, 1u);
+                s_idx[w] = (int)idx;
+                int nt = 0;
+                bool all = L < st.k && deg <= kRingPref;
+#pragma unroll
+                for (int q = 0; q < kRingPref; q++) {
+                    const int B = lb[q];
+                    if (!all || B == L || B >= st.k) continue;
+                    bool dup = false;
+#pragma unroll
+                    for (int r = 0; r < q; r++) dup |= lb[r] == B;
+                    if (dup) continue;
+                    if (nt == kMaxTgt) {
+                        all = false;
+                        continue;
+                    }
+                    s_tgt[w][nt++] = B;
+                }
+                if (all) {
+                    s_nt[w] = (signed char)nt;
+                    n_tgt += (unsigned)nt;
+                    if (nt > 0) {
+                        const unsigned base = atomicAdd(&s_ntask, (unsigned)nt + 1u);
+                        for (int j = 0; j < nt; j++) s_task[base + j] = (unsigned short)((w << 4) | j);
+                        s_task[base + nt] = (unsigned short)((w << 4) | kTaskRemove);
+                    }
+                } else {
+                    s_nt[w] = -1;
+                }
+            } else {
+                st.evald[i] = sw.sweep;   // evaluated: nothing it may do
+            }
         }
     }
     __syncthreads();
-    int my_cand = -1;
-    if (threadIdx.x < s_nwork) {
-        const int widx = s_work[threadIdx.x];
-        const int i = items[widx];
-        const int L = st.label[i];
-        const int p0 = st.row[i], p1 = st.row[i + 1];
+    // B1: energy parts
+    const unsigned ntask = s_ntask;
+    for (unsigned t = threadIdx.x; t < ntask; t += 256) {
+        const unsigned code = s_task[t];
+        const int w = (int)(code >> 4), j = (int)(code & 15u);
+        const int i = items[s_idx[w]];
         ItemRec it;
         load_item<M>(st, i, it);
+        if (j == kTaskRemove) {
+            EvalRec eL;
+            load_eval<M>(st, st.label[i], eL);
+            float xc[3];
+            s_val[w][kMaxTgt] = remove_part<M>(eL, it, fl, xc);
+        } else {
+            EvalRec eB;
+            load_eval<M>(st, s_tgt[w][j], eB);
+            s_val[w][j] = add_part<M>(eB, it, fl);
+        }
+    }
+    __syncthreads();
+    // B2: decision
+    int my_cand = -1;
+    if (threadIdx.x < s_nwork) {
+        const int w = threadIdx.x;
+        const int widx = s_idx[w];
+        const int i = items[widx];
+        const int L = st.label[i];
+        const int nt = s_nt[w];
         int best = -1;
         unsigned pr = 0u;
-        if (L >= st.k) {
-            // unassigned item: joins the neighbouring cluster it is cheapest to join
-            float bv = 0.0f;
-            for (int p = p0; p < p1; p++) {
-                const int B = st.label[st.col[p]];
-                if (B >= st.k) continue;
-                const float4 e0 = st.ev[(int64_t)B * Layout<M>::ev];
-                const float dx = it.x[0] - e0.x, dy = it.x[1] - e0.y, dz = it.x[2] - e0.z;
-                const float v = it.w * e0.w / (e0.w + it.w) * (dx * dx + dy * dy + dz * dz);
-                n_tgt++;
-                if (best < 0 || v < bv || (v == bv && B < best)) { best = B; bv = v; }
+        if (nt >= 0) {
+            if (nt > 0) {
+                const float rem = s_val[w][kMaxTgt];
+                float bde = 0.0f, badd = 0.0f;
+                for (int j = 0; j < nt; j++) {
+                    const int B = s_tgt[w][j];
+                    const float add = s_val[w][j];
+                    const float de = rem + add;
+                    if (de < bde || (de == bde && best >= 0 && B < best)) { best = B; bde = de; badd = add; }
+                }
+                // a move must gain more than the float32 error of its own test
+                // (two near-tie moves could otherwise both test negative and
+                // alternate); the reference keeps an item on ties (:960)
+                if (best >= 0 && !(bde < -kAcceptTol * (fabsf(rem) + fabsf(badd)))) best = -1;
+                if (best >= 0) pr = prio_of_delta(bde);
             }
         } else {
-            EvalRec eL;
-            load_eval<M>(st, L, eL);
-            float xc[3];
-            const float rem = remove_part<M>(eL, it, fl, xc);
-            float bde = 0.0f, badd = 0.0f;
-            for (int p = p0; p < p1; p++) {
-                const int B = st.label[st.col[p]];
-                if (B == L || B >= st.k) continue;
-                bool dup = false;
-                for (int q = p0; q < p; q++) dup |= (st.label[st.col[q]] == B);
-                if (dup) continue;
-                EvalRec eB;
-                load_eval<M>(st, B, eB);
-                const float add = add_part<M>(eB, it, fl);
-                const float de = rem + add;
-                n_tgt++;
-                if (de < bde || (de == bde && best >= 0 && B < best)) { best = B; bde = de; badd = add; }
+            const int p0 = st.row[i], p1 = st.row[i + 1];
+            ItemRec it;
+            load_item<M>(st, i, it);
+            if (L >= st.k) {
+                // unassigned item: joins the neighbouring cluster it is cheapest to join
+                float bv = 0.0f;
+                for (int p = p0; p < p1; p++) {
+                    const int B = st.label[st.col[p]];
+                    if (B >= st.k) continue;
+                    const float4 e0 = st.ev[(int64_t)B * Layout<M>::ev];
+                    const float dx = it.x[0] - e0.x, dy = it.x[1] - e0.y, dz = it.x[2] - e0.z;
+                    const float v = it.w * e0.w / (e0.w + it.w) * (dx * dx + dy * dy + dz * dz);
+                    n_tgt++;
+                    if (best < 0 || v < bv || (v == bv && B < best)) { best = B; bv = v; }
+                }
+            } else {
+                EvalRec eL;
+                load_eval<M>(st, L, eL);
+                float xc[3];
+                const float rem = remove_part<M>(eL, it, fl, xc);
+                float bde = 0.0f, badd = 0.0f;
+                for (int p = p0; p < p1; p++) {
+                    const int B = st.label[st.col[p]];
+                    if (B == L || B >= st.k) continue;
+                    bool dup = false;
+                    for (int q = p0; q < p; q++) dup |= (st.label[st.col[q]] == B);
+                    if (dup) continue;
+                    EvalRec eB;
+                    load_eval<M>(st, B, eB);
+                    const float add = add_part<M>(eB, it, fl);
+                    const float de = rem + add;
+                    n_tgt++;
+                    if (de < bde || (de == bde && best >= 0 && B < best)) { best = B; bde = de; badd = add; }
+                }
+                if (best >= 0 && !(bde < -kAcceptTol * (fabsf(rem) + fabsf(badd)))) best = -1;
+                if (best >= 0) pr = prio_of_delta(bde);
             }
-            // a move must gain more than the float32 error of its own test
-            // (two near-tie moves could otherwise both test negative and
-            // alternate); the reference keeps an item on ties (:960)
-            if (best >= 0 && !(bde < -kAcceptTol * (fabsf(rem) + fabsf(badd)))) best = -1;
-            if (best >= 0) pr = prio_of_delta(bde);
         }
         if (best >= 0) {
             cand_dest[widx] = best;
@@ -328,6 +457,12 @@ __global__ void __launch_bounds__(256, 3) eval_kernel(DevState st, const int* __
     warp_count(&st.counters[kCntBoundary], n_bnd);
     warp_count(&st.counters[kCntTargets], n_tgt);
     warp_count(&st.counters[kCntCand], n_cand);
+}
+
+template <int M>
+__global__ void __launch_bounds__(256, 3) eval_kernel(DevState st, const int* __restrict__ items, int64_t count,
+                                                      int color, int* cand_dest, unsigned* cand_prio, int claims) {
+    eval_tile<M>(st, items, count, color, cand_dest, cand_prio, claims, blockIdx.x);
 }
 
 // ---------------------------------------------------------------------------
@@ -368,16 +503,84 @@ ACVD_DEV void accumulate_item(df* acc, const ItemRec& it, float sgn) {
     }
 }
 
-// Per-cluster evaluation record and FP64 energy from the accumulators
-// (ComputeClusterCentroid + ComputeClusterEnergy of the metric plugins).  FULL:
-// the quadric placement with the reference's thresholded pseudo-inverse in FP64
-// (full recompute, final results).  Otherwise (a committed move): m and the
-// residual r = b - A m in FP64 from the compensated sums, the 3x3
-// pseudo-inverse in FP32 like the evaluation kernel's.
+// Per-cluster evaluation record and energy from the compensated accumulators, in
+// float32 and double-float arithmetic only: the incremental path after committed
+// moves (float64 throughput on this part is a small fraction of float32).  Same
+// formulas as the FP64 full recompute below (ComputeClusterCentroid +
+// ComputeClusterEnergy of the metric plugins): m = S / W, residual r = b - A m,
+// placement delta = pinv(A) r in float32 (the evaluation kernel's), P = W |delta|^2.
+// Writes the record to ev[0 .. Layout<M>::ev) and returns the energy.
+template <int M>
+ACVD_DEV double cluster_record_df(const df* a, const RunFlags& fl, float4* ev) {
+    const df W = a[3];
+    if (!(W.hi > 0.0f)) {
+#pragma unroll
+        for (int j = 0; j < Layout<M>::ev; j++) ev[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+        return 0.0;
+    }
+    const df m[3] = {df_div(a[0], W), df_div(a[1], W), df_div(a[2], W)};
+    ev[0] = make_float4(m[0].hi, m[1].hi, m[2].hi, W.hi);
+    // |S|^2 / W = S . m
+    const df S2W = df_add(df_add(df_mul(a[0], m[0]), df_mul(a[1], m[1])), df_mul(a[2], m[2]));
+    if (M == kIso) return -df_to_d(S2W);
+    const df* A = a + 4;    // a00 a01 a02 a11 a12 a22
+    const df* b = a + 10;
+    const int rowi[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
+    df r[3];
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        const df Am = df_add(df_add(df_mul(A[rowi[c][0]], m[0]), df_mul(A[rowi[c][1]], m[1])),
+                             df_mul(A[rowi[c][2]], m[2]));
+        r[c] = df_sub(b[c], Am);
+    }
+    float d[3] = {0.f, 0.f, 0.f};
+    const bool place = (M == kAniso) || (fl.constrained && fl.level > 0);
+    if (place) {
+        const float Af[6] = {A[0].hi, A[1].hi, A[2].hi, A[3].hi, A[4].hi, A[5].hi};
+        const float rf[3] = {r[0].hi, r[1].hi, r[2].hi};
+        pinv_apply<float>(Af, rf, d, fl.level, fl.thr, 8);
+    }
+    const df dd = df_add(df_add(two_prod(d[0], d[0]), two_prod(d[1], d[1])), two_prod(d[2], d[2]));
+    const df P = df_mul(W, dd);
+    ev[1] = make_float4(d[0], d[1], d[2], P.hi);
+    ev[2] = make_float4(r[0].hi, r[1].hi, r[2].hi, 0.f);
+    ev[3] = make_float4(A[0].hi, A[1].hi, A[2].hi, A[3].hi);
+    ev[4] = make_float4(A[4].hi, A[5].hi, 0.f, 0.f);
+    if (M == kQEM) return df_to_d(df_sub(P, S2W));
+    const df* T = a + 13;
+    const df* u = a + 19;
+    const df c[3] = {df_add_f(m[0], d[0]), df_add_f(m[1], d[1]), df_add_f(m[2], d[2])};
+    df Tc[3];
+#pragma unroll
+    for (int q = 0; q < 3; q++)
+        Tc[q] = df_add(df_add(df_mul(T[rowi[q][0]], c[0]), df_mul(T[rowi[q][1]], c[1])), df_mul(T[rowi[q][2]], c[2]));
+    const df g[3] = {df_sub(u[0], Tc[0]), df_sub(u[1], Tc[1]), df_sub(u[2], Tc[2])};
+    ev[5] = make_float4(T[0].hi, T[1].hi, T[2].hi, T[3].hi);
+    ev[6] = make_float4(T[4].hi, T[5].hi, g[0].hi, g[1].hi);
+    ev[7] = make_float4(g[2].hi, 0.f, 0.f, 0.f);
+    const df cTc = df_add(df_add(df_mul(c[0], Tc[0]), df_mul(c[1], Tc[1])), df_mul(c[2], Tc[2]));
+    const df cu = df_add(df_add(df_mul(c[0], u[0]), df_mul(c[1], u[1])), df_mul(c[2], u[2]));
+    return df_to_d(df_sub(cTc, df_add(cu, cu)));
+}
+
+// Record and energy of cluster k.  FULL: the quadric placement with the
+// reference's thresholded pseudo-inverse in FP64 (full recompute, final
+// results).  Otherwise the double-float path above.
 template <int M, bool FULL>
 ACVD_DEV void update_cluster(const DevState& st, int k) {
     const df* a = st.acc + (int64_t)k * Layout<M>::acc;
     float4* ev = st.ev + (int64_t)k * Layout<M>::ev;
+    if (!FULL) {
+        df al[Layout<M>::acc];
+#pragma unroll
+        for (int q = 0; q < Layout<M>::acc; q++) al[q] = a[q];
+        float4 el[Layout<M>::ev];
+        const double e = cluster_record_df<M>(al, *st.flags, el);
+#pragma unroll
+        for (int q = 0; q < Layout<M>::ev; q++) ev[q] = el[q];
+        st.energy[k] = e;
+        return;
+    }
     const double W = df_to_d(a[3]);
     const double S[3] = {df_to_d(a[0]), df_to_d(a[1]), df_to_d(a[2])};
     if (!(W > 0.0)) {
@@ -402,17 +605,7 @@ ACVD_DEV void update_cluster(const DevState& st, int k) {
     const double r[3] = {b[0] - Am[0], b[1] - Am[1], b[2] - Am[2]};
     double d[3] = {0.0, 0.0, 0.0};
     const bool place = (M == kAniso) || (fl.constrained && fl.level > 0);
-    if (place) {
-        if (FULL) {
-            pinv_apply<double>(A, r, d, fl.level, (double)fl.thr, 32);
-        } else {
-            const float Af[6] = {(float)A[0], (float)A[1], (float)A[2], (float)A[3], (float)A[4], (float)A[5]};
-            const float rf[3] = {(float)r[0], (float)r[1], (float)r[2]};
-            float dfl[3];
-            pinv_apply<float>(Af, rf, dfl, fl.level, fl.thr, 8);
-            d[0] = dfl[0]; d[1] = dfl[1]; d[2] = dfl[2];
-        }
-    }
+    if (place) pinv_apply<double>(A, r, d, fl.level, (double)fl.thr, 32);
     const double P = W * (d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
     ev[1] = make_float4((float)d[0], (float)d[1], (float)d[2], (float)P);
     ev[2] = make_float4((float)r[0], (float)r[1], (float)r[2], 0.f);
@@ -440,14 +633,14 @@ ACVD_DEV void update_cluster(const DevState& st, int k) {
 // apply: commit the proposals that hold both claims (grid-stride over the
 // step's compact proposal list)
 // ---------------------------------------------------------------------------
+// gtid / gstride: this thread's position and the number of threads walking the list
 template <int M>
-__global__ void __launch_bounds__(256) apply_kernel(DevState st, const int* __restrict__ items, int color,
-                                                    int round, int* __restrict__ cand_dest,
-                                                    const unsigned* __restrict__ cand_prio) {
+ACVD_DEV void apply_range(const DevState& st, const int* __restrict__ items, int color, int round, int* cand_dest,
+                          const unsigned* cand_prio, unsigned gtid, unsigned gstride) {
     const unsigned n = st.cand_count[color];
     const unsigned epoch = (unsigned)(color * kRounds + round);
     unsigned won_total = 0;
-    for (unsigned j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+    for (unsigned j = gtid; j < n; j += gstride) {
         const int idx = st.cand_list[j];
         const int B = cand_dest[idx];
         if (B < 0) continue;                     // committed or dropped in an earlier round
@@ -475,37 +668,35 @@ __global__ void __launch_bounds__(256) apply_kernel(DevState st, const int* __re
         st.claim[L] = 0ull;
         df* aL = st.acc + (int64_t)L * Layout<M>::acc;
         float4* eL = st.ev + (int64_t)L * Layout<M>::ev;
-        // keep the two clusters' records: the commit is undone unless the tracked
-        // energy of the pair strictly decreases (the float32 test can disagree with
-        // the updated records, e.g. when a pseudo-inverse eigenvalue sits at the
-        // threshold), so the minimisation descends monotonically and terminates
-        df saveB[Layout<M>::acc], saveL[Layout<M>::acc];
-        float4 sevB[Layout<M>::ev], sevL[Layout<M>::ev];
+        // the two clusters' new records are built in registers and written only
+        // if the tracked energy of the pair strictly decreases (the float32 test
+        // can disagree with the updated records, e.g. when a pseudo-inverse
+        // eigenvalue sits at the threshold), so the minimisation descends
+        // monotonically and terminates
+        const RunFlags fl = *st.flags;
+        const double e_old = st.energy[B] + st.energy[L];
+        df nB[Layout<M>::acc], nL[Layout<M>::acc];
 #pragma unroll
-        for (int q = 0; q < Layout<M>::acc; q++) { saveB[q] = aB[q]; saveL[q] = aL[q]; }
-#pragma unroll
-        for (int q = 0; q < Layout<M>::ev; q++) { sevB[q] = eB[q]; sevL[q] = eL[q]; }
-        const double eB_old = st.energy[B], eL_old = st.energy[L];
-        const double e_old = eB_old + eL_old;
-        accumulate_item<M>(aB, it, 1.0f);
-        accumulate_item<M>(aL, it, -1.0f);
-        update_cluster<M, false>(st, B);
-        update_cluster<M, false>(st, L);
-        const double e_new = st.energy[B] + st.energy[L];
-        if (e_new < e_old) {
+        for (int q = 0; q < Layout<M>::acc; q++) { nB[q] = aB[q]; nL[q] = aL[q]; }
+        accumulate_item<M>(nB, it, 1.0f);
+        accumulate_item<M>(nL, it, -1.0f);
+        float4 rB[Layout<M>::ev], rL[Layout<M>::ev];
+        const double eBn = cluster_record_df<M>(nB, fl, rB);
+        const double eLn = cluster_record_df<M>(nL, fl, rL);
+        if (eBn + eLn < e_old) {
             won_total++;
+#pragma unroll
+            for (int q = 0; q < Layout<M>::acc; q++) { aB[q] = nB[q]; aL[q] = nL[q]; }
+#pragma unroll
+            for (int q = 0; q < Layout<M>::ev; q++) { eB[q] = rB[q]; eL[q] = rL[q]; }
+            st.energy[B] = eBn;
+            st.energy[L] = eLn;
             st.label[i] = B;
             st.size[B] += 1;
             st.size[L] -= 1;
             st.stamp[B] = now;
             st.stamp[L] = now;
         } else {
-#pragma unroll
-            for (int q = 0; q < Layout<M>::acc; q++) { aB[q] = saveB[q]; aL[q] = saveL[q]; }
-#pragma unroll
-            for (int q = 0; q < Layout<M>::ev; q++) { eB[q] = sevB[q]; eL[q] = sevL[q]; }
-            st.energy[B] = eB_old;
-            st.energy[L] = eL_old;
             atomicAdd(&st.counters[kCntReverted], 1ull);
         }
     }
@@ -513,15 +704,22 @@ __global__ void __launch_bounds__(256) apply_kernel(DevState st, const int* __re
     warp_count(&st.counters[kCntMoves], won_total);
 }
 
+template <int M>
+__global__ void __launch_bounds__(256) apply_kernel(DevState st, const int* __restrict__ items, int color,
+                                                    int round, int* cand_dest, const unsigned* cand_prio) {
+    apply_range<M>(st, items, color, round, cand_dest, cand_prio, blockIdx.x * blockDim.x + threadIdx.x,
+                   gridDim.x * blockDim.x);
+}
+
 // Next matching round of a step: a proposal whose two clusters were not touched
 // by this step's commits still carries an exact energy change and claims again
 // with a newer epoch; one that lost a cluster to a commit is dropped (its item
 // is evaluated again next sweep).
-__global__ void reclaim_kernel(DevState st, const int* __restrict__ items, int color, int round,
-                               int* __restrict__ cand_dest, const unsigned* __restrict__ cand_prio) {
+ACVD_DEV void reclaim_range(const DevState& st, const int* __restrict__ items, int color, int round, int* cand_dest,
+                            const unsigned* cand_prio, unsigned gtid, unsigned gstride) {
     const unsigned n = st.cand_count[color];
     const unsigned epoch = (unsigned)(color * kRounds + round);
-    for (unsigned j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+    for (unsigned j = gtid; j < n; j += gstride) {
         const int idx = st.cand_list[j];
         const int B = cand_dest[idx];
         if (B < 0) continue;
@@ -536,6 +734,12 @@ __global__ void reclaim_kernel(DevState st, const int* __restrict__ items, int c
     }
 }
 
+__global__ void reclaim_kernel(DevState st, const int* __restrict__ items, int color, int round, int* cand_dest,
+                               const unsigned* cand_prio) {
+    reclaim_range(st, items, color, round, cand_dest, cand_prio, blockIdx.x * blockDim.x + threadIdx.x,
+                  gridDim.x * blockDim.x);
+}
+
 // ---------------------------------------------------------------------------
 // relaxed step (phases without the connectivity constraint): every proposal of
 // the colour class commits at once, except that a cluster is never emptied.
@@ -544,40 +748,60 @@ __global__ void reclaim_kernel(DevState st, const int* __restrict__ items, int c
 // not matter -- and folded into the compensated accumulators by fx_finalize.
 // ---------------------------------------------------------------------------
 
-// item contribution j (the accumulate_item components) in FP64
+// item contribution j (the accumulate_item components) as a double-float: the
+// products w x, A x and T x are formed exactly (TwoProd) and summed compensated
 template <int M>
-ACVD_DEV double contrib(const ItemRec& it, int j) {
+ACVD_DEV df contrib_df(const ItemRec& it, int j) {
     const int rowi[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
-    if (j < 3) return (double)it.w * (double)it.x[j];
-    if (j == 3) return (double)it.w;
-    if (j < 10) return (double)it.A[j - 4];
+    if (j < 3) return two_prod(it.w, it.x[j]);
+    if (j == 3) return df_make(it.w);
+    if (j < 10) return df_make(it.A[j - 4]);
     if (j < 13) {
         const int c = j - 10;
-        return (double)it.A[rowi[c][0]] * it.x[0] + (double)it.A[rowi[c][1]] * it.x[1] +
-               (double)it.A[rowi[c][2]] * it.x[2];
+        return df_add(df_add(two_prod(it.A[rowi[c][0]], it.x[0]), two_prod(it.A[rowi[c][1]], it.x[1])),
+                      two_prod(it.A[rowi[c][2]], it.x[2]));
     }
-    if (j < 19) return (double)it.T[j - 13];
+    if (j < 19) return df_make(it.T[j - 13]);
     const int c = j - 19;
-    return (double)it.T[rowi[c][0]] * it.x[0] + (double)it.T[rowi[c][1]] * it.x[1] + (double)it.T[rowi[c][2]] * it.x[2];
+    return df_add(df_add(two_prod(it.T[rowi[c][0]], it.x[0]), two_prod(it.T[rowi[c][1]], it.x[1])),
+                  two_prod(it.T[rowi[c][2]], it.x[2]));
 }
 
-__global__ void relaxed_count_kernel(DevState st, const int* __restrict__ items, int color,
-                                     const int* __restrict__ cand_dest) {
+// Fixed-point units of component q: the scale is a power of two 2^e held as two
+// float factors (x, y; inverses in z, w), so both conversions are exact scalings.
+ACVD_DEV long long to_fixed(df v, float4 p) {
+    const float h = __fmul_rn(__fmul_rn(v.hi, p.x), p.y);
+    const float l = __fmul_rn(__fmul_rn(v.lo, p.x), p.y);
+    return __float2ll_rn(h) + __float2ll_rn(l);
+}
+
+ACVD_DEV df from_fixed(long long d, float4 p) {
+    const float h = __ll2float_rn(d);
+    const float l = __ll2float_rn(d - __float2ll_rn(h));
+    return df_renorm(__fmul_rn(__fmul_rn(h, p.z), p.w), __fmul_rn(__fmul_rn(l, p.z), p.w));
+}
+
+ACVD_DEV void relaxed_count_range(const DevState& st, const int* __restrict__ items, int color, unsigned gtid,
+                                  unsigned gstride) {
     const unsigned n = st.cand_count[color];
-    for (unsigned j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+    for (unsigned j = gtid; j < n; j += gstride) {
         const int L = st.label[items[st.cand_list[j]]];
         if (L < st.k) atomicAdd(&st.out_cnt[L], 1);
     }
 }
 
+__global__ void relaxed_count_kernel(DevState st, const int* __restrict__ items, int color) {
+    relaxed_count_range(st, items, color, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
+}
+
 template <int M>
-__global__ void relaxed_commit_kernel(DevState st, const int* __restrict__ items, int color,
-                                      const int* __restrict__ cand_dest) {
+ACVD_DEV void relaxed_commit_range(const DevState& st, const int* __restrict__ items, int color,
+                                   const int* cand_dest, unsigned gtid, unsigned gstride) {
     constexpr int NA = Layout<M>::acc;
     const unsigned n = st.cand_count[color];
     unsigned won = 0;
     const int now = st.sweep->sweep;
-    for (unsigned j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+    for (unsigned j = gtid; j < n; j += gstride) {
         const int idx = st.cand_list[j];
         const int i = items[idx];
         const int B = cand_dest[idx];
@@ -592,45 +816,66 @@ __global__ void relaxed_commit_kernel(DevState st, const int* __restrict__ items
         atomicAdd(&st.in_done[B], 1);
         st.stamp[B] = now;
         long long* dB = st.fx_delta + (int64_t)B * NA;
-#pragma unroll
-        for (int q = 0; q < NA; q++) {
-            const long long v = __double2ll_rn(contrib<M>(it, q) * st.fx_scale[q]);
-            atomicAdd((unsigned long long*)&dB[q], (unsigned long long)v);
-        }
+        long long* dL = st.fx_delta + (int64_t)(L < st.k ? L : 0) * NA;
         if (L < st.k) {
             atomicAdd(&st.out_done[L], 1);
             st.stamp[L] = now;
-            long long* dL = st.fx_delta + (int64_t)L * NA;
+        }
 #pragma unroll
-            for (int q = 0; q < NA; q++) {
-                const long long v = __double2ll_rn(contrib<M>(it, q) * st.fx_scale[q]);
-                atomicAdd((unsigned long long*)&dL[q], (unsigned long long)(-v));
-            }
+        for (int q = 0; q < NA; q++) {
+            const long long v = to_fixed(contrib_df<M>(it, q), st.fx_pow[q]);
+            atomicAdd((unsigned long long*)&dB[q], (unsigned long long)v);
+            if (L < st.k) atomicAdd((unsigned long long*)&dL[q], (unsigned long long)(-v));
         }
     }
     warp_count(&st.counters[kCntMoves], won);
 }
 
 template <int M>
-__global__ void fx_finalize_kernel(DevState st) {
+__global__ void relaxed_commit_kernel(DevState st, const int* __restrict__ items, int color, const int* cand_dest) {
+    relaxed_commit_range<M>(st, items, color, cand_dest, blockIdx.x * blockDim.x + threadIdx.x,
+                            gridDim.x * blockDim.x);
+}
+
+template <int M>
+ACVD_DEV void fx_finalize_range(const DevState& st, int64_t k0, int64_t kstride) {
     constexpr int NA = Layout<M>::acc;
-    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= st.k) return;
-    const int in = st.in_done[k], out = st.out_done[k];
-    st.out_cnt[k] = 0;
-    if (in == 0 && out == 0) return;
-    st.in_done[k] = 0;
-    st.out_done[k] = 0;
-    st.size[k] += in - out;
-    df* a = st.acc + k * NA;
-    long long* d = st.fx_delta + k * NA;
+    for (int64_t k = k0; k < st.k; k += kstride) {
+        const int in = st.in_done[k], out = st.out_done[k];
+        st.out_cnt[k] = 0;
+        if (in == 0 && out == 0) continue;
+        st.in_done[k] = 0;
+        st.out_done[k] = 0;
+        st.size[k] += in - out;
+        df* a = st.acc + k * NA;
+        long long* d = st.fx_delta + k * NA;
+        // every load first (independent), then the arithmetic, then the stores
+        df al[NA];
+        long long dl[NA];
 #pragma unroll
-    for (int q = 0; q < NA; q++) {
-        const double v = (double)d[q] / st.fx_scale[q];
-        d[q] = 0;
-        a[q] = df_add(a[q], df_from_d(v));
+        for (int q = 0; q < NA; q++) {
+            al[q] = a[q];
+            dl[q] = d[q];
+        }
+#pragma unroll
+        for (int q = 0; q < NA; q++) al[q] = df_add(al[q], from_fixed(dl[q], st.fx_pow[q]));
+        float4 el[Layout<M>::ev];
+        const double e = cluster_record_df<M>(al, *st.flags, el);
+        float4* ev = st.ev + k * Layout<M>::ev;
+#pragma unroll
+        for (int q = 0; q < NA; q++) {
+            a[q] = al[q];
+            d[q] = 0;
+        }
+#pragma unroll
+        for (int q = 0; q < Layout<M>::ev; q++) ev[q] = el[q];
+        st.energy[k] = e;
     }
-    update_cluster<M, false>(st, (int)k);
+}
+
+template <int M>
+__global__ void fx_finalize_kernel(DevState st) {
+    fx_finalize_range<M>(st, (int64_t)blockIdx.x * blockDim.x + threadIdx.x, (int64_t)gridDim.x * blockDim.x);
 }
 
 // per accumulator component: the largest |contribution| over the items (as float
@@ -646,7 +891,7 @@ __global__ void fx_maxabs_kernel(DevState st, unsigned* __restrict__ maxbits) {
         ItemRec it;
         load_item<M>(st, (int)i, it);
 #pragma unroll
-        for (int q = 0; q < NA; q++) mx[q] = (float)fabs(contrib<M>(it, q));
+        for (int q = 0; q < NA; q++) mx[q] = fabsf(contrib_df<M>(it, q).hi);
     }
 #pragma unroll
     for (int q = 0; q < NA; q++) {
@@ -661,6 +906,171 @@ __global__ void begin_sweep_kernel(DevState st, int ncolors) {
     const int t = threadIdx.x;
     if (t == 0) st.sweep->sweep += 1;
     if (t < ncolors) st.cand_count[t] = 0u;
+}
+
+// ---------------------------------------------------------------------------
+// Persistent sweep kernel: the sweeps between two convergence events in one
+// cooperative launch.  Each phase of a sweep (claim reset, evaluation, commit
+// steps, finalisation, energy sum) is a grid-stride pass over the same device
+// functions as the per-phase kernels, in the same order, with a grid barrier
+// between phases, so both schedules give bitwise the same clustering.  Block 0
+// takes the host loop's after-sweep decisions (relaxed -> exact switch, move
+// count, convergence test, sweep cap); the other blocks read them after the
+// sweep's last barrier.
+// ---------------------------------------------------------------------------
+constexpr long long kBarrierSpins = 1ll << 24;   // about 1-2 s of 64 ns naps
+
+ACVD_DEV unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+ACVD_DEV unsigned ld_acquire(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Every thread of every block calls it.  Writes made by any thread before the
+// barrier are visible to every thread after it (release fence before the
+// arrival, acquire load of the generation, fence after).  A wait that runs out
+// of spins sets the error flag; every later call then returns false and the
+// kernel ends.
+ACVD_DEV bool grid_barrier(GridBar* b) {
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const unsigned g = ld_acquire(&b->gen);
+        __threadfence();
+        const unsigned arrived = atomicAdd(&b->count, 1u) + 1u;
+        int ok = 1;
+        if (arrived == gridDim.x) {
+            atomicExch(&b->count, 0u);
+            __threadfence();
+            atomicAdd(&b->gen, 1u);
+        } else {
+            long long spins = 0;
+            while (ld_acquire(&b->gen) == g) {
+                if (*(volatile int*)&b->err) {   // another block gave up already
+                    ok = 0;
+                    break;
+                }
+                if (++spins > kBarrierSpins) {
+                    atomicExch(&b->err, 1);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+        if (*(volatile int*)&b->err) ok = 0;
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+template <int M>
+__global__ void __launch_bounds__(256, 2) sweep_run_kernel(SweepRun a) {
+    const DevState& st = a.st;
+    const unsigned gtid = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned gstride = gridDim.x * blockDim.x;
+    const bool lead = blockIdx.x == 0 && threadIdx.x == 0;
+    volatile LoopState* vls = a.ls;
+    for (;;) {
+        const bool relaxed = vls->relaxed_ok && !st.flags->connexity;
+        if (lead) {
+            st.sweep->sweep += 1;
+            for (int c = 0; c < a.nclasses; c++) st.cand_count[c] = 0u;
+            st.counters[kCntMoves] = 0ull;
+        }
+        if (!grid_barrier(a.bar)) return;
+        for (int c = 0; c < a.nclasses; c++) {
+            const long long o0 = a.off[c];
+            const int64_t cnt = a.off[c + 1] - o0;
+            if (cnt == 0) continue;
+            const int* items = a.items + o0;
+            if (!relaxed) {
+                for (int64_t k = gtid; k <= st.k; k += gstride) st.claim[k] = ~0ull;
+                if (!grid_barrier(a.bar)) return;
+            }
+            const unsigned long long t0 = lead ? global_ns() : 0ull;
+            const int64_t ntiles = (cnt + 255) / 256;
+            for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x)
+                eval_tile<M>(st, items, cnt, c, a.cand_dest, a.cand_prio, relaxed ? 0 : 1, t);
+            if (!grid_barrier(a.bar)) return;
+            if (lead) a.ls->eval_ns += global_ns() - t0;
+            if (relaxed) {
+                relaxed_count_range(st, items, c, gtid, gstride);
+                if (!grid_barrier(a.bar)) return;
+                relaxed_commit_range<M>(st, items, c, a.cand_dest, gtid, gstride);
+                if (!grid_barrier(a.bar)) return;
+                fx_finalize_range<M>(st, gtid, gstride);
+                if (!grid_barrier(a.bar)) return;
+            } else {
+                apply_range<M>(st, items, c, 0, a.cand_dest, a.cand_prio, gtid, gstride);
+                if (!grid_barrier(a.bar)) return;
+                for (int r = 1; r < a.match_rounds; r++) {
+                    reclaim_range(st, items, c, r, a.cand_dest, a.cand_prio, gtid, gstride);
+                    if (!grid_barrier(a.bar)) return;
+                    apply_range<M>(st, items, c, r, a.cand_dest, a.cand_prio, gtid, gstride);
+                    if (!grid_barrier(a.bar)) return;
+                }
+            }
+        }
+        double e_now = 0.0;
+        if (relaxed) {
+            // the energy after the sweep, in sum_f64's tree
+            const int64_t per = (int64_t)kSumThreads * kSumPer;
+            int64_t nb = ((int64_t)st.k + per - 1) / per;
+            if (nb < 1) nb = 1;
+            double* pa = a.esum;
+            double* pb = a.esum + nb + 1;
+            for (int64_t ch = blockIdx.x; ch < nb; ch += gridDim.x) sum_f64_chunk(st.energy, st.k, ch, pa);
+            if (!grid_barrier(a.bar)) return;
+            const double* cur = pa;
+            int64_t m = nb;
+            double* dst = pb;
+            double* other = pa;
+            while (m > 1) {
+                const int64_t mb = (m + per - 1) / per;
+                for (int64_t ch = blockIdx.x; ch < mb; ch += gridDim.x) sum_f64_chunk(cur, m, ch, dst);
+                if (!grid_barrier(a.bar)) return;
+                cur = dst;
+                m = mb;
+                double* t = dst;
+                dst = other;
+                other = t;
+            }
+            if (lead) e_now = *(volatile const double*)cur;
+        }
+        if (lead) {
+            LoopState* L = a.ls;
+            const long long mods = (long long)*(volatile unsigned long long*)&st.counters[kCntMoves];
+            if (relaxed) {
+                if (L->have_prev && !(e_now < L->e_prev)) L->relaxed_ok = 0;
+                L->e_prev = e_now;
+                L->have_prev = 1;
+                L->relaxed_run += 1;
+            }
+            if (L->sweeps < a.log_cap) {
+                SweepLog& g = a.log[L->sweeps];
+                g.moves = mods;
+                g.energy = e_now;
+                g.relaxed = relaxed ? 1 : 0;
+            }
+            L->sweeps += 1;
+            L->run += 1;
+            L->moves += mods;
+            L->last_moves = mods;
+            if (mods == 0 || L->sweeps > L->max_loops || (mods <= L->early / 1000 && L->convergences <= 1))
+                L->status = 1;
+        }
+        if (!grid_barrier(a.bar)) return;
+        if (vls->status != 0) return;
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -950,9 +1360,9 @@ cudaError_t launch_relaxed_step(int metric, const DevState& st, const int* items
                                 const int* cand_dest, cudaStream_t s) {
     if (count == 0) return cudaSuccess;
     ++g_launches;
-    relaxed_count_kernel<<<list_grid(count), 256, 0, s>>>(st, items, color, cand_dest);
+    relaxed_count_kernel<<<list_grid(count), 256, 0, s>>>(st, items, color);
     ACVD_DISPATCH(metric, relaxed_commit_kernel, list_grid(count), 256, s, st, items, color, cand_dest);
-    ACVD_DISPATCH(metric, fx_finalize_kernel, nblk(st.k), 256, s, st);
+    ACVD_DISPATCH(metric, fx_finalize_kernel, nblk(st.k, 64), 64, s, st);   // small blocks: every SM gets some
     return cudaGetLastError();
 }
 
@@ -966,6 +1376,25 @@ cudaError_t launch_begin_sweep(const DevState& st, int ncolors, cudaStream_t s) 
     ++g_launches;
     begin_sweep_kernel<<<1, 64, 0, s>>>(st, ncolors);
     return cudaGetLastError();
+}
+
+int sweep_run_blocks_per_sm(int metric) {
+    int nb = 0;
+    cudaError_t e;
+    if (metric == kIso) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, sweep_run_kernel<kIso>, 256, 0);
+    else if (metric == kQEM) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, sweep_run_kernel<kQEM>, 256, 0);
+    else e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, sweep_run_kernel<kAniso>, 256, 0);
+    return e == cudaSuccess ? nb : 0;
+}
+
+cudaError_t launch_sweep_run(int metric, const SweepRun& a, int grid, cudaStream_t s) {
+    ++g_launches;
+    SweepRun arg = a;
+    void* args[] = {(void*)&arg};
+    const void* fn = metric == kIso ? (const void*)sweep_run_kernel<kIso>
+                     : metric == kQEM ? (const void*)sweep_run_kernel<kQEM>
+                                      : (const void*)sweep_run_kernel<kAniso>;
+    return cudaLaunchCooperativeKernel(fn, dim3((unsigned)grid), dim3(256), args, 0, s);
 }
 
 cudaError_t launch_update_all(int metric, const DevState& st, cudaStream_t s) {

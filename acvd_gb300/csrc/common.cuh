@@ -61,6 +61,41 @@ ACVD_DEV df two_prod(float a, float b) {
 
 ACVD_DEV double df_to_d(df x) { return (double)x.hi + (double)x.lo; }
 
+ACVD_DEV df df_renorm(float s, float e) {
+    float h, l;
+    fast_two_sum(s, e, h, l);
+    return {h, l};
+}
+
+ACVD_DEV df df_sub(df x, df y) { return df_add(x, df_neg(y)); }
+
+// Products and quotient of double-floats (Dekker 1971, "A floating-point
+// technique for extending the available precision"; the same steps as Hida, Li
+// and Bailey's double-double library): one exact TwoProd of the leading parts
+// plus the cross terms, renormalised.  About 2^-47 relative error.
+ACVD_DEV df df_mul(df x, df y) {
+    df p = two_prod(x.hi, y.hi);
+    p.lo = __fmaf_rn(x.hi, y.lo, p.lo);
+    p.lo = __fmaf_rn(x.lo, y.hi, p.lo);
+    return df_renorm(p.hi, p.lo);
+}
+
+ACVD_DEV df df_mul_f(df x, float y) {
+    df p = two_prod(x.hi, y);
+    p.lo = __fmaf_rn(x.lo, y, p.lo);
+    return df_renorm(p.hi, p.lo);
+}
+
+// x / y: a float quotient, then one correction from the remainder x - y q1
+ACVD_DEV df df_div(df x, df y) {
+    const float q1 = __fdiv_rn(x.hi, y.hi);
+    const df r = df_sub(x, df_mul_f(y, q1));
+    const float q2 = __fdiv_rn(r.hi, y.hi);
+    return df_renorm(q1, q2);
+}
+
+
+
 ACVD_DEV df df_from_d(double v) {
     const float h = __double2float_rn(v);
     const float l = __double2float_rn(v - (double)h);

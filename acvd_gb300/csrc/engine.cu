@@ -3,6 +3,7 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstdlib>
+#include <chrono>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -84,7 +85,7 @@ struct acvd_ctx {
     DBuf<SweepState> dsweep;
     // relaxed steps
     DBuf<long long> fx_delta;
-    DBuf<double> fx_scale;
+    DBuf<float4> fx_pow;
     DBuf<int> out_cnt, in_done, out_done;
     bool use_relaxed = true;       // ACVD_RELAXED=0 turns relaxed steps off
     DBuf<df> acc;
@@ -115,6 +116,16 @@ struct acvd_ctx {
     int64_t exact_kernels = 0, relaxed_kernels = 0;
     DBuf<int> label_init;          // the assignment given to acvd_set_labels (for acvd_rewind)
 
+    // persistent sweep kernel: loop state, grid barrier, energy partials, class
+    // offsets, per-sweep log; grid = SMs x co-resident blocks (0: not available)
+    DBuf<LoopState> dls;
+    DBuf<GridBar> dbar;
+    DBuf<double> esum;
+    DBuf<long long> doff;
+    DBuf<SweepLog> slog;
+    int run_grid = -1;
+    int run_grid_metric = -1;
+
     DevState state() {
         DevState st;
         st.n = nV;
@@ -141,7 +152,7 @@ struct acvd_ctx {
         st.cand_list = cand_list.p;
         st.cand_count = cand_count.p;
         st.fx_delta = fx_delta.p;
-        st.fx_scale = fx_scale.p;
+        st.fx_pow = fx_pow.p;
         st.out_cnt = out_cnt.p;
         st.in_done = in_done.p;
         st.out_done = out_done.p;
@@ -281,6 +292,7 @@ void acvd_default_opts(acvd_opts* o) {
     o->max_loops = 5000000;
     o->max_convergences = 1000000000;
     o->kernel_timing = 0;
+    o->persistent = 0;
 }
 
 acvd_ctx* acvd_create(const acvd_opts* opts) {
@@ -442,14 +454,20 @@ int acvd_set_metric(acvd_ctx* ctx, int metric, const double* indicator, const fl
         unsigned hb[32];
         CK(cudaMemcpyAsync(hb, maxbits.p, sizeof hb, cudaMemcpyDeviceToHost, ctx->s));
         CK(cudaStreamSynchronize(ctx->s));
-        double sc[32];
+        // the largest power of two 2^e with N * max|contribution| * 2^e < 2^62 (hi part
+        // bound, with a margin for the lo parts), split into two factors 2^e1 2^e2
+        float4 sc[32];
         for (int q = 0; q < 32; q++) {
             float mx;
             std::memcpy(&mx, &hb[q], sizeof mx);
-            sc[q] = mx > 0.f ? std::ldexp(1.0, 62) / ((double)nv * (double)mx * 1.0000001) : 1.0;
+            int e = 0;
+            if (mx > 0.f) e = (int)std::floor(62.0 - std::log2((double)nv * (double)mx * 1.0001));
+            const int e1 = e / 2, e2 = e - e1;
+            sc[q] = make_float4(std::ldexp(1.0f, e1), std::ldexp(1.0f, e2), std::ldexp(1.0f, -e1),
+                                std::ldexp(1.0f, -e2));
         }
-        CK(ctx->fx_scale.resize(32));
-        CK(cudaMemcpyAsync(ctx->fx_scale.p, sc, sizeof sc, cudaMemcpyHostToDevice, ctx->s));
+        CK(ctx->fx_pow.resize(32));
+        CK(cudaMemcpyAsync(ctx->fx_pow.p, sc, sizeof sc, cudaMemcpyHostToDevice, ctx->s));
     }
     CK(cudaStreamSynchronize(ctx->s));
     ctx->ready_metric = true;
@@ -702,6 +720,80 @@ static int run_sweep(acvd_ctx* ctx, bool timing, bool relaxed, double* eval_ms, 
     return ACVD_OK;
 }
 
+constexpr int kSweepLogCap = 1 << 16;
+
+// Grid of the persistent sweep kernel on this device: every SM times the
+// co-resident blocks of the metric's kernel; 0 when cooperative launch is
+// unavailable (the per-phase schedule runs instead).
+static int sweep_run_grid(acvd_ctx* ctx) {
+    if (ctx->run_grid_metric == ctx->metric) return ctx->run_grid;
+    int coop = 0, sms = 0;
+    if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, ctx->opts.device) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->opts.device) != cudaSuccess) {
+        cudaGetLastError();
+        coop = 0;
+    }
+    const int per_sm = coop ? sweep_run_blocks_per_sm(ctx->metric) : 0;
+    ctx->run_grid = coop ? sms * per_sm : 0;
+    ctx->run_grid_metric = ctx->metric;
+    return ctx->run_grid;
+}
+
+// Runs colour sweeps on the device until the host loop's convergence test is
+// met (one cooperative launch).  hl carries the loop state in and out.
+static int run_sweeps_persistent(acvd_ctx* ctx, LoopState& hl, acvd_stats& local) {
+    const int grid = sweep_run_grid(ctx);
+    const int64_t per = 2048;
+    const int64_t nb = std::max<int64_t>(1, (ctx->K + per - 1) / per);
+    CK(ctx->dls.resize(1));
+    CK(ctx->dbar.resize(1));
+    CK(ctx->esum.resize(nb + (nb + per - 1) / per + 2));
+    CK(ctx->doff.resize(ctx->nclasses + 1));
+    CK(ctx->slog.resize(kSweepLogCap));
+    std::vector<long long> off(ctx->sweep_off.begin(), ctx->sweep_off.end());
+    hl.status = 0;
+    hl.run = 0;
+    hl.relaxed_run = 0;
+    hl.moves = 0;
+    hl.last_moves = 0;
+    hl.eval_ns = 0;
+    CK(cudaMemcpyAsync(ctx->dls.p, &hl, sizeof hl, cudaMemcpyHostToDevice, ctx->s));
+    CK(cudaMemsetAsync(ctx->dbar.p, 0, sizeof(GridBar), ctx->s));
+    CK(cudaMemcpyAsync(ctx->doff.p, off.data(), off.size() * sizeof(long long), cudaMemcpyHostToDevice, ctx->s));
+    SweepRun a;
+    a.st = ctx->state();
+    a.items = ctx->sweep_items;
+    a.off = ctx->doff.p;
+    a.nclasses = ctx->nclasses;
+    a.match_rounds = ctx->match_rounds;
+    a.cand_dest = ctx->cand_dest.p;
+    a.cand_prio = ctx->cand_prio.p;
+    a.ls = ctx->dls.p;
+    a.bar = ctx->dbar.p;
+    a.esum = ctx->esum.p;
+    a.log = ctx->slog.p;
+    a.log_cap = kSweepLogCap;
+    CK(cudaEventRecord(ctx->ev0, ctx->s));
+    CK(launch_sweep_run(ctx->metric, a, grid, ctx->s));
+    CK(cudaEventRecord(ctx->ev1, ctx->s));
+    GridBar hb;
+    CK(cudaMemcpyAsync(&hl, ctx->dls.p, sizeof hl, cudaMemcpyDeviceToHost, ctx->s));
+    CK(cudaMemcpyAsync(&hb, ctx->dbar.p, sizeof hb, cudaMemcpyDeviceToHost, ctx->s));
+    int r = sync_counters(ctx);
+    if (r) return r;
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+    local.sweep_kernel_ms += ms;
+    local.sweep_kernel_launches += 1;
+    local.eval_ms += (double)hl.eval_ns * 1e-6;
+    int nonempty = 0;
+    for (int c = 0; c < ctx->nclasses; c++) nonempty += ctx->sweep_off[c + 1] > ctx->sweep_off[c];
+    local.eval_launches += hl.run * nonempty;
+    if (hb.err) return fail(ctx, ACVD_ERR_DEVICE_CHECK, "persistent sweep kernel: a grid barrier wait gave up");
+    if (hl.status != 1) return fail(ctx, ACVD_ERR_DEVICE_CHECK, "persistent sweep kernel ended before its loop test");
+    return ACVD_OK;
+}
+
 // sum of the tracked per-cluster energies (fixed-order FP64 tree)
 static int energy_total(acvd_ctx* ctx, double* out) {
     CK(ctx->dtmp.resize(2));
@@ -762,9 +854,51 @@ extern "C" int acvd_minimize(acvd_ctx* ctx, acvd_stats* stats) {
         bool have_prev = false;
         if (relaxed_ok && (r = energy_total(ctx, &e_prev))) { status = r; break; }
         have_prev = relaxed_ok;
+        const bool trace = std::getenv("ACVD_TRACE") != nullptr;
+        auto t_trace = std::chrono::steady_clock::now();
+        const bool persistent = ctx->opts.persistent && sweep_run_grid(ctx) > 0;
         for (;;) {
             int64_t mods = 0;
             const bool relaxed = relaxed_ok && !ctx->flags.connexity;
+            if (persistent) {
+                // every sweep up to the next convergence test, on the device
+                LoopState hl;
+                std::memset(&hl, 0, sizeof hl);
+                hl.early = early;
+                hl.sweeps = sweeps;
+                hl.max_loops = ctx->opts.max_loops;
+                hl.convergences = convergences;
+                hl.relaxed_ok = relaxed_ok ? 1 : 0;
+                hl.have_prev = have_prev ? 1 : 0;
+                hl.e_prev = e_prev;
+                if ((r = run_sweeps_persistent(ctx, hl, local))) { status = r; break; }
+                if (trace) {
+                    const int first = sweeps, last = std::min(hl.sweeps, kSweepLogCap);
+                    std::vector<SweepLog> lg(std::max(0, last - first));
+                    if (!lg.empty() &&
+                        cudaMemcpy(lg.data(), ctx->slog.p + first, lg.size() * sizeof(SweepLog),
+                                   cudaMemcpyDeviceToHost) != cudaSuccess) {
+                        status = fail(ctx, ACVD_ERR_CUDA, "trace log copy failed");
+                        break;
+                    }
+                    const auto now = std::chrono::steady_clock::now();
+                    std::fprintf(stderr, "acvd persistent run: sweeps %d-%d in %.3f ms (device eval %.3f ms)\n",
+                                 first + 1, hl.sweeps, std::chrono::duration<double, std::milli>(now - t_trace).count(),
+                                 hl.eval_ns * 1e-6);
+                    for (size_t q = 0; q < lg.size(); q++)
+                        std::fprintf(stderr, "acvd sweep %d %s moves %lld energy %.17g conv %d flags %d%d\n",
+                                     first + 1 + (int)q, lg[q].relaxed ? "relaxed" : "exact", lg[q].moves,
+                                     lg[q].energy, convergences, ctx->flags.constrained, ctx->flags.connexity);
+                    t_trace = now;
+                }
+                sweeps = hl.sweeps;
+                relaxed_ok = hl.relaxed_ok != 0;
+                have_prev = hl.have_prev != 0;
+                e_prev = hl.e_prev;
+                local.relaxed_sweeps += hl.relaxed_run;
+                local.moves += hl.moves;
+                mods = hl.last_moves;
+            } else {
             if ((r = run_sweep(ctx, timing, relaxed, &local.eval_ms, &local.eval_launches, &mods))) { status = r; break; }
             if (relaxed) {
                 local.relaxed_sweeps++;
@@ -776,12 +910,19 @@ extern "C" int acvd_minimize(acvd_ctx* ctx, acvd_stats* stats) {
             }
             sweeps++;
             local.moves += mods;
-            if (std::getenv("ACVD_TRACE"))
+            }
+            if (trace && !persistent) {
+                const auto now = std::chrono::steady_clock::now();
                 std::fprintf(stderr,
-                             "acvd sweep %d moves %lld cand %llu boundary %llu targets %llu reverted %llu conv %d flags %d%d\n",
-                             sweeps, (long long)mods, ctx->h_counters[kCntCand], ctx->h_counters[kCntBoundary],
-                             ctx->h_counters[kCntTargets], ctx->h_counters[kCntReverted], convergences,
+                             "acvd sweep %d %s %.3f ms moves %lld cand %llu boundary %llu targets %llu visited %llu "
+                             "reverted %llu conv %d flags %d%d\n",
+                             sweeps, relaxed ? "relaxed" : "exact",
+                             std::chrono::duration<double, std::milli>(now - t_trace).count(), (long long)mods,
+                             ctx->h_counters[kCntCand], ctx->h_counters[kCntBoundary], ctx->h_counters[kCntTargets],
+                             ctx->h_counters[kCntVisited], ctx->h_counters[kCntReverted], convergences,
                              ctx->flags.constrained, ctx->flags.connexity);
+                t_trace = now;
+            }
             if (mods == 0 || sweeps > ctx->opts.max_loops || (mods <= early / 1000 && convergences <= 1)) {
                 bool flags_changed = false;
                 if (ctx->unconstrained && convergences == 0 && ctx->metric == kQEM) {

@@ -133,26 +133,9 @@ cudaError_t exclusive_scan_u32_raw(const uint32_t* in, uint32_t* out, int64_t n,
 // ---------------------------------------------------------------------------
 // deterministic FP64 sum: fixed-shape tree (256-thread blocks, 8 values/thread)
 // ---------------------------------------------------------------------------
-constexpr int kSumThreads = 256;
-constexpr int kSumPer = 8;
 
 __global__ void sum_f64_kernel(const double* __restrict__ in, int64_t n, double* __restrict__ out) {
-    __shared__ double sh[kSumThreads];
-    const int tid = threadIdx.x;
-    const int64_t base = (int64_t)blockIdx.x * kSumThreads * kSumPer;
-    double acc = 0.0;
-#pragma unroll
-    for (int k = 0; k < kSumPer; k++) {
-        const int64_t i = base + (int64_t)k * kSumThreads + tid;
-        if (i < n) acc += in[i];
-    }
-    sh[tid] = acc;
-    __syncthreads();
-    for (int o = kSumThreads / 2; o > 0; o >>= 1) {
-        if (tid < o) sh[tid] += sh[tid + o];
-        __syncthreads();
-    }
-    if (tid == 0) out[blockIdx.x] = sh[0];
+    sum_f64_chunk(in, n, blockIdx.x, out);
 }
 
 cudaError_t sum_f64(const double* in, int64_t n, double* out_dev, Scratch& scratch, cudaStream_t s) {

@@ -37,6 +37,34 @@ cudaError_t exclusive_scan_u32_raw(const uint32_t* in, uint32_t* out, int64_t n,
 // Deterministic sum of n doubles (fixed reduction tree) into *out_dev.
 cudaError_t sum_f64(const double* in, int64_t n, double* out_dev, Scratch& scratch, cudaStream_t s);
 
+#ifdef __CUDACC__
+// One chunk of the deterministic FP64 sum: 256 threads (the whole block, every
+// thread calls it) add values chunk*2048 .. +2047 in a fixed tree; out[chunk]
+// receives the chunk's sum.  sum_f64 applies it level by level.
+constexpr int kSumThreads = 256;
+constexpr int kSumPer = 8;
+
+__device__ __forceinline__ void sum_f64_chunk(const double* in, int64_t n, int64_t chunk, double* out) {
+    __shared__ double sh[kSumThreads];
+    const int tid = threadIdx.x;
+    const int64_t base = chunk * kSumThreads * kSumPer;
+    double acc = 0.0;
+#pragma unroll
+    for (int k = 0; k < kSumPer; k++) {
+        const int64_t i = base + (int64_t)k * kSumThreads + tid;
+        if (i < n) acc += in[i];
+    }
+    __syncthreads();   // a previous chunk of this block is done with sh
+    sh[tid] = acc;
+    __syncthreads();
+    for (int o = kSumThreads / 2; o > 0; o >>= 1) {
+        if (tid < o) sh[tid] += sh[tid + o];
+        __syncthreads();
+    }
+    if (tid == 0) out[chunk] = sh[0];
+}
+#endif
+
 // Number of bits needed to represent values in [0, v].
 inline int bits_for(uint64_t v) {
     int b = 1;

@@ -101,10 +101,63 @@ struct DevState {
     // relaxed steps: per cluster, exact fixed-point sums of the committed moves'
     // contributions (order-independent, hence deterministic with atomics)
     long long* fx_delta;   // K x acc stride
-    const double* fx_scale;  // per accumulator component: fixed-point units per unit
+    const float4* fx_pow;  // per accumulator component: fixed-point scale 2^e as two float factors
+                           // (x, y) and their inverses (z, w)
     int* out_cnt;          // proposals leaving the cluster in this step
     int* in_done;          // committed moves into the cluster
     int* out_done;         // committed moves out of the cluster
+};
+
+// Persistent sweep kernel: the loop that runs colour sweeps back to back on the
+// device between two convergence events.  Host-written fields are marked "in";
+// the kernel updates the others (block 0 decides after each sweep, every block
+// reads the decision after a grid barrier).
+struct LoopState {
+    long long early;          // in: items of non-frozen clusters (base of the early-convergence test)
+    long long moves;          // out: moves committed by this launch's sweeps
+    long long last_moves;     // out: moves of the last sweep
+    double e_prev;            // in/out: energy after the previous relaxed sweep
+    unsigned long long eval_ns;  // out: device time spent in the evaluation phases
+    int sweeps;               // in/out: sweeps of this minimisation so far
+    int max_loops;            // in: sweep cap
+    int convergences;         // in: convergence events so far
+    int relaxed_ok;           // in/out: relaxed sweeps allowed
+    int have_prev;            // in/out: e_prev is valid
+    int relaxed_run;          // out: relaxed sweeps run by this launch
+    int run;                  // out: sweeps run by this launch
+    int status;               // out: 0 running, 1 convergence test met, 2 grid barrier gave up
+};
+
+// Grid-wide barrier of the persistent kernel (all blocks co-resident: cooperative launch).
+struct GridBar {
+    unsigned count;           // blocks arrived in the current generation
+    unsigned gen;             // generation, bumped by the last block to arrive
+    int err;                  // set when a wait gave up
+    int pad;
+};
+
+// One record per sweep (trace output).
+struct SweepLog {
+    long long moves;
+    double energy;            // relaxed sweeps: the energy after the sweep
+    int relaxed;
+    int pad;
+};
+
+// Arguments of the persistent sweep kernel.
+struct SweepRun {
+    DevState st;
+    const int* items;         // sweep classes, concatenated
+    const long long* off;     // class offsets (nclasses + 1)
+    int nclasses;
+    int match_rounds;
+    int* cand_dest;
+    unsigned* cand_prio;
+    LoopState* ls;
+    GridBar* bar;
+    double* esum;             // energy-sum partials: ceil(K/2048) + ceil(K/2048^2) + 2 doubles
+    SweepLog* log;
+    int log_cap;
 };
 
 // ---- items / topology (topology.cu) ----
@@ -136,6 +189,10 @@ cudaError_t launch_apply(int metric, const DevState& st, const int* items, int64
                          int* cand_dest, const unsigned* cand_prio, cudaStream_t s);
 cudaError_t launch_reclaim(const DevState& st, const int* items, int64_t count, int color, int round,
                            int* cand_dest, const unsigned* cand_prio, cudaStream_t s);
+// Persistent sweep kernel (cooperative launch).  blocks_per_sm: co-resident
+// blocks per SM for this metric (0 when the kernel cannot be co-resident).
+int sweep_run_blocks_per_sm(int metric);
+cudaError_t launch_sweep_run(int metric, const SweepRun& a, int grid, cudaStream_t s);
 cudaError_t launch_update_all(int metric, const DevState& st, cudaStream_t s);
 cudaError_t launch_cluster_keys(const DevState& st, uint32_t* keys, uint32_t* vals, uint32_t* counts,
                                 cudaStream_t s);

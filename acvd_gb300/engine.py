@@ -28,7 +28,7 @@ class AcvdError(RuntimeError):
 
 class Opts(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int), ("use_graphs", ctypes.c_int), ("max_loops", ctypes.c_int),
-                ("max_convergences", ctypes.c_int), ("kernel_timing", ctypes.c_int)]
+                ("max_convergences", ctypes.c_int), ("kernel_timing", ctypes.c_int), ("persistent", ctypes.c_int)]
 
 
 class Stats(ctypes.Structure):
@@ -38,7 +38,8 @@ class Stats(ctypes.Structure):
                 ("disconnected", ctypes.c_int), ("unassigned", ctypes.c_int), ("device_ms", ctypes.c_double),
                 ("eval_ms", ctypes.c_double), ("eval_launches", ctypes.c_int), ("energy", ctypes.c_double),
                 ("eval_bytes", ctypes.c_int64), ("kernel_launches", ctypes.c_int64), ("hit_loop_cap", ctypes.c_int),
-                ("reverted", ctypes.c_int64), ("relaxed_sweeps", ctypes.c_int)]
+                ("reverted", ctypes.c_int64), ("relaxed_sweeps", ctypes.c_int), ("sweep_kernel_ms", ctypes.c_double),
+                ("sweep_kernel_launches", ctypes.c_int)]
 
     def as_dict(self) -> dict:
         return {name: getattr(self, name) for name, _ in self._fields_}
@@ -168,12 +169,13 @@ class Engine:
     DEFAULT_MAX_LOOPS = 20000
 
     def __init__(self, device: int = 0, use_graphs: bool = True, kernel_timing: bool = False,
-                 max_loops: int | None = DEFAULT_MAX_LOOPS):
+                 max_loops: int | None = DEFAULT_MAX_LOOPS, persistent: bool = False):
         lib = load()
         o = Opts()
         lib.acvd_default_opts(ctypes.byref(o))
         o.device = device
         o.use_graphs = 1 if use_graphs else 0
+        o.persistent = 1 if persistent else 0
         o.kernel_timing = 1 if kernel_timing else 0
         if max_loops is not None:
             o.max_loops = int(max_loops)

@@ -49,6 +49,8 @@ typedef struct acvd_opts {
     int max_loops;           /* sweep cap; reference MaxNumberOfLoops = 5,000,000 (:1407) */
     int max_convergences;    /* reference MaxNumberOfConvergences = 1e9 (:1406) */
     int kernel_timing;       /* record CUDA events around every evaluation kernel */
+    int persistent;          /* run the sweeps between two convergence events in one cooperative
+                                kernel with grid barriers (0, default; needs cooperative launch) */
 } acvd_opts;
 
 typedef struct acvd_stats {
@@ -63,7 +65,8 @@ typedef struct acvd_stats {
     int disconnected;         /* clusters split at the last convergence */
     int unassigned;           /* items left unassigned after hole filling */
     double device_ms;         /* MinimizeEnergy on the device (CUDA events) */
-    double eval_ms;           /* sum of evaluation-kernel times (kernel_timing only) */
+    double eval_ms;           /* evaluation time: CUDA events per evaluation kernel (kernel_timing), or the
+                                 device clock around the persistent kernel's evaluation phases */
     int eval_launches;        /* evaluation kernels timed */
     double energy;            /* global energy (FP64) of the final clustering */
     int64_t eval_bytes;       /* algorithmic bytes of all evaluation kernels (counted on device) */
@@ -71,9 +74,11 @@ typedef struct acvd_stats {
     int hit_loop_cap;         /* 1 if max_loops ended the minimisation (the reference just stops there too) */
     int64_t reverted;         /* commits undone because the pair's tracked energy did not decrease */
     int relaxed_sweeps;       /* sweeps run in relaxed (multi-move) mode */
+    double sweep_kernel_ms;   /* persistent sweep kernels: CUDA-event time of all their launches */
+    int sweep_kernel_launches; /* persistent sweep kernels launched (0 on the per-phase schedule) */
 } acvd_stats;
 
-/* Defaults: device 0, graphs on, the reference's loop caps. */
+/* Defaults: device 0, graphs on, per-phase kernels, the reference's loop caps. */
 void acvd_default_opts(acvd_opts* opts);
 
 acvd_ctx* acvd_create(const acvd_opts* opts);

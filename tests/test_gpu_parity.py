@@ -213,3 +213,35 @@ def test_batched_meshes_match_individual_runs(oracle_lib):
         assert chk.clean() == 0
         assert abs(mesh_e[m] - e_gpu) < REL_ACC * abs(e_gpu)
     e.close()
+
+
+@pytest.mark.parametrize("case", [RUNS[0], RUNS[2], RUNS[4]], ids=[RUNS[i][0] for i in (0, 2, 4)])
+def test_persistent_schedule_matches_per_phase_kernels(oracle_lib, case):
+    """The persistent sweep kernel (one cooperative launch per phase of the
+    minimisation) runs the same device functions in the same order as the
+    per-phase kernels: the clusterings, energies and counts are identical."""
+    name, metric, mk, k, grad, uinit, seeds = case
+    m = mk()
+    ind = m.indicator if (grad > 0 or metric == "aniso") else None
+    pd = m.principal_dirs if metric == "aniso" else None
+    init = synth.seed_labels(m.n_points, k, seed=11) if seeds else None
+    ref = oracle_lib.Port(metric, m.points, m.faces, k, grad, ind, pd, unconstrained_init=uinit)
+    ref.init(init)
+    lab0 = ref.labels()
+    row, col, ev = acvd_gb300.build_topology(m.n_points, m.faces)
+    out = []
+    for persistent in (True, False):
+        e = acvd_gb300.Engine(persistent=persistent)
+        e.set_mesh(m.points, m.faces, row, col, ev)
+        e.set_metric(metric, ind, pd, grad)
+        e.set_unconstrained_initialization(uinit)
+        e.set_labels(k, lab0)
+        st = e.minimize()
+        out.append((e.labels(), st))
+        e.close()
+    (lab_p, st_p), (lab_k, st_k) = out
+    assert st_p["sweep_kernel_launches"] >= 1 and st_k["sweep_kernel_launches"] == 0
+    np.testing.assert_array_equal(lab_p, lab_k)
+    for key in ("sweeps", "moves", "relaxed_sweeps", "convergences", "candidates", "reverted"):
+        assert st_p[key] == st_k[key], (key, st_p[key], st_k[key])
+    assert st_p["energy"] == st_k["energy"]
