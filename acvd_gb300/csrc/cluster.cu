@@ -435,6 +435,8 @@ ACVD_DEV void eval_tile(const DevState& st, const int* __restrict__ items, int64
                 const unsigned long long c = make_claim((unsigned)epoch, pr, (unsigned)widx);
                 if (L < st.k) atomicMin(&st.claim[L], c);
                 atomicMin(&st.claim[best], c);
+            } else if (L < st.k) {
+                atomicAdd(&st.out_cnt[L], 1);   // relaxed step: proposals leaving L
             }
             n_cand = 1;
             my_cand = widx;
@@ -633,14 +635,19 @@ ACVD_DEV void update_cluster(const DevState& st, int k) {
 // apply: commit the proposals that hold both claims (grid-stride over the
 // step's compact proposal list)
 // ---------------------------------------------------------------------------
-// gtid / gstride: this thread's position and the number of threads walking the list
+// gtid / gstride: this thread's position and the number of threads walking the
+// list.  A lane pair handles one proposal: the even lane the destination
+// cluster B, the odd lane the source cluster L; the pair exchanges the two new
+// energies and both take the same decision.
 template <int M>
 ACVD_DEV void apply_range(const DevState& st, const int* __restrict__ items, int color, int round, int* cand_dest,
                           const unsigned* cand_prio, unsigned gtid, unsigned gstride) {
     const unsigned n = st.cand_count[color];
     const unsigned epoch = (unsigned)(color * kRounds + round);
+    const int role = (int)(gtid & 1u);
+    const unsigned pair_mask = 3u << ((threadIdx.x & 31u) & ~1u);
     unsigned won_total = 0;
-    for (unsigned j = gtid; j < n; j += gstride) {
+    for (unsigned j = gtid >> 1; j < n; j += gstride >> 1) {
         const int idx = st.cand_list[j];
         const int B = cand_dest[idx];
         if (B < 0) continue;                     // committed or dropped in an earlier round
@@ -648,56 +655,64 @@ ACVD_DEV void apply_range(const DevState& st, const int* __restrict__ items, int
         const int L = st.label[i];
         const unsigned long long key = make_claim(epoch, cand_prio[idx], (unsigned)idx);
         if (st.claim[B] != key || (L < st.k && st.claim[L] != key)) continue;
+        __syncwarp(pair_mask);                   // both lanes have read the claims and cand_dest
         ItemRec it;
         load_item<M>(st, i, it);
         const int now = st.sweep->sweep;
-        st.claim[B] = 0ull;                      // taken for the rest of this step
-        cand_dest[idx] = -1;
-        df* aB = st.acc + (int64_t)B * Layout<M>::acc;
-        float4* eB = st.ev + (int64_t)B * Layout<M>::ev;
         if (L >= st.k) {
             // unassigned item joining a cluster: always committed
-            won_total++;
-            st.label[i] = B;
-            st.size[B] += 1;
-            st.stamp[B] = now;
-            accumulate_item<M>(aB, it, 1.0f);
-            update_cluster<M, false>(st, B);
+            if (role == 0) {
+                st.claim[B] = 0ull;              // taken for the rest of this step
+                cand_dest[idx] = -1;
+                won_total++;
+                st.label[i] = B;
+                st.size[B] += 1;
+                st.stamp[B] = now;
+                accumulate_item<M>(st.acc + (int64_t)B * Layout<M>::acc, it, 1.0f);
+                update_cluster<M, false>(st, B);
+            }
             continue;
         }
-        st.claim[L] = 0ull;
-        df* aL = st.acc + (int64_t)L * Layout<M>::acc;
-        float4* eL = st.ev + (int64_t)L * Layout<M>::ev;
-        // the two clusters' new records are built in registers and written only
-        // if the tracked energy of the pair strictly decreases (the float32 test
-        // can disagree with the updated records, e.g. when a pseudo-inverse
-        // eigenvalue sits at the threshold), so the minimisation descends
-        // monotonically and terminates
+        // the new records are built in registers and written only if the tracked
+        // energy of the pair strictly decreases (the float32 test can disagree with
+        // the updated records, e.g. when a pseudo-inverse eigenvalue sits at the
+        // threshold), so the minimisation descends monotonically and terminates
+        const int C = role ? L : B;
+        df* aC = st.acc + (int64_t)C * Layout<M>::acc;
+        float4* eC = st.ev + (int64_t)C * Layout<M>::ev;
         const RunFlags fl = *st.flags;
-        const double e_old = st.energy[B] + st.energy[L];
-        df nB[Layout<M>::acc], nL[Layout<M>::acc];
+        const double e_mine = st.energy[C];
+        df nC[Layout<M>::acc];
 #pragma unroll
-        for (int q = 0; q < Layout<M>::acc; q++) { nB[q] = aB[q]; nL[q] = aL[q]; }
-        accumulate_item<M>(nB, it, 1.0f);
-        accumulate_item<M>(nL, it, -1.0f);
-        float4 rB[Layout<M>::ev], rL[Layout<M>::ev];
-        const double eBn = cluster_record_df<M>(nB, fl, rB);
-        const double eLn = cluster_record_df<M>(nL, fl, rL);
-        if (eBn + eLn < e_old) {
-            won_total++;
+        for (int q = 0; q < Layout<M>::acc; q++) nC[q] = aC[q];
+        accumulate_item<M>(nC, it, role ? -1.0f : 1.0f);
+        float4 rC[Layout<M>::ev];
+        const double en_mine = cluster_record_df<M>(nC, fl, rC);
+        const double e_other = __shfl_xor_sync(pair_mask, e_mine, 1);
+        const double en_other = __shfl_xor_sync(pair_mask, en_mine, 1);
+        // energy of the pair in the order B + L on both lanes
+        const double e_old = role ? e_other + e_mine : e_mine + e_other;
+        const double e_new = role ? en_other + en_mine : en_mine + en_other;
+        if (e_new < e_old) {
 #pragma unroll
-            for (int q = 0; q < Layout<M>::acc; q++) { aB[q] = nB[q]; aL[q] = nL[q]; }
+            for (int q = 0; q < Layout<M>::acc; q++) aC[q] = nC[q];
 #pragma unroll
-            for (int q = 0; q < Layout<M>::ev; q++) { eB[q] = rB[q]; eL[q] = rL[q]; }
-            st.energy[B] = eBn;
-            st.energy[L] = eLn;
-            st.label[i] = B;
-            st.size[B] += 1;
-            st.size[L] -= 1;
-            st.stamp[B] = now;
-            st.stamp[L] = now;
+            for (int q = 0; q < Layout<M>::ev; q++) eC[q] = rC[q];
+            st.energy[C] = en_mine;
+            st.size[C] += role ? -1 : 1;
+            st.stamp[C] = now;
+            st.claim[C] = 0ull;                  // taken for the rest of this step
+            if (role == 0) {
+                won_total++;
+                st.label[i] = B;
+                cand_dest[idx] = -1;
+            }
         } else {
-            atomicAdd(&st.counters[kCntReverted], 1ull);
+            st.claim[C] = 0ull;
+            if (role == 0) {
+                cand_dest[idx] = -1;
+                atomicAdd(&st.counters[kCntReverted], 1ull);
+            }
         }
     }
     // every thread of the grid reaches this point: warp-aggregated count
@@ -779,19 +794,6 @@ ACVD_DEV df from_fixed(long long d, float4 p) {
     const float h = __ll2float_rn(d);
     const float l = __ll2float_rn(d - __float2ll_rn(h));
     return df_renorm(__fmul_rn(__fmul_rn(h, p.z), p.w), __fmul_rn(__fmul_rn(l, p.z), p.w));
-}
-
-ACVD_DEV void relaxed_count_range(const DevState& st, const int* __restrict__ items, int color, unsigned gtid,
-                                  unsigned gstride) {
-    const unsigned n = st.cand_count[color];
-    for (unsigned j = gtid; j < n; j += gstride) {
-        const int L = st.label[items[st.cand_list[j]]];
-        if (L < st.k) atomicAdd(&st.out_cnt[L], 1);
-    }
-}
-
-__global__ void relaxed_count_kernel(DevState st, const int* __restrict__ items, int color) {
-    relaxed_count_range(st, items, color, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
 }
 
 template <int M>
@@ -1003,8 +1005,6 @@ __global__ void __launch_bounds__(256, 2) sweep_run_kernel(SweepRun a) {
             if (!grid_barrier(a.bar)) return;
             if (lead) a.ls->eval_ns += global_ns() - t0;
             if (relaxed) {
-                relaxed_count_range(st, items, c, gtid, gstride);
-                if (!grid_barrier(a.bar)) return;
                 relaxed_commit_range<M>(st, items, c, a.cand_dest, gtid, gstride);
                 if (!grid_barrier(a.bar)) return;
                 fx_finalize_range<M>(st, gtid, gstride);
@@ -1359,8 +1359,6 @@ cudaError_t launch_reclaim(const DevState& st, const int* items, int64_t count, 
 cudaError_t launch_relaxed_step(int metric, const DevState& st, const int* items, int64_t count, int color,
                                 const int* cand_dest, cudaStream_t s) {
     if (count == 0) return cudaSuccess;
-    ++g_launches;
-    relaxed_count_kernel<<<list_grid(count), 256, 0, s>>>(st, items, color);
     ACVD_DISPATCH(metric, relaxed_commit_kernel, list_grid(count), 256, s, st, items, color, cand_dest);
     ACVD_DISPATCH(metric, fx_finalize_kernel, nblk(st.k, 64), 64, s, st);   // small blocks: every SM gets some
     return cudaGetLastError();

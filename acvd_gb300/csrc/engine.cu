@@ -654,7 +654,7 @@ static int enqueue_sweep(acvd_ctx* ctx, bool timing, bool relaxed) {
         if (timing) CK(cudaEventRecordWithFlags(ctx->ev_eval[2 * c + 1], ctx->s, cudaEventRecordExternal));
         if (relaxed) {
             CK(launch_relaxed_step(ctx->metric, st, items, cnt, c, ctx->cand_dest.p, ctx->s));
-            kernels += 4;
+            kernels += 3;
             continue;
         }
         CK(launch_apply(ctx->metric, st, items, cnt, c, 0, ctx->cand_dest.p, ctx->cand_prio.p, ctx->s));

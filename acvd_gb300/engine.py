@@ -265,8 +265,13 @@ class Engine:
         self._ck(self._lib.acvd_minimize(self.ctx, ctypes.byref(st)), "acvd_minimize")
         return st.as_dict()
 
-    def labels(self) -> np.ndarray:
-        out = np.empty(self.n, dtype=np.int32)
+    def labels(self, out: np.ndarray | None = None) -> np.ndarray:
+        """GetClustering(); `out` (int32, n items, contiguous) may be a caller's buffer,
+        e.g. in pinned host memory."""
+        if out is None:
+            out = np.empty(self.n, dtype=np.int32)
+        elif out.dtype != np.int32 or out.shape != (self.n,) or not out.flags.c_contiguous:
+            raise ValueError("labels(out=...) needs a contiguous int32 array of n items")
         self._ck(self._lib.acvd_get_labels(self.ctx, _ptr(out)), "acvd_get_labels")
         return out
 

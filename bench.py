@@ -300,6 +300,62 @@ def run_reference_arm(args):
     print(json.dumps(line), flush=True)
 
 
+STEP_KEYS = ("eval_ms", "eval_bytes", "eval_launches", "kernel_launches", "sweeps", "moves", "hit_loop_cap",
+             "reverted", "relaxed_sweeps", "sweep_kernel_ms", "sweep_kernel_launches")
+
+
+def run_steps(torch, e, steps, warmup, device, ws, flush):
+    """`warmup` untimed minimisations, then `steps` minimisations (rewind + minimize
+    on resident inputs) timed with CUDA events on the engine's stream, the L2
+    flushed before each (outside the events).  Returns per-step ms, summed stats and
+    the last step's stats."""
+    stream = torch.cuda.ExternalStream(e.stream(), device=device)
+    for _ in range(warmup):
+        e.rewind()
+        e.minimize()
+    torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    step_ms = []
+    tot = {k: 0 for k in STEP_KEYS}
+    st = None
+    for _ in range(steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        e.rewind()
+        st = e.minimize()
+        e1.record(stream)
+        e1.synchronize()
+        step_ms.append(e0.elapsed_time(e1))
+        for k in tot:
+            tot[k] += st[k]
+    torch.cuda.synchronize()
+    return step_ms, tot, st
+
+
+def pinned(torch, a):
+    """A copy of numpy array `a` in pinned (page-locked) host memory, as a numpy view."""
+    if a is None:
+        return None
+    t = torch.empty(a.shape, dtype=getattr(torch, str(a.dtype)), pin_memory=True)
+    out = t.numpy()          # the view's base keeps the pinned tensor alive
+    out[...] = a
+    return out
+
+
+def roofline_kernel(persistent, tot_t):
+    """The dominant kernel and its event-timed duration from the instrumented pass:
+    the evaluation kernel on the per-phase schedule, the persistent sweep kernel
+    (all evaluation bytes over its duration) on the persistent one."""
+    if persistent:
+        return "sweep_run_kernel", tot_t["sweep_kernel_ms"], tot_t["sweep_kernel_launches"]
+    return "eval_kernel", tot_t["eval_ms"], tot_t["eval_launches"]
+
+
 def run_batch_arm(args):
     """Batched workload: every mesh of the batch in one packed CSR, one minimisation."""
     import torch
@@ -317,39 +373,26 @@ def run_batch_arm(args):
     t0 = time.perf_counter()
     b = B.synthetic_batch(w["n_meshes"], w["seed"], metric=w["metric"], gradation=w["gradation"])
     gen_s = time.perf_counter() - t0
-    eng = E.Engine(device=device, kernel_timing=True)
+    persistent = args.schedule == "persistent"
     row, col, ev = E.build_topology(b.n_points, b.faces)
-    eng.set_mesh(b.points, b.faces, row, col, ev)
-    eng.set_batch(b.v_off, b.k_off)
-    eng.set_metric(w["metric"], b.indicator, None, w["gradation"])
-    eng.set_unconstrained_initialization(w["uinit"])
-    eng.set_labels(b.k_total, b.labels0)
-    stream = torch.cuda.ExternalStream(eng.stream(), device=device)
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=f"cuda:{device}")
-    for _ in range(args.warmup):
-        eng.rewind()
-        eng.minimize()
-    torch.cuda.synchronize()
-    if ws > 1:
-        torch.distributed.barrier()
-    step_ms = []
-    tot = {"eval_ms": 0.0, "eval_bytes": 0, "eval_launches": 0, "kernel_launches": 0, "sweeps": 0, "moves": 0,
-           "relaxed_sweeps": 0}
+
+    def make_engine(kernel_timing):
+        e = E.Engine(device=device, kernel_timing=kernel_timing, persistent=persistent)
+        e.set_mesh(b.points, b.faces, row, col, ev)
+        e.set_batch(b.v_off, b.k_off)
+        e.set_metric(w["metric"], b.indicator, None, w["gradation"])
+        e.set_unconstrained_initialization(w["uinit"])
+        e.set_labels(b.k_total, b.labels0)
+        return e
+
+    # pass 1 (the headline): no instrumentation; pass 2: events around the evaluation kernels
+    eng = make_engine(False)
     with ClockSampler(device) as clk:
-        for _ in range(args.steps):
-            with torch.cuda.stream(stream):
-                flush.zero_()
-            torch.cuda.synchronize()
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            eng.rewind()
-            st = eng.minimize()
-            e1.record(stream)
-            e1.synchronize()
-            step_ms.append(e0.elapsed_time(e1))
-            for k in tot:
-                tot[k] += st[k]
+        step_ms, tot, st = run_steps(torch, eng, args.steps, args.warmup, device, ws, flush)
+    engt = make_engine(True)
+    _, tot_t, _ = run_steps(torch, engt, args.steps, 1, device, ws, flush)
+    engt.close()
     ms = statistics.mean(step_ms)
     if ws > 1:
         t = torch.tensor([ms], device=f"cuda:{device}")
@@ -363,17 +406,25 @@ def run_batch_arm(args):
         h2d = (b.points.nbytes + b.faces.nbytes + row.nbytes + col.nbytes + ev.nbytes + b.labels0.nbytes +
                (b.indicator.nbytes if b.indicator is not None else 0))
         e2e_ms = []
-        eng2 = E.Engine(device=device)
+        eng2 = E.Engine(device=device, persistent=persistent)
+        # the step's inputs and its output buffer in pinned host memory
+        c = np.ascontiguousarray
+        h_pts, h_faces, h_row, h_col, h_ev = (pinned(torch, a) for a in (
+            c(b.points, dtype=np.float64), c(b.faces, dtype=np.int32), c(row, dtype=np.int32),
+            c(col, dtype=np.int32), c(ev, dtype=np.int32)))
+        h_ind = pinned(torch, None if b.indicator is None else c(b.indicator, dtype=np.float64))
+        h_lab0 = pinned(torch, c(b.labels0, dtype=np.int32))
+        out = pinned(torch, c(b.labels0, dtype=np.int32))
         for _ in range(max(1, args.steps)):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            eng2.set_mesh(b.points, b.faces, row, col, ev)
+            eng2.set_mesh(h_pts, h_faces, h_row, h_col, h_ev)
             eng2.set_batch(b.v_off, b.k_off)
-            eng2.set_metric(w["metric"], b.indicator, None, w["gradation"])
+            eng2.set_metric(w["metric"], h_ind, None, w["gradation"])
             eng2.set_unconstrained_initialization(w["uinit"])
-            eng2.set_labels(b.k_total, b.labels0)
+            eng2.set_labels(b.k_total, h_lab0)
             eng2.minimize()
-            out = eng2.labels()
+            eng2.labels(out=out)
             torch.cuda.synchronize()
             e2e_ms.append(1000.0 * (time.perf_counter() - t0))
         eng2.close()
@@ -415,20 +466,24 @@ def run_batch_arm(args):
     except (OSError, ValueError):
         pass
     peak = peaks.get("hbm_gbs", 6800.0)
-    achieved = (tot["eval_bytes"] / 1e9) / (tot["eval_ms"] / 1000.0) if tot["eval_ms"] > 0 else None
+    kname, kms, klaunch = roofline_kernel(persistent, tot_t)
+    achieved = (tot_t["eval_bytes"] / 1e9) / (kms / 1000.0) if kms > 0 else None
     line = {
         "metric": METRIC, "value": value, "unit": "meshes/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": args.workload, "description": w["desc"], "meshes": b.n_mesh, "items": b.n_points,
                    "clusters": b.k_total, "faces": int(b.faces.shape[0]), "generation_s": gen_s,
-                   "parallelism": "replicas" if ws > 1 else "single", "l2": "flushed between timed steps (256 MB write)"},
-        "roofline": {"bound": "hbm", "kernel": "eval_kernel", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                   "parallelism": "replicas" if ws > 1 else "single", "l2": "flushed between timed steps (256 MB write)",
+                   "schedule": args.schedule},
+        "roofline": {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None,
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if "hbm_gbs" in peaks else "fallback",
-                     "traffic": None, "launches": tot["eval_launches"],
-                     "algorithmic_bytes_per_launch": tot["eval_bytes"] / max(1, tot["eval_launches"]),
-                     "avg_launch_us": 1000.0 * tot["eval_ms"] / max(1, tot["eval_launches"])},
+                     "traffic": None, "launches": klaunch,
+                     "algorithmic_bytes_per_launch": tot_t["eval_bytes"] / max(1, klaunch),
+                     "avg_launch_us": 1000.0 * kms / max(1, klaunch),
+                     "timing": "CUDA events around each launch, in a second pass of the same steps "
+                               "(the headline pass carries no events)"},
         "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(tot["kernel_launches"]),
         "sweeps_per_step": tot["sweeps"] / max(1, args.steps),
         "relaxed_sweeps_per_step": tot["relaxed_sweeps"] / max(1, args.steps),
@@ -455,43 +510,28 @@ def run_gpu_arm(args):
     lab0, (row, col, ev) = initial_labels(m, w["metric"], ind, w["gradation"], w["k"], w.get("init"))
     n = m.n_points
 
-    eng = E.Engine(device=device, kernel_timing=True)
-    eng.set_mesh(m.points, m.faces, row, col, ev)
-    eng.set_metric(w["metric"], ind, pd, w["gradation"])
-    eng.set_unconstrained_initialization(w["uinit"])
-    eng.set_labels(w["k"], lab0)
-    stream = torch.cuda.ExternalStream(eng.stream(), device=device)
+    persistent = args.schedule == "persistent"
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=f"cuda:{device}")
 
-    def step():
-        eng.rewind()
-        return eng.minimize()
+    def make_engine(kernel_timing):
+        e = E.Engine(device=device, kernel_timing=kernel_timing, persistent=persistent)
+        e.set_mesh(m.points, m.faces, row, col, ev)
+        e.set_metric(w["metric"], ind, pd, w["gradation"])
+        e.set_unconstrained_initialization(w["uinit"])
+        e.set_labels(w["k"], lab0)
+        return e
 
-    for _ in range(args.warmup):
-        step()
-    torch.cuda.synchronize()
-    if ws > 1:
-        torch.distributed.barrier()
-
-    step_ms = []
-    tot = {"eval_ms": 0.0, "eval_bytes": 0, "eval_launches": 0, "kernel_launches": 0, "sweeps": 0, "moves": 0,
-           "hit_loop_cap": 0, "reverted": 0, "relaxed_sweeps": 0}
+    # pass 1 (the headline): no instrumentation inside the sweeps
+    eng = make_engine(False)
     with ClockSampler(device) as clk:
-        for _ in range(args.steps):
-            with torch.cuda.stream(stream):
-                flush.zero_()          # L2 flush between timed iterations (outside the events)
-            torch.cuda.synchronize()
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            st = step()
-            e1.record(stream)
-            e1.synchronize()
-            step_ms.append(e0.elapsed_time(e1))
-            for k in tot:
-                tot[k] += st[k]
-    torch.cuda.synchronize()
+        step_ms, tot, st = run_steps(torch, eng, args.steps, args.warmup, device, ws, flush)
     ms = statistics.mean(step_ms)
+    # pass 2 (the roofline): the same steps with CUDA events around every evaluation
+    # kernel (event nodes inside the sweep graph; on the persistent schedule the
+    # events bracket each persistent launch)
+    engt = make_engine(True)
+    _, tot_t, _ = run_steps(torch, engt, args.steps, 1, device, ws, flush)
+    engt.close()
     if ws > 1:
         t = torch.tensor([ms], device=f"cuda:{device}")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -507,16 +547,25 @@ def run_gpu_arm(args):
                (ind.nbytes if ind is not None else 0) + (pd.nbytes if pd is not None else 0) + lab0.nbytes)
         d2h = lab0.nbytes
         e2e_ms = []
-        eng2 = E.Engine(device=device)
+        eng2 = E.Engine(device=device, persistent=persistent)
+        # the step's inputs and its output buffer in pinned host memory
+        c = np.ascontiguousarray
+        h_pts, h_faces, h_row, h_col, h_ev = (pinned(torch, a) for a in (
+            c(m.points, dtype=np.float64), c(m.faces, dtype=np.int32), c(row, dtype=np.int32),
+            c(col, dtype=np.int32), c(ev, dtype=np.int32)))
+        h_ind = pinned(torch, None if ind is None else c(ind, dtype=np.float64))
+        h_pd = pinned(torch, None if pd is None else c(pd, dtype=np.float32))
+        h_lab0 = pinned(torch, c(lab0, dtype=np.int32))
+        out = pinned(torch, c(lab0, dtype=np.int32))
         for it in range(max(1, args.steps)):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            eng2.set_mesh(m.points, m.faces, row, col, ev)
-            eng2.set_metric(w["metric"], ind, pd, w["gradation"])
+            eng2.set_mesh(h_pts, h_faces, h_row, h_col, h_ev)
+            eng2.set_metric(w["metric"], h_ind, h_pd, w["gradation"])
             eng2.set_unconstrained_initialization(w["uinit"])
-            eng2.set_labels(w["k"], lab0)
+            eng2.set_labels(w["k"], h_lab0)
             eng2.minimize()
-            out = eng2.labels()
+            eng2.labels(out=out)
             torch.cuda.synchronize()
             e2e_ms.append(1000.0 * (time.perf_counter() - t0))
         eng2.close()
@@ -567,7 +616,8 @@ def run_gpu_arm(args):
     except (OSError, ValueError):
         pass
     peak = peaks.get("hbm_gbs", 6800.0)
-    achieved = (tot["eval_bytes"] / 1e9) / (tot["eval_ms"] / 1000.0) if tot["eval_ms"] > 0 else None
+    kname, kms, klaunch = roofline_kernel(persistent, tot_t)
+    achieved = (tot_t["eval_bytes"] / 1e9) / (kms / 1000.0) if kms > 0 else None
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "eval_traffic.json")
     if os.path.exists(tpath):
@@ -581,13 +631,15 @@ def run_gpu_arm(args):
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": args.workload, "description": w["desc"], "items": n, "clusters": w["k"],
                    "faces": m.n_faces, "parallelism": "replicas" if ws > 1 else "single",
-                   "l2": "flushed between timed steps (256 MB write)"},
-        "roofline": {"bound": "hbm", "kernel": "eval_kernel", "achieved": achieved,
+                   "l2": "flushed between timed steps (256 MB write)", "schedule": args.schedule},
+        "roofline": {"bound": "hbm", "kernel": kname, "achieved": achieved,
                      "peak": peak, "unit": "GB/s", "frac": (achieved / peak) if achieved else None,
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if "hbm_gbs" in peaks else "fallback",
-                     "traffic": traffic, "launches": tot["eval_launches"],
-                     "algorithmic_bytes_per_launch": tot["eval_bytes"] / max(1, tot["eval_launches"]),
-                     "avg_launch_us": 1000.0 * tot["eval_ms"] / max(1, tot["eval_launches"])},
+                     "traffic": traffic, "launches": klaunch,
+                     "algorithmic_bytes_per_launch": tot_t["eval_bytes"] / max(1, klaunch),
+                     "avg_launch_us": 1000.0 * kms / max(1, klaunch),
+                     "timing": "CUDA events around each launch, in a second pass of the same steps "
+                               "(the headline pass carries no events)"},
         "cpu_baseline": cpu,
         "e2e": e2e,
         "gpu_launches": int(tot["kernel_launches"]),
@@ -608,6 +660,9 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--schedule", default="phases", choices=["phases", "persistent"],
+                    help="sweep schedule: per-phase kernels in CUDA graphs, or one persistent "
+                         "cooperative kernel between convergence events")
     ap.add_argument("--workload", default="torus_1024x512_qem",
                     choices=sorted(WORKLOADS) + sorted(BATCH_WORKLOADS) + sorted(ADJOINT_WORKLOADS))
     ap.add_argument("--no-e2e", action="store_true")
