@@ -1135,10 +1135,13 @@ __global__ void update_all_kernel(DevState st) {
 // pointer jumping; each cluster keeps its largest component (ties -> the one
 // containing the smallest item id), the rest become unassigned
 // ---------------------------------------------------------------------------
+// Components carry the smallest ORIGINAL vertex id among their items (the
+// tie-break between equally large components follows the reference's item
+// order, not the internal one); inv maps such an id back to its item.
 __global__ void comp_init_kernel(DevState st, int* __restrict__ comp) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= st.n) return;
-    comp[i] = st.label[i] < st.k ? (int)i : -1;
+    comp[i] = st.label[i] < st.k ? st.orig[i] : -1;
 }
 
 __global__ void comp_step_kernel(DevState st, int* __restrict__ comp) {
@@ -1153,7 +1156,7 @@ __global__ void comp_step_kernel(DevState st, int* __restrict__ comp) {
         if (st.label[j] == L) m = min(m, comp[j]);
     }
     for (int hop = 0; hop < 64; hop++) {
-        const int mm = comp[m];
+        const int mm = comp[st.inv[m]];
         if (mm >= m) break;
         m = mm;
     }
@@ -1174,8 +1177,9 @@ __global__ void comp_best_kernel(DevState st, const int* __restrict__ comp, cons
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= st.n) return;
     const int L = st.label[i];
-    if (L >= st.k || comp[i] != (int)i) return;
-    const unsigned long long key = ((unsigned long long)(unsigned)csize[i] << 32) | (0xffffffffull - (uint32_t)i);
+    const int o = st.orig[i];
+    if (L >= st.k || comp[i] != o) return;
+    const unsigned long long key = ((unsigned long long)(unsigned)csize[o] << 32) | (0xffffffffull - (uint32_t)o);
     atomicMax(&best[L], key);
 }
 

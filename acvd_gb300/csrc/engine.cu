@@ -54,6 +54,9 @@ struct acvd_ctx {
     int ncolors = 0;
     std::vector<int64_t> color_off;
     DBuf<int> color_items, cand_dest, cand_list;
+    // internal item order: colour classes contiguous (perm: item -> original
+    // vertex id, inv: original vertex id -> item); faces and edges in item ids
+    DBuf<int> perm, inv, tri_int, edge_int, label_orig;
     // sweep classes: either the colour classes, or one class holding every item
     // (claims alone keep committed moves on disjoint clusters; colours are kept
     // for hole filling)
@@ -156,6 +159,8 @@ struct acvd_ctx {
         st.out_cnt = out_cnt.p;
         st.in_done = in_done.p;
         st.out_done = out_done.p;
+        st.orig = perm.p;
+        st.inv = inv.p;
         return st;
     }
     cudaGraphExec_t relaxed_exec = nullptr;
@@ -245,25 +250,46 @@ static int setup_colors(acvd_ctx* ctx) {
     CK(ctx->wk_d.resize(n));
     CK(cudaMemcpyAsync(ctx->wk_a.p, ctx->wk_int.p, n * sizeof(int), cudaMemcpyDeviceToDevice, ctx->s));
     CK(ctx->color_items.resize(n));
-    std::vector<uint32_t> iota(n);
-    for (int64_t i = 0; i < n; i++) iota[i] = (uint32_t)i;
-    CK(cudaMemcpyAsync(ctx->wk_b.p, iota.data(), n * sizeof(uint32_t), cudaMemcpyHostToDevice, ctx->s));
+    CK(launch_iota(n, (int*)ctx->wk_b.p, ctx->s));
     CK(radix_sort_pairs(ctx->wk_a.p, ctx->wk_b.p, ctx->wk_c.p, ctx->wk_d.p, n, 8, ctx->scratch, ctx->s));
     CK(cudaMemcpyAsync(ctx->color_items.p, ctx->wk_b.p, n * sizeof(int), cudaMemcpyDeviceToDevice, ctx->s));
-    CK(ctx->wk_cnt.resize(64));
-    CK(cudaMemsetAsync(ctx->wk_cnt.p, 0, 64 * sizeof(uint32_t), ctx->s));
-    CK(launch_count_keys(ctx->wk_a.p, n, ctx->wk_cnt.p, ctx->s));
-    std::vector<uint32_t> cnt(64);
-    CK(cudaMemcpyAsync(cnt.data(), ctx->wk_cnt.p, 64 * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->s));
+    CK(ctx->wk_cnt.resize(65));
+    CK(launch_segment_offsets(ctx->wk_a.p, n, (uint32_t)ctx->ncolors, ctx->wk_cnt.p, ctx->s));
+    std::vector<uint32_t> off(ctx->ncolors + 1);
+    CK(cudaMemcpyAsync(off.data(), ctx->wk_cnt.p, off.size() * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->s));
     CK(cudaStreamSynchronize(ctx->s));
     ctx->color_off.assign(ctx->ncolors + 1, 0);
     int64_t mx = 0;
     for (int c = 0; c < ctx->ncolors; c++) {
-        ctx->color_off[c + 1] = ctx->color_off[c] + cnt[c];
-        mx = std::max<int64_t>(mx, cnt[c]);
+        ctx->color_off[c + 1] = off[c + 1];
+        mx = std::max<int64_t>(mx, (int64_t)off[c + 1] - off[c]);
     }
+    // renumber: item t = the t-th entry of the colour-sorted list, so that every
+    // colour class is the contiguous item range [color_off[c], color_off[c+1])
+    CK(ctx->perm.resize(n));
+    CK(ctx->inv.resize(n));
+    CK(ctx->wk_a.resize(n + 1));
+    CK(ctx->wk_b.resize(n + 1));
+    CK(cudaMemcpyAsync(ctx->perm.p, ctx->color_items.p, n * sizeof(int), cudaMemcpyDeviceToDevice, ctx->s));
+    CK(launch_scatter_inv(ctx->perm.p, n, ctx->inv.p, ctx->s));
+    {
+        const int64_t ne2 = 2 * ctx->nE;
+        DBuf<int> col_new;
+        CK(col_new.resize(ne2));
+        CK(launch_perm_degree(ctx->row.p, ctx->perm.p, n, ctx->wk_a.p, ctx->s));
+        CK(exclusive_scan_u32(ctx->wk_a.p, ctx->wk_b.p, n + 1, nullptr, ctx->scratch, ctx->s));
+        CK(launch_perm_ring(ctx->row.p, ctx->col.p, ctx->perm.p, ctx->inv.p, ctx->wk_b.p, n, col_new.p, ctx->s));
+        CK(cudaMemcpyAsync(ctx->row.p, ctx->wk_b.p, (n + 1) * sizeof(int), cudaMemcpyDeviceToDevice, ctx->s));
+        CK(cudaMemcpyAsync(ctx->col.p, col_new.p, ne2 * sizeof(int), cudaMemcpyDeviceToDevice, ctx->s));
+        CK(cudaStreamSynchronize(ctx->s));
+    }
+    CK(ctx->tri_int.resize(3 * ctx->nF));
+    CK(ctx->edge_int.resize(2 * ctx->nE));
+    CK(launch_map_ids(ctx->tri.p, 3 * ctx->nF, ctx->inv.p, ctx->tri_int.p, ctx->s));
+    CK(launch_map_ids(ctx->edge_v.p, 2 * ctx->nE, ctx->inv.p, ctx->edge_int.p, ctx->s));
     CK(ctx->all_items.resize(n));
-    CK(cudaMemcpyAsync(ctx->all_items.p, iota.data(), n * sizeof(int), cudaMemcpyHostToDevice, ctx->s));
+    CK(launch_iota(n, ctx->all_items.p, ctx->s));
+    CK(launch_iota(n, ctx->color_items.p, ctx->s));
     if (ctx->sweep_by_color) {
         ctx->sweep_off = ctx->color_off;
         ctx->sweep_items = ctx->color_items.p;
@@ -362,6 +388,9 @@ int acvd_set_mesh(acvd_ctx* ctx, int64_t n_vertices, const double* xyz, int64_t 
     CK(cudaMemcpyAsync(ctx->row.p, csr_row, (n_vertices + 1) * sizeof(int), cudaMemcpyHostToDevice, ctx->s));
     CK(cudaMemcpyAsync(ctx->col.p, csr_col, 2 * n_edges * sizeof(int), cudaMemcpyHostToDevice, ctx->s));
     CK(cudaMemcpyAsync(ctx->edge_v.p, edge_v, 2 * n_edges * sizeof(int), cudaMemcpyHostToDevice, ctx->s));
+    // colouring on the input rings, then the items in internal order
+    int r = setup_colors(ctx);
+    if (r) return r;
     int* d_maxdeg = nullptr;
     CK(ctx->dtmp.resize(2));
     d_maxdeg = (int*)ctx->dtmp.p;
@@ -369,8 +398,6 @@ int acvd_set_mesh(acvd_ctx* ctx, int64_t n_vertices, const double* xyz, int64_t 
     CK(launch_ring_adjacency(ctx->row.p, ctx->col.p, n_vertices, ctx->adj.p, d_maxdeg, ctx->s));
     CK(cudaMemcpyAsync(&ctx->max_deg, d_maxdeg, sizeof(int), cudaMemcpyDeviceToHost, ctx->s));
     CK(cudaStreamSynchronize(ctx->s));
-    int r = setup_colors(ctx);
-    if (r) return r;
     ctx->ready_mesh = true;
     return ACVD_OK;
 }
@@ -412,10 +439,8 @@ int acvd_set_metric(acvd_ctx* ctx, int metric, const double* indicator, const fl
     CK(v2.resize(3 * nf));
     CK(vrow.resize(nv + 1));
     CK(launch_vertex_keys(ctx->tri.p, nf, k1.p, v1.p, ctx->s));
-    CK(cudaMemsetAsync(vrow.p, 0, (nv + 1) * sizeof(uint32_t), ctx->s));
-    CK(launch_count_keys(k1.p, 3 * nf, vrow.p, ctx->s));
     CK(radix_sort_pairs(k1.p, v1.p, k2.p, v2.p, 3 * nf, bits_for((uint64_t)nv), ctx->scratch, ctx->s));
-    CK(exclusive_scan_u32(vrow.p, vrow.p, nv + 1, nullptr, ctx->scratch, ctx->s));
+    CK(launch_segment_offsets(k1.p, 3 * nf, (uint32_t)nv, vrow.p, ctx->s));
     CK(ctx->xw.resize(nv));
     if (metric != kIso) {
         CK(ctx->qa.resize(nv));
@@ -442,6 +467,28 @@ int acvd_set_metric(acvd_ctx* ctx, int metric, const double* indicator, const fl
         CK(sum_f64(wd.p, nv, wsum.p, ctx->scratch, ctx->s));
         CK(launch_finish_items(metric, nv, ctx->xyz.p, wd.p, varea.p, wsum.p, nullptr, 0, ratio, pd.p, ctx->xw.p,
                                ctx->ta.p, ctx->tb.p, ctx->s));
+    }
+    // item records into internal order
+    {
+        DBuf<float4> t4;
+        DBuf<float2> t2;
+        CK(t4.resize(nv));
+        CK(launch_gather_f4(ctx->xw.p, ctx->perm.p, nv, t4.p, ctx->s));
+        CK(cudaMemcpyAsync(ctx->xw.p, t4.p, nv * sizeof(float4), cudaMemcpyDeviceToDevice, ctx->s));
+        if (metric != kIso) {
+            CK(t2.resize(nv));
+            CK(launch_gather_f4(ctx->qa.p, ctx->perm.p, nv, t4.p, ctx->s));
+            CK(cudaMemcpyAsync(ctx->qa.p, t4.p, nv * sizeof(float4), cudaMemcpyDeviceToDevice, ctx->s));
+            CK(launch_gather_f2(ctx->qb.p, ctx->perm.p, nv, t2.p, ctx->s));
+            CK(cudaMemcpyAsync(ctx->qb.p, t2.p, nv * sizeof(float2), cudaMemcpyDeviceToDevice, ctx->s));
+        }
+        if (metric == kAniso) {
+            CK(launch_gather_f4(ctx->ta.p, ctx->perm.p, nv, t4.p, ctx->s));
+            CK(cudaMemcpyAsync(ctx->ta.p, t4.p, nv * sizeof(float4), cudaMemcpyDeviceToDevice, ctx->s));
+            CK(launch_gather_f2(ctx->tb.p, ctx->perm.p, nv, t2.p, ctx->s));
+            CK(cudaMemcpyAsync(ctx->tb.p, t2.p, nv * sizeof(float2), cudaMemcpyDeviceToDevice, ctx->s));
+        }
+        CK(cudaStreamSynchronize(ctx->s));
     }
     // fixed-point scales of the relaxed steps: any sum of up to N contributions of
     // component j stays below 2^62 units
@@ -538,7 +585,9 @@ int acvd_set_labels(acvd_ctx* ctx, int32_t k, const int32_t* labels) {
     CK(ctx->energy.resize(k + 1));
     (void)ms;
     CK(ctx->label_init.resize(ctx->nV));
-    CK(cudaMemcpyAsync(ctx->label.p, labels, ctx->nV * sizeof(int), cudaMemcpyHostToDevice, ctx->s));
+    CK(ctx->label_orig.resize(ctx->nV));
+    CK(cudaMemcpyAsync(ctx->label_orig.p, labels, ctx->nV * sizeof(int), cudaMemcpyHostToDevice, ctx->s));
+    CK(launch_gather_i32(ctx->label_orig.p, ctx->perm.p, ctx->nV, ctx->label.p, ctx->s));
     CK(cudaMemcpyAsync(ctx->label_init.p, ctx->label.p, ctx->nV * sizeof(int), cudaMemcpyDeviceToDevice, ctx->s));
     CK(cudaStreamSynchronize(ctx->s));
     ctx->ready_labels = true;
@@ -999,7 +1048,9 @@ extern "C" int acvd_get_labels(acvd_ctx* ctx, int32_t* labels) {
     if (!ctx || !labels) return ACVD_ERR_ARG;
     if (!ctx->ready_labels) return fail(ctx, ACVD_ERR_ARG, "no labels");
     CK(cudaSetDevice(ctx->opts.device));
-    CK(cudaMemcpyAsync(labels, ctx->label.p, ctx->nV * sizeof(int), cudaMemcpyDeviceToHost, ctx->s));
+    CK(ctx->label_orig.resize(ctx->nV));
+    CK(launch_gather_i32(ctx->label.p, ctx->inv.p, ctx->nV, ctx->label_orig.p, ctx->s));
+    CK(cudaMemcpyAsync(labels, ctx->label_orig.p, ctx->nV * sizeof(int), cudaMemcpyDeviceToHost, ctx->s));
     CK(cudaStreamSynchronize(ctx->s));
     return ACVD_OK;
 }
@@ -1081,7 +1132,7 @@ extern "C" int acvd_get_boundary_edges(acvd_ctx* ctx, int32_t* ids, int64_t* cou
     CK(pos.resize(ne + 1));
     CK(ctx->dtmp.resize(2));
     uint32_t* total = (uint32_t*)ctx->dtmp.p;
-    CK(launch_boundary_edges(ctx->edge_v.p, ne, ctx->label.p, flags.p, ctx->s));
+    CK(launch_boundary_edges(ctx->edge_int.p, ne, ctx->label.p, flags.p, ctx->s));
     CK(exclusive_scan_u32(flags.p, pos.p, ne, total, ctx->scratch, ctx->s));
     uint32_t t = 0;
     CK(cudaMemcpyAsync(&t, total, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->s));
@@ -1107,7 +1158,7 @@ extern "C" int acvd_get_dual_mesh(acvd_ctx* ctx, int32_t* tris, int64_t* n_tris)
     CK(pos.resize(nf + 1));
     CK(ctx->dtmp.resize(2));
     uint32_t* total = (uint32_t*)ctx->dtmp.p;
-    CK(launch_dual_faces(ctx->tri.p, nf, ctx->label.p, ctx->K, flags.p, ctx->s));
+    CK(launch_dual_faces(ctx->tri_int.p, nf, ctx->label.p, ctx->K, flags.p, ctx->s));
     CK(exclusive_scan_u32(flags.p, pos.p, nf, total, ctx->scratch, ctx->s));
     uint32_t m = 0;
     CK(cudaMemcpyAsync(&m, total, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->s));
@@ -1117,7 +1168,7 @@ extern "C" int acvd_get_dual_mesh(acvd_ctx* ctx, int32_t* tris, int64_t* n_tris)
     CK(launch_compact(flags.p, pos.p, nf, faces.p, ctx->s));
     CK(klo.resize(m)); CK(khi.resize(m)); CK(order.resize(m)); CK(t1.resize(m)); CK(t2.resize(m));
     CK(keep.resize(m + 1)); CK(kpos.resize(m + 1));
-    CK(launch_dual_keys(ctx->tri.p, faces.p, m, ctx->label.p, klo.p, khi.p, order.p, ctx->s));
+    CK(launch_dual_keys(ctx->tri_int.p, faces.p, m, ctx->label.p, klo.p, khi.p, order.p, ctx->s));
     // stable LSD sort on (khi, klo): by klo first, then by khi
     CK(radix_sort_pairs(klo.p, order.p, t1.p, t2.p, m, 32, ctx->scratch, ctx->s));
     CK(launch_gather_u32(khi.p, order.p, m, t1.p, ctx->s));           // khi in klo-sorted order
@@ -1144,7 +1195,7 @@ extern "C" int acvd_get_dual_mesh(acvd_ctx* ctx, int32_t* tris, int64_t* n_tris)
         CK(sel.resize(t));
         CK(out.resize(3 * (size_t)t));
         CK(launch_compact(keep.p, kpos.p, m, sel.p, ctx->s));
-        CK(launch_dual_write(ctx->tri.p, faces.p, sel.p, t, ctx->label.p, out.p, ctx->s));
+        CK(launch_dual_write(ctx->tri_int.p, faces.p, sel.p, t, ctx->label.p, out.p, ctx->s));
         CK(cudaMemcpyAsync(tris, out.p, 3 * (size_t)t * sizeof(int), cudaMemcpyDeviceToHost, ctx->s));
         CK(cudaStreamSynchronize(ctx->s));
     }
@@ -1170,8 +1221,11 @@ extern "C" int acvd_adjoint(acvd_ctx* ctx, const double* xyz, const double* rho,
     CK(cudaSetDevice(ctx->opts.device));
     const int64_t nv = ctx->nV, nf = ctx->nF;
     const int K = ctx->K;
-    // items sorted by cluster (fixed clustering)
+    // items sorted by cluster (fixed clustering), in original vertex ids
+    CK(ctx->label_orig.resize(nv));
+    CK(launch_gather_i32(ctx->label.p, ctx->inv.p, nv, ctx->label_orig.p, ctx->s));
     DevState st = ctx->state();
+    st.label = ctx->label_orig.p;
     CK(ctx->wk_a.resize(nv)); CK(ctx->wk_b.resize(nv)); CK(ctx->wk_c.resize(nv)); CK(ctx->wk_d.resize(nv));
     CK(ctx->wk_cnt.resize(K + 1)); CK(ctx->wk_off.resize(K + 1));
     CK(cudaMemsetAsync(ctx->wk_cnt.p, 0, (K + 1) * sizeof(uint32_t), ctx->s));
@@ -1185,7 +1239,7 @@ extern "C" int acvd_adjoint(acvd_ctx* ctx, const double* xyz, const double* rho,
     a.rho = rho;
     a.grad = gradation;
     a.tri = ctx->tri.p;
-    a.label = ctx->label.p;
+    a.label = ctx->label_orig.p;
     a.vf_row = ctx->vf_row.p;
     a.vf_face = ctx->vf_face.p;
     CK(ctx->dtmp.resize(4));

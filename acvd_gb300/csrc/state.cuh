@@ -106,6 +106,10 @@ struct DevState {
     int* out_cnt;          // proposals leaving the cluster in this step
     int* in_done;          // committed moves into the cluster
     int* out_done;         // committed moves out of the cluster
+    // internal item order (colour classes contiguous): original vertex id of
+    // each item, and the item of each original vertex id
+    const int* orig;
+    const int* inv;
 };
 
 // Persistent sweep kernel: the loop that runs colour sweeps back to back on the
@@ -168,7 +172,8 @@ cudaError_t launch_color_round(const int* row, const int* col, int64_t n, int* c
 cudaError_t launch_face_geometry(const double* xyz, const int* tri, int64_t nf, double* farea, double* fnorm,
                                  cudaStream_t s);
 cudaError_t launch_vertex_keys(const int* tri, int64_t nf, uint32_t* keys, uint32_t* vals, cudaStream_t s);
-cudaError_t launch_count_keys(const uint32_t* keys, int64_t n, uint32_t* counts, cudaStream_t s);
+cudaError_t launch_segment_offsets(const uint32_t* sorted_keys, int64_t n, uint32_t nkeys, uint32_t* off,
+                                   cudaStream_t s);
 cudaError_t launch_vertex_items(int metric, int64_t nv, const double* xyz, const uint32_t* vf_row,
                                 const uint32_t* vf_face, const double* farea, const double* fnorm,
                                 const double* indicator, double gradation, double* wd, double* varea,
@@ -177,6 +182,17 @@ cudaError_t launch_mesh_sums(const double* wd, const int64_t* v_off, int nmesh, 
 cudaError_t launch_finish_items(int metric, int64_t nv, const double* xyz, const double* wd, const double* vrea,
                                 const double* wsum, const int64_t* v_off, int nmesh, double ratio, const float* pdirs,
                                 float4* xw, float4* ta, float2* tb, cudaStream_t s);
+
+// ---- internal item order (topology.cu) ----
+cudaError_t launch_scatter_inv(const int* perm, int64_t n, int* inv, cudaStream_t s);
+cudaError_t launch_perm_degree(const int* row, const int* perm, int64_t n, uint32_t* deg, cudaStream_t s);
+cudaError_t launch_perm_ring(const int* row, const int* col, const int* perm, const int* inv, const uint32_t* row_new,
+                             int64_t n, int* col_new, cudaStream_t s);
+cudaError_t launch_map_ids(const int* in, int64_t m, const int* inv, int* out, cudaStream_t s);
+cudaError_t launch_gather_i32(const int* src, const int* idx, int64_t n, int* dst, cudaStream_t s);
+cudaError_t launch_gather_f4(const float4* src, const int* idx, int64_t n, float4* dst, cudaStream_t s);
+cudaError_t launch_gather_f2(const float2* src, const int* idx, int64_t n, float2* dst, cudaStream_t s);
+cudaError_t launch_iota(int64_t n, int* out, cudaStream_t s);
 
 // ---- clustering (cluster.cu) ----
 cudaError_t launch_begin_sweep(const DevState& st, int ncolors, cudaStream_t s);

@@ -148,15 +148,23 @@ cudaError_t launch_vertex_keys(const int* tri, int64_t nf, uint32_t* keys, uint3
     return cudaGetLastError();
 }
 
-__global__ void count_keys_kernel(const uint32_t* __restrict__ keys, int64_t n, uint32_t* __restrict__ counts) {
+// Segment offsets of sorted keys in [0, nkeys): off[c] = first position whose key
+// is >= c, off[nkeys] = n.  Thread j writes the offsets of the keys from the
+// previous element's key (exclusive) to its own (inclusive); thread n closes the
+// tail.  Every offset is written exactly once; no atomics.
+__global__ void segment_offsets_kernel(const uint32_t* __restrict__ keys, int64_t n, uint32_t nkeys,
+                                       uint32_t* __restrict__ off) {
     const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (j < n) atomicAdd(&counts[keys[j]], 1u);
+    if (j > n) return;
+    const uint32_t lo = j == 0 ? 0u : keys[j - 1] + 1u;
+    const uint32_t hi = j == n ? nkeys : keys[j];
+    for (uint32_t c = lo; c <= hi && c <= nkeys; c++) off[c] = (uint32_t)j;
 }
 
-cudaError_t launch_count_keys(const uint32_t* keys, int64_t n, uint32_t* counts, cudaStream_t s) {
-    if (n == 0) return cudaSuccess;
+cudaError_t launch_segment_offsets(const uint32_t* sorted_keys, int64_t n, uint32_t nkeys, uint32_t* off,
+                                   cudaStream_t s) {
     ++g_launches;
-    count_keys_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(keys, n, counts);
+    segment_offsets_kernel<<<(unsigned)((n + 1 + 255) / 256), 256, 0, s>>>(sorted_keys, n, nkeys, off);
     return cudaGetLastError();
 }
 
@@ -287,6 +295,120 @@ cudaError_t launch_finish_items(int metric, int64_t nv, const double* xyz, const
     ++g_launches;
     finish_items_kernel<<<(unsigned)((nv + 255) / 256), 256, 0, s>>>(metric, nv, xyz, wd, varea, wsum, v_off, nmesh,
                                                                       ratio, pdirs, xw, ta, tb);
+    return cudaGetLastError();
+}
+
+}  // namespace acvd
+
+namespace acvd {
+
+// ---------------------------------------------------------------------------
+// Internal item order.  After colouring, items are renumbered so that every
+// colour class is one contiguous range (class by class, increasing original id
+// inside a class): perm[t] = original id of internal item t, inv[v] = internal
+// id of original vertex v.  The ring CSR is rebuilt in internal ids with each
+// ring's order kept, so the per-item streams of a colour step are coalesced.
+// ---------------------------------------------------------------------------
+__global__ void scatter_inv_kernel(const int* __restrict__ perm, int64_t n, int* __restrict__ inv) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) inv[perm[t]] = (int)t;
+}
+
+__global__ void perm_degree_kernel(const int* __restrict__ row, const int* __restrict__ perm, int64_t n,
+                                   uint32_t* __restrict__ deg) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) {
+        const int v = perm[t];
+        deg[t] = (uint32_t)(row[v + 1] - row[v]);
+    } else if (t == n) {
+        deg[n] = 0u;
+    }
+}
+
+__global__ void perm_ring_kernel(const int* __restrict__ row, const int* __restrict__ col,
+                                 const int* __restrict__ perm, const int* __restrict__ inv,
+                                 const uint32_t* __restrict__ row_new, int64_t n, int* __restrict__ col_new) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const int v = perm[t];
+    const int p0 = row[v], p1 = row[v + 1];
+    const uint32_t o = row_new[t];
+    for (int q = 0; q < p1 - p0; q++) col_new[o + q] = inv[col[p0 + q]];
+}
+
+__global__ void map_ids_kernel(const int* __restrict__ in, int64_t m, const int* __restrict__ inv,
+                               int* __restrict__ out) {
+    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < m) out[j] = inv[in[j]];
+}
+
+template <typename T>
+__global__ void gather_kernel(const T* __restrict__ src, const int* __restrict__ idx, int64_t n,
+                              T* __restrict__ dst) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) dst[t] = src[idx[t]];
+}
+
+__global__ void iota_kernel(int64_t n, int* __restrict__ out) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) out[t] = (int)t;
+}
+
+static inline unsigned grid_of(int64_t n) { return (unsigned)((n + 255) / 256); }
+
+cudaError_t launch_scatter_inv(const int* perm, int64_t n, int* inv, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    ++g_launches;
+    scatter_inv_kernel<<<grid_of(n), 256, 0, s>>>(perm, n, inv);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_perm_degree(const int* row, const int* perm, int64_t n, uint32_t* deg, cudaStream_t s) {
+    ++g_launches;
+    perm_degree_kernel<<<grid_of(n + 1), 256, 0, s>>>(row, perm, n, deg);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_perm_ring(const int* row, const int* col, const int* perm, const int* inv, const uint32_t* row_new,
+                             int64_t n, int* col_new, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    ++g_launches;
+    perm_ring_kernel<<<grid_of(n), 256, 0, s>>>(row, col, perm, inv, row_new, n, col_new);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_map_ids(const int* in, int64_t m, const int* inv, int* out, cudaStream_t s) {
+    if (m == 0) return cudaSuccess;
+    ++g_launches;
+    map_ids_kernel<<<grid_of(m), 256, 0, s>>>(in, m, inv, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gather_i32(const int* src, const int* idx, int64_t n, int* dst, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    ++g_launches;
+    gather_kernel<int><<<grid_of(n), 256, 0, s>>>(src, idx, n, dst);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gather_f4(const float4* src, const int* idx, int64_t n, float4* dst, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    ++g_launches;
+    gather_kernel<float4><<<grid_of(n), 256, 0, s>>>(src, idx, n, dst);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gather_f2(const float2* src, const int* idx, int64_t n, float2* dst, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    ++g_launches;
+    gather_kernel<float2><<<grid_of(n), 256, 0, s>>>(src, idx, n, dst);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_iota(int64_t n, int* out, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    ++g_launches;
+    iota_kernel<<<grid_of(n), 256, 0, s>>>(n, out);
     return cudaGetLastError();
 }
 
