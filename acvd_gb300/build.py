@@ -37,8 +37,12 @@ def _stale(obj: str, deps: list[str]) -> bool:
 
 
 def build(verbose: bool = False, force: bool = False) -> str:
+    """ACVD_NVCC_FLAGS (environment) adds nvcc flags, e.g. the tuning macros
+    -DACVD_EVAL_MINB=<blocks per SM of the evaluation kernel>; pass force=True
+    (or --force) when they change."""
     os.makedirs(OUT, exist_ok=True)
     nvcc = _nvcc()
+    extra = os.environ.get("ACVD_NVCC_FLAGS", "").split()
     headers = [os.path.join(SRC, f) for f in os.listdir(SRC) if f.endswith((".cuh", ".h"))]
     headers.append(os.path.join(os.path.dirname(HERE), "include", "acvd_gpu.h"))
     jobs = []
@@ -49,7 +53,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
         objs.append(obj)
         if force or _stale(obj, [src] + headers):
             jobs.append([nvcc, ARCH, "-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
-                         "-diag-suppress", "128", "-c", src, "-o", obj])
+                         "-diag-suppress", "128"] + extra + ["-c", src, "-o", obj])
     for f in CXX_SOURCES:
         src = os.path.join(SRC, f)
         obj = os.path.join(OUT, f + ".o")
@@ -72,4 +76,5 @@ def build(verbose: bool = False, force: bool = False) -> str:
 
 
 if __name__ == "__main__":
-    print(build(verbose=True))
+    import sys
+    print(build(verbose=True, force="--force" in sys.argv))

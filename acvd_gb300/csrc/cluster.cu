@@ -461,8 +461,14 @@ ACVD_DEV void eval_tile(const DevState& st, const int* __restrict__ items, int64
     warp_count(&st.counters[kCntCand], n_cand);
 }
 
+// blocks per SM the evaluation kernel is compiled for (registers per thread
+// follow: 3 -> 80, 4 -> 64; 4 measured fastest on the torus and heightfield workloads)
+#ifndef ACVD_EVAL_MINB
+#define ACVD_EVAL_MINB 4
+#endif
+
 template <int M>
-__global__ void __launch_bounds__(256, 3) eval_kernel(DevState st, const int* __restrict__ items, int64_t count,
+__global__ void __launch_bounds__(256, ACVD_EVAL_MINB) eval_kernel(DevState st, const int* __restrict__ items, int64_t count,
                                                       int color, int* cand_dest, unsigned* cand_prio, int claims) {
     eval_tile<M>(st, items, count, color, cand_dest, cand_prio, claims, blockIdx.x);
 }
