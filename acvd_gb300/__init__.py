@@ -5,7 +5,7 @@ include/acvd_gpu.h (libacvd_gb300.so, built in-tree by acvd_gb300.build).
 """
 from .engine import AcvdError, Engine, build_topology, initial_sampling, load, vertex_weights  # noqa: F401
 from .remesh import (AnisotropicDiscreteRemeshing, IsotropicDiscreteRemeshing,  # noqa: F401
-                     QIsotropicDiscreteRemeshing, Surface)
+                     QIsotropicDiscreteRemeshing, QuadricPostPlacement, Surface)
 
 __all__ = ["AcvdError", "Engine", "Surface", "IsotropicDiscreteRemeshing", "QIsotropicDiscreteRemeshing",
-           "AnisotropicDiscreteRemeshing", "build_topology", "initial_sampling", "vertex_weights", "load"]
+           "AnisotropicDiscreteRemeshing", "QuadricPostPlacement", "build_topology", "initial_sampling", "vertex_weights", "load"]

@@ -52,14 +52,15 @@ def build(verbose: bool = False, force: bool = False) -> str:
         obj = os.path.join(OUT, f + ".o")
         objs.append(obj)
         if force or _stale(obj, [src] + headers):
-            jobs.append([nvcc, ARCH, "-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
+            jobs.append([nvcc, ARCH, "-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off",
                          "-diag-suppress", "128"] + extra + ["-c", src, "-o", obj])
     for f in CXX_SOURCES:
         src = os.path.join(SRC, f)
         obj = os.path.join(OUT, f + ".o")
         objs.append(obj)
         if force or _stale(obj, [src] + headers):
-            jobs.append(["g++", "-O3", "-std=c++17", "-fPIC", "-c", src, "-o", obj])
+            # no FMA contraction: the host arithmetic gives the same bits on x86 and Arm
+            jobs.append(["g++", "-O3", "-std=c++17", "-fPIC", "-ffp-contract=off", "-c", src, "-o", obj])
 
     def run(cmd):
         r = subprocess.run(cmd, capture_output=True, text=True)

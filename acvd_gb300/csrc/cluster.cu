@@ -1322,6 +1322,69 @@ __global__ void centroids_kernel(DevState st, double* __restrict__ out) {
 }
 
 // ---------------------------------------------------------------------------
+// ACVD's quadric post-placement (DiscreteRemeshing/Examples/ACVD.cxx:217-291), FP64.
+// (1) per vertex: the unweighted plane quadrics (vtkQuadricTools::AddTriangleQuadric,
+// FullQuadric = false, Common/vtkQuadricTools.cxx:56-79) of its faces, in increasing
+// face id; (2) per cluster: the sum over its items in increasing vertex id, then the
+// output vertex moved by ComputeRepresentativePoint (.cxx:83-177): P + pinv(A)(b - A P),
+// A = (Q0 Q1 Q2 / Q4 Q5 / Q7), b = -(Q3, Q6, Q8), `level` singular values above
+// 1e-3 of the largest.
+// ---------------------------------------------------------------------------
+__global__ void vertex_quadric_kernel(const double* __restrict__ xyz, const int* __restrict__ tri,
+                                      const uint32_t* __restrict__ vf_row, const uint32_t* __restrict__ vf_face,
+                                      int64_t nv, double* __restrict__ qv) {
+    const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nv) return;
+    double q[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (uint32_t t = vf_row[v]; t < vf_row[v + 1]; t++) {
+        const int f = (int)vf_face[t];
+        const int a = tri[3 * f], b = tri[3 * f + 1], c = tri[3 * f + 2];
+        const double x1[3] = {xyz[3 * a], xyz[3 * a + 1], xyz[3 * a + 2]};
+        const double e1[3] = {xyz[3 * b] - x1[0], xyz[3 * b + 1] - x1[1], xyz[3 * b + 2] - x1[2]};
+        const double e2[3] = {xyz[3 * c] - x1[0], xyz[3 * c + 1] - x1[1], xyz[3 * c + 2] - x1[2]};
+        double n[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
+        const double len = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+        if (len > 0.0) { n[0] /= len; n[1] /= len; n[2] /= len; } else { n[0] = n[1] = n[2] = 0.0; }
+        const double d = -(n[0] * x1[0] + n[1] * x1[1] + n[2] * x1[2]);
+        q[0] += n[0] * n[0]; q[1] += n[0] * n[1]; q[2] += n[0] * n[2]; q[3] += n[0] * d;
+        q[4] += n[1] * n[1]; q[5] += n[1] * n[2]; q[6] += n[1] * d;
+        q[7] += n[2] * n[2]; q[8] += n[2] * d;
+    }
+    for (int j = 0; j < 9; j++) qv[9 * v + j] = q[j];
+}
+
+__global__ void first_nonempty_kernel(const int* __restrict__ size, int k, int* __restrict__ first) {
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c < k && size[c] > 0) atomicMin(first, (int)c);
+}
+
+// start: the output vertices (3K, the metric's cluster centroids); sorted: items
+// by cluster (original ids), seg_off / seg_cnt per cluster
+__global__ void post_place_kernel(const double* __restrict__ qv, const uint32_t* __restrict__ sorted,
+                                  const uint32_t* __restrict__ seg_off, const uint32_t* __restrict__ seg_cnt,
+                                  const int* __restrict__ size, const int* __restrict__ first,
+                                  const double* __restrict__ start, int k, int level, double* __restrict__ out) {
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= k) return;
+    double q[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (uint32_t t = 0; t < seg_cnt[c]; t++) {
+        const uint32_t v = sorted[seg_off[c] + t];
+        for (int j = 0; j < 9; j++) q[j] += qv[9 * (int64_t)v + j];
+    }
+    const int64_t src = size[c] > 0 ? c : (int64_t)(*first < k ? *first : 0);
+    const double P[3] = {start[3 * src], start[3 * src + 1], start[3 * src + 2]};
+    const double A[6] = {q[0], q[1], q[2], q[4], q[5], q[7]};
+    double AP[3];
+    sym_mul<double>(A, P, AP);
+    const double r[3] = {-q[3] - AP[0], -q[6] - AP[1], -q[8] - AP[2]};
+    double d[3];
+    pinv_apply<double>(A, r, d, level, 1e-3, 32);
+    out[3 * c] = P[0] + d[0];
+    out[3 * c + 1] = P[1] + d[1];
+    out[3 * c + 2] = P[2] + d[2];
+}
+
+// ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
 static inline unsigned nblk(int64_t n, int b = 256) { return (unsigned)((n + b - 1) / b); }
@@ -1514,6 +1577,30 @@ cudaError_t launch_dual_write(const int* tri, const int* faces, const int* sel, 
 cudaError_t launch_centroids(int metric, const DevState& st, double* out, cudaStream_t s) {
     if (st.k == 0) return cudaSuccess;
     ACVD_DISPATCH(metric, centroids_kernel, nblk(st.k), 256, s, st, out);
+    return cudaGetLastError();
+}
+
+}  // namespace acvd
+
+namespace acvd {
+
+cudaError_t launch_vertex_quadrics(const double* xyz, const int* tri, const uint32_t* vf_row, const uint32_t* vf_face,
+                                   int64_t nv, double* qv, cudaStream_t s) {
+    if (nv == 0) return cudaSuccess;
+    ++g_launches;
+    vertex_quadric_kernel<<<nblk(nv), 256, 0, s>>>(xyz, tri, vf_row, vf_face, nv, qv);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_post_place(const double* qv, const uint32_t* sorted, const uint32_t* seg_off,
+                              const uint32_t* seg_cnt, const int* size, int* first, const double* start, int k,
+                              int level, double* out, cudaStream_t s) {
+    if (k == 0) return cudaSuccess;
+    cudaError_t e = cudaMemsetAsync(first, 0x7f, sizeof(int), s);
+    if (e != cudaSuccess) return e;
+    g_launches += 2;
+    first_nonempty_kernel<<<nblk(k), 256, 0, s>>>(size, k, first);
+    post_place_kernel<<<nblk(k, 128), 128, 0, s>>>(qv, sorted, seg_off, seg_cnt, size, first, start, k, level, out);
     return cudaGetLastError();
 }
 

@@ -1147,6 +1147,47 @@ extern "C" int acvd_get_boundary_edges(acvd_ctx* ctx, int32_t* ids, int64_t* cou
     return ACVD_OK;
 }
 
+// ACVD's quadric post-placement of the output vertices (ACVD.cxx:217-291) for the
+// current clustering; points: 3K doubles.
+extern "C" int acvd_post_placement(acvd_ctx* ctx, int level, double* points) {
+    if (!ctx || !points) return ACVD_ERR_ARG;
+    if (!ctx->ready_metric || !ctx->ready_labels) return fail(ctx, ACVD_ERR_ARG, "no metric or labels");
+    if (level < 0 || level > 3) return fail(ctx, ACVD_ERR_ARG, "acvd_post_placement: level outside [0, 3]");
+    CK(cudaSetDevice(ctx->opts.device));
+    ctx->flags.level = ctx->level;
+    int r = upload_flags(ctx);
+    if (r) return r;
+    r = recompute(ctx);
+    if (r) return r;
+    const int64_t nv = ctx->nV;
+    const int K = ctx->K;
+    // the output vertices before placement: the metric's cluster centroids
+    DBuf<double> start, qv, out;
+    CK(start.resize(3 * (size_t)K));
+    CK(launch_centroids(ctx->metric, ctx->state(), start.p, ctx->s));
+    // items by cluster, in original vertex ids
+    CK(ctx->label_orig.resize(nv));
+    CK(launch_gather_i32(ctx->label.p, ctx->inv.p, nv, ctx->label_orig.p, ctx->s));
+    DevState st = ctx->state();
+    st.label = ctx->label_orig.p;
+    CK(ctx->wk_a.resize(nv)); CK(ctx->wk_b.resize(nv)); CK(ctx->wk_c.resize(nv)); CK(ctx->wk_d.resize(nv));
+    CK(ctx->wk_cnt.resize(K + 1)); CK(ctx->wk_off.resize(K + 1));
+    CK(cudaMemsetAsync(ctx->wk_cnt.p, 0, (K + 1) * sizeof(uint32_t), ctx->s));
+    CK(launch_cluster_keys(st, ctx->wk_a.p, ctx->wk_b.p, ctx->wk_cnt.p, ctx->s));
+    CK(radix_sort_pairs(ctx->wk_a.p, ctx->wk_b.p, ctx->wk_c.p, ctx->wk_d.p, nv, bits_for((uint64_t)K), ctx->scratch,
+                        ctx->s));
+    CK(exclusive_scan_u32(ctx->wk_cnt.p, ctx->wk_off.p, K + 1, nullptr, ctx->scratch, ctx->s));
+    CK(qv.resize(9 * (size_t)nv));
+    CK(launch_vertex_quadrics(ctx->xyz.p, ctx->tri.p, ctx->vf_row.p, ctx->vf_face.p, nv, qv.p, ctx->s));
+    CK(out.resize(3 * (size_t)K));
+    CK(ctx->dtmp.resize(2));
+    CK(launch_post_place(qv.p, ctx->wk_b.p, ctx->wk_off.p, ctx->wk_cnt.p, (const int*)ctx->wk_cnt.p, (int*)ctx->dtmp.p,
+                         start.p, K, level, out.p, ctx->s));
+    CK(cudaMemcpyAsync(points, out.p, 3 * (size_t)K * sizeof(double), cudaMemcpyDeviceToHost, ctx->s));
+    CK(cudaStreamSynchronize(ctx->s));
+    return ACVD_OK;
+}
+
 extern "C" int acvd_get_dual_mesh(acvd_ctx* ctx, int32_t* tris, int64_t* n_tris) {
     if (!ctx || !n_tris) return ACVD_ERR_ARG;
     if (!ctx->ready_labels) return fail(ctx, ACVD_ERR_ARG, "no labels");

@@ -232,6 +232,11 @@ cudaError_t launch_dual_unique(const uint32_t* klo, const uint32_t* khi, const u
 cudaError_t launch_dual_write(const int* tri, const int* faces, const int* sel, int64_t t, const int* label,
                               int* out, cudaStream_t s);
 cudaError_t launch_centroids(int metric, const DevState& st, double* out, cudaStream_t s);
+cudaError_t launch_vertex_quadrics(const double* xyz, const int* tri, const uint32_t* vf_row, const uint32_t* vf_face,
+                                   int64_t nv, double* qv, cudaStream_t s);
+cudaError_t launch_post_place(const double* qv, const uint32_t* sorted, const uint32_t* seg_off,
+                              const uint32_t* seg_cnt, const int* size, int* first, const double* start, int k,
+                              int level, double* out, cudaStream_t s);
 
 // ---- adjoint (adjoint.cu) ----
 // Work arrays and inputs of the fixed-clustering adjoint (FP64).

@@ -92,6 +92,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         "acvd_get_boundary_edges": (ctypes.c_int, [_P, _P, ctypes.POINTER(_i64)]),
         "acvd_get_dual_mesh": (ctypes.c_int, [_P, _P, ctypes.POINTER(_i64)]),
         "acvd_boundary_edges_noalloc": (ctypes.c_int, [_P, _i64, _P, _P, _P, _P]),
+        "acvd_post_placement": (ctypes.c_int, [_P, ctypes.c_int, _P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -264,6 +265,12 @@ class Engine:
         st = Stats()
         self._ck(self._lib.acvd_minimize(self.ctx, ctypes.byref(st)), "acvd_minimize")
         return st.as_dict()
+
+    def post_placement(self, level: int = 1) -> np.ndarray:
+        """ACVD's quadric post-placement of the output vertices (ACVD.cxx:217-291): (K, 3)."""
+        out = np.empty((self.k, 3), dtype=np.float64)
+        self._ck(self._lib.acvd_post_placement(self.ctx, int(level), _ptr(out)), "acvd_post_placement")
+        return out
 
     def labels(self, out: np.ndarray | None = None) -> np.ndarray:
         """GetClustering(); `out` (int32, n items, contiguous) may be a caller's buffer,

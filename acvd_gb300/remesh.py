@@ -227,6 +227,18 @@ class AnisotropicDiscreteRemeshing(_DiscreteRemeshing):
     _metric_name = "aniso"
 
 
+def QuadricPostPlacement(remesh: _DiscreteRemeshing, level: int = 1) -> Surface:
+    """The ACVD driver's step after Remesh() (DiscreteRemeshing/Examples/ACVD.cxx:217-291,
+    run there when QuadricsOptimizationLevel != 0; its default is 1): every output
+    vertex moves to the point minimising the summed plane quadrics of the faces
+    around its cluster's items.  Updates remesh.GetOutput() in place and returns it."""
+    if level == 0:
+        return remesh.Output
+    pts = remesh._engine.post_placement(level)
+    remesh.Output.points = pts
+    return remesh.Output
+
+
 # the reference's class names
 vtkIsotropicDiscreteRemeshing = IsotropicDiscreteRemeshing
 vtkQIsotropicDiscreteRemeshing = QIsotropicDiscreteRemeshing

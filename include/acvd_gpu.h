@@ -205,6 +205,17 @@ int acvd_boundary_edges_noalloc(const int32_t* d_edge_v, int64_t n_edges, const 
                                 int32_t* d_ids, uint32_t* d_count, void* stream);
 
 /*
+ * ACVD's quadric post-placement of the output vertices
+ * (DiscreteRemeshing/Examples/ACVD.cxx:217-291, the ACVD driver's step after
+ * Remesh()): per cluster, the unweighted plane quadrics of every face adjacent to
+ * each of its items; each output vertex -- the metric's cluster centroid, the first
+ * non-empty cluster's for an empty one -- moved by
+ * vtkQuadricTools::ComputeRepresentativePoint with `level` singular values (ACVD's
+ * default is 1).  FP64.  points: 3K doubles.
+ */
+int acvd_post_placement(acvd_ctx* ctx, int level, double* points);
+
+/*
  * Dual mesh (BuildDelaunayTriangulation, DiscreteRemeshing/vtkDiscreteRemeshing.h:1003-1152,
  * vertex clustering, without manifold repair): one triangle per input face whose
  * three labels are valid and distinct, in face order, duplicates (same label set)

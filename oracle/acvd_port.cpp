@@ -939,4 +939,32 @@ long long port_dual_mesh(void* hp, int* tris, double* verts) {
     return count;
 }
 
+// ACVD's quadric post-placement (DiscreteRemeshing/Examples/ACVD.cxx:217-291): per
+// cluster, the unweighted plane quadrics (FullQuadric = false) of all faces adjacent to
+// each of its items (a face once per item, items in increasing id, faces in the
+// vertex's ring order); the output vertex -- the cluster centroid, or the first
+// non-empty cluster's for an empty one (BuildDelaunayTriangulation,
+// vtkDiscreteRemeshing.h:1024-1033) -- moved by ComputeRepresentativePoint with
+// `level` singular values.  verts: 3K.
+void port_post_placement(void* hp, int level, double* verts) {
+    EngineBase* e = ((PortHandle*)hp)->eng;
+    const Mesh& m = e->mesh;
+    std::vector<double> Q(9 * (size_t)e->K, 0.0);
+    std::vector<idt> fl;
+    for (idt i = 0; i < m.nV; i++) {
+        const int c = e->labels[i];
+        if (c < 0 || c >= e->K) continue;
+        m.vertex_faces(i, fl);
+        for (idt f : fl) m.add_triangle_quadric(&Q[9 * (size_t)c], f);
+    }
+    int valid = 0;
+    for (int k = 0; k < e->K; k++) if (e->sizes[k] > 0) { valid = k; break; }
+    for (int k = 0; k < e->K; k++) {
+        double S[3], W, Qc[9], c[3];
+        e->cluster_accum(e->sizes[k] == 0 ? valid : k, S, &W, Qc, c);
+        representative_point(&Q[9 * (size_t)k], c, level);
+        verts[3 * k] = c[0]; verts[3 * k + 1] = c[1]; verts[3 * k + 2] = c[2];
+    }
+}
+
 }  // extern "C"

@@ -66,6 +66,7 @@ def _bind(lib, prefix):
         "get_clusters": f("get_clusters", None, _P, _pd, _pd, _pd, _pd, _pd, _pi),
         "clean": f("clean", ctypes.c_int, _P),
         "fill_holes": f("fill_holes", ctypes.c_int, _P),
+        "post_placement": f("post_placement", None, _P, ctypes.c_int, _pd),
     }
     return fns
 
@@ -154,6 +155,13 @@ class _Base:
 
     def clean(self) -> int:
         return int(self.f["clean"](self.h))
+
+    def post_placement(self, level: int = 1) -> np.ndarray:
+        """ACVD's quadric post-placement of the output vertices (ACVD.cxx:217-291) for
+        the current clustering and cluster statistics (call evaluate first)."""
+        out = np.empty((self.k, 3), dtype=np.float64)
+        self.f["post_placement"](self.h, int(level), out.ravel())
+        return out
 
     def fill_holes(self) -> int:
         return int(self.f["fill_holes"](self.h))

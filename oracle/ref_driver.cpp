@@ -52,6 +52,7 @@ struct RefBase {
     virtual int fill() = 0;
     virtual void set_labels(const int* lab) = 0;
     virtual int loops() = 0;
+    virtual void post_placement(int level, double* out) = 0;
 };
 
 template <class M>
@@ -159,6 +160,32 @@ struct Ref : RefBase {
         return bad;
     }
     int loops() override { return p->NumberOfLoops; }
+    // The post-placement loop of DiscreteRemeshing/Examples/ACVD.cxx:217-291 (a driver
+    // program, restated here as a loop) over the reference's own
+    // vtkQuadricTools::AddTriangleQuadric / ComputeRepresentativePoint and the
+    // metric's GetClusterCentroid (the output vertices of BuildDelaunayTriangulation,
+    // vtkDiscreteRemeshing.h:1024-1033).  Needs the cluster statistics (evaluate).
+    void post_placement(int level, double* out) override {
+        vtkSurface* mesh = p->GetInput();
+        std::vector<double> Q(9 * (size_t)K, 0.0);
+        vtkIdList* fl = vtkIdList::New();
+        for (long long i = 0; i < n; i++) {
+            const int c = p->Clustering->GetValue(i);
+            if (c < 0 || c >= K) continue;
+            mesh->GetVertexNeighbourFaces(i, fl);
+            for (vtkIdType j = 0; j < fl->GetNumberOfIds(); j++)
+                vtkQuadricTools::AddTriangleQuadric(&Q[9 * (size_t)c], mesh, fl->GetId(j), false);
+        }
+        fl->Delete();
+        int valid = 0;
+        for (int k = 0; k < K; k++) if (p->ClustersSizes->GetValue(k) > 0) { valid = k; break; }
+        for (int k = 0; k < K; k++) {
+            double P[3];
+            p->GetMetric()->GetClusterCentroid(p->GetCluster(p->ClustersSizes->GetValue(k) == 0 ? valid : k), P);
+            vtkQuadricTools::ComputeRepresentativePoint(&Q[9 * (size_t)k], P, level);
+            out[3 * k] = P[0]; out[3 * k + 1] = P[1]; out[3 * k + 2] = P[2];
+        }
+    }
 };
 
 extern "C" {
@@ -184,5 +211,6 @@ void ref_get_clusters(void* h, double* S, double* W, double* Q, double* C, doubl
 int ref_clean(void* h) { return ((RefBase*)h)->clean(); }
 int ref_fill_holes(void* h) { return ((RefBase*)h)->fill(); }
 int ref_loops(void* h) { return ((RefBase*)h)->loops(); }
+void ref_post_placement(void* h, int level, double* out) { ((RefBase*)h)->post_placement(level, out); }
 
 }  // extern "C"

@@ -5,7 +5,8 @@ The reference's clustering headers are compiled unmodified against the VTK shim
 $ACVD_REFERENCE_ROOT).  For each small case below this script stores the inputs
 (so that no platform's libm is needed to regenerate them) and the reference's
 outputs: the initial sampling, the converged labels, global energy, per-cluster
-sizes / centroids / energies, and the accumulators of a fixed assignment.
+sizes / centroids / energies, the accumulators of a fixed assignment and its
+quadric post-placement (the ACVD driver's last step) at levels 1 and 3.
 
     python tests/golden/gen_golden.py
 """
@@ -61,7 +62,9 @@ def main():
                  size=cl["size"], centroid=cl["centroid"], cluster_energy=cl["energy"],
                  fixed_labels=fixed, fixed_S=cf["S"], fixed_W=cf["W"], fixed_Q=cf["Q"],
                  fixed_centroid=cf["centroid"], fixed_cluster_energy=cf["energy"],
-                 fixed_energy=r2.global_energy())
+                 fixed_energy=r2.global_energy(),
+                 # ACVD's quadric post-placement (ACVD.cxx:217-291) of the fixed assignment
+                 fixed_post1=r2.post_placement(1), fixed_post3=r2.post_placement(3))
         if initial is not None:
             d["initial"] = initial
         if ind is not None:

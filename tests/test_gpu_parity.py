@@ -164,6 +164,11 @@ def test_remesh_api_end_to_end():
     assert out.GetNumberOfCells() > 500
     lab = r.GetClustering()
     assert lab.shape == (m.n_points,) and lab.max() < 300
+    # the ACVD driver's quadric post-placement moves the output vertices in place
+    before = out.points.copy()
+    placed = acvd_gb300.QuadricPostPlacement(r, 1)
+    assert placed is out and np.all(np.isfinite(placed.points))
+    assert not np.array_equal(before, placed.points)
 
 
 def test_error_paths():
@@ -245,3 +250,25 @@ def test_persistent_schedule_matches_per_phase_kernels(oracle_lib, case):
     for key in ("sweeps", "moves", "relaxed_sweeps", "convergences", "candidates", "reverted"):
         assert st_p[key] == st_k[key], (key, st_p[key], st_k[key])
     assert st_p["energy"] == st_k["energy"]
+
+
+@pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p)[:-4] for p in GOLDEN])
+def test_post_placement_matches_reference(path):
+    """ACVD's quadric post-placement (ACVD.cxx:217-291) of the reference's fixed
+    assignment against the reference's own output (golden).  The face quadrics and the
+    placement are FP64; the start points are the metric's cluster centroids, built from
+    the float32 item records like every accumulator here, hence REL_ACC relative to the
+    mesh size (a placement with fewer than three singular values keeps the start point
+    along the unused directions)."""
+    g = _load(path)
+    metric = str(g["metric"])
+    grad = float(g["gradation"])
+    ind = g.get("indicator")
+    e, _ = _engine(g["points"], g["faces"], metric, ind if (grad > 0 or metric == "aniso") else None,
+                   g.get("principal_dirs"), grad)
+    e.set_labels(int(g["k"]), g["fixed_labels"])
+    scale = float(np.ptp(g["points"], axis=0).max())
+    for level, key in ((1, "fixed_post1"), (3, "fixed_post3")):
+        got = e.post_placement(level)
+        np.testing.assert_allclose(got, g[key], rtol=0, atol=REL_ACC * scale)
+    e.close()

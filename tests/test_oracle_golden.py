@@ -52,3 +52,13 @@ def test_fixed_assignment_accumulators(oracle_lib, path):
     np.testing.assert_array_equal(cl["centroid"], g["fixed_centroid"])
     np.testing.assert_array_equal(cl["energy"], g["fixed_cluster_energy"])
     assert p.global_energy() == float(g["fixed_energy"])
+
+
+@pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p)[:-4] for p in GOLDEN])
+def test_fixed_assignment_post_placement(oracle_lib, path):
+    """ACVD's quadric post-placement (ACVD.cxx:217-291) of the fixed assignment."""
+    g = _load(path)
+    p = _port(oracle_lib, g)
+    p.evaluate(g["fixed_labels"], 1)
+    np.testing.assert_array_equal(p.post_placement(1), g["fixed_post1"])
+    np.testing.assert_array_equal(p.post_placement(3), g["fixed_post3"])

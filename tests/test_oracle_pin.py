@@ -72,3 +72,26 @@ def test_clean_and_fill_equal_reference(oracle_lib):
     np.testing.assert_array_equal(res[0][1], res[1][1])
     assert res[0][2] == res[1][2]
     np.testing.assert_array_equal(res[0][3], res[1][3])
+
+
+@pytest.mark.parametrize("case", [0, 3, 6])
+def test_post_placement_equals_reference(oracle_lib, case):
+    """ACVD's quadric post-placement (ACVD.cxx:217-291): the restatement against the
+    same loop over the reference's own vtkQuadricTools, bit for bit."""
+    O = oracle_lib
+    _need_ref(O)
+    metric, mk, k, grad, uinit, seeds = CASES[case]
+    m = mk()
+    ind = m.indicator if (grad > 0 or metric == "aniso") else None
+    pd = m.principal_dirs if metric == "aniso" else None
+    r = O.Ref(metric, m.points, m.faces, k, grad, ind, pd, unconstrained_init=uinit)
+    r.init(None)
+    r.run()
+    lab = r.labels()
+    out = []
+    for cls in (O.Port, O.Ref):
+        p = cls(metric, m.points, m.faces, k, grad, ind, pd)
+        p.evaluate(lab, 1)
+        out.append((p.post_placement(1), p.post_placement(3)))
+    np.testing.assert_array_equal(out[0][0], out[1][0])
+    np.testing.assert_array_equal(out[0][1], out[1][1])
