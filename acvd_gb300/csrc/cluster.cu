@@ -254,7 +254,7 @@ ACVD_DEV bool ring_connected_pref(const DevState& st, int p0, int p1, int L, con
 // proposal and its claims.  Unassigned items and items with more than kMaxTgt
 // destinations run the whole test in B2.
 template <int M>
-ACVD_DEV void eval_tile(const DevState& st, const int* __restrict__ items, int64_t count, int color,
+ACVD_DEV void eval_tile(const DevState& st, int item0, int64_t count, int color,
                         int* cand_dest, unsigned* cand_prio, int claims, int64_t tile) {
     __shared__ int s_idx[256];                 // work item -> colour-list position
     __shared__ int s_tgt[256][kMaxTgt];        // work item -> destination clusters (ring order)
@@ -275,14 +275,20 @@ ACVD_DEV void eval_tile(const DevState& st, const int* __restrict__ items, int64
     const RunFlags fl = *st.flags;
     unsigned n_slots = 0, n_bnd = 0, n_tgt = 0, n_cand = 0;
     if (in) {
-        const int i = items[idx];
+        const int i = item0 + (int)idx;
+        const int4 ra = st.ring8[2 * (int64_t)i], rb = st.ring8[2 * (int64_t)i + 1];
         const int L = st.label[i];
-        const int p0 = st.row[i], p1 = st.row[i + 1];
         const int ev_i = st.evald[i];
-        const int deg = p1 - p0;
-        int lb[kRingPref];
+        int lb[kRingPref] = {ra.x, ra.y, ra.z, ra.w, rb.x, rb.y, rb.z, rb.w};
+        const bool longer = lb[7] == -2;   // ring longer than 8: bounds and tail from the CSR
+        int deg = 0;
+        if (longer) {
+            deg = st.row[i + 1] - st.row[i];
+            lb[7] = st.col[st.row[i] + 7];
+        } else {
 #pragma unroll
-        for (int q = 0; q < kRingPref; q++) lb[q] = q < deg ? st.col[p0 + q] : -1;
+            for (int q = 0; q < kRingPref; q++) deg += lb[q] >= 0;
+        }
 #pragma unroll
         for (int q = 0; q < kRingPref; q++) lb[q] = lb[q] >= 0 ? st.label[lb[q]] : L;
         bool fresh = ev_i <= sw.floor || (L < st.k && st.stamp[L] >= ev_i);
@@ -296,17 +302,21 @@ ACVD_DEV void eval_tile(const DevState& st, const int* __restrict__ items, int64
                 if (B < st.k && st.stamp[B] >= ev_i) fresh = true;
             }
         }
-        for (int q = kRingPref; q < deg; q++) {
-            const int B = st.label[st.col[p0 + q]];
-            if (B != L) {
-                boundary = true;
-                if (B < st.k && st.stamp[B] >= ev_i) fresh = true;
+        if (longer) {
+            const int p0 = st.row[i];
+            for (int q = kRingPref; q < deg; q++) {
+                const int B = st.label[st.col[p0 + q]];
+                if (B != L) {
+                    boundary = true;
+                    if (B < st.k && st.stamp[B] >= ev_i) fresh = true;
+                }
             }
         }
         if (boundary && fresh) {
             n_bnd = 1;
             const bool movable =
-                L >= st.k || (st.size[L] > 1 && (!fl.connexity || ring_connected_pref(st, p0, p1, L, lb)));
+                L >= st.k ||
+                (st.size[L] > 1 && (!fl.connexity || ring_connected_pref(st, st.row[i], st.row[i] + deg, L, lb)));
             if (movable) {
                 const int w = (int)atomicAdd(&s_nwork, 1u);
                 s_idx[w] = (int)idx;
@@ -348,7 +358,7 @@ ACVD_DEV void eval_tile(const DevState& st, const int* __restrict__ items, int64
     for (unsigned t = threadIdx.x; t < ntask; t += 256) {
         const unsigned code = s_task[t];
         const int w = (int)(code >> 4), j = (int)(code & 15u);
-        const int i = items[s_idx[w]];
+        const int i = item0 + s_idx[w];
         ItemRec it;
         load_item<M>(st, i, it);
         if (j == kTaskRemove) {
@@ -368,7 +378,7 @@ ACVD_DEV void eval_tile(const DevState& st, const int* __restrict__ items, int64
     if (threadIdx.x < s_nwork) {
         const int w = threadIdx.x;
         const int widx = s_idx[w];
-        const int i = items[widx];
+        const int i = item0 + widx;
         const int L = st.label[i];
         const int nt = s_nt[w];
         int best = -1;
@@ -468,9 +478,9 @@ ACVD_DEV void eval_tile(const DevState& st, const int* __restrict__ items, int64
 #endif
 
 template <int M>
-__global__ void __launch_bounds__(256, ACVD_EVAL_MINB) eval_kernel(DevState st, const int* __restrict__ items, int64_t count,
+__global__ void __launch_bounds__(256, ACVD_EVAL_MINB) eval_kernel(DevState st, int item0, int64_t count,
                                                       int color, int* cand_dest, unsigned* cand_prio, int claims) {
-    eval_tile<M>(st, items, count, color, cand_dest, cand_prio, claims, blockIdx.x);
+    eval_tile<M>(st, item0, count, color, cand_dest, cand_prio, claims, blockIdx.x);
 }
 
 // ---------------------------------------------------------------------------
@@ -646,7 +656,7 @@ ACVD_DEV void update_cluster(const DevState& st, int k) {
 // cluster B, the odd lane the source cluster L; the pair exchanges the two new
 // energies and both take the same decision.
 template <int M>
-ACVD_DEV void apply_range(const DevState& st, const int* __restrict__ items, int color, int round, int* cand_dest,
+ACVD_DEV void apply_range(const DevState& st, int item0, int color, int round, int* cand_dest,
                           const unsigned* cand_prio, unsigned gtid, unsigned gstride) {
     const unsigned n = st.cand_count[color];
     const unsigned epoch = (unsigned)(color * kRounds + round);
@@ -657,7 +667,7 @@ ACVD_DEV void apply_range(const DevState& st, const int* __restrict__ items, int
         const int idx = st.cand_list[j];
         const int B = cand_dest[idx];
         if (B < 0) continue;                     // committed or dropped in an earlier round
-        const int i = items[idx];
+        const int i = item0 + (int)idx;
         const int L = st.label[i];
         const unsigned long long key = make_claim(epoch, cand_prio[idx], (unsigned)idx);
         if (st.claim[B] != key || (L < st.k && st.claim[L] != key)) continue;
@@ -726,9 +736,9 @@ ACVD_DEV void apply_range(const DevState& st, const int* __restrict__ items, int
 }
 
 template <int M>
-__global__ void __launch_bounds__(256) apply_kernel(DevState st, const int* __restrict__ items, int color,
+__global__ void __launch_bounds__(256) apply_kernel(DevState st, int item0, int color,
                                                     int round, int* cand_dest, const unsigned* cand_prio) {
-    apply_range<M>(st, items, color, round, cand_dest, cand_prio, blockIdx.x * blockDim.x + threadIdx.x,
+    apply_range<M>(st, item0, color, round, cand_dest, cand_prio, blockIdx.x * blockDim.x + threadIdx.x,
                    gridDim.x * blockDim.x);
 }
 
@@ -736,7 +746,7 @@ __global__ void __launch_bounds__(256) apply_kernel(DevState st, const int* __re
 // by this step's commits still carries an exact energy change and claims again
 // with a newer epoch; one that lost a cluster to a commit is dropped (its item
 // is evaluated again next sweep).
-ACVD_DEV void reclaim_range(const DevState& st, const int* __restrict__ items, int color, int round, int* cand_dest,
+ACVD_DEV void reclaim_range(const DevState& st, int item0, int color, int round, int* cand_dest,
                             const unsigned* cand_prio, unsigned gtid, unsigned gstride) {
     const unsigned n = st.cand_count[color];
     const unsigned epoch = (unsigned)(color * kRounds + round);
@@ -744,7 +754,7 @@ ACVD_DEV void reclaim_range(const DevState& st, const int* __restrict__ items, i
         const int idx = st.cand_list[j];
         const int B = cand_dest[idx];
         if (B < 0) continue;
-        const int L = st.label[items[idx]];
+        const int L = st.label[item0 + idx];
         if (st.claim[B] == 0ull || (L < st.k && st.claim[L] == 0ull)) {
             cand_dest[idx] = -1;
             continue;
@@ -755,9 +765,9 @@ ACVD_DEV void reclaim_range(const DevState& st, const int* __restrict__ items, i
     }
 }
 
-__global__ void reclaim_kernel(DevState st, const int* __restrict__ items, int color, int round, int* cand_dest,
+__global__ void reclaim_kernel(DevState st, int item0, int color, int round, int* cand_dest,
                                const unsigned* cand_prio) {
-    reclaim_range(st, items, color, round, cand_dest, cand_prio, blockIdx.x * blockDim.x + threadIdx.x,
+    reclaim_range(st, item0, color, round, cand_dest, cand_prio, blockIdx.x * blockDim.x + threadIdx.x,
                   gridDim.x * blockDim.x);
 }
 
@@ -803,7 +813,7 @@ ACVD_DEV df from_fixed(long long d, float4 p) {
 }
 
 template <int M>
-ACVD_DEV void relaxed_commit_range(const DevState& st, const int* __restrict__ items, int color,
+ACVD_DEV void relaxed_commit_range(const DevState& st, int item0, int color,
                                    const int* cand_dest, unsigned gtid, unsigned gstride) {
     constexpr int NA = Layout<M>::acc;
     const unsigned n = st.cand_count[color];
@@ -811,7 +821,7 @@ ACVD_DEV void relaxed_commit_range(const DevState& st, const int* __restrict__ i
     const int now = st.sweep->sweep;
     for (unsigned j = gtid; j < n; j += gstride) {
         const int idx = st.cand_list[j];
-        const int i = items[idx];
+        const int i = item0 + (int)idx;
         const int B = cand_dest[idx];
         const int L = st.label[i];
         // sizes are untouched until fx_finalize: a cluster whose every member would
@@ -840,8 +850,8 @@ ACVD_DEV void relaxed_commit_range(const DevState& st, const int* __restrict__ i
 }
 
 template <int M>
-__global__ void relaxed_commit_kernel(DevState st, const int* __restrict__ items, int color, const int* cand_dest) {
-    relaxed_commit_range<M>(st, items, color, cand_dest, blockIdx.x * blockDim.x + threadIdx.x,
+__global__ void relaxed_commit_kernel(DevState st, int item0, int color, const int* cand_dest) {
+    relaxed_commit_range<M>(st, item0, color, cand_dest, blockIdx.x * blockDim.x + threadIdx.x,
                             gridDim.x * blockDim.x);
 }
 
@@ -999,7 +1009,7 @@ __global__ void __launch_bounds__(256, 2) sweep_run_kernel(SweepRun a) {
             const long long o0 = a.off[c];
             const int64_t cnt = a.off[c + 1] - o0;
             if (cnt == 0) continue;
-            const int* items = a.items + o0;
+            const int item0 = (int)o0;
             if (!relaxed) {
                 for (int64_t k = gtid; k <= st.k; k += gstride) st.claim[k] = ~0ull;
                 if (!grid_barrier(a.bar)) return;
@@ -1007,21 +1017,21 @@ __global__ void __launch_bounds__(256, 2) sweep_run_kernel(SweepRun a) {
             const unsigned long long t0 = lead ? global_ns() : 0ull;
             const int64_t ntiles = (cnt + 255) / 256;
             for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x)
-                eval_tile<M>(st, items, cnt, c, a.cand_dest, a.cand_prio, relaxed ? 0 : 1, t);
+                eval_tile<M>(st, item0, cnt, c, a.cand_dest, a.cand_prio, relaxed ? 0 : 1, t);
             if (!grid_barrier(a.bar)) return;
             if (lead) a.ls->eval_ns += global_ns() - t0;
             if (relaxed) {
-                relaxed_commit_range<M>(st, items, c, a.cand_dest, gtid, gstride);
+                relaxed_commit_range<M>(st, item0, c, a.cand_dest, gtid, gstride);
                 if (!grid_barrier(a.bar)) return;
                 fx_finalize_range<M>(st, gtid, gstride);
                 if (!grid_barrier(a.bar)) return;
             } else {
-                apply_range<M>(st, items, c, 0, a.cand_dest, a.cand_prio, gtid, gstride);
+                apply_range<M>(st, item0, c, 0, a.cand_dest, a.cand_prio, gtid, gstride);
                 if (!grid_barrier(a.bar)) return;
                 for (int r = 1; r < a.match_rounds; r++) {
-                    reclaim_range(st, items, c, r, a.cand_dest, a.cand_prio, gtid, gstride);
+                    reclaim_range(st, item0, c, r, a.cand_dest, a.cand_prio, gtid, gstride);
                     if (!grid_barrier(a.bar)) return;
-                    apply_range<M>(st, items, c, r, a.cand_dest, a.cand_prio, gtid, gstride);
+                    apply_range<M>(st, item0, c, r, a.cand_dest, a.cand_prio, gtid, gstride);
                     if (!grid_barrier(a.bar)) return;
                 }
             }
@@ -1397,10 +1407,10 @@ static inline unsigned nblk(int64_t n, int b = 256) { return (unsigned)((n + b -
         else KERNEL<kAniso><<<grid, block, 0, stream>>>(__VA_ARGS__);                     \
     } while (0)
 
-cudaError_t launch_eval(int metric, const DevState& st, const int* items, int64_t count, int color,
+cudaError_t launch_eval(int metric, const DevState& st, int item0, int64_t count, int color,
                         int* cand_dest, unsigned* cand_prio, bool claims, cudaStream_t s) {
     if (count == 0) return cudaSuccess;
-    ACVD_DISPATCH(metric, eval_kernel, nblk(count), 256, s, st, items, count, color, cand_dest, cand_prio,
+    ACVD_DISPATCH(metric, eval_kernel, nblk(count), 256, s, st, item0, count, color, cand_dest, cand_prio,
                   claims ? 1 : 0);
     return cudaGetLastError();
 }
@@ -1414,25 +1424,25 @@ static unsigned list_grid(int64_t count) {
     return (unsigned)std::min<int64_t>(nblk(count), 2 * (int64_t)sms);
 }
 
-cudaError_t launch_apply(int metric, const DevState& st, const int* items, int64_t count, int color, int round,
+cudaError_t launch_apply(int metric, const DevState& st, int item0, int64_t count, int color, int round,
                          int* cand_dest, const unsigned* cand_prio, cudaStream_t s) {
     if (count == 0) return cudaSuccess;
-    ACVD_DISPATCH(metric, apply_kernel, list_grid(count), 256, s, st, items, color, round, cand_dest, cand_prio);
+    ACVD_DISPATCH(metric, apply_kernel, list_grid(count), 256, s, st, item0, color, round, cand_dest, cand_prio);
     return cudaGetLastError();
 }
 
-cudaError_t launch_reclaim(const DevState& st, const int* items, int64_t count, int color, int round,
+cudaError_t launch_reclaim(const DevState& st, int item0, int64_t count, int color, int round,
                            int* cand_dest, const unsigned* cand_prio, cudaStream_t s) {
     if (count == 0) return cudaSuccess;
     ++g_launches;
-    reclaim_kernel<<<list_grid(count), 256, 0, s>>>(st, items, color, round, cand_dest, cand_prio);
+    reclaim_kernel<<<list_grid(count), 256, 0, s>>>(st, item0, color, round, cand_dest, cand_prio);
     return cudaGetLastError();
 }
 
-cudaError_t launch_relaxed_step(int metric, const DevState& st, const int* items, int64_t count, int color,
+cudaError_t launch_relaxed_step(int metric, const DevState& st, int item0, int64_t count, int color,
                                 const int* cand_dest, cudaStream_t s) {
     if (count == 0) return cudaSuccess;
-    ACVD_DISPATCH(metric, relaxed_commit_kernel, list_grid(count), 256, s, st, items, color, cand_dest);
+    ACVD_DISPATCH(metric, relaxed_commit_kernel, list_grid(count), 256, s, st, item0, color, cand_dest);
     ACVD_DISPATCH(metric, fx_finalize_kernel, nblk(st.k, 64), 64, s, st);   // small blocks: every SM gets some
     return cudaGetLastError();
 }

@@ -57,6 +57,7 @@ struct acvd_ctx {
     // internal item order: colour classes contiguous (perm: item -> original
     // vertex id, inv: original vertex id -> item); faces and edges in item ids
     DBuf<int> perm, inv, tri_int, edge_int, label_orig;
+    DBuf<int4> ring8;              // first 8 ring slots per item
     // sweep classes: either the colour classes, or one class holding every item
     // (claims alone keep committed moves on disjoint clusters; colours are kept
     // for hole filling)
@@ -159,6 +160,7 @@ struct acvd_ctx {
         st.out_cnt = out_cnt.p;
         st.in_done = in_done.p;
         st.out_done = out_done.p;
+        st.ring8 = ring8.p;
         st.orig = perm.p;
         st.inv = inv.p;
         return st;
@@ -283,6 +285,8 @@ static int setup_colors(acvd_ctx* ctx) {
         CK(cudaMemcpyAsync(ctx->col.p, col_new.p, ne2 * sizeof(int), cudaMemcpyDeviceToDevice, ctx->s));
         CK(cudaStreamSynchronize(ctx->s));
     }
+    CK(ctx->ring8.resize(2 * n));
+    CK(launch_ring8(ctx->row.p, ctx->col.p, n, (int*)ctx->ring8.p, ctx->s));
     CK(ctx->tri_int.resize(3 * ctx->nF));
     CK(ctx->edge_int.resize(2 * ctx->nE));
     CK(launch_map_ids(ctx->tri.p, 3 * ctx->nF, ctx->inv.p, ctx->tri_int.p, ctx->s));
@@ -693,24 +697,24 @@ static int enqueue_sweep(acvd_ctx* ctx, bool timing, bool relaxed) {
     CK(launch_begin_sweep(st, ctx->nclasses, ctx->s));
     int64_t kernels = 1;
     for (int c = 0; c < ctx->nclasses; c++) {
-        const int* items = ctx->sweep_items + ctx->sweep_off[c];
+        const int item0 = (int)ctx->sweep_off[c];   // classes are contiguous item ranges
         const int64_t cnt = ctx->sweep_off[c + 1] - ctx->sweep_off[c];
         if (cnt == 0) continue;
         if (!relaxed) CK(cudaMemsetAsync(ctx->claim.p, 0xff, (ctx->K + 1) * sizeof(unsigned long long), ctx->s));
         // cudaEventRecordExternal makes the records real graph nodes when captured
         if (timing) CK(cudaEventRecordWithFlags(ctx->ev_eval[2 * c], ctx->s, cudaEventRecordExternal));
-        CK(launch_eval(ctx->metric, st, items, cnt, c, ctx->cand_dest.p, ctx->cand_prio.p, !relaxed, ctx->s));
+        CK(launch_eval(ctx->metric, st, item0, cnt, c, ctx->cand_dest.p, ctx->cand_prio.p, !relaxed, ctx->s));
         if (timing) CK(cudaEventRecordWithFlags(ctx->ev_eval[2 * c + 1], ctx->s, cudaEventRecordExternal));
         if (relaxed) {
-            CK(launch_relaxed_step(ctx->metric, st, items, cnt, c, ctx->cand_dest.p, ctx->s));
+            CK(launch_relaxed_step(ctx->metric, st, item0, cnt, c, ctx->cand_dest.p, ctx->s));
             kernels += 3;
             continue;
         }
-        CK(launch_apply(ctx->metric, st, items, cnt, c, 0, ctx->cand_dest.p, ctx->cand_prio.p, ctx->s));
+        CK(launch_apply(ctx->metric, st, item0, cnt, c, 0, ctx->cand_dest.p, ctx->cand_prio.p, ctx->s));
         kernels += 2;
         for (int r = 1; r < ctx->match_rounds; r++) {
-            CK(launch_reclaim(st, items, cnt, c, r, ctx->cand_dest.p, ctx->cand_prio.p, ctx->s));
-            CK(launch_apply(ctx->metric, st, items, cnt, c, r, ctx->cand_dest.p, ctx->cand_prio.p, ctx->s));
+            CK(launch_reclaim(st, item0, cnt, c, r, ctx->cand_dest.p, ctx->cand_prio.p, ctx->s));
+            CK(launch_apply(ctx->metric, st, item0, cnt, c, r, ctx->cand_dest.p, ctx->cand_prio.p, ctx->s));
             kernels += 2;
         }
     }
@@ -811,7 +815,6 @@ static int run_sweeps_persistent(acvd_ctx* ctx, LoopState& hl, acvd_stats& local
     CK(cudaMemcpyAsync(ctx->doff.p, off.data(), off.size() * sizeof(long long), cudaMemcpyHostToDevice, ctx->s));
     SweepRun a;
     a.st = ctx->state();
-    a.items = ctx->sweep_items;
     a.off = ctx->doff.p;
     a.nclasses = ctx->nclasses;
     a.match_rounds = ctx->match_rounds;

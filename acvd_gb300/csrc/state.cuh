@@ -106,6 +106,9 @@ struct DevState {
     int* out_cnt;          // proposals leaving the cluster in this step
     int* in_done;          // committed moves into the cluster
     int* out_done;         // committed moves out of the cluster
+    // per item, the first 8 ring neighbours (two int4, ring order, -1 padded; slot
+    // 7 = -2 when the ring is longer than 8, which then is read from row / col)
+    const int4* ring8;
     // internal item order (colour classes contiguous): original vertex id of
     // each item, and the item of each original vertex id
     const int* orig;
@@ -151,7 +154,6 @@ struct SweepLog {
 // Arguments of the persistent sweep kernel.
 struct SweepRun {
     DevState st;
-    const int* items;         // sweep classes, concatenated
     const long long* off;     // class offsets (nclasses + 1)
     int nclasses;
     int match_rounds;
@@ -193,17 +195,20 @@ cudaError_t launch_gather_i32(const int* src, const int* idx, int64_t n, int* ds
 cudaError_t launch_gather_f4(const float4* src, const int* idx, int64_t n, float4* dst, cudaStream_t s);
 cudaError_t launch_gather_f2(const float2* src, const int* idx, int64_t n, float2* dst, cudaStream_t s);
 cudaError_t launch_iota(int64_t n, int* out, cudaStream_t s);
+cudaError_t launch_ring8(const int* row, const int* col, int64_t n, int* ring8, cudaStream_t s);
 
 // ---- clustering (cluster.cu) ----
+// The sweep kernels take a colour class as the contiguous item range
+// [item0, item0 + count) of the internal order.
 cudaError_t launch_begin_sweep(const DevState& st, int ncolors, cudaStream_t s);
-cudaError_t launch_relaxed_step(int metric, const DevState& st, const int* items, int64_t count, int color,
+cudaError_t launch_relaxed_step(int metric, const DevState& st, int item0, int64_t count, int color,
                                 const int* cand_dest, cudaStream_t s);
 cudaError_t launch_fx_scale(int metric, const DevState& st, unsigned* maxbits, cudaStream_t s);
-cudaError_t launch_eval(int metric, const DevState& st, const int* items, int64_t count, int color,
+cudaError_t launch_eval(int metric, const DevState& st, int item0, int64_t count, int color,
                         int* cand_dest, unsigned* cand_prio, bool claims, cudaStream_t s);
-cudaError_t launch_apply(int metric, const DevState& st, const int* items, int64_t count, int color, int round,
+cudaError_t launch_apply(int metric, const DevState& st, int item0, int64_t count, int color, int round,
                          int* cand_dest, const unsigned* cand_prio, cudaStream_t s);
-cudaError_t launch_reclaim(const DevState& st, const int* items, int64_t count, int color, int round,
+cudaError_t launch_reclaim(const DevState& st, int item0, int64_t count, int color, int round,
                            int* cand_dest, const unsigned* cand_prio, cudaStream_t s);
 // Persistent sweep kernel (cooperative launch).  blocks_per_sm: co-resident
 // blocks per SM for this metric (0 when the kernel cannot be co-resident).

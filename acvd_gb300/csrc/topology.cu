@@ -354,7 +354,26 @@ __global__ void iota_kernel(int64_t n, int* __restrict__ out) {
     if (t < n) out[t] = (int)t;
 }
 
+// Fixed-width copy of the first 8 ring slots (ring order), -1 padded; slot 7 =
+// -2 when the ring has more than 8 neighbours.  The evaluation reads an item's
+// neighbours without first reading its CSR bounds.
+__global__ void ring8_kernel(const int* __restrict__ row, const int* __restrict__ col, int64_t n,
+                             int* __restrict__ ring8) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const int p0 = row[t], d = row[t + 1] - p0;
+    for (int q = 0; q < 8; q++) ring8[8 * t + q] = q < d ? col[p0 + q] : -1;
+    if (d > 8) ring8[8 * t + 7] = -2;
+}
+
 static inline unsigned grid_of(int64_t n) { return (unsigned)((n + 255) / 256); }
+
+cudaError_t launch_ring8(const int* row, const int* col, int64_t n, int* ring8, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    ++g_launches;
+    ring8_kernel<<<grid_of(n), 256, 0, s>>>(row, col, n, ring8);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_scatter_inv(const int* perm, int64_t n, int* inv, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
