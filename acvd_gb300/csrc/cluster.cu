@@ -196,6 +196,12 @@ ACVD_DEV bool ring_connected(const DevState& st, int p0, int p1, int L) {
     return vis == msk;
 }
 
+// An item changed cluster: it and its ring may now lie on a boundary.
+ACVD_DEV void mark_ring(const DevState& st, int i) {
+    st.bflag[i] = 1;
+    for (int p = st.row[i]; p < st.row[i + 1]; p++) st.bflag[st.col[p]] = 1;
+}
+
 ACVD_DEV void warp_count(unsigned long long* ctr, unsigned v) {
     const unsigned tot = __reduce_add_sync(kFull, v);
     if ((threadIdx.x & 31) == 0 && tot) atomicAdd(ctr, (unsigned long long)tot);
@@ -261,21 +267,39 @@ ACVD_DEV void eval_tile(const DevState& st, int item0, int64_t count, int color,
     __shared__ float s_val[256][kMaxTgt + 1];  // energy parts: [j] add to s_tgt[j], [kMaxTgt] remove
     __shared__ signed char s_nt[256];          // destinations; -1: the whole test runs in B2
     __shared__ unsigned short s_task[256 * (kMaxTgt + 1)];
-    __shared__ unsigned s_nwork, s_ntask;
+    __shared__ int s_scr[256];                 // flagged items of the tile (colour-list positions)
+    __shared__ unsigned s_nwork, s_ntask, s_nscr;
     __syncthreads();                     // the previous tile is done with the shared arrays
     if (threadIdx.x == 0) {
         s_nwork = 0u;
         s_ntask = 0u;
+        s_nscr = 0u;
     }
     __syncthreads();
     const int epoch = color * kRounds;   // claim epoch of this step's first matching round
-    const int64_t idx = tile * 256 + threadIdx.x;
-    const bool in = idx < count;
+    const int64_t idx_t = tile * 256 + threadIdx.x;
+    const bool in = idx_t < count;
     const SweepState sw = *st.sweep;
     const RunFlags fl = *st.flags;
-    unsigned n_slots = 0, n_bnd = 0, n_tgt = 0, n_cand = 0;
-    if (in) {
+    unsigned n_slots = 0, n_bnd = 0, n_tgt = 0, n_cand = 0, n_scr = 0;
+    // A0: only items that may lie on a boundary go on to the ring screen, packed
+    // so that warps without one issue nothing
+    {
+        const bool flagged = in && st.bflag[item0 + idx_t] != 0;
+        const unsigned bal = __ballot_sync(kFull, flagged);
+        if (bal) {
+            const int lane = threadIdx.x & 31;
+            unsigned base = 0;
+            if (lane == 0) base = atomicAdd(&s_nscr, (unsigned)__popc(bal));
+            base = __shfl_sync(kFull, base, 0);
+            if (flagged) s_scr[base + __popc(bal & ((1u << lane) - 1u))] = (int)idx_t;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < s_nscr) {
+        const int64_t idx = s_scr[threadIdx.x];
         const int i = item0 + (int)idx;
+        n_scr = 1;
         const int4 ra = st.ring8[2 * (int64_t)i], rb = st.ring8[2 * (int64_t)i + 1];
         const int L = st.label[i];
         const int ev_i = st.evald[i];
@@ -312,6 +336,7 @@ ACVD_DEV void eval_tile(const DevState& st, int item0, int64_t count, int color,
                 }
             }
         }
+        if (!boundary) st.bflag[i] = 0;   // interior until a commit touches its ring
         if (boundary && fresh) {
             n_bnd = 1;
             const bool movable =
@@ -465,6 +490,7 @@ ACVD_DEV void eval_tile(const DevState& st, int item0, int64_t count, int color,
         if (my_cand >= 0) st.cand_list[base + __popc(bal & ((1u << lane) - 1u))] = my_cand;
     }
     warp_count(&st.counters[kCntVisited], in ? 1u : 0u);
+    warp_count(&st.counters[kCntScreened], n_scr);
     warp_count(&st.counters[kCntSlots], n_slots);
     warp_count(&st.counters[kCntBoundary], n_bnd);
     warp_count(&st.counters[kCntTargets], n_tgt);
@@ -682,6 +708,7 @@ ACVD_DEV void apply_range(const DevState& st, int item0, int color, int round, i
                 cand_dest[idx] = -1;
                 won_total++;
                 st.label[i] = B;
+                mark_ring(st, i);
                 st.size[B] += 1;
                 st.stamp[B] = now;
                 accumulate_item<M>(st.acc + (int64_t)B * Layout<M>::acc, it, 1.0f);
@@ -721,6 +748,7 @@ ACVD_DEV void apply_range(const DevState& st, int item0, int color, int round, i
             if (role == 0) {
                 won_total++;
                 st.label[i] = B;
+                mark_ring(st, i);
                 cand_dest[idx] = -1;
             }
         } else {
@@ -831,6 +859,7 @@ ACVD_DEV void relaxed_commit_range(const DevState& st, int item0, int color,
         ItemRec it;
         load_item<M>(st, i, it);
         st.label[i] = B;
+        mark_ring(st, i);
         atomicAdd(&st.in_done[B], 1);
         st.stamp[B] = now;
         long long* dB = st.fx_delta + (int64_t)B * NA;

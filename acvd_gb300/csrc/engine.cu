@@ -58,6 +58,7 @@ struct acvd_ctx {
     // vertex id, inv: original vertex id -> item); faces and edges in item ids
     DBuf<int> perm, inv, tri_int, edge_int, label_orig;
     DBuf<int4> ring8;              // first 8 ring slots per item
+    DBuf<unsigned char> bflag;     // per item: maybe on a cluster boundary
     // sweep classes: either the colour classes, or one class holding every item
     // (claims alone keep committed moves on disjoint clusters; colours are kept
     // for hole filling)
@@ -161,6 +162,7 @@ struct acvd_ctx {
         st.in_done = in_done.p;
         st.out_done = out_done.p;
         st.ring8 = ring8.p;
+        st.bflag = bflag.p;
         st.orig = perm.p;
         st.inv = inv.p;
         return st;
@@ -210,9 +212,13 @@ static int upload_flags(acvd_ctx* ctx) {
 }
 
 // sweep counter and invalidation floor (every cluster counts as modified after `floor`)
+// Also marks every item as maybe on a boundary: it is called whenever the labels
+// changed wholesale (start, clean / fill at a convergence).
 static int set_sweep_state(acvd_ctx* ctx, int sweep, int floor) {
     SweepState h{sweep, floor};
     CK(cudaMemcpyAsync(ctx->dsweep.p, &h, sizeof h, cudaMemcpyHostToDevice, ctx->s));
+    CK(ctx->bflag.resize(ctx->nV));
+    CK(cudaMemsetAsync(ctx->bflag.p, 1, ctx->nV, ctx->s));
     CK(cudaStreamSynchronize(ctx->s));
     return ACVD_OK;
 }
@@ -1028,13 +1034,15 @@ extern "C" int acvd_minimize(acvd_ctx* ctx, acvd_stats* stats) {
     local.kernel_launches = g_launches - launches0;
     local.reverted = (int64_t)ctx->h_counters[kCntReverted];
     {
-        // algorithmic bytes of the evaluation kernels: per visited item its colour-list
-        // entry, ring bounds and label; per ring slot the neighbour id and label; per
+        // algorithmic bytes of the evaluation kernels: per visited item its boundary
+        // flag; per screened item its 8-slot ring, label and evaluation sweep; per
+        // ring slot the neighbour's label; per
         // boundary item its record, its cluster's record and size; per destination
         // cluster its record; per proposal the candidate slots and two claim words
         const int64_t R = ctx->metric == kIso ? 16 : (ctx->metric == kQEM ? 40 : 64);
         const int64_t C = 16 * (int64_t)ev_stride(ctx->metric);
-        local.eval_bytes = 16 * local.visited + 8 * local.slots + (R + C + 4) * local.boundary_items +
+        const int64_t screened = (int64_t)ctx->h_counters[kCntScreened];
+        local.eval_bytes = 1 * local.visited + 40 * screened + 4 * local.slots + (R + C + 4) * local.boundary_items +
                            C * local.targets + 24 * local.candidates;
     }
     if (status == ACVD_OK) {

@@ -63,6 +63,7 @@ enum Counter {
     kCntDisconnected = 8,
     kCntAssigned = 9,
     kCntReverted = 10,   // commits undone because the pair's energy did not decrease
+    kCntScreened = 11,   // visited items whose boundary flag sent them to the ring screen
     kNumCounters = 16
 };
 
@@ -106,6 +107,12 @@ struct DevState {
     int* out_cnt;          // proposals leaving the cluster in this step
     int* in_done;          // committed moves into the cluster
     int* out_done;         // committed moves out of the cluster
+    // per item: 0 = certainly interior (every ring label equals its own), 1 = maybe
+    // on a cluster boundary.  A commit sets it on the moved item and its ring; the
+    // ring screen clears it when it finds the item interior.  The reference keeps
+    // only boundary edges in its queue and re-queues a moved item's ring
+    // (vtkUniformClustering.h:858-872, 971, 985).
+    unsigned char* bflag;
     // per item, the first 8 ring neighbours (two int4, ring order, -1 padded; slot
     // 7 = -2 when the ring is longer than 8, which then is read from row / col)
     const int4* ring8;
