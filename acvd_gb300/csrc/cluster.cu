@@ -489,12 +489,12 @@ ACVD_DEV void eval_tile(const DevState& st, int item0, int64_t count, int color,
         base = __shfl_sync(kFull, base, 0);
         if (my_cand >= 0) st.cand_list[base + __popc(bal & ((1u << lane) - 1u))] = my_cand;
     }
-    warp_count(&st.counters[kCntVisited], in ? 1u : 0u);
-    warp_count(&st.counters[kCntScreened], n_scr);
-    warp_count(&st.counters[kCntSlots], n_slots);
-    warp_count(&st.counters[kCntBoundary], n_bnd);
-    warp_count(&st.counters[kCntTargets], n_tgt);
-    warp_count(&st.counters[kCntCand], n_cand);
+    warp_count(ctr(st.counters, kCntVisited), in ? 1u : 0u);
+    warp_count(ctr(st.counters, kCntScreened), n_scr);
+    warp_count(ctr(st.counters, kCntSlots), n_slots);
+    warp_count(ctr(st.counters, kCntBoundary), n_bnd);
+    warp_count(ctr(st.counters, kCntTargets), n_tgt);
+    warp_count(ctr(st.counters, kCntCand), n_cand);
 }
 
 // blocks per SM the evaluation kernel is compiled for (registers per thread
@@ -755,12 +755,12 @@ ACVD_DEV void apply_range(const DevState& st, int item0, int color, int round, i
             st.claim[C] = 0ull;
             if (role == 0) {
                 cand_dest[idx] = -1;
-                atomicAdd(&st.counters[kCntReverted], 1ull);
+                atomicAdd(ctr(st.counters, kCntReverted), 1ull);
             }
         }
     }
     // every thread of the grid reaches this point: warp-aggregated count
-    warp_count(&st.counters[kCntMoves], won_total);
+    warp_count(ctr(st.counters, kCntMoves), won_total);
 }
 
 template <int M>
@@ -875,7 +875,7 @@ ACVD_DEV void relaxed_commit_range(const DevState& st, int item0, int color,
             if (L < st.k) atomicAdd((unsigned long long*)&dL[q], (unsigned long long)(-v));
         }
     }
-    warp_count(&st.counters[kCntMoves], won);
+    warp_count(ctr(st.counters, kCntMoves), won);
 }
 
 template <int M>
@@ -953,6 +953,7 @@ __global__ void begin_sweep_kernel(DevState st, int ncolors) {
     const int t = threadIdx.x;
     if (t == 0) st.sweep->sweep += 1;
     if (t < ncolors) st.cand_count[t] = 0u;
+    if (t < kStripes) st.counters[t * kNumCounters + kCntMoves] = 0ull;   // this sweep's moves
 }
 
 // ---------------------------------------------------------------------------
@@ -1031,7 +1032,7 @@ __global__ void __launch_bounds__(256, 2) sweep_run_kernel(SweepRun a) {
         if (lead) {
             st.sweep->sweep += 1;
             for (int c = 0; c < a.nclasses; c++) st.cand_count[c] = 0u;
-            st.counters[kCntMoves] = 0ull;
+            for (int q = 0; q < kStripes; q++) st.counters[q * kNumCounters + kCntMoves] = 0ull;
         }
         if (!grid_barrier(a.bar)) return;
         for (int c = 0; c < a.nclasses; c++) {
@@ -1093,7 +1094,9 @@ __global__ void __launch_bounds__(256, 2) sweep_run_kernel(SweepRun a) {
         }
         if (lead) {
             LoopState* L = a.ls;
-            const long long mods = (long long)*(volatile unsigned long long*)&st.counters[kCntMoves];
+            long long mods = 0;
+            for (int q = 0; q < kStripes; q++)
+                mods += (long long)*(volatile unsigned long long*)(st.counters + q * kNumCounters + kCntMoves);
             if (relaxed) {
                 if (L->have_prev && !(e_now < L->e_prev)) L->relaxed_ok = 0;
                 L->e_prev = e_now;
@@ -1207,7 +1210,7 @@ __global__ void comp_step_kernel(DevState st, int* __restrict__ comp) {
     }
     if (m < cur) {
         comp[i] = m;
-        atomicAdd(&st.counters[kCntChanged], 1ull);
+        atomicAdd(ctr(st.counters, kCntChanged), 1ull);
     }
 }
 
@@ -1237,7 +1240,7 @@ __global__ void comp_reset_kernel(DevState st, const int* __restrict__ comp,
     const uint32_t root = 0xffffffffu - (uint32_t)(best[L] & 0xffffffffull);
     if ((uint32_t)comp[i] != root) {
         st.label[i] = st.k;
-        if (atomicExch(&multi[L], 1) == 0) atomicAdd(&st.counters[kCntDisconnected], 1ull);
+        if (atomicExch(&multi[L], 1) == 0) atomicAdd(ctr(st.counters, kCntDisconnected), 1ull);
     }
 }
 
@@ -1266,7 +1269,7 @@ __global__ void fill_color_kernel(DevState st, const int* __restrict__ items, in
             }
         }
     }
-    warp_count(&st.counters[kCntAssigned], done);
+    warp_count(ctr(st.counters, kCntAssigned), done);
 }
 
 // ---------------------------------------------------------------------------

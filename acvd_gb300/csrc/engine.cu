@@ -97,7 +97,8 @@ struct acvd_ctx {
     DBuf<float4> ev;
     DBuf<double> energy;
     DBuf<unsigned long long> counters;
-    unsigned long long* h_counters = nullptr;
+    unsigned long long* h_raw = nullptr;      // pinned copy of the counter stripes
+    unsigned long long h_counters[kNumCounters] = {};   // stripes summed
     DBuf<RunFlags> dflags;
     RunFlags flags{1, 0, 3, 1e-3f};
     int level = 3;
@@ -199,9 +200,14 @@ static int fail_cuda(acvd_ctx* ctx, cudaError_t e, const char* what, int line) {
 }
 
 static int sync_counters(acvd_ctx* ctx) {
-    CK(cudaMemcpyAsync(ctx->h_counters, ctx->counters.p, kNumCounters * sizeof(unsigned long long),
+    CK(cudaMemcpyAsync(ctx->h_raw, ctx->counters.p, kCounterWords * sizeof(unsigned long long),
                        cudaMemcpyDeviceToHost, ctx->s));
     CK(cudaStreamSynchronize(ctx->s));
+    for (int c = 0; c < kNumCounters; c++) {
+        unsigned long long v = 0;
+        for (int q = 0; q < kStripes; q++) v += ctx->h_raw[q * kNumCounters + c];
+        ctx->h_counters[c] = v;
+    }
     return ACVD_OK;
 }
 
@@ -223,8 +229,10 @@ static int set_sweep_state(acvd_ctx* ctx, int sweep, int floor) {
     return ACVD_OK;
 }
 
+// every stripe of one counter
 static cudaError_t zero_counter(acvd_ctx* ctx, int which) {
-    return cudaMemsetAsync(ctx->counters.p + which, 0, sizeof(unsigned long long), ctx->s);
+    return cudaMemset2DAsync(ctx->counters.p + which, kNumCounters * sizeof(unsigned long long), 0,
+                             sizeof(unsigned long long), kStripes, ctx->s);
 }
 
 // ---------------------------------------------------------------------------
@@ -343,15 +351,15 @@ acvd_ctx* acvd_create(const acvd_opts* opts) {
     }
     if (cudaSetDevice(ctx->opts.device) != cudaSuccess ||
         cudaStreamCreateWithFlags(&ctx->s, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaMallocHost((void**)&ctx->h_counters, kNumCounters * sizeof(unsigned long long)) != cudaSuccess ||
-        ctx->counters.resize(kNumCounters) != cudaSuccess || ctx->dflags.resize(1) != cudaSuccess ||
+        cudaMallocHost((void**)&ctx->h_raw, kCounterWords * sizeof(unsigned long long)) != cudaSuccess ||
+        ctx->counters.resize(kCounterWords) != cudaSuccess || ctx->dflags.resize(1) != cudaSuccess ||
         ctx->dsweep.resize(1) != cudaSuccess ||
         cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess) {
         cudaGetLastError();
         delete ctx;
         return nullptr;
     }
-    cudaMemset(ctx->counters.p, 0, kNumCounters * sizeof(unsigned long long));
+    cudaMemset(ctx->counters.p, 0, kCounterWords * sizeof(unsigned long long));
     return ctx;
 }
 
@@ -361,7 +369,7 @@ void acvd_destroy(acvd_ctx* ctx) {
     if (ctx->s) cudaStreamSynchronize(ctx->s);
     ctx->drop_graph();
     ctx->drop_events();
-    if (ctx->h_counters) cudaFreeHost(ctx->h_counters);
+    if (ctx->h_raw) cudaFreeHost(ctx->h_raw);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     if (ctx->s) cudaStreamDestroy(ctx->s);
@@ -699,7 +707,6 @@ static int clean(acvd_ctx* ctx, int* n_disconnected) {
 // are recorded inside the captured graph and read after the sweep's sync.
 static int enqueue_sweep(acvd_ctx* ctx, bool timing, bool relaxed) {
     DevState st = ctx->state();
-    CK(cudaMemsetAsync(ctx->counters.p + kCntMoves, 0, sizeof(unsigned long long), ctx->s));
     CK(launch_begin_sweep(st, ctx->nclasses, ctx->s));
     int64_t kernels = 1;
     for (int c = 0; c < ctx->nclasses; c++) {
@@ -876,7 +883,7 @@ extern "C" int acvd_minimize(acvd_ctx* ctx, acvd_stats* stats) {
     ctx->flags.thr = 1e-3f;
     int r = upload_flags(ctx);
     if (r) return r;
-    CK(cudaMemsetAsync(ctx->counters.p, 0, kNumCounters * sizeof(unsigned long long), ctx->s));
+    CK(cudaMemsetAsync(ctx->counters.p, 0, kCounterWords * sizeof(unsigned long long), ctx->s));
     const long long launches0 = g_launches;
     cudaEvent_t t0, t1;
     CK(cudaEventCreate(&t0));

@@ -67,6 +67,15 @@ enum Counter {
     kNumCounters = 16
 };
 
+// The counters are striped over kStripes 128-byte lines: a block adds into the
+// stripe of its index, so tens of thousands of warps do not serialise on one
+// address; the host sums the stripes.
+constexpr int kStripes = 32;
+constexpr int kCounterWords = kStripes * kNumCounters;
+__device__ __forceinline__ unsigned long long* ctr(unsigned long long* counters, int which) {
+    return counters + (blockIdx.x & (kStripes - 1)) * kNumCounters + which;
+}
+
 // Sweep bookkeeping on the device (one captured graph serves every sweep):
 // `sweep` counts sweeps, `floor` is the sweep after which every cluster counts as
 // modified (the reference's SetAllClustersToModified, vtkUniformClustering.h:717-722).
