@@ -480,14 +480,25 @@ ACVD_DEV void eval_tile(const DevState& st, int item0, int64_t count, int color,
             st.evald[i] = sw.sweep;
         }
     }
-    // warp-aggregated append to the compact proposal list
-    const unsigned bal = __ballot_sync(kFull, my_cand >= 0);
-    if (bal) {
-        const int lane = threadIdx.x & 31;
-        unsigned base = 0;
-        if (lane == 0) base = atomicAdd(&st.cand_count[color], (unsigned)__popc(bal));
-        base = __shfl_sync(kFull, base, 0);
-        if (my_cand >= 0) st.cand_list[base + __popc(bal & ((1u << lane) - 1u))] = my_cand;
+    // block-aggregated append to the compact proposal list: one atomic per block
+    // (tens of thousands of warps would otherwise serialise on the class's count)
+    {
+        __shared__ unsigned s_wc[8], s_base;
+        const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+        const unsigned bal = __ballot_sync(kFull, my_cand >= 0);
+        if (lane == 0) s_wc[wid] = (unsigned)__popc(bal);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            unsigned tot = 0;
+            for (int w = 0; w < 8; w++) {
+                const unsigned c = s_wc[w];
+                s_wc[w] = tot;
+                tot += c;
+            }
+            s_base = tot ? atomicAdd(&st.cand_count[color], tot) : 0u;
+        }
+        __syncthreads();
+        if (my_cand >= 0) st.cand_list[s_base + s_wc[wid] + __popc(bal & ((1u << lane) - 1u))] = my_cand;
     }
     warp_count(ctr(st.counters, kCntVisited), in ? 1u : 0u);
     warp_count(ctr(st.counters, kCntScreened), n_scr);
@@ -928,25 +939,30 @@ __global__ void fx_finalize_kernel(DevState st) {
 // per accumulator component: the largest |contribution| over the items (as float
 // bits, monotone for non-negative values), from which the fixed-point scales follow
 template <int M>
-__global__ void fx_maxabs_kernel(DevState st, unsigned* __restrict__ maxbits) {
+__global__ void __launch_bounds__(256) fx_maxabs_kernel(DevState st, unsigned* __restrict__ maxbits) {
     constexpr int NA = Layout<M>::acc;
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    __shared__ unsigned s_mx[NA];
+    if (threadIdx.x < NA) s_mx[threadIdx.x] = 0u;
+    __syncthreads();
     float mx[NA];
 #pragma unroll
     for (int q = 0; q < NA; q++) mx[q] = 0.f;
-    if (i < st.n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < st.n; i += (int64_t)gridDim.x * blockDim.x) {
         ItemRec it;
         load_item<M>(st, (int)i, it);
 #pragma unroll
-        for (int q = 0; q < NA; q++) mx[q] = fabsf(contrib_df<M>(it, q).hi);
+        for (int q = 0; q < NA; q++) mx[q] = fmaxf(mx[q], fabsf(contrib_df<M>(it, q).hi));
     }
+    // warp, then block maxima; one global atomic per block and component
 #pragma unroll
     for (int q = 0; q < NA; q++) {
         float v = mx[q];
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(kFull, v, o));
-        if ((threadIdx.x & 31) == 0) atomicMax(&maxbits[q], __float_as_uint(v));
+        if ((threadIdx.x & 31) == 0) atomicMax(&s_mx[q], __float_as_uint(v));
     }
+    __syncthreads();
+    if (threadIdx.x < NA) atomicMax(&maxbits[threadIdx.x], s_mx[threadIdx.x]);
 }
 
 __global__ void begin_sweep_kernel(DevState st, int ncolors) {
@@ -1481,7 +1497,7 @@ cudaError_t launch_relaxed_step(int metric, const DevState& st, int item0, int64
 
 cudaError_t launch_fx_scale(int metric, const DevState& st, unsigned* maxbits, cudaStream_t s) {
     if (st.n == 0) return cudaSuccess;
-    ACVD_DISPATCH(metric, fx_maxabs_kernel, nblk(st.n), 256, s, st, maxbits);
+    ACVD_DISPATCH(metric, fx_maxabs_kernel, list_grid(st.n), 256, s, st, maxbits);
     return cudaGetLastError();
 }
 

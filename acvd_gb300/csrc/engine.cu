@@ -122,6 +122,18 @@ struct acvd_ctx {
     int64_t exact_kernels = 0, relaxed_kernels = 0;
     DBuf<int> label_init;          // the assignment given to acvd_set_labels (for acvd_rewind)
 
+    // set-up work buffers, kept between calls: a repeated set-up (same or smaller
+    // mesh) allocates nothing, and so does not synchronise the device in cudaFree
+    struct SetupWork {
+        DBuf<int> col_new;
+        DBuf<double> ind, farea, fnorm, wd, varea, wsum;
+        DBuf<float> pd;
+        DBuf<uint32_t> k1, v1, k2, v2, vrow;
+        DBuf<float4> t4;
+        DBuf<float2> t2;
+        DBuf<unsigned> maxbits;
+    } setup;
+
     // persistent sweep kernel: loop state, grid barrier, energy partials, class
     // offsets, per-sweep log; grid = SMs x co-resident blocks (0: not available)
     DBuf<LoopState> dls;
@@ -245,15 +257,20 @@ static int setup_colors(acvd_ctx* ctx) {
     CK(ctx->dtmp.resize(2));
     int* d_maxc = (int*)ctx->dtmp.p;
     CK(cudaMemsetAsync(d_maxc, 0, sizeof(int), ctx->s));
+    // rounds in groups of four between host checks (a round after the last one
+    // finds every item coloured and does nothing); the count left is the last
+    // round's number of items still waiting for a neighbour
     int rounds = 0;
     for (;;) {
-        CK(zero_counter(ctx, kCntChanged));
-        CK(launch_color_round(ctx->row.p, ctx->col.p, n, ctx->wk_int.p, ctx->counters.p + kCntChanged, d_maxc,
-                              ctx->s));
+        for (int g = 0; g < 4; g++) {
+            CK(zero_counter(ctx, kCntChanged));
+            CK(launch_color_round(ctx->row.p, ctx->col.p, n, ctx->wk_int.p, ctx->counters.p + kCntChanged, d_maxc,
+                                  ctx->s));
+        }
         int r = sync_counters(ctx);
         if (r) return r;
         if (ctx->h_counters[kCntChanged] == 0) break;
-        if (++rounds > 100000) return fail(ctx, ACVD_ERR_ITER_LIMIT, "graph colouring did not finish");
+        if ((rounds += 4) > 100000) return fail(ctx, ACVD_ERR_ITER_LIMIT, "graph colouring did not finish");
     }
     int maxc = 0;
     CK(cudaMemcpy(&maxc, d_maxc, sizeof(int), cudaMemcpyDeviceToHost));
@@ -290,7 +307,7 @@ static int setup_colors(acvd_ctx* ctx) {
     CK(launch_scatter_inv(ctx->perm.p, n, ctx->inv.p, ctx->s));
     {
         const int64_t ne2 = 2 * ctx->nE;
-        DBuf<int> col_new;
+        DBuf<int>& col_new = ctx->setup.col_new;
         CK(col_new.resize(ne2));
         CK(launch_perm_degree(ctx->row.p, ctx->perm.p, n, ctx->wk_a.p, ctx->s));
         CK(exclusive_scan_u32(ctx->wk_a.p, ctx->wk_b.p, n + 1, nullptr, ctx->scratch, ctx->s));
@@ -433,8 +450,9 @@ int acvd_set_metric(acvd_ctx* ctx, int metric, const double* indicator, const fl
     ctx->drop_graph();
     ctx->metric = metric;
     const int64_t nv = ctx->nV, nf = ctx->nF;
-    DBuf<double> ind, farea, fnorm, wd, varea, wsum;
-    DBuf<float> pd;
+    DBuf<double>&ind = ctx->setup.ind, &farea = ctx->setup.farea, &fnorm = ctx->setup.fnorm, &wd = ctx->setup.wd,
+                &varea = ctx->setup.varea, &wsum = ctx->setup.wsum;
+    DBuf<float>& pd = ctx->setup.pd;
     if (use_ind) {
         CK(ind.resize(nv));
         CK(cudaMemcpyAsync(ind.p, indicator, nv * sizeof(double), cudaMemcpyHostToDevice, ctx->s));
@@ -450,7 +468,8 @@ int acvd_set_metric(acvd_ctx* ctx, int metric, const double* indicator, const fl
     CK(wsum.resize(1));
     CK(launch_face_geometry(ctx->xyz.p, ctx->tri.p, nf, farea.p, fnorm.p, ctx->s));
     // vertex -> faces in increasing face id
-    DBuf<uint32_t> k1, v1, k2, v2, vrow;
+    DBuf<uint32_t>&k1 = ctx->setup.k1, &v1 = ctx->setup.v1, &k2 = ctx->setup.k2, &v2 = ctx->setup.v2,
+                  &vrow = ctx->setup.vrow;
     CK(k1.resize(3 * nf));
     CK(v1.resize(3 * nf));
     CK(k2.resize(3 * nf));
@@ -488,8 +507,8 @@ int acvd_set_metric(acvd_ctx* ctx, int metric, const double* indicator, const fl
     }
     // item records into internal order
     {
-        DBuf<float4> t4;
-        DBuf<float2> t2;
+        DBuf<float4>& t4 = ctx->setup.t4;
+        DBuf<float2>& t2 = ctx->setup.t2;
         CK(t4.resize(nv));
         CK(launch_gather_f4(ctx->xw.p, ctx->perm.p, nv, t4.p, ctx->s));
         CK(cudaMemcpyAsync(ctx->xw.p, t4.p, nv * sizeof(float4), cudaMemcpyDeviceToDevice, ctx->s));
@@ -511,7 +530,7 @@ int acvd_set_metric(acvd_ctx* ctx, int metric, const double* indicator, const fl
     // fixed-point scales of the relaxed steps: any sum of up to N contributions of
     // component j stays below 2^62 units
     {
-        DBuf<unsigned> maxbits;
+        DBuf<unsigned>& maxbits = ctx->setup.maxbits;
         CK(maxbits.resize(32));
         CK(cudaMemsetAsync(maxbits.p, 0, 32 * sizeof(unsigned), ctx->s));
         DevState st = ctx->state();

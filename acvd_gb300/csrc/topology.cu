@@ -17,10 +17,12 @@ namespace acvd {
 __global__ void ring_adjacency_kernel(const int* __restrict__ row, const int* __restrict__ col, int64_t n,
                                       unsigned* __restrict__ adj, int* __restrict__ max_deg) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int d_or = i < n ? row[i + 1] - row[i] : 0;
+    const int dmax = __reduce_max_sync(kFull, d_or);   // one atomic per warp
+    if ((threadIdx.x & 31) == 0) atomicMax(max_deg, dmax);
     if (i >= n) return;
     const int p0 = row[i], p1 = row[i + 1];
     const int d = p1 - p0;
-    atomicMax(max_deg, d);
     if (d > 32) {
         for (int p = p0; p < p1; p++) adj[p] = 0u;
         return;
@@ -57,31 +59,39 @@ __device__ __forceinline__ uint32_t jp_hash(uint32_t x) {
     return x;
 }
 
+// remaining: the counter stripes (the block adds into its own); max_color: the
+// largest colour handed out.  Both are updated once per warp.
 __global__ void color_round_kernel(const int* __restrict__ row, const int* __restrict__ col, int64_t n,
                                    int* __restrict__ color, unsigned long long* __restrict__ remaining,
                                    int* __restrict__ max_color) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    if (color[i] >= 0) return;
-    const uint32_t hi = jp_hash((uint32_t)i);
-    const int p0 = row[i], p1 = row[i + 1];
-    unsigned long long used = 0ull;
-    for (int p = p0; p < p1; p++) {
-        const int j = col[p];
-        const int cj = color[j];
-        if (cj < 0) {
-            const uint32_t hj = jp_hash((uint32_t)j);
-            if (hj > hi || (hj == hi && j > i)) {
-                atomicAdd(remaining, 1ull);
-                return;
+    bool blocked = false;
+    int c = -1;
+    if (i < n && color[i] < 0) {
+        const uint32_t hi = jp_hash((uint32_t)i);
+        const int p0 = row[i], p1 = row[i + 1];
+        unsigned long long used = 0ull;
+        for (int p = p0; p < p1 && !blocked; p++) {
+            const int j = col[p];
+            const int cj = color[j];
+            if (cj < 0) {
+                const uint32_t hj = jp_hash((uint32_t)j);
+                if (hj > hi || (hj == hi && j > i)) blocked = true;
+            } else if (cj < 64) {
+                used |= 1ull << cj;
             }
-        } else if (cj < 64) {
-            used |= 1ull << cj;
+        }
+        if (!blocked) {
+            c = used == ~0ull ? 64 : __ffsll((long long)~used) - 1;
+            color[i] = c;
         }
     }
-    const int c = used == ~0ull ? 64 : __ffsll((long long)~used) - 1;
-    color[i] = c;
-    atomicMax(max_color, c);
+    const unsigned nb = __popc(__ballot_sync(kFull, blocked));
+    const int cmax = __reduce_max_sync(kFull, c);
+    if ((threadIdx.x & 31) == 0) {
+        if (nb) atomicAdd(remaining + (blockIdx.x & (kStripes - 1)) * kNumCounters, (unsigned long long)nb);
+        if (cmax >= 0) atomicMax(max_color, cmax);
+    }
 }
 
 cudaError_t launch_color_round(const int* row, const int* col, int64_t n, int* color,
