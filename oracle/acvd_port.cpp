@@ -939,6 +939,163 @@ long long port_dual_mesh(void* hp, int* tris, double* verts) {
     return count;
 }
 
+// Curvature of vertex clustering (vtkDiscreteRemeshing::SamplingPreProcessing,
+// DiscreteRemeshing/vtkDiscreteRemeshing.h:630-637 -> Common/vtkCurvatureMeasure.cxx,
+// polynomial fitting, vertices, 3-ring).
+//
+// Faces of the 3-ring of vertex v (vtkNeighbourhoodComputation::ComputeNRingCells,
+// Common/vtkNeighbourhoodComputation.cxx:38-100): v's own faces first, then ring by
+// ring the faces of the edges of every not yet visited vertex, in ring order.
+static void nring_faces(const Mesh& m, idt v, int rings, std::vector<idt>& faces, std::vector<char>& ftag,
+                        std::vector<char>& vtag, std::vector<idt>& touched_f, std::vector<idt>& touched_v) {
+    m.vertex_faces(v, faces);
+    for (idt f : faces) { ftag[f] = 1; touched_f.push_back(f); }
+    std::vector<idt> cur{v}, next;
+    for (int r = 0; r < rings; r++) {
+        next.clear();
+        for (idt u : cur) {
+            if (vtag[u]) continue;
+            vtag[u] = 1;
+            touched_v.push_back(u);
+            for (idt e : m.ring[u]) {
+                next.push_back(m.ev1[e] == u ? m.ev2[e] : m.ev1[e]);
+                const idt f1 = m.poly1[e], f2 = m.poly2[e];
+                if (f1 >= 0) {
+                    if (!ftag[f1]) { faces.push_back(f1); ftag[f1] = 1; touched_f.push_back(f1); }
+                    if (f2 >= 0 && !ftag[f2]) { faces.push_back(f2); ftag[f2] = 1; touched_f.push_back(f2); }
+                }
+            }
+        }
+        std::swap(cur, next);
+    }
+}
+
+// vtkSurface::GetCellMassProperties for a triangle (Common/vtkSurface.cxx:1380-1419)
+static void face_mass(const Mesh& m, idt f, double& area, double* bary) {
+    double p1[3], p2[3], p3[3];
+    m.point(m.F[3 * f], p1); m.point(m.F[3 * f + 1], p2); m.point(m.F[3 * f + 2], p3);
+    area = 0;
+    bary[0] = bary[1] = bary[2] = 0;
+    const double a2 = rmath::tri_area(p1, p2, p3);
+    for (int i = 0; i < 3; i++) bary[i] += a2 * (p1[i] + p2[i] + p3[i]) / 3.0;
+    area += a2;
+    if (area > 0)
+        for (int i = 0; i < 3; i++) bary[i] /= area;
+}
+
+// vtkSinglePolynomialMeasure::ComputeFitting (Common/vtkCurvatureMeasure.cxx:188-505):
+// local frame from the area-weighted mean normal, least-squares quadratic height
+// field z = q0 + q1 x + q2 y + q3 x^2 + q4 xy + q5 y^2 through the face barycentres,
+// shape operator from the fundamental forms, its eigen-decomposition; returns
+// sqrt(k1^2 + k2^2) and writes the two principal directions scaled by sqrt|k|,
+// the larger |k| first.
+static double fit_curvature(const Mesh& m, const std::vector<idt>& fl, double info[6]) {
+    double sarea = 0, origin[3] = {0, 0, 0}, frame[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    for (idt f : fl) {
+        double p1[3], p2[3], p3[3], nrm[3], area, bary[3];
+        m.point(m.F[3 * f], p1); m.point(m.F[3 * f + 1], p2); m.point(m.F[3 * f + 2], p3);
+        rmath::tri_normal(p1, p2, p3, nrm);
+        face_mass(m, f, area, bary);
+        for (int k = 0; k < 3; k++) {
+            origin[k] += area * bary[k];
+            frame[0][k] += area * nrm[k];
+        }
+        sarea += area;
+    }
+    for (int j = 0; j < 3; j++) origin[j] = origin[j] / sarea;
+    auto normalize = [](double* a) {
+        const double n = std::sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
+        if (n != 0.0) { a[0] /= n; a[1] /= n; a[2] /= n; }
+    };
+    auto cross = [](const double* a, const double* b, double* c) {
+        const double x = a[1] * b[2] - a[2] * b[1], y = a[2] * b[0] - a[0] * b[2], z = a[0] * b[1] - a[1] * b[0];
+        c[0] = x; c[1] = y; c[2] = z;
+    };
+    auto dot = [](const double* a, const double* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; };
+    normalize(frame[0]);
+    for (int k = 0; k < 3; k++) frame[2][k] = frame[0][k];
+    frame[1][1] = frame[2][0]; frame[1][2] = frame[2][1]; frame[1][0] = frame[2][2];
+    cross(frame[1], frame[2], frame[0]);
+    normalize(frame[0]);
+    cross(frame[2], frame[0], frame[1]);
+    for (int i = 0; i < 6; i++) info[i] = 0;
+    const int nf = (int)fl.size();
+    if (nf <= 6) return 0;
+    std::vector<double> V((size_t)nf * 6), Z(nf);
+    double h = 0;
+    for (int j = 0; j < nf; j++) {
+        double area, bary[3];
+        face_mass(m, fl[j], area, bary);
+        for (int k = 0; k < 3; k++) bary[k] -= origin[k];
+        const double x = dot(bary, frame[0]), y = dot(bary, frame[1]), z = dot(bary, frame[2]);
+        double* r = &V[(size_t)j * 6];
+        r[0] = 1.0; r[1] = x; r[2] = y; r[3] = x * x; r[4] = x * y; r[5] = y * y;
+        Z[j] = z;
+        h += std::sqrt(x * x + y * y);
+    }
+    h = h / ((double)nf);
+    for (int j = 0; j < nf; j++) {
+        double* r = &V[(size_t)j * 6];
+        r[1] /= h; r[2] /= h; r[3] /= h * h; r[4] /= h * h; r[5] /= h * h;
+    }
+    // normal equations (upper half, then mirrored), the reference's SolveLeastSquares (:508-616)
+    double xxt[6][6] = {}, xxti[6][6] = {}, xyt[6] = {}, q[6];
+    for (int k = 0; k < nf; k++) {
+        const double* r = &V[(size_t)k * 6];
+        for (int i = 0; i < 6; i++) {
+            for (int j = i; j < 6; j++) xxt[i][j] += r[i] * r[j];
+            xyt[i] += r[i] * Z[k];
+        }
+    }
+    for (int i = 0; i < 6; i++)
+        for (int j = 0; j < i; j++) xxt[i][j] = xxt[j][i];
+    double* xr[6]; double* xir[6];
+    for (int i = 0; i < 6; i++) { xr[i] = xxt[i]; xir[i] = xxti[i]; }
+    if (!rmath::lu_invert(xr, xir, 6)) return 0;
+    for (int i = 0; i < 6; i++) {
+        q[i] = 0.0;
+        for (int k = 0; k < 6; k++) q[i] += xxti[i][k] * xyt[k];
+    }
+    q[1] /= h; q[2] /= h; q[3] /= h * h; q[4] /= h * h; q[5] /= h * h;
+    const double E = 1.0 + q[1] * q[1], F = q[1] * q[2], G = 1.0 + q[2] * q[2];
+    const double e = 2.0 * q[3] / std::sqrt(q[1] * q[1] + 1.0 + q[2] * q[2]);
+    const double ff = 2.0 * q[4] / std::sqrt(q[1] * q[1] + 1.0 + q[2] * q[2]);
+    const double g = 2.0 * q[5] / std::sqrt(q[1] * q[1] + 1.0 + q[2] * q[2]);
+    double A[2][2] = {{E, F}, {F, G}}, B[2][2];
+    double* ar[2] = {A[0], A[1]}; double* br[2] = {B[0], B[1]};
+    if (!rmath::lu_invert(ar, br, 2)) return 0;
+    A[0][0] = -(e * B[0][0] + ff * B[1][0]);
+    A[1][0] = -(e * B[0][1] + ff * B[1][1]);
+    A[0][1] = -(ff * B[0][0] + g * B[1][0]);
+    A[1][1] = -(ff * B[0][1] + g * B[1][1]);
+    double ev[2], evec[2][2];
+    double* vr[2] = {evec[0], evec[1]};
+    if (!rmath::jacobi_upper(ar, 2, ev, vr)) return 0;
+    for (int i = 0; i < 2; i++)
+        for (int j = 0; j < 2; j++)
+            for (int k = 0; k < 3; k++) info[k + 3 * j] += std::sqrt(std::fabs(ev[j])) * evec[i][j] * frame[i][k];
+    if (std::fabs(ev[0]) < std::fabs(ev[1]))
+        for (int i = 0; i < 3; i++) std::swap(info[i], info[i + 3]);
+    return std::sqrt(ev[0] * ev[0] + ev[1] * ev[1]);
+}
+
+// Per-vertex curvature indicator (nV) and principal directions (6 nV, float as the
+// reference stores them).
+void port_curvature(void* hp, double* indicator, float* principal_dirs) {
+    const Mesh& m = ((PortHandle*)hp)->eng->mesh;
+    std::vector<char> ftag(m.nF, 0), vtag(m.nV, 0);
+    std::vector<idt> faces, tf, tv;
+    for (idt v = 0; v < m.nV; v++) {
+        faces.clear(); tf.clear(); tv.clear();
+        nring_faces(m, v, 3, faces, ftag, vtag, tf, tv);
+        double info[6];
+        indicator[v] = fit_curvature(m, faces, info);
+        for (int i = 0; i < 6; i++) principal_dirs[6 * v + i] = (float)info[i];
+        for (idt f : tf) ftag[f] = 0;
+        for (idt u : tv) vtag[u] = 0;
+    }
+}
+
 // ACVD's quadric post-placement (DiscreteRemeshing/Examples/ACVD.cxx:217-291): per
 // cluster, the unweighted plane quadrics (FullQuadric = false) of all faces adjacent to
 // each of its items (a face once per item, items in increasing id, faces in the

@@ -67,6 +67,7 @@ def _bind(lib, prefix):
         "clean": f("clean", ctypes.c_int, _P),
         "fill_holes": f("fill_holes", ctypes.c_int, _P),
         "post_placement": f("post_placement", None, _P, ctypes.c_int, _pd),
+        "curvature": f("curvature", None, _P, _pd, np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")),
     }
     return fns
 
@@ -162,6 +163,14 @@ class _Base:
         out = np.empty((self.k, 3), dtype=np.float64)
         self.f["post_placement"](self.h, int(level), out.ravel())
         return out
+
+    def curvature(self):
+        """Per-vertex curvature indicator (nV) and principal directions (nV x 6, float32)
+        of the mesh, vtkCurvatureMeasure's polynomial fitting on the vertex 3-ring."""
+        ind = np.empty(self.n, dtype=np.float64)
+        pd = np.empty(6 * self.n, dtype=np.float32)
+        self.f["curvature"](self.h, ind, pd)
+        return ind, pd.reshape(-1, 6)
 
     def fill_holes(self) -> int:
         return int(self.f["fill_holes"](self.h))

@@ -12,6 +12,7 @@
 #include "vtkIsotropicMetricForClustering.h"
 #include "vtkQEMetricForClustering.h"
 #include "vtkQuadricAnisotropicMetricForClustering.h"
+#include "vtkCurvatureMeasure.h"
 
 #include <chrono>
 #include <type_traits>
@@ -53,6 +54,7 @@ struct RefBase {
     virtual void set_labels(const int* lab) = 0;
     virtual int loops() = 0;
     virtual void post_placement(int level, double* out) = 0;
+    virtual void curvature(double* indicator, float* principal_dirs) = 0;
 };
 
 template <class M>
@@ -165,6 +167,23 @@ struct Ref : RefBase {
     // vtkQuadricTools::AddTriangleQuadric / ComputeRepresentativePoint and the
     // metric's GetClusterCentroid (the output vertices of BuildDelaunayTriangulation,
     // vtkDiscreteRemeshing.h:1024-1033).  Needs the cluster statistics (evaluate).
+    // What vtkDiscreteRemeshing::SamplingPreProcessing runs for vertex clustering
+    // (DiscreteRemeshing/vtkDiscreteRemeshing.h:630-637): the reference's own
+    // vtkCurvatureMeasure, polynomial fitting (method 1) on vertices with its
+    // default 3-ring neighbourhood and principal directions on.
+    void curvature(double* indicator, float* principal_dirs) override {
+        vtkCurvatureMeasure* cm = vtkCurvatureMeasure::New();
+        cm->SetInputData(p->GetInput());
+        cm->SetComputationMethod(1);
+        cm->SetElementsType(1);
+        cm->SetComputePrincipalDirections(1);
+        vtkDataArrayCollection* coll = cm->GetCurvatureIndicator();
+        vtkDoubleArray* ind = (vtkDoubleArray*)coll->GetItem(0);
+        vtkFloatArray* pd = (vtkFloatArray*)coll->GetItem(1);
+        for (long long i = 0; i < n; i++) indicator[i] = ind->GetValue(i);
+        for (long long i = 0; i < 6 * n; i++) principal_dirs[i] = pd->GetValue(i);
+        cm->Delete();
+    }
     void post_placement(int level, double* out) override {
         vtkSurface* mesh = p->GetInput();
         std::vector<double> Q(9 * (size_t)K, 0.0);
@@ -212,5 +231,8 @@ int ref_clean(void* h) { return ((RefBase*)h)->clean(); }
 int ref_fill_holes(void* h) { return ((RefBase*)h)->fill(); }
 int ref_loops(void* h) { return ((RefBase*)h)->loops(); }
 void ref_post_placement(void* h, int level, double* out) { ((RefBase*)h)->post_placement(level, out); }
+void ref_curvature(void* h, double* indicator, float* principal_dirs) {
+    ((RefBase*)h)->curvature(indicator, principal_dirs);
+}
 
 }  // extern "C"

@@ -13,7 +13,10 @@
 // these same functions, so the two agree to the last bit wherever the reference's
 // own arithmetic is restated faithfully.
 #pragma once
+#include <algorithm>
 #include <cmath>
+#include <utility>
+#include <vector>
 
 namespace rmath {
 
@@ -45,6 +48,116 @@ inline void tri_quadric(const double* x1, const double* x2, const double* x3, do
     n[3] = -(n[0] * x1[0] + n[1] * x1[1] + n[2] * x1[2]);
     for (int i = 0; i < 4; i++)
         for (int j = 0; j < 4; j++) q[i][j] = n[i] * n[j];
+}
+
+// Unit normal of the triangle (x1, x2, x3) from the cross product
+// (x3 - x2) x (x1 - x2) (right-handed in the vertex order); zero for a
+// degenerate triangle.  The direction convention is the one the reference's
+// vtkTriangle::ComputeNormal callers rely on (VTK >= 9.0, unpinned here).
+inline void tri_normal(const double* x1, const double* x2, const double* x3, double n[3]) {
+    const double a[3] = {x3[0] - x2[0], x3[1] - x2[1], x3[2] - x2[2]};
+    const double b[3] = {x1[0] - x2[0], x1[1] - x2[1], x1[2] - x2[2]};
+    n[0] = a[1] * b[2] - a[2] * b[1];
+    n[1] = a[2] * b[0] - a[0] * b[2];
+    n[2] = a[0] * b[1] - a[1] * b[0];
+    const double l = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+    if (l != 0.0) { n[0] /= l; n[1] /= l; n[2] /= l; }
+}
+
+// Inverse of the n x n matrix a (rows a[i]) by LU decomposition with partial
+// pivoting (Doolittle), then one forward / back substitution per unit vector.
+// Returns 0 when a pivot is exactly zero (singular), 1 otherwise.  Stands for
+// vtkMath::InvertMatrix (VTK >= 9.0, unpinned here).
+inline int lu_invert(double** a, double** ai, int n) {
+    std::vector<double> lu((size_t)n * n);
+    std::vector<int> piv(n);
+    for (int i = 0; i < n; i++)
+        for (int j = 0; j < n; j++) lu[(size_t)i * n + j] = a[i][j];
+    for (int k = 0; k < n; k++) {
+        int p = k;
+        double best = std::fabs(lu[(size_t)k * n + k]);
+        for (int i = k + 1; i < n; i++) {
+            const double v = std::fabs(lu[(size_t)i * n + k]);
+            if (v > best) { best = v; p = i; }
+        }
+        if (best == 0.0) return 0;
+        piv[k] = p;
+        if (p != k)
+            for (int j = 0; j < n; j++) std::swap(lu[(size_t)k * n + j], lu[(size_t)p * n + j]);
+        const double d = lu[(size_t)k * n + k];
+        for (int i = k + 1; i < n; i++) {
+            const double f = lu[(size_t)i * n + k] / d;
+            lu[(size_t)i * n + k] = f;
+            for (int j = k + 1; j < n; j++) lu[(size_t)i * n + j] -= f * lu[(size_t)k * n + j];
+        }
+    }
+    std::vector<double> x(n);
+    for (int c = 0; c < n; c++) {
+        for (int i = 0; i < n; i++) x[i] = (i == c) ? 1.0 : 0.0;
+        for (int k = 0; k < n; k++) if (piv[k] != k) std::swap(x[k], x[piv[k]]);
+        for (int i = 0; i < n; i++)
+            for (int j = 0; j < i; j++) x[i] -= lu[(size_t)i * n + j] * x[j];
+        for (int i = n - 1; i >= 0; i--) {
+            for (int j = i + 1; j < n; j++) x[i] -= lu[(size_t)i * n + j] * x[j];
+            x[i] /= lu[(size_t)i * n + i];
+        }
+        for (int i = 0; i < n; i++) ai[i][c] = x[i];
+    }
+    return 1;
+}
+
+// Eigen-decomposition of the symmetric matrix given by the upper triangle of the
+// n x n matrix a (a is not modified), by cyclic Jacobi rotations (Jacobi 1846;
+// Golub & Van Loan sec. 8.5): eigenvalues w in decreasing order, unit
+// eigenvectors in the columns of v.  Returns 1.  Stands for vtkMath::JacobiN
+// (VTK >= 9.0, unpinned here); the eigenvector signs are not specified.
+inline int jacobi_upper(double** a, int n, double* w, double** v) {
+    std::vector<double> m((size_t)n * n);
+    for (int i = 0; i < n; i++)
+        for (int j = 0; j < n; j++) m[(size_t)i * n + j] = (i <= j) ? a[i][j] : a[j][i];
+    for (int i = 0; i < n; i++)
+        for (int j = 0; j < n; j++) v[i][j] = (i == j) ? 1.0 : 0.0;
+    for (int sweep = 0; sweep < 64; sweep++) {
+        double off = 0.0;
+        for (int p = 0; p < n; p++)
+            for (int q = p + 1; q < n; q++) off += m[(size_t)p * n + q] * m[(size_t)p * n + q];
+        if (off == 0.0) break;
+        for (int p = 0; p < n; p++)
+            for (int q = p + 1; q < n; q++) {
+                const double apq = m[(size_t)p * n + q];
+                if (apq == 0.0) continue;
+                const double theta = (m[(size_t)q * n + q] - m[(size_t)p * n + p]) / (2.0 * apq);
+                const double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
+                const double c = 1.0 / std::sqrt(t * t + 1.0), s = t * c;
+                for (int k = 0; k < n; k++) {
+                    const double mkp = m[(size_t)k * n + p], mkq = m[(size_t)k * n + q];
+                    m[(size_t)k * n + p] = c * mkp - s * mkq;
+                    m[(size_t)k * n + q] = s * mkp + c * mkq;
+                }
+                for (int k = 0; k < n; k++) {
+                    const double mpk = m[(size_t)p * n + k], mqk = m[(size_t)q * n + k];
+                    m[(size_t)p * n + k] = c * mpk - s * mqk;
+                    m[(size_t)q * n + k] = s * mpk + c * mqk;
+                }
+                m[(size_t)p * n + q] = m[(size_t)q * n + p] = 0.0;
+                for (int k = 0; k < n; k++) {
+                    const double vkp = v[k][p], vkq = v[k][q];
+                    v[k][p] = c * vkp - s * vkq;
+                    v[k][q] = s * vkp + c * vkq;
+                }
+            }
+    }
+    for (int i = 0; i < n; i++) w[i] = m[(size_t)i * n + i];
+    // decreasing order (stable selection)
+    for (int i = 0; i < n; i++) {
+        int b = i;
+        for (int j = i + 1; j < n; j++) if (w[j] > w[b]) b = j;
+        if (b != i) {
+            std::swap(w[i], w[b]);
+            for (int k = 0; k < n; k++) std::swap(v[k][i], v[k][b]);
+        }
+    }
+    return 1;
 }
 
 // Symmetric 3x3 eigen-decomposition by cyclic Jacobi rotations.

@@ -14,6 +14,12 @@ public:
 
     void CreateFromArrays(vtkIdType nV, const double* pts, vtkIdType nF, const int* tri) {
         M.build(nV, pts, nF, tri);
+        for (int k = 0; k < 3; k++) { Pts.B[2 * k] = 1e300; Pts.B[2 * k + 1] = -1e300; }
+        for (vtkIdType v = 0; v < nV; v++)
+            for (int k = 0; k < 3; k++) {
+                Pts.B[2 * k] = std::min(Pts.B[2 * k], pts[3 * v + k]);
+                Pts.B[2 * k + 1] = std::max(Pts.B[2 * k + 1], pts[3 * v + k]);
+            }
         Faces.assign(M.F.begin(), M.F.end());
         Ring.resize(nV);
         for (vtkIdType v = 0; v < nV; v++) Ring[v].assign(M.ring[v].begin(), M.ring[v].end());
@@ -24,6 +30,8 @@ public:
     }
 
     vtkIdType GetNumberOfPoints() { return M.nV; }
+    // the point set's bounding box (vtkCurvatureMeasure reads it)
+    vtkPoints* GetPoints() { return &Pts; }
     vtkIdType GetNumberOfCells() { return M.nF; }
     vtkIdType GetNumberOfEdges() { return M.n_edges(); }
     bool IsFaceActive(vtkIdType) { return true; }
@@ -57,6 +65,31 @@ public:
     void GetPoint(vtkIdType i, double* p) { M.point(i, p); }
     void GetPointCoordinates(vtkIdType i, double* p) { M.point(i, p); }
     double GetFaceArea(vtkIdType f) { return M.face_area(f); }
+    // vtkSurface::GetCellMassProperties (Common/vtkSurface.cxx:1380-1419), triangles:
+    // area-weighted vertex mean, divided by the area when it is positive
+    void GetCellMassProperties(vtkIdType f, double& area, double* bary) {
+        double p1[3], p2[3], p3[3];
+        M.point(Faces[3 * f], p1); M.point(Faces[3 * f + 1], p2); M.point(Faces[3 * f + 2], p3);
+        area = 0;
+        bary[0] = bary[1] = bary[2] = 0;
+        const double a2 = rmath::tri_area(p1, p2, p3);
+        for (int i = 0; i < 3; i++) bary[i] += a2 * (p1[i] + p2[i] + p3[i]) / 3.0;
+        area += a2;
+        if (area > 0)
+            for (int i = 0; i < 3; i++) bary[i] /= area;
+    }
+    vtkIdType IsEdge(vtkIdType a, vtkIdType b) { return M.is_edge(a, b); }
+    vtkIdType GetThirdPoint(vtkIdType f, vtkIdType a, vtkIdType b) {
+        for (int j = 0; j < 3; j++) {
+            const vtkIdType v = Faces[3 * f + j];
+            if (v != a && v != b) return v;
+        }
+        return -1;
+    }
+    vtkDoubleArray* GetEdgeLengths() {
+        std::cerr << "shim vtkSurface: GetEdgeLengths (display only) is not available" << std::endl;
+        std::abort();
+    }
     double GetVertexArea(vtkIdType v) { return M.vertex_area(v); }
     vtkDoubleArray* GetVerticesAreas() {
         if (!Areas) {
@@ -70,6 +103,7 @@ public:
 
     port::Mesh M;
 private:
+    vtkPoints Pts;
     std::vector<vtkIdType> Faces;
     std::vector<std::vector<vtkIdType>> Ring;
     vtkDoubleArray* Areas = nullptr;

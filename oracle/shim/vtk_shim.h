@@ -48,6 +48,12 @@ typedef long long vtkIdType;
     virtual type Get##name() { return this->name; }
 #define vtkStandardNewMacro(thisClass) \
     thisClass* thisClass::New() { return new thisClass; }
+#define vtkTypeMacro(thisClass, superClass) typedef superClass Superclass;
+#define vtkGetObjectMacro(name, type) \
+    virtual type* Get##name() { return this->name; }
+#define vtkGenericWarningMacro(x) \
+    do { std::cerr << "warning: " << x << std::endl; } while (0)
+#define VTK_LINE 3
 
 class vtkObjectBase {
 public:
@@ -118,6 +124,7 @@ public:
     void SetNumberOfTuples(vtkIdType n) { V.resize(n * NumComp); }
     vtkIdType GetNumberOfTuples() const { return (vtkIdType)V.size() / NumComp; }
     vtkIdType GetNumberOfValues() const { return (vtkIdType)V.size(); }
+    vtkIdType GetSize() const { return (vtkIdType)V.size(); }
     T GetValue(vtkIdType i) const { return V[i]; }
     void SetValue(vtkIdType i, T v) { V[i] = v; }
     vtkIdType InsertNextValue(T v) { V.push_back(v); return (vtkIdType)V.size() - 1; }
@@ -200,6 +207,12 @@ public:
     static void SingularValueDecomposition3x3(const double A[3][3], double U[3][3], double w[3], double VT[3][3]) {
         rmath::svd3(A, U, w, VT);
     }
+    static int InvertMatrix(double** a, double** ai, int n) { return rmath::lu_invert(a, ai, n); }
+    static int JacobiN(double** a, int n, double* w, double** v) { return rmath::jacobi_upper(a, n, w, v); }
+    static void Diagonalize3x3(const double[3][3], double[3], double[3][3]) {
+        std::cerr << "shim vtkMath: Diagonalize3x3 (curvature by normal analysis) is not available" << std::endl;
+        std::abort();
+    }
     // Random numbers (only the non-default InitialSamplingType 0 uses them):
     // a 64-bit LCG, not VTK's generator.
     static void RandomSeed(int s) { state() = (unsigned long long)s; }
@@ -221,14 +234,7 @@ public:
         rmath::tri_quadric(x1, x2, x3, q);
     }
     static void ComputeNormal(const double x1[3], const double x2[3], const double x3[3], double n[3]) {
-        double q[4][4];
-        rmath::tri_quadric(x1, x2, x3, q);
-        const double l = std::sqrt(q[0][0] + q[1][1] + q[2][2]);
-        // recover the unit normal up to sign from the quadric's outer product
-        n[0] = q[0][0] > 0 ? std::sqrt(q[0][0]) : 0;
-        n[1] = n[0] != 0 ? q[0][1] / n[0] : std::sqrt(q[1][1]);
-        n[2] = n[0] != 0 ? q[0][2] / n[0] : (n[1] != 0 ? q[1][2] / n[1] : std::sqrt(q[2][2]));
-        (void)l;
+        rmath::tri_normal(x1, x2, x3, n);
     }
 };
 
@@ -240,12 +246,31 @@ public:
 class vtkCellData : public vtkDataSetAttributes {};
 class vtkPointData : public vtkDataSetAttributes {};
 
+// Compile-only: the principal-direction display polydata of vtkCurvatureMeasure.
+class vtkPoints : public vtkObject {
+public:
+    static vtkPoints* New() { return new vtkPoints; }
+    void Allocate(vtkIdType) {}
+    vtkIdType InsertNextPoint(const double p[3]) { P.insert(P.end(), p, p + 3); return (vtkIdType)P.size() / 3 - 1; }
+    void ComputeBounds() {}
+    double* GetBounds() { return B; }
+    void GetBounds(double b[6]) { for (int i = 0; i < 6; i++) b[i] = B[i]; }
+    double B[6] = {0, 0, 0, 0, 0, 0};
+private:
+    std::vector<double> P;
+};
+
 class vtkPolyData : public vtkObject {
 public:
     static vtkPolyData* New() { return new vtkPolyData; }
     vtkCellData* GetCellData() { return &CD; }
     vtkPointData* GetPointData() { return &PD; }
     void ShallowCopy(vtkPolyData*) {}
+    void Allocate(vtkIdType) {}
+    void SetPoints(vtkPoints* p) { Pts = p; }
+    vtkPoints* GetPoints() { return Pts; }
+    vtkIdType InsertNextCell(int, vtkIdList*) { return 0; }
+    vtkPoints* Pts = nullptr;
 private:
     vtkCellData CD;
     vtkPointData PD;
@@ -318,4 +343,10 @@ private:
 class vtkLookupTable : public vtkObject {
 public:
     static vtkLookupTable* New() { return new vtkLookupTable; }
+    void SetTableRange(double, double) {}
+    void SetSaturationRange(double, double) {}
+    void SetHueRange(double, double) {}
+    void SetValueRange(double, double) {}
+    void SetScaleToLog10() {}
+    void Build() {}
 };

@@ -6,7 +6,8 @@ $ACVD_REFERENCE_ROOT).  For each small case below this script stores the inputs
 (so that no platform's libm is needed to regenerate them) and the reference's
 outputs: the initial sampling, the converged labels, global energy, per-cluster
 sizes / centroids / energies, the accumulators of a fixed assignment and its
-quadric post-placement (the ACVD driver's last step) at levels 1 and 3.
+quadric post-placement (the ACVD driver's last step) at levels 1 and 3, and the
+reference's curvature indicator / principal directions of the mesh.
 
     python tests/golden/gen_golden.py
 """
@@ -65,6 +66,9 @@ def main():
                  fixed_energy=r2.global_energy(),
                  # ACVD's quadric post-placement (ACVD.cxx:217-291) of the fixed assignment
                  fixed_post1=r2.post_placement(1), fixed_post3=r2.post_placement(3))
+        # the reference's curvature of the mesh (vtkCurvatureMeasure, polynomial fitting,
+        # vertices, 3-ring), as vtkDiscreteRemeshing's pre-processing computes it
+        d["curv_indicator"], d["curv_dirs"] = O.Ref(metric, m.points, m.faces, k, 0.0).curvature()
         if initial is not None:
             d["initial"] = initial
         if ind is not None:

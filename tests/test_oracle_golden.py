@@ -62,3 +62,13 @@ def test_fixed_assignment_post_placement(oracle_lib, path):
     p.evaluate(g["fixed_labels"], 1)
     np.testing.assert_array_equal(p.post_placement(1), g["fixed_post1"])
     np.testing.assert_array_equal(p.post_placement(3), g["fixed_post3"])
+
+
+@pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p)[:-4] for p in GOLDEN])
+def test_curvature_matches_reference(oracle_lib, path):
+    """Curvature indicator and principal directions (vtkCurvatureMeasure, polynomial
+    fitting on the vertex 3-ring) of the restatement against the reference's own."""
+    g = _load(path)
+    ind, pd = oracle_lib.Port(str(g["metric"]), g["points"], g["faces"], int(g["k"]), 0.0).curvature()
+    np.testing.assert_array_equal(ind, g["curv_indicator"])
+    np.testing.assert_array_equal(pd, g["curv_dirs"])
