@@ -18,7 +18,10 @@ SRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libacvd_gb300.so")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
-CU_SOURCES = ["primitives.cu", "topology.cu", "cluster.cu", "adjoint.cu", "engine.cu", "noalloc.cu"]
+CU_SOURCES = ["primitives.cu", "topology.cu", "cluster.cu", "adjoint.cu", "engine.cu", "noalloc.cu", "curvature.cu"]
+# per-file flags: the curvature kernel keeps every FP64 product and sum separately
+# rounded, so that it reproduces the CPU restatement bit for bit
+CU_FILE_FLAGS = {"curvature.cu": ["-fmad=false"]}
 CXX_SOURCES = ["host.cpp"]
 
 
@@ -53,7 +56,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
         objs.append(obj)
         if force or _stale(obj, [src] + headers):
             jobs.append([nvcc, ARCH, "-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off",
-                         "-diag-suppress", "128"] + extra + ["-c", src, "-o", obj])
+                         "-diag-suppress", "128"] + CU_FILE_FLAGS.get(f, []) + extra + ["-c", src, "-o", obj])
     for f in CXX_SOURCES:
         src = os.path.join(SRC, f)
         obj = os.path.join(OUT, f + ".o")

@@ -58,6 +58,11 @@ struct acvd_ctx {
     // vertex id, inv: original vertex id -> item); faces and edges in item ids
     DBuf<int> perm, inv, tri_int, edge_int, label_orig;
     DBuf<int4> ring8;              // first 8 ring slots per item
+    // curvature: faces of every edge, edge of every ring slot, per-vertex outputs
+    DBuf<int2> curv_poly;
+    DBuf<int> curv_slot;
+    DBuf<double> curv_ind;
+    DBuf<float> curv_dirs;
     DBuf<unsigned char> bflag;     // per item: maybe on a cluster boundary
     // sweep classes: either the colour classes, or one class holding every item
     // (claims alone keep committed moves on disjoint clusters; colours are kept
@@ -128,7 +133,7 @@ struct acvd_ctx {
         DBuf<int> col_new;
         DBuf<double> ind, farea, fnorm, wd, varea, wsum;
         DBuf<float> pd;
-        DBuf<uint32_t> k1, v1, k2, v2, vrow;
+        DBuf<uint32_t> k1, k2, v2;
         DBuf<float4> t4;
         DBuf<float2> t2;
         DBuf<unsigned> maxbits;
@@ -423,6 +428,20 @@ int acvd_set_mesh(acvd_ctx* ctx, int64_t n_vertices, const double* xyz, int64_t 
     CK(cudaMemcpyAsync(ctx->row.p, csr_row, (n_vertices + 1) * sizeof(int), cudaMemcpyHostToDevice, ctx->s));
     CK(cudaMemcpyAsync(ctx->col.p, csr_col, 2 * n_edges * sizeof(int), cudaMemcpyHostToDevice, ctx->s));
     CK(cudaMemcpyAsync(ctx->edge_v.p, edge_v, 2 * n_edges * sizeof(int), cudaMemcpyHostToDevice, ctx->s));
+    // vertex -> faces in increasing face id (original ids): item build, curvature,
+    // adjoint and post-placement read it
+    {
+        DBuf<uint32_t>&k1 = ctx->setup.k1, &k2 = ctx->setup.k2, &v2 = ctx->setup.v2;
+        CK(k1.resize(3 * n_faces));
+        CK(k2.resize(3 * n_faces));
+        CK(v2.resize(3 * n_faces));
+        CK(ctx->vf_row.resize(n_vertices + 1));
+        CK(ctx->vf_face.resize(3 * n_faces));
+        CK(launch_vertex_keys(ctx->tri.p, n_faces, k1.p, ctx->vf_face.p, ctx->s));
+        CK(radix_sort_pairs(k1.p, ctx->vf_face.p, k2.p, v2.p, 3 * n_faces, bits_for((uint64_t)n_vertices),
+                            ctx->scratch, ctx->s));
+        CK(launch_segment_offsets(k1.p, 3 * n_faces, (uint32_t)n_vertices, ctx->vf_row.p, ctx->s));
+    }
     // colouring on the input rings, then the items in internal order
     int r = setup_colors(ctx);
     if (r) return r;
@@ -467,17 +486,6 @@ int acvd_set_metric(acvd_ctx* ctx, int metric, const double* indicator, const fl
     CK(varea.resize(nv));
     CK(wsum.resize(1));
     CK(launch_face_geometry(ctx->xyz.p, ctx->tri.p, nf, farea.p, fnorm.p, ctx->s));
-    // vertex -> faces in increasing face id
-    DBuf<uint32_t>&k1 = ctx->setup.k1, &v1 = ctx->setup.v1, &k2 = ctx->setup.k2, &v2 = ctx->setup.v2,
-                  &vrow = ctx->setup.vrow;
-    CK(k1.resize(3 * nf));
-    CK(v1.resize(3 * nf));
-    CK(k2.resize(3 * nf));
-    CK(v2.resize(3 * nf));
-    CK(vrow.resize(nv + 1));
-    CK(launch_vertex_keys(ctx->tri.p, nf, k1.p, v1.p, ctx->s));
-    CK(radix_sort_pairs(k1.p, v1.p, k2.p, v2.p, 3 * nf, bits_for((uint64_t)nv), ctx->scratch, ctx->s));
-    CK(launch_segment_offsets(k1.p, 3 * nf, (uint32_t)nv, vrow.p, ctx->s));
     CK(ctx->xw.resize(nv));
     if (metric != kIso) {
         CK(ctx->qa.resize(nv));
@@ -487,12 +495,8 @@ int acvd_set_metric(acvd_ctx* ctx, int metric, const double* indicator, const fl
         CK(ctx->ta.resize(nv));
         CK(ctx->tb.resize(nv));
     }
-    CK(launch_vertex_items(metric, nv, ctx->xyz.p, vrow.p, v1.p, farea.p, fnorm.p, use_ind ? ind.p : nullptr,
+    CK(launch_vertex_items(metric, nv, ctx->xyz.p, ctx->vf_row.p, ctx->vf_face.p, farea.p, fnorm.p, use_ind ? ind.p : nullptr,
                            gradation, wd.p, varea.p, ctx->qa.p, ctx->qb.p, ctx->s));
-    CK(ctx->vf_row.resize(nv + 1));
-    CK(ctx->vf_face.resize(3 * nf));
-    CK(cudaMemcpyAsync(ctx->vf_row.p, vrow.p, (nv + 1) * sizeof(uint32_t), cudaMemcpyDeviceToDevice, ctx->s));
-    CK(cudaMemcpyAsync(ctx->vf_face.p, v1.p, 3 * nf * sizeof(uint32_t), cudaMemcpyDeviceToDevice, ctx->s));
     ctx->gradation = gradation;
     const double ratio = metric == kQEM ? 10000.0 : 100000.0;
     if (ctx->nmesh > 0) {
@@ -1181,6 +1185,38 @@ extern "C" int acvd_get_boundary_edges(acvd_ctx* ctx, int32_t* ids, int64_t* cou
         CK(cudaMemcpyAsync(ids, out.p, t * sizeof(int), cudaMemcpyDeviceToHost, ctx->s));
         CK(cudaStreamSynchronize(ctx->s));
     }
+    return ACVD_OK;
+}
+
+// Curvature of vertex clustering (vtkDiscreteRemeshing.h:630-637 ->
+// vtkCurvatureMeasure, polynomial fitting on the vertex 3-ring): indicator[nV]
+// and principal_dirs[6 nV], either may be NULL.
+extern "C" int acvd_compute_curvature(acvd_ctx* ctx, double* indicator, float* principal_dirs) {
+    if (!ctx) return ACVD_ERR_ARG;
+    if (!ctx->ready_mesh) return fail(ctx, ACVD_ERR_ARG, "acvd_compute_curvature before acvd_set_mesh");
+    CK(cudaSetDevice(ctx->opts.device));
+    const int64_t nv = ctx->nV, ne = ctx->nE;
+    CK(ctx->curv_poly.resize(ne));
+    CK(ctx->curv_slot.resize(2 * ne));
+    CK(ctx->curv_ind.resize(nv));
+    CK(ctx->curv_dirs.resize(6 * nv));
+    CK(ctx->dtmp.resize(2));
+    unsigned long long* overflow = (unsigned long long*)ctx->dtmp.p;
+    CK(cudaMemsetAsync(overflow, 0, sizeof(unsigned long long), ctx->s));
+    CK(launch_curvature(ctx->xyz.p, ctx->tri.p, nv, ne, ctx->edge_v.p, ctx->edge_int.p, ctx->vf_row.p,
+                        ctx->vf_face.p, ctx->row.p, ctx->col.p, ctx->perm.p, ctx->inv.p, ctx->curv_poly.p,
+                        ctx->curv_slot.p, ctx->curv_ind.p, ctx->curv_dirs.p, overflow, ctx->s));
+    unsigned long long h_over = 0;
+    CK(cudaMemcpyAsync(&h_over, overflow, sizeof h_over, cudaMemcpyDeviceToHost, ctx->s));
+    if (indicator)
+        CK(cudaMemcpyAsync(indicator, ctx->curv_ind.p, nv * sizeof(double), cudaMemcpyDeviceToHost, ctx->s));
+    if (principal_dirs)
+        CK(cudaMemcpyAsync(principal_dirs, ctx->curv_dirs.p, 6 * nv * sizeof(float), cudaMemcpyDeviceToHost,
+                           ctx->s));
+    CK(cudaStreamSynchronize(ctx->s));
+    if (h_over)
+        return fail(ctx, ACVD_ERR_UNSUPPORTED,
+                    std::to_string(h_over) + " vertices have a 3-ring larger than the curvature kernel's buffers");
     return ACVD_OK;
 }
 

@@ -93,6 +93,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         "acvd_get_dual_mesh": (ctypes.c_int, [_P, _P, ctypes.POINTER(_i64)]),
         "acvd_boundary_edges_noalloc": (ctypes.c_int, [_P, _i64, _P, _P, _P, _P]),
         "acvd_post_placement": (ctypes.c_int, [_P, ctypes.c_int, _P]),
+        "acvd_compute_curvature": (ctypes.c_int, [_P, _P, _P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -265,6 +266,14 @@ class Engine:
         st = Stats()
         self._ck(self._lib.acvd_minimize(self.ctx, ctypes.byref(st)), "acvd_minimize")
         return st.as_dict()
+
+    def compute_curvature(self):
+        """Per-vertex curvature indicator (nV) and principal directions (nV x 6,
+        float32), vtkCurvatureMeasure's polynomial fitting on the vertex 3-ring."""
+        ind = np.empty(self.n, dtype=np.float64)
+        pd = np.empty((self.n, 6), dtype=np.float32)
+        self._ck(self._lib.acvd_compute_curvature(self.ctx, _ptr(ind), _ptr(pd)), "acvd_compute_curvature")
+        return ind, pd
 
     def post_placement(self, level: int = 1) -> np.ndarray:
         """ACVD's quadric post-placement of the output vertices (ACVD.cxx:217-291): (K, 3)."""

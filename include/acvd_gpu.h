@@ -205,6 +205,18 @@ int acvd_boundary_edges_noalloc(const int32_t* d_edge_v, int64_t n_edges, const 
                                 int32_t* d_ids, uint32_t* d_count, void* stream);
 
 /*
+ * Curvature of the mesh for vertex clustering, as vtkDiscreteRemeshing's
+ * pre-processing computes it (DiscreteRemeshing/vtkDiscreteRemeshing.h:630-637 ->
+ * Common/vtkCurvatureMeasure.cxx, polynomial fitting, vertices, 3-ring): per vertex
+ * the indicator sqrt(k1^2 + k2^2) (indicator[nV]) and the two principal directions
+ * scaled by sqrt|k|, the larger |k| first (principal_dirs[6 nV]); either output may
+ * be NULL.  These are the arrays acvd_set_metric takes.  FP64 on the device.
+ * Needs acvd_set_mesh.  A vertex whose 3-ring exceeds 192 faces returns
+ * ACVD_ERR_UNSUPPORTED.
+ */
+int acvd_compute_curvature(acvd_ctx* ctx, double* indicator, float* principal_dirs);
+
+/*
  * ACVD's quadric post-placement of the output vertices
  * (DiscreteRemeshing/Examples/ACVD.cxx:217-291, the ACVD driver's step after
  * Remesh()): per cluster, the unweighted plane quadrics of every face adjacent to
