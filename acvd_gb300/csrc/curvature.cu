@@ -49,9 +49,19 @@ __global__ void slot_edges_kernel(const int* __restrict__ edge_int, int64_t ne, 
         if (col[p] == a) { slot_edge[p] = (int)e; break; }
 }
 
+// Per face, once: unit normal, area and area-weighted barycentre, the values the
+// fit reads for every vertex whose 3-ring holds the face.
+struct FaceProps {
+    double n[3];
+    double area;
+    double bary[3];
+    double pad;
+};
+
 struct CurvMesh {
     const double* xyz;
     const int* tri;
+    const FaceProps* fp;
     int64_t nv;
     const int* row;        // internal ring CSR
     const int* col;
@@ -60,10 +70,6 @@ struct CurvMesh {
     const int* slot_edge;
     const int2* poly;
 };
-
-__device__ __forceinline__ void curv_point(const CurvMesh& m, int v, double p[3]) {
-    p[0] = m.xyz[3 * (int64_t)v]; p[1] = m.xyz[3 * (int64_t)v + 1]; p[2] = m.xyz[3 * (int64_t)v + 2];
-}
 
 // area by the side-length form (Common/vtkSurface.cxx:1283) and the
 // area-weighted vertex mean (vtkSurface::GetCellMassProperties, :1380-1419)
@@ -105,6 +111,23 @@ __device__ __forceinline__ void curv_cross(const double a[3], const double b[3],
 
 __device__ __forceinline__ double curv_dot(const double a[3], const double b[3]) {
     return a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
+}
+
+__global__ void face_props_kernel(const double* __restrict__ xyz, const int* __restrict__ tri, int64_t nf,
+                                  FaceProps* __restrict__ fp) {
+    const int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= nf) return;
+    double p1[3], p2[3], p3[3];
+    for (int k = 0; k < 3; k++) {
+        p1[k] = xyz[3 * (int64_t)tri[3 * f] + k];
+        p2[k] = xyz[3 * (int64_t)tri[3 * f + 1] + k];
+        p3[k] = xyz[3 * (int64_t)tri[3 * f + 2] + k];
+    }
+    FaceProps r;
+    curv_normal(p1, p2, p3, r.n);
+    curv_face_mass(p1, p2, p3, r.area, r.bary);
+    r.pad = 0.0;
+    fp[f] = r;
 }
 
 // Inverse of the n x n matrix a by LU decomposition with partial pivoting
@@ -195,14 +218,11 @@ __device__ double curv_fit(const CurvMesh& m, const int* fl, int nf, double* xs,
                            double info[6]) {
     double sarea = 0, origin[3] = {0, 0, 0}, frame[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
     for (int j = 0; j < nf; j++) {
-        const int f = fl[j];
-        double p1[3], p2[3], p3[3], nrm[3], area, bary[3];
-        curv_point(m, m.tri[3 * f], p1); curv_point(m, m.tri[3 * f + 1], p2); curv_point(m, m.tri[3 * f + 2], p3);
-        curv_normal(p1, p2, p3, nrm);
-        curv_face_mass(p1, p2, p3, area, bary);
+        const FaceProps& q = m.fp[fl[j]];
+        const double area = q.area;
         for (int k = 0; k < 3; k++) {
-            origin[k] += area * bary[k];
-            frame[0][k] += area * nrm[k];
+            origin[k] += area * q.bary[k];
+            frame[0][k] += area * q.n[k];
         }
         sarea += area;
     }
@@ -217,10 +237,8 @@ __device__ double curv_fit(const CurvMesh& m, const int* fl, int nf, double* xs,
     if (nf <= 6) return 0;
     double h = 0;
     for (int j = 0; j < nf; j++) {
-        const int f = fl[j];
-        double p1[3], p2[3], p3[3], area, bary[3];
-        curv_point(m, m.tri[3 * f], p1); curv_point(m, m.tri[3 * f + 1], p2); curv_point(m, m.tri[3 * f + 2], p3);
-        curv_face_mass(p1, p2, p3, area, bary);
+        const FaceProps& fq = m.fp[fl[j]];
+        double bary[3] = {fq.bary[0], fq.bary[1], fq.bary[2]};
         for (int k = 0; k < 3; k++) bary[k] -= origin[k];
         const double x = curv_dot(bary, frame[0]), y = curv_dot(bary, frame[1]), z = curv_dot(bary, frame[2]);
         xs[j] = x; ys[j] = y; zs[j] = z;
@@ -342,17 +360,22 @@ __global__ void __launch_bounds__(64) curvature_kernel(CurvMesh m, double* __res
 
 static inline unsigned cgrid(int64_t n, int b) { return (unsigned)((n + b - 1) / b); }
 
-cudaError_t launch_curvature(const double* xyz, const int* tri, int64_t nv, int64_t ne, const int* edge_v,
-                             const int* edge_int, const uint32_t* vf_row, const uint32_t* vf_face, const int* row,
-                             const int* col, const int* perm, const int* inv, int2* poly, int* slot_edge,
-                             double* indicator, float* dirs, unsigned long long* overflow, cudaStream_t s) {
+size_t curvature_face_bytes(int64_t nf) { return (size_t)nf * sizeof(FaceProps); }
+
+cudaError_t launch_curvature(const double* xyz, const int* tri, int64_t nv, int64_t nf, int64_t ne,
+                             const int* edge_v, const int* edge_int, const uint32_t* vf_row, const uint32_t* vf_face,
+                             const int* row, const int* col, const int* perm, const int* inv, int2* poly,
+                             int* slot_edge, void* face_work, double* indicator, float* dirs,
+                             unsigned long long* overflow, cudaStream_t s) {
     if (nv == 0) return cudaSuccess;
     cudaError_t err = cudaMemsetAsync(slot_edge, 0xff, 2 * ne * sizeof(int), s);   // -1: no edge
     if (err != cudaSuccess) return err;
-    g_launches += 3;
+    g_launches += 4;
+    FaceProps* fp = (FaceProps*)face_work;
+    face_props_kernel<<<cgrid(nf, 256), 256, 0, s>>>(xyz, tri, nf, fp);
     edge_faces_kernel<<<cgrid(ne, 256), 256, 0, s>>>(edge_v, ne, tri, vf_row, vf_face, poly);
     slot_edges_kernel<<<cgrid(ne, 256), 256, 0, s>>>(edge_int, ne, row, col, slot_edge);
-    CurvMesh m{xyz, tri, nv, row, col, perm, inv, slot_edge, poly};
+    CurvMesh m{xyz, tri, fp, nv, row, col, perm, inv, slot_edge, poly};
     curvature_kernel<<<cgrid(nv, 64), 64, 0, s>>>(m, indicator, dirs, overflow);
     return cudaGetLastError();
 }

@@ -63,6 +63,7 @@ struct acvd_ctx {
     DBuf<int> curv_slot;
     DBuf<double> curv_ind;
     DBuf<float> curv_dirs;
+    DBuf<char> curv_faces;
     DBuf<unsigned char> bflag;     // per item: maybe on a cluster boundary
     // sweep classes: either the colour classes, or one class holding every item
     // (claims alone keep committed moves on disjoint clusters; colours are kept
@@ -1203,9 +1204,10 @@ extern "C" int acvd_compute_curvature(acvd_ctx* ctx, double* indicator, float* p
     CK(ctx->dtmp.resize(2));
     unsigned long long* overflow = (unsigned long long*)ctx->dtmp.p;
     CK(cudaMemsetAsync(overflow, 0, sizeof(unsigned long long), ctx->s));
-    CK(launch_curvature(ctx->xyz.p, ctx->tri.p, nv, ne, ctx->edge_v.p, ctx->edge_int.p, ctx->vf_row.p,
+    CK(ctx->curv_faces.resize(curvature_face_bytes(ctx->nF)));
+    CK(launch_curvature(ctx->xyz.p, ctx->tri.p, nv, ctx->nF, ne, ctx->edge_v.p, ctx->edge_int.p, ctx->vf_row.p,
                         ctx->vf_face.p, ctx->row.p, ctx->col.p, ctx->perm.p, ctx->inv.p, ctx->curv_poly.p,
-                        ctx->curv_slot.p, ctx->curv_ind.p, ctx->curv_dirs.p, overflow, ctx->s));
+                        ctx->curv_slot.p, ctx->curv_faces.p, ctx->curv_ind.p, ctx->curv_dirs.p, overflow, ctx->s));
     unsigned long long h_over = 0;
     CK(cudaMemcpyAsync(&h_over, overflow, sizeof h_over, cudaMemcpyDeviceToHost, ctx->s));
     if (indicator)

@@ -260,10 +260,12 @@ cudaError_t launch_post_place(const double* qv, const uint32_t* sorted, const ui
                               int level, double* out, cudaStream_t s);
 
 // ---- curvature (curvature.cu) ----
-cudaError_t launch_curvature(const double* xyz, const int* tri, int64_t nv, int64_t ne, const int* edge_v,
-                             const int* edge_int, const uint32_t* vf_row, const uint32_t* vf_face, const int* row,
-                             const int* col, const int* perm, const int* inv, int2* poly, int* slot_edge,
-                             double* indicator, float* dirs, unsigned long long* overflow, cudaStream_t s);
+size_t curvature_face_bytes(int64_t nf);
+cudaError_t launch_curvature(const double* xyz, const int* tri, int64_t nv, int64_t nf, int64_t ne,
+                             const int* edge_v, const int* edge_int, const uint32_t* vf_row, const uint32_t* vf_face,
+                             const int* row, const int* col, const int* perm, const int* inv, int2* poly,
+                             int* slot_edge, void* face_work, double* indicator, float* dirs,
+                             unsigned long long* overflow, cudaStream_t s);
 
 // ---- adjoint (adjoint.cu) ----
 // Work arrays and inputs of the fixed-clustering adjoint (FP64).

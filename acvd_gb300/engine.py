@@ -267,11 +267,20 @@ class Engine:
         self._ck(self._lib.acvd_minimize(self.ctx, ctypes.byref(st)), "acvd_minimize")
         return st.as_dict()
 
-    def compute_curvature(self):
+    def compute_curvature(self, indicator: np.ndarray | None = None, principal_dirs: np.ndarray | None = None,
+                          copy_out: bool = True):
         """Per-vertex curvature indicator (nV) and principal directions (nV x 6,
-        float32), vtkCurvatureMeasure's polynomial fitting on the vertex 3-ring."""
-        ind = np.empty(self.n, dtype=np.float64)
-        pd = np.empty((self.n, 6), dtype=np.float32)
+        float32), vtkCurvatureMeasure's polynomial fitting on the vertex 3-ring.
+        Writes into the given arrays when passed (e.g. pinned buffers); with
+        copy_out=False the results stay on the device and None is returned."""
+        if not copy_out:
+            self._ck(self._lib.acvd_compute_curvature(self.ctx, None, None), "acvd_compute_curvature")
+            return None
+        ind = indicator if indicator is not None else np.empty(self.n, dtype=np.float64)
+        pd = principal_dirs if principal_dirs is not None else np.empty((self.n, 6), dtype=np.float32)
+        if ind.dtype != np.float64 or pd.dtype != np.float32 or ind.size != self.n or pd.size != 6 * self.n \
+                or not ind.flags.c_contiguous or not pd.flags.c_contiguous:
+            raise ValueError("compute_curvature needs contiguous float64 (n) and float32 (n x 6) outputs")
         self._ck(self._lib.acvd_compute_curvature(self.ctx, _ptr(ind), _ptr(pd)), "acvd_compute_curvature")
         return ind, pd
 

@@ -10,16 +10,17 @@ vtkAnisotropicDiscreteRemeshing.h:49-71), backed by the GPU engine:
     r.SetNumberOfClusters(20000)
     r.SetSubsamplingThreshold(10)
     r.GetMetric().SetGradation(1.5)
-    r.SetCurvatureInfo(indicator)                # per-vertex curvature indicator
+    r.SetCurvatureInfo(indicator)                # optional: otherwise computed on the GPU
     r.SetUnconstrainedInitialization(1)
     r.Remesh()
     coarse = r.GetOutput()                       # Surface
     labels = r.GetClustering()
 
-Differences from the reference, by design: the curvature indicator / principal
-directions are inputs (SetCurvatureInfo) rather than computed inside Remesh();
-meshes that would need subdivision (N < threshold * K) are rejected; display
-options must stay 0.
+Remesh() computes the curvature indicator / principal directions the metric needs
+on the GPU (vtkCurvatureMeasure's polynomial fitting, as the reference's
+SamplingPreProcessing does); SetCurvatureInfo supplies them instead.  Differences
+from the reference, by design: meshes that would need subdivision
+(N < threshold * K) are rejected; display options must stay 0.
 """
 from __future__ import annotations
 
@@ -155,15 +156,20 @@ class _DiscreteRemeshing:
         if n < self.SubsamplingThreshold * k:
             raise _eng.AcvdError(5, f"{n} vertices < SubsamplingThreshold * K = {self.SubsamplingThreshold * k}: "
                                     "the input would need subdivision, which this build does not do")
-        if self._needs_indicator() and self.Indicator is None:
-            raise _eng.AcvdError(1, "gradation > 0 needs SetCurvatureInfo(indicator)")
-        if self._metric_name == "aniso" and self.PrincipalDirections is None:
-            raise _eng.AcvdError(1, "the anisotropic metric needs SetCurvatureInfo(indicator, principal_dirs)")
         row, col, ev = self.Input.topology()
         if self._engine is None:
             self._engine = _eng.Engine(self._device, max_loops=self.MaxNumberOfLoops)
         e = self._engine
         e.set_mesh(self.Input.points, self.Input.faces, row, col, ev)
+        # SamplingPreProcessing (vtkDiscreteRemeshing.h:583-700): the curvature the
+        # metric needs, computed here (on the GPU) unless SetCurvatureInfo gave it
+        need_pd = self._metric_name == "aniso"
+        if (self._needs_indicator() and self.Indicator is None) or (need_pd and self.PrincipalDirections is None):
+            ind_c, pd_c = e.compute_curvature()
+            if self.Indicator is None:
+                self.Indicator = ind_c
+            if need_pd and self.PrincipalDirections is None:
+                self.PrincipalDirections = pd_c
         ind = self.Indicator if self._needs_indicator() else None
         e.set_metric(self._metric_name, ind, self.PrincipalDirections, self._metric.Gradation)
         e.set_level(self._metric.QuadricsOptimizationLevel)

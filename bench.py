@@ -69,6 +69,167 @@ ADJOINT_WORKLOADS = {
 }
 
 
+CURVATURE_WORKLOADS = {
+    "curvature_torus_1024x512": dict(kind="torus", mesh=dict(nu=1024, nv=512, seed=0),
+                                     desc="vertex curvature (vtkCurvatureMeasure polynomial fitting on the "
+                                          "3-ring) of the torus 1024x512 (524,288 vertices)"),
+    "curvature_heightfield_4096": dict(kind="heightfield", mesh=dict(n=4096, seed=0),
+                                       desc="vertex curvature (vtkCurvatureMeasure polynomial fitting on the "
+                                            "3-ring) of the heightfield 4096^2 (16,777,216 vertices)"),
+}
+CURV_CHECK = 4096        # vertices compared bit for bit with the oracle
+CURV_CPU_SAMPLE = 65536  # vertices of the single-core CPU baseline
+
+
+def run_curvature_arm(args):
+    """Per-vertex curvature on the GPU: resident (device time) and end to end (set_mesh
+    from pinned host buffers, outputs back into pinned buffers)."""
+    import torch
+    import acvd_gb300
+    from acvd_gb300 import engine as E
+    from acvd_gb300 import synth
+
+    ws, rank, local = _dist()
+    device = local
+    torch.cuda.set_device(device)
+    w = CURVATURE_WORKLOADS[args.workload]
+    m = synth.make(w["kind"], with_curvature=False, **w["mesh"])
+    n = m.n_points
+    row, col, ev = acvd_gb300.build_topology(n, m.faces)
+    eng = E.Engine(device=device)
+    eng.set_mesh(m.points, m.faces, row, col, ev)
+    stream = torch.cuda.ExternalStream(eng.stream(), device=device)
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=f"cuda:{device}")
+    for _ in range(args.warmup):
+        eng.compute_curvature(copy_out=False)
+    torch.cuda.synchronize()
+    step_ms = []
+    with ClockSampler(device) as clk:
+        for _ in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            eng.compute_curvature(copy_out=False)
+            e1.record(stream)
+            e1.synchronize()
+            step_ms.append(e0.elapsed_time(e1))
+    ms = statistics.mean(step_ms)
+    ind, pd = eng.compute_curvature()
+    eng.close()
+    e2e = None
+    if not args.no_e2e:
+        c = np.ascontiguousarray
+        h_pts, h_faces, h_row, h_col, h_ev = (pinned(torch, a) for a in (
+            c(m.points, dtype=np.float64), c(m.faces, dtype=np.int32), c(row, dtype=np.int32),
+            c(col, dtype=np.int32), c(ev, dtype=np.int32)))
+        o_ind = pinned(torch, np.zeros(n, dtype=np.float64))
+        o_pd = pinned(torch, np.zeros((n, 6), dtype=np.float32))
+        eng2 = E.Engine(device=device)
+        e2e_ms = []
+        for _ in range(max(1, args.steps)):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            eng2.set_mesh(h_pts, h_faces, h_row, h_col, h_ev)
+            eng2.compute_curvature(o_ind, o_pd)
+            e2e_ms.append(1000.0 * (time.perf_counter() - t0))
+        eng2.close()
+        assert np.array_equal(o_ind, ind) and np.array_equal(o_pd, pd), "end-to-end curvature differs"
+        e2e = {"value": n / (statistics.mean(e2e_ms) / 1000.0), "unit": "vertices/s",
+               "h2d_bytes_per_step": int(h_pts.nbytes + h_faces.nbytes + h_row.nbytes + h_col.nbytes + h_ev.nbytes),
+               "d2h_bytes_per_step": int(o_ind.nbytes + o_pd.nbytes), "ms_per_step": statistics.mean(e2e_ms),
+               "includes": "acvd_set_mesh (topology upload, colouring, item order, vertex-face CSR) + curvature"}
+    if rank != 0:
+        return
+    from oracle import oracle
+    oracle.build(ref=False)
+    port = oracle.Port("iso", m.points, m.faces, 10, 0.0)
+    step = max(1, n // CURV_CHECK)
+    chk = np.arange(0, n, step)[:CURV_CHECK]
+    exact = True
+    for v in chk[:64]:
+        ci, cp = port.curvature_range(int(v), int(v) + 1)
+        exact &= bool(ci[v] == ind[v]) and bool(np.array_equal(cp[v], pd[v]))
+    cpu = None
+    if not args.no_cpu_baseline:
+        sample = min(n, CURV_CPU_SAMPLE)
+        t0 = time.perf_counter()
+        port.curvature_range(0, sample)
+        secs = time.perf_counter() - t0
+        cpu = {"value": sample / secs, "unit": "vertices/s", "cores": 1, "kind": "port",
+               "sample": f"vertices 0..{sample} of the workload mesh, one core ({secs:.2f} s)"}
+    line = {
+        "metric": "vertex curvature throughput (vtkCurvatureMeasure polynomial fitting, 3-ring)",
+        "value": n / (ms / 1000.0), "unit": "vertices/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": args.workload, "description": w["desc"], "vertices": n, "faces": m.n_faces,
+                   "l2": "flushed between timed steps (256 MB write)"},
+        "roofline": None,
+        "roofline_note": "FP64-ALU bound (one thread per vertex, about 8,000 FP64 operations each); "
+                         "MEASURED_PEAKS.json holds no FP64 peak",
+        "parity": {"vertices_checked_bit_exact_vs_oracle": 64, "bit_exact": exact},
+        "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": 3,
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+
+
+def _curv_job(a):
+    """Reference-arm worker: curvature of the vertices [v0, v1) of the workload mesh."""
+    name, v0, v1 = a
+    from acvd_gb300 import synth
+    from oracle import oracle
+    global _CURV_PORT
+    if _CURV_PORT is None or _CURV_PORT[0] != name:
+        w = CURVATURE_WORKLOADS[name]
+        m = synth.make(w["kind"], with_curvature=False, **w["mesh"])
+        _CURV_PORT = (name, oracle.Port("iso", m.points, m.faces, 10, 0.0))
+    t0 = time.perf_counter()
+    _CURV_PORT[1].curvature_range(v0, v1)
+    return time.perf_counter() - t0
+
+
+_CURV_PORT = None
+
+
+def run_curvature_reference_arm(args):
+    """CPU arm for the curvature workloads: the restatement of vtkCurvatureMeasure with
+    the vertices dealt to every host core, as the reference's threads deal them."""
+    ws, rank, _ = _dist()
+    if rank != 0:
+        return
+    import multiprocessing as mp
+    from acvd_gb300 import synth
+    from oracle import oracle
+    oracle.build(ref=False)
+    cores = os.cpu_count() or 1
+    w = CURVATURE_WORKLOADS[args.workload]
+    m = synth.make(w["kind"], with_curvature=False, **w["mesh"])
+    n = m.n_points
+    bounds = [(args.workload, (n * c) // cores, (n * (c + 1)) // cores) for c in range(cores)]
+    times = []
+    with mp.get_context("spawn").Pool(cores) as pool:
+        pool.map(_curv_job, [(args.workload, 0, 1)] * cores)   # every worker builds its mesh first
+        for step in range(args.warmup + args.steps):
+            t = pool.map(_curv_job, bounds)
+            if step >= args.warmup:
+                times.append(max(t))
+    ms = 1000.0 * statistics.mean(times)
+    value = n / (ms / 1000.0)
+    print(json.dumps({"impl": "reference", "metric": "vertex curvature throughput (vtkCurvatureMeasure polynomial "
+                      "fitting, 3-ring)", "value": value, "unit": "vertices/s", "n_gpus": ws,
+                      "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+                      "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                      "config": {"workload": args.workload, "description": w["desc"], "vertices": n},
+                      "cpu_baseline": {"value": value, "unit": "vertices/s", "cores": cores, "kind": "port",
+                                       "sample": f"all {n} vertices dealt over {cores} cores"},
+                      "e2e": {"value": value, "unit": "vertices/s", "h2d_bytes_per_step": 0,
+                              "d2h_bytes_per_step": 0}}), flush=True)
+
+
 def run_adjoint_arm(args):
     """Adjoint workload: converge, fix the clustering, time forward + backward of
     E + sum_k G_k . c_k, and check 64 random coordinates against FP64 central
@@ -664,12 +825,17 @@ def main():
                     help="sweep schedule: per-phase kernels in CUDA graphs, or one persistent "
                          "cooperative kernel between convergence events")
     ap.add_argument("--workload", default="torus_1024x512_qem",
-                    choices=sorted(WORKLOADS) + sorted(BATCH_WORKLOADS) + sorted(ADJOINT_WORKLOADS))
+                    choices=sorted(WORKLOADS) + sorted(BATCH_WORKLOADS) + sorted(ADJOINT_WORKLOADS) +
+                    sorted(CURVATURE_WORKLOADS))
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.impl == "reference" and args.workload in CURVATURE_WORKLOADS:
+        run_curvature_reference_arm(args)
+    elif args.impl == "reference":
         run_reference_arm(args)
+    elif args.workload in CURVATURE_WORKLOADS:
+        run_curvature_arm(args)
     elif args.workload in BATCH_WORKLOADS:
         run_batch_arm(args)
     elif args.workload in ADJOINT_WORKLOADS:

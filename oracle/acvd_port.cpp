@@ -1079,13 +1079,15 @@ static double fit_curvature(const Mesh& m, const std::vector<idt>& fl, double in
     return std::sqrt(ev[0] * ev[0] + ev[1] * ev[1]);
 }
 
-// Per-vertex curvature indicator (nV) and principal directions (6 nV, float as the
-// reference stores them).
-void port_curvature(void* hp, double* indicator, float* principal_dirs) {
+// Per-vertex curvature indicator and principal directions (6 per vertex, float as
+// the reference stores them) of the vertices [v0, v1); outputs indexed by vertex.
+// The reference's vtkCurvatureMeasure deals the vertices to its threads the same way
+// (each vertex is independent, Common/vtkCurvatureMeasure.cxx:625-718).
+void port_curvature_range(void* hp, long long v0, long long v1, double* indicator, float* principal_dirs) {
     const Mesh& m = ((PortHandle*)hp)->eng->mesh;
     std::vector<char> ftag(m.nF, 0), vtag(m.nV, 0);
     std::vector<idt> faces, tf, tv;
-    for (idt v = 0; v < m.nV; v++) {
+    for (idt v = v0; v < v1; v++) {
         faces.clear(); tf.clear(); tv.clear();
         nring_faces(m, v, 3, faces, ftag, vtag, tf, tv);
         double info[6];
@@ -1094,6 +1096,10 @@ void port_curvature(void* hp, double* indicator, float* principal_dirs) {
         for (idt f : tf) ftag[f] = 0;
         for (idt u : tv) vtag[u] = 0;
     }
+}
+
+void port_curvature(void* hp, double* indicator, float* principal_dirs) {
+    port_curvature_range(hp, 0, ((PortHandle*)hp)->eng->mesh.nV, indicator, principal_dirs);
 }
 
 // ACVD's quadric post-placement (DiscreteRemeshing/Examples/ACVD.cxx:217-291): per

@@ -164,6 +164,17 @@ class _Base:
         self.f["post_placement"](self.h, int(level), out.ravel())
         return out
 
+    def curvature_range(self, v0: int, v1: int):
+        """curvature() for the vertices [v0, v1) only (full-size outputs, others zero)."""
+        ind = np.zeros(self.n, dtype=np.float64)
+        pd = np.zeros(6 * self.n, dtype=np.float32)
+        fn = self._lib.port_curvature_range
+        fn.restype = None
+        fn.argtypes = [_P, ctypes.c_longlong, ctypes.c_longlong, _pd,
+                       np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")]
+        fn(self.h, int(v0), int(v1), ind, pd)
+        return ind, pd.reshape(-1, 6)
+
     def curvature(self):
         """Per-vertex curvature indicator (nV) and principal directions (nV x 6, float32)
         of the mesh, vtkCurvatureMeasure's polynomial fitting on the vertex 3-ring."""
