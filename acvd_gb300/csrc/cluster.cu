@@ -341,7 +341,8 @@ ACVD_DEV void eval_tile(const DevState& st, int item0, int64_t count, int color,
             n_bnd = 1;
             const bool movable =
                 L >= st.k ||
-                (st.size[L] > 1 && (!fl.connexity || ring_connected_pref(st, st.row[i], st.row[i] + deg, L, lb)));
+                (st.size[L] > 1 && !(st.frozen && st.frozen[L]) &&
+                 (!fl.connexity || ring_connected_pref(st, st.row[i], st.row[i] + deg, L, lb)));
             if (movable) {
                 const int w = (int)atomicAdd(&s_nwork, 1u);
                 s_idx[w] = (int)idx;
@@ -350,7 +351,7 @@ ACVD_DEV void eval_tile(const DevState& st, int item0, int64_t count, int color,
 #pragma unroll
                 for (int q = 0; q < kRingPref; q++) {
                     const int B = lb[q];
-                    if (!all || B == L || B >= st.k) continue;
+                    if (!all || B == L || B >= st.k || (st.frozen && st.frozen[B])) continue;
                     bool dup = false;
 #pragma unroll
                     for (int r = 0; r < q; r++) dup |= lb[r] == B;
@@ -448,7 +449,7 @@ ACVD_DEV void eval_tile(const DevState& st, int item0, int64_t count, int color,
                 float bde = 0.0f, badd = 0.0f;
                 for (int p = p0; p < p1; p++) {
                     const int B = st.label[st.col[p]];
-                    if (B == L || B >= st.k) continue;
+                    if (B == L || B >= st.k || (st.frozen && st.frozen[B])) continue;
                     bool dup = false;
                     for (int q = p0; q < p; q++) dup |= (st.label[st.col[q]] == B);
                     if (dup) continue;

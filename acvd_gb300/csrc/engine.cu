@@ -1,6 +1,7 @@
 // Host orchestration of the GPU clustering (the MinimizeEnergy() seam) and the
 // C ABI declared in include/acvd_gpu.h.
 #include <algorithm>
+#include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <chrono>
@@ -127,6 +128,9 @@ struct acvd_ctx {
     int64_t sweep_kernels = 0;     // kernels in the sweep last enqueued
     int64_t exact_kernels = 0, relaxed_kernels = 0;
     DBuf<int> label_init;          // the assignment given to acvd_set_labels (for acvd_rewind)
+    DBuf<unsigned char> frozen;    // per cluster (K + 1): IsClusterFreezed; used when has_frozen
+    bool has_frozen = false;
+    std::vector<unsigned char> h_frozen;
 
     // set-up work buffers, kept between calls: a repeated set-up (same or smaller
     // mesh) allocates nothing, and so does not synchronise the device in cudaFree
@@ -184,6 +188,7 @@ struct acvd_ctx {
         st.bflag = bflag.p;
         st.orig = perm.p;
         st.inv = inv.p;
+        st.frozen = has_frozen ? frozen.p : nullptr;
         return st;
     }
     cudaGraphExec_t relaxed_exec = nullptr;
@@ -611,7 +616,8 @@ int acvd_set_labels(acvd_ctx* ctx, int32_t k, const int32_t* labels) {
     for (int64_t i = 0; i < ctx->nV; i++)
         if (labels[i] < 0 || labels[i] > k) return fail(ctx, ACVD_ERR_ARG, "label outside [0, K]");
     CK(cudaSetDevice(ctx->opts.device));
-    if (ctx->K != k) ctx->drop_graph();
+    if (ctx->K != k || ctx->has_frozen) ctx->drop_graph();
+    ctx->has_frozen = false;   // a new clustering starts with no frozen cluster
     ctx->K = k;
     const int ms = ctx->metric >= 0 ? ctx->metric : kAniso;
     CK(ctx->label.resize(ctx->nV));
@@ -633,6 +639,25 @@ int acvd_set_labels(acvd_ctx* ctx, int32_t k, const int32_t* labels) {
     CK(cudaMemcpyAsync(ctx->label_init.p, ctx->label.p, ctx->nV * sizeof(int), cudaMemcpyDeviceToDevice, ctx->s));
     CK(cudaStreamSynchronize(ctx->s));
     ctx->ready_labels = true;
+    return ACVD_OK;
+}
+
+int acvd_set_frozen_clusters(acvd_ctx* ctx, const uint8_t* frozen) {
+    if (!ctx) return ACVD_ERR_ARG;
+    if (!ctx->ready_labels) return fail(ctx, ACVD_ERR_ARG, "acvd_set_frozen_clusters before acvd_set_labels");
+    CK(cudaSetDevice(ctx->opts.device));
+    ctx->drop_graph();   // the captured sweeps hold the state's pointers
+    if (!frozen) {
+        ctx->has_frozen = false;
+        return ACVD_OK;
+    }
+    ctx->h_frozen.assign(frozen, frozen + ctx->K);
+    for (auto& f : ctx->h_frozen) f = f ? 1 : 0;
+    ctx->h_frozen.push_back(0);   // the null label K is never frozen
+    CK(ctx->frozen.resize(ctx->K + 1));
+    CK(cudaMemcpyAsync(ctx->frozen.p, ctx->h_frozen.data(), ctx->K + 1, cudaMemcpyHostToDevice, ctx->s));
+    CK(cudaStreamSynchronize(ctx->s));
+    ctx->has_frozen = true;
     return ACVD_OK;
 }
 
@@ -933,7 +958,19 @@ extern "C" int acvd_minimize(acvd_ctx* ctx, acvd_stats* stats) {
         if ((r = fill_holes(ctx, &unassigned))) { status = r; break; }
         if ((r = recompute(ctx))) { status = r; break; }
         // items of non-frozen clusters, the base of the early-convergence test (:733-736)
-        const int64_t early = ctx->nV - unassigned;
+        int64_t early = ctx->nV - unassigned;
+        if (ctx->has_frozen) {
+            std::vector<int> h_size(ctx->K);
+            if (cudaMemcpyAsync(h_size.data(), ctx->size.p, ctx->K * sizeof(int), cudaMemcpyDeviceToHost, ctx->s) !=
+                    cudaSuccess ||
+                cudaStreamSynchronize(ctx->s) != cudaSuccess) {
+                status = fail(ctx, ACVD_ERR_CUDA, "reading the cluster sizes failed");
+                break;
+            }
+            early = 0;
+            for (int c = 0; c < ctx->K; c++)
+                if (!ctx->h_frozen[c]) early += h_size[c];
+        }
         int convergences = 0;
         int sweeps = 0;
         // relaxed sweeps while the connectivity constraint is off; back to exact
@@ -1219,6 +1256,61 @@ extern "C" int acvd_compute_curvature(acvd_ctx* ctx, double* indicator, float* p
     if (h_over)
         return fail(ctx, ACVD_ERR_UNSUPPORTED,
                     std::to_string(h_over) + " vertices have a 3-ring larger than the curvature kernel's buffers");
+    return ACVD_OK;
+}
+
+// One level of midpoint subdivision (vtkSurface::Subdivide, Common/vtkSurface.cxx:605-677)
+// with the parent interpolation of the indicator (vtkDiscreteRemeshing.h:731-745).
+// Independent of the context's mesh: the context gives the device and the stream.
+extern "C" int acvd_subdivide(acvd_ctx* ctx, int64_t n_vertices, const double* xyz, int64_t n_faces,
+                              const int32_t* tri, const int32_t* csr_row, const int32_t* csr_col, int64_t n_edges,
+                              const int32_t* edge_v, const double* indicator, double* out_xyz, int32_t* out_tri,
+                              int32_t* parent1, int32_t* parent2, double* out_indicator) {
+    if (!ctx) return ACVD_ERR_ARG;
+    if (n_vertices < 0 || n_faces < 0 || n_edges < 0 || !xyz || !tri || !csr_row || !csr_col || !edge_v ||
+        !out_xyz || !out_tri || !parent1 || !parent2)
+        return fail(ctx, ACVD_ERR_ARG, "acvd_subdivide: null or negative argument");
+    if ((indicator == nullptr) != (out_indicator == nullptr))
+        return fail(ctx, ACVD_ERR_ARG, "acvd_subdivide: indicator and out_indicator go together");
+    if (n_vertices + n_edges > INT32_MAX || 4 * n_faces > INT32_MAX)
+        return fail(ctx, ACVD_ERR_UNSUPPORTED, "acvd_subdivide: the subdivided mesh exceeds 32-bit ids");
+    if (csr_row[n_vertices] != 2 * n_edges)
+        return fail(ctx, ACVD_ERR_ARG, "acvd_subdivide: ring CSR does not hold 2 n_edges slots");
+    // vtkSurface::Subdivide skips inactive faces (first two corners equal); this
+    // build keeps the 4 f .. 4 f + 3 numbering and rejects them instead
+    for (int64_t f = 0; f < n_faces; f++)
+        if (tri[3 * f] == tri[3 * f + 1])
+            return fail(ctx, ACVD_ERR_UNSUPPORTED, "acvd_subdivide: face " + std::to_string(f) + " is degenerate");
+    CK(cudaSetDevice(ctx->opts.device));
+    const int64_t nv = n_vertices, nf = n_faces, ne = n_edges, nout = n_vertices + n_edges;
+    DBuf<double> d_xyz, d_ind, d_oxyz, d_oind;
+    DBuf<int> d_tri, d_row, d_col, d_ev, d_slot, d_otri, d_p1, d_p2;
+    DBuf<unsigned int> d_missing;
+    CK(d_xyz.resize(3 * nv)); CK(d_tri.resize(3 * nf)); CK(d_row.resize(nv + 1)); CK(d_col.resize(2 * ne));
+    CK(d_ev.resize(2 * ne)); CK(d_slot.resize(2 * ne)); CK(d_oxyz.resize(3 * nout)); CK(d_otri.resize(12 * nf));
+    CK(d_p1.resize(ne)); CK(d_p2.resize(ne)); CK(d_missing.resize(1));
+    if (indicator) { CK(d_ind.resize(nv)); CK(d_oind.resize(nout)); }
+    CK(cudaMemcpyAsync(d_xyz.p, xyz, 3 * nv * sizeof(double), cudaMemcpyHostToDevice, ctx->s));
+    CK(cudaMemcpyAsync(d_tri.p, tri, 3 * nf * sizeof(int), cudaMemcpyHostToDevice, ctx->s));
+    CK(cudaMemcpyAsync(d_row.p, csr_row, (nv + 1) * sizeof(int), cudaMemcpyHostToDevice, ctx->s));
+    CK(cudaMemcpyAsync(d_col.p, csr_col, 2 * ne * sizeof(int), cudaMemcpyHostToDevice, ctx->s));
+    CK(cudaMemcpyAsync(d_ev.p, edge_v, 2 * ne * sizeof(int), cudaMemcpyHostToDevice, ctx->s));
+    if (indicator) CK(cudaMemcpyAsync(d_ind.p, indicator, nv * sizeof(double), cudaMemcpyHostToDevice, ctx->s));
+    CK(cudaMemsetAsync(d_missing.p, 0, sizeof(unsigned int), ctx->s));
+    CK(launch_subdivide(d_xyz.p, nv, d_tri.p, nf, d_row.p, d_col.p, d_ev.p, ne, d_ind.p, d_slot.p, d_oxyz.p,
+                        d_otri.p, d_p1.p, d_p2.p, d_oind.p, d_missing.p, ctx->s));
+    unsigned int missing = 0;
+    CK(cudaMemcpyAsync(&missing, d_missing.p, sizeof missing, cudaMemcpyDeviceToHost, ctx->s));
+    CK(cudaMemcpyAsync(out_xyz, d_oxyz.p, 3 * nout * sizeof(double), cudaMemcpyDeviceToHost, ctx->s));
+    CK(cudaMemcpyAsync(out_tri, d_otri.p, 12 * nf * sizeof(int), cudaMemcpyDeviceToHost, ctx->s));
+    CK(cudaMemcpyAsync(parent1, d_p1.p, ne * sizeof(int), cudaMemcpyDeviceToHost, ctx->s));
+    CK(cudaMemcpyAsync(parent2, d_p2.p, ne * sizeof(int), cudaMemcpyDeviceToHost, ctx->s));
+    if (indicator)
+        CK(cudaMemcpyAsync(out_indicator, d_oind.p, nout * sizeof(double), cudaMemcpyDeviceToHost, ctx->s));
+    CK(cudaStreamSynchronize(ctx->s));
+    if (missing)
+        return fail(ctx, ACVD_ERR_ARG, "acvd_subdivide: " + std::to_string(missing) +
+                                            " faces have an edge missing from the ring CSR");
     return ACVD_OK;
 }
 

@@ -129,6 +129,9 @@ struct DevState {
     // each item, and the item of each original vertex id
     const int* orig;
     const int* inv;
+    // per cluster: 1 = frozen (IsClusterFreezed, vtkUniformClustering.h:912-915): no
+    // item leaves it and none joins it, except unassigned items; null: none frozen
+    const unsigned char* frozen;
 };
 
 // Persistent sweep kernel: the loop that runs colour sweeps back to back on the
@@ -266,6 +269,14 @@ cudaError_t launch_curvature(const double* xyz, const int* tri, int64_t nv, int6
                              const int* row, const int* col, const int* perm, const int* inv, int2* poly,
                              int* slot_edge, void* face_work, double* indicator, float* dirs,
                              unsigned long long* overflow, cudaStream_t s);
+
+// ---- midpoint subdivision (subdivide.cu) ----
+// One level of vtkSurface::Subdivide over a mesh in the reference's numbering
+// (ring CSR and edge list of acvd_build_topology); ind / out_ind may be null.
+cudaError_t launch_subdivide(const double* xyz, int64_t nv, const int* tri, int64_t nf, const int* row,
+                             const int* col, const int* edge_v, int64_t ne, const double* ind, int* slot_edge,
+                             double* out_xyz, int* out_tri, int* parent1, int* parent2, double* out_ind,
+                             unsigned int* missing, cudaStream_t s);
 
 // ---- adjoint (adjoint.cu) ----
 // Work arrays and inputs of the fixed-clustering adjoint (FP64).

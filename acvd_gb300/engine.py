@@ -94,6 +94,8 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         "acvd_boundary_edges_noalloc": (ctypes.c_int, [_P, _i64, _P, _P, _P, _P]),
         "acvd_post_placement": (ctypes.c_int, [_P, ctypes.c_int, _P]),
         "acvd_compute_curvature": (ctypes.c_int, [_P, _P, _P]),
+        "acvd_set_frozen_clusters": (ctypes.c_int, [_P, _P]),
+        "acvd_subdivide": (ctypes.c_int, [_P, _i64, _P, _i64, _P, _P, _P, _i64, _P, _P, _P, _P, _P, _P, _P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -283,6 +285,44 @@ class Engine:
             raise ValueError("compute_curvature needs contiguous float64 (n) and float32 (n x 6) outputs")
         self._ck(self._lib.acvd_compute_curvature(self.ctx, _ptr(ind), _ptr(pd)), "acvd_compute_curvature")
         return ind, pd
+
+    def set_frozen_clusters(self, frozen: np.ndarray | None):
+        """IsClusterFreezed for the next minimize(): K flags (nonzero = frozen) or None."""
+        if frozen is None:
+            self._ck(self._lib.acvd_set_frozen_clusters(self.ctx, None), "acvd_set_frozen_clusters")
+            return
+        f = np.ascontiguousarray(frozen, dtype=np.uint8)
+        if f.size != self.k:
+            raise ValueError("set_frozen_clusters needs one flag per cluster")
+        self._frozen = f
+        self._ck(self._lib.acvd_set_frozen_clusters(self.ctx, _ptr(f)), "acvd_set_frozen_clusters")
+
+    def subdivide(self, points: np.ndarray, faces: np.ndarray, row: np.ndarray, col: np.ndarray,
+                  edge_v: np.ndarray, indicator: np.ndarray | None = None):
+        """One level of vtkSurface::Subdivide on the device (this context's device and
+        stream; its mesh is untouched).  Returns (points (nV+nE, 3) float64 holding
+        float values, faces (4 nF, 3) int32, parent1 (nE), parent2 (nE), indicator
+        (nV+nE) or None)."""
+        pts = np.ascontiguousarray(points, dtype=np.float64)
+        tri = np.ascontiguousarray(faces, dtype=np.int32)
+        row = np.ascontiguousarray(row, dtype=np.int32)
+        col = np.ascontiguousarray(col, dtype=np.int32)
+        ev = np.ascontiguousarray(edge_v, dtype=np.int32).reshape(-1)
+        nv, nf, ne = pts.shape[0], tri.shape[0], ev.size // 2
+        o_pts = np.empty((nv + ne, 3), dtype=np.float64)
+        o_tri = np.empty((4 * nf, 3), dtype=np.int32)
+        p1 = np.empty(ne, dtype=np.int32)
+        p2 = np.empty(ne, dtype=np.int32)
+        ind = o_ind = None
+        if indicator is not None:
+            ind = np.ascontiguousarray(indicator, dtype=np.float64)
+            if ind.size != nv:
+                raise ValueError("subdivide: the indicator needs one value per vertex")
+            o_ind = np.empty(nv + ne, dtype=np.float64)
+        self._ck(self._lib.acvd_subdivide(self.ctx, nv, _ptr(pts), nf, _ptr(tri), _ptr(row), _ptr(col), ne, _ptr(ev),
+                                          _ptr(ind) if ind is not None else None, _ptr(o_pts), _ptr(o_tri), _ptr(p1),
+                                          _ptr(p2), _ptr(o_ind) if o_ind is not None else None), "acvd_subdivide")
+        return o_pts, o_tri, p1, p2, o_ind
 
     def post_placement(self, level: int = 1) -> np.ndarray:
         """ACVD's quadric post-placement of the output vertices (ACVD.cxx:217-291): (K, 3)."""

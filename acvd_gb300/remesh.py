@@ -16,11 +16,16 @@ vtkAnisotropicDiscreteRemeshing.h:49-71), backed by the GPU engine:
     coarse = r.GetOutput()                       # Surface
     labels = r.GetClustering()
 
-Remesh() computes the curvature indicator / principal directions the metric needs
-on the GPU (vtkCurvatureMeasure's polynomial fitting, as the reference's
-SamplingPreProcessing does); SetCurvatureInfo supplies them instead.  Differences
-from the reference, by design: meshes that would need subdivision
-(N < threshold * K) are rejected; display options must stay 0.
+Remesh() first subdivides the input on the GPU while it has fewer than
+SubsamplingThreshold x K vertices (CheckSubsamplingRatio, vtkSurface::Subdivide);
+GetInput() is then the subdivided mesh and OriginalInput the given one.  It computes
+the curvature indicator / principal directions the metric needs on the GPU
+(vtkCurvatureMeasure's polynomial fitting on the original mesh, as the reference's
+SamplingPreProcessing does, the indicator interpolated to the subdivided vertices);
+SetCurvatureInfo supplies them instead.  Differences from the reference, by design:
+the quadric-anisotropic metric on a mesh that needs subdivision is rejected (the
+reference keeps the original mesh's principal-direction array and reads past its
+end); display options must stay 0.
 """
 from __future__ import annotations
 
@@ -80,6 +85,10 @@ class _DiscreteRemeshing:
     def __init__(self, device: int = 0):
         self._device = device
         self.Input = None
+        self.OriginalInput = None
+        self.NumberOfSubdivisionsBeforeClustering = 0
+        self.VerticesParent1 = None
+        self.VerticesParent2 = None
         self.NumberOfClusters = 0
         self.SubsamplingThreshold = 10
         self.UnconstrainedInitialization = 0
@@ -103,6 +112,8 @@ class _DiscreteRemeshing:
     # -- setters of the reference API --
     def SetInput(self, mesh: Surface):
         self.Input = mesh
+        self.OriginalInput = None
+        self.NumberOfSubdivisionsBeforeClustering = 0
 
     def GetInput(self) -> Surface:
         return self.Input
@@ -146,31 +157,78 @@ class _DiscreteRemeshing:
         g = self._metric.Gradation
         return g != 0.0 if self._metric_name == "aniso" else g > 0.0
 
+    def _check_subsampling_ratio(self, e, indicator):
+        """CheckSubsamplingRatio (vtkDiscreteRemeshing.h:841-875): subdivide on the GPU
+        while the mesh has fewer than SubsamplingThreshold x K vertices; the indicator
+        (of the original mesh, or None) is carried through each level by the parent
+        interpolation of vtkDiscreteRemeshing.h:731-745.  Returns the indicator of the
+        mesh that is clustered."""
+        mesh = self.Input
+        k = self.NumberOfClusters
+        levels = []
+        while mesh.GetNumberOfPoints() < self.SubsamplingThreshold * k:
+            if self._metric_name == "aniso":
+                raise _eng.AcvdError(5, "the quadric-anisotropic metric on a mesh that needs subdivision: the "
+                                        "reference does not interpolate the principal directions")
+            if mesh.GetNumberOfCells() == 0 or len(levels) >= 99:
+                raise _eng.AcvdError(1, "the mesh cannot be subdivided to SubsamplingThreshold x K vertices")
+            if self.ConsoleOutput:
+                print("Subdividing mesh")
+            row, col, ev = mesh.topology()
+            pts, tri, p1, p2, indicator = e.subdivide(mesh.points, mesh.faces, row, col, ev, indicator=indicator)
+            levels.append((mesh.GetNumberOfPoints(), p1, p2))
+            mesh = Surface(pts, tri)
+        if levels:
+            self.OriginalInput = self.Input
+            self.Input = mesh
+            self.NumberOfSubdivisionsBeforeClustering = len(levels)
+            # VerticesParent1/2, indexed by vertex id (-1 for the original vertices)
+            n = mesh.GetNumberOfPoints()
+            self.VerticesParent1 = np.full(n, -1, dtype=np.int32)
+            self.VerticesParent2 = np.full(n, -1, dtype=np.int32)
+            for n0, p1, p2 in levels:
+                self.VerticesParent1[n0:n0 + p1.size] = p1
+                self.VerticesParent2[n0:n0 + p2.size] = p2
+        return indicator
+
     def _prepare(self):
         if self.Input is None:
             raise _eng.AcvdError(1, "SetInput first")
         k = self.NumberOfClusters
         if k <= 0:
             raise _eng.AcvdError(1, "must set NumberOfClusters to more than zero")
-        n = self.Input.GetNumberOfPoints()
-        if n < self.SubsamplingThreshold * k:
-            raise _eng.AcvdError(5, f"{n} vertices < SubsamplingThreshold * K = {self.SubsamplingThreshold * k}: "
-                                    "the input would need subdivision, which this build does not do")
-        row, col, ev = self.Input.topology()
         if self._engine is None:
             self._engine = _eng.Engine(self._device, max_loops=self.MaxNumberOfLoops)
         e = self._engine
-        e.set_mesh(self.Input.points, self.Input.faces, row, col, ev)
-        # SamplingPreProcessing (vtkDiscreteRemeshing.h:583-700): the curvature the
-        # metric needs, computed here (on the GPU) unless SetCurvatureInfo gave it
+        # SamplingPreProcessing (vtkDiscreteRemeshing.h:583-753): the curvature the
+        # metric needs, computed here on the GPU on the original mesh unless
+        # SetCurvatureInfo gave it
         need_pd = self._metric_name == "aniso"
+        on_device = None
         if (self._needs_indicator() and self.Indicator is None) or (need_pd and self.PrincipalDirections is None):
+            src = self.OriginalInput if self.OriginalInput is not None else self.Input
+            row, col, ev = src.topology()
+            e.set_mesh(src.points, src.faces, row, col, ev)
+            on_device = src
             ind_c, pd_c = e.compute_curvature()
             if self.Indicator is None:
                 self.Indicator = ind_c
             if need_pd and self.PrincipalDirections is None:
                 self.PrincipalDirections = pd_c
+        if self.OriginalInput is None:
+            carry = self.Indicator if self._needs_indicator() else None
+            if carry is not None and carry.size != self.Input.GetNumberOfPoints():
+                raise _eng.AcvdError(1, "the curvature indicator needs one value per input vertex")
+            carry = self._check_subsampling_ratio(e, carry)
+            if carry is not None:
+                self.Indicator = carry
+        n = self.Input.GetNumberOfPoints()
         ind = self.Indicator if self._needs_indicator() else None
+        if ind is not None and ind.size != n:
+            raise _eng.AcvdError(1, "the curvature indicator needs one value per clustered vertex")
+        row, col, ev = self.Input.topology()
+        if on_device is not self.Input:
+            e.set_mesh(self.Input.points, self.Input.faces, row, col, ev)
         e.set_metric(self._metric_name, ind, self.PrincipalDirections, self._metric.Gradation)
         e.set_level(self._metric.QuadricsOptimizationLevel)
         e.set_unconstrained_initialization(self.UnconstrainedInitialization)

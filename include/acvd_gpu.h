@@ -154,8 +154,20 @@ int acvd_get_mesh_energies(acvd_ctx* ctx, double* energies);
 int acvd_set_quadrics_optimization_level(acvd_ctx* ctx, int level);
 int acvd_set_unconstrained_initialization(acvd_ctx* ctx, int on);
 
-/* SetNumberOfClusters + SetInitialClustering: K clusters, labels[nV] in [0, K]. */
+/* SetNumberOfClusters + SetInitialClustering: K clusters, labels[nV] in [0, K].
+ * Clears the frozen set below. */
 int acvd_set_labels(acvd_ctx* ctx, int32_t k, const int32_t* labels);
+
+/*
+ * IsClusterFreezed (Common/vtkUniformClustering.h:329, tested at :912-915 and
+ * :1049-1052): frozen[K] bytes, nonzero = frozen, or NULL for none.  The next
+ * acvd_minimize moves no item out of a frozen cluster and none into it (an
+ * unassigned item may still join one, as in the reference), and its early-
+ * convergence base counts the items of the other clusters only (:733-736).
+ * vtkDiscreteRemeshing's ForceManifold loop sets it before re-entering
+ * MinimizeEnergy.  Call after acvd_set_labels.
+ */
+int acvd_set_frozen_clusters(acvd_ctx* ctx, const uint8_t* frozen);
 
 /*
  * MinimizeEnergy(): hole filling, statistics, colour sweeps until the
@@ -215,6 +227,28 @@ int acvd_boundary_edges_noalloc(const int32_t* d_edge_v, int64_t n_edges, const 
  * ACVD_ERR_UNSUPPORTED.
  */
 int acvd_compute_curvature(acvd_ctx* ctx, double* indicator, float* principal_dirs);
+
+/*
+ * One level of midpoint subdivision, as vtkDiscreteRemeshing::CheckSubsamplingRatio
+ * applies it while the input has fewer than SubsamplingThreshold x K vertices
+ * (DiscreteRemeshing/vtkDiscreteRemeshing.h:841-875 -> vtkSurface::Subdivide,
+ * Common/vtkSurface.cxx:605-677), with the parent interpolation of the vertex
+ * indicator that the pre-processing applies afterwards (vtkDiscreteRemeshing.h:731-745).
+ * Input: a mesh with its ring CSR and edge list from acvd_build_topology.
+ * Outputs (host): out_xyz[3 (nV + nE)] -- the old points, then the midpoint of edge e
+ * as vertex nV + e, each rounded to float as the reference's float vtkPoints stores
+ * them; out_tri[12 nF] -- face f becomes faces 4f..4f+3 = (V1,V4,V6), (V4,V2,V5),
+ * (V5,V3,V6), (V4,V5,V6), V4/V5/V6 the children of edges V1V2/V2V3/V3V1;
+ * parent1/parent2[nE] -- the endpoints of edge e (VerticesParent1/2 of vertex nV + e);
+ * out_indicator[nV + nE] -- indicator copied, then (ind[p1] + ind[p2]) * 0.5 (both
+ * indicator and out_indicator NULL to skip).  The context gives the device and stream
+ * only; its mesh is untouched.  A degenerate face (first two corners equal, which
+ * vtkSurface treats as inactive) returns ACVD_ERR_UNSUPPORTED.
+ */
+int acvd_subdivide(acvd_ctx* ctx, int64_t n_vertices, const double* xyz, int64_t n_faces, const int32_t* tri,
+                   const int32_t* csr_row, const int32_t* csr_col, int64_t n_edges, const int32_t* edge_v,
+                   const double* indicator, double* out_xyz, int32_t* out_tri, int32_t* parent1, int32_t* parent2,
+                   double* out_indicator);
 
 /*
  * ACVD's quadric post-placement of the output vertices

@@ -1098,6 +1098,62 @@ void port_curvature_range(void* hp, long long v0, long long v1, double* indicato
     }
 }
 
+// vtkSurface::Subdivide (Common/vtkSurface.cxx:605-677): the old points, then one
+// midpoint per active edge in edge order (stored in a float vtkPoints, hence the
+// rounding), then four faces per active face; VerticesParent1/2 of the new vertex
+// nV + e are the edge's endpoints.  With an indicator, the parent interpolation of
+// vtkDiscreteRemeshing::SamplingPreProcessing (vtkDiscreteRemeshing.h:731-745):
+// old values copied, new (ind[p1] + ind[p2]) * 0.5.  Returns the number of output
+// faces; out_pts: 3 (nV + nE), out_tri: 12 nF, p1/p2: nE, ind_out: nV + nE.
+long long port_subdivide(long long nv, const double* pts, long long nf, const int* tri, double* out_pts,
+                         int* out_tri, int* p1, int* p2, const double* ind, double* ind_out) {
+    Mesh m;
+    m.build(nv, pts, nf, tri);
+    const idt ne = m.n_edges();
+    std::vector<idt> child(ne, -1);
+    idt nout = 0;
+    auto add_vertex = [&](const double* P) {
+        for (int c = 0; c < 3; c++) out_pts[3 * nout + c] = (double)(float)P[c];
+        return nout++;
+    };
+    for (idt i = 0; i < nv; i++) {
+        double P[3];
+        m.point(i, P);
+        add_vertex(P);
+        if (ind) ind_out[i] = ind[i];
+    }
+    for (idt e = 0; e < ne; e++) {
+        const idt v1 = m.ev1[e], v2 = m.ev2[e];
+        double P1[3], P2[3], P[3];
+        m.point(v1, P1);
+        m.point(v2, P2);
+        P[0] = 0.5 * (P1[0] + P2[0]);
+        P[1] = 0.5 * (P1[1] + P2[1]);
+        P[2] = 0.5 * (P1[2] + P2[2]);
+        const idt v3 = add_vertex(P);
+        child[e] = v3;
+        p1[e] = (int)v1;
+        p2[e] = (int)v2;
+    }
+    // the reference interpolates in increasing vertex id; a new vertex's parents are
+    // old vertices of this level
+    if (ind)
+        for (idt i = nv; i < nv + ne; i++)
+            ind_out[i] = (ind_out[p1[i - nv]] + ind_out[p2[i - nv]]) * 0.5;
+    long long of = 0;
+    for (idt f = 0; f < nf; f++) {
+        const idt V1 = m.F[3 * f], V2 = m.F[3 * f + 1], V3 = m.F[3 * f + 2];
+        if (V1 == V2) continue;  // inactive face
+        const int V4 = (int)child[m.is_edge(V1, V2)];
+        const int V5 = (int)child[m.is_edge(V2, V3)];
+        const int V6 = (int)child[m.is_edge(V3, V1)];
+        const int t[12] = {(int)V1, V4, V6, V4, (int)V2, V5, V5, (int)V3, V6, V4, V5, V6};
+        for (int j = 0; j < 12; j++) out_tri[12 * of + j] = t[j];
+        of++;
+    }
+    return 4 * of;
+}
+
 void port_curvature(void* hp, double* indicator, float* principal_dirs) {
     port_curvature_range(hp, 0, ((PortHandle*)hp)->eng->mesh.nV, indicator, principal_dirs);
 }

@@ -263,3 +263,30 @@ class Ref(_Base):
 
     def loops(self) -> int:
         return int(self._lib.ref_loops(self.h))
+
+
+def subdivide(points: np.ndarray, faces: np.ndarray, indicator: np.ndarray | None = None):
+    """vtkSurface::Subdivide restated (acvd_port.cpp ``port_subdivide``), with the
+    parent interpolation of the indicator.  Returns (points (nV+nE, 3), faces (4 nF', 3),
+    parent1 (nE), parent2 (nE), indicator (nV+nE) or None)."""
+    Port._load()
+    lib = Port._lib
+    fn = lib.port_subdivide
+    fn.restype = ctypes.c_longlong
+    fn.argtypes = [ctypes.c_longlong, _pd, ctypes.c_longlong, _pi, _pd, _pi, _pi, _pi, ctypes.c_void_p,
+                   ctypes.c_void_p]
+    pts = np.ascontiguousarray(points, dtype=np.float64)
+    tri = np.ascontiguousarray(faces, dtype=np.int32)
+    nv, nf = pts.shape[0], tri.shape[0]
+    ne = int(Port("iso", pts, tri, 1).topology()[0].shape[0])
+    o_pts = np.empty(3 * (nv + ne))
+    o_tri = np.empty(12 * max(nf, 1), dtype=np.int32)
+    p1 = np.empty(max(ne, 1), dtype=np.int32)
+    p2 = np.empty(max(ne, 1), dtype=np.int32)
+    ind = o_ind = None
+    if indicator is not None:
+        ind = np.ascontiguousarray(indicator, dtype=np.float64)
+        o_ind = np.empty(nv + ne)
+    nt = int(fn(nv, pts.reshape(-1), nf, tri.reshape(-1), o_pts, o_tri, p1, p2,
+                None if ind is None else ind.ctypes.data, None if o_ind is None else o_ind.ctypes.data))
+    return o_pts.reshape(-1, 3), o_tri[:3 * nt].reshape(-1, 3), p1[:ne], p2[:ne], o_ind

@@ -185,10 +185,10 @@ def test_error_paths():
     e.set_metric("iso")
     with pytest.raises(acvd_gb300.AcvdError):
         e.set_labels(10, np.full(m.n_points, 11, dtype=np.int32))  # label > K
-    r = acvd_gb300.IsotropicDiscreteRemeshing()
+    r = acvd_gb300.AnisotropicDiscreteRemeshing()
     r.SetInput(acvd_gb300.Surface(m.points, m.faces))
-    r.SetNumberOfClusters(500)                 # 642 < 10 * 500: would need subdivision
-    with pytest.raises(acvd_gb300.AcvdError):
+    r.SetNumberOfClusters(500)                 # 642 < 10 * 500: needs subdivision, which the
+    with pytest.raises(acvd_gb300.AcvdError):  # reference's aniso path cannot take
         r.Remesh()
     e.close()
 
@@ -301,3 +301,81 @@ def test_curvature_matches_oracle(oracle_lib, mk):
     np.testing.assert_array_equal(ind, ref_ind)
     np.testing.assert_array_equal(pd, ref_pd)
     e.close()
+
+
+def test_remesh_computes_curvature_like_the_reference(oracle_lib):
+    """Remesh() without SetCurvatureInfo computes the curvature on the GPU (the
+    reference's SamplingPreProcessing); it is bit-identical to the reference's, so the
+    remesh equals one fed with the oracle's curvature."""
+    m = synth.torus(96, 48, seed=6)
+    ind, pd = oracle_lib.Port("qem", m.points, m.faces, 10, 0.0).curvature()
+    outs = []
+    for given in (True, False):
+        r = acvd_gb300.QIsotropicDiscreteRemeshing()
+        r.SetInput(acvd_gb300.Surface(m.points, m.faces))
+        r.SetNumberOfClusters(300)
+        r.GetMetric().SetGradation(1.5)
+        r.SetUnconstrainedInitialization(1)
+        if given:
+            r.SetCurvatureInfo(ind)
+        r.Remesh()
+        outs.append(r.GetClustering())
+    np.testing.assert_array_equal(outs[0], outs[1])
+
+
+@pytest.mark.parametrize("mk", [lambda: synth.torus(40, 20, seed=3), lambda: synth.icosphere(3, seed=1),
+                                lambda: synth.heightfield(24, seed=5), synth.tetrahedron],
+                         ids=["torus", "icosphere", "heightfield", "tetrahedron"])
+def test_subdivision_matches_oracle(oracle_lib, mk):
+    """vtkSurface::Subdivide on the GPU: points (float-rounded midpoints), faces, parents
+    and the interpolated indicator bit-exact against the restatement, two levels."""
+    m = mk()
+    e = acvd_gb300.Engine()
+    pts, tri = m.points, m.faces
+    ind = np.linspace(0.5, 2.0, m.n_points) ** 1.7
+    for _ in range(2):
+        row, col, ev = acvd_gb300.build_topology(pts.shape[0], tri)
+        g = e.subdivide(pts, tri, row, col, ev, indicator=ind)
+        o = oracle_lib.subdivide(pts, tri, ind)
+        for a, b in zip(g, o):
+            np.testing.assert_array_equal(a, b)
+        pts, tri, ind = g[0], g[1], g[4]
+    e.close()
+
+
+def test_remesh_subdivides_like_the_reference(oracle_lib):
+    """Remesh() on a mesh with fewer than SubsamplingThreshold x K vertices: two levels
+    of subdivision (CheckSubsamplingRatio), the curvature of the original mesh
+    interpolated to the new vertices, and a clustering of the subdivided mesh as good as
+    the reference arithmetic's own run on it."""
+    m = synth.icosphere(2, seed=3)                  # 162 vertices; 10 x 100 needs 2 levels
+    k, grad = 100, 1.0
+    r = acvd_gb300.QIsotropicDiscreteRemeshing()
+    r.SetInput(acvd_gb300.Surface(m.points, m.faces))
+    r.SetNumberOfClusters(k)
+    r.GetMetric().SetGradation(grad)
+    r.Remesh()
+    assert r.NumberOfSubdivisionsBeforeClustering == 2
+    assert r.OriginalInput.GetNumberOfPoints() == m.n_points
+    # the mesh and indicator the reference would cluster
+    ind0, _ = oracle_lib.Port("qem", m.points, m.faces, 10, 0.0).curvature()
+    pts, tri, ind = m.points, m.faces, ind0
+    for _ in range(2):
+        pts, tri, _, _, ind = oracle_lib.subdivide(pts, tri, ind)
+    sub = r.GetInput()
+    np.testing.assert_array_equal(sub.points, pts)
+    np.testing.assert_array_equal(sub.faces, tri)
+    np.testing.assert_array_equal(r.Indicator, ind)
+    assert sub.GetNumberOfPoints() >= 10 * k
+    lab = r.GetClustering()
+    assert lab.shape == (pts.shape[0],) and lab.max() < k
+    ev = oracle_lib.Port("qem", pts, tri, k, grad, ind)
+    ev.evaluate(lab, 1)
+    e_gpu = ev.global_energy()
+    assert ev.clean() == 0 and np.all(ev.clusters()["size"] > 0)
+    ref = oracle_lib.Port("qem", pts, tri, k, grad, ind)
+    ref.init(None)
+    ref.run()
+    e_ref = ref.global_energy()
+    assert e_gpu <= e_ref + 0.02 * abs(e_ref), (e_gpu, e_ref)
+    assert r.GetOutput().GetNumberOfPoints() == k
