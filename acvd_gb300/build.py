@@ -18,11 +18,12 @@ SRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libacvd_gb300.so")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
-CU_SOURCES = ["primitives.cu", "topology.cu", "cluster.cu", "adjoint.cu", "engine.cu", "noalloc.cu", "curvature.cu", "subdivide.cu"]
+CU_SOURCES = ["primitives.cu", "topology.cu", "cluster.cu", "adjoint.cu", "engine.cu", "noalloc.cu", "curvature.cu", "subdivide.cu",
+              "manifold.cu"]
 # per-file flags: the curvature kernel keeps every FP64 product and sum separately
 # rounded, so that it reproduces the CPU restatement bit for bit
 CU_FILE_FLAGS = {"curvature.cu": ["-fmad=false"]}
-CXX_SOURCES = ["host.cpp"]
+CXX_SOURCES = ["host.cpp", "io.cpp"]
 
 
 def _nvcc() -> str:

@@ -1,0 +1,121 @@
+"""Command-line drivers with the reference programs' arguments, on the GPU engine.
+
+    python -m acvd_gb300.acvd  file nvertices gradation [options]   # DiscreteRemeshing/Examples/ACVD.cxx
+    python -m acvd_gb300.acvdq file nvertices gradation [options]   # DiscreteRemeshing/Examples/ACVDQ.cxx
+
+Options are "-key value" pairs as in the reference:
+
+    -b 0/1    boundary fixing (default 0)
+    -m 0/1    manifold output (ForceManifold, default 0)
+    -s t      subsampling threshold (default 10)
+    -o dir    output directory
+    -of name  output file name (default simplification.ply)
+    -q n      ACVD: eigenvalues of the quadric post-placement (default 1, 0 = none);
+              ACVDQ: the QEM metric's QuadricsOptimizationLevel (default 3)
+    -d 0      display (only 0: there is no graphics stack)
+    -np n     threads of the reference's threaded engine (accepted, unused)
+
+Options of the reference that need parts this package does not build -- -l (long-edge
+splitting), -w (energy log), -cd/-cmin/-cmax/-cf (custom density image), -p (pooling),
+-fv/-ft (fixed vertices) -- stop with an error rather than being ignored.
+
+Outputs follow the reference: ACVD writes <dir>smooth_<name> before the post-placement
+and <dir>/<name> after it, in the format the name's extension selects; ACVDQ writes
+<dir><name> as binary PLY whatever the extension.
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+from . import engine as _eng
+from .remesh import (IsotropicDiscreteRemeshing, QIsotropicDiscreteRemeshing, QuadricPostPlacement, Surface)
+
+_UNBUILT = {
+    "-l": "long-edge splitting (vtkSurface::SplitLongEdges)",
+    "-w": "the global energy log",
+    "-cd": "custom density images",
+    "-cmin": "custom density images",
+    "-cmax": "custom density images",
+    "-cf": "custom density images",
+    "-p": "pooling (the threaded engine)",
+    "-fv": "fixed vertices",
+    "-ft": "fixed vertices",
+}
+
+
+def _usage(prog: str) -> str:
+    return (f"Usage : {prog} file nvertices gradation [options]\n"
+            "nvertices is the desired number of vertices\n"
+            "gradation defines the influence of local curvature (0=uniform meshing)\n"
+            "options: -b 0/1, -m 0/1, -s threshold, -o directory, -of file, -q level, -d 0")
+
+
+def _parse(argv: list[str], prog: str):
+    if len(argv) < 3:
+        raise SystemExit(_usage(prog))
+    opts = {"file": argv[0], "n": int(argv[1]), "gradation": float(argv[2])}
+    rest = argv[3:]
+    if len(rest) % 2:
+        raise SystemExit(f"{prog}: option {rest[-1]} without a value")
+    for key, value in zip(rest[0::2], rest[1::2]):
+        if key in _UNBUILT:
+            raise SystemExit(f"{prog}: option {key} needs {_UNBUILT[key]}, which this build does not have")
+        if key == "-d" and int(value) != 0:
+            raise SystemExit(f"{prog}: display needs a graphics stack; only -d 0 is available")
+        opts[key] = value
+    return opts
+
+
+def _remesh(opts, cls, console: int):
+    mesh = Surface.CreateFromFile(opts["file"])
+    mesh.DisplayMeshProperties()
+    r = cls()
+    r.SetForceManifold(int(opts.get("-m", 0)))
+    r.SetBoundaryFixing(int(opts.get("-b", 0)))
+    r.SetInput(mesh)
+    r.SetNumberOfClusters(opts["n"])
+    r.SetConsoleOutput(console)
+    r.SetSubsamplingThreshold(int(opts.get("-s", 10)))
+    r.GetMetric().SetGradation(opts["gradation"])
+    return r
+
+
+def main_acvd(argv: list[str] | None = None) -> int:
+    """ACVD (DiscreteRemeshing/Examples/ACVD.cxx): isotropic metric, then the quadric
+    post-placement of the output vertices with -q eigenvalues."""
+    argv = sys.argv[1:] if argv is None else argv
+    opts = _parse(argv, "ACVD")
+    level = int(opts.get("-q", 1))
+    outdir = opts.get("-o")
+    outfile = opts.get("-of", "simplification.ply")
+    r = _remesh(opts, IsotropicDiscreteRemeshing, 2)
+    r.Remesh()
+    if level != 0:
+        r.GetOutput().WriteToFile((outdir or "") + "smooth_" + outfile)
+        QuadricPostPlacement(r, level)
+        print("After Quadrics Post-processing : ")
+        r.GetOutput().DisplayMeshProperties()
+    r.GetOutput().WriteToFile((outdir + "/" if outdir else "") + outfile)
+    return 0
+
+
+def main_acvdq(argv: list[str] | None = None) -> int:
+    """ACVDQ (DiscreteRemeshing/Examples/ACVDQ.cxx): QEM metric with the unconstrained
+    first phase; the output is written as binary PLY."""
+    argv = sys.argv[1:] if argv is None else argv
+    opts = _parse(argv, "ACVDQ")
+    r = _remesh(opts, QIsotropicDiscreteRemeshing, 2)
+    if "-q" in opts:
+        r.GetMetric().SetQuadricsOptimizationLevel(int(opts["-q"]))
+    r.SetUnconstrainedInitialization(1)
+    r.Remesh()
+    out = r.GetOutput()
+    path = (opts.get("-o") or "") + opts.get("-of", "simplification.ply")
+    # the reference writes with vtkPLYWriter whatever the name says
+    tmp = path if ".ply" in path.lower() and ".vtk" not in path.lower() else \
+        os.path.join(os.path.dirname(path) or ".", f".acvdq_{os.getpid()}.ply")
+    _eng.write_mesh(tmp, out.points, out.faces)
+    if tmp != path:
+        os.replace(tmp, path)
+    return 0

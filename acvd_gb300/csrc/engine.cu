@@ -661,6 +661,13 @@ int acvd_set_frozen_clusters(acvd_ctx* ctx, const uint8_t* frozen) {
     return ACVD_OK;
 }
 
+int acvd_get_frozen_clusters(acvd_ctx* ctx, uint8_t* frozen) {
+    if (!ctx || !frozen) return ACVD_ERR_ARG;
+    if (!ctx->ready_labels) return fail(ctx, ACVD_ERR_ARG, "acvd_get_frozen_clusters before acvd_set_labels");
+    for (int c = 0; c < ctx->K; c++) frozen[c] = ctx->has_frozen ? ctx->h_frozen[c] : 0;
+    return ACVD_OK;
+}
+
 int acvd_rewind(acvd_ctx* ctx) {
     if (!ctx) return ACVD_ERR_ARG;
     if (!ctx->ready_labels) return fail(ctx, ACVD_ERR_ARG, "acvd_rewind before acvd_set_labels");
@@ -1355,13 +1362,11 @@ extern "C" int acvd_post_placement(acvd_ctx* ctx, int level, double* points) {
     return ACVD_OK;
 }
 
-extern "C" int acvd_get_dual_mesh(acvd_ctx* ctx, int32_t* tris, int64_t* n_tris) {
-    if (!ctx || !n_tris) return ACVD_ERR_ARG;
-    if (!ctx->ready_labels) return fail(ctx, ACVD_ERR_ARG, "no labels");
-    CK(cudaSetDevice(ctx->opts.device));
+// The dual mesh's triangles on the device (cluster ids), *n_tris of them in `out`.
+static int build_dual(acvd_ctx* ctx, DBuf<int>& out, int64_t* n_tris) {
     const int64_t nf = ctx->nF;
     DBuf<uint32_t> flags, pos, klo, khi, order, t1, t2, keep, kpos;
-    DBuf<int> faces, sel, out;
+    DBuf<int> faces, sel;
     CK(flags.resize(nf + 1));
     CK(pos.resize(nf + 1));
     CK(ctx->dtmp.resize(2));
@@ -1399,11 +1404,275 @@ extern "C" int acvd_get_dual_mesh(acvd_ctx* ctx, int32_t* tris, int64_t* n_tris)
     CK(cudaMemcpyAsync(&t, total, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->s));
     CK(cudaStreamSynchronize(ctx->s));
     *n_tris = t;
-    if (tris && t) {
+    if (t) {
         CK(sel.resize(t));
         CK(out.resize(3 * (size_t)t));
         CK(launch_compact(keep.p, kpos.p, m, sel.p, ctx->s));
         CK(launch_dual_write(ctx->tri_int.p, faces.p, sel.p, t, ctx->label.p, out.p, ctx->s));
+    }
+    return ACVD_OK;
+}
+
+// One pass of vtkDiscreteRemeshing::DetectNonManifoldOutputVertices
+// (DiscreteRemeshing/vtkDiscreteRemeshing.h:165-383) on the current clustering.
+// The device finds the clusters whose output vertex is not manifold and which hold
+// no non-manifold input vertex, and their output-mesh neighbours; the host then
+// adds the new clusters in the reference's order (an item is taken from the cluster,
+// or from a neighbour's cluster when it has a single item) and freezes every other
+// cluster.  The next acvd_minimize is the reference's re-entry into MinimizeEnergy.
+extern "C" int acvd_force_manifold_step(acvd_ctx* ctx, int32_t* n_issues, int32_t* n_clusters) {
+    if (!ctx || !n_issues || !n_clusters) return ACVD_ERR_ARG;
+    if (!ctx->ready_metric || !ctx->ready_labels)
+        return fail(ctx, ACVD_ERR_ARG, "acvd_force_manifold_step needs a metric and a clustering");
+    CK(cudaSetDevice(ctx->opts.device));
+    *n_issues = 0;
+    *n_clusters = ctx->K;
+    int r = recompute(ctx);   // current cluster sizes
+    if (r) return r;
+    DBuf<int> dt;
+    int64_t t = 0;
+    if ((r = build_dual(ctx, dt, &t))) return r;
+    const int K = ctx->K;
+    const int64_t nv = ctx->nV, ne = ctx->nE;
+    DBuf<unsigned> cnt, off, cursor;
+    DBuf<int> list;
+    DBuf<unsigned char> bad, has_nm, issue, unf;
+    CK(cnt.resize(K + 1)); CK(off.resize(K + 1)); CK(cursor.resize(K + 1)); CK(list.resize(3 * (size_t)t));
+    CK(bad.resize(K)); CK(has_nm.resize(K)); CK(issue.resize(K)); CK(unf.resize(K));
+    CK(cudaMemsetAsync(cnt.p, 0, (K + 1) * sizeof(unsigned), ctx->s));
+    CK(cudaMemsetAsync(cursor.p, 0, (K + 1) * sizeof(unsigned), ctx->s));
+    CK(cudaMemsetAsync(has_nm.p, 0, K, ctx->s));
+    CK(cudaMemsetAsync(unf.p, 0, K, ctx->s));
+    CK(launch_dual_incidence(dt.p, t, cnt.p, nullptr, nullptr, nullptr, false, ctx->s));
+    CK(exclusive_scan_u32(cnt.p, off.p, K + 1, nullptr, ctx->scratch, ctx->s));
+    CK(launch_dual_incidence(dt.p, t, nullptr, off.p, cursor.p, list.p, true, ctx->s));
+    CK(launch_manifold_checks(dt.p, off.p, list.p, K, ctx->edge_int.p, ne, ctx->label.p, nv, ctx->perm.p,
+                              ctx->vf_row.p, ctx->vf_face.p, ctx->tri.p, ctx->row.p, ctx->size.p, bad.p, has_nm.p,
+                              issue.p, unf.p, ctx->s));
+    std::vector<unsigned char> h_issue(K), h_unf(K);
+    std::vector<int> h_size(K);
+    CK(cudaMemcpyAsync(h_issue.data(), issue.p, K, cudaMemcpyDeviceToHost, ctx->s));
+    CK(cudaMemcpyAsync(h_unf.data(), unf.p, K, cudaMemcpyDeviceToHost, ctx->s));
+    CK(cudaMemcpyAsync(h_size.data(), ctx->size.p, K * sizeof(int), cudaMemcpyDeviceToHost, ctx->s));
+    CK(cudaStreamSynchronize(ctx->s));
+    int issues = 0;
+    for (int c = 0; c < K; c++) issues += h_issue[c];
+    if (issues == 0) return ACVD_OK;
+
+    // the clustering in vertex ids
+    std::vector<int> lab(nv);
+    CK(ctx->label_orig.resize(nv));
+    CK(launch_gather_i32(ctx->label.p, ctx->inv.p, nv, ctx->label_orig.p, ctx->s));
+    CK(cudaMemcpyAsync(lab.data(), ctx->label_orig.p, nv * sizeof(int), cudaMemcpyDeviceToHost, ctx->s));
+    CK(cudaStreamSynchronize(ctx->s));
+    // ClusterItems of the clusters with issues, in increasing item id (:175-200)
+    std::vector<std::vector<int>> items(K);
+    for (int64_t i = 0; i < nv; i++) {
+        const int c = lab[i];
+        if (c >= 0 && c < K && h_issue[c]) items[c].push_back((int)i);
+    }
+    // IsClusterFreezed: all but the clusters with issues and their neighbours (:171-174, :236-240)
+    std::vector<unsigned char> frozen(K, 1);
+    for (int c = 0; c < K; c++)
+        if (h_issue[c] || h_unf[c]) frozen[c] = 0;
+    std::vector<int> sz(h_size.begin(), h_size.end());
+    // vtkIdList::DeleteId: the list's last id takes the freed slot
+    auto drop = [&](int c, int item) {
+        sz[c]--;
+        if (c < K && h_issue[c]) {
+            std::vector<int>& v = items[c];
+            auto at = std::find(v.begin(), v.end(), item);
+            *at = v.back();
+            v.pop_back();
+        }
+    };
+    int k_now = K;
+    for (int c = 0; c < K; c++) {
+        if (!h_issue[c]) continue;
+        const int nc = k_now++;          // the new cluster, unfrozen (:257-269)
+        frozen.push_back(0);
+        sz.push_back(0);
+        if (items[c].size() > 1) {
+            const int it = items[c][0];
+            lab[it] = nc;
+            drop(c, it);
+            sz[nc] = 1;
+            continue;
+        }
+        // a single item: take the first neighbour item whose cluster has more than one (:285-304)
+        const int it = items[c][0];
+        int j = 0, rr[2] = {0, 0};
+        CK(cudaMemcpy(&j, ctx->inv.p + it, sizeof(int), cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(rr, ctx->row.p + j, 2 * sizeof(int), cudaMemcpyDeviceToHost));
+        std::vector<int> ring(rr[1] - rr[0]);
+        if (!ring.empty()) {
+            CK(cudaMemcpy(ring.data(), ctx->col.p + rr[0], ring.size() * sizeof(int), cudaMemcpyDeviceToHost));
+            for (int& q : ring) CK(cudaMemcpy(&q, ctx->perm.p + q, sizeof(int), cudaMemcpyDeviceToHost));
+        }
+        bool found = false;
+        for (int nb : ring) {
+            // a cluster added in this pass holds one item; labels >= K are unassigned
+            // items, which the reference never meets here (MinimizeEnergy fills holes)
+            const int ncl = lab[nb];
+            if (ncl < 0 || ncl >= K) continue;
+            if (sz[ncl] > 1) {
+                lab[nb] = nc;
+                drop(ncl, nb);
+                sz[nc] = 1;
+                found = true;
+                break;
+            }
+        }
+        if (!found) {                    // no freeable neighbour: the new cluster is cancelled (:336-347)
+            k_now--;
+            frozen.pop_back();
+            sz.pop_back();
+        }
+    }
+    // the reference's metric stays in its constrained state after the first run
+    ctx->unconstrained = 0;
+    if ((r = acvd_set_labels(ctx, k_now, lab.data()))) return r;
+    if ((r = acvd_set_frozen_clusters(ctx, frozen.data()))) return r;
+    *n_issues = issues;
+    *n_clusters = k_now;
+    return ACVD_OK;
+}
+
+// vtkDiscreteRemeshing::FixMeshBoundaries (DiscreteRemeshing/vtkDiscreteRemeshing.h:426-579)
+// for the current clustering.  The device lists the input boundary edges (one face)
+// with their endpoints, clusters, valences and points; the host replays the three
+// passes over that list in the reference's order.  New output vertices are numbered
+// from K; their coordinates are float-rounded as the output's float vtkPoints stores
+// them.  Call with NULL buffers to get the counts.
+extern "C" int acvd_fix_mesh_boundaries(acvd_ctx* ctx, double* new_points, int64_t* n_new_points, int32_t* new_faces,
+                                        int64_t* n_new_faces) {
+    if (!ctx || !n_new_points || !n_new_faces) return ACVD_ERR_ARG;
+    if (!ctx->ready_labels) return fail(ctx, ACVD_ERR_ARG, "acvd_fix_mesh_boundaries needs a clustering");
+    CK(cudaSetDevice(ctx->opts.device));
+    const int64_t nv = ctx->nV, ne = ctx->nE;
+    const int K = ctx->K;
+    DBuf<uint32_t> flag, pos;
+    DBuf<int> ids;
+    DBuf<BoundaryEdge> bedges;
+    CK(flag.resize(ne + 1));
+    CK(pos.resize(ne + 1));
+    CK(ctx->dtmp.resize(2));
+    uint32_t* total = (uint32_t*)ctx->dtmp.p;
+    CK(launch_boundary_edge_flags(ctx->edge_v.p, ne, ctx->vf_row.p, ctx->vf_face.p, ctx->tri.p, flag.p, ctx->s));
+    CK(exclusive_scan_u32(flag.p, pos.p, ne, total, ctx->scratch, ctx->s));
+    uint32_t nb = 0;
+    CK(cudaMemcpyAsync(&nb, total, sizeof nb, cudaMemcpyDeviceToHost, ctx->s));
+    CK(cudaStreamSynchronize(ctx->s));
+    std::vector<BoundaryEdge> be(nb);
+    if (nb) {
+        CK(ids.resize(nb));
+        CK(bedges.resize(nb));
+        CK(launch_compact(flag.p, pos.p, ne, ids.p, ctx->s));
+        CK(ctx->label_orig.resize(nv));
+        CK(launch_gather_i32(ctx->label.p, ctx->inv.p, nv, ctx->label_orig.p, ctx->s));
+        CK(launch_boundary_gather(ids.p, nb, ctx->edge_v.p, ctx->label_orig.p, ctx->inv.p, ctx->row.p, ctx->xyz.p,
+                                  bedges.p, ctx->s));
+        CK(cudaMemcpyAsync(be.data(), bedges.p, nb * sizeof(BoundaryEdge), cudaMemcpyDeviceToHost, ctx->s));
+        CK(cudaStreamSynchronize(ctx->s));
+    }
+    // per vertex, its boundary edges (list positions) in ring order = increasing edge id
+    std::vector<std::pair<int, int>> vb;   // (vertex, position)
+    vb.reserve(2 * (size_t)nb);
+    for (uint32_t b = 0; b < nb; b++) {
+        vb.push_back({be[b].v[0], (int)b});
+        vb.push_back({be[b].v[1], (int)b});
+    }
+    std::stable_sort(vb.begin(), vb.end(), [](const std::pair<int, int>& x, const std::pair<int, int>& y) {
+        return x.first < y.first;
+    });
+    auto ring_of = [&](int v, size_t& lo, size_t& hi) {
+        lo = std::lower_bound(vb.begin(), vb.end(), std::make_pair(v, INT32_MIN)) - vb.begin();
+        hi = lo;
+        while (hi < vb.size() && vb[hi].first == v) hi++;
+    };
+    std::vector<int> np(nb, -2);   // EdgesNewPoint
+    std::vector<double> pts;
+    std::vector<int32_t> faces;
+    int n_pts = 0;
+    // pass 1: a new vertex and face on every boundary edge between two clusters (:437-465)
+    for (uint32_t b = 0; b < nb; b++) {
+        const int c1 = be[b].c[0], c2 = be[b].c[1];
+        if (c1 == c2) continue;
+        for (int q = 0; q < 3; q++)
+            pts.push_back((double)(float)(0.5 * (be[b].p1[q] + be[b].p2[q])));
+        np[b] = K + n_pts++;
+        faces.insert(faces.end(), {np[b], c1, c2});
+    }
+    // pass 2: every run of boundary edges inside one cluster joins the new vertices
+    // at its ends (:467-540)
+    std::vector<int> elist;
+    for (uint32_t b0 = 0; b0 < nb; b0++) {
+        if (np[b0] >= 0) continue;
+        const int cluster = be[b0].c[0];
+        std::vector<int> queue{(int)b0};
+        size_t head = 0;
+        elist.clear();
+        while (head < queue.size()) {
+            const int b = queue[head++];
+            if (np[b] == -2) {
+                np[b] = -1;
+                for (int s = 0; s < 2; s++) {
+                    size_t lo, hi;
+                    ring_of(be[b].v[s], lo, hi);
+                    for (size_t q = lo; q < hi; q++) queue.push_back(vb[q].second);
+                }
+            } else if (np[b] >= 0) {
+                if (std::find(elist.begin(), elist.end(), b) == elist.end()) elist.push_back(b);
+            }
+        }
+        if (elist.size() >= 2) faces.insert(faces.end(), {cluster, np[elist[0]], np[elist[1]]});
+    }
+    // pass 3: vertices between two new vertices (:542-565).  GetNumberOfBoundaries
+    // (Common/vtkSurfaceBase.cxx:939-949) counts the boundary edges among the edges
+    // numbered 0 .. valence-1 of the whole mesh, not of the vertex's ring; it is > 0
+    // exactly when the valence reaches one past the second boundary edge's number.
+    const int64_t need = nb >= 2 ? (int64_t)be[1].edge + 1 : INT64_MAX;
+    std::vector<int> verts;
+    for (auto& x : vb) if (verts.empty() || verts.back() != x.first) verts.push_back(x.first);
+    std::vector<int> nl;
+    for (int v : verts) {
+        size_t lo, hi;
+        ring_of(v, lo, hi);
+        const uint32_t b = (uint32_t)vb[lo].second;
+        const int deg = be[b].v[0] == v ? be[b].deg[0] : be[b].deg[1];
+        const int cl = be[b].v[0] == v ? be[b].c[0] : be[b].c[1];
+        if (deg < need) continue;
+        nl.clear();
+        for (size_t q = lo; q < hi; q++) {
+            const int p = np[vb[q].second];
+            if (p >= 0 && std::find(nl.begin(), nl.end(), p) == nl.end()) nl.push_back(p);
+        }
+        if (nl.size() > 1) faces.insert(faces.end(), {cl, nl[0], nl[1]});
+    }
+    const int64_t nfaces = (int64_t)faces.size() / 3;
+    if (new_points && n_pts) {
+        if (*n_new_points < n_pts) return fail(ctx, ACVD_ERR_ARG, "acvd_fix_mesh_boundaries: new_points too small");
+        std::memcpy(new_points, pts.data(), pts.size() * sizeof(double));
+    }
+    if (new_faces && nfaces) {
+        if (*n_new_faces < nfaces) return fail(ctx, ACVD_ERR_ARG, "acvd_fix_mesh_boundaries: new_faces too small");
+        std::memcpy(new_faces, faces.data(), faces.size() * sizeof(int32_t));
+    }
+    *n_new_points = n_pts;
+    *n_new_faces = nfaces;
+    return ACVD_OK;
+}
+
+extern "C" int acvd_get_dual_mesh(acvd_ctx* ctx, int32_t* tris, int64_t* n_tris) {
+    if (!ctx || !n_tris) return ACVD_ERR_ARG;
+    if (!ctx->ready_labels) return fail(ctx, ACVD_ERR_ARG, "no labels");
+    CK(cudaSetDevice(ctx->opts.device));
+    DBuf<int> out;
+    int64_t t = 0;
+    const int r = build_dual(ctx, out, &t);
+    if (r) return r;
+    *n_tris = t;
+    if (tris && t) {
         CK(cudaMemcpyAsync(tris, out.p, 3 * (size_t)t * sizeof(int), cudaMemcpyDeviceToHost, ctx->s));
         CK(cudaStreamSynchronize(ctx->s));
     }

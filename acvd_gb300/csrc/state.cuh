@@ -278,6 +278,34 @@ cudaError_t launch_subdivide(const double* xyz, int64_t nv, const int* tri, int6
                              double* out_xyz, int* out_tri, int* parent1, int* parent2, double* out_ind,
                              unsigned int* missing, cudaStream_t s);
 
+// ---- manifold checks of the ForceManifold loop, input boundary edges (manifold.cu) ----
+// fill = false: per-vertex incidence counts of the dual triangles; fill = true: the
+// incidence lists at the scanned offsets (order within a list unspecified)
+cudaError_t launch_dual_incidence(const int* dt, int64_t t, unsigned* cnt, const unsigned* off, unsigned* cursor,
+                                  int* list, bool fill, cudaStream_t s);
+// bad[k]: output vertex not manifold; has_nm[k]: holds a non-manifold input vertex
+// (evaluated for the bad clusters only); issue[k]; unf[k]: neighbour of an issue
+// cluster.  has_nm and unf must be zeroed by the caller.
+cudaError_t launch_manifold_checks(const int* dt, const unsigned* off, const int* list, int k, const int* edge_int,
+                                   int64_t ne, const int* label, int64_t n, const int* orig, const uint32_t* vf_row,
+                                   const uint32_t* vf_face, const int* tri, const int* row, const int* size,
+                                   unsigned char* bad, unsigned char* has_nm, unsigned char* issue,
+                                   unsigned char* unf, cudaStream_t s);
+cudaError_t launch_boundary_edge_flags(const int* edge_v, int64_t ne, const uint32_t* vf_row, const uint32_t* vf_face,
+                                       const int* tri, uint32_t* flag, cudaStream_t s);
+// one input boundary edge as FixMeshBoundaries reads it (vertex ids, clusters, ring sizes, points)
+struct BoundaryEdge {
+    int edge;
+    int v[2];
+    int c[2];
+    int deg[2];
+    int pad;
+    double p1[3];
+    double p2[3];
+};
+cudaError_t launch_boundary_gather(const int* ids, int64_t nb, const int* edge_v, const int* label_ext, const int* inv,
+                                   const int* row, const double* xyz, BoundaryEdge* out, cudaStream_t s);
+
 // ---- adjoint (adjoint.cu) ----
 // Work arrays and inputs of the fixed-clustering adjoint (FP64).
 struct AdjState {

@@ -95,6 +95,16 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         "acvd_post_placement": (ctypes.c_int, [_P, ctypes.c_int, _P]),
         "acvd_compute_curvature": (ctypes.c_int, [_P, _P, _P]),
         "acvd_set_frozen_clusters": (ctypes.c_int, [_P, _P]),
+        "acvd_get_frozen_clusters": (ctypes.c_int, [_P, _P]),
+        "acvd_fix_mesh_boundaries": (ctypes.c_int, [_P, _P, ctypes.POINTER(_i64), _P, ctypes.POINTER(_i64)]),
+        "acvd_force_manifold_step": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int32),
+                                                    ctypes.POINTER(ctypes.c_int32)]),
+        "acvd_read_mesh": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(ctypes.POINTER(ctypes.c_double)),
+                                          ctypes.POINTER(_i64), ctypes.POINTER(ctypes.POINTER(ctypes.c_int32)),
+                                          ctypes.POINTER(_i64)]),
+        "acvd_write_mesh": (ctypes.c_int, [ctypes.c_char_p, _P, _i64, _P, _i64]),
+        "acvd_free": (None, [_P]),
+        "acvd_io_last_error": (ctypes.c_char_p, []),
         "acvd_subdivide": (ctypes.c_int, [_P, _i64, _P, _i64, _P, _P, _P, _i64, _P, _P, _P, _P, _P, _P, _P]),
     }
     for name, (res, args) in sig.items():
@@ -137,6 +147,38 @@ def build_topology(n_vertices: int, faces: np.ndarray):
     _check(lib.acvd_build_topology(n_vertices, tri.shape[0], _ptr(tri), _ptr(row), _ptr(col), _ptr(ev),
                                    ctypes.byref(ne)), what="acvd_build_topology")
     return row, col, ev.reshape(-1, 2)
+
+
+def read_mesh(path: str):
+    """vtkSurface::CreateFromFile for triangle meshes (.ply .off .obj .stl .vtk):
+    (points (nV, 3) float64, faces (nF, 3) int32)."""
+    lib = load()
+    xp = ctypes.POINTER(ctypes.c_double)()
+    tp = ctypes.POINTER(ctypes.c_int32)()
+    nv, nf = _i64(0), _i64(0)
+    code = lib.acvd_read_mesh(os.fsencode(path), ctypes.byref(xp), ctypes.byref(nv), ctypes.byref(tp),
+                              ctypes.byref(nf))
+    if code != ACVD_OK:
+        raise AcvdError(code, (lib.acvd_io_last_error() or b"").decode())
+    try:
+        pts = np.ctypeslib.as_array(xp, shape=(3 * nv.value,)).copy().reshape(-1, 3) if nv.value else \
+            np.zeros((0, 3))
+        tri = np.ctypeslib.as_array(tp, shape=(3 * nf.value,)).copy().reshape(-1, 3) if nf.value else \
+            np.zeros((0, 3), dtype=np.int32)
+    finally:
+        lib.acvd_free(ctypes.cast(xp, ctypes.c_void_p))
+        lib.acvd_free(ctypes.cast(tp, ctypes.c_void_p))
+    return pts, tri
+
+
+def write_mesh(path: str, points: np.ndarray, faces: np.ndarray) -> None:
+    """vtkSurface::WriteToFile (.ply binary, .off, .obj, .stl binary, .vtk ascii)."""
+    lib = load()
+    pts = np.ascontiguousarray(points, dtype=np.float64).reshape(-1, 3)
+    tri = np.ascontiguousarray(faces, dtype=np.int32).reshape(-1, 3)
+    code = lib.acvd_write_mesh(os.fsencode(path), _ptr(pts), pts.shape[0], _ptr(tri), tri.shape[0])
+    if code != ACVD_OK:
+        raise AcvdError(code, (lib.acvd_io_last_error() or b"").decode())
 
 
 def vertex_weights(metric: str, points: np.ndarray, faces: np.ndarray, indicator=None, gradation: float = 0.0):
@@ -296,6 +338,33 @@ class Engine:
             raise ValueError("set_frozen_clusters needs one flag per cluster")
         self._frozen = f
         self._ck(self._lib.acvd_set_frozen_clusters(self.ctx, _ptr(f)), "acvd_set_frozen_clusters")
+
+    def frozen_clusters(self) -> np.ndarray:
+        out = np.empty(self.k, dtype=np.uint8)
+        self._ck(self._lib.acvd_get_frozen_clusters(self.ctx, _ptr(out)), "acvd_get_frozen_clusters")
+        return out
+
+    def force_manifold_step(self) -> int:
+        """One pass of Remesh()'s ForceManifold loop: the number of topology issues (0:
+        nothing changed); otherwise new clusters were added (self.k grows) and the
+        others frozen for the next minimize()."""
+        n, k = ctypes.c_int32(0), ctypes.c_int32(0)
+        self._ck(self._lib.acvd_force_manifold_step(self.ctx, ctypes.byref(n), ctypes.byref(k)),
+                 "acvd_force_manifold_step")
+        self.k = int(k.value)
+        return int(n.value)
+
+    def fix_mesh_boundaries(self):
+        """FixMeshBoundaries for the current clustering: (new points (n, 3) float64
+        holding float values, numbered from K; new faces (m, 3) int32)."""
+        n, m = _i64(0), _i64(0)
+        self._ck(self._lib.acvd_fix_mesh_boundaries(self.ctx, None, ctypes.byref(n), None, ctypes.byref(m)),
+                 "acvd_fix_mesh_boundaries")
+        pts = np.empty((max(n.value, 1), 3), dtype=np.float64)
+        tri = np.empty((max(m.value, 1), 3), dtype=np.int32)
+        self._ck(self._lib.acvd_fix_mesh_boundaries(self.ctx, _ptr(pts), ctypes.byref(n), _ptr(tri), ctypes.byref(m)),
+                 "acvd_fix_mesh_boundaries")
+        return pts[:n.value], tri[:m.value]
 
     def subdivide(self, points: np.ndarray, faces: np.ndarray, row: np.ndarray, col: np.ndarray,
                   edge_v: np.ndarray, indicator: np.ndarray | None = None):

@@ -59,6 +59,20 @@ class Surface:
     def GetPointCoordinates(self, i: int):
         return self.points[i].copy()
 
+    @classmethod
+    def CreateFromFile(cls, path: str) -> "Surface":
+        """vtkSurface::CreateFromFile (Common/vtkSurface.cxx:2013-2132), triangle meshes."""
+        pts, tri = _eng.read_mesh(path)
+        return cls(pts, tri)
+
+    def WriteToFile(self, path: str) -> None:
+        """vtkSurface::WriteToFile (Common/vtkSurface.cxx:1958-2009)."""
+        _eng.write_mesh(path, self.points, self.faces)
+
+    def DisplayMeshProperties(self) -> None:
+        print(f"Mesh with {self.GetNumberOfPoints()} vertices, {self.GetNumberOfCells()} faces, "
+              f"{self.GetNumberOfEdges()} edges")
+
 
 class _Metric:
     def __init__(self, owner):
@@ -96,6 +110,9 @@ class _DiscreteRemeshing:
         self.Display = 0
         self.MaxNumberOfLoops = 5000000
         self.InitialClustering = None
+        self.ForceManifold = False
+        self.BoundaryFixing = 0          # the constructor's value (vtkDiscreteRemeshing.h:1192)
+        self.MaxNumberOfManifoldPasses = 1000
         self.Indicator = None
         self.PrincipalDirections = None
         self.Output = None
@@ -140,6 +157,15 @@ class _DiscreteRemeshing:
         if v:
             raise _eng.AcvdError(5, "display needs a graphics stack; only Display = 0 is available")
         self.Display = 0
+
+    def SetForceManifold(self, on):
+        """ForceManifold: after the clustering, add clusters next to non-manifold output
+        vertices and minimise again until none is left (vtkDiscreteRemeshing.h:937-950)."""
+        self.ForceManifold = bool(on)
+
+    def SetBoundaryFixing(self, on: int):
+        """Close the coarse mesh along the input's boundary (FixMeshBoundaries)."""
+        self.BoundaryFixing = int(on)
 
     def SetMaxNumberOfLoops(self, n: int):
         self.MaxNumberOfLoops = int(n)
@@ -251,6 +277,9 @@ class _DiscreteRemeshing:
         return self.Clustering
 
     def BuildDelaunayTriangulation(self):
+        """The coarse mesh (vtkDiscreteRemeshing.h:1003-1112): one vertex per cluster at
+        its metric centroid (the first non-empty cluster's for an empty one), stored
+        float-rounded as the output's float vtkPoints holds it, and the dual triangles."""
         e = self._engine
         cl = e.clusters()
         sizes = cl["size"]
@@ -258,13 +287,50 @@ class _DiscreteRemeshing:
         nonempty = np.nonzero(sizes > 0)[0]
         valid = int(nonempty[0]) if nonempty.size else 0
         verts[sizes == 0] = verts[valid]
-        self.Output = Surface(verts, e.dual_mesh())
+        self.Output = Surface(verts.astype(np.float32).astype(np.float64), e.dual_mesh())
         self.Energy = cl["energy_total"]
         return self.Output
 
+    def _force_manifold(self):
+        """Remesh()'s ForceManifold loop (vtkDiscreteRemeshing.h:937-950): while
+        DetectNonManifoldOutputVertices finds issues, MinimizeEnergy again with the
+        other clusters frozen."""
+        e = self._engine
+        passes = 0
+        while True:
+            n = e.force_manifold_step()
+            if n == 0:
+                break
+            if self.ConsoleOutput:
+                print(f"{n} topology issues, restarting minimization")
+            st = e.minimize()
+            for key in ("sweeps", "moves", "device_ms"):
+                if self.Stats is not None and key in self.Stats:
+                    self.Stats[key] += st[key]
+            passes += 1
+            if passes >= self.MaxNumberOfManifoldPasses:
+                raise _eng.AcvdError(3, f"ForceManifold: issues left after {passes} passes")
+        self.NumberOfManifoldPasses = passes
+        self.NumberOfClusters = e.k
+        self.Clustering = e.labels()
+
+    def FixMeshBoundaries(self) -> bool:
+        """FixMeshBoundaries (vtkDiscreteRemeshing.h:426-579): appends the boundary
+        vertices and faces to GetOutput(); True when it added any."""
+        if not self.BoundaryFixing:
+            return False
+        pts, tri = self._engine.fix_mesh_boundaries()
+        if pts.shape[0] == 0 and tri.shape[0] == 0:
+            return False
+        self.Output = Surface(np.concatenate([self.Output.points, pts]), np.concatenate([self.Output.faces, tri]))
+        return pts.shape[0] > 0
+
     def Remesh(self):
         self.ProcessClustering()
+        if self.ForceManifold:
+            self._force_manifold()
         self.BuildDelaunayTriangulation()
+        self.FixMeshBoundaries()
 
     def GetOutput(self) -> Surface:
         return self.Output

@@ -168,6 +168,8 @@ int acvd_set_labels(acvd_ctx* ctx, int32_t k, const int32_t* labels);
  * MinimizeEnergy.  Call after acvd_set_labels.
  */
 int acvd_set_frozen_clusters(acvd_ctx* ctx, const uint8_t* frozen);
+/* The frozen set in force (K bytes, 1 = frozen; all 0 when none is set). */
+int acvd_get_frozen_clusters(acvd_ctx* ctx, uint8_t* frozen);
 
 /*
  * MinimizeEnergy(): hole filling, statistics, colour sweeps until the
@@ -262,6 +264,45 @@ int acvd_subdivide(acvd_ctx* ctx, int64_t n_vertices, const double* xyz, int64_t
 int acvd_post_placement(acvd_ctx* ctx, int level, double* points);
 
 /*
+ * One pass of the ForceManifold loop of Remesh() (DiscreteRemeshing/vtkDiscreteRemeshing.h:
+ * 937-950 -> DetectNonManifoldOutputVertices, :165-383) on the current clustering.  An
+ * output vertex is checked on the coarse surface that BuildDelaunayTriangulation builds
+ * under ForceManifold (the dual triangles plus an edge between every two adjacent
+ * clusters, :1114-1132) with vtkSurfaceBase::IsVertexManifold's rule (at least two
+ * edges, each with exactly two faces, one fan).  A non-empty cluster whose output
+ * vertex fails and which holds no non-manifold input vertex is an issue: a new cluster
+ * takes its first item (by vertex id; from a neighbouring cluster with more than one
+ * item when it has a single one), and every cluster but the issues, their output
+ * neighbours and the new ones is frozen.  On return *n_issues is the count (0: labels,
+ * K and the frozen set unchanged -- the reference would leave every cluster frozen, which
+ * only matters to a further MinimizeEnergy that Remesh() does not run); otherwise the context holds the new labels, K and frozen set, the
+ * unconstrained first phase is off (the reference's metric stays constrained), and
+ * acvd_minimize is the reference's re-entry into MinimizeEnergy.  *n_clusters is the
+ * new K.  Loop while *n_issues > 0.
+ */
+int acvd_force_manifold_step(acvd_ctx* ctx, int32_t* n_issues, int32_t* n_clusters);
+
+/*
+ * FixMeshBoundaries (DiscreteRemeshing/vtkDiscreteRemeshing.h:426-579, Remesh()'s last
+ * step when SetBoundaryFixing is on): the vertices and faces that close the coarse
+ * mesh along the input's boundary, for the current clustering.  Pass 1: every input
+ * boundary edge (one face) whose ends lie in two clusters gets a new vertex at its
+ * midpoint (float-rounded, as the output's float vtkPoints stores it) and a face
+ * (new, c1, c2).  Pass 2: every run of boundary edges inside one cluster joins that
+ * cluster and the new vertices of the first two split edges it reaches.  Pass 3: a
+ * boundary vertex next to two new vertices gets the face (its cluster, first, second)
+ * -- only when the reference's GetNumberOfBoundaries (Common/vtkSurfaceBase.cxx:939-949,
+ * which counts among the mesh's first `valence` edges rather than the vertex's) is
+ * positive, as in the reference.  New vertices are numbered from K in order; faces are
+ * listed in the order the reference adds them, corners as it passes them (its
+ * vtkSurface may reorder corners to conquer an orientation; that is not replayed).
+ * new_points: 3 x *n_new_points doubles, new_faces: 3 x *n_new_faces; on input the two
+ * counts are the buffers' capacities.  Call with NULL buffers to get the counts.
+ */
+int acvd_fix_mesh_boundaries(acvd_ctx* ctx, double* new_points, int64_t* n_new_points, int32_t* new_faces,
+                             int64_t* n_new_faces);
+
+/*
  * Dual mesh (BuildDelaunayTriangulation, DiscreteRemeshing/vtkDiscreteRemeshing.h:1003-1152,
  * vertex clustering, without manifold repair): one triangle per input face whose
  * three labels are valid and distinct, in face order, duplicates (same label set)
@@ -290,6 +331,23 @@ int acvd_adjoint(acvd_ctx* ctx, const double* xyz, const double* rho, double gra
 
 /* The CUDA stream (cudaStream_t) the context launches on. */
 void* acvd_stream(acvd_ctx* ctx);
+
+/*
+ * Triangle-mesh files, host only: the formats vtkSurface::CreateFromFile / WriteToFile
+ * dispatch on by name (Common/vtkSurface.cxx:1958-2136; the lower-cased name contains
+ * ".vtk", ".ply", ".off", ".obj" or ".stl", tested in the reference's order).  Read:
+ * PLY (ascii / binary either endian), OFF, OBJ, STL (ascii / binary; identical corners
+ * merged in order of first appearance, triangles left degenerate dropped), legacy VTK
+ * POLYDATA (ascii / binary).  Write: PLY (binary little endian, float points), OFF, OBJ,
+ * STL (binary), legacy VTK (ascii).  Only triangles: another polygon is
+ * ACVD_ERR_UNSUPPORTED, as are .vtp and .wrl.  acvd_read_mesh allocates *xyz (3 nV
+ * doubles) and *tri (3 nF int32) with malloc; release them with acvd_free.  The text of
+ * the last failure of this thread is acvd_io_last_error().
+ */
+int acvd_read_mesh(const char* path, double** xyz, int64_t* n_vertices, int32_t** tri, int64_t* n_faces);
+int acvd_write_mesh(const char* path, const double* xyz, int64_t n_vertices, const int32_t* tri, int64_t n_faces);
+void acvd_free(void* p);
+const char* acvd_io_last_error(void);
 
 #ifdef __cplusplus
 }

@@ -19,7 +19,9 @@
  * vtkGPUMetric<M> is the reference metric M plus a copy of the curvature data
  * handed to it (SetCurvatureInfo, vtkDiscreteRemeshing.h:783) -- the metric keeps
  * them private, and the anisotropic metric overwrites its principal-direction
- * array in BuildMetric.  The engine's only extra state is the device ordinal.
+ * array in BuildMetric.  The engine's only extra state is the device ordinal and
+ * whether a minimisation already ran: vtkDiscreteRemeshing's ForceManifold loop
+ * re-enters MinimizeEnergy with IsClusterFreezed set, which is forwarded.
  * Errors of the C ABI are thrown as std::runtime_error; there is no CPU fallback.
  */
 #ifndef VTK_GPU_CLUSTERING_H
@@ -99,6 +101,7 @@ protected:
     ~vtkGPUClustering() {}
 
     int Device = 0;
+    bool Minimized = false;
     acvd_stats LastStats = {};
 
     static void check(acvd_ctx* ctx, int code, const char* what) {
@@ -161,9 +164,19 @@ protected:
                                    g),
               "acvd_set_metric");
         check(ctx, acvd_set_quadrics_optimization_level(ctx, metric.Level), "acvd_set_quadrics_optimization_level");
-        check(ctx, acvd_set_unconstrained_initialization(ctx, this->UnconstrainedInitialization),
+        // a re-entry (vtkDiscreteRemeshing's ForceManifold loop) finds the metric
+        // already switched to constrained placement
+        check(ctx, acvd_set_unconstrained_initialization(ctx, this->UnconstrainedInitialization && !this->Minimized),
               "acvd_set_unconstrained_initialization");
         check(ctx, acvd_set_labels(ctx, this->NumberOfClusters, this->Clustering->GetPointer(0)), "acvd_set_labels");
+        // IsClusterFreezed (vtkUniformClustering.h:329), set by DetectNonManifoldOutputVertices
+        std::vector<uint8_t> frozen(this->NumberOfClusters, 0);
+        bool any_frozen = false;
+        for (int c = 0; c < this->NumberOfClusters; c++) {
+            frozen[c] = this->IsClusterFreezed->GetValue(c) ? 1 : 0;
+            any_frozen = any_frozen || frozen[c];
+        }
+        if (any_frozen) check(ctx, acvd_set_frozen_clusters(ctx, frozen.data()), "acvd_set_frozen_clusters");
         check(ctx, acvd_minimize(ctx, &this->LastStats), "acvd_minimize");
         check(ctx, acvd_get_labels(ctx, this->Clustering->GetPointer(0)), "acvd_get_labels");
         acvd_destroy(ctx);
@@ -171,6 +184,7 @@ protected:
         // the state the reference's own loop ends in (:778-790)
         if (this->UnconstrainedInitialization) this->MetricContext.SetConstrainedClustering(1);
         this->ConnexityConstraint = 1;
+        this->Minimized = true;
         this->ReComputeStatistics();
     }
 };

@@ -316,6 +316,9 @@ struct EngineBase {
     virtual double item_weight(idt i) const = 0;
     virtual double cluster_energy(int k) const = 0;
     virtual void cluster_accum(int k, double* S, double* W, double* Q, double* c) const = 0;
+    // a new empty cluster (vtkDiscreteRemeshing.h:257-269)
+    virtual void add_cluster() = 0;
+    virtual void remove_last_cluster() = 0;
 
     idt n_items() const { return mesh.nV; }
 
@@ -616,6 +619,22 @@ struct Engine : EngineBase {
     void cluster_accum(int k, double* S, double* W, double* Q, double* c) const override {
         metric.accum(&clusters[k], S, W, Q);
         metric.get_centroid(&clusters[k], c);
+    }
+
+    void add_cluster() override {
+        clusters.emplace_back();
+        metric.reset(&clusters.back());
+        frozen.push_back(0);
+        last_mod.push_back(n_loops);
+        sizes.push_back(0);
+        K++;
+    }
+    void remove_last_cluster() override {
+        clusters.pop_back();
+        frozen.pop_back();
+        last_mod.pop_back();
+        sizes.pop_back();
+        K--;
     }
 
     void set_k(int k) {   // SetNumberOfClusters (:62-69)
@@ -937,6 +956,223 @@ long long port_dual_mesh(void* hp, int* tris, double* verts) {
         count++;
     }
     return count;
+}
+
+// The coarse surface of BuildDelaunayTriangulation (vtkDiscreteRemeshing.h:1003-1132)
+// for vertex clustering: a face per input face whose clusters are three distinct valid
+// ones (GetDualItemNeighbourClusters, :956-984; AddFace skips a face already present,
+// :990-999), then, under ForceManifold, an edge (without face) between every pair of
+// adjacent clusters not yet joined (:1114-1132).
+static void dual_surface(const EngineBase* e, Mesh& d, bool force_manifold) {
+    const Mesh& m = e->mesh;
+    d.start(e->K);
+    for (idt f = 0; f < m.nF; f++) {
+        int cl[3];
+        int n = 0;
+        for (int j = 0; j < 3; j++) {
+            const int c = e->labels[m.F[3 * f + j]];
+            if (c >= e->K) continue;
+            bool dup = false;
+            for (int t = 0; t < n; t++) if (cl[t] == c) dup = true;
+            if (!dup) cl[n++] = c;
+        }
+        if (n != 3) continue;
+        if (d.is_face(cl[0], cl[1], cl[2]) < 0) d.add_face(cl[0], cl[1], cl[2]);
+    }
+    if (!force_manifold) return;
+    for (idt i = 0; i < m.n_edges(); i++) {
+        const int c1 = e->labels[m.ev1[i]], c2 = e->labels[m.ev2[i]];
+        if (c1 != c2 && c1 >= 0 && c1 < e->K && c2 >= 0 && c2 < e->K && d.is_edge(c1, c2) < 0) d.add_edge(c1, c2, -1);
+    }
+}
+
+// vtkIdList::DeleteId: every occurrence removed, the last id taking the freed slot
+static void delete_id(std::vector<int>& v, int id) {
+    size_t i = 0;
+    while (i < v.size()) {
+        if (v[i] == id) { v[i] = v.back(); v.pop_back(); }
+        else i++;
+    }
+}
+
+// DetectNonManifoldOutputVertices (vtkDiscreteRemeshing.h:165-383): returns the number
+// of topology issues; adds the new clusters and sets IsClusterFreezed.
+static int detect_nonmanifold(EngineBase* e) {
+    Mesh d;
+    dual_surface(e, d, true);
+    const int K0 = e->K;
+    std::vector<std::vector<int>> items(K0);
+    for (int c = 0; c < K0; c++) e->frozen[c] = 1;
+    for (idt i = 0; i < e->n_items(); i++) {
+        const int c = e->labels[i];
+        if (c >= 0 && c < K0) items[c].push_back((int)i);
+    }
+    int issues = 0;
+    std::vector<int> with_issues;
+    std::vector<idt> cl;
+    for (int c = 0; c < K0; c++) {
+        if (d.is_vertex_manifold(c)) continue;
+        if (items[c].empty()) continue;
+        bool problem = true;
+        for (int it : items[c])
+            if (!e->mesh.is_vertex_manifold(it)) { problem = false; break; }
+        if (!problem) continue;
+        issues++;
+        with_issues.push_back(c);
+        e->frozen[c] = 0;
+        d.vertex_neighbours(c, cl);
+        for (idt x : cl) e->frozen[x] = 0;
+    }
+    std::vector<idt> il;
+    for (int c : with_issues) {
+        e->add_cluster();
+        const int nc = e->K - 1;
+        items.emplace_back();
+        if (items[c].size() > 1) {
+            const int it = items[c][0];
+            e->labels[it] = nc;
+            items[nc].push_back(it);
+            delete_id(items[c], it);
+            continue;
+        }
+        const int it = items[c][0];
+        e->mesh.vertex_neighbours(it, il);   // GetItemNeighbours (vtkVerticesProcessing.h)
+        bool found = false;
+        for (idt nb : il) {
+            // a cluster added in this pass holds one item; labels >= K0 are unassigned
+            // items, which the reference never meets here (MinimizeEnergy fills holes)
+            const int ncl = e->labels[nb];
+            if (ncl < 0 || ncl >= K0) continue;
+            if (items[ncl].size() > 1) {
+                e->labels[nb] = nc;
+                delete_id(items[ncl], (int)nb);
+                items[nc].push_back((int)nb);
+                found = true;
+                break;
+            }
+        }
+        if (!found) {
+            e->remove_last_cluster();
+            items.pop_back();
+        }
+    }
+    e->recompute_sizes();
+    return issues;
+}
+
+// One detection pass on the handle's clustering; *k_out = the new K.
+int port_detect_nonmanifold(void* hp, int* k_out) {
+    EngineBase* e = ((PortHandle*)hp)->eng;
+    const int n = detect_nonmanifold(e);
+    *k_out = e->K;
+    return n;
+}
+
+void port_set_frozen(void* hp, const unsigned char* in) {
+    EngineBase* e = ((PortHandle*)hp)->eng;
+    for (int k = 0; k < e->K; k++) e->frozen[k] = in[k] ? 1 : 0;
+}
+
+// MinimizeEnergy again on the current clustering (the ForceManifold re-entry)
+void port_minimize(void* hp) {
+    EngineBase* e = ((PortHandle*)hp)->eng;
+    e->connexity = 0;
+    e->minimize_energy();
+}
+
+void port_get_frozen(void* hp, unsigned char* out) {
+    EngineBase* e = ((PortHandle*)hp)->eng;
+    for (int k = 0; k < e->K; k++) out[k] = e->frozen[k];
+}
+
+// IsVertexManifold of every vertex of the coarse surface (ForceManifold edges included)
+// and of the input mesh.
+void port_manifold_flags(void* hp, unsigned char* dual, unsigned char* input) {
+    EngineBase* e = ((PortHandle*)hp)->eng;
+    Mesh d;
+    dual_surface(e, d, true);
+    if (dual) for (int c = 0; c < e->K; c++) dual[c] = d.is_vertex_manifold(c) ? 1 : 0;
+    if (input) for (idt i = 0; i < e->n_items(); i++) input[i] = e->mesh.is_vertex_manifold(i) ? 1 : 0;
+}
+
+// Remesh()'s ForceManifold loop (vtkDiscreteRemeshing.h:937-950) after ProcessClustering:
+// detect, then MinimizeEnergy without the connectivity constraint, until no issue is
+// left or max_rounds passes ran.  Returns the passes that found issues.
+int port_force_manifold(void* hp, int max_rounds) {
+    EngineBase* e = ((PortHandle*)hp)->eng;
+    int rounds = 0;
+    while (rounds < max_rounds && detect_nonmanifold(e)) {
+        rounds++;
+        e->connexity = 0;
+        e->minimize_energy();
+    }
+    return rounds;
+}
+
+int port_get_k(void* hp) { return ((PortHandle*)hp)->eng->K; }
+
+// FixMeshBoundaries (vtkDiscreteRemeshing.h:426-579), pass for pass over the whole edge
+// table: the new output vertices (numbered from K, float-rounded as the output's float
+// vtkPoints stores them) and the faces it adds.  Returns the face count; *n_pts = the
+// vertex count.  pts / faces may be null (counting call).
+long long port_fix_mesh_boundaries(void* hp, double* pts, int* faces, long long* n_pts) {
+    EngineBase* e = ((PortHandle*)hp)->eng;
+    const Mesh& m = e->mesh;
+    const idt ne = m.n_edges();
+    std::vector<idt> np(ne, -2);   // EdgesNewPoint
+    std::vector<double> P;
+    std::vector<int> F;
+    const int K = e->K;
+    int nnew = 0;
+    auto is_boundary = [&](idt i) { return m.poly2[i] < 0 && m.poly1[i] >= 0; };
+    for (idt i = 0; i < ne; i++) {
+        if (!is_boundary(i)) continue;
+        const idt v1 = m.ev1[i], v2 = m.ev2[i];
+        const int c1 = e->labels[v1], c2 = e->labels[v2];
+        if (c1 == c2) continue;
+        double P1[3], P2[3];
+        m.point(v1, P1);
+        m.point(v2, P2);
+        for (int q = 0; q < 3; q++) P.push_back((double)(float)(0.5 * (P1[q] + P2[q])));
+        np[i] = K + nnew++;
+        F.insert(F.end(), {(int)np[i], c1, c2});
+    }
+    std::vector<idt> elist;
+    for (idt i = 0; i < ne; i++) {
+        if (np[i] >= 0 || !is_boundary(i)) continue;
+        const int cluster = e->labels[m.ev1[i]];
+        std::queue<idt> q;
+        q.push(i);
+        elist.clear();
+        while (!q.empty()) {
+            const idt edge = q.front();
+            q.pop();
+            if (np[edge] == -2) {
+                np[edge] = -1;
+                for (idt v : {m.ev1[edge], m.ev2[edge]})
+                    for (idt j : m.ring[v])
+                        if (m.poly2[j] < 0) q.push(j);
+            } else if (np[edge] >= 0) {
+                if (std::find(elist.begin(), elist.end(), edge) == elist.end()) elist.push_back(edge);
+            }
+        }
+        if (elist.size() >= 2) F.insert(F.end(), {cluster, (int)np[elist[0]], (int)np[elist[1]]});
+    }
+    std::vector<idt> nl;
+    for (idt v = 0; v < m.nV; v++) {
+        // GetNumberOfBoundaries as the reference writes it: Edges[i] for i < valence
+        int nb = 0;
+        for (idt i = 0; i < (idt)m.ring[v].size(); i++) if (m.poly2[i] < 0) nb++;
+        if (nb / 2 <= 0) continue;
+        nl.clear();
+        for (idt j : m.ring[v])
+            if (np[j] >= 0 && std::find(nl.begin(), nl.end(), np[j]) == nl.end()) nl.push_back(np[j]);
+        if (nl.size() > 1) F.insert(F.end(), {e->labels[v], (int)nl[0], (int)nl[1]});
+    }
+    if (pts) std::memcpy(pts, P.data(), P.size() * sizeof(double));
+    if (faces) std::memcpy(faces, F.data(), F.size() * sizeof(int));
+    *n_pts = nnew;
+    return (long long)F.size() / 3;
 }
 
 // Curvature of vertex clustering (vtkDiscreteRemeshing::SamplingPreProcessing,

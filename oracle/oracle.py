@@ -206,6 +206,23 @@ class Port(_Base):
         lib.port_stats.restype = None
         lib.port_dual_mesh.argtypes = [_P, ctypes.c_void_p, ctypes.c_void_p]
         lib.port_dual_mesh.restype = ctypes.c_longlong
+        lib.port_detect_nonmanifold.argtypes = [_P, ctypes.POINTER(ctypes.c_int)]
+        lib.port_detect_nonmanifold.restype = ctypes.c_int
+        lib.port_get_frozen.argtypes = [_P, ctypes.c_void_p]
+        lib.port_get_frozen.restype = None
+        lib.port_manifold_flags.argtypes = [_P, ctypes.c_void_p, ctypes.c_void_p]
+        lib.port_manifold_flags.restype = None
+        lib.port_force_manifold.argtypes = [_P, ctypes.c_int]
+        lib.port_force_manifold.restype = ctypes.c_int
+        lib.port_set_frozen.argtypes = [_P, ctypes.c_void_p]
+        lib.port_set_frozen.restype = None
+        lib.port_minimize.argtypes = [_P]
+        lib.port_minimize.restype = None
+        lib.port_get_k.argtypes = [_P]
+        lib.port_get_k.restype = ctypes.c_int
+        lib.port_fix_mesh_boundaries.argtypes = [_P, ctypes.c_void_p, ctypes.c_void_p,
+                                                 ctypes.POINTER(ctypes.c_longlong)]
+        lib.port_fix_mesh_boundaries.restype = ctypes.c_longlong
 
     def items(self) -> dict:
         n = self.n
@@ -234,6 +251,50 @@ class Port(_Base):
         a, b, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_longlong()
         self._lib.port_stats(self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c))
         return {"loops": a.value, "convergences": b.value, "moves": c.value}
+
+    def detect_nonmanifold(self) -> int:
+        """DetectNonManifoldOutputVertices on the current clustering: the number of
+        issues; new clusters added (self.k), IsClusterFreezed set (frozen())."""
+        k = ctypes.c_int(0)
+        n = int(self._lib.port_detect_nonmanifold(self.h, ctypes.byref(k)))
+        self.k = int(k.value)
+        return n
+
+    def set_frozen(self, frozen: np.ndarray) -> None:
+        self._frozen_in = np.ascontiguousarray(frozen, dtype=np.uint8)
+        self._lib.port_set_frozen(self.h, self._frozen_in.ctypes.data)
+
+    def minimize(self) -> None:
+        """MinimizeEnergy again (connectivity constraint off first), keeping IsClusterFreezed."""
+        self._lib.port_minimize(self.h)
+
+    def frozen(self) -> np.ndarray:
+        out = np.empty(self.k, dtype=np.uint8)
+        self._lib.port_get_frozen(self.h, out.ctypes.data)
+        return out
+
+    def manifold_flags(self):
+        """IsVertexManifold of every coarse-surface vertex (ForceManifold edges
+        included) and of every input vertex."""
+        d = np.empty(self.k, dtype=np.uint8)
+        i = np.empty(self.n, dtype=np.uint8)
+        self._lib.port_manifold_flags(self.h, d.ctypes.data, i.ctypes.data)
+        return d, i
+
+    def force_manifold(self, max_rounds: int = 1000) -> int:
+        """Remesh()'s ForceManifold loop after run(): the passes that found issues."""
+        r = int(self._lib.port_force_manifold(self.h, int(max_rounds)))
+        self.k = int(self._lib.port_get_k(self.h))
+        return r
+
+    def fix_mesh_boundaries(self):
+        """FixMeshBoundaries for the current clustering: (new points (n, 3), faces (m, 3))."""
+        n = ctypes.c_longlong(0)
+        nf = int(self._lib.port_fix_mesh_boundaries(self.h, None, None, ctypes.byref(n)))
+        pts = np.empty((max(n.value, 1), 3))
+        tri = np.empty((max(nf, 1), 3), dtype=np.int32)
+        self._lib.port_fix_mesh_boundaries(self.h, pts.ctypes.data, tri.ctypes.data, ctypes.byref(n))
+        return pts[:n.value], tri[:nf]
 
     def dual_mesh(self):
         nt = int(self._lib.port_dual_mesh(self.h, None, None))

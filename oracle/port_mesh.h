@@ -69,6 +69,88 @@ struct Mesh {
         }
     }
 
+    // an empty surface of n vertices grown by add_face / add_edge (the coarse mesh of
+    // BuildDelaunayTriangulation; no coordinates)
+    void start(idt n) {
+        nV = n; nF = 0;
+        P.clear(); F.clear(); ev1.clear(); ev2.clear(); poly1.clear(); poly2.clear(); nonmanifold.clear();
+        ring.assign(n, {});
+    }
+
+    // vtkSurfaceBase::AddFace -> AddPolygon (.cxx:1236-1320): edges in corner order
+    idt add_face(idt a, idt b, idt c) {
+        const idt f = nF++;
+        F.push_back(a); F.push_back(b); F.push_back(c);
+        add_edge(a, b, f); add_edge(b, c, f); add_edge(c, a, f);
+        return f;
+    }
+
+    // vtkSurfaceBase::GetThirdPoint (vtkSurfaceBase.h:384-400)
+    idt third_point(idt f, idt v1, idt v2) const {
+        const idt v3 = F[3 * f], v4 = F[3 * f + 1], v5 = F[3 * f + 2];
+        if (v1 != v3 && v2 != v3) return v3;
+        if (v1 != v4 && v2 != v4) return v4;
+        return v5;
+    }
+
+    // vtkSurfaceBase::IsFace (.cxx:724-764)
+    idt is_face(idt v1, idt v2, idt v3) const {
+        const idt e = is_edge(v1, v2);
+        if (e < 0) return -1;
+        const idt f1 = poly1[e], f2 = poly2[e];
+        if (f1 < 0) return -1;
+        if (v3 == third_point(f1, v1, v2)) return f1;
+        if (f2 < 0) return -1;
+        if (v3 == third_point(f2, v1, v2)) return f2;
+        for (idt k = (idt)nonmanifold[e].size() - 1; k >= 0; k--)
+            if (v3 == third_point(nonmanifold[e][k], v1, v2)) return nonmanifold[e][k];
+        return -1;
+    }
+
+    // vtkSurfaceBase::Conquer (vtkSurfaceBase.h:402-426)
+    void conquer(idt f1, idt v1, idt v2, idt& f2, idt& v3) const {
+        const idt e = is_edge(v1, v2);
+        if (e < 0) { f2 = -1; v3 = -1; return; }
+        f2 = poly2[e];
+        if (f2 == -1) { v3 = -1; return; }
+        if (f2 == f1) f2 = poly1[e];
+        v3 = third_point(f2, v1, v2);
+    }
+
+    // vtkSurfaceBase::IsEdgeManifold (vtkSurfaceBase.h:521-528)
+    bool is_edge_manifold(idt e) const { return poly2[e] >= 0 && nonmanifold[e].empty(); }
+
+    // vtkSurfaceBase::IsVertexManifold (.cxx:259-315), walk for walk
+    bool is_vertex_manifold(idt iV) const {
+        const std::vector<idt>& edges = ring[iV];
+        idt remaining = (idt)edges.size();
+        if (remaining < 2) return false;
+        for (idt e : edges) if (!is_edge_manifold(e)) return false;
+        const idt first_edge = edges[0];
+        idt first_vertex = ev1[first_edge], v1 = ev2[first_edge];
+        if (first_vertex == iV) first_vertex = v1;
+        v1 = first_vertex;
+        remaining--;
+        idt f1 = poly1[first_edge], f2 = poly2[first_edge], f3;
+        idt v2 = third_point(f1, iV, first_vertex);
+        do {
+            if (--remaining == 0) return true;
+            conquer(f1, iV, v2, f3, v1);
+            f1 = f3;
+            v2 = v1;
+        } while (f1 >= 0 && v2 != first_vertex);
+        if (f2 < 0 || v2 == first_vertex) return false;
+        v1 = first_vertex;
+        v2 = third_point(f2, iV, first_vertex);
+        do {
+            if (--remaining == 0) return true;
+            conquer(f2, iV, v2, f3, v1);
+            f2 = f3;
+            v2 = v1;
+        } while (f2 >= 0 && v2 != first_vertex);
+        return false;
+    }
+
     void point(idt i, double* p) const { p[0] = P[3 * i]; p[1] = P[3 * i + 1]; p[2] = P[3 * i + 2]; }
 
     // vtkSurfaceBase::GetVertexNeighbourFaces (.cxx:964-984)

@@ -1,0 +1,42 @@
+"""The ACVD / ACVDQ command-line drivers end to end on the GPU: file in, remesh
+(with subdivision, ForceManifold, boundary fixing and the quadric post-placement as the
+options ask), file out."""
+import os
+
+import numpy as np
+import pytest
+
+import acvd_gb300
+from acvd_gb300 import cli, synth
+from acvd_gb300 import engine as E
+
+pytestmark = pytest.mark.gpu
+
+
+def test_acvd_program(tmp_path):
+    m = synth.torus(80, 40, seed=2)
+    src = str(tmp_path / "in.ply")
+    E.write_mesh(src, m.points, m.faces)
+    out = str(tmp_path / "out")
+    os.makedirs(out)
+    assert cli.main_acvd([src, "300", "0.5", "-o", out, "-of", "coarse.obj", "-q", "2"]) == 0
+    smooth = E.read_mesh(out + "smooth_coarse.obj")           # written before the post-placement
+    final = E.read_mesh(os.path.join(out, "coarse.obj"))
+    assert smooth[0].shape == final[0].shape == (300, 3)
+    np.testing.assert_array_equal(smooth[1], final[1])
+    assert not np.array_equal(smooth[0], final[0])
+
+
+def test_acvdq_program_with_subdivision_and_options(tmp_path):
+    h = synth.heightfield(30, seed=2)                          # 900 vertices, open
+    src = str(tmp_path / "in.off")
+    E.write_mesh(src, h.points, h.faces)
+    dst = str(tmp_path) + "/"
+    assert cli.main_acvdq([src, "200", "0", "-o", dst, "-of", "q.vtk", "-m", "1", "-b", "1", "-q", "2"]) == 0
+    # 900 < 10 x 200: subdivided twice before clustering; written as PLY whatever the name
+    raw = open(dst + "q.vtk", "rb").read(3)
+    assert raw == b"ply"
+    os.replace(dst + "q.vtk", dst + "q.ply")
+    pts, tri = E.read_mesh(dst + "q.ply")
+    assert pts.shape[0] > 200                                  # boundary vertices appended
+    assert tri.max() < pts.shape[0]

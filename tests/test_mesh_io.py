@@ -1,0 +1,135 @@
+"""Mesh files (vtkSurface::CreateFromFile / WriteToFile, Common/vtkSurface.cxx:1958-2136):
+round trips through every written format, hand-written files in the variants the
+readers accept, and the error paths.  Host code only."""
+import os
+
+import numpy as np
+import pytest
+
+import acvd_gb300
+from acvd_gb300 import engine as E
+from acvd_gb300 import synth
+
+TET_P = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1.5]])
+TET_F = np.array([[0, 1, 2], [0, 3, 1], [0, 2, 3], [1, 3, 2]], dtype=np.int32)
+
+
+def _f32(a):
+    return np.asarray(a, dtype=np.float32).astype(np.float64)
+
+
+@pytest.mark.parametrize("ext", ["ply", "off", "obj", "vtk", "PLY"])
+def test_round_trip(tmp_path, ext):
+    m = synth.torus(20, 10, seed=1)
+    p = str(tmp_path / f"m.{ext}")
+    E.write_mesh(p, m.points, m.faces)
+    pts, tri = E.read_mesh(p)
+    np.testing.assert_array_equal(tri, m.faces)
+    # PLY stores float points (as the reference's float vtkPoints); the text formats keep doubles
+    np.testing.assert_array_equal(pts, _f32(m.points) if ext.lower() == "ply" else m.points)
+
+
+def test_stl_merges_corners(tmp_path):
+    m = synth.torus(20, 10, seed=1)
+    p = str(tmp_path / "m.stl")
+    E.write_mesh(p, m.points, m.faces)
+    pts, tri = E.read_mesh(p)
+    assert pts.shape == m.points.shape and tri.shape == m.faces.shape
+    np.testing.assert_array_equal(pts[tri], _f32(m.points)[m.faces])
+    # vertices numbered by first appearance in the facets
+    first = []
+    for v in m.faces.reshape(-1):
+        if v not in first:
+            first.append(v)
+    np.testing.assert_array_equal(pts, _f32(m.points)[first])
+
+
+def test_ascii_stl_and_surface_api(tmp_path):
+    p = tmp_path / "t.stl"
+    lines = ["solid t"]
+    for f in TET_F:
+        lines += ["facet normal 0 0 0", "outer loop"] + [f"vertex {x} {y} {z}" for x, y, z in TET_P[f]] + \
+                 ["endloop", "endfacet"]
+    p.write_text("\n".join(lines + ["endsolid t"]) + "\n")
+    s = acvd_gb300.Surface.CreateFromFile(str(p))
+    assert s.GetNumberOfPoints() == 4 and s.GetNumberOfCells() == 4 and s.GetNumberOfEdges() == 6
+    np.testing.assert_array_equal(s.points[s.faces], TET_P[TET_F])
+
+
+def test_ply_variants(tmp_path):
+    # ascii, extra properties and elements, uint indices
+    head = ("ply\nformat ascii 1.0\ncomment test\nelement vertex 4\nproperty double x\nproperty double y\n"
+            "property double z\nproperty uchar red\nelement face 4\nproperty list uchar uint vertex_indices\n"
+            "property float quality\nelement edge 1\nproperty int vertex1\nproperty int vertex2\nend_header\n")
+    body = "".join(f"{x} {y} {z} 7\n" for x, y, z in TET_P) + "".join(f"3 {a} {b} {c} 0.5\n" for a, b, c in TET_F)
+    p = tmp_path / "a.ply"
+    p.write_text(head + body + "0 1\n")
+    pts, tri = E.read_mesh(str(p))
+    np.testing.assert_array_equal(pts, TET_P)
+    np.testing.assert_array_equal(tri, TET_F)
+    # binary big endian, int count, vertex_index name, normals before the coordinates
+    head = ("ply\nformat binary_big_endian 1.0\nelement vertex 4\nproperty float nx\nproperty float x\n"
+            "property float y\nproperty float z\nelement face 4\nproperty list int int vertex_index\nend_header\n")
+    raw = bytearray(head.encode())
+    for x, y, z in TET_P:
+        raw += np.array([9, x, y, z], dtype=">f4").tobytes()
+    for f in TET_F:
+        raw += np.array([3, *f], dtype=">i4").tobytes()
+    p = tmp_path / "b.ply"
+    p.write_bytes(bytes(raw))
+    pts, tri = E.read_mesh(str(p))
+    np.testing.assert_array_equal(pts, _f32(TET_P))
+    np.testing.assert_array_equal(tri, TET_F)
+
+
+def test_obj_off_vtk_variants(tmp_path):
+    obj = tmp_path / "a.obj"
+    obj.write_text("# c\no x\n" + "".join(f"v {x} {y} {z}\n" for x, y, z in TET_P) + "vn 0 0 1\n" +
+                   "f 1/1/1 2/2/1 3/3/1\nf 1//1 4//1 2//1\nf -4 -2 -1\nf 2 4 3\n")
+    pts, tri = E.read_mesh(str(obj))
+    np.testing.assert_array_equal(pts, TET_P)
+    np.testing.assert_array_equal(tri, TET_F)
+    off = tmp_path / "a.off"
+    off.write_text("OFF 4 4 6\n# comment\n" + "".join(f"{x} {y} {z}\n" for x, y, z in TET_P) +
+                   "".join(f"3 {a} {b} {c} 255 0 0\n" for a, b, c in TET_F))
+    pts, tri = E.read_mesh(str(off))
+    np.testing.assert_array_equal(pts, TET_P)
+    np.testing.assert_array_equal(tri, TET_F)
+    vtk = tmp_path / "a.vtk"
+    vtk.write_text("# vtk DataFile Version 5.1\nt\nASCII\nDATASET POLYDATA\nPOINTS 4 float\n" +
+                   " ".join(f"{x} {y} {z}" for x, y, z in TET_P) +
+                   "\nPOLYGONS 5 12\nOFFSETS vtktypeint64\n0 3 6 9 12\nCONNECTIVITY vtktypeint64\n" +
+                   " ".join(str(v) for v in TET_F.reshape(-1)) + "\nPOINT_DATA 4\n")
+    pts, tri = E.read_mesh(str(vtk))
+    np.testing.assert_array_equal(pts, TET_P)
+    np.testing.assert_array_equal(tri, TET_F)
+
+
+def test_errors(tmp_path):
+    quad = tmp_path / "q.obj"
+    quad.write_text("v 0 0 0\nv 1 0 0\nv 1 1 0\nv 0 1 0\nf 1 2 3 4\n")
+    with pytest.raises(acvd_gb300.AcvdError) as ei:
+        E.read_mesh(str(quad))
+    assert ei.value.code == 5
+    bad = tmp_path / "b.off"
+    bad.write_text("OFF\n3 1 0\n0 0 0\n1 0 0\n0 1 0\n3 0 1 7\n")
+    with pytest.raises(acvd_gb300.AcvdError):
+        E.read_mesh(str(bad))
+    for name in ("x.vtp", "x.wrl", "x.xyz"):
+        (tmp_path / name).write_text("")
+        with pytest.raises(acvd_gb300.AcvdError):
+            E.read_mesh(str(tmp_path / name))
+    with pytest.raises(acvd_gb300.AcvdError):
+        E.read_mesh(str(tmp_path / "missing.ply"))
+    with pytest.raises(acvd_gb300.AcvdError):
+        E.write_mesh(str(tmp_path / "o.ply"), TET_P, np.array([[0, 1, 9]]))
+
+
+def test_cli_rejects_unbuilt_options():
+    from acvd_gb300 import cli
+    with pytest.raises(SystemExit):
+        cli.main_acvd(["x.ply", "100", "0", "-l", "2"])
+    with pytest.raises(SystemExit):
+        cli.main_acvdq(["x.ply", "100", "0", "-d", "1"])
+    with pytest.raises(SystemExit):
+        cli.main_acvd(["x.ply"])
