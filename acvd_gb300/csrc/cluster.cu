@@ -196,7 +196,8 @@ ACVD_DEV bool ring_connected(const DevState& st, int p0, int p1, int L) {
     return vis == msk;
 }
 
-// An item changed cluster: it and its ring may now lie on a boundary.
+// An item changed cluster: it and its ring may now lie on a boundary, and their
+// cached screens (bflag 2) no longer hold.
 ACVD_DEV void mark_ring(const DevState& st, int i) {
     st.bflag[i] = 1;
     for (int p = st.row[i]; p < st.row[i + 1]; p++) st.bflag[st.col[p]] = 1;
@@ -218,6 +219,7 @@ ACVD_DEV void warp_count(unsigned long long* ctr, unsigned v) {
 constexpr int kRingPref = 8;   // ring slots whose labels phase A loads up front
 constexpr int kMaxTgt = 8;     // destination clusters per item on the task path
 constexpr int kTaskRemove = 15;  // task code of an item's remove part
+constexpr int kScrCached = 1 << 30;  // screen list entry: the item's screen is cached (bflag 2)
 
 // Local connectivity with the first kRingPref ring labels already loaded.
 ACVD_DEV bool ring_connected_pref(const DevState& st, int p0, int p1, int L, const int* lb) {
@@ -281,28 +283,69 @@ ACVD_DEV void eval_tile(const DevState& st, int item0, int64_t count, int color,
     const bool in = idx_t < count;
     const SweepState sw = *st.sweep;
     const RunFlags fl = *st.flags;
-    unsigned n_slots = 0, n_bnd = 0, n_tgt = 0, n_cand = 0, n_scr = 0;
+    unsigned n_slots = 0, n_bnd = 0, n_tgt = 0, n_cand = 0, n_scr = 0, n_cached = 0;
     // A0: only items that may lie on a boundary go on to the ring screen, packed
     // so that warps without one issue nothing
     {
-        const bool flagged = in && st.bflag[item0 + idx_t] != 0;
+        const unsigned char bf = in ? st.bflag[item0 + idx_t] : (unsigned char)0;
+        const bool flagged = bf != 0;
         const unsigned bal = __ballot_sync(kFull, flagged);
         if (bal) {
             const int lane = threadIdx.x & 31;
             unsigned base = 0;
             if (lane == 0) base = atomicAdd(&s_nscr, (unsigned)__popc(bal));
             base = __shfl_sync(kFull, base, 0);
-            if (flagged) s_scr[base + __popc(bal & ((1u << lane) - 1u))] = (int)idx_t;
+            if (flagged) s_scr[base + __popc(bal & ((1u << lane) - 1u))] = (int)idx_t | (bf == 2 ? kScrCached : 0);
         }
     }
     __syncthreads();
     if (threadIdx.x < s_nscr) {
-        const int64_t idx = s_scr[threadIdx.x];
+        const int code = s_scr[threadIdx.x];
+        const int64_t idx = code & ~kScrCached;
         const int i = item0 + (int)idx;
         n_scr = 1;
-        const int4 ra = st.ring8[2 * (int64_t)i], rb = st.ring8[2 * (int64_t)i + 1];
         const int L = st.label[i];
         const int ev_i = st.evald[i];
+        bool screened = false;
+        if (code & kScrCached) {
+            // the ring kept its labels since the last full screen: its distinct
+            // neighbour clusters and the connectivity test are in the cache
+            const int4 c = st.tcache[i];
+            const int n = c.w & 3;
+            const bool conn_known = (c.w & 4) != 0, conn_ok = (c.w & 8) != 0;
+            const bool may_move = st.size[L] > 1 && !(st.frozen && st.frozen[L]);
+            if (!(fl.connexity && may_move && !conn_known)) {
+                screened = true;
+                n_cached = 1;
+                const int tg[3] = {c.x, c.y, c.z};
+                bool fresh = ev_i <= sw.floor || st.stamp[L] >= ev_i;
+#pragma unroll
+                for (int q = 0; q < 3; q++)
+                    if (q < n && st.stamp[tg[q]] >= ev_i) fresh = true;
+                if (fresh) {
+                    n_bnd = 1;
+                    if (may_move && (!fl.connexity || conn_ok)) {
+                        const int w = (int)atomicAdd(&s_nwork, 1u);
+                        s_idx[w] = (int)idx;
+                        int nt = 0;
+#pragma unroll
+                        for (int q = 0; q < 3; q++)
+                            if (q < n && !(st.frozen && st.frozen[tg[q]])) s_tgt[w][nt++] = tg[q];
+                        s_nt[w] = (signed char)nt;
+                        n_tgt += (unsigned)nt;
+                        if (nt > 0) {
+                            const unsigned base = atomicAdd(&s_ntask, (unsigned)nt + 1u);
+                            for (int j = 0; j < nt; j++) s_task[base + j] = (unsigned short)((w << 4) | j);
+                            s_task[base + nt] = (unsigned short)((w << 4) | kTaskRemove);
+                        }
+                    } else {
+                        st.evald[i] = sw.sweep;   // evaluated: nothing it may do
+                    }
+                }
+            }
+        }
+        if (!screened) {
+        const int4 ra = st.ring8[2 * (int64_t)i], rb = st.ring8[2 * (int64_t)i + 1];
         int lb[kRingPref] = {ra.x, ra.y, ra.z, ra.w, rb.x, rb.y, rb.z, rb.w};
         const bool longer = lb[7] == -2;   // ring longer than 8: bounds and tail from the CSR
         int deg = 0;
@@ -337,12 +380,39 @@ ACVD_DEV void eval_tile(const DevState& st, int item0, int64_t count, int color,
             }
         }
         if (!boundary) st.bflag[i] = 0;   // interior until a commit touches its ring
+        const bool may_move = L < st.k && st.size[L] > 1 && !(st.frozen && st.frozen[L]);
+        int conn = -1;   // the local connectivity test, evaluated at most once
+        // cache a boundary screen of a ring of at most 8 with at most 3 neighbour
+        // clusters: they hold until a commit touches the ring (mark_ring)
+        if (boundary && !longer && L < st.k) {
+            int tg[3] = {0, 0, 0};
+            int n = 0;
+#pragma unroll
+            for (int q = 0; q < kRingPref; q++) {
+                const int B = lb[q];
+                if (B == L || B >= st.k) continue;
+                bool dup = false;
+#pragma unroll
+                for (int r = 0; r < q; r++) dup |= lb[r] == B;
+                if (dup) continue;
+                if (n < 3) tg[n] = B;
+                n++;
+            }
+            if (n <= 3) {
+                int meta = n;
+                if (fl.connexity && may_move) {
+                    conn = ring_connected_pref(st, st.row[i], st.row[i] + deg, L, lb) ? 1 : 0;
+                    meta |= 4 | (conn ? 8 : 0);
+                }
+                st.tcache[i] = make_int4(tg[0], tg[1], tg[2], meta);
+                st.bflag[i] = 2;
+            }
+        }
         if (boundary && fresh) {
             n_bnd = 1;
-            const bool movable =
-                L >= st.k ||
-                (st.size[L] > 1 && !(st.frozen && st.frozen[L]) &&
-                 (!fl.connexity || ring_connected_pref(st, st.row[i], st.row[i] + deg, L, lb)));
+            if (fl.connexity && may_move && conn < 0)
+                conn = ring_connected_pref(st, st.row[i], st.row[i] + deg, L, lb) ? 1 : 0;
+            const bool movable = L >= st.k || (may_move && (!fl.connexity || conn == 1));
             if (movable) {
                 const int w = (int)atomicAdd(&s_nwork, 1u);
                 s_idx[w] = (int)idx;
@@ -376,6 +446,7 @@ ACVD_DEV void eval_tile(const DevState& st, int item0, int64_t count, int color,
             } else {
                 st.evald[i] = sw.sweep;   // evaluated: nothing it may do
             }
+        }
         }
     }
     __syncthreads();
@@ -481,12 +552,20 @@ ACVD_DEV void eval_tile(const DevState& st, int item0, int64_t count, int color,
             st.evald[i] = sw.sweep;
         }
     }
-    // block-aggregated append to the compact proposal list: one atomic per block
-    // (tens of thousands of warps would otherwise serialise on the class's count)
+    // block-aggregated append to the compact proposal list and block totals of the
+    // counters: one atomic per block and counter (tens of thousands of warps would
+    // otherwise serialise on the class's count and the counter stripes)
     {
-        __shared__ unsigned s_wc[8], s_base;
+        constexpr int kNC = 7;
+        __shared__ unsigned s_wc[8], s_base, s_cnt[8][kNC];
         const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
         const unsigned bal = __ballot_sync(kFull, my_cand >= 0);
+        const unsigned v[kNC] = {in ? 1u : 0u, n_scr - n_cached, n_cached, n_slots, n_bnd, n_tgt, n_cand};
+#pragma unroll
+        for (int c = 0; c < kNC; c++) {
+            const unsigned t = __reduce_add_sync(kFull, v[c]);
+            if (lane == 0) s_cnt[wid][c] = t;
+        }
         if (lane == 0) s_wc[wid] = (unsigned)__popc(bal);
         __syncthreads();
         if (threadIdx.x == 0) {
@@ -497,16 +576,17 @@ ACVD_DEV void eval_tile(const DevState& st, int item0, int64_t count, int color,
                 tot += c;
             }
             s_base = tot ? atomicAdd(&st.cand_count[color], tot) : 0u;
+        } else if (threadIdx.x >= 32 && threadIdx.x < 32 + kNC) {
+            const int c = threadIdx.x - 32;
+            const int which[kNC] = {kCntVisited, kCntScreened, kCntCached, kCntSlots, kCntBoundary, kCntTargets,
+                                    kCntCand};
+            unsigned t = 0;
+            for (int w = 0; w < 8; w++) t += s_cnt[w][c];
+            if (t) atomicAdd(ctr(st.counters, which[c]), (unsigned long long)t);
         }
         __syncthreads();
         if (my_cand >= 0) st.cand_list[s_base + s_wc[wid] + __popc(bal & ((1u << lane) - 1u))] = my_cand;
     }
-    warp_count(ctr(st.counters, kCntVisited), in ? 1u : 0u);
-    warp_count(ctr(st.counters, kCntScreened), n_scr);
-    warp_count(ctr(st.counters, kCntSlots), n_slots);
-    warp_count(ctr(st.counters, kCntBoundary), n_bnd);
-    warp_count(ctr(st.counters, kCntTargets), n_tgt);
-    warp_count(ctr(st.counters, kCntCand), n_cand);
 }
 
 // blocks per SM the evaluation kernel is compiled for (registers per thread
@@ -716,7 +796,7 @@ ACVD_DEV void apply_range(const DevState& st, int item0, int color, int round, i
         if (L >= st.k) {
             // unassigned item joining a cluster: always committed
             if (role == 0) {
-                st.claim[B] = 0ull;              // taken for the rest of this step
+                st.claim[B] = claim_taken(color);   // taken for the rest of this step
                 cand_dest[idx] = -1;
                 won_total++;
                 st.label[i] = B;
@@ -756,7 +836,7 @@ ACVD_DEV void apply_range(const DevState& st, int item0, int color, int round, i
             st.energy[C] = en_mine;
             st.size[C] += role ? -1 : 1;
             st.stamp[C] = now;
-            st.claim[C] = 0ull;                  // taken for the rest of this step
+            st.claim[C] = claim_taken(color);   // taken for the rest of this step
             if (role == 0) {
                 won_total++;
                 st.label[i] = B;
@@ -764,7 +844,7 @@ ACVD_DEV void apply_range(const DevState& st, int item0, int color, int round, i
                 cand_dest[idx] = -1;
             }
         } else {
-            st.claim[C] = 0ull;
+            st.claim[C] = claim_taken(color);
             if (role == 0) {
                 cand_dest[idx] = -1;
                 atomicAdd(ctr(st.counters, kCntReverted), 1ull);
@@ -795,7 +875,8 @@ ACVD_DEV void reclaim_range(const DevState& st, int item0, int color, int round,
         const int B = cand_dest[idx];
         if (B < 0) continue;
         const int L = st.label[item0 + idx];
-        if (st.claim[B] == 0ull || (L < st.k && st.claim[L] == 0ull)) {
+        const unsigned long long taken = claim_taken(color);
+        if (st.claim[B] == taken || (L < st.k && st.claim[L] == taken)) {
             cand_dest[idx] = -1;
             continue;
         }
@@ -966,11 +1047,16 @@ __global__ void __launch_bounds__(256) fx_maxabs_kernel(DevState st, unsigned* _
     if (threadIdx.x < NA) atomicMax(&maxbits[threadIdx.x], s_mx[threadIdx.x]);
 }
 
-__global__ void begin_sweep_kernel(DevState st, int ncolors) {
+__global__ void begin_sweep_kernel(DevState st, int ncolors, int reset_claims) {
     const int t = threadIdx.x;
-    if (t == 0) st.sweep->sweep += 1;
-    if (t < ncolors) st.cand_count[t] = 0u;
-    if (t < kStripes) st.counters[t * kNumCounters + kCntMoves] = 0ull;   // this sweep's moves
+    if (blockIdx.x == 0) {
+        if (t == 0) st.sweep->sweep += 1;
+        if (t < ncolors) st.cand_count[t] = 0u;
+        if (t < kStripes) st.counters[t * kNumCounters + kCntMoves] = 0ull;   // this sweep's moves
+    }
+    if (reset_claims)
+        for (int64_t k = (int64_t)blockIdx.x * blockDim.x + t; k <= st.k; k += (int64_t)gridDim.x * blockDim.x)
+            st.claim[k] = ~0ull;
 }
 
 // ---------------------------------------------------------------------------
@@ -1502,9 +1588,11 @@ cudaError_t launch_fx_scale(int metric, const DevState& st, unsigned* maxbits, c
     return cudaGetLastError();
 }
 
-cudaError_t launch_begin_sweep(const DevState& st, int ncolors, cudaStream_t s) {
+cudaError_t launch_begin_sweep(const DevState& st, int ncolors, bool reset_claims, cudaStream_t s) {
     ++g_launches;
-    begin_sweep_kernel<<<1, 64, 0, s>>>(st, ncolors);
+    // 64 threads per block cover the colour counts and counter stripes in block 0
+    const unsigned grid = reset_claims ? (unsigned)std::min<int64_t>(nblk(st.k + 1, 64), 4 * 152) : 1u;
+    begin_sweep_kernel<<<grid, 64, 0, s>>>(st, ncolors, reset_claims ? 1 : 0);
     return cudaGetLastError();
 }
 

@@ -66,6 +66,7 @@ struct acvd_ctx {
     DBuf<float> curv_dirs;
     DBuf<char> curv_faces;
     DBuf<unsigned char> bflag;     // per item: maybe on a cluster boundary
+    DBuf<int4> tcache;             // per item: cached boundary screen
     // sweep classes: either the colour classes, or one class holding every item
     // (claims alone keep committed moves on disjoint clusters; colours are kept
     // for hole filling)
@@ -186,6 +187,7 @@ struct acvd_ctx {
         st.out_done = out_done.p;
         st.ring8 = ring8.p;
         st.bflag = bflag.p;
+        st.tcache = tcache.p;
         st.orig = perm.p;
         st.inv = inv.p;
         st.frozen = has_frozen ? frozen.p : nullptr;
@@ -247,6 +249,7 @@ static int set_sweep_state(acvd_ctx* ctx, int sweep, int floor) {
     SweepState h{sweep, floor};
     CK(cudaMemcpyAsync(ctx->dsweep.p, &h, sizeof h, cudaMemcpyHostToDevice, ctx->s));
     CK(ctx->bflag.resize(ctx->nV));
+    CK(ctx->tcache.resize(ctx->nV));
     CK(cudaMemsetAsync(ctx->bflag.p, 1, ctx->nV, ctx->s));
     CK(cudaStreamSynchronize(ctx->s));
     return ACVD_OK;
@@ -763,13 +766,12 @@ static int clean(acvd_ctx* ctx, int* n_disconnected) {
 // are recorded inside the captured graph and read after the sweep's sync.
 static int enqueue_sweep(acvd_ctx* ctx, bool timing, bool relaxed) {
     DevState st = ctx->state();
-    CK(launch_begin_sweep(st, ctx->nclasses, ctx->s));
+    CK(launch_begin_sweep(st, ctx->nclasses, !relaxed, ctx->s));   // exact sweeps: claims reset once
     int64_t kernels = 1;
     for (int c = 0; c < ctx->nclasses; c++) {
         const int item0 = (int)ctx->sweep_off[c];   // classes are contiguous item ranges
         const int64_t cnt = ctx->sweep_off[c + 1] - ctx->sweep_off[c];
         if (cnt == 0) continue;
-        if (!relaxed) CK(cudaMemsetAsync(ctx->claim.p, 0xff, (ctx->K + 1) * sizeof(unsigned long long), ctx->s));
         // cudaEventRecordExternal makes the records real graph nodes when captured
         if (timing) CK(cudaEventRecordWithFlags(ctx->ev_eval[2 * c], ctx->s, cudaEventRecordExternal));
         CK(launch_eval(ctx->metric, st, item0, cnt, c, ctx->cand_dest.p, ctx->cand_prio.p, !relaxed, ctx->s));
@@ -1048,11 +1050,12 @@ extern "C" int acvd_minimize(acvd_ctx* ctx, acvd_stats* stats) {
                 const auto now = std::chrono::steady_clock::now();
                 std::fprintf(stderr,
                              "acvd sweep %d %s %.3f ms moves %lld cand %llu boundary %llu targets %llu visited %llu "
-                             "reverted %llu conv %d flags %d%d\n",
+                             "screened %llu cached %llu reverted %llu conv %d flags %d%d\n",
                              sweeps, relaxed ? "relaxed" : "exact",
                              std::chrono::duration<double, std::milli>(now - t_trace).count(), (long long)mods,
                              ctx->h_counters[kCntCand], ctx->h_counters[kCntBoundary], ctx->h_counters[kCntTargets],
-                             ctx->h_counters[kCntVisited], ctx->h_counters[kCntReverted], convergences,
+                             ctx->h_counters[kCntVisited], ctx->h_counters[kCntScreened], ctx->h_counters[kCntCached],
+                             ctx->h_counters[kCntReverted], convergences,
                              ctx->flags.constrained, ctx->flags.connexity);
                 t_trace = now;
             }
@@ -1111,14 +1114,16 @@ extern "C" int acvd_minimize(acvd_ctx* ctx, acvd_stats* stats) {
     {
         // algorithmic bytes of the evaluation kernels: per visited item its boundary
         // flag; per screened item its 8-slot ring, label and evaluation sweep; per
-        // ring slot the neighbour's label; per
+        // ring slot the neighbour's label; per cached screen its cache entry, label,
+        // evaluation sweep and up to 3 cluster stamps; per
         // boundary item its record, its cluster's record and size; per destination
         // cluster its record; per proposal the candidate slots and two claim words
         const int64_t R = ctx->metric == kIso ? 16 : (ctx->metric == kQEM ? 40 : 64);
         const int64_t C = 16 * (int64_t)ev_stride(ctx->metric);
         const int64_t screened = (int64_t)ctx->h_counters[kCntScreened];
-        local.eval_bytes = 1 * local.visited + 40 * screened + 4 * local.slots + (R + C + 4) * local.boundary_items +
-                           C * local.targets + 24 * local.candidates;
+        const int64_t cached = (int64_t)ctx->h_counters[kCntCached];
+        local.eval_bytes = 1 * local.visited + 40 * screened + 36 * cached + 4 * local.slots +
+                           (R + C + 4) * local.boundary_items + C * local.targets + 24 * local.candidates;
     }
     if (status == ACVD_OK) {
         double et = 0.0;

@@ -33,6 +33,14 @@ enum Metric { kIso = 0, kQEM = 1, kAniso = 2 };
 // most 64 colours, so epochs fit the claim word's 8-bit field).
 constexpr int kRounds = 4;
 
+// A cluster taken by a commit keeps this value for the rest of the colour step: it
+// is below every claim of the step's rounds (same or older epoch; a real claim's
+// priority is never 0) and above every claim of the following steps, so claims need
+// resetting once per sweep only.
+ACVD_HD unsigned long long claim_taken(int color) {
+    return make_claim((unsigned)(color * kRounds + kRounds - 1), 0u, 0u);
+}
+
 template <int M> struct Layout;
 template <> struct Layout<kIso> { static constexpr int acc = 4, ev = 1; };
 template <> struct Layout<kQEM> { static constexpr int acc = 13, ev = 5; };
@@ -64,6 +72,7 @@ enum Counter {
     kCntAssigned = 9,
     kCntReverted = 10,   // commits undone because the pair's energy did not decrease
     kCntScreened = 11,   // visited items whose boundary flag sent them to the ring screen
+    kCntCached = 12,     // ring screens answered from the item's screen cache
     kNumCounters = 16
 };
 
@@ -117,11 +126,16 @@ struct DevState {
     int* in_done;          // committed moves into the cluster
     int* out_done;         // committed moves out of the cluster
     // per item: 0 = certainly interior (every ring label equals its own), 1 = maybe
-    // on a cluster boundary.  A commit sets it on the moved item and its ring; the
-    // ring screen clears it when it finds the item interior.  The reference keeps
-    // only boundary edges in its queue and re-queues a moved item's ring
+    // on a cluster boundary, 2 = on a boundary with its screen in tcache.  A commit
+    // sets 1 on the moved item and its ring; the ring screen sets 0 when it finds the
+    // item interior, 2 when it caches the screen.  The reference keeps only boundary
+    // edges in its queue and re-queues a moved item's ring
     // (vtkUniformClustering.h:858-872, 971, 985).
     unsigned char* bflag;
+    // per item with bflag 2: its distinct neighbour clusters (x, y, z; ring order) and
+    // w = count | 4 if the connectivity test is known | 8 if it passed.  Valid while
+    // no label in the ring changes.
+    int4* tcache;
     // per item, the first 8 ring neighbours (two int4, ring order, -1 padded; slot
     // 7 = -2 when the ring is longer than 8, which then is read from row / col)
     const int4* ring8;
@@ -219,7 +233,7 @@ cudaError_t launch_ring8(const int* row, const int* col, int64_t n, int* ring8, 
 // ---- clustering (cluster.cu) ----
 // The sweep kernels take a colour class as the contiguous item range
 // [item0, item0 + count) of the internal order.
-cudaError_t launch_begin_sweep(const DevState& st, int ncolors, cudaStream_t s);
+cudaError_t launch_begin_sweep(const DevState& st, int ncolors, bool reset_claims, cudaStream_t s);
 cudaError_t launch_relaxed_step(int metric, const DevState& st, int item0, int64_t count, int color,
                                 const int* cand_dest, cudaStream_t s);
 cudaError_t launch_fx_scale(int metric, const DevState& st, unsigned* maxbits, cudaStream_t s);
