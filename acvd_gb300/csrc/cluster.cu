@@ -1225,6 +1225,56 @@ __global__ void __launch_bounds__(256, 2) sweep_run_kernel(SweepRun a) {
 }
 
 // ---------------------------------------------------------------------------
+// Device-side sweep loop: a CUDA-graph WHILE node repeats an IF / ELSE of the
+// relaxed and the exact sweep; these single-thread kernels take, on the device,
+// the decisions the host loop takes after each sweep (the same ones as block 0 of
+// the persistent kernel), so the sweeps between two convergence events run without
+// returning to the host.
+// ---------------------------------------------------------------------------
+__global__ void loop_start_kernel(const LoopState* ls, const RunFlags* flags, cudaGraphConditionalHandle h_loop,
+                                  cudaGraphConditionalHandle h_mode) {
+    cudaGraphSetConditional(h_loop, 1u);
+    cudaGraphSetConditional(h_mode, (ls->relaxed_ok && !flags->connexity) ? 1u : 0u);
+}
+
+__global__ void loop_decide_kernel(LoopState* L, const unsigned long long* counters, const double* e_now,
+                                   const RunFlags* flags, int relaxed, cudaGraphConditionalHandle h_loop,
+                                   cudaGraphConditionalHandle h_mode) {
+    long long mods = 0;
+    for (int q = 0; q < kStripes; q++) mods += (long long)counters[q * kNumCounters + kCntMoves];
+    if (relaxed) {
+        const double e = *e_now;
+        if (L->have_prev && !(e < L->e_prev)) L->relaxed_ok = 0;
+        L->e_prev = e;
+        L->have_prev = 1;
+        L->relaxed_run += 1;
+    }
+    L->sweeps += 1;
+    L->run += 1;
+    L->moves += mods;
+    L->last_moves = mods;
+    const bool stop = mods == 0 || L->sweeps > L->max_loops || (mods <= L->early / 1000 && L->convergences <= 1);
+    if (stop) L->status = 1;
+    cudaGraphSetConditional(h_loop, stop ? 0u : 1u);
+    cudaGraphSetConditional(h_mode, (L->relaxed_ok && !flags->connexity) ? 1u : 0u);
+}
+
+cudaError_t launch_loop_start(const LoopState* ls, const RunFlags* flags, cudaGraphConditionalHandle h_loop,
+                              cudaGraphConditionalHandle h_mode, cudaStream_t s) {
+    ++g_launches;
+    loop_start_kernel<<<1, 1, 0, s>>>(ls, flags, h_loop, h_mode);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_loop_decide(LoopState* ls, const unsigned long long* counters, const double* e_now,
+                               const RunFlags* flags, bool relaxed, cudaGraphConditionalHandle h_loop,
+                               cudaGraphConditionalHandle h_mode, cudaStream_t s) {
+    ++g_launches;
+    loop_decide_kernel<<<1, 1, 0, s>>>(ls, counters, e_now, flags, relaxed ? 1 : 0, h_loop, h_mode);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
 // full recompute of the accumulators: items sorted by cluster, one warp per
 // cluster, fixed-order butterfly reduction (deterministic)
 // ---------------------------------------------------------------------------

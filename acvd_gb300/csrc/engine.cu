@@ -127,6 +127,7 @@ struct acvd_ctx {
     bool timing_broken = false;    // event timing unavailable on this device / driver
     int match_rounds = 1;          // claim/commit rounds per colour step (ACVD_MATCH_ROUNDS, up to kRounds)
     int64_t sweep_kernels = 0;     // kernels in the sweep last enqueued
+    int64_t loop_relaxed_kernels = 0, loop_exact_kernels = 0;   // kernels per sweep of the graph loop
     int64_t exact_kernels = 0, relaxed_kernels = 0;
     DBuf<int> label_init;          // the assignment given to acvd_set_labels (for acvd_rewind)
     DBuf<unsigned char> frozen;    // per cluster (K + 1): IsClusterFreezed; used when has_frozen
@@ -194,11 +195,17 @@ struct acvd_ctx {
         return st;
     }
     cudaGraphExec_t relaxed_exec = nullptr;
+    cudaGraphExec_t loop_exec = nullptr;   // device-side sweep loop (WHILE around relaxed / exact sweep)
+    DBuf<double> loop_energy;              // energy after the loop's last relaxed sweep
+    Scratch loop_scratch;                  // the loop graph's own summation scratch (never shared,
+                                           // so no other call can move it under the graph)
     void drop_graph() {
         if (sweep_exec) cudaGraphExecDestroy(sweep_exec);
         sweep_exec = nullptr;
         if (relaxed_exec) cudaGraphExecDestroy(relaxed_exec);
         relaxed_exec = nullptr;
+        if (loop_exec) cudaGraphExecDestroy(loop_exec);
+        loop_exec = nullptr;
     }
     void drop_events() {
         for (cudaEvent_t e : ev_eval) cudaEventDestroy(e);
@@ -616,8 +623,6 @@ int acvd_set_labels(acvd_ctx* ctx, int32_t k, const int32_t* labels) {
     if (!ctx->ready_mesh) return fail(ctx, ACVD_ERR_ARG, "acvd_set_labels before acvd_set_mesh");
     if (k <= 0 || !labels) return fail(ctx, ACVD_ERR_ARG, "acvd_set_labels: K must be positive");
     if (k >= (1 << 21)) return fail(ctx, ACVD_ERR_UNSUPPORTED, "more than 2^21 clusters");
-    for (int64_t i = 0; i < ctx->nV; i++)
-        if (labels[i] < 0 || labels[i] > k) return fail(ctx, ACVD_ERR_ARG, "label outside [0, K]");
     CK(cudaSetDevice(ctx->opts.device));
     if (ctx->K != k || ctx->has_frozen) ctx->drop_graph();
     ctx->has_frozen = false;   // a new clustering starts with no frozen cluster
@@ -638,9 +643,19 @@ int acvd_set_labels(acvd_ctx* ctx, int32_t k, const int32_t* labels) {
     CK(ctx->label_init.resize(ctx->nV));
     CK(ctx->label_orig.resize(ctx->nV));
     CK(cudaMemcpyAsync(ctx->label_orig.p, labels, ctx->nV * sizeof(int), cudaMemcpyHostToDevice, ctx->s));
-    CK(launch_gather_i32(ctx->label_orig.p, ctx->perm.p, ctx->nV, ctx->label.p, ctx->s));
+    // the range check runs in the gather: a label outside [0, K] fails the call
+    CK(ctx->dtmp.resize(2));
+    unsigned* bad = (unsigned*)ctx->dtmp.p;
+    CK(cudaMemsetAsync(bad, 0, sizeof(unsigned), ctx->s));
+    CK(launch_gather_labels(ctx->label_orig.p, ctx->perm.p, ctx->nV, k, ctx->label.p, bad, ctx->s));
     CK(cudaMemcpyAsync(ctx->label_init.p, ctx->label.p, ctx->nV * sizeof(int), cudaMemcpyDeviceToDevice, ctx->s));
+    unsigned h_bad = 0;
+    CK(cudaMemcpyAsync(&h_bad, bad, sizeof h_bad, cudaMemcpyDeviceToHost, ctx->s));
     CK(cudaStreamSynchronize(ctx->s));
+    if (h_bad) {
+        ctx->ready_labels = false;
+        return fail(ctx, ACVD_ERR_ARG, std::to_string(h_bad) + " labels outside [0, K]");
+    }
     ctx->ready_labels = true;
     return ACVD_OK;
 }
@@ -844,6 +859,100 @@ static int run_sweep(acvd_ctx* ctx, bool timing, bool relaxed, double* eval_ms, 
     return ACVD_OK;
 }
 
+// The sweeps between two convergence events as one graph: a kernel sets the loop
+// and mode conditions, then a WHILE node repeats an IF / ELSE whose bodies are the
+// relaxed sweep (+ the energy sum) and the exact sweep, each ending with the
+// decision kernel.  Built once per context (dropped with the sweep graphs).
+static int build_loop_graph(acvd_ctx* ctx) {
+    CK(ctx->dls.resize(1));
+    CK(ctx->loop_energy.resize(1));
+    // sizes the loop's summation scratch outside the capture
+    CK(sum_f64(ctx->energy.p, ctx->K, ctx->loop_energy.p, ctx->loop_scratch, ctx->s));
+    CK(cudaStreamSynchronize(ctx->s));
+    int r = ACVD_OK;
+    cudaGraph_t g;
+    CK(cudaGraphCreate(&g, 0));
+    cudaGraphConditionalHandle h_loop, h_mode;
+    CK(cudaGraphConditionalHandleCreate(&h_loop, g, 0, 0));
+    CK(cudaGraphConditionalHandleCreate(&h_mode, g, 0, 0));
+    const long long before = g_launches;
+    auto fail_capture = [&](int code) {
+        cudaGraph_t junk;
+        cudaStreamEndCapture(ctx->s, &junk);
+        cudaGraphDestroy(g);
+        g_launches = before;
+        return code;
+    };
+    CK(cudaStreamBeginCaptureToGraph(ctx->s, g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    if (launch_loop_start(ctx->dls.p, ctx->dflags.p, h_loop, h_mode, ctx->s) != cudaSuccess)
+        return fail_capture(fail(ctx, ACVD_ERR_CUDA, "loop graph: start kernel"));
+    cudaGraph_t g2;
+    CK(cudaStreamEndCapture(ctx->s, &g2));
+    size_t n = 0;
+    CK(cudaGraphGetNodes(g, nullptr, &n));
+    std::vector<cudaGraphNode_t> roots(n);
+    CK(cudaGraphGetNodes(g, roots.data(), &n));
+    cudaGraphNodeParams wp = {};
+    wp.type = cudaGraphNodeTypeConditional;
+    wp.conditional.handle = h_loop;
+    wp.conditional.type = cudaGraphCondTypeWhile;
+    wp.conditional.size = 1;
+    cudaGraphNode_t wnode;
+    CK(cudaGraphAddNode(&wnode, g, roots.data(), nullptr, n, &wp));
+    cudaGraph_t body = wp.conditional.phGraph_out[0];
+    cudaGraphNodeParams ip = {};
+    ip.type = cudaGraphNodeTypeConditional;
+    ip.conditional.handle = h_mode;
+    ip.conditional.type = cudaGraphCondTypeIf;
+    ip.conditional.size = 2;
+    cudaGraphNode_t inode;
+    CK(cudaGraphAddNode(&inode, body, nullptr, nullptr, 0, &ip));
+    for (int b = 0; b < 2; b++) {
+        const bool relaxed = b == 0;   // IF body: relaxed sweep; ELSE body: exact sweep
+        cudaGraph_t bg = ip.conditional.phGraph_out[b];
+        const long long k0 = g_launches;
+        CK(cudaStreamBeginCaptureToGraph(ctx->s, bg, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+        if ((r = enqueue_sweep(ctx, false, relaxed))) return fail_capture(r);
+        if (relaxed && sum_f64(ctx->energy.p, ctx->K, ctx->loop_energy.p, ctx->loop_scratch, ctx->s) != cudaSuccess)
+            return fail_capture(fail(ctx, ACVD_ERR_CUDA, "loop graph: energy sum"));
+        if (launch_loop_decide(ctx->dls.p, ctx->counters.p, ctx->loop_energy.p, ctx->dflags.p, relaxed, h_loop,
+                               h_mode, ctx->s) != cudaSuccess)
+            return fail_capture(fail(ctx, ACVD_ERR_CUDA, "loop graph: decision kernel"));
+        cudaGraph_t bg2;
+        CK(cudaStreamEndCapture(ctx->s, &bg2));
+        (relaxed ? ctx->loop_relaxed_kernels : ctx->loop_exact_kernels) = g_launches - k0;
+    }
+    g_launches = before;
+    cudaError_t e = cudaGraphInstantiate(&ctx->loop_exec, g, 0);
+    cudaGraphDestroy(g);
+    CK(e);
+    return ACVD_OK;
+}
+
+// Runs the device-side loop from the host's loop state; hl comes back updated.
+static int run_sweeps_graph(acvd_ctx* ctx, LoopState& hl, acvd_stats& local) {
+    if (!ctx->loop_exec) {
+        int r = build_loop_graph(ctx);
+        if (r) return r;
+    }
+    hl.status = 0;
+    hl.run = 0;
+    hl.relaxed_run = 0;
+    hl.moves = 0;
+    hl.last_moves = 0;
+    hl.eval_ns = 0;
+    CK(cudaMemcpyAsync(ctx->dls.p, &hl, sizeof hl, cudaMemcpyHostToDevice, ctx->s));
+    CK(cudaGraphLaunch(ctx->loop_exec, ctx->s));
+    CK(cudaMemcpyAsync(&hl, ctx->dls.p, sizeof hl, cudaMemcpyDeviceToHost, ctx->s));
+    int r = sync_counters(ctx);
+    if (r) return r;
+    g_launches += 1 + (int64_t)hl.relaxed_run * ctx->loop_relaxed_kernels +
+                  (int64_t)(hl.run - hl.relaxed_run) * ctx->loop_exact_kernels;
+    local.relaxed_sweeps += hl.relaxed_run;
+    local.moves += hl.moves;
+    return ACVD_OK;
+}
+
 constexpr int kSweepLogCap = 1 << 16;
 
 // Grid of the persistent sweep kernel on this device: every SM times the
@@ -992,6 +1101,9 @@ extern "C" int acvd_minimize(acvd_ctx* ctx, acvd_stats* stats) {
         const bool trace = std::getenv("ACVD_TRACE") != nullptr;
         auto t_trace = std::chrono::steady_clock::now();
         const bool persistent = ctx->opts.persistent && sweep_run_grid(ctx) > 0;
+        // graph-looped sweeps unless per-sweep events or the per-sweep trace are wanted
+        const bool device_loop = !persistent && !timing && !trace && ctx->opts.use_graphs &&
+                                 std::getenv("ACVD_HOST_LOOP") == nullptr;
         for (;;) {
             int64_t mods = 0;
             const bool relaxed = relaxed_ok && !ctx->flags.connexity;
@@ -1033,6 +1145,23 @@ extern "C" int acvd_minimize(acvd_ctx* ctx, acvd_stats* stats) {
                 local.relaxed_sweeps += hl.relaxed_run;
                 local.moves += hl.moves;
                 mods = hl.last_moves;
+            } else if (device_loop) {
+                // every sweep up to the next convergence test, looped on the device by the graph
+                LoopState hl;
+                std::memset(&hl, 0, sizeof hl);
+                hl.early = early;
+                hl.sweeps = sweeps;
+                hl.max_loops = ctx->opts.max_loops;
+                hl.convergences = convergences;
+                hl.relaxed_ok = relaxed_ok ? 1 : 0;
+                hl.have_prev = have_prev ? 1 : 0;
+                hl.e_prev = e_prev;
+                if ((r = run_sweeps_graph(ctx, hl, local))) { status = r; break; }
+                sweeps = hl.sweeps;
+                relaxed_ok = hl.relaxed_ok != 0;
+                have_prev = hl.have_prev != 0;
+                e_prev = hl.e_prev;
+                mods = hl.last_moves;
             } else {
             if ((r = run_sweep(ctx, timing, relaxed, &local.eval_ms, &local.eval_launches, &mods))) { status = r; break; }
             if (relaxed) {
@@ -1046,7 +1175,7 @@ extern "C" int acvd_minimize(acvd_ctx* ctx, acvd_stats* stats) {
             sweeps++;
             local.moves += mods;
             }
-            if (trace && !persistent) {
+            if (trace && !persistent && !device_loop) {
                 const auto now = std::chrono::steady_clock::now();
                 std::fprintf(stderr,
                              "acvd sweep %d %s %.3f ms moves %lld cand %llu boundary %llu targets %llu visited %llu "

@@ -224,6 +224,9 @@ cudaError_t launch_perm_degree(const int* row, const int* perm, int64_t n, uint3
 cudaError_t launch_perm_ring(const int* row, const int* col, const int* perm, const int* inv, const uint32_t* row_new,
                              int64_t n, int* col_new, cudaStream_t s);
 cudaError_t launch_map_ids(const int* in, int64_t m, const int* inv, int* out, cudaStream_t s);
+// gather of labels that also counts those outside [0, k] in *bad
+cudaError_t launch_gather_labels(const int* src, const int* idx, int64_t n, int k, int* dst, unsigned* bad,
+                                 cudaStream_t s);
 cudaError_t launch_gather_i32(const int* src, const int* idx, int64_t n, int* dst, cudaStream_t s);
 cudaError_t launch_gather_f4(const float4* src, const int* idx, int64_t n, float4* dst, cudaStream_t s);
 cudaError_t launch_gather_f2(const float2* src, const int* idx, int64_t n, float2* dst, cudaStream_t s);
@@ -234,6 +237,13 @@ cudaError_t launch_ring8(const int* row, const int* col, int64_t n, int* ring8, 
 // The sweep kernels take a colour class as the contiguous item range
 // [item0, item0 + count) of the internal order.
 cudaError_t launch_begin_sweep(const DevState& st, int ncolors, bool reset_claims, cudaStream_t s);
+// device-side sweep loop (graph WHILE node): set the loop and mode conditions at the
+// start, and after each sweep (relaxed: e_now holds the energy after the sweep)
+cudaError_t launch_loop_start(const LoopState* ls, const RunFlags* flags, cudaGraphConditionalHandle h_loop,
+                              cudaGraphConditionalHandle h_mode, cudaStream_t s);
+cudaError_t launch_loop_decide(LoopState* ls, const unsigned long long* counters, const double* e_now,
+                               const RunFlags* flags, bool relaxed, cudaGraphConditionalHandle h_loop,
+                               cudaGraphConditionalHandle h_mode, cudaStream_t s);
 cudaError_t launch_relaxed_step(int metric, const DevState& st, int item0, int64_t count, int color,
                                 const int* cand_dest, cudaStream_t s);
 cudaError_t launch_fx_scale(int metric, const DevState& st, unsigned* maxbits, cudaStream_t s);

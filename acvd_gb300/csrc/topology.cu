@@ -420,6 +420,24 @@ cudaError_t launch_gather_i32(const int* src, const int* idx, int64_t n, int* ds
     return cudaGetLastError();
 }
 
+// dst[t] = src[idx[t]] for labels, counting the values outside [0, k] in *bad
+__global__ void gather_labels_kernel(const int* __restrict__ src, const int* __restrict__ idx, int64_t n, int k,
+                                     int* __restrict__ dst, unsigned* __restrict__ bad) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const int v = src[idx[t]];
+    dst[t] = v;
+    if (v < 0 || v > k) atomicAdd(bad, 1u);
+}
+
+cudaError_t launch_gather_labels(const int* src, const int* idx, int64_t n, int k, int* dst, unsigned* bad,
+                                 cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    ++g_launches;
+    gather_labels_kernel<<<grid_of(n), 256, 0, s>>>(src, idx, n, k, dst, bad);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_gather_f4(const float4* src, const int* idx, int64_t n, float4* dst, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
     ++g_launches;
