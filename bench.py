@@ -50,6 +50,12 @@ WORKLOADS = {
                                    # the sequential CPU solve of the full mesh takes far longer than the
                                    # bench budget: time a 1024^2 patch with the same items per cluster
                                    cpu_sample=dict(mesh=dict(n=1024, seed=0), k=12500)),
+    # the 4096^2 workload at a quarter of the items (same items per cluster): small enough
+    # for multi-pass ncu captures, whose per-launch figures scale to the full mesh
+    "heightfield_2048_aniso": dict(kind="heightfield", mesh=dict(n=2048, seed=0), metric="aniso", k=50000,
+                                   gradation=1.5, uinit=0,
+                                   desc="quadric-anisotropic heightfield 2048^2 (4,194,304 items), K=50,000",
+                                   cpu_sample=dict(mesh=dict(n=512, seed=0), k=3125)),
 }
 
 
@@ -815,6 +821,25 @@ def run_gpu_arm(args):
     print(json.dumps(line), flush=True)
 
 
+def solve_once(args):
+    """One engine set-up and one converged solve of a clustering workload, untimed: the
+    program that ncu captures are taken on (launch lists, per-launch DRAM traffic)."""
+    import acvd_gb300
+    from acvd_gb300 import engine as E
+    m, ind, pd, w = make_workload(args.workload)
+    lab0, (row, col, ev) = initial_labels(m, w["metric"], ind, w["gradation"], w["k"], w.get("init"))
+    e = E.Engine()
+    e.set_mesh(m.points, m.faces, row, col, ev)
+    e.set_metric(w["metric"], ind, pd, w["gradation"])
+    e.set_unconstrained_initialization(w["uinit"])
+    e.set_labels(w["k"], lab0)
+    st = e.minimize()
+    e.close()
+    print(json.dumps({"workload": args.workload, "sweeps": st["sweeps"], "moves": st["moves"],
+                      "device_ms": st["device_ms"], "eval_bytes": st["eval_bytes"],
+                      "kernel_launches": st["kernel_launches"]}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -829,7 +854,14 @@ def main():
                     sorted(CURVATURE_WORKLOADS))
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--solve-once", action="store_true",
+                    help="set up and run one converged solve of a clustering workload, untimed (for ncu)")
     args = ap.parse_args()
+    if args.solve_once:
+        if args.workload not in WORKLOADS:
+            raise SystemExit("--solve-once takes a clustering workload")
+        solve_once(args)
+        return
     if args.impl == "reference" and args.workload in CURVATURE_WORKLOADS:
         run_curvature_reference_arm(args)
     elif args.impl == "reference":
