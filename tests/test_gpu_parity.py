@@ -252,6 +252,41 @@ def test_persistent_schedule_matches_per_phase_kernels(oracle_lib, case):
     assert st_p["energy"] == st_k["energy"]
 
 
+@pytest.mark.parametrize("case", [RUNS[0], RUNS[2], RUNS[4]], ids=[RUNS[i][0] for i in (0, 2, 4)])
+def test_device_loop_matches_host_loop(oracle_lib, case, monkeypatch):
+    """The sweeps between convergence events looped on the device (graph WHILE node
+    with decision kernels) take the host loop's decisions: the clusterings, energies
+    and counts are identical."""
+    name, metric, mk, k, grad, uinit, seeds = case
+    m = mk()
+    ind = m.indicator if (grad > 0 or metric == "aniso") else None
+    pd = m.principal_dirs if metric == "aniso" else None
+    init = synth.seed_labels(m.n_points, k, seed=11) if seeds else None
+    ref = oracle_lib.Port(metric, m.points, m.faces, k, grad, ind, pd, unconstrained_init=uinit)
+    ref.init(init)
+    lab0 = ref.labels()
+    row, col, ev = acvd_gb300.build_topology(m.n_points, m.faces)
+    out = []
+    for host_loop in (True, False):
+        if host_loop:
+            monkeypatch.setenv("ACVD_HOST_LOOP", "1")
+        else:
+            monkeypatch.delenv("ACVD_HOST_LOOP", raising=False)
+        e = acvd_gb300.Engine()
+        e.set_mesh(m.points, m.faces, row, col, ev)
+        e.set_metric(metric, ind, pd, grad)
+        e.set_unconstrained_initialization(uinit)
+        e.set_labels(k, lab0)
+        st = e.minimize()
+        out.append((e.labels(), st))
+        e.close()
+    (lab_h, st_h), (lab_d, st_d) = out
+    np.testing.assert_array_equal(lab_h, lab_d)
+    for key in ("sweeps", "moves", "relaxed_sweeps", "convergences", "candidates", "reverted"):
+        assert st_h[key] == st_d[key], (key, st_h[key], st_d[key])
+    assert st_h["energy"] == st_d["energy"]
+
+
 @pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p)[:-4] for p in GOLDEN])
 def test_post_placement_matches_reference(path):
     """ACVD's quadric post-placement (ACVD.cxx:217-291) of the reference's fixed
