@@ -1641,7 +1641,7 @@ cudaError_t launch_fx_scale(int metric, const DevState& st, unsigned* maxbits, c
 cudaError_t launch_begin_sweep(const DevState& st, int ncolors, bool reset_claims, cudaStream_t s) {
     ++g_launches;
     // 64 threads per block cover the colour counts and counter stripes in block 0
-    const unsigned grid = reset_claims ? (unsigned)std::min<int64_t>(nblk(st.k + 1, 64), 4 * 152) : 1u;
+    const unsigned grid = reset_claims ? (unsigned)std::min<int64_t>(nblk(st.k + 1, 64), 4 * (int64_t)sm_count()) : 1u;
     begin_sweep_kernel<<<grid, 64, 0, s>>>(st, ncolors, reset_claims ? 1 : 0);
     return cudaGetLastError();
 }
