@@ -1600,13 +1600,17 @@ cudaError_t launch_eval(int metric, const DevState& st, int item0, int64_t count
     return cudaGetLastError();
 }
 
-static unsigned list_grid(int64_t count) {
-    // the proposal count is only known on the device: a grid of 2 blocks per SM
-    // strides over the list
+static int64_t sm_count() {
     int dev = 0, sms = 152;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    return (unsigned)std::min<int64_t>(nblk(count), 2 * (int64_t)sms);
+    return sms;
+}
+
+static unsigned list_grid(int64_t count) {
+    // the proposal count is only known on the device: a grid of 2 blocks per SM
+    // strides over the list
+    return (unsigned)std::min<int64_t>(nblk(count), 2 * sm_count());
 }
 
 cudaError_t launch_apply(int metric, const DevState& st, int item0, int64_t count, int color, int round,
@@ -1641,7 +1645,7 @@ cudaError_t launch_fx_scale(int metric, const DevState& st, unsigned* maxbits, c
 cudaError_t launch_begin_sweep(const DevState& st, int ncolors, bool reset_claims, cudaStream_t s) {
     ++g_launches;
     // 64 threads per block cover the colour counts and counter stripes in block 0
-    const unsigned grid = reset_claims ? (unsigned)std::min<int64_t>(nblk(st.k + 1, 64), 4 * (int64_t)sm_count()) : 1u;
+    const unsigned grid = reset_claims ? (unsigned)std::min<int64_t>(nblk(st.k + 1, 64), 4 * sm_count()) : 1u;
     begin_sweep_kernel<<<grid, 64, 0, s>>>(st, ncolors, reset_claims ? 1 : 0);
     return cudaGetLastError();
 }
