@@ -1425,11 +1425,12 @@ extern "C" int acvd_subdivide(acvd_ctx* ctx, int64_t n_vertices, const double* x
     CK(cudaSetDevice(ctx->opts.device));
     const int64_t nv = n_vertices, nf = n_faces, ne = n_edges, nout = n_vertices + n_edges;
     DBuf<double> d_xyz, d_ind, d_oxyz, d_oind;
-    DBuf<int> d_tri, d_row, d_col, d_ev, d_slot, d_otri, d_p1, d_p2;
-    DBuf<unsigned int> d_missing;
+    DBuf<int> d_tri, d_row, d_col, d_ev, d_otri, d_p1, d_p2;
+    DBuf<int4> d_work;
     CK(d_xyz.resize(3 * nv)); CK(d_tri.resize(3 * nf)); CK(d_row.resize(nv + 1)); CK(d_col.resize(2 * ne));
-    CK(d_ev.resize(2 * ne)); CK(d_slot.resize(2 * ne)); CK(d_oxyz.resize(3 * nout)); CK(d_otri.resize(12 * nf));
-    CK(d_p1.resize(ne)); CK(d_p2.resize(ne)); CK(d_missing.resize(1));
+    CK(d_ev.resize(2 * ne)); CK(d_oxyz.resize(3 * nout)); CK(d_otri.resize(12 * nf));
+    CK(d_p1.resize(ne)); CK(d_p2.resize(ne));
+    CK(d_work.resize((acvd_subdivide_work_bytes(ne) + 15) / 16));
     if (indicator) { CK(d_ind.resize(nv)); CK(d_oind.resize(nout)); }
     CK(cudaMemcpyAsync(d_xyz.p, xyz, 3 * nv * sizeof(double), cudaMemcpyHostToDevice, ctx->s));
     CK(cudaMemcpyAsync(d_tri.p, tri, 3 * nf * sizeof(int), cudaMemcpyHostToDevice, ctx->s));
@@ -1437,11 +1438,11 @@ extern "C" int acvd_subdivide(acvd_ctx* ctx, int64_t n_vertices, const double* x
     CK(cudaMemcpyAsync(d_col.p, csr_col, 2 * ne * sizeof(int), cudaMemcpyHostToDevice, ctx->s));
     CK(cudaMemcpyAsync(d_ev.p, edge_v, 2 * ne * sizeof(int), cudaMemcpyHostToDevice, ctx->s));
     if (indicator) CK(cudaMemcpyAsync(d_ind.p, indicator, nv * sizeof(double), cudaMemcpyHostToDevice, ctx->s));
-    CK(cudaMemsetAsync(d_missing.p, 0, sizeof(unsigned int), ctx->s));
-    CK(launch_subdivide(d_xyz.p, nv, d_tri.p, nf, d_row.p, d_col.p, d_ev.p, ne, d_ind.p, d_slot.p, d_oxyz.p,
-                        d_otri.p, d_p1.p, d_p2.p, d_oind.p, d_missing.p, ctx->s));
+    int r = acvd_subdivide_device(ctx, nv, d_xyz.p, nf, d_tri.p, d_row.p, d_col.p, ne, d_ev.p, d_ind.p, d_oxyz.p,
+                                  d_otri.p, d_p1.p, d_p2.p, d_oind.p, d_work.p);
+    if (r) return r;
     unsigned int missing = 0;
-    CK(cudaMemcpyAsync(&missing, d_missing.p, sizeof missing, cudaMemcpyDeviceToHost, ctx->s));
+    CK(cudaMemcpyAsync(&missing, (const int*)d_work.p + 2 * ne, sizeof missing, cudaMemcpyDeviceToHost, ctx->s));
     CK(cudaMemcpyAsync(out_xyz, d_oxyz.p, 3 * nout * sizeof(double), cudaMemcpyDeviceToHost, ctx->s));
     CK(cudaMemcpyAsync(out_tri, d_otri.p, 12 * nf * sizeof(int), cudaMemcpyDeviceToHost, ctx->s));
     CK(cudaMemcpyAsync(parent1, d_p1.p, ne * sizeof(int), cudaMemcpyDeviceToHost, ctx->s));
@@ -1451,7 +1452,39 @@ extern "C" int acvd_subdivide(acvd_ctx* ctx, int64_t n_vertices, const double* x
     CK(cudaStreamSynchronize(ctx->s));
     if (missing)
         return fail(ctx, ACVD_ERR_ARG, "acvd_subdivide: " + std::to_string(missing) +
-                                            " faces have an edge missing from the ring CSR");
+                                            " faces refer to a missing vertex or to an edge missing from the ring CSR");
+    return ACVD_OK;
+}
+
+// Work bytes of acvd_subdivide_device: the ring slots' edge ids and the fault count.
+extern "C" int64_t acvd_subdivide_work_bytes(int64_t n_edges) {
+    return 2 * n_edges * (int64_t)sizeof(int) + 16;
+}
+
+// acvd_subdivide on device buffers, enqueued on the context's stream (no
+// allocation, no synchronisation).  The count of faces with an edge missing from
+// the ring CSR lands in the uint32 at d_work + 2 n_edges ints.
+extern "C" int acvd_subdivide_device(acvd_ctx* ctx, int64_t n_vertices, const double* d_xyz, int64_t n_faces,
+                                     const int32_t* d_tri, const int32_t* d_row, const int32_t* d_col,
+                                     int64_t n_edges, const int32_t* d_edge_v, const double* d_ind,
+                                     double* d_out_xyz, int32_t* d_out_tri, int32_t* d_parent1,
+                                     int32_t* d_parent2, double* d_out_ind, void* d_work) {
+    if (!ctx) return ACVD_ERR_ARG;
+    if (n_vertices < 0 || n_faces < 0 || n_edges < 0 || !d_xyz || !d_tri || !d_row || !d_col || !d_edge_v ||
+        !d_out_xyz || !d_out_tri || !d_parent1 || !d_parent2 || !d_work)
+        return fail(ctx, ACVD_ERR_ARG, "acvd_subdivide_device: null or negative argument");
+    if ((d_ind == nullptr) != (d_out_ind == nullptr))
+        return fail(ctx, ACVD_ERR_ARG, "acvd_subdivide_device: d_ind and d_out_ind go together");
+    if (n_vertices + n_edges > INT32_MAX || 4 * n_faces > INT32_MAX)
+        return fail(ctx, ACVD_ERR_UNSUPPORTED, "acvd_subdivide_device: the subdivided mesh exceeds 32-bit ids");
+    if ((reinterpret_cast<uintptr_t>(d_work) & 15u) != 0)
+        return fail(ctx, ACVD_ERR_ARG, "acvd_subdivide_device: d_work must be 16-byte aligned");
+    CK(cudaSetDevice(ctx->opts.device));
+    int* slot = (int*)d_work;
+    unsigned int* missing = (unsigned int*)(slot + 2 * n_edges);
+    CK(cudaMemsetAsync(missing, 0, sizeof(unsigned int), ctx->s));
+    CK(launch_subdivide(d_xyz, n_vertices, d_tri, n_faces, d_row, d_col, d_edge_v, n_edges, d_ind, slot, d_out_xyz,
+                        d_out_tri, d_parent1, d_parent2, d_out_ind, missing, ctx->s));
     return ACVD_OK;
 }
 

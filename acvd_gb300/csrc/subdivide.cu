@@ -17,11 +17,13 @@ namespace {
 
 inline unsigned sgrid(int64_t n, int b) { return (unsigned)((n + b - 1) / b); }
 
-__global__ void subdiv_slot_edges_kernel(const int* __restrict__ edge_v, int64_t ne, const int* __restrict__ row,
-                                         const int* __restrict__ col, int* __restrict__ slot_edge) {
+__global__ void subdiv_slot_edges_kernel(const int* __restrict__ edge_v, int64_t ne, int64_t nv,
+                                         const int* __restrict__ row, const int* __restrict__ col,
+                                         int* __restrict__ slot_edge) {
     const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= ne) return;
     const int a = edge_v[2 * e], b = edge_v[2 * e + 1];
+    if (a < 0 || b < 0 || a >= nv || b >= nv) return;   // left -1: the faces on it are reported
     for (int p = row[a]; p < row[a + 1]; p++)
         if (col[p] == b) { slot_edge[p] = (int)e; break; }
     for (int p = row[b]; p < row[b + 1]; p++)
@@ -42,6 +44,7 @@ __global__ void subdiv_points_kernel(const double* __restrict__ xyz, int64_t nv,
     }
     const int64_t e = i - nv;
     const int a = edge_v[2 * e], b = edge_v[2 * e + 1];
+    if (a < 0 || b < 0 || a >= nv || b >= nv) return;
     for (int c = 0; c < 3; c++) {
         const double m = 0.5 * (xyz[3 * (int64_t)a + c] + xyz[3 * (int64_t)b + c]);
         out_xyz[3 * i + c] = (double)__double2float_rn(m);
@@ -65,6 +68,11 @@ __global__ void subdiv_faces_kernel(const int* __restrict__ tri, int64_t nf, int
     const int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= nf) return;
     const int v1 = tri[3 * f], v2 = tri[3 * f + 1], v3 = tri[3 * f + 2];
+    if (v1 == v2 || v1 < 0 || v2 < 0 || v3 < 0 || v1 >= nv || v2 >= nv || v3 >= nv) {
+        // an inactive face for vtkSurface, or a vertex id out of range: reported, not subdivided
+        atomicAdd(missing, 1u);
+        return;
+    }
     const int e12 = subdiv_edge_of(row, col, slot_edge, v1, v2);
     const int e23 = subdiv_edge_of(row, col, slot_edge, v2, v3);
     const int e31 = subdiv_edge_of(row, col, slot_edge, v3, v1);
@@ -88,7 +96,7 @@ cudaError_t launch_subdivide(const double* xyz, int64_t nv, const int* tri, int6
                              unsigned int* missing, cudaStream_t s) {
     cudaError_t err = cudaMemsetAsync(slot_edge, 0xff, 2 * (size_t)ne * sizeof(int), s);
     if (err != cudaSuccess) return err;
-    if (ne > 0) subdiv_slot_edges_kernel<<<sgrid(ne, 256), 256, 0, s>>>(edge_v, ne, row, col, slot_edge);
+    if (ne > 0) subdiv_slot_edges_kernel<<<sgrid(ne, 256), 256, 0, s>>>(edge_v, ne, nv, row, col, slot_edge);
     if (nv + ne > 0)
         subdiv_points_kernel<<<sgrid(nv + ne, 256), 256, 0, s>>>(xyz, nv, edge_v, ne, ind, out_xyz, parent1, parent2,
                                                                   out_ind);

@@ -105,6 +105,9 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         "acvd_write_mesh": (ctypes.c_int, [ctypes.c_char_p, _P, _i64, _P, _i64]),
         "acvd_free": (None, [_P]),
         "acvd_io_last_error": (ctypes.c_char_p, []),
+        "acvd_subdivide_work_bytes": (_i64, [_i64]),
+        "acvd_subdivide_device": (ctypes.c_int, [_P, _i64, _P, _i64, _P, _P, _P, _i64, _P, _P, _P, _P, _P, _P, _P,
+                                                 _P]),
         "acvd_subdivide": (ctypes.c_int, [_P, _i64, _P, _i64, _P, _P, _P, _i64, _P, _P, _P, _P, _P, _P, _P]),
     }
     for name, (res, args) in sig.items():
@@ -392,6 +395,17 @@ class Engine:
                                           _ptr(ind) if ind is not None else None, _ptr(o_pts), _ptr(o_tri), _ptr(p1),
                                           _ptr(p2), _ptr(o_ind) if o_ind is not None else None), "acvd_subdivide")
         return o_pts, o_tri, p1, p2, o_ind
+
+    def subdivide_device(self, nv: int, d_xyz: int, nf: int, d_tri: int, d_row: int, d_col: int, ne: int,
+                         d_edge_v: int, d_ind: int | None, d_out_xyz: int, d_out_tri: int, d_p1: int, d_p2: int,
+                         d_out_ind: int | None, d_work: int) -> None:
+        """acvd_subdivide_device: device pointers (ints), enqueued on this context's stream."""
+        self._ck(self._lib.acvd_subdivide_device(self.ctx, nv, d_xyz, nf, d_tri, d_row, d_col, ne, d_edge_v,
+                                                 d_ind, d_out_xyz, d_out_tri, d_p1, d_p2, d_out_ind, d_work),
+                 "acvd_subdivide_device")
+
+    def subdivide_work_bytes(self, ne: int) -> int:
+        return int(self._lib.acvd_subdivide_work_bytes(ne))
 
     def post_placement(self, level: int = 1) -> np.ndarray:
         """ACVD's quadric post-placement of the output vertices (ACVD.cxx:217-291): (K, 3)."""

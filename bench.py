@@ -84,6 +84,170 @@ CURVATURE_WORKLOADS = {
                                             "3-ring) of the heightfield 4096^2 (16,777,216 vertices)"),
 }
 CURV_CHECK = 4096        # vertices compared bit for bit with the oracle
+
+SUBDIVISION_WORKLOADS = {
+    "subdivide_torus_1024x512": dict(kind="torus", mesh=dict(nu=1024, nv=512, seed=0),
+                                     desc="one level of midpoint subdivision (vtkSurface::Subdivide) with the "
+                                          "indicator's parent interpolation, torus 1024x512 (524,288 vertices, "
+                                          "1,048,576 faces -> 2,097,152 vertices, 4,194,304 faces)"),
+}
+
+
+def subdivision_bytes(nv, ne, nf):
+    """Compulsory bytes of one subdivision launch sequence: points (24 B), indicator (8 B),
+    ring offsets (4 B) per vertex, faces (12 B), ring slots and edge ends (2 x 8 B per edge)
+    read once; new points and indicator (32 B per output vertex), parents (8 B per edge),
+    faces (48 B per input face) written once; the slot-to-edge table written and read (16 B
+    per edge)."""
+    return (24 + 8 + 4) * nv + 12 * nf + 16 * ne + 32 * (nv + ne) + 8 * ne + 48 * nf + 16 * ne
+
+
+def run_subdivision_reference_arm(args):
+    """Reference arm of the subdivision workload: the restatement of vtkSurface::Subdivide
+    (sequential, one core -- the reference's loop is not threaded), after the edge table is
+    built, one full subdivision per step."""
+    ws, rank, local = _dist()
+    if rank != 0:
+        return
+    from acvd_gb300 import synth
+    from oracle import oracle
+    oracle.build(ref=False)
+    w = SUBDIVISION_WORKLOADS[args.workload]
+    m = synth.make(w["kind"], with_curvature=False, **w["mesh"])
+    ind = np.random.default_rng(0).uniform(0.5, 2.0, size=m.n_points)
+    for _ in range(args.warmup):
+        oracle.subdivide(m.points, m.faces, ind)
+    secs = []
+    for _ in range(args.steps):
+        out = oracle.subdivide(m.points, m.faces, ind, timing=secs)
+    n_out = out[0].shape[0]
+    ms = 1000.0 * statistics.mean(secs)
+    value = n_out / (ms / 1000.0)
+    print(json.dumps({
+        "impl": "reference", "metric": "midpoint subdivision throughput (vtkSurface::Subdivide + indicator "
+                                       "interpolation)",
+        "value": value, "unit": "output vertices/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": {"workload": args.workload, "description": w["desc"]},
+        "cpu_baseline": {"value": value, "unit": "output vertices/s", "cores": 1, "kind": "port",
+                         "sample": "the whole mesh per step, one core, after the edge table is built"},
+        "e2e": {"value": value, "unit": "output vertices/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
+def run_subdivision_arm(args):
+    """One level of subdivision on the GPU: resident (device pointers, CUDA events on the
+    context's stream, L2 flushed between steps) and end to end (host buffers)."""
+    import torch
+    import acvd_gb300
+    from acvd_gb300 import engine as E
+    from acvd_gb300 import synth
+
+    ws, rank, local = _dist()
+    device = local
+    torch.cuda.set_device(device)
+    w = SUBDIVISION_WORKLOADS[args.workload]
+    m = synth.make(w["kind"], with_curvature=False, **w["mesh"])
+    nv, nf = m.n_points, m.n_faces
+    row, col, ev = acvd_gb300.build_topology(nv, m.faces)
+    ne = ev.shape[0]
+    ind = np.random.default_rng(0).uniform(0.5, 2.0, size=nv)
+    dev = f"cuda:{device}"
+    t = lambda a, dt: torch.from_numpy(np.ascontiguousarray(a, dtype=dt)).to(dev)
+    d_xyz, d_tri, d_row, d_col, d_ev, d_ind = (t(m.points, np.float64), t(m.faces, np.int32), t(row, np.int32),
+                                               t(col, np.int32), t(ev, np.int32), t(ind, np.float64))
+    o_xyz = torch.empty((nv + ne, 3), dtype=torch.float64, device=dev)
+    o_tri = torch.empty((4 * nf, 3), dtype=torch.int32, device=dev)
+    o_p1 = torch.empty(ne, dtype=torch.int32, device=dev)
+    o_p2 = torch.empty(ne, dtype=torch.int32, device=dev)
+    o_ind = torch.empty(nv + ne, dtype=torch.float64, device=dev)
+    eng = E.Engine(device=device)
+    work = torch.empty(eng.subdivide_work_bytes(ne), dtype=torch.uint8, device=dev)
+    stream = torch.cuda.ExternalStream(eng.stream(), device=device)
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=dev)
+
+    def call():
+        eng.subdivide_device(nv, d_xyz.data_ptr(), nf, d_tri.data_ptr(), d_row.data_ptr(), d_col.data_ptr(), ne,
+                             d_ev.data_ptr(), d_ind.data_ptr(), o_xyz.data_ptr(), o_tri.data_ptr(),
+                             o_p1.data_ptr(), o_p2.data_ptr(), o_ind.data_ptr(), work.data_ptr())
+
+    for _ in range(args.warmup):
+        call()
+    torch.cuda.synchronize()
+    step_ms = []
+    with ClockSampler(device) as clk:
+        for _ in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            call()
+            e1.record(stream)
+            e1.synchronize()
+            step_ms.append(e0.elapsed_time(e1))
+    ms = statistics.mean(step_ms)
+    faults = int(work[8 * ne:8 * ne + 4].view(torch.int32).item())
+    g_xyz, g_tri, g_p1, g_p2, g_ind = (o_xyz.cpu().numpy(), o_tri.cpu().numpy(), o_p1.cpu().numpy(),
+                                       o_p2.cpu().numpy(), o_ind.cpu().numpy())
+    e2e = None
+    if not args.no_e2e:
+        c = np.ascontiguousarray
+        h_pts, h_faces, h_row, h_col, h_ev, h_ind = (pinned(torch, a) for a in (
+            c(m.points, dtype=np.float64), c(m.faces, dtype=np.int32), c(row, dtype=np.int32),
+            c(col, dtype=np.int32), c(ev, dtype=np.int32), c(ind, dtype=np.float64)))
+        e2e_ms = []
+        for _ in range(max(1, args.steps)):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            out = eng.subdivide(h_pts, h_faces, h_row, h_col, h_ev, indicator=h_ind)
+            e2e_ms.append(1000.0 * (time.perf_counter() - t0))
+        assert np.array_equal(out[0], g_xyz) and np.array_equal(out[1], g_tri), "end-to-end subdivision differs"
+        e2e = {"value": (nv + ne) / (statistics.mean(e2e_ms) / 1000.0), "unit": "output vertices/s",
+               "h2d_bytes_per_step": int(h_pts.nbytes + h_faces.nbytes + h_row.nbytes + h_col.nbytes + h_ev.nbytes +
+                                         h_ind.nbytes),
+               "d2h_bytes_per_step": int(out[0].nbytes + out[1].nbytes + out[2].nbytes + out[3].nbytes +
+                                         out[4].nbytes),
+               "ms_per_step": statistics.mean(e2e_ms),
+               "includes": "host->device inputs, the three kernels, device->host outputs (pageable results)"}
+    eng.close()
+    if rank != 0:
+        return
+    from oracle import oracle
+    oracle.build(ref=False)
+    secs = []
+    r = oracle.subdivide(m.points, m.faces, ind, timing=secs)
+    exact = (faults == 0 and np.array_equal(r[0], g_xyz) and np.array_equal(r[1], g_tri) and
+             np.array_equal(r[2], g_p1) and np.array_equal(r[3], g_p2) and np.array_equal(r[4], g_ind))
+    cpu = None
+    if not args.no_cpu_baseline:
+        cpu = {"value": (nv + ne) / secs[0], "unit": "output vertices/s", "cores": 1, "kind": "port",
+               "sample": f"the whole mesh, one core, after the edge table is built ({secs[0]:.3f} s)"}
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    peak = peaks.get("hbm_gbs", 6800.0)
+    alg = subdivision_bytes(nv, ne, nf)
+    achieved = alg / 1e9 / (ms / 1000.0)
+    line = {
+        "metric": "midpoint subdivision throughput (vtkSurface::Subdivide + indicator interpolation)",
+        "value": (nv + ne) / (ms / 1000.0), "unit": "output vertices/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": args.workload, "description": w["desc"], "vertices": nv, "edges": ne, "faces": nf,
+                   "l2": "flushed between timed steps (256 MB write)"},
+        "roofline": {"bound": "hbm", "kernel": "subdiv_* (three kernels and a memset, timed together)",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback",
+                     "traffic": None, "algorithmic_bytes_per_launch": alg},
+        "parity": {"bit_exact_vs_oracle": bool(exact), "faces_reported": faults},
+        "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": 4 * (args.steps + args.warmup),
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
 CURV_CPU_SAMPLE = 65536  # vertices of the single-core CPU baseline
 
 
@@ -851,7 +1015,7 @@ def main():
                          "cooperative kernel between convergence events")
     ap.add_argument("--workload", default="torus_1024x512_qem",
                     choices=sorted(WORKLOADS) + sorted(BATCH_WORKLOADS) + sorted(ADJOINT_WORKLOADS) +
-                    sorted(CURVATURE_WORKLOADS))
+                    sorted(CURVATURE_WORKLOADS) + sorted(SUBDIVISION_WORKLOADS))
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--solve-once", action="store_true",
@@ -862,12 +1026,16 @@ def main():
             raise SystemExit("--solve-once takes a clustering workload")
         solve_once(args)
         return
-    if args.impl == "reference" and args.workload in CURVATURE_WORKLOADS:
+    if args.impl == "reference" and args.workload in SUBDIVISION_WORKLOADS:
+        run_subdivision_reference_arm(args)
+    elif args.impl == "reference" and args.workload in CURVATURE_WORKLOADS:
         run_curvature_reference_arm(args)
     elif args.impl == "reference":
         run_reference_arm(args)
     elif args.workload in CURVATURE_WORKLOADS:
         run_curvature_arm(args)
+    elif args.workload in SUBDIVISION_WORKLOADS:
+        run_subdivision_arm(args)
     elif args.workload in BATCH_WORKLOADS:
         run_batch_arm(args)
     elif args.workload in ADJOINT_WORKLOADS:

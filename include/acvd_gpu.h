@@ -253,6 +253,21 @@ int acvd_subdivide(acvd_ctx* ctx, int64_t n_vertices, const double* xyz, int64_t
                    double* out_indicator);
 
 /*
+ * acvd_subdivide on device buffers (the same layouts, all in device memory of the
+ * context's device), enqueued on the context's stream (acvd_stream): no allocation and
+ * no synchronisation, for callers whose mesh is already resident.  d_work: at least
+ * acvd_subdivide_work_bytes(n_edges) bytes, 16-byte aligned; after the stream reaches
+ * this call, the uint32 at d_work + 8 n_edges bytes counts the faces that are
+ * degenerate or have an edge missing from the ring CSR (their four output faces are
+ * not written).  d_ind / d_out_ind may be NULL together.
+ */
+int64_t acvd_subdivide_work_bytes(int64_t n_edges);
+int acvd_subdivide_device(acvd_ctx* ctx, int64_t n_vertices, const double* d_xyz, int64_t n_faces,
+                          const int32_t* d_tri, const int32_t* d_row, const int32_t* d_col, int64_t n_edges,
+                          const int32_t* d_edge_v, const double* d_ind, double* d_out_xyz, int32_t* d_out_tri,
+                          int32_t* d_parent1, int32_t* d_parent2, double* d_out_ind, void* d_work);
+
+/*
  * ACVD's quadric post-placement of the output vertices
  * (DiscreteRemeshing/Examples/ACVD.cxx:217-291, the ACVD driver's step after
  * Remesh()): per cluster, the unweighted plane quadrics of every face adjacent to

@@ -1342,9 +1342,11 @@ void port_curvature_range(void* hp, long long v0, long long v1, double* indicato
 // old values copied, new (ind[p1] + ind[p2]) * 0.5.  Returns the number of output
 // faces; out_pts: 3 (nV + nE), out_tri: 12 nF, p1/p2: nE, ind_out: nV + nE.
 long long port_subdivide(long long nv, const double* pts, long long nf, const int* tri, double* out_pts,
-                         int* out_tri, int* p1, int* p2, const double* ind, double* ind_out) {
+                         int* out_tri, int* p1, int* p2, const double* ind, double* ind_out, double* seconds) {
     Mesh m;
     m.build(nv, pts, nf, tri);
+    // the reference subdivides a vtkSurface whose edge table exists: time from here
+    const auto t0 = std::chrono::steady_clock::now();
     const idt ne = m.n_edges();
     std::vector<idt> child(ne, -1);
     idt nout = 0;
@@ -1387,6 +1389,7 @@ long long port_subdivide(long long nv, const double* pts, long long nf, const in
         for (int j = 0; j < 12; j++) out_tri[12 * of + j] = t[j];
         of++;
     }
+    if (seconds) *seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     return 4 * of;
 }
 

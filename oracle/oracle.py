@@ -326,16 +326,17 @@ class Ref(_Base):
         return int(self._lib.ref_loops(self.h))
 
 
-def subdivide(points: np.ndarray, faces: np.ndarray, indicator: np.ndarray | None = None):
+def subdivide(points: np.ndarray, faces: np.ndarray, indicator: np.ndarray | None = None, timing: list | None = None):
     """vtkSurface::Subdivide restated (acvd_port.cpp ``port_subdivide``), with the
     parent interpolation of the indicator.  Returns (points (nV+nE, 3), faces (4 nF', 3),
-    parent1 (nE), parent2 (nE), indicator (nV+nE) or None)."""
+    parent1 (nE), parent2 (nE), indicator (nV+nE) or None).  ``timing`` (a list) gets the
+    seconds of the subdivision proper, after the edge table is built."""
     Port._load()
     lib = Port._lib
     fn = lib.port_subdivide
     fn.restype = ctypes.c_longlong
     fn.argtypes = [ctypes.c_longlong, _pd, ctypes.c_longlong, _pi, _pd, _pi, _pi, _pi, ctypes.c_void_p,
-                   ctypes.c_void_p]
+                   ctypes.c_void_p, ctypes.c_void_p]
     pts = np.ascontiguousarray(points, dtype=np.float64)
     tri = np.ascontiguousarray(faces, dtype=np.int32)
     nv, nf = pts.shape[0], tri.shape[0]
@@ -348,6 +349,10 @@ def subdivide(points: np.ndarray, faces: np.ndarray, indicator: np.ndarray | Non
     if indicator is not None:
         ind = np.ascontiguousarray(indicator, dtype=np.float64)
         o_ind = np.empty(nv + ne)
+    secs = ctypes.c_double(0.0)
     nt = int(fn(nv, pts.reshape(-1), nf, tri.reshape(-1), o_pts, o_tri, p1, p2,
-                None if ind is None else ind.ctypes.data, None if o_ind is None else o_ind.ctypes.data))
+                None if ind is None else ind.ctypes.data, None if o_ind is None else o_ind.ctypes.data,
+                ctypes.addressof(secs)))
+    if timing is not None:
+        timing.append(secs.value)   # the subdivision proper, after the edge table is built
     return o_pts.reshape(-1, 3), o_tri[:3 * nt].reshape(-1, 3), p1[:ne], p2[:ne], o_ind

@@ -414,3 +414,38 @@ def test_remesh_subdivides_like_the_reference(oracle_lib):
     e_ref = ref.global_energy()
     assert e_gpu <= e_ref + 0.02 * abs(e_ref), (e_gpu, e_ref)
     assert r.GetOutput().GetNumberOfPoints() == k
+
+
+def test_subdivide_device_matches_host_call():
+    """acvd_subdivide_device (device buffers, the context's stream, no allocation) gives
+    the host call's outputs; an out-of-range vertex id is reported, not read."""
+    torch = pytest.importorskip("torch")
+    m = synth.torus(40, 20, seed=3)
+    row, col, ev = acvd_gb300.build_topology(m.n_points, m.faces)
+    ind = np.linspace(0.5, 2.0, m.n_points)
+    e = acvd_gb300.Engine()
+    ref = e.subdivide(m.points, m.faces, row, col, ev, indicator=ind)
+    nv, nf, ne = m.n_points, m.faces.shape[0], ev.shape[0]
+    t = lambda a, dt: torch.from_numpy(np.ascontiguousarray(a, dtype=dt)).cuda()
+    d = [t(m.points, np.float64), t(m.faces, np.int32), t(row, np.int32), t(col, np.int32), t(ev, np.int32),
+         t(ind, np.float64)]
+    o = [torch.empty((nv + ne, 3), dtype=torch.float64, device="cuda"),
+         torch.empty((4 * nf, 3), dtype=torch.int32, device="cuda"),
+         torch.empty(ne, dtype=torch.int32, device="cuda"), torch.empty(ne, dtype=torch.int32, device="cuda"),
+         torch.empty(nv + ne, dtype=torch.float64, device="cuda")]
+    work = torch.empty(e.subdivide_work_bytes(ne), dtype=torch.uint8, device="cuda")
+
+    def run(tri):
+        e.subdivide_device(nv, d[0].data_ptr(), nf, tri.data_ptr(), d[2].data_ptr(), d[3].data_ptr(), ne,
+                           d[4].data_ptr(), d[5].data_ptr(), o[0].data_ptr(), o[1].data_ptr(), o[2].data_ptr(),
+                           o[3].data_ptr(), o[4].data_ptr(), work.data_ptr())
+        torch.cuda.synchronize()
+        return int(work[8 * ne:8 * ne + 4].view(torch.int32).item())
+
+    assert run(d[1]) == 0
+    for got, want in zip(o, ref):
+        np.testing.assert_array_equal(got.cpu().numpy(), want)
+    bad = d[1].clone()
+    bad[5, 1] = nv + 7                         # a vertex that does not exist
+    assert run(bad) == 1
+    e.close()
