@@ -93,6 +93,119 @@ SUBDIVISION_WORKLOADS = {
 }
 
 
+MANIFOLD_WORKLOADS = {
+    "force_manifold_torus_1024x512": dict(kind="torus", mesh=dict(nu=1024, nv=512, seed=0), k=20000,
+                                          desc="one ForceManifold detection pass (DetectNonManifoldOutputVertices) "
+                                               "on the torus 1024x512 (524,288 items), K=20,000, from the "
+                                               "reference's initial sampling with its holes filled"),
+}
+
+
+def run_manifold_arm(args):
+    """One detection pass of the ForceManifold loop: the device checks (dual triangles,
+    manifold tests of output and input vertices) and the host's new-cluster bookkeeping,
+    timed on the wall clock around the call (the pass ends with a device-to-host read)."""
+    import torch
+    import acvd_gb300
+    from acvd_gb300 import engine as E
+    from acvd_gb300 import synth
+    from oracle import oracle
+
+    ws, rank, local = _dist()
+    device = local
+    torch.cuda.set_device(device)
+    w = MANIFOLD_WORKLOADS[args.workload]
+    m = synth.make(w["kind"], with_curvature=False, **w["mesh"])
+    k = w["k"]
+    oracle.build(ref=False)
+    p = oracle.Port("qem", m.points, m.faces, k, 0.0)
+    p.init(None)
+    p.fill_holes()
+    lab = p.labels()
+    row, col, ev = acvd_gb300.build_topology(m.n_points, m.faces)
+    eng = E.Engine(device=device)
+    eng.set_mesh(m.points, m.faces, row, col, ev)
+    eng.set_metric("qem")
+    for _ in range(args.warmup):
+        eng.set_labels(k, lab)
+        eng.force_manifold_step()
+    step_ms, issues = [], 0
+    with ClockSampler(device) as clk:
+        for _ in range(args.steps):
+            eng.set_labels(k, lab)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            issues = eng.force_manifold_step()
+            step_ms.append(1000.0 * (time.perf_counter() - t0))
+    g_lab, g_k, g_frozen = eng.labels(), eng.k, eng.frozen_clusters()
+    eng.close()
+    if rank != 0:
+        return
+    t0 = time.perf_counter()
+    n_ref = p.detect_nonmanifold()
+    secs = time.perf_counter() - t0
+    exact = n_ref == issues and p.k == g_k and np.array_equal(p.labels(), g_lab) and \
+        np.array_equal(p.frozen(), g_frozen)
+    ms = statistics.mean(step_ms)
+    n = m.n_points
+    cpu = None if args.no_cpu_baseline else {
+        "value": n / secs, "unit": "items/s", "cores": 1, "kind": "port",
+        "sample": f"the same pass on the same clustering, one core ({secs:.3f} s)"}
+    print(json.dumps({
+        "metric": "ForceManifold detection pass throughput (items of the clustering per second)",
+        "value": n / (ms / 1000.0), "unit": "items/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+        "data": "synthetic",
+        "config": {"workload": args.workload, "description": w["desc"], "items": n, "clusters": k,
+                   "issues": issues, "timing": "wall clock around acvd_force_manifold_step (host-synchronous)"},
+        "roofline": None,
+        "roofline_note": "a pass of short kernels (dual mesh sort, incidence lists, per-vertex fan walks) and "
+                         "host bookkeeping; no single kernel dominates",
+        "parity": {"identical_to_oracle": bool(exact), "issues_oracle": n_ref},
+        "cpu_baseline": cpu,
+        "e2e": {"value": n / (ms / 1000.0), "unit": "items/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": int(4 * n), "ms_per_step": ms},
+        "clocks": clk.summary(),
+    }), flush=True)
+
+
+def run_manifold_reference_arm(args):
+    """Reference arm of the ForceManifold workload: the restated detection pass
+    (sequential, as the reference's), one per step from the same clustering."""
+    ws, rank, local = _dist()
+    if rank != 0:
+        return
+    from acvd_gb300 import synth
+    from oracle import oracle
+    oracle.build(ref=False)
+    w = MANIFOLD_WORKLOADS[args.workload]
+    m = synth.make(w["kind"], with_curvature=False, **w["mesh"])
+    base = oracle.Port("qem", m.points, m.faces, w["k"], 0.0)
+    base.init(None)
+    base.fill_holes()
+    lab = base.labels()
+    secs = []
+    for it in range(args.warmup + args.steps):
+        p = oracle.Port("qem", m.points, m.faces, w["k"], 0.0)
+        p.init(lab)
+        p.fill_holes()
+        t0 = time.perf_counter()
+        p.detect_nonmanifold()
+        if it >= args.warmup:
+            secs.append(time.perf_counter() - t0)
+    ms = 1000.0 * statistics.mean(secs)
+    value = m.n_points / (ms / 1000.0)
+    print(json.dumps({
+        "impl": "reference", "metric": "ForceManifold detection pass throughput (items of the clustering per second)",
+        "value": value, "unit": "items/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+        "data": "synthetic", "config": {"workload": args.workload, "description": w["desc"]},
+        "cpu_baseline": {"value": value, "unit": "items/s", "cores": 1, "kind": "port",
+                         "sample": "the whole pass per step, one core"},
+        "e2e": {"value": value, "unit": "items/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
 def subdivision_bytes(nv, ne, nf):
     """Compulsory bytes of one subdivision launch sequence: points (24 B), indicator (8 B),
     ring offsets (4 B) per vertex, faces (12 B), ring slots and edge ends (2 x 8 B per edge)
@@ -1015,7 +1128,7 @@ def main():
                          "cooperative kernel between convergence events")
     ap.add_argument("--workload", default="torus_1024x512_qem",
                     choices=sorted(WORKLOADS) + sorted(BATCH_WORKLOADS) + sorted(ADJOINT_WORKLOADS) +
-                    sorted(CURVATURE_WORKLOADS) + sorted(SUBDIVISION_WORKLOADS))
+                    sorted(CURVATURE_WORKLOADS) + sorted(SUBDIVISION_WORKLOADS) + sorted(MANIFOLD_WORKLOADS))
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--solve-once", action="store_true",
@@ -1028,6 +1141,8 @@ def main():
         return
     if args.impl == "reference" and args.workload in SUBDIVISION_WORKLOADS:
         run_subdivision_reference_arm(args)
+    elif args.impl == "reference" and args.workload in MANIFOLD_WORKLOADS:
+        run_manifold_reference_arm(args)
     elif args.impl == "reference" and args.workload in CURVATURE_WORKLOADS:
         run_curvature_reference_arm(args)
     elif args.impl == "reference":
@@ -1036,6 +1151,8 @@ def main():
         run_curvature_arm(args)
     elif args.workload in SUBDIVISION_WORKLOADS:
         run_subdivision_arm(args)
+    elif args.workload in MANIFOLD_WORKLOADS:
+        run_manifold_arm(args)
     elif args.workload in BATCH_WORKLOADS:
         run_batch_arm(args)
     elif args.workload in ADJOINT_WORKLOADS:
