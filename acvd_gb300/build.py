@@ -42,7 +42,8 @@ def _stale(obj: str, deps: list[str]) -> bool:
 
 def build(verbose: bool = False, force: bool = False) -> str:
     """ACVD_NVCC_FLAGS (environment) adds nvcc flags, e.g. the tuning macros
-    -DACVD_EVAL_MINB=<blocks per SM of the evaluation kernel>; pass force=True
+    -DACVD_EVAL_MINB=<blocks per SM of the evaluation kernel> (isotropic / QEM) and
+    -DACVD_EVAL_MINB_ANISO=<the same for the quadric-anisotropic metric>; pass force=True
     (or --force) when they change."""
     os.makedirs(OUT, exist_ok=True)
     nvcc = _nvcc()

@@ -590,13 +590,20 @@ ACVD_DEV void eval_tile(const DevState& st, int item0, int64_t count, int color,
 }
 
 // blocks per SM the evaluation kernel is compiled for (registers per thread
-// follow: 3 -> 80, 4 -> 64; 4 measured fastest on the torus and heightfield workloads)
+// follow: 3 -> 80, 4 -> 64, 5 -> 48)
 #ifndef ACVD_EVAL_MINB
 #define ACVD_EVAL_MINB 4
 #endif
+// the quadric-anisotropic evaluation at 5 blocks per SM (48 registers, more spills):
+// faster on the 4096^2 heightfield (330 ms against 347 ms); 4 stays faster for QEM
+#ifndef ACVD_EVAL_MINB_ANISO
+#define ACVD_EVAL_MINB_ANISO 5
+#endif
+template <int M> struct EvalMinBlocks { static constexpr int value = ACVD_EVAL_MINB; };
+template <> struct EvalMinBlocks<kAniso> { static constexpr int value = ACVD_EVAL_MINB_ANISO; };
 
 template <int M>
-__global__ void __launch_bounds__(256, ACVD_EVAL_MINB) eval_kernel(DevState st, int item0, int64_t count,
+__global__ void __launch_bounds__(256, EvalMinBlocks<M>::value) eval_kernel(DevState st, int item0, int64_t count,
                                                       int color, int* cand_dest, unsigned* cand_prio, int claims) {
     eval_tile<M>(st, item0, count, color, cand_dest, cand_prio, claims, blockIdx.x);
 }
