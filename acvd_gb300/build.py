@@ -24,6 +24,8 @@ CU_SOURCES = ["primitives.cu", "topology.cu", "cluster.cu", "adjoint.cu", "engin
 # rounded, so that it reproduces the CPU restatement bit for bit
 CU_FILE_FLAGS = {"curvature.cu": ["-fmad=false"]}
 CXX_SOURCES = ["host.cpp", "io.cpp"]
+# command-line programs built from csrc/acvd_cli.cpp: name -> compile definitions
+CLI_PROGRAMS = {"acvd": [], "acvdq": ["-DACVD_CLI_QEM"]}
 
 
 def _nvcc() -> str:
@@ -74,10 +76,25 @@ def build(verbose: bool = False, force: bool = False) -> str:
         if verbose and (r.stdout or r.stderr):
             print(r.stdout + r.stderr)
 
+    # the native ACVD / ACVDQ programs over the C ABI
+    cli_src = os.path.join(SRC, "acvd_cli.cpp")
+    cli_jobs = []
+    for name, defs in CLI_PROGRAMS.items():
+        obj = os.path.join(OUT, name + ".o")
+        if force or _stale(obj, [cli_src] + headers):
+            jobs.append(["g++", "-O2", "-std=c++17", "-ffp-contract=off"] + defs + ["-c", cli_src, "-o", obj])
+            cli_jobs.append(name)
+
     with concurrent.futures.ThreadPoolExecutor(max_workers=max(1, len(jobs))) as ex:
         list(ex.map(run, jobs))
-    if force or jobs or not os.path.exists(LIB):
+    relinked = force or bool(jobs) or not os.path.exists(LIB)
+    if relinked:
         run([nvcc, ARCH, "-shared", "-o", LIB] + objs + ["-lcudart"])
+    for name in CLI_PROGRAMS:
+        exe = os.path.join(OUT, name)
+        if relinked or name in cli_jobs or not os.path.exists(exe):
+            run(["g++", "-o", exe, os.path.join(OUT, name + ".o"), "-L" + OUT, "-lacvd_gb300",
+                 "-Wl,-rpath,$ORIGIN"])
     return LIB
 
 

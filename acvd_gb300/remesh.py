@@ -104,6 +104,7 @@ class _DiscreteRemeshing:
         self.VerticesParent1 = None
         self.VerticesParent2 = None
         self.NumberOfClusters = 0
+        self.RequestedNumberOfClusters = 0
         self.SubsamplingThreshold = 10
         self.UnconstrainedInitialization = 0
         self.ConsoleOutput = 0
@@ -137,6 +138,7 @@ class _DiscreteRemeshing:
 
     def SetNumberOfClusters(self, k: int):
         self.NumberOfClusters = int(k)
+        self.RequestedNumberOfClusters = int(k)
 
     def GetNumberOfClusters(self) -> int:
         return self.NumberOfClusters
@@ -365,7 +367,13 @@ def QuadricPostPlacement(remesh: _DiscreteRemeshing, level: int = 1) -> Surface:
     if level == 0:
         return remesh.Output
     pts = remesh._engine.post_placement(level)
-    remesh.Output.points = pts
+    # the driver moves its NumberOfSamples vertices only (clusters ForceManifold added and
+    # FixMeshBoundaries' vertices keep their place) and stores them in the output's float
+    # vtkPoints
+    k = min(remesh.RequestedNumberOfClusters, pts.shape[0])
+    out = remesh.Output.points.copy()
+    out[:k] = pts[:k].astype(np.float32).astype(np.float64)
+    remesh.Output.points = out
     return remesh.Output
 
 

@@ -40,3 +40,29 @@ def test_acvdq_program_with_subdivision_and_options(tmp_path):
     pts, tri = E.read_mesh(dst + "q.ply")
     assert pts.shape[0] > 200                                  # boundary vertices appended
     assert tri.max() < pts.shape[0]
+
+
+@pytest.mark.parametrize("prog,args", [
+    ("acvd", ["300", "0.5", "-q", "2"]),
+    ("acvdq", ["200", "0", "-m", "1", "-b", "1", "-q", "2"]),
+])
+def test_native_programs_match_the_python_drivers(tmp_path, prog, args):
+    """The native programs (C++ over the C ABI) and the Python drivers run the same steps:
+    their output files are byte for byte the same."""
+    import subprocess
+    from acvd_gb300 import build as B
+    mesh = synth.torus(80, 40, seed=2) if prog == "acvd" else synth.heightfield(30, seed=2)
+    src = str(tmp_path / "in.ply")
+    E.write_mesh(src, mesh.points, mesh.faces)
+    native, python = tmp_path / "native", tmp_path / "python"
+    native.mkdir()
+    python.mkdir()
+    r = subprocess.run([os.path.join(B.OUT, prog), src] + args + ["-o", str(native) + "/"], capture_output=True,
+                       text=True)
+    assert r.returncode == 0, r.stderr
+    main = cli.main_acvd if prog == "acvd" else cli.main_acvdq
+    assert main([src] + args + ["-o", str(python) + "/"]) == 0
+    names = sorted(os.listdir(native))
+    assert names == sorted(os.listdir(python)) and names
+    for n in names:
+        assert (native / n).read_bytes() == (python / n).read_bytes(), n

@@ -133,3 +133,18 @@ def test_cli_rejects_unbuilt_options():
         cli.main_acvdq(["x.ply", "100", "0", "-d", "1"])
     with pytest.raises(SystemExit):
         cli.main_acvd(["x.ply"])
+
+
+def test_native_programs_parse_like_the_reference():
+    """The native ACVD / ACVDQ programs (csrc/acvd_cli.cpp) are built beside the library;
+    without arguments they print the usage, an option that needs an unbuilt part stops
+    them before any file or device is touched."""
+    import subprocess
+    from acvd_gb300 import build as B
+    for name in ("acvd", "acvdq"):
+        exe = os.path.join(B.OUT, name)
+        assert os.access(exe, os.X_OK)
+        r = subprocess.run([exe], capture_output=True, text=True)
+        assert r.returncode == 0 and "Usage" in r.stdout
+        r = subprocess.run([exe, "missing.ply", "100", "0", "-cd", "density.mhd"], capture_output=True, text=True)
+        assert r.returncode == 1 and "-cd" in r.stderr
