@@ -30,6 +30,8 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
+from acvd_gb300 import replicas  # noqa: E402  (after the repository root is on the path)
+
 METRIC = "time to converged ACVDQ energy (<=0.1% of ref), items/s, batched meshes/s"
 L2_BYTES = 129 * 1024 * 1024
 
@@ -602,10 +604,7 @@ def run_adjoint_arm(args):
 
 
 def _dist():
-    ws = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return ws, rank, local
+    return replicas.world()
 
 
 def make_workload(name):
@@ -758,8 +757,7 @@ def run_steps(torch, e, steps, warmup, device, ws, flush):
         e.rewind()
         e.minimize()
     torch.cuda.synchronize()
-    if ws > 1:
-        torch.distributed.barrier()
+    replicas.barrier()
     step_ms = []
     tot = {k: 0 for k in STEP_KEYS}
     st = None
@@ -808,9 +806,8 @@ def run_batch_arm(args):
 
     ws, rank, local = _dist()
     if ws > 1:
-        import torch.distributed as dist
         torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
+        replicas.init("nccl")
     device = local
     torch.cuda.set_device(device)
     w = BATCH_WORKLOADS[args.workload]
@@ -838,10 +835,7 @@ def run_batch_arm(args):
     _, tot_t, _ = run_steps(torch, engt, args.steps, 1, device, ws, flush)
     engt.close()
     ms = statistics.mean(step_ms)
-    if ws > 1:
-        t = torch.tensor([ms], device=f"cuda:{device}")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = replicas.max_over_ranks(ms, device=f"cuda:{device}")   # the slowest replica
     value = ws * b.n_mesh / (ms / 1000.0)
     packed = eng.labels()
     mesh_e = eng.mesh_energies()
@@ -876,8 +870,7 @@ def run_batch_arm(args):
         e2e = {"value": ws * b.n_mesh / (statistics.mean(e2e_ms) / 1000.0), "unit": "meshes/s",
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(b.labels0.nbytes),
                "ms_per_step": statistics.mean(e2e_ms)}
-    if ws > 1:
-        torch.distributed.barrier()
+    replicas.barrier()
     if rank != 0:
         return
     cpu = None
@@ -944,9 +937,8 @@ def run_gpu_arm(args):
 
     ws, rank, local = _dist()
     if ws > 1:
-        import torch.distributed as dist
         torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
+        replicas.init("nccl")
     device = local
     torch.cuda.set_device(device)
 
@@ -976,10 +968,7 @@ def run_gpu_arm(args):
     engt = make_engine(True)
     _, tot_t, _ = run_steps(torch, engt, args.steps, 1, device, ws, flush)
     engt.close()
-    if ws > 1:
-        t = torch.tensor([ms], device=f"cuda:{device}")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = replicas.max_over_ranks(ms, device=f"cuda:{device}")   # the slowest replica
     value = ws * n / (ms / 1000.0)
     lab = eng.labels()
     gpu_energy_fp64 = st["energy"]
@@ -1018,8 +1007,7 @@ def run_gpu_arm(args):
         e2e = {"value": e2e_val, "unit": "items/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                "ms_per_step": statistics.mean(e2e_ms)}
 
-    if ws > 1:
-        torch.distributed.barrier()
+    replicas.barrier()
     if rank != 0:
         return
 
