@@ -168,7 +168,8 @@ int acvd_set_labels(acvd_ctx* ctx, int32_t k, const int32_t* labels);
  * MinimizeEnergy.  Call after acvd_set_labels.
  */
 int acvd_set_frozen_clusters(acvd_ctx* ctx, const uint8_t* frozen);
-/* The frozen set in force (K bytes, 1 = frozen; all 0 when none is set). */
+/* The frozen set in force (K bytes, 1 = frozen; all 0 when none is set).  Reads what
+ * the reference keeps in IsClusterFreezed; no entry of the reference corresponds. */
 int acvd_get_frozen_clusters(acvd_ctx* ctx, uint8_t* frozen);
 
 /*
@@ -255,7 +256,8 @@ int acvd_subdivide(acvd_ctx* ctx, int64_t n_vertices, const double* xyz, int64_t
 /*
  * acvd_subdivide on device buffers (the same layouts, all in device memory of the
  * context's device), enqueued on the context's stream (acvd_stream): no allocation and
- * no synchronisation, for callers whose mesh is already resident.  d_work: at least
+ * no synchronisation, for callers whose mesh is already resident.  No counterpart in the
+ * reference, whose meshes live on the host.  d_work: at least
  * acvd_subdivide_work_bytes(n_edges) bytes, 16-byte aligned; after the stream reaches
  * this call, the uint32 at d_work + 8 n_edges bytes counts the faces that are
  * degenerate or have an edge missing from the ring CSR (their four output faces are
@@ -357,7 +359,9 @@ void* acvd_stream(acvd_ctx* ctx);
  * STL (binary), legacy VTK (ascii).  Only triangles: another polygon is
  * ACVD_ERR_UNSUPPORTED, as are .vtp and .wrl.  acvd_read_mesh allocates *xyz (3 nV
  * doubles) and *tri (3 nF int32) with malloc; release them with acvd_free.  The text of
- * the last failure of this thread is acvd_io_last_error().
+ * the last failure of this thread is acvd_io_last_error().  acvd_free and
+ * acvd_io_last_error have no counterpart in the reference (VTK owns its readers' memory
+ * and reports through its error macros).
  */
 int acvd_read_mesh(const char* path, double** xyz, int64_t* n_vertices, int32_t** tri, int64_t* n_faces);
 int acvd_write_mesh(const char* path, const double* xyz, int64_t n_vertices, const int32_t* tri, int64_t n_faces);
