@@ -1095,7 +1095,7 @@ ACVD_DEV unsigned ld_acquire(const unsigned* p) {
 // arrival, acquire load of the generation, fence after).  A wait that runs out
 // of spins sets the error flag; every later call then returns false and the
 // kernel ends.
-ACVD_DEV bool grid_barrier(GridBar* b) {
+ACVD_DEV bool grid_barrier(GridBar* b, long long max_spins = kBarrierSpins) {
     __shared__ int s_ok;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -1114,7 +1114,7 @@ ACVD_DEV bool grid_barrier(GridBar* b) {
                     ok = 0;
                     break;
                 }
-                if (++spins > kBarrierSpins) {
+                if (++spins > max_spins) {
                     atomicExch(&b->err, 1);
                     ok = 0;
                     break;
@@ -1128,6 +1128,19 @@ ACVD_DEV bool grid_barrier(GridBar* b) {
     }
     __syncthreads();
     return s_ok != 0;
+}
+
+// Self-check of the barrier's wait limit: block 1 never arrives, so block 0's wait
+// runs out after max_spins naps, sets the error flag and returns.
+__global__ void barrier_wait_limit_kernel(GridBar* bar, long long max_spins) {
+    if (blockIdx.x == 1) return;
+    grid_barrier(bar, max_spins);
+}
+
+cudaError_t launch_barrier_wait_limit(GridBar* bar, long long max_spins, cudaStream_t s) {
+    ++g_launches;
+    barrier_wait_limit_kernel<<<2, 32, 0, s>>>(bar, max_spins);
+    return cudaGetLastError();
 }
 
 template <int M>

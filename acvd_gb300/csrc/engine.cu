@@ -444,6 +444,20 @@ int acvd_set_mesh(acvd_ctx* ctx, int64_t n_vertices, const double* xyz, int64_t 
     CK(cudaMemcpyAsync(ctx->row.p, csr_row, (n_vertices + 1) * sizeof(int), cudaMemcpyHostToDevice, ctx->s));
     CK(cudaMemcpyAsync(ctx->col.p, csr_col, 2 * n_edges * sizeof(int), cudaMemcpyHostToDevice, ctx->s));
     CK(cudaMemcpyAsync(ctx->edge_v.p, edge_v, 2 * n_edges * sizeof(int), cudaMemcpyHostToDevice, ctx->s));
+    {
+        // every id in range before any kernel indexes with it
+        CK(ctx->dtmp.resize(2));
+        unsigned* bad = (unsigned*)ctx->dtmp.p;
+        unsigned h_bad = 0;
+        CK(cudaMemsetAsync(bad, 0, sizeof(unsigned), ctx->s));
+        CK(launch_validate_mesh(ctx->row.p, ctx->col.p, n_vertices, 2 * n_edges, ctx->tri.p, 3 * n_faces,
+                                ctx->edge_v.p, 2 * n_edges, bad, ctx->s));
+        CK(cudaMemcpyAsync(&h_bad, bad, sizeof h_bad, cudaMemcpyDeviceToHost, ctx->s));
+        CK(cudaStreamSynchronize(ctx->s));
+        if (h_bad)
+            return fail(ctx, ACVD_ERR_ARG, "acvd_set_mesh: " + std::to_string(h_bad) +
+                                                " ring offsets decrease or vertex ids lie outside [0, n_vertices)");
+    }
     // vertex -> faces in increasing face id (original ids): item build, curvature,
     // adjoint and post-placement read it
     {
@@ -1827,6 +1841,23 @@ extern "C" int acvd_fix_mesh_boundaries(acvd_ctx* ctx, double* new_points, int64
     }
     *n_new_points = n_pts;
     *n_new_faces = nfaces;
+    return ACVD_OK;
+}
+
+// Self-check of the device waits' limit (failure detection without a fault): the
+// persistent kernel's grid barrier, with one of two blocks never arriving.
+extern "C" int acvd_check_wait_limit(acvd_ctx* ctx, int64_t max_spins, int32_t* gave_up) {
+    if (!ctx || !gave_up || max_spins <= 0 || max_spins > (1ll << 24))
+        return fail(ctx, ACVD_ERR_ARG, "acvd_check_wait_limit: max_spins outside (0, 2^24]");
+    CK(cudaSetDevice(ctx->opts.device));
+    DBuf<GridBar> bar;
+    CK(bar.resize(1));
+    CK(cudaMemsetAsync(bar.p, 0, sizeof(GridBar), ctx->s));
+    CK(launch_barrier_wait_limit(bar.p, max_spins, ctx->s));
+    GridBar hb;
+    CK(cudaMemcpyAsync(&hb, bar.p, sizeof hb, cudaMemcpyDeviceToHost, ctx->s));
+    CK(cudaStreamSynchronize(ctx->s));
+    *gave_up = hb.err ? 1 : 0;
     return ACVD_OK;
 }
 

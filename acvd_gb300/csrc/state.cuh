@@ -224,6 +224,9 @@ cudaError_t launch_perm_degree(const int* row, const int* perm, int64_t n, uint3
 cudaError_t launch_perm_ring(const int* row, const int* col, const int* perm, const int* inv, const uint32_t* row_new,
                              int64_t n, int* col_new, cudaStream_t s);
 cudaError_t launch_map_ids(const int* in, int64_t m, const int* inv, int* out, cudaStream_t s);
+// the uploaded mesh arrays' ids and ring offsets checked on the device (*bad: violations)
+cudaError_t launch_validate_mesh(const int* row, const int* col, int64_t n, int64_t ncol, const int* tri,
+                                 int64_t ntri, const int* ev, int64_t nev, unsigned* bad, cudaStream_t s);
 // gather of labels that also counts those outside [0, k] in *bad
 cudaError_t launch_gather_labels(const int* src, const int* idx, int64_t n, int k, int* dst, unsigned* bad,
                                  cudaStream_t s);
@@ -237,6 +240,8 @@ cudaError_t launch_ring8(const int* row, const int* col, int64_t n, int* ring8, 
 // The sweep kernels take a colour class as the contiguous item range
 // [item0, item0 + count) of the internal order.
 cudaError_t launch_begin_sweep(const DevState& st, int ncolors, bool reset_claims, cudaStream_t s);
+// the grid barrier with one block that never arrives (its wait limit's self-check)
+cudaError_t launch_barrier_wait_limit(GridBar* bar, long long max_spins, cudaStream_t s);
 // device-side sweep loop (graph WHILE node): set the loop and mode conditions at the
 // start, and after each sweep (relaxed: e_now holds the energy after the sweep)
 cudaError_t launch_loop_start(const LoopState* ls, const RunFlags* flags, cudaGraphConditionalHandle h_loop,

@@ -420,6 +420,35 @@ cudaError_t launch_gather_i32(const int* src, const int* idx, int64_t n, int* ds
     return cudaGetLastError();
 }
 
+// Mesh arrays as uploaded: ring offsets non-decreasing, every vertex id (ring
+// neighbours, face corners, edge ends) in [0, n).  Counts the violations in *bad,
+// before any kernel indexes with those ids.
+__global__ void validate_mesh_kernel(const int* __restrict__ row, const int* __restrict__ col, int64_t n,
+                                     int64_t ncol, const int* __restrict__ tri, int64_t ntri,
+                                     const int* __restrict__ ev, int64_t nev, unsigned* __restrict__ bad) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    unsigned cnt = 0;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += stride)
+        cnt += row[t] > row[t + 1];
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < ncol; t += stride)
+        cnt += (unsigned)col[t] >= (unsigned)n;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < ntri; t += stride)
+        cnt += (unsigned)tri[t] >= (unsigned)n;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < nev; t += stride)
+        cnt += (unsigned)ev[t] >= (unsigned)n;
+    if (cnt) atomicAdd(bad, cnt);
+}
+
+cudaError_t launch_validate_mesh(const int* row, const int* col, int64_t n, int64_t ncol, const int* tri,
+                                 int64_t ntri, const int* ev, int64_t nev, unsigned* bad, cudaStream_t s) {
+    ++g_launches;
+    int dev = 0, sms = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    validate_mesh_kernel<<<4 * sms, 256, 0, s>>>(row, col, n, ncol, tri, ntri, ev, nev, bad);
+    return cudaGetLastError();
+}
+
 // dst[t] = src[idx[t]] for labels, counting the values outside [0, k] in *bad
 __global__ void gather_labels_kernel(const int* __restrict__ src, const int* __restrict__ idx, int64_t n, int k,
                                      int* __restrict__ dst, unsigned* __restrict__ bad) {

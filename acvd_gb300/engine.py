@@ -95,6 +95,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         "acvd_post_placement": (ctypes.c_int, [_P, ctypes.c_int, _P]),
         "acvd_compute_curvature": (ctypes.c_int, [_P, _P, _P]),
         "acvd_set_frozen_clusters": (ctypes.c_int, [_P, _P]),
+        "acvd_check_wait_limit": (ctypes.c_int, [_P, _i64, ctypes.POINTER(ctypes.c_int32)]),
         "acvd_get_frozen_clusters": (ctypes.c_int, [_P, _P]),
         "acvd_fix_mesh_boundaries": (ctypes.c_int, [_P, _P, ctypes.POINTER(_i64), _P, ctypes.POINTER(_i64)]),
         "acvd_force_manifold_step": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int32),
@@ -341,6 +342,13 @@ class Engine:
             raise ValueError("set_frozen_clusters needs one flag per cluster")
         self._frozen = f
         self._ck(self._lib.acvd_set_frozen_clusters(self.ctx, _ptr(f)), "acvd_set_frozen_clusters")
+
+    def check_wait_limit(self, max_spins: int = 1 << 18) -> bool:
+        """Runs the device barrier with one block never arriving: True when its wait
+        gave up (as it must) and returned."""
+        g = ctypes.c_int32(0)
+        self._ck(self._lib.acvd_check_wait_limit(self.ctx, int(max_spins), ctypes.byref(g)), "acvd_check_wait_limit")
+        return bool(g.value)
 
     def frozen_clusters(self) -> np.ndarray:
         out = np.empty(self.k, dtype=np.uint8)

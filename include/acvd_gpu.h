@@ -350,6 +350,16 @@ int acvd_adjoint(acvd_ctx* ctx, const double* xyz, const double* rho, double gra
 void* acvd_stream(acvd_ctx* ctx);
 
 /*
+ * Failure detection without a fault: every device wait of this library (the grid
+ * barrier of the persistent sweep kernel) gives up after a limited number of naps,
+ * sets an error flag that the host reads, and returns, leaving the context usable.
+ * This runs that barrier with one of two blocks never arriving and a limit of
+ * max_spins naps of 64 ns (at most 2^24); *gave_up is 1 when the wait ran out as it
+ * must.  A self-check with no counterpart in the reference.
+ */
+int acvd_check_wait_limit(acvd_ctx* ctx, int64_t max_spins, int32_t* gave_up);
+
+/*
  * Triangle-mesh files, host only: the formats vtkSurface::CreateFromFile / WriteToFile
  * dispatch on by name (Common/vtkSurface.cxx:1958-2136; the lower-cased name contains
  * ".vtk", ".ply", ".off", ".obj" or ".stl", tested in the reference's order).  Read:
