@@ -306,7 +306,7 @@ ACVD_DEV void eval_tile(const DevState& st, int item0, int64_t count, int color,
         n_scr = 1;
         const int L = st.label[i];
         const int ev_i = st.evald[i];
-        bool screened = false;
+        bool screened = !ACVD_VALID(st, L >= 0 && L <= st.k);   // a bad label is skipped
         if (code & kScrCached) {
             // the ring kept its labels since the last full screen: its distinct
             // neighbour clusters and the connectivity test are in the cache
@@ -794,6 +794,7 @@ ACVD_DEV void apply_range(const DevState& st, int item0, int color, int round, i
         if (B < 0) continue;                     // committed or dropped in an earlier round
         const int i = item0 + (int)idx;
         const int L = st.label[i];
+        if (!ACVD_VALID(st, B < st.k && L >= 0 && L <= st.k)) continue;
         const unsigned long long key = make_claim(epoch, cand_prio[idx], (unsigned)idx);
         if (st.claim[B] != key || (L < st.k && st.claim[L] != key)) continue;
         __syncwarp(pair_mask);                   // both lanes have read the claims and cand_dest
@@ -952,6 +953,7 @@ ACVD_DEV void relaxed_commit_range(const DevState& st, int item0, int color,
         const int i = item0 + (int)idx;
         const int B = cand_dest[idx];
         const int L = st.label[i];
+        if (!ACVD_VALID(st, B >= 0 && B < st.k && L >= 0 && L <= st.k)) continue;
         // sizes are untouched until fx_finalize: a cluster whose every member would
         // leave keeps them all
         if (L < st.k && st.size[L] - st.out_cnt[L] < 1) continue;

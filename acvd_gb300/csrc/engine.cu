@@ -1253,6 +1253,9 @@ extern "C" int acvd_minimize(acvd_ctx* ctx, acvd_stats* stats) {
     local.visited = (int64_t)ctx->h_counters[kCntVisited];
     local.slots = (int64_t)ctx->h_counters[kCntSlots];
     local.kernel_launches = g_launches - launches0;
+    if (ctx->h_counters[kCntError] && status == ACVD_OK)
+        status = fail(ctx, ACVD_ERR_DEVICE_CHECK,
+                      std::to_string(ctx->h_counters[kCntError]) + " device-side index checks failed");
     local.reverted = (int64_t)ctx->h_counters[kCntReverted];
     {
         // algorithmic bytes of the evaluation kernels: per visited item its boundary

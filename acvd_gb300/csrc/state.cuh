@@ -85,6 +85,16 @@ __device__ __forceinline__ unsigned long long* ctr(unsigned long long* counters,
     return counters + (blockIdx.x & (kStripes - 1)) * kNumCounters + which;
 }
 
+// Bounds checks of device-side indices, compiled in with -DACVD_DEVICE_CHECKS (the
+// build that stands in for a sanitizer): a failed check counts in kCntError, the access
+// is skipped and the host fails the call with ACVD_ERR_DEVICE_CHECK.  Without the flag
+// the checks compile away.
+#ifdef ACVD_DEVICE_CHECKS
+#define ACVD_VALID(st, cond) ((cond) || (atomicAdd(ctr((st).counters, kCntError), 1ull), false))
+#else
+#define ACVD_VALID(st, cond) true
+#endif
+
 // Sweep bookkeeping on the device (one captured graph serves every sweep):
 // `sweep` counts sweeps, `floor` is the sweep after which every cluster counts as
 // modified (the reference's SetAllClustersToModified, vtkUniformClustering.h:717-722).
