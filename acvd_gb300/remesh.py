@@ -111,6 +111,7 @@ class _DiscreteRemeshing:
         self.Display = 0
         self.MaxNumberOfLoops = 5000000
         self.InitialClustering = None
+        self._resume = False              # LoadClustering: take the clustering as computed
         self.ForceManifold = False
         self.BoundaryFixing = 0          # the constructor's value (vtkDiscreteRemeshing.h:1192)
         self.MaxNumberOfManifoldPasses = 1000
@@ -328,7 +329,12 @@ class _DiscreteRemeshing:
         return pts.shape[0] > 0
 
     def Remesh(self):
-        self.ProcessClustering()
+        if self._resume:
+            e = self._prepare()                    # uploads the loaded clustering
+            self.Clustering = e.labels()
+            self.Stats = None
+        else:
+            self.ProcessClustering()
         if self.ForceManifold:
             self._force_manifold()
         self.BuildDelaunayTriangulation()
@@ -342,6 +348,34 @@ class _DiscreteRemeshing:
 
     def GetBoundaryEdges(self) -> np.ndarray:
         return self._engine.boundary_edges()
+
+    # -- checkpoint / resume: the reference's FileLoadSaveOption files
+    # (vtkDiscreteRemeshing.h:899-932 clustering.dat, :655-700 curvature.dat), raw
+    # native-endian int32 / float64 per item, without the interactive prompts --
+    def SaveClustering(self, path: str = "clustering.dat") -> None:
+        if self.Clustering is None:
+            raise _eng.AcvdError(1, "no clustering to save")
+        np.ascontiguousarray(self.Clustering, dtype=np.int32).tofile(path)
+
+    def LoadClustering(self, path: str = "clustering.dat") -> np.ndarray:
+        """Reads a clustering written by SaveClustering (or the reference): the next
+        Remesh() takes it as computed and skips the minimisation, as the reference's load
+        path does (Init, read, ReComputeStatistics, then the coarse mesh).  The number of
+        values must match the mesh that is clustered (after any subdivision)."""
+        lab = np.fromfile(path, dtype=np.int32)
+        self.SetInitialClustering(lab)
+        self._resume = True
+        return lab
+
+    def SaveCurvature(self, path: str = "curvature.dat") -> None:
+        if self.Indicator is None:
+            raise _eng.AcvdError(1, "no curvature indicator to save")
+        np.ascontiguousarray(self.Indicator, dtype=np.float64).tofile(path)
+
+    def LoadCurvature(self, path: str = "curvature.dat") -> np.ndarray:
+        ind = np.fromfile(path, dtype=np.float64)
+        self.SetCurvatureInfo(ind, self.PrincipalDirections)
+        return ind
 
 
 class IsotropicDiscreteRemeshing(_DiscreteRemeshing):

@@ -66,3 +66,23 @@ def test_native_programs_match_the_python_drivers(tmp_path, prog, args):
     assert names == sorted(os.listdir(python)) and names
     for n in names:
         assert (native / n).read_bytes() == (python / n).read_bytes(), n
+
+
+def test_resume_from_a_saved_clustering(tmp_path):
+    """A clustering saved to clustering.dat and loaded again (the reference's load path:
+    no minimisation) gives the same clustering and the same coarse mesh."""
+    m = synth.torus(60, 30, seed=5)
+    r = acvd_gb300.QIsotropicDiscreteRemeshing()
+    r.SetInput(acvd_gb300.Surface(m.points, m.faces))
+    r.SetNumberOfClusters(150)
+    r.Remesh()
+    r.SaveClustering(str(tmp_path / "clustering.dat"))
+    r2 = acvd_gb300.QIsotropicDiscreteRemeshing()
+    r2.SetInput(acvd_gb300.Surface(m.points, m.faces))
+    r2.SetNumberOfClusters(150)
+    r2.LoadClustering(str(tmp_path / "clustering.dat"))
+    r2.Remesh()
+    np.testing.assert_array_equal(r2.GetClustering(), r.GetClustering())
+    assert r2.Stats is None                                     # nothing was minimised
+    np.testing.assert_array_equal(r2.GetOutput().points, r.GetOutput().points)
+    np.testing.assert_array_equal(r2.GetOutput().faces, r.GetOutput().faces)

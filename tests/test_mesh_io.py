@@ -148,3 +148,22 @@ def test_native_programs_parse_like_the_reference():
         assert r.returncode == 0 and "Usage" in r.stdout
         r = subprocess.run([exe, "missing.ply", "100", "0", "-cd", "density.mhd"], capture_output=True, text=True)
         assert r.returncode == 1 and "-cd" in r.stderr
+
+
+def test_checkpoint_files_round_trip(tmp_path):
+    """clustering.dat / curvature.dat as the reference's FileLoadSaveOption writes them:
+    raw int32 and float64 per item."""
+    r = acvd_gb300.QIsotropicDiscreteRemeshing()
+    lab = np.arange(50, dtype=np.int32) % 7
+    ind = np.linspace(0.1, 2.0, 50)
+    r.Clustering = lab
+    r.Indicator = ind
+    r.SaveClustering(str(tmp_path / "clustering.dat"))
+    r.SaveCurvature(str(tmp_path / "curvature.dat"))
+    assert (tmp_path / "clustering.dat").stat().st_size == 4 * 50
+    assert (tmp_path / "curvature.dat").stat().st_size == 8 * 50
+    r2 = acvd_gb300.QIsotropicDiscreteRemeshing()
+    np.testing.assert_array_equal(r2.LoadClustering(str(tmp_path / "clustering.dat")), lab)
+    np.testing.assert_array_equal(r2.InitialClustering, lab)
+    np.testing.assert_array_equal(r2.LoadCurvature(str(tmp_path / "curvature.dat")), ind)
+    np.testing.assert_array_equal(r2.Indicator, ind)
