@@ -33,7 +33,8 @@ from .remesh import (IsotropicDiscreteRemeshing, QIsotropicDiscreteRemeshing, Qu
 
 _UNBUILT = {
     "-l": "long-edge splitting (vtkSurface::SplitLongEdges)",
-    "-w": "the global energy log",
+    "-w": "the global energy log (which the reference's ACVD / ACVDQ write through an uninitialised "
+          "timer, vtkUniformClustering.h:1384-1395)",
     "-cd": "custom density images",
     "-cmin": "custom density images",
     "-cmax": "custom density images",
