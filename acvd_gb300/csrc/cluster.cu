@@ -268,13 +268,15 @@ ACVD_DEV void eval_tile(const DevState& st, int item0, int64_t count, int color,
     __shared__ int s_tgt[256][kMaxTgt];        // work item -> destination clusters (ring order)
     __shared__ float s_val[256][kMaxTgt + 1];  // energy parts: [j] add to s_tgt[j], [kMaxTgt] remove
     __shared__ signed char s_nt[256];          // destinations; -1: the whole test runs in B2
-    __shared__ unsigned short s_task[256 * (kMaxTgt + 1)];
+    __shared__ unsigned short s_task[256 * kMaxTgt];   // add tasks: (work item << 4) | destination
+    __shared__ unsigned char s_rem[256];                // work items whose remove part B1 computes
     __shared__ int s_scr[256];                 // flagged items of the tile (colour-list positions)
-    __shared__ unsigned s_nwork, s_ntask, s_nscr;
+    __shared__ unsigned s_nwork, s_ntask, s_nrem, s_nscr;
     __syncthreads();                     // the previous tile is done with the shared arrays
     if (threadIdx.x == 0) {
         s_nwork = 0u;
         s_ntask = 0u;
+        s_nrem = 0u;
         s_nscr = 0u;
     }
     __syncthreads();
@@ -334,9 +336,9 @@ ACVD_DEV void eval_tile(const DevState& st, int item0, int64_t count, int color,
                         s_nt[w] = (signed char)nt;
                         n_tgt += (unsigned)nt;
                         if (nt > 0) {
-                            const unsigned base = atomicAdd(&s_ntask, (unsigned)nt + 1u);
+                            const unsigned base = atomicAdd(&s_ntask, (unsigned)nt);
                             for (int j = 0; j < nt; j++) s_task[base + j] = (unsigned short)((w << 4) | j);
-                            s_task[base + nt] = (unsigned short)((w << 4) | kTaskRemove);
+                            s_rem[atomicAdd(&s_nrem, 1u)] = (unsigned char)w;
                         }
                     } else {
                         st.evald[i] = sw.sweep;   // evaluated: nothing it may do
@@ -436,9 +438,9 @@ ACVD_DEV void eval_tile(const DevState& st, int item0, int64_t count, int color,
                     s_nt[w] = (signed char)nt;
                     n_tgt += (unsigned)nt;
                     if (nt > 0) {
-                        const unsigned base = atomicAdd(&s_ntask, (unsigned)nt + 1u);
+                        const unsigned base = atomicAdd(&s_ntask, (unsigned)nt);
                         for (int j = 0; j < nt; j++) s_task[base + j] = (unsigned short)((w << 4) | j);
-                        s_task[base + nt] = (unsigned short)((w << 4) | kTaskRemove);
+                        s_rem[atomicAdd(&s_nrem, 1u)] = (unsigned char)w;
                     }
                 } else {
                     s_nt[w] = -1;
@@ -450,10 +452,11 @@ ACVD_DEV void eval_tile(const DevState& st, int item0, int64_t count, int color,
         }
     }
     __syncthreads();
-    // B1: energy parts
-    const unsigned ntask = s_ntask;
+    // B1: energy parts -- the remove parts first, then the add parts, so that a warp
+    // runs one kind
+    const unsigned nrem = s_nrem, ntask = nrem + s_ntask;
     for (unsigned t = threadIdx.x; t < ntask; t += 256) {
-        const unsigned code = s_task[t];
+        const unsigned code = t < nrem ? ((unsigned)s_rem[t] << 4) | (unsigned)kTaskRemove : s_task[t - nrem];
         const int w = (int)(code >> 4), j = (int)(code & 15u);
         const int i = item0 + s_idx[w];
         ItemRec it;
