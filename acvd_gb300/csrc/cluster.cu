@@ -271,12 +271,13 @@ ACVD_DEV void eval_tile(const DevState& st, int item0, int64_t count, int color,
     __shared__ unsigned short s_task[256 * kMaxTgt];   // add tasks: (work item << 4) | destination
     __shared__ unsigned char s_rem[256];                // work items whose remove part B1 computes
     __shared__ int s_scr[256];                 // flagged items of the tile (colour-list positions)
-    __shared__ unsigned s_nwork, s_ntask, s_nrem, s_nscr;
+    __shared__ unsigned s_nwork, s_ntask, s_nrem, s_nscr, s_nfull;
     __syncthreads();                     // the previous tile is done with the shared arrays
     if (threadIdx.x == 0) {
         s_nwork = 0u;
         s_ntask = 0u;
         s_nrem = 0u;
+        s_nfull = 0u;
         s_nscr = 0u;
     }
     __syncthreads();
@@ -287,21 +288,29 @@ ACVD_DEV void eval_tile(const DevState& st, int item0, int64_t count, int color,
     const RunFlags fl = *st.flags;
     unsigned n_slots = 0, n_bnd = 0, n_tgt = 0, n_cand = 0, n_scr = 0, n_cached = 0;
     // A0: only items that may lie on a boundary go on to the ring screen, packed
-    // so that warps without one issue nothing
+    // so that warps without one issue nothing: cached screens from the front of the
+    // list, full screens from its back, so that a warp runs one kind
     {
         const unsigned char bf = in ? st.bflag[item0 + idx_t] : (unsigned char)0;
-        const bool flagged = bf != 0;
-        const unsigned bal = __ballot_sync(kFull, flagged);
-        if (bal) {
-            const int lane = threadIdx.x & 31;
+        const int lane = threadIdx.x & 31;
+        const unsigned below = (1u << lane) - 1u;
+        const unsigned bal_c = __ballot_sync(kFull, bf == 2);
+        const unsigned bal_f = __ballot_sync(kFull, bf == 1);
+        if (bal_c) {
             unsigned base = 0;
-            if (lane == 0) base = atomicAdd(&s_nscr, (unsigned)__popc(bal));
+            if (lane == 0) base = atomicAdd(&s_nscr, (unsigned)__popc(bal_c));
             base = __shfl_sync(kFull, base, 0);
-            if (flagged) s_scr[base + __popc(bal & ((1u << lane) - 1u))] = (int)idx_t | (bf == 2 ? kScrCached : 0);
+            if (bf == 2) s_scr[base + __popc(bal_c & below)] = (int)idx_t | kScrCached;
+        }
+        if (bal_f) {
+            unsigned base = 0;
+            if (lane == 0) base = atomicAdd(&s_nfull, (unsigned)__popc(bal_f));
+            base = __shfl_sync(kFull, base, 0);
+            if (bf == 1) s_scr[255 - (base + __popc(bal_f & below))] = (int)idx_t;
         }
     }
     __syncthreads();
-    if (threadIdx.x < s_nscr) {
+    if (threadIdx.x < s_nscr || threadIdx.x >= 256u - s_nfull) {
         const int code = s_scr[threadIdx.x];
         const int64_t idx = code & ~kScrCached;
         const int i = item0 + (int)idx;
