@@ -14,10 +14,13 @@ Options are "-key value" pairs as in the reference:
               ACVDQ: the QEM metric's QuadricsOptimizationLevel (default 3)
     -d 0      display (only 0: there is no graphics stack)
     -np n     threads of the reference's threaded engine (accepted, unused)
+    -fv file  ACVDQ: vertex ids (whitespace separated) that stay output vertices
+    -ft file  ACVDQ: face ids whose three vertices stay output vertices
 
 Options of the reference that need parts this package does not build -- -l (long-edge
-splitting), -w (energy log), -cd/-cmin/-cmax/-cf (custom density image), -p (pooling),
--fv/-ft (fixed vertices) -- stop with an error rather than being ignored.
+splitting), -w (energy log), -cd/-cmin/-cmax/-cf (custom density image), -p (pooling)
+-- stop with an error rather than being ignored.  Other keys are ignored, as the
+reference programs ignore them.
 
 Outputs follow the reference: ACVD writes <dir>smooth_<name> before the post-placement
 and <dir>/<name> after it, in the format the name's extension selects; ACVDQ writes
@@ -27,6 +30,8 @@ from __future__ import annotations
 
 import os
 import sys
+
+import numpy as np
 
 from . import engine as _eng
 from .remesh import (IsotropicDiscreteRemeshing, QIsotropicDiscreteRemeshing, QuadricPostPlacement, Surface)
@@ -40,8 +45,6 @@ _UNBUILT = {
     "-cmax": "custom density images",
     "-cf": "custom density images",
     "-p": "pooling (the threaded engine)",
-    "-fv": "fixed vertices",
-    "-ft": "fixed vertices",
 }
 
 
@@ -59,12 +62,14 @@ def _parse(argv: list[str], prog: str):
     rest = argv[3:]
     if len(rest) % 2:
         raise SystemExit(f"{prog}: option {rest[-1]} without a value")
+    opts["_order"] = []
     for key, value in zip(rest[0::2], rest[1::2]):
         if key in _UNBUILT:
             raise SystemExit(f"{prog}: option {key} needs {_UNBUILT[key]}, which this build does not have")
         if key == "-d" and int(value) != 0:
             raise SystemExit(f"{prog}: display needs a graphics stack; only -d 0 is available")
         opts[key] = value
+        opts["_order"].append((key, value))
     return opts
 
 
@@ -101,17 +106,64 @@ def main_acvd(argv: list[str] | None = None) -> int:
     return 0
 
 
+def _read_ids(path: str) -> list[int]:
+    """Integers read one after the other until one does not parse (`input >> id`); an
+    unreadable file gives none."""
+    ids = []
+    try:
+        with open(path) as f:
+            for tok in f.read().split():
+                try:
+                    ids.append(int(tok))
+                except ValueError:
+                    break
+    except OSError:
+        pass
+    return ids
+
+
+def _fixed_vertices(opts, mesh: Surface):
+    """-fv / -ft (ACVDQ.cxx:246-280): the last of them given wins."""
+    fixed = None
+    for key, value in opts.get("_order", []):
+        if key == "-fv":
+            fixed = _read_ids(value)
+        elif key == "-ft":
+            faces = _read_ids(value)
+            mark = np.zeros(mesh.GetNumberOfPoints(), dtype=bool)
+            for f in faces:
+                mark[mesh.faces[f]] = True
+            fixed = [int(v) for v in np.nonzero(mark)[0]]
+            print(f"Added {len(faces)} constraints on triangles")
+    return None if fixed is None else np.asarray(fixed, dtype=np.int32)
+
+
 def main_acvdq(argv: list[str] | None = None) -> int:
     """ACVDQ (DiscreteRemeshing/Examples/ACVDQ.cxx): QEM metric with the unconstrained
-    first phase; the output is written as binary PLY."""
+    first phase; the output is written as binary PLY.  With -fv / -ft the fixed vertices
+    are the first output vertices, anchored in place (:327-363)."""
     argv = sys.argv[1:] if argv is None else argv
     opts = _parse(argv, "ACVDQ")
     r = _remesh(opts, QIsotropicDiscreteRemeshing, 2)
     if "-q" in opts:
         r.GetMetric().SetQuadricsOptimizationLevel(int(opts["-q"]))
     r.SetUnconstrainedInitialization(1)
+    mesh = r.GetInput()
+    fixed = _fixed_vertices(opts, mesh)
+    if fixed is not None:
+        r.SetFixedClusters(fixed)
+        r.SetNumberOfClusters(opts["n"] + len(fixed))
+        print(f"Read {len(fixed)} fixed Ids")
+        for i, v in enumerate(fixed):
+            r.GetCluster(i).AnchorItem = int(v)
     r.Remesh()
     out = r.GetOutput()
+    if fixed is not None:
+        for i, v in enumerate(fixed):
+            if not np.array_equal(mesh.points[v], out.points[i]):
+                print(f"Error, vertex {v} has been lost")
+                return 1
+        print("Constraints on vertices have been checked")
     path = (opts.get("-o") or "") + opts.get("-of", "simplification.ply")
     # the reference writes with vtkPLYWriter whatever the name says
     tmp = path if ".ply" in path.lower() and ".vtk" not in path.lower() else \

@@ -9,13 +9,16 @@
 // gradation asks for it (interpolated through the subdivision), the reference's initial
 // sampling, MinimizeEnergy, the ForceManifold loop, the coarse mesh (centroids stored as
 // floats, dual triangles), FixMeshBoundaries; then ACVD's quadric post-placement
-// (ACVD.cxx:217-291) or ACVDQ's PLY output (ACVDQ.cxx:368-376).  Options that need
-// parts this build does not have stop with an error.
+// (ACVD.cxx:217-291) or ACVDQ's PLY output (ACVDQ.cxx:368-376).  ACVDQ's fixed
+// vertices (-fv ids, -ft faces; ACVDQ.cxx:246-280, 327-363) become the first clusters,
+// anchored at those vertices.  Options that need parts this build does not have stop
+// with an error; keys the program does not know are ignored, as the reference's are.
 #include <cctype>
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <fstream>
 #include <string>
 #include <vector>
 
@@ -67,6 +70,15 @@ void set_mesh(acvd_ctx* ctx, const Mesh& m) {
           "acvd_set_mesh");
 }
 
+// integers read one after the other until one does not parse (`input >> id`)
+std::vector<int32_t> read_ids(const char* path) {
+    std::vector<int32_t> ids;
+    std::ifstream in(path);
+    int id;
+    while (in >> id) ids.push_back(id);
+    return ids;
+}
+
 void write_mesh(const std::string& path, const std::vector<double>& xyz, const std::vector<int32_t>& tri) {
     if (acvd_write_mesh(path.c_str(), xyz.data(), (int64_t)xyz.size() / 3, tri.data(), (int64_t)tri.size() / 3))
         die("writing " + path + ": " + acvd_io_last_error());
@@ -85,7 +97,7 @@ int main(int argc, char** argv) {
         return 0;
     }
     const char* file = argv[1];
-    const int k = std::atoi(argv[2]);
+    int k = std::atoi(argv[2]);
     const double gradation = std::atof(argv[3]);
     int boundary_fixing = 0, force_manifold = 0, threshold = 10;
 #ifdef ACVD_CLI_QEM
@@ -95,6 +107,7 @@ int main(int argc, char** argv) {
 #endif
     std::string outdir, outfile = "simplification.ply";
     bool have_outdir = false;
+    std::string fixed_key, fixed_file;   // the last -fv / -ft given (ACVDQ)
     for (int a = 4; a < argc; a += 2) {
         if (a + 1 >= argc) die(std::string("option ") + argv[a] + " without a value");
         const std::string key = argv[a];
@@ -109,9 +122,15 @@ int main(int argc, char** argv) {
         else if (key == "-d") {
             if (std::atoi(value) != 0) die("display needs a graphics stack; only -d 0 is available");
         } else if (key == "-l" || key == "-w" || key == "-cd" || key == "-cmin" || key == "-cmax" || key == "-cf" ||
-                   key == "-p" || key == "-fv" || key == "-ft") {
+                   key == "-p") {
             die("option " + key + " needs a part this build does not have");
         }
+#ifdef ACVD_CLI_QEM
+        else if (key == "-fv" || key == "-ft") {
+            fixed_key = key;
+            fixed_file = value;
+        }
+#endif
     }
     if (k <= 0) die("nvertices must be positive");
 
@@ -129,6 +148,29 @@ int main(int argc, char** argv) {
     topology(m);
     std::printf("load : %s\nMesh with %lld vertices, %lld faces, %lld edges\n", file, (long long)m.nv(),
                 (long long)m.nf(), (long long)m.ne());
+    // fixed vertices: -fv lists vertex ids, -ft face ids whose vertices are fixed
+    std::vector<int32_t> fixed;
+    const bool has_fixed = !fixed_key.empty();
+    const std::vector<double> input_xyz = has_fixed ? m.xyz : std::vector<double>();
+    if (fixed_key == "-fv") {
+        fixed = read_ids(fixed_file.c_str());
+    } else if (fixed_key == "-ft") {
+        const std::vector<int32_t> faces = read_ids(fixed_file.c_str());
+        std::vector<char> mark(m.nv(), 0);
+        for (int32_t f : faces) {
+            if (f < 0 || f >= m.nf()) die("-ft: face id " + std::to_string(f) + " outside the mesh");
+            for (int q = 0; q < 3; q++) mark[m.tri[3 * (int64_t)f + q]] = 1;
+        }
+        for (int64_t v = 0; v < m.nv(); v++)
+            if (mark[v]) fixed.push_back((int32_t)v);
+        std::printf("Added %d constraints on triangles\n", (int)faces.size());
+    }
+    if (has_fixed) {
+        for (int32_t v : fixed)
+            if (v < 0 || v >= m.nv()) die("fixed vertex id " + std::to_string(v) + " outside the mesh");
+        k += (int)fixed.size();   // SetNumberOfClusters(numberOfSamples + fixed vertices)
+        std::printf("Read %d fixed Ids\n", (int)fixed.size());
+    }
 
     acvd_opts opts;
     acvd_default_opts(&opts);
@@ -180,9 +222,14 @@ int main(int argc, char** argv) {
                                        nullptr, need_ind ? ind.data() : nullptr, gradation, weights.data()),
           "acvd_vertex_weights");
     std::vector<int32_t> labels(m.nv());
-    check(nullptr, acvd_initial_sampling(m.nv(), m.row.data(), m.col.data(), weights.data(), k, labels.data()),
+    check(nullptr, acvd_initial_sampling_fixed(m.nv(), m.row.data(), m.col.data(), weights.data(), k,
+                                               (int32_t)fixed.size(), fixed.data(), labels.data()),
           "acvd_initial_sampling");
     check(ctx, acvd_set_labels(ctx, k, labels.data()), "acvd_set_labels");
+    if (has_fixed) {
+        check(ctx, acvd_set_fixed_clusters(ctx, (int32_t)fixed.size(), fixed.data()), "acvd_set_fixed_clusters");
+        check(ctx, acvd_set_anchor_items(ctx, (int32_t)fixed.size(), fixed.data()), "acvd_set_anchor_items");
+    }
     acvd_stats st;
     check(ctx, acvd_minimize(ctx, &st), "acvd_minimize");
     std::printf("The clustering took :%g seconds.\nNumber of loops:\t%d\n", st.device_ms / 1000.0, st.sweeps);
@@ -224,6 +271,17 @@ int main(int argc, char** argv) {
     }
     std::printf("Coarse mesh: %lld vertices, %lld faces\n", (long long)out_xyz.size() / 3, (long long)nt);
 #ifdef ACVD_CLI_QEM
+    // the fixed vertices are the first output vertices, in place (ACVDQ.cxx:341-363)
+    if (has_fixed) {
+        for (size_t i = 0; i < fixed.size(); i++)
+            for (int q = 0; q < 3; q++)
+                if (input_xyz[3 * (size_t)fixed[i] + q] != out_xyz[3 * i + q]) {
+                    std::printf("Error, vertex %d has been lost\n", (int)fixed[i]);
+                    acvd_destroy(ctx);
+                    return 1;
+                }
+        std::printf("Constraints on vertices have been checked\n");
+    }
     // ACVDQ writes PLY whatever the name says
     const std::string path = outdir + outfile;
     std::string low = path;

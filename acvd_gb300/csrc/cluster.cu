@@ -54,18 +54,32 @@ struct EvalRec {
     float A[6];
     float T[6];
     float g[3];
+    float anc;      // QEM: nonzero for an anchored cluster, whose m is the anchor vertex
+    int anc_item;   // ... and the anchor's item
 };
+
+// Cluster k's anchor item (QEM Cluster::AnchorItem), -1 for none
+template <int M>
+ACVD_DEV int anchor_of(const DevState& st, int64_t k) {
+    return (M == kQEM && st.anchor) ? st.anchor[k] : -1;
+}
 
 template <int M>
 ACVD_DEV void load_eval(const DevState& st, int k, EvalRec& e) {
     const float4* p = st.ev + (int64_t)k * Layout<M>::ev;
     const float4 e0 = p[0];
     e.m[0] = e0.x; e.m[1] = e0.y; e.m[2] = e0.z; e.W = e0.w;
+    e.anc = 0.0f;
+    e.anc_item = -1;
     if (M != kIso) {
         const float4 e1 = p[1], e2 = p[2], e3 = p[3], e4 = p[4];
         e.d[0] = e1.x; e.d[1] = e1.y; e.d[2] = e1.z; e.P = e1.w;
         e.r[0] = e2.x; e.r[1] = e2.y; e.r[2] = e2.z;
         e.A[0] = e3.x; e.A[1] = e3.y; e.A[2] = e3.z; e.A[3] = e3.w; e.A[4] = e4.x; e.A[5] = e4.y;
+        if (M == kQEM) {
+            e.anc = e4.z;
+            e.anc_item = __float_as_int(e4.w);
+        }
     }
     if (M == kAniso) {
         const float4 e5 = p[5], e6 = p[6], e7 = p[7];
@@ -123,6 +137,15 @@ ACVD_DEV float item_quad(const float T[6], const float v[3]) {
     return v[0] * Tv[0] + v[1] * Tv[1] + v[2] * Tv[2];
 }
 
+// Removing its anchor item from a QEM cluster breaks the anchor, which the reference
+// prices at 1e100 (vtkQEMetricForClustering.h:194-200, 259): such a move is never taken.
+constexpr float kBrokenAnchor = 1e30f;
+
+template <int M>
+ACVD_DEV bool is_anchor_item(const EvalRec& eL, int i) {
+    return M == kQEM && eL.anc != 0.0f && eL.anc_item == i;
+}
+
 // Part of the energy change that depends on the source cluster L only.
 template <int M>
 ACVD_DEV float remove_part(const EvalRec& eL, const ItemRec& it, const RunFlags& fl, float cprime[3]) {
@@ -130,6 +153,7 @@ ACVD_DEV float remove_part(const EvalRec& eL, const ItemRec& it, const RunFlags&
     const float d2 = xm[0] * xm[0] + xm[1] * xm[1] + xm[2] * xm[2];
     if (M == kIso) return -it.w * eL.W / (eL.W - it.w) * d2;
     if (M == kQEM) {
+        if (eL.anc != 0.0f) return -it.w * d2;   // placed vertex fixed at the anchor: -w |x - p|^2
         float v = -it.w * eL.W / (eL.W - it.w) * d2;
         if (fl.constrained && fl.level > 0) {
             float Wn, dm[3], dn[3];
@@ -153,6 +177,7 @@ ACVD_DEV float add_part(const EvalRec& eB, const ItemRec& it, const RunFlags& fl
     const float d2 = xm[0] * xm[0] + xm[1] * xm[1] + xm[2] * xm[2];
     if (M == kIso) return it.w * eB.W / (eB.W + it.w) * d2;
     if (M == kQEM) {
+        if (eB.anc != 0.0f) return it.w * d2;
         float v = it.w * eB.W / (eB.W + it.w) * d2;
         if (fl.constrained && fl.level > 0) {
             float Wn, dm[3], dn[3];
@@ -474,7 +499,7 @@ ACVD_DEV void eval_tile(const DevState& st, int item0, int64_t count, int color,
             EvalRec eL;
             load_eval<M>(st, st.label[i], eL);
             float xc[3];
-            s_val[w][kMaxTgt] = remove_part<M>(eL, it, fl, xc);
+            s_val[w][kMaxTgt] = is_anchor_item<M>(eL, i) ? kBrokenAnchor : remove_part<M>(eL, it, fl, xc);
         } else {
             EvalRec eB;
             load_eval<M>(st, s_tgt[w][j], eB);
@@ -528,7 +553,7 @@ ACVD_DEV void eval_tile(const DevState& st, int item0, int64_t count, int color,
                 EvalRec eL;
                 load_eval<M>(st, L, eL);
                 float xc[3];
-                const float rem = remove_part<M>(eL, it, fl, xc);
+                const float rem = is_anchor_item<M>(eL, i) ? kBrokenAnchor : remove_part<M>(eL, it, fl, xc);
                 float bde = 0.0f, badd = 0.0f;
                 for (int p = p0; p < p1; p++) {
                     const int B = st.label[st.col[p]];
@@ -664,9 +689,10 @@ ACVD_DEV void accumulate_item(df* acc, const ItemRec& it, float sgn) {
 // formulas as the FP64 full recompute below (ComputeClusterCentroid +
 // ComputeClusterEnergy of the metric plugins): m = S / W, residual r = b - A m,
 // placement delta = pinv(A) r in float32 (the evaluation kernel's), P = W |delta|^2.
-// Writes the record to ev[0 .. Layout<M>::ev) and returns the energy.
+// Writes the record to ev[0 .. Layout<M>::ev) and returns the energy.  anc: the
+// anchor vertex of an anchored QEM cluster (null: none) and anc_item its item.
 template <int M>
-ACVD_DEV double cluster_record_df(const df* a, const RunFlags& fl, float4* ev) {
+ACVD_DEV double cluster_record_df(const df* a, const RunFlags& fl, float4* ev, const double* anc, int anc_item) {
     const df W = a[3];
     if (!(W.hi > 0.0f)) {
 #pragma unroll
@@ -680,6 +706,19 @@ ACVD_DEV double cluster_record_df(const df* a, const RunFlags& fl, float4* ev) {
     if (M == kIso) return -df_to_d(S2W);
     const df* A = a + 4;    // a00 a01 a02 a11 a12 a22
     const df* b = a + 10;
+    if (M == kQEM && anc) {
+        // the placed vertex is the anchor p (ComputeClusterCentroid,
+        // vtkQEMetricForClustering.h:268-275): E = W |p|^2 - 2 p.S = W |p - m|^2 - |S|^2 / W
+        const df q[3] = {df_sub(df_from_d(anc[0]), m[0]), df_sub(df_from_d(anc[1]), m[1]),
+                         df_sub(df_from_d(anc[2]), m[2])};
+        const df qq = df_add(df_add(df_mul(q[0], q[0]), df_mul(q[1], q[1])), df_mul(q[2], q[2]));
+        ev[0] = make_float4((float)anc[0], (float)anc[1], (float)anc[2], W.hi);
+        ev[1] = make_float4(0.f, 0.f, 0.f, 0.f);
+        ev[2] = make_float4(0.f, 0.f, 0.f, 0.f);
+        ev[3] = make_float4(A[0].hi, A[1].hi, A[2].hi, A[3].hi);
+        ev[4] = make_float4(A[4].hi, A[5].hi, 1.0f, __int_as_float(anc_item));
+        return df_to_d(df_sub(df_mul(W, qq), S2W));
+    }
     const int rowi[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
     df r[3];
 #pragma unroll
@@ -730,7 +769,9 @@ ACVD_DEV void update_cluster(const DevState& st, int k) {
 #pragma unroll
         for (int q = 0; q < Layout<M>::acc; q++) al[q] = a[q];
         float4 el[Layout<M>::ev];
-        const double e = cluster_record_df<M>(al, *st.flags, el);
+        const int ak = anchor_of<M>(st, k);
+        const double e =
+            cluster_record_df<M>(al, *st.flags, el, ak >= 0 ? st.anchor_xyz + 3 * (int64_t)k : nullptr, ak);
 #pragma unroll
         for (int q = 0; q < Layout<M>::ev; q++) ev[q] = el[q];
         st.energy[k] = e;
@@ -755,6 +796,19 @@ ACVD_DEV void update_cluster(const DevState& st, int k) {
     double A[6], b[3];
     for (int j = 0; j < 6; j++) A[j] = df_to_d(a[4 + j]);
     for (int j = 0; j < 3; j++) b[j] = df_to_d(a[10 + j]);
+    const int ak = anchor_of<M>(st, k);
+    if (M == kQEM && ak >= 0) {
+        // anchored: the vertex itself, and ComputeClusterEnergy's expression
+        // (vtkQEMetricForClustering.h:194-208) as written
+        const double* c = st.anchor_xyz + 3 * (int64_t)k;
+        ev[0] = make_float4((float)c[0], (float)c[1], (float)c[2], (float)W);
+        ev[1] = make_float4(0.f, 0.f, 0.f, 0.f);
+        ev[2] = make_float4(0.f, 0.f, 0.f, 0.f);
+        ev[3] = make_float4((float)A[0], (float)A[1], (float)A[2], (float)A[3]);
+        ev[4] = make_float4((float)A[4], (float)A[5], 1.0f, __int_as_float(ak));
+        st.energy[k] = (c[0] * c[0] + c[1] * c[1] + c[2] * c[2]) * W - 2.0 * (c[0] * S[0] + c[1] * S[1] + c[2] * S[2]);
+        return;
+    }
     double Am[3];
     sym_mul<double>(A, m, Am);
     const double r[3] = {b[0] - Am[0], b[1] - Am[1], b[2] - Am[2]};
@@ -842,7 +896,9 @@ ACVD_DEV void apply_range(const DevState& st, int item0, int color, int round, i
         for (int q = 0; q < Layout<M>::acc; q++) nC[q] = aC[q];
         accumulate_item<M>(nC, it, role ? -1.0f : 1.0f);
         float4 rC[Layout<M>::ev];
-        const double en_mine = cluster_record_df<M>(nC, fl, rC);
+        const int anc = anchor_of<M>(st, C);
+        const double en_mine =
+            cluster_record_df<M>(nC, fl, rC, anc >= 0 ? st.anchor_xyz + 3 * (int64_t)C : nullptr, anc);
         const double e_other = __shfl_xor_sync(pair_mask, e_mine, 1);
         const double en_other = __shfl_xor_sync(pair_mask, en_mine, 1);
         // energy of the pair in the order B + L on both lanes
@@ -1021,7 +1077,8 @@ ACVD_DEV void fx_finalize_range(const DevState& st, int64_t k0, int64_t kstride)
 #pragma unroll
         for (int q = 0; q < NA; q++) al[q] = df_add(al[q], from_fixed(dl[q], st.fx_pow[q]));
         float4 el[Layout<M>::ev];
-        const double e = cluster_record_df<M>(al, *st.flags, el);
+        const int ak = anchor_of<M>(st, k);
+        const double e = cluster_record_df<M>(al, *st.flags, el, ak >= 0 ? st.anchor_xyz + 3 * k : nullptr, ak);
         float4* ev = st.ev + k * Layout<M>::ev;
 #pragma unroll
         for (int q = 0; q < NA; q++) {
@@ -1404,7 +1461,12 @@ __global__ void comp_step_kernel(DevState st, int* __restrict__ comp) {
 __global__ void comp_size_kernel(DevState st, const int* __restrict__ comp, int* __restrict__ csize) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= st.n) return;
-    if (st.label[i] < st.k) atomicAdd(&csize[comp[i]], 1);
+    const int L = st.label[i];
+    if (L >= st.k) return;
+    // the component holding the cluster's fixed item outweighs any other
+    // (vtkUniformClustering.h:439-447)
+    const bool fixed_item = L < st.nfixed && st.fixed[L] == (int)i;
+    atomicAdd(&csize[comp[i]], fixed_item ? 1000000000 : 1);
 }
 
 __global__ void comp_best_kernel(DevState st, const int* __restrict__ comp, const int* __restrict__ csize,
@@ -1532,6 +1594,10 @@ template <int M>
 __global__ void centroids_kernel(DevState st, double* __restrict__ out) {
     const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= st.k) return;
+    if (anchor_of<M>(st, k) >= 0) {   // an anchored cluster's vertex is its anchor
+        for (int j = 0; j < 3; j++) out[3 * k + j] = st.anchor_xyz[3 * k + j];
+        return;
+    }
     const df* a = st.acc + k * Layout<M>::acc;
     const double W = df_to_d(a[3]);
     double m[3] = {df_to_d(a[0]) / W, df_to_d(a[1]) / W, df_to_d(a[2]) / W};

@@ -133,6 +133,12 @@ struct acvd_ctx {
     DBuf<unsigned char> frozen;    // per cluster (K + 1): IsClusterFreezed; used when has_frozen
     bool has_frozen = false;
     std::vector<unsigned char> h_frozen;
+    // fixed vertices (FixedClusters) and anchored QEM clusters (Cluster::AnchorItem), as
+    // vertex ids; the device copies hold items and are rebuilt for every K
+    std::vector<int> h_fixed, h_anchor;
+    DBuf<int> fixed_item, anchor_item, anchor_ids;
+    DBuf<double> anchor_xyz;
+    bool has_anchor = false;
 
     // set-up work buffers, kept between calls: a repeated set-up (same or smaller
     // mesh) allocates nothing, and so does not synchronise the device in cudaFree
@@ -192,6 +198,10 @@ struct acvd_ctx {
         st.orig = perm.p;
         st.inv = inv.p;
         st.frozen = has_frozen ? frozen.p : nullptr;
+        st.anchor = has_anchor ? anchor_item.p : nullptr;
+        st.anchor_xyz = has_anchor ? anchor_xyz.p : nullptr;
+        st.nfixed = (int)h_fixed.size();
+        st.fixed = h_fixed.empty() ? nullptr : fixed_item.p;
         return st;
     }
     cudaGraphExec_t relaxed_exec = nullptr;
@@ -429,6 +439,9 @@ int acvd_set_mesh(acvd_ctx* ctx, int64_t n_vertices, const double* xyz, int64_t 
     CK(cudaSetDevice(ctx->opts.device));
     ctx->drop_graph();
     ctx->ready_mesh = ctx->ready_metric = ctx->ready_labels = false;
+    ctx->h_fixed.clear();    // vertex ids of the previous mesh
+    ctx->h_anchor.clear();
+    ctx->has_anchor = false;
     ctx->nmesh = 0;
     ctx->nV = n_vertices;
     ctx->nF = n_faces;
@@ -632,6 +645,8 @@ int acvd_set_unconstrained_initialization(acvd_ctx* ctx, int on) {
     return ACVD_OK;
 }
 
+static int sync_fixed(acvd_ctx* ctx);
+
 int acvd_set_labels(acvd_ctx* ctx, int32_t k, const int32_t* labels) {
     if (!ctx) return ACVD_ERR_ARG;
     if (!ctx->ready_mesh) return fail(ctx, ACVD_ERR_ARG, "acvd_set_labels before acvd_set_mesh");
@@ -671,7 +686,67 @@ int acvd_set_labels(acvd_ctx* ctx, int32_t k, const int32_t* labels) {
         return fail(ctx, ACVD_ERR_ARG, std::to_string(h_bad) + " labels outside [0, K]");
     }
     ctx->ready_labels = true;
+    if (!ctx->h_fixed.empty() || ctx->has_anchor || !ctx->h_anchor.empty()) return sync_fixed(ctx);
     return ACVD_OK;
+}
+
+// Device copies of the fixed items and the anchored clusters for the current K
+// (clusters added since the anchors were given have none).
+static int sync_fixed(acvd_ctx* ctx) {
+    const int nf = (int)ctx->h_fixed.size(), K = ctx->K;
+    if (nf > K) return fail(ctx, ACVD_ERR_ARG, std::to_string(nf) + " fixed vertices for " + std::to_string(K) +
+                                                   " clusters");
+    std::vector<int> ids(ctx->h_fixed);
+    bool any = false;
+    for (int c = 0; c < K; c++) {
+        const int a = c < (int)ctx->h_anchor.size() ? ctx->h_anchor[c] : -1;
+        ids.push_back(a);
+        any |= a >= 0;
+    }
+    ctx->drop_graph();   // the captured sweeps hold the state's pointers
+    CK(ctx->anchor_ids.resize(nf + K));
+    CK(cudaMemcpyAsync(ctx->anchor_ids.p, ids.data(), ids.size() * sizeof(int), cudaMemcpyHostToDevice, ctx->s));
+    if (nf > 0) {
+        CK(ctx->fixed_item.resize(nf));
+        CK(launch_anchor_setup(ctx->anchor_ids.p, nf, ctx->inv.p, ctx->xyz.p, ctx->fixed_item.p, nullptr, ctx->s));
+    }
+    ctx->has_anchor = any;
+    if (any) {
+        CK(ctx->anchor_item.resize(K));
+        CK(ctx->anchor_xyz.resize(3 * (size_t)K));
+        CK(launch_anchor_setup(ctx->anchor_ids.p + nf, K, ctx->inv.p, ctx->xyz.p, ctx->anchor_item.p,
+                               ctx->anchor_xyz.p, ctx->s));
+    }
+    CK(cudaStreamSynchronize(ctx->s));
+    return ACVD_OK;
+}
+
+int acvd_set_fixed_clusters(acvd_ctx* ctx, int32_t n_fixed, const int32_t* vertex_ids) {
+    if (!ctx) return ACVD_ERR_ARG;
+    if (!ctx->ready_mesh) return fail(ctx, ACVD_ERR_ARG, "acvd_set_fixed_clusters before acvd_set_mesh");
+    if (n_fixed < 0 || (n_fixed > 0 && !vertex_ids)) return fail(ctx, ACVD_ERR_ARG, "acvd_set_fixed_clusters: bad list");
+    for (int c = 0; c < n_fixed; c++)
+        if (vertex_ids[c] < 0 || vertex_ids[c] >= ctx->nV)
+            return fail(ctx, ACVD_ERR_ARG, "acvd_set_fixed_clusters: vertex id outside [0, n_vertices)");
+    if (ctx->ready_labels && n_fixed > ctx->K)
+        return fail(ctx, ACVD_ERR_ARG, "acvd_set_fixed_clusters: more fixed vertices than clusters");
+    CK(cudaSetDevice(ctx->opts.device));
+    ctx->h_fixed.assign(vertex_ids, vertex_ids + n_fixed);
+    return ctx->ready_labels ? sync_fixed(ctx) : ACVD_OK;
+}
+
+int acvd_set_anchor_items(acvd_ctx* ctx, int32_t n, const int32_t* anchors) {
+    if (!ctx) return ACVD_ERR_ARG;
+    if (!ctx->ready_metric) return fail(ctx, ACVD_ERR_ARG, "acvd_set_anchor_items before acvd_set_metric");
+    if (ctx->metric != kQEM && n > 0)
+        return fail(ctx, ACVD_ERR_UNSUPPORTED, "anchor items belong to the QEM metric's clusters");
+    if (n < 0 || (n > 0 && !anchors)) return fail(ctx, ACVD_ERR_ARG, "acvd_set_anchor_items: bad list");
+    for (int c = 0; c < n; c++)
+        if (anchors[c] < -1 || anchors[c] >= ctx->nV)
+            return fail(ctx, ACVD_ERR_ARG, "acvd_set_anchor_items: vertex id outside [-1, n_vertices)");
+    CK(cudaSetDevice(ctx->opts.device));
+    ctx->h_anchor.assign(anchors, anchors + n);
+    return ctx->ready_labels ? sync_fixed(ctx) : ACVD_OK;
 }
 
 int acvd_set_frozen_clusters(acvd_ctx* ctx, const uint8_t* frozen) {
@@ -787,6 +862,17 @@ static int clean(acvd_ctx* ctx, int* n_disconnected) {
     int r = sync_counters(ctx);
     if (r) return r;
     *n_disconnected = (int)ctx->h_counters[kCntDisconnected];
+    return ACVD_OK;
+}
+
+extern "C" int acvd_clean_clustering(acvd_ctx* ctx, int32_t* n_disconnected) {
+    if (!ctx || !n_disconnected) return ACVD_ERR_ARG;
+    if (!ctx->ready_labels) return fail(ctx, ACVD_ERR_ARG, "acvd_clean_clustering before acvd_set_labels");
+    CK(cudaSetDevice(ctx->opts.device));
+    int n = 0;
+    const int r = clean(ctx, &n);
+    if (r) return r;
+    *n_disconnected = n;
     return ACVD_OK;
 }
 

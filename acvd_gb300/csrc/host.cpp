@@ -171,9 +171,22 @@ int acvd_vertex_weights(int metric, int64_t n_vertices, const double* xyz, int64
 
 int acvd_initial_sampling(int64_t n_vertices, const int32_t* csr_row, const int32_t* csr_col,
                           const double* weights, int32_t k, int32_t* labels) {
+    return acvd_initial_sampling_fixed(n_vertices, csr_row, csr_col, weights, k, 0, nullptr, labels);
+}
+
+int acvd_initial_sampling_fixed(int64_t n_vertices, const int32_t* csr_row, const int32_t* csr_col,
+                                const double* weights, int32_t k, int32_t n_fixed, const int32_t* fixed_ids,
+                                int32_t* labels) {
     if (n_vertices <= 0 || k <= 0 || !csr_row || !csr_col || !weights || !labels) return ACVD_ERR_ARG;
+    if (n_fixed < 0 || n_fixed > k || (n_fixed > 0 && !fixed_ids)) return ACVD_ERR_ARG;
     const int64_t n = n_vertices;
     for (int64_t i = 0; i < n; i++) labels[i] = k;
+    // the fixed vertices take clusters 0 .. F-1; the grown regions the labels above
+    const int32_t offset = n_fixed;
+    for (int32_t o = 0; o < offset; o++) {
+        if (fixed_ids[o] < 0 || fixed_ids[o] >= n) return ACVD_ERR_ARG;
+        labels[fixed_ids[o]] = o;
+    }
     std::vector<int32_t> items(n);
     for (int64_t i = 0; i < n; i++) items[i] = (int32_t)i;
     std::mt19937 rng;
@@ -183,7 +196,7 @@ int acvd_initial_sampling(int64_t n_vertices, const int32_t* csr_row, const int3
     for (int64_t i = 0; i < n; i++) sw += weights[i];
     const double target = sw / (double)k;
     int64_t remaining_items = n;
-    int32_t remaining = k;
+    int32_t remaining = k - offset;
     int64_t first = 0;
     std::queue<int32_t> q;
     while (remaining_items > 0 && remaining > 0) {
@@ -202,7 +215,7 @@ int acvd_initial_sampling(int64_t n_vertices, const int32_t* csr_row, const int3
             item = q.front();
             q.pop();
             if (labels[item] != k) continue;
-            labels[item] = remaining;
+            labels[item] = remaining + offset;
             sw += weights[item];
             remaining_items--;
             for (int32_t p = csr_row[item]; p < csr_row[item + 1]; p++) q.push(csr_col[p]);
@@ -226,13 +239,13 @@ int acvd_initial_sampling(int64_t n_vertices, const int32_t* csr_row, const int3
             const int32_t cl = labels[item];
             if (cl == k) break;
             if (sizes[cl] == 1) continue;
-            labels[item] = remaining;
+            labels[item] = remaining + offset;
             sizes[cl]--;
-            sizes[remaining]++;
+            sizes[remaining + offset]++;
             break;
         }
         remaining--;
-        labels[item] = remaining;
+        labels[item] = remaining + offset;
     }
     return ACVD_OK;
 }

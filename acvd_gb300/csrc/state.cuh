@@ -156,6 +156,15 @@ struct DevState {
     // per cluster: 1 = frozen (IsClusterFreezed, vtkUniformClustering.h:912-915): no
     // item leaves it and none joins it, except unassigned items; null: none frozen
     const unsigned char* frozen;
+    // per cluster, QEM metric: the item of its anchor vertex (Cluster::AnchorItem,
+    // vtkQEMetricForClustering.h:127-128; -1 = none) and that vertex's coordinates;
+    // null: no anchored cluster
+    const int* anchor;
+    const double* anchor_xyz;
+    // fixed items (FixedClusters, vtkUniformClustering.h:134): cluster c < nfixed
+    // holds item fixed[c]; cleaning keeps the component that contains it
+    const int* fixed;
+    int nfixed;
 };
 
 // Persistent sweep kernel: the loop that runs colour sweeps back to back on the
@@ -238,6 +247,10 @@ cudaError_t launch_map_ids(const int* in, int64_t m, const int* inv, int* out, c
 cudaError_t launch_validate_mesh(const int* row, const int* col, int64_t n, int64_t ncol, const int* tri,
                                  int64_t ntri, const int* ev, int64_t nev, unsigned* bad, cudaStream_t s);
 // gather of labels that also counts those outside [0, k] in *bad
+// per cluster c < n: the item of vertex ids[c] (-1 stays -1) and, when xyz_out
+// is given, the vertex's coordinates (0 for -1)
+cudaError_t launch_anchor_setup(const int* ids, int n, const int* inv, const double* xyz, int* item_out,
+                                double* xyz_out, cudaStream_t s);
 cudaError_t launch_gather_labels(const int* src, const int* idx, int64_t n, int k, int* dst, unsigned* bad,
                                  cudaStream_t s);
 cudaError_t launch_gather_i32(const int* src, const int* idx, int64_t n, int* dst, cudaStream_t s);

@@ -467,6 +467,26 @@ cudaError_t launch_gather_labels(const int* src, const int* idx, int64_t n, int 
     return cudaGetLastError();
 }
 
+// ids were range-checked on the host: -1 or a vertex id
+__global__ void anchor_setup_kernel(const int* __restrict__ ids, int n, const int* __restrict__ inv,
+                                    const double* __restrict__ xyz, int* __restrict__ item_out,
+                                    double* __restrict__ xyz_out) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    const int v = ids[c];
+    item_out[c] = v >= 0 ? inv[v] : -1;
+    if (xyz_out)
+        for (int j = 0; j < 3; j++) xyz_out[3 * (int64_t)c + j] = v >= 0 ? xyz[3 * (int64_t)v + j] : 0.0;
+}
+
+cudaError_t launch_anchor_setup(const int* ids, int n, const int* inv, const double* xyz, int* item_out,
+                                double* xyz_out, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    ++g_launches;
+    anchor_setup_kernel<<<grid_of(n), 256, 0, s>>>(ids, n, inv, xyz, item_out, xyz_out);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_gather_f4(const float4* src, const int* idx, int64_t n, float4* dst, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
     ++g_launches;

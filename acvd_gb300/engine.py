@@ -77,6 +77,10 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         "acvd_build_topology": (ctypes.c_int, [_i64, _i64, _P, _P, _P, _P, ctypes.POINTER(_i64)]),
         "acvd_vertex_weights": (ctypes.c_int, [ctypes.c_int, _i64, _P, _i64, _P, _P, _P, _P, _P, ctypes.c_double, _P]),
         "acvd_initial_sampling": (ctypes.c_int, [_i64, _P, _P, _P, ctypes.c_int32, _P]),
+        "acvd_initial_sampling_fixed": (ctypes.c_int, [_i64, _P, _P, _P, ctypes.c_int32, ctypes.c_int32, _P, _P]),
+        "acvd_set_fixed_clusters": (ctypes.c_int, [_P, ctypes.c_int32, _P]),
+        "acvd_set_anchor_items": (ctypes.c_int, [_P, ctypes.c_int32, _P]),
+        "acvd_clean_clustering": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int32)]),
         "acvd_set_mesh": (ctypes.c_int, [_P, _i64, _P, _i64, _P, _P, _P, _i64, _P]),
         "acvd_set_metric": (ctypes.c_int, [_P, ctypes.c_int, _P, _P, ctypes.c_double]),
         "acvd_set_quadrics_optimization_level": (ctypes.c_int, [_P, ctypes.c_int]),
@@ -196,14 +200,22 @@ def vertex_weights(metric: str, points: np.ndarray, faces: np.ndarray, indicator
     return w
 
 
-def initial_sampling(row: np.ndarray, col: np.ndarray, weights: np.ndarray, k: int) -> np.ndarray:
+def initial_sampling(row: np.ndarray, col: np.ndarray, weights: np.ndarray, k: int,
+                     fixed: np.ndarray | None = None) -> np.ndarray:
+    """ComputeInitialRandomSampling; `fixed` (vertex ids) start in clusters 0 .. F-1."""
     lib = load()
     row = np.ascontiguousarray(row, dtype=np.int32)
     col = np.ascontiguousarray(col, dtype=np.int32)
     w = np.ascontiguousarray(weights, dtype=np.float64)
     lab = np.empty(row.shape[0] - 1, dtype=np.int32)
-    _check(lib.acvd_initial_sampling(row.shape[0] - 1, _ptr(row), _ptr(col), _ptr(w), int(k), _ptr(lab)),
-           what="acvd_initial_sampling")
+    if fixed is None or len(fixed) == 0:
+        _check(lib.acvd_initial_sampling(row.shape[0] - 1, _ptr(row), _ptr(col), _ptr(w), int(k), _ptr(lab)),
+               what="acvd_initial_sampling")
+        return lab
+    f = np.ascontiguousarray(fixed, dtype=np.int32)
+    _check(lib.acvd_initial_sampling_fixed(row.shape[0] - 1, _ptr(row), _ptr(col), _ptr(w), int(k), f.shape[0],
+                                           _ptr(f), _ptr(lab)),
+           what="acvd_initial_sampling_fixed")
     return lab
 
 
@@ -342,6 +354,29 @@ class Engine:
             raise ValueError("set_frozen_clusters needs one flag per cluster")
         self._frozen = f
         self._ck(self._lib.acvd_set_frozen_clusters(self.ctx, _ptr(f)), "acvd_set_frozen_clusters")
+
+    def set_fixed_clusters(self, vertex_ids):
+        """SetFixedClusters: cluster c < len(vertex_ids) is the cluster of vertex_ids[c]
+        (cleaning keeps the component holding it); empty or None clears the list."""
+        f = np.ascontiguousarray([] if vertex_ids is None else vertex_ids, dtype=np.int32)
+        self._fixed = f
+        self._ck(self._lib.acvd_set_fixed_clusters(self.ctx, f.shape[0], _ptr(f) if f.size else None),
+                 "acvd_set_fixed_clusters")
+
+    def set_anchor_items(self, anchors):
+        """QEM Cluster::AnchorItem of clusters 0 .. len(anchors)-1 (-1: none); empty or
+        None clears them."""
+        a = np.ascontiguousarray([] if anchors is None else anchors, dtype=np.int32)
+        self._anchors = a
+        self._ck(self._lib.acvd_set_anchor_items(self.ctx, a.shape[0], _ptr(a) if a.size else None),
+                 "acvd_set_anchor_items")
+
+    def clean_clustering(self) -> int:
+        """CleanClustering on the current labels: the number of clusters that had
+        several connected components (their smaller ones are now unassigned)."""
+        n = ctypes.c_int32(0)
+        self._ck(self._lib.acvd_clean_clustering(self.ctx, ctypes.byref(n)), "acvd_clean_clustering")
+        return int(n.value)
 
     def check_wait_limit(self, max_spins: int = 1 << 18) -> bool:
         """Runs the device barrier with one block never arriving: True when its wait

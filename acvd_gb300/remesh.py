@@ -123,6 +123,8 @@ class _DiscreteRemeshing:
         self._metric = _Metric(self)
         self._engine = None
         self._constrained_request = None
+        self.FixedClusters = None         # SetFixedClusters (vtkUniformClustering.h:134)
+        self._anchors = {}                # QEM Cluster::AnchorItem, by cluster
 
     @classmethod
     def New(cls, device: int = 0):
@@ -169,6 +171,18 @@ class _DiscreteRemeshing:
     def SetBoundaryFixing(self, on: int):
         """Close the coarse mesh along the input's boundary (FixMeshBoundaries)."""
         self.BoundaryFixing = int(on)
+
+    def SetFixedClusters(self, vertex_ids):
+        """Cluster c < len(vertex_ids) is the cluster of vertex vertex_ids[c]: the initial
+        sampling places it there and cleaning keeps its component (vtkUniformClustering.h:
+        134, 439-447, 1186-1190).  None clears the list."""
+        self.FixedClusters = None if vertex_ids is None else np.asarray(vertex_ids, dtype=np.int32).copy()
+
+    def GetCluster(self, c: int) -> "_ClusterRef":
+        """The cluster record whose AnchorItem ACVDQ sets (ACVDQ.cxx:333-334)."""
+        if not 0 <= int(c) < self.NumberOfClusters:
+            raise IndexError("cluster index outside [0, NumberOfClusters)")
+        return _ClusterRef(self, int(c))
 
     def SetMaxNumberOfLoops(self, n: int):
         self.MaxNumberOfLoops = int(n)
@@ -266,8 +280,15 @@ class _DiscreteRemeshing:
         else:
             w = _eng.vertex_weights(self._metric_name, self.Input.points, self.Input.faces, ind,
                                     self._metric.Gradation)
-            lab = _eng.initial_sampling(row, col, w, k)
+            lab = _eng.initial_sampling(row, col, w, k, fixed=self.FixedClusters)
         e.set_labels(k, lab)
+        if self.FixedClusters is not None:
+            e.set_fixed_clusters(self.FixedClusters)
+        if self._anchors:
+            anchors = np.full(max(self._anchors) + 1, -1, dtype=np.int32)
+            for c, v in self._anchors.items():
+                anchors[c] = v
+            e.set_anchor_items(anchors)
         return e
 
     def ProcessClustering(self):
@@ -376,6 +397,35 @@ class _DiscreteRemeshing:
         ind = np.fromfile(path, dtype=np.float64)
         self.SetCurvatureInfo(ind, self.PrincipalDirections)
         return ind
+
+
+class _ClusterRef:
+    """GetCluster(c): the metric's cluster record, here its AnchorItem only -- a member of
+    the QEM metric's clusters (vtkQEMetricForClustering.h:127-128), -1 when unset."""
+
+    def __init__(self, owner: _DiscreteRemeshing, c: int):
+        self._owner = owner
+        self._c = c
+
+    @property
+    def AnchorItem(self) -> int:
+        self._check()
+        return self._owner._anchors.get(self._c, -1)
+
+    @AnchorItem.setter
+    def AnchorItem(self, v: int):
+        self._check()
+        v = int(v)
+        if v < -1:
+            raise ValueError("AnchorItem is a vertex id, or -1")
+        if v == -1:
+            self._owner._anchors.pop(self._c, None)
+        else:
+            self._owner._anchors[self._c] = v
+
+    def _check(self):
+        if self._owner._metric_name != "qem":
+            raise AttributeError("AnchorItem is a member of the QEM metric's clusters only")
 
 
 class IsotropicDiscreteRemeshing(_DiscreteRemeshing):

@@ -116,6 +116,19 @@ int acvd_initial_sampling(int64_t n_vertices, const int32_t* csr_row, const int3
                           const double* weights, int32_t k, int32_t* labels);
 
 /*
+ * The same with fixed vertices (SetFixedClusters, Common/vtkUniformClustering.h:134,
+ * :1186-1190): vertex fixed_ids[c] starts in cluster c for c < n_fixed, the grown
+ * regions take the labels n_fixed .. K-1 (acvd_initial_sampling is n_fixed = 0).  Where
+ * every vertex is taken before the last region has started, the reference's loop
+ * repeats forever (:1218-1232, the fixed vertices are never counted off); this
+ * function goes on to split single vertices off the larger regions instead, as it
+ * does when the regions outnumber what the growth reached.
+ */
+int acvd_initial_sampling_fixed(int64_t n_vertices, const int32_t* csr_row, const int32_t* csr_col,
+                                const double* weights, int32_t k, int32_t n_fixed, const int32_t* fixed_ids,
+                                int32_t* labels);
+
+/*
  * Mesh upload (SetInput, vtkSurfaceClustering.h:179-211): coordinates, triangles
  * and the ring CSR / edge list from acvd_build_topology (or the caller's own
  * vtkSurface, exported in the same order).
@@ -171,6 +184,39 @@ int acvd_set_frozen_clusters(acvd_ctx* ctx, const uint8_t* frozen);
 /* The frozen set in force (K bytes, 1 = frozen; all 0 when none is set).  Reads what
  * the reference keeps in IsClusterFreezed; no entry of the reference corresponds. */
 int acvd_get_frozen_clusters(acvd_ctx* ctx, uint8_t* frozen);
+
+/*
+ * SetFixedClusters (Common/vtkUniformClustering.h:134): cluster c < n_fixed is the
+ * cluster of vertex vertex_ids[c].  CleanClustering keeps the component holding
+ * that vertex, however small (:439-447); acvd_initial_sampling_fixed places the
+ * vertices.  n_fixed = 0 clears the list.  Call after acvd_set_mesh; the list holds
+ * until the next acvd_set_mesh, and n_fixed must not exceed K.
+ */
+int acvd_set_fixed_clusters(acvd_ctx* ctx, int32_t n_fixed, const int32_t* vertex_ids);
+
+/*
+ * Cluster::AnchorItem of the QEM metric (DiscreteRemeshing/vtkQEMetricForClustering.h:
+ * 127-128; ACVDQ.cxx:333-334 sets it with the fixed vertices): cluster c < n is
+ * anchored at vertex anchors[c] (-1: not anchored).  An anchored cluster's vertex
+ * is its anchor (ComputeClusterCentroid :268-275), its energy W |p|^2 - 2 p.S
+ * (:194-208), and a move of the anchor vertex out of it is never taken (the
+ * reference prices it at 1e100, :194-200, :259).  ACVD_ERR_UNSUPPORTED for the other
+ * metrics, whose clusters have no anchor.  Call after acvd_set_metric; the anchors
+ * hold until the next acvd_set_mesh, across acvd_set_labels (clusters beyond n have
+ * none).  n = 0 clears them.
+ */
+int acvd_set_anchor_items(acvd_ctx* ctx, int32_t n, const int32_t* anchors);
+
+/*
+ * CleanClustering (Common/vtkUniformClustering.h:406-549) on the current labels:
+ * every cluster keeps its largest connected component (the earliest in vertex order
+ * among equals; the one holding its fixed vertex, if any) and the items of the
+ * others become unassigned (label K).  n_disconnected = the clusters that had
+ * several components.  acvd_minimize runs it at each convergence; this entry runs it
+ * alone.  Unlike the reference, the cluster whose first component starts at vertex 0
+ * is cleaned as well (the reference's test VisitedCluster[Type] == 0, :463, skips it).
+ */
+int acvd_clean_clustering(acvd_ctx* ctx, int32_t* n_disconnected);
 
 /*
  * MinimizeEnergy(): hole filling, statistics, colour sweeps until the

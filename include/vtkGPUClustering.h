@@ -21,7 +21,8 @@
  * them private, and the anisotropic metric overwrites its principal-direction
  * array in BuildMetric.  The engine's only extra state is the device ordinal and
  * whether a minimisation already ran: vtkDiscreteRemeshing's ForceManifold loop
- * re-enters MinimizeEnergy with IsClusterFreezed set, which is forwarded.
+ * re-enters MinimizeEnergy with IsClusterFreezed set, which is forwarded, as are
+ * FixedClusters and the QEM clusters' AnchorItem (ACVDQ's fixed vertices).
  * Errors of the C ABI are thrown as std::runtime_error; there is no CPU fallback.
  */
 #ifndef VTK_GPU_CLUSTERING_H
@@ -29,9 +30,17 @@
 
 #include <stdexcept>
 #include <string>
+#include <type_traits>
+#include <utility>
 #include <vector>
 
 #include "acvd_gpu.h"
+
+// whether a metric's Cluster has the QEM metric's AnchorItem member
+template <class C, class = void>
+struct acvd_has_anchor : std::false_type {};
+template <class C>
+struct acvd_has_anchor<C, decltype((void)std::declval<C&>().AnchorItem)> : std::true_type {};
 
 template <class M>
 struct acvd_metric_of {
@@ -103,6 +112,15 @@ protected:
     int Device = 0;
     bool Minimized = false;
     acvd_stats LastStats = {};
+
+    void collect_anchors(std::vector<int32_t>& out, bool& any, std::true_type) {
+        out.resize(this->NumberOfClusters);
+        for (int c = 0; c < this->NumberOfClusters; c++) {
+            out[c] = (int32_t)this->GetCluster(c)->AnchorItem;
+            any = any || out[c] >= 0;
+        }
+    }
+    void collect_anchors(std::vector<int32_t>&, bool&, std::false_type) {}
 
     static void check(acvd_ctx* ctx, int code, const char* what) {
         if (code == ACVD_OK) return;
@@ -177,6 +195,18 @@ protected:
             any_frozen = any_frozen || frozen[c];
         }
         if (any_frozen) check(ctx, acvd_set_frozen_clusters(ctx, frozen.data()), "acvd_set_frozen_clusters");
+        // FixedClusters (vtkUniformClustering.h:134) and, for the QEM metric, every
+        // cluster's AnchorItem (vtkQEMetricForClustering.h:127-128)
+        if (this->FixedClusters && this->FixedClusters->GetNumberOfIds() > 0) {
+            std::vector<int32_t> f(this->FixedClusters->GetNumberOfIds());
+            for (size_t i = 0; i < f.size(); i++) f[i] = (int32_t)this->FixedClusters->GetId((vtkIdType)i);
+            check(ctx, acvd_set_fixed_clusters(ctx, (int32_t)f.size(), f.data()), "acvd_set_fixed_clusters");
+        }
+        std::vector<int32_t> anchors;
+        bool any_anchor = false;
+        collect_anchors(anchors, any_anchor, acvd_has_anchor<typename GPUMetric::Cluster>());
+        if (any_anchor)
+            check(ctx, acvd_set_anchor_items(ctx, (int32_t)anchors.size(), anchors.data()), "acvd_set_anchor_items");
         check(ctx, acvd_minimize(ctx, &this->LastStats), "acvd_minimize");
         check(ctx, acvd_get_labels(ctx, this->Clustering->GetPointer(0)), "acvd_get_labels");
         acvd_destroy(ctx);

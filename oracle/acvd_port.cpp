@@ -22,6 +22,7 @@
 #include <cstring>
 #include <queue>
 #include <random>
+#include <type_traits>
 #include <vector>
 
 #include "restated_math.h"
@@ -295,6 +296,7 @@ struct EngineBase {
     std::vector<int> sizes;        // ClustersSizes
     std::vector<int> last_mod;     // ClustersLastModification
     std::vector<unsigned char> frozen;
+    std::vector<idt> fixed;        // FixedClusters (:134, :332): cluster c < fixed.size() holds item fixed[c]
     std::vector<unsigned char> edges_last_loop;
     unsigned char rel_loops = 1;
     int n_loops = 0;
@@ -319,6 +321,9 @@ struct EngineBase {
     // a new empty cluster (vtkDiscreteRemeshing.h:257-269)
     virtual void add_cluster() = 0;
     virtual void remove_last_cluster() = 0;
+    // Cluster::AnchorItem of the QEM metric (vtkQEMetricForClustering.h:127-128);
+    // false for the metrics without it
+    virtual bool set_anchor(int, idt) { return false; }
 
     idt n_items() const { return mesh.nV; }
 
@@ -380,10 +385,12 @@ struct EngineBase {
             int size = 0;
             q.push(i);
             const int type = labels[i];
+            // the component holding the cluster's fixed item outweighs any other (:439-447)
+            const idt fixed_item = type < (int)fixed.size() ? fixed[type] : -1;
             while (!q.empty()) {
                 const idt a = q.front(); q.pop();
                 if (visited[a]) continue;
-                size += 1;
+                size += a == fixed_item ? 1000000000 : 1;
                 visited[a] = 1;
                 mesh.vertex_neighbours(a, nb);
                 for (idt b : nb) if (!visited[b] && labels[b] == type) q.push(b);
@@ -470,13 +477,16 @@ struct EngineBase {
         while (!queue.empty()) queue.pop();
     }
 
-    // ComputeInitialRandomSampling (:1178-1316), no fixed clusters
+    // ComputeInitialRandomSampling (:1178-1316): the fixed items take clusters
+    // 0 .. F-1, the grown regions the labels above them
     void initial_random_sampling() {
         const idt n = n_items();
         for (idt i = 0; i < n; i++) labels[i] = K;
+        const int offset = (int)fixed.size();
+        for (int o = 0; o < offset; o++) labels[fixed[o]] = o;
         std::vector<int> itm(n);
         idt remaining_items = n;
-        int remaining_regions = K;
+        int remaining_regions = K - offset;
         for (idt i = 0; i < n; i++) itm[i] = (int)i;
         std::mt19937 rng;
         rng.seed(0);
@@ -494,7 +504,9 @@ struct EngineBase {
                 item = itm[first];
                 if (labels[item] == K) found = true; else first++;
             }
-            if (!found) continue;
+            // the reference continues here, which with fixed items (never counted off
+            // remaining_items) can repeat forever once every item is taken
+            if (!found) break;
             while (!q.empty()) q.pop();
             q.push(item);
             sw = 0;
@@ -502,7 +514,7 @@ struct EngineBase {
             while (!q.empty()) {
                 item = q.front(); q.pop();
                 if (labels[item] != K) continue;
-                labels[item] = remaining_regions;
+                labels[item] = remaining_regions + offset;
                 sw += item_weight(item);
                 remaining_items--;
                 mesh.vertex_neighbours(item, nb);
@@ -527,13 +539,13 @@ struct EngineBase {
                 const int cl = labels[item];
                 if (cl == K) break;
                 if (sizes[cl] == 1) continue;
-                labels[item] = remaining_regions;
+                labels[item] = remaining_regions + offset;
                 sizes[cl]--;
-                sizes[remaining_regions]++;
+                sizes[remaining_regions + offset]++;
                 break;
             }
             remaining_regions--;
-            labels[item] = remaining_regions;
+            labels[item] = remaining_regions + offset;
         }
     }
 
@@ -635,6 +647,15 @@ struct Engine : EngineBase {
         last_mod.pop_back();
         sizes.pop_back();
         K--;
+    }
+
+    bool set_anchor(int k, idt item) override {
+        if constexpr (std::is_same<M, QEMMetric>::value) {
+            if (k < 0 || k >= K) return false;
+            clusters[k].anchor = item;
+            return true;
+        }
+        return false;
     }
 
     void set_k(int k) {   // SetNumberOfClusters (:62-69)
@@ -1066,6 +1087,22 @@ int port_detect_nonmanifold(void* hp, int* k_out) {
     const int n = detect_nonmanifold(e);
     *k_out = e->K;
     return n;
+}
+
+// SetFixedClusters (vtkUniformClustering.h:134): before port_init, so that the
+// initial sampling places the fixed items
+void port_set_fixed(void* hp, int n, const int* ids) {
+    EngineBase* e = ((PortHandle*)hp)->eng;
+    e->fixed.assign(ids, ids + n);
+}
+
+// GetCluster(c)->AnchorItem = anchors[c] for c < n (QEM only, as ACVDQ.cxx:333-334
+// does); -1 for a metric without anchors
+int port_set_anchors(void* hp, int n, const int* anchors) {
+    EngineBase* e = ((PortHandle*)hp)->eng;
+    for (int c = 0; c < n; c++)
+        if (!e->set_anchor(c, anchors[c])) return -1;
+    return 0;
 }
 
 void port_set_frozen(void* hp, const unsigned char* in) {

@@ -68,6 +68,8 @@ def _bind(lib, prefix):
         "fill_holes": f("fill_holes", ctypes.c_int, _P),
         "post_placement": f("post_placement", None, _P, ctypes.c_int, _pd),
         "curvature": f("curvature", None, _P, _pd, np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")),
+        "set_fixed": f("set_fixed", None, _P, ctypes.c_int, _pi),
+        "set_anchors": f("set_anchors", ctypes.c_int, _P, ctypes.c_int, _pi),
     }
     return fns
 
@@ -121,6 +123,18 @@ class _Base:
 
     def set_option(self, name: str, value: float) -> None:
         self.f["set_option"](self.h, name.encode(), float(value))
+
+    def set_fixed(self, ids) -> None:
+        """SetFixedClusters: cluster c < len(ids) holds vertex ids[c] (before init)."""
+        a = np.ascontiguousarray(ids, dtype=np.int32)
+        self._fixed = a
+        self.f["set_fixed"](self.h, a.shape[0], a)
+
+    def set_anchors(self, anchors) -> None:
+        """QEM Cluster::AnchorItem of clusters 0 .. len(anchors)-1 (-1: none)."""
+        a = np.ascontiguousarray(anchors, dtype=np.int32)
+        if self.f["set_anchors"](self.h, a.shape[0], a) != 0:
+            raise ValueError("anchor items exist for the QEM metric only")
 
     def init(self, initial: np.ndarray | None = None) -> None:
         if initial is None:

@@ -55,11 +55,14 @@ struct RefBase {
     virtual int loops() = 0;
     virtual void post_placement(int level, double* out) = 0;
     virtual void curvature(double* indicator, float* principal_dirs) = 0;
+    virtual void set_fixed(int n, const int* ids) = 0;
+    virtual int set_anchors(int n, const int* anchors) = 0;
 };
 
 template <class M>
 struct Ref : RefBase {
     Probe<M>* p = nullptr;
+    vtkIdList* fixed = nullptr;   // the engine keeps the pointer (SetFixedClusters)
     long long n = 0;
     int K = 0;
 
@@ -93,7 +96,25 @@ struct Ref : RefBase {
             coll->Delete();
         }
     }
-    ~Ref() override { p->Delete(); }
+    ~Ref() override {
+        p->Delete();
+        if (fixed) fixed->Delete();
+    }
+
+    // what ACVDQ.cxx:327-334 does with a list of fixed vertices
+    void set_fixed(int nf, const int* ids) override {
+        if (fixed) fixed->Delete();
+        fixed = vtkIdList::New();
+        for (int i = 0; i < nf; i++) fixed->InsertNextId(ids[i]);
+        p->SetFixedClusters(fixed);
+    }
+    int set_anchors(int na, const int* anchors) override {
+        if constexpr (std::is_same<M, vtkQEMetricForClustering>::value) {
+            for (int c = 0; c < na; c++) p->GetCluster(c)->AnchorItem = anchors[c];
+            return 0;
+        }
+        return -1;
+    }
 
     void set_option(const char* name, double v) override {
         if (!std::strcmp(name, "unconstrained_init")) p->SetUnconstrainedInitialization((int)v);
@@ -231,6 +252,8 @@ int ref_clean(void* h) { return ((RefBase*)h)->clean(); }
 int ref_fill_holes(void* h) { return ((RefBase*)h)->fill(); }
 int ref_loops(void* h) { return ((RefBase*)h)->loops(); }
 void ref_post_placement(void* h, int level, double* out) { ((RefBase*)h)->post_placement(level, out); }
+void ref_set_fixed(void* h, int n, const int* ids) { ((RefBase*)h)->set_fixed(n, ids); }
+int ref_set_anchors(void* h, int n, const int* anchors) { return ((RefBase*)h)->set_anchors(n, anchors); }
 void ref_curvature(void* h, double* indicator, float* principal_dirs) {
     ((RefBase*)h)->curvature(indicator, principal_dirs);
 }

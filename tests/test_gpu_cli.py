@@ -68,6 +68,40 @@ def test_native_programs_match_the_python_drivers(tmp_path, prog, args):
         assert (native / n).read_bytes() == (python / n).read_bytes(), n
 
 
+@pytest.mark.parametrize("key", ["-fv", "-ft"])
+def test_acvdq_fixed_vertices(tmp_path, key, capfd):
+    """ACVDQ -fv / -ft (ACVDQ.cxx:246-280, 327-363): the fixed vertices are the first
+    output vertices, unchanged; the native program and the Python driver write the same
+    file."""
+    import subprocess
+    from acvd_gb300 import build as B
+    m = synth.torus(80, 40, seed=2)
+    src = str(tmp_path / "in.ply")
+    E.write_mesh(src, m.points, m.faces)
+    pts, tri = E.read_mesh(src)                                 # as stored (float)
+    if key == "-fv":
+        fixed = np.array([5, 77, 400, 1203, 2900], dtype=np.int32)
+        (tmp_path / "ids.txt").write_text(" ".join(str(v) for v in fixed) + "\n")
+    else:
+        faces = np.array([10, 3000, 5100], dtype=np.int32)
+        fixed = np.unique(tri[faces].reshape(-1)).astype(np.int32)
+        (tmp_path / "ids.txt").write_text("\n".join(str(f) for f in faces))
+    native, python = tmp_path / "native", tmp_path / "python"
+    native.mkdir()
+    python.mkdir()
+    args = [src, "250", "0.5", key, str(tmp_path / "ids.txt")]
+    r = subprocess.run([os.path.join(B.OUT, "acvdq")] + args + ["-o", str(native) + "/"], capture_output=True,
+                       text=True)
+    assert r.returncode == 0, r.stderr
+    assert "Constraints on vertices have been checked" in r.stdout
+    assert cli.main_acvdq(args + ["-o", str(python) + "/"]) == 0
+    assert "Constraints on vertices have been checked" in capfd.readouterr().out
+    out_pts, _ = E.read_mesh(str(python / "simplification.ply"))
+    assert out_pts.shape[0] == 250 + len(fixed)
+    np.testing.assert_array_equal(out_pts[: len(fixed)], pts[fixed])
+    assert (native / "simplification.ply").read_bytes() == (python / "simplification.ply").read_bytes()
+
+
 def test_resume_from_a_saved_clustering(tmp_path):
     """A clustering saved to clustering.dat and loaded again (the reference's load path:
     no minimisation) gives the same clustering and the same coarse mesh."""

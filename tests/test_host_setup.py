@@ -76,3 +76,25 @@ def test_bad_inputs_raise(lib):
     with pytest.raises(acvd_gb300.AcvdError):
         acvd_gb300.initial_sampling(np.array([0, 0], dtype=np.int32), np.zeros(0, dtype=np.int32),
                                     np.ones(1), 0)
+
+
+@pytest.mark.parametrize("metric,k,nfix,grad", [("qem", 150, 12, 1.5), ("iso", 60, 5, 0.0), ("qem", 40, 40, 0.0),
+                                                 ("iso", 9, 3, 0.0)])
+def test_initial_sampling_with_fixed_vertices_matches_reference(oracle_lib, lib, metric, k, nfix, grad):
+    """SetFixedClusters before InitSamples: the fixed vertices take clusters 0 .. F-1
+    and the grown regions the labels above (vtkUniformClustering.h:1186-1316)."""
+    m = synth.torus(56, 28, seed=2)
+    ind = m.indicator if grad > 0 else None
+    row, col, ev = acvd_gb300.build_topology(m.n_points, m.faces)
+    w = acvd_gb300.vertex_weights(metric, m.points, m.faces, ind, grad)
+    fixed = np.random.default_rng(k).choice(m.n_points, size=nfix, replace=False).astype(np.int32)
+    lab = acvd_gb300.initial_sampling(row, col, w, k, fixed=fixed)
+    p = oracle_lib.Port(metric, m.points, m.faces, k, grad, ind)
+    p.set_fixed(fixed)
+    p.init(None)
+    np.testing.assert_array_equal(lab, p.labels())
+    np.testing.assert_array_equal(lab[fixed], np.arange(nfix))
+    with pytest.raises(acvd_gb300.AcvdError):
+        acvd_gb300.initial_sampling(row, col, w, k, fixed=np.array([m.n_points], dtype=np.int32))
+    with pytest.raises(acvd_gb300.AcvdError):
+        acvd_gb300.initial_sampling(row, col, w, nfix - 1, fixed=fixed)

@@ -37,6 +37,11 @@ PROGRAM = textwrap.dedent(r"""
         static_assert(GQ::acvd_metric == ACVD_METRIC_QEM, "qem");
         static_assert(GI::acvd_metric == ACVD_METRIC_ISOTROPIC, "iso");
         static_assert(GA::acvd_metric == ACVD_METRIC_QUADRIC_ANISOTROPIC, "aniso");
+        // AnchorItem is forwarded for the QEM metric's clusters only
+        static_assert(acvd_has_anchor<GQ::Cluster>::value, "qem anchors");
+        static_assert(!acvd_has_anchor<GI::Cluster>::value, "iso has no anchors");
+        static_assert(!acvd_has_anchor<GA::Cluster>::value, "aniso has no anchors");
+        GPUI::New()->Delete();   // instantiates the iso engine's MinimizeEnergy too
         // octahedron subdivided once: 18 vertices, 32 faces
         const double P[18][3] = {{1,0,0},{-1,0,0},{0,1,0},{0,-1,0},{0,0,1},{0,0,-1},
             {.7,.7,0},{-.7,.7,0},{-.7,-.7,0},{.7,-.7,0},{.7,0,.7},{0,.7,.7},{-.7,0,.7},{0,-.7,.7},

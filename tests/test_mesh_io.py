@@ -135,6 +135,22 @@ def test_cli_rejects_unbuilt_options():
         cli.main_acvd(["x.ply"])
 
 
+def test_acvdq_fixed_vertex_files(tmp_path):
+    """-fv reads vertex ids until one does not parse; -ft marks the vertices of the listed
+    faces; the last of the two given wins (ACVDQ.cxx:246-280)."""
+    from acvd_gb300 import cli
+    mesh = acvd_gb300.Surface(TET_P, np.array([[0, 1, 2], [0, 3, 1], [1, 3, 2], [2, 3, 0]], dtype=np.int32))
+    (tmp_path / "v.txt").write_text("3 1\n2 x 0\n")
+    (tmp_path / "f.txt").write_text("1\n")
+    opts = cli._parse(["m.ply", "10", "0", "-fv", str(tmp_path / "v.txt")], "ACVDQ")
+    np.testing.assert_array_equal(cli._fixed_vertices(opts, mesh), [3, 1, 2])
+    opts = cli._parse(["m.ply", "10", "0", "-fv", str(tmp_path / "v.txt"), "-ft", str(tmp_path / "f.txt")], "ACVDQ")
+    np.testing.assert_array_equal(cli._fixed_vertices(opts, mesh), [0, 1, 3])
+    opts = cli._parse(["m.ply", "10", "0", "-fv", str(tmp_path / "missing.txt")], "ACVDQ")
+    assert cli._fixed_vertices(opts, mesh).size == 0
+    assert cli._fixed_vertices(cli._parse(["m.ply", "10", "0"], "ACVDQ"), mesh) is None
+
+
 def test_native_programs_parse_like_the_reference():
     """The native ACVD / ACVDQ programs (csrc/acvd_cli.cpp) are built beside the library;
     without arguments they print the usage, an option that needs an unbuilt part stops

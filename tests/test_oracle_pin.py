@@ -110,3 +110,69 @@ def test_curvature_equals_reference(oracle_lib, case):
     b = O.Ref(metric, m.points, m.faces, k, 0.0).curvature()
     np.testing.assert_array_equal(a[0], b[0])
     np.testing.assert_array_equal(a[1], b[1])
+
+
+FIXED_CASES = [
+    ("qem", lambda: synth.torus(80, 40, seed=1), 300, 1.5, 1, 12),
+    ("qem", lambda: synth.heightfield(32, seed=2), 80, 0.0, 0, 5),
+    ("iso", lambda: synth.icosphere(4, seed=5), 120, 0.0, 0, 9),
+]
+
+
+def _fixed_ids(n, count, seed):
+    return np.sort(np.random.default_rng(seed).choice(n, size=count, replace=False)).astype(np.int32)
+
+
+@pytest.mark.parametrize("case", range(len(FIXED_CASES)))
+def test_fixed_vertices_equal_reference(oracle_lib, case):
+    """Fixed vertices as ACVDQ.cxx:327-334 sets them (SetFixedClusters, and for QEM
+    the clusters' AnchorItem): initial sampling, converged clustering, energies and
+    cluster records bit for bit; the anchored clusters' centroids are their vertices."""
+    O = oracle_lib
+    _need_ref(O)
+    metric, mk, k, grad, uinit, nfix = FIXED_CASES[case]
+    m = mk()
+    ind = m.indicator if grad > 0 else None
+    fixed = _fixed_ids(m.n_points, nfix, 100 + case)
+    out = []
+    for cls in (O.Port, O.Ref):
+        o = cls(metric, m.points, m.faces, k + nfix, grad, ind, None, unconstrained_init=uinit)
+        o.set_fixed(fixed)
+        if metric == "qem":
+            o.set_anchors(fixed)
+        o.init(None)
+        l0 = o.labels()
+        o.run()
+        out.append((l0, o.labels(), o.global_energy(), o.clusters()))
+    (pl0, pl, pe, pc), (rl0, rl, re, rc) = out
+    np.testing.assert_array_equal(pl0, rl0)
+    np.testing.assert_array_equal(pl0[fixed], np.arange(nfix))
+    np.testing.assert_array_equal(pl, rl)
+    assert pe == re
+    for key in ("S", "W", "Q", "centroid", "energy", "size"):
+        np.testing.assert_array_equal(pc[key], rc[key])
+    np.testing.assert_array_equal(pl[fixed], np.arange(nfix))
+    if metric == "qem":
+        np.testing.assert_array_equal(pc["centroid"][:nfix], m.points[fixed])
+
+
+def test_clean_with_fixed_items_equals_reference(oracle_lib):
+    """CleanClustering keeps the component holding a cluster's fixed item, however
+    small (vtkUniformClustering.h:439-447)."""
+    O = oracle_lib
+    _need_ref(O)
+    m = synth.icosphere(3, seed=3)
+    rng = np.random.default_rng(1)
+    k = 30
+    lab = rng.integers(0, k, size=m.n_points).astype(np.int32)
+    fixed = np.array([int(np.flatnonzero(lab == c)[-1]) for c in range(6)], dtype=np.int32)
+    res = []
+    for cls in (O.Port, O.Ref):
+        o = cls("iso", m.points, m.faces, k)
+        o.set_fixed(fixed)
+        o.init(lab)
+        n_disc = o.clean()
+        res.append((n_disc, o.labels()))
+    assert res[0][0] == res[1][0]
+    np.testing.assert_array_equal(res[0][1], res[1][1])
+    np.testing.assert_array_equal(res[0][1][fixed], np.arange(6))
