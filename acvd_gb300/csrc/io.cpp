@@ -3,8 +3,10 @@
 // read and written by this file's own parsers from the formats' published layouts.
 //
 //   read : .ply (ascii, binary little / big endian), .off, .obj, .stl (ascii, binary),
-//          .vtk (legacy POLYDATA, ascii or binary, both POLYGONS layouts)
-//   write: .ply (binary little endian, float points), .off, .obj, .stl (binary), .vtk (ascii)
+//          .vtk (legacy POLYDATA, ascii or binary, both POLYGONS layouts),
+//          .vtp (VTK XML PolyData: ascii, base64 or appended data, zlib-compressed or not)
+//   write: .ply (binary little endian, float points), .off, .obj, .stl (binary), .vtk (ascii),
+//          .vtp (inline base64, uncompressed)
 //
 // The extension test is the reference's: the lower-cased name contains ".vtk", ".ply", ...
 // (checked in its order).  Polygons other than triangles are rejected: the clustering path
@@ -511,6 +513,553 @@ int read_vtk(const std::string& buf, MeshData& m) {
     return check_faces(m);
 }
 
+// ---------------------------------------------------------------- zlib inflate
+// Decoder for zlib streams (RFC 1950) holding DEFLATE data (RFC 1951), written from the
+// two specifications: stored, fixed-Huffman and dynamic-Huffman blocks; canonical
+// Huffman codes (RFC 1951 sec. 3.2.2) decoded one bit at a time from the per-length
+// code counts; the Adler-32 checksum verified.  VTK's XML writers compress their data
+// arrays with it by default.
+class BitReader {
+public:
+    BitReader(const unsigned char* p, size_t n) : p_(p), n_(n) {}
+    // `count` bits, least significant first (count <= 16)
+    uint32_t take(int count) {
+        while (have_ < count) {
+            if (pos_ >= n_) {
+                failed_ = true;
+                return 0;
+            }
+            acc_ |= (uint32_t)p_[pos_++] << have_;
+            have_ += 8;
+        }
+        const uint32_t v = acc_ & ((1u << count) - 1u);
+        acc_ >>= count;
+        have_ -= count;
+        return v;
+    }
+    void to_byte() {   // drop the bits left in the current byte
+        acc_ = 0;
+        have_ = 0;
+    }
+    size_t pos() const { return pos_; }
+    bool failed() const { return failed_; }
+    const unsigned char* data() const { return p_; }
+    size_t size() const { return n_; }
+    void skip(size_t bytes) { pos_ += bytes; }
+
+private:
+    const unsigned char* p_;
+    size_t n_, pos_ = 0;
+    uint32_t acc_ = 0;
+    int have_ = 0;
+    bool failed_ = false;
+};
+
+// canonical code: symbols sorted by (code length, symbol); the codes of one length are
+// consecutive integers starting at first_code[len]
+struct Canonical {
+    int count[16] = {0};
+    int first_code[16] = {0};
+    int first_index[16] = {0};
+    std::vector<int> sorted;
+    bool build(const uint8_t* len, int n) {
+        for (int l = 0; l < 16; l++) count[l] = 0;
+        for (int s = 0; s < n; s++) count[len[s]]++;
+        count[0] = 0;
+        int code = 0, index = 0;
+        for (int l = 1; l < 16; l++) {
+            code = (code + (l > 1 ? count[l - 1] : 0)) << (l > 1 ? 1 : 0);
+            first_code[l] = code;
+            first_index[l] = index;
+            index += count[l];
+            if (count[l] > (1 << l)) return false;
+        }
+        // over-subscription: more codes than the lengths can hold
+        long room = 1;
+        for (int l = 1; l < 16; l++) {
+            room = 2 * room - count[l];
+            if (room < 0) return false;
+        }
+        sorted.assign(index, 0);
+        std::vector<int> next(16);
+        for (int l = 1; l < 16; l++) next[l] = first_index[l];
+        for (int s = 0; s < n; s++)
+            if (len[s]) sorted[next[len[s]]++] = s;
+        return true;
+    }
+    int decode(BitReader& in) const {
+        int code = 0;
+        for (int l = 1; l < 16; l++) {
+            code = (code << 1) | (int)in.take(1);
+            if (in.failed()) return -1;
+            const int d = code - first_code[l];
+            if (d >= 0 && d < count[l]) return sorted[first_index[l] + d];
+        }
+        return -1;
+    }
+};
+
+bool inflate_deflate(BitReader& in, std::string& out, size_t limit) {
+    // length and distance bases of RFC 1951 sec. 3.2.5, built from their pattern
+    int len_base[29], len_extra[29], dist_base[30], dist_extra[30];
+    for (int i = 0; i < 8; i++) { len_base[i] = 3 + i; len_extra[i] = 0; }
+    for (int i = 8, base = 11; i < 28; i++) {
+        len_extra[i] = (i - 4) / 4;
+        len_base[i] = base;
+        base += 1 << len_extra[i];
+    }
+    len_base[28] = 258;
+    len_extra[28] = 0;
+    for (int i = 0; i < 4; i++) { dist_base[i] = 1 + i; dist_extra[i] = 0; }
+    for (int i = 4, base = 5; i < 30; i++) {
+        dist_extra[i] = (i - 2) / 2;
+        dist_base[i] = base;
+        base += 1 << dist_extra[i];
+    }
+    static const int kOrder[19] = {16, 17, 18, 0, 8, 7, 9, 6, 10, 5, 11, 4, 12, 3, 13, 2, 14, 1, 15};
+    for (;;) {
+        const uint32_t final_block = in.take(1);
+        const uint32_t type = in.take(2);
+        if (in.failed()) return false;
+        if (type == 0) {   // stored
+            in.to_byte();
+            const size_t at = in.pos();
+            if (at + 4 > in.size()) return false;
+            const unsigned char* q = in.data() + at;
+            const unsigned len = q[0] | (q[1] << 8), nlen = q[2] | (q[3] << 8);
+            if ((len ^ 0xffffu) != nlen || at + 4 + len > in.size() || out.size() + len > limit) return false;
+            out.append((const char*)q + 4, len);
+            in.skip(4 + len);
+        } else if (type == 1 || type == 2) {
+            Canonical lit, dist;
+            uint8_t lens[320];
+            if (type == 1) {   // fixed codes (sec. 3.2.6)
+                for (int s = 0; s < 288; s++) lens[s] = s < 144 ? 8 : s < 256 ? 9 : s < 280 ? 7 : 8;
+                for (int s = 0; s < 30; s++) lens[288 + s] = 5;
+                if (!lit.build(lens, 288) || !dist.build(lens + 288, 30)) return false;
+            } else {           // dynamic codes (sec. 3.2.7)
+                const int nlit = (int)in.take(5) + 257, ndist = (int)in.take(5) + 1, nclen = (int)in.take(4) + 4;
+                if (in.failed() || nlit > 286 || ndist > 30) return false;
+                uint8_t cl[19] = {0};
+                for (int i = 0; i < nclen; i++) cl[kOrder[i]] = (uint8_t)in.take(3);
+                Canonical clc;
+                if (!clc.build(cl, 19)) return false;
+                int got = 0;
+                while (got < nlit + ndist) {
+                    const int sym = clc.decode(in);
+                    if (sym < 0) return false;
+                    if (sym < 16) {
+                        lens[got++] = (uint8_t)sym;
+                        continue;
+                    }
+                    int rep = 0;
+                    uint8_t val = 0;
+                    if (sym == 16) {
+                        if (got == 0) return false;
+                        val = lens[got - 1];
+                        rep = 3 + (int)in.take(2);
+                    } else if (sym == 17) {
+                        rep = 3 + (int)in.take(3);
+                    } else {
+                        rep = 11 + (int)in.take(7);
+                    }
+                    if (in.failed() || got + rep > nlit + ndist) return false;
+                    while (rep--) lens[got++] = val;
+                }
+                if (lens[256] == 0) return false;   // no end-of-block code
+                if (!lit.build(lens, nlit) || !dist.build(lens + nlit, ndist)) return false;
+            }
+            for (;;) {
+                const int sym = lit.decode(in);
+                if (sym < 0) return false;
+                if (sym < 256) {
+                    if (out.size() >= limit) return false;
+                    out.push_back((char)sym);
+                    continue;
+                }
+                if (sym == 256) break;
+                if (sym > 285) return false;
+                const int length = len_base[sym - 257] + (int)in.take(len_extra[sym - 257]);
+                const int dsym = dist.decode(in);
+                if (dsym < 0 || dsym > 29) return false;
+                const size_t d = (size_t)dist_base[dsym] + in.take(dist_extra[dsym]);
+                if (in.failed() || d > out.size() || out.size() + length > limit) return false;
+                const size_t from = out.size() - d;
+                for (int j = 0; j < length; j++) out.push_back(out[from + j]);
+            }
+        } else {
+            return false;
+        }
+        if (final_block) return true;
+    }
+}
+
+uint32_t adler32(const std::string& s) {
+    uint32_t a = 1, b = 0;
+    for (unsigned char c : s) {
+        a = (a + c) % 65521u;
+        b = (b + a) % 65521u;
+    }
+    return (b << 16) | a;
+}
+
+// one zlib stream (header, DEFLATE data, Adler-32) holding exactly `expect` bytes
+bool zlib_inflate(const unsigned char* p, size_t n, size_t expect, std::string& out) {
+    out.clear();
+    if (n < 6) return false;
+    const unsigned cmf = p[0], flg = p[1];
+    if ((cmf & 15u) != 8u || (cmf >> 4) > 7u || ((cmf << 8) | flg) % 31u != 0u || (flg & 32u)) return false;
+    BitReader in(p + 2, n - 2);
+    if (!inflate_deflate(in, out, expect)) return false;
+    const size_t at = 2 + in.pos();
+    if (at + 4 > n || out.size() != expect) return false;
+    const uint32_t want = ((uint32_t)p[at] << 24) | ((uint32_t)p[at + 1] << 16) | ((uint32_t)p[at + 2] << 8) | p[at + 3];
+    return want == adler32(out);
+}
+
+// ---------------------------------------------------------------- VTK XML PolyData
+// The .vtp layout of VTK's XML file formats: a VTKFile element (byte_order, header_type
+// UInt32 / UInt64, optional vtkZLibDataCompressor) holding PolyData Pieces, each with a
+// Points DataArray and the Polys' "connectivity" / "offsets" arrays, in ascii, inline
+// base64 ("binary") or appended (raw or base64) form.  A binary block is a header -- the
+// byte count, or for compressed data [blocks, block size, last block size, compressed
+// sizes...] -- followed by the data.  Pieces are concatenated.  Only triangles are read;
+// triangle strips are refused, vertices and lines (no faces) are ignored.
+struct XmlTag {
+    std::string name;
+    std::map<std::string, std::string> attr;
+    size_t open = 0, close = 0;   // '<' and one past '>'
+    bool empty = false;           // <... />
+};
+
+// the next element tag at or after `from` (comments and declarations skipped)
+bool next_tag(const std::string& s, size_t from, size_t stop, XmlTag& t) {
+    size_t i = from;
+    for (;;) {
+        i = s.find('<', i);
+        if (i == std::string::npos || i >= stop) return false;
+        if (s.compare(i, 4, "<!--") == 0) {
+            i = s.find("-->", i);
+            if (i == std::string::npos) return false;
+            continue;
+        }
+        if (i + 1 < s.size() && (s[i + 1] == '?' || s[i + 1] == '!' || s[i + 1] == '/')) {
+            i++;
+            continue;
+        }
+        break;
+    }
+    const size_t end = s.find('>', i);
+    if (end == std::string::npos) return false;
+    t = XmlTag();
+    t.open = i;
+    t.close = end + 1;
+    t.empty = s[end - 1] == '/';
+    size_t k = i + 1;
+    while (k < end && !std::isspace((unsigned char)s[k]) && s[k] != '/' && s[k] != '>') t.name += s[k++];
+    for (;;) {
+        while (k < end && (std::isspace((unsigned char)s[k]) || s[k] == '/')) k++;
+        if (k >= end) break;
+        std::string key;
+        while (k < end && s[k] != '=' && !std::isspace((unsigned char)s[k])) key += s[k++];
+        while (k < end && s[k] != '"' && s[k] != '\'') k++;
+        if (k >= end) break;
+        const char q = s[k++];
+        const size_t v = k;
+        while (k < end && s[k] != q) k++;
+        t.attr[key] = s.substr(v, k - v);
+        k++;
+    }
+    return true;
+}
+
+std::string attr_of(const XmlTag& t, const char* key, const char* dflt = "") {
+    const auto it = t.attr.find(key);
+    return it == t.attr.end() ? std::string(dflt) : it->second;
+}
+
+int b64_value(unsigned char c) {
+    if (c >= 'A' && c <= 'Z') return c - 'A';
+    if (c >= 'a' && c <= 'z') return c - 'a' + 26;
+    if (c >= '0' && c <= '9') return c - '0' + 52;
+    if (c == '+') return 62;
+    if (c == '/') return 63;
+    return -1;
+}
+
+// base64 text to bytes; '=' ends a quantum, after which decoding starts afresh, so text
+// made of separately encoded pieces (VTK encodes a compressed block's header apart from
+// its data) decodes to the pieces' concatenation
+bool b64_decode(const char* p, size_t n, std::string& out) {
+    out.clear();
+    uint32_t acc = 0;
+    int have = 0;
+    for (size_t i = 0; i < n; i++) {
+        const unsigned char c = (unsigned char)p[i];
+        if (std::isspace(c)) continue;
+        if (c == '=') {
+            acc = 0;
+            have = 0;
+            continue;
+        }
+        const int v = b64_value(c);
+        if (v < 0) return false;
+        acc = (acc << 6) | (uint32_t)v;
+        have += 6;
+        if (have >= 8) {
+            have -= 8;
+            out.push_back((char)((acc >> have) & 0xffu));
+        }
+    }
+    return true;
+}
+
+void b64_encode(const std::string& in, std::string& out) {
+    static const char* kAlphabet = "ABCDEFGHIJKLMNOPQRSTUVWXYZabcdefghijklmnopqrstuvwxyz0123456789+/";
+    size_t i = 0;
+    for (; i + 3 <= in.size(); i += 3) {
+        const uint32_t v = ((uint32_t)(unsigned char)in[i] << 16) | ((uint32_t)(unsigned char)in[i + 1] << 8) |
+                           (unsigned char)in[i + 2];
+        for (int s = 18; s >= 0; s -= 6) out += kAlphabet[(v >> s) & 63u];
+    }
+    const size_t rest = in.size() - i;
+    if (rest) {
+        uint32_t v = (uint32_t)(unsigned char)in[i] << 16;
+        if (rest == 2) v |= (uint32_t)(unsigned char)in[i + 1] << 8;
+        out += kAlphabet[(v >> 18) & 63u];
+        out += kAlphabet[(v >> 12) & 63u];
+        out += rest == 2 ? kAlphabet[(v >> 6) & 63u] : '=';
+        out += '=';
+    }
+}
+
+struct VtpFile {
+    bool little = true;
+    int header_bytes = 4;         // UInt32 / UInt64
+    bool zlib = false;
+    std::string appended;         // the appended data after '_' (raw), or its base64 text
+    bool appended_b64 = false;
+    std::vector<size_t> offsets;  // every appended DataArray offset, sorted (base64 piece ends)
+};
+
+uint64_t vtp_header_value(const VtpFile& f, const unsigned char* p) {
+    return f.header_bytes == 8 ? load_scalar<uint64_t>(p, f.little) : load_scalar<uint32_t>(p, f.little);
+}
+
+// a binary block (header + data) to the array's raw bytes; `avail` bounds the block
+bool vtp_block(const VtpFile& f, const unsigned char* p, size_t avail, std::string& raw) {
+    const size_t hb = (size_t)f.header_bytes;
+    if (!f.zlib) {
+        if (avail < hb) return false;
+        const uint64_t nbytes = vtp_header_value(f, p);
+        if (nbytes > avail - hb) return false;
+        raw.assign((const char*)p + hb, (size_t)nbytes);
+        return true;
+    }
+    if (avail < 3 * hb) return false;
+    const uint64_t nblocks = vtp_header_value(f, p), bsize = vtp_header_value(f, p + hb),
+                   last = vtp_header_value(f, p + 2 * hb);
+    if (nblocks > (avail - 3 * hb) / hb) return false;
+    size_t at = (3 + (size_t)nblocks) * hb;
+    raw.clear();
+    std::string part;
+    for (uint64_t b = 0; b < nblocks; b++) {
+        const uint64_t csize = vtp_header_value(f, p + (3 + b) * hb);
+        const uint64_t usize = (b + 1 == nblocks && last != 0) ? last : bsize;
+        if (csize > avail - at || usize > ((uint64_t)1 << 40)) return false;
+        if (!zlib_inflate(p + at, (size_t)csize, (size_t)usize, part)) return false;
+        raw += part;
+        at += (size_t)csize;
+    }
+    return true;
+}
+
+bool vtp_type(const std::string& t, int& size, bool& is_float, bool& is_signed) {
+    is_float = t == "Float32" || t == "Float64";
+    is_signed = t[0] == 'I' || is_float;
+    if (t == "Int8" || t == "UInt8") size = 1;
+    else if (t == "Int16" || t == "UInt16") size = 2;
+    else if (t == "Int32" || t == "UInt32" || t == "Float32") size = 4;
+    else if (t == "Int64" || t == "UInt64" || t == "Float64") size = 8;
+    else return false;
+    return true;
+}
+
+// one DataArray's values, as doubles (coordinates) or integers (ids)
+int vtp_array(const std::string& s, const VtpFile& f, const XmlTag& t, std::vector<double>* dv,
+              std::vector<int64_t>* iv) {
+    const std::string type = attr_of(t, "type"), format = attr_of(t, "format", "ascii");
+    int size = 0;
+    bool is_float = false, is_signed = false;
+    if (!vtp_type(type, size, is_float, is_signed))
+        return io_fail(ACVD_ERR_UNSUPPORTED, "VTK XML: data type " + type + " not read");
+    if (format == "ascii") {
+        if (t.empty) return ACVD_OK;
+        const size_t end = s.find("</DataArray>", t.close);
+        if (end == std::string::npos) return io_fail(ACVD_ERR_ARG, "VTK XML: unterminated DataArray");
+        std::istringstream in(s.substr(t.close, end - t.close));
+        std::string tok;
+        while (in >> tok) {
+            char* e = nullptr;
+            if (dv) dv->push_back(std::strtod(tok.c_str(), &e));
+            else iv->push_back((int64_t)std::strtoll(tok.c_str(), &e, 10));
+            if (!e || *e) return io_fail(ACVD_ERR_ARG, "VTK XML: bad ascii value '" + tok + "'");
+        }
+        return ACVD_OK;
+    }
+    std::string block, raw;
+    if (format == "binary") {
+        const size_t end = s.find("</DataArray>", t.close);
+        if (t.empty || end == std::string::npos) return io_fail(ACVD_ERR_ARG, "VTK XML: unterminated DataArray");
+        if (!b64_decode(s.data() + t.close, end - t.close, block))
+            return io_fail(ACVD_ERR_ARG, "VTK XML: bad base64 data");
+    } else if (format == "appended") {
+        const size_t off = (size_t)std::strtoull(attr_of(t, "offset", "0").c_str(), nullptr, 10);
+        if (off > f.appended.size()) return io_fail(ACVD_ERR_ARG, "VTK XML: appended offset past the data");
+        if (f.appended_b64) {
+            auto nx = std::upper_bound(f.offsets.begin(), f.offsets.end(), off);
+            const size_t stop = nx == f.offsets.end() ? f.appended.size() : *nx;
+            if (!b64_decode(f.appended.data() + off, stop - off, block))
+                return io_fail(ACVD_ERR_ARG, "VTK XML: bad base64 data");
+        } else {
+            block.assign(f.appended, off, std::string::npos);
+        }
+    } else {
+        return io_fail(ACVD_ERR_UNSUPPORTED, "VTK XML: DataArray format " + format + " not read");
+    }
+    if (!vtp_block(f, (const unsigned char*)block.data(), block.size(), raw))
+        return io_fail(ACVD_ERR_ARG, "VTK XML: corrupt or truncated binary data");
+    const size_t n = raw.size() / (size_t)size;
+    const unsigned char* p = (const unsigned char*)raw.data();
+    for (size_t i = 0; i < n; i++, p += size) {
+        double d = 0.0;
+        int64_t v = 0;
+        if (is_float) {
+            d = size == 4 ? (double)load_scalar<float>(p, f.little) : load_scalar<double>(p, f.little);
+            v = (int64_t)d;
+        } else if (size == 1) {
+            v = is_signed ? (int64_t)(int8_t)p[0] : (int64_t)p[0];
+        } else if (size == 2) {
+            v = is_signed ? (int64_t)load_scalar<int16_t>(p, f.little) : (int64_t)load_scalar<uint16_t>(p, f.little);
+        } else if (size == 4) {
+            v = is_signed ? (int64_t)load_scalar<int32_t>(p, f.little) : (int64_t)load_scalar<uint32_t>(p, f.little);
+        } else {
+            v = is_signed ? load_scalar<int64_t>(p, f.little) : (int64_t)load_scalar<uint64_t>(p, f.little);
+        }
+        if (dv) dv->push_back(is_float ? d : (double)v);
+        else iv->push_back(v);
+    }
+    return ACVD_OK;
+}
+
+// the first DataArray in [from, stop) whose Name is `name` (any name when null)
+bool vtp_find_array(const std::string& s, size_t from, size_t stop, const char* name, XmlTag& out) {
+    XmlTag t;
+    size_t at = from;
+    while (next_tag(s, at, stop, t)) {
+        at = t.close;
+        if (t.name == "DataArray" && (!name || attr_of(t, "Name") == name)) {
+            out = t;
+            return true;
+        }
+    }
+    return false;
+}
+
+int read_vtp(const std::string& s, MeshData& m) {
+    VtpFile f;
+    XmlTag t;
+    size_t at = 0;
+    bool found = false;
+    const size_t app = s.find("<AppendedData");
+    const size_t stop = app == std::string::npos ? s.size() : app;
+    while (next_tag(s, at, stop, t)) {
+        at = t.close;
+        if (t.name == "VTKFile") {
+            found = true;
+            break;
+        }
+    }
+    if (!found) return io_fail(ACVD_ERR_ARG, "not a VTK XML file");
+    if (attr_of(t, "type") != "PolyData") return io_fail(ACVD_ERR_UNSUPPORTED, "VTK XML: not a PolyData file");
+    f.little = attr_of(t, "byte_order", "LittleEndian") != "BigEndian";
+    const std::string ht = attr_of(t, "header_type", "UInt32");
+    if (ht != "UInt32" && ht != "UInt64") return io_fail(ACVD_ERR_UNSUPPORTED, "VTK XML: header_type " + ht);
+    f.header_bytes = ht == "UInt64" ? 8 : 4;
+    const std::string comp = attr_of(t, "compressor");
+    if (!comp.empty() && comp != "vtkZLibDataCompressor")
+        return io_fail(ACVD_ERR_UNSUPPORTED, "VTK XML: compressor " + comp + " not read (zlib only)");
+    f.zlib = !comp.empty();
+    if (app != std::string::npos) {
+        XmlTag a;
+        if (!next_tag(s, app, s.size(), a)) return io_fail(ACVD_ERR_ARG, "VTK XML: bad AppendedData");
+        const size_t mark = s.find('_', a.close);
+        if (mark == std::string::npos) return io_fail(ACVD_ERR_ARG, "VTK XML: AppendedData without '_'");
+        f.appended_b64 = attr_of(a, "encoding", "raw") == "base64";
+        if (f.appended_b64) {
+            const size_t end = s.find('<', mark + 1);
+            f.appended = s.substr(mark + 1, (end == std::string::npos ? s.size() : end) - mark - 1);
+        } else {
+            f.appended = s.substr(mark + 1);
+        }
+        XmlTag d;
+        size_t k = 0;
+        while (next_tag(s, k, stop, d)) {
+            k = d.close;
+            if (d.name == "DataArray" && attr_of(d, "format") == "appended")
+                f.offsets.push_back((size_t)std::strtoull(attr_of(d, "offset", "0").c_str(), nullptr, 10));
+        }
+        std::sort(f.offsets.begin(), f.offsets.end());
+    }
+    // pieces
+    int pieces = 0;
+    while (next_tag(s, at, stop, t)) {
+        at = t.close;
+        if (t.name != "Piece") continue;
+        pieces++;
+        const size_t pend_raw = s.find("</Piece>", t.close);
+        const size_t pend = pend_raw == std::string::npos || pend_raw > stop ? stop : pend_raw;
+        if (std::strtoll(attr_of(t, "NumberOfStrips", "0").c_str(), nullptr, 10) > 0)
+            return io_fail(ACVD_ERR_UNSUPPORTED, "VTK XML: triangle strips are not read");
+        const int64_t np = std::strtoll(attr_of(t, "NumberOfPoints", "0").c_str(), nullptr, 10);
+        const int64_t npoly = std::strtoll(attr_of(t, "NumberOfPolys", "0").c_str(), nullptr, 10);
+        const int64_t base = (int64_t)m.xyz.size() / 3;
+        std::vector<double> pts;
+        const size_t ptag = s.find("<Points", t.close);
+        XmlTag arr;
+        if (np > 0) {
+            if (ptag == std::string::npos || ptag > pend || !vtp_find_array(s, ptag, pend, nullptr, arr))
+                return io_fail(ACVD_ERR_ARG, "VTK XML: a Piece without Points");
+            if (int rc = vtp_array(s, f, arr, &pts, nullptr)) return rc;
+            if ((int64_t)pts.size() != 3 * np) return io_fail(ACVD_ERR_ARG, "VTK XML: Points count mismatch");
+        }
+        m.xyz.insert(m.xyz.end(), pts.begin(), pts.end());
+        if (npoly == 0) continue;
+        const size_t ytag = s.find("<Polys", t.close);
+        if (ytag == std::string::npos || ytag > pend) return io_fail(ACVD_ERR_ARG, "VTK XML: Polys missing");
+        std::vector<int64_t> conn, offs;
+        if (!vtp_find_array(s, ytag, pend, "connectivity", arr)) return io_fail(ACVD_ERR_ARG, "VTK XML: no connectivity");
+        if (int rc = vtp_array(s, f, arr, nullptr, &conn)) return rc;
+        if (!vtp_find_array(s, ytag, pend, "offsets", arr)) return io_fail(ACVD_ERR_ARG, "VTK XML: no offsets");
+        if (int rc = vtp_array(s, f, arr, nullptr, &offs)) return rc;
+        if ((int64_t)offs.size() != npoly) return io_fail(ACVD_ERR_ARG, "VTK XML: Polys count mismatch");
+        int64_t prev = 0;
+        std::vector<int64_t> poly;
+        for (int64_t e : offs) {
+            if (e < prev || e > (int64_t)conn.size()) return io_fail(ACVD_ERR_ARG, "VTK XML: bad Polys offsets");
+            poly.assign(conn.begin() + prev, conn.begin() + e);
+            for (int64_t& v : poly) {
+                if (v < 0 || v >= np) return io_fail(ACVD_ERR_ARG, "VTK XML: a face refers to a missing point");
+                v += base;
+            }
+            if (int rc = add_polygon(m, poly)) return rc;
+            prev = e;
+        }
+    }
+    if (!pieces) return io_fail(ACVD_ERR_ARG, "VTK XML: no Piece");
+    return check_faces(m);
+}
+
 // ---------------------------------------------------------------- writers
 void fmt_double(std::string& out, double v) {
     char b[40];
@@ -582,6 +1131,36 @@ std::string write_stl(const double* xyz, int64_t nv, const int32_t* tri, int64_t
     return out;
 }
 
+// VTK XML PolyData: inline base64 blocks with a UInt64 byte-count header, little endian,
+// float32 points (the float vtkPoints of vtkSurface), Int64 connectivity and offsets
+std::string write_vtp(const double* xyz, int64_t nv, const int32_t* tri, int64_t nf) {
+    auto block = [](const std::string& raw) {
+        std::string b;
+        store_scalar<uint64_t>(b, (uint64_t)raw.size(), true);
+        b += raw;
+        std::string enc;
+        b64_encode(b, enc);
+        return enc;
+    };
+    std::string pts, conn, offs;
+    for (int64_t i = 0; i < 3 * nv; i++) store_scalar<float>(pts, (float)xyz[i], true);
+    for (int64_t i = 0; i < 3 * nf; i++) store_scalar<int64_t>(conn, (int64_t)tri[i], true);
+    for (int64_t f = 1; f <= nf; f++) store_scalar<int64_t>(offs, 3 * f, true);
+    std::string out = "<?xml version=\"1.0\"?>\n"
+                      "<VTKFile type=\"PolyData\" version=\"1.0\" byte_order=\"LittleEndian\" header_type=\"UInt64\">\n"
+                      "  <PolyData>\n    <Piece NumberOfPoints=\"" + std::to_string(nv) +
+                      "\" NumberOfVerts=\"0\" NumberOfLines=\"0\" NumberOfStrips=\"0\" NumberOfPolys=\"" +
+                      std::to_string(nf) + "\">\n      <Points>\n"
+                      "        <DataArray type=\"Float32\" Name=\"Points\" NumberOfComponents=\"3\" format=\"binary\">\n"
+                      "          " + block(pts) + "\n        </DataArray>\n      </Points>\n      <Polys>\n"
+                      "        <DataArray type=\"Int64\" Name=\"connectivity\" format=\"binary\">\n"
+                      "          " + block(conn) + "\n        </DataArray>\n"
+                      "        <DataArray type=\"Int64\" Name=\"offsets\" format=\"binary\">\n"
+                      "          " + block(offs) + "\n        </DataArray>\n      </Polys>\n    </Piece>\n"
+                      "  </PolyData>\n</VTKFile>\n";
+    return out;
+}
+
 std::string write_vtk(const double* xyz, int64_t nv, const int32_t* tri, int64_t nf) {
     std::string out = "# vtk DataFile Version 4.2\nvtk output\nASCII\nDATASET POLYDATA\nPOINTS " +
                       std::to_string(nv) + " double\n";
@@ -618,8 +1197,7 @@ int acvd_read_mesh(const char* path, double** xyz, int64_t* n_vertices, int32_t*
     MeshData m;
     int rc;
     if (name.find(".vtk") != std::string::npos) rc = read_vtk(buf, m);
-    else if (name.find(".vtp") != std::string::npos)
-        return io_fail(ACVD_ERR_UNSUPPORTED, "VTK XML (.vtp) is not read by this build");
+    else if (name.find(".vtp") != std::string::npos) rc = read_vtp(buf, m);
     else if (name.find(".ply") != std::string::npos) rc = read_ply(buf, m);
     else if (name.find(".wrl") != std::string::npos)
         return io_fail(ACVD_ERR_UNSUPPORTED, "VRML import needs a render window; not read by this build");
@@ -655,6 +1233,7 @@ int acvd_write_mesh(const char* path, const double* xyz, int64_t n_vertices, con
     if (name.find(".vtk") != std::string::npos) out = write_vtk(xyz, n_vertices, tri, n_faces);
     else if (name.find(".ply") != std::string::npos) out = write_ply(xyz, n_vertices, tri, n_faces);
     else if (name.find(".stl") != std::string::npos) out = write_stl(xyz, n_vertices, tri, n_faces);
+    else if (name.find(".vtp") != std::string::npos) out = write_vtp(xyz, n_vertices, tri, n_faces);
     else if (name.find(".off") != std::string::npos) out = write_off(xyz, n_vertices, tri, n_faces);
     else if (name.find(".obj") != std::string::npos) out = write_obj(xyz, n_vertices, tri, n_faces);
     else return io_fail(ACVD_ERR_UNSUPPORTED, std::string("unknown mesh file type: ") + path);

@@ -408,12 +408,14 @@ int acvd_check_wait_limit(acvd_ctx* ctx, int64_t max_spins, int32_t* gave_up);
 /*
  * Triangle-mesh files, host only: the formats vtkSurface::CreateFromFile / WriteToFile
  * dispatch on by name (Common/vtkSurface.cxx:1958-2136; the lower-cased name contains
- * ".vtk", ".ply", ".off", ".obj" or ".stl", tested in the reference's order).  Read:
+ * ".vtk", ".vtp", ".ply", ".off", ".obj" or ".stl", tested in the reference's order).  Read:
  * PLY (ascii / binary either endian), OFF, OBJ, STL (ascii / binary; identical corners
  * merged in order of first appearance, triangles left degenerate dropped), legacy VTK
- * POLYDATA (ascii / binary).  Write: PLY (binary little endian, float points), OFF, OBJ,
- * STL (binary), legacy VTK (ascii).  Only triangles: another polygon is
- * ACVD_ERR_UNSUPPORTED, as are .vtp and .wrl.  acvd_read_mesh allocates *xyz (3 nV
+ * POLYDATA (ascii / binary), VTK XML PolyData (ascii, inline base64 or appended data;
+ * uncompressed or zlib; pieces concatenated).  Write: PLY (binary little endian, float
+ * points), OFF, OBJ, STL (binary), legacy VTK (ascii), VTK XML (inline base64, float
+ * points).  Only triangles: another polygon is ACVD_ERR_UNSUPPORTED, as are .wrl, triangle
+ * strips and .vtp data under another compressor.  acvd_read_mesh allocates *xyz (3 nV
  * doubles) and *tri (3 nF int32) with malloc; release them with acvd_free.  The text of
  * the last failure of this thread is acvd_io_last_error().  acvd_free and
  * acvd_io_last_error have no counterpart in the reference (VTK owns its readers' memory

@@ -115,7 +115,7 @@ def test_errors(tmp_path):
     bad.write_text("OFF\n3 1 0\n0 0 0\n1 0 0\n0 1 0\n3 0 1 7\n")
     with pytest.raises(acvd_gb300.AcvdError):
         E.read_mesh(str(bad))
-    for name in ("x.vtp", "x.wrl", "x.xyz"):
+    for name in ("x.vtp", "x.wrl", "x.xyz"):   # an empty .vtp is no VTK XML file
         (tmp_path / name).write_text("")
         with pytest.raises(acvd_gb300.AcvdError):
             E.read_mesh(str(tmp_path / name))
