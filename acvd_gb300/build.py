@@ -25,7 +25,7 @@ CU_SOURCES = ["primitives.cu", "topology.cu", "cluster.cu", "adjoint.cu", "engin
 CU_FILE_FLAGS = {"curvature.cu": ["-fmad=false"]}
 CXX_SOURCES = ["host.cpp", "io.cpp"]
 # command-line programs built from csrc/acvd_cli.cpp: name -> compile definitions
-CLI_PROGRAMS = {"acvd": [], "acvdq": ["-DACVD_CLI_QEM"]}
+CLI_PROGRAMS = {"acvd": [], "acvdq": ["-DACVD_CLI_QEM"], "anisotropic_remeshing_q": ["-DACVD_CLI_ANISO"]}
 
 
 def _nvcc() -> str:

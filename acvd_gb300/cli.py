@@ -2,16 +2,18 @@
 
     python -m acvd_gb300.acvd  file nvertices gradation [options]   # DiscreteRemeshing/Examples/ACVD.cxx
     python -m acvd_gb300.acvdq file nvertices gradation [options]   # DiscreteRemeshing/Examples/ACVDQ.cxx
+    python -m acvd_gb300.anisotropic_remeshing_q file nvertices gradation [options]
+                                         # DiscreteRemeshing/Examples/AnisotropicRemeshingQ.cxx
 
 Options are "-key value" pairs as in the reference:
 
     -b 0/1    boundary fixing (default 0)
-    -m 0/1    manifold output (ForceManifold, default 0)
+    -m 0/1    manifold output (ForceManifold, default 0; not an AnisotropicRemeshingQ option)
     -s t      subsampling threshold (default 10)
     -o dir    output directory
     -of name  output file name (default simplification.ply)
     -q n      ACVD: eigenvalues of the quadric post-placement (default 1, 0 = none);
-              ACVDQ: the QEM metric's QuadricsOptimizationLevel (default 3)
+              ACVDQ, AnisotropicRemeshingQ: the metric's QuadricsOptimizationLevel (default 3)
     -d 0      display (only 0: there is no graphics stack)
     -np n     threads of the reference's threaded engine (accepted, unused)
     -fv file  ACVDQ: vertex ids (whitespace separated) that stay output vertices
@@ -24,7 +26,8 @@ reference programs ignore them.
 
 Outputs follow the reference: ACVD writes <dir>smooth_<name> before the post-placement
 and <dir>/<name> after it, in the format the name's extension selects; ACVDQ writes
-<dir><name> as binary PLY whatever the extension.
+<dir><name> as binary PLY whatever the extension; AnisotropicRemeshingQ writes
+<dir>Remeshing.ply.
 """
 from __future__ import annotations
 
@@ -34,7 +37,8 @@ import sys
 import numpy as np
 
 from . import engine as _eng
-from .remesh import (IsotropicDiscreteRemeshing, QIsotropicDiscreteRemeshing, QuadricPostPlacement, Surface)
+from .remesh import (AnisotropicDiscreteRemeshing, IsotropicDiscreteRemeshing, QIsotropicDiscreteRemeshing,
+                     QuadricPostPlacement, Surface)
 
 _UNBUILT = {
     "-l": "long-edge splitting (vtkSurface::SplitLongEdges)",
@@ -73,11 +77,11 @@ def _parse(argv: list[str], prog: str):
     return opts
 
 
-def _remesh(opts, cls, console: int):
+def _remesh(opts, cls, console: int, manifold: bool = True):
     mesh = Surface.CreateFromFile(opts["file"])
     mesh.DisplayMeshProperties()
     r = cls()
-    r.SetForceManifold(int(opts.get("-m", 0)))
+    r.SetForceManifold(int(opts.get("-m", 0)) if manifold else 0)
     r.SetBoundaryFixing(int(opts.get("-b", 0)))
     r.SetInput(mesh)
     r.SetNumberOfClusters(opts["n"])
@@ -171,4 +175,18 @@ def main_acvdq(argv: list[str] | None = None) -> int:
     _eng.write_mesh(tmp, out.points, out.faces)
     if tmp != path:
         os.replace(tmp, path)
+    return 0
+
+
+def main_anisotropic_remeshing_q(argv: list[str] | None = None) -> int:
+    """AnisotropicRemeshingQ (DiscreteRemeshing/Examples/AnisotropicRemeshingQ.cxx): the
+    quadric-anisotropic metric with options -s, -o, -q, -b, -d 0; the output is
+    <dir>Remeshing.ply."""
+    argv = sys.argv[1:] if argv is None else argv
+    opts = _parse(argv, "AnisotropicRemeshingQ")
+    r = _remesh(opts, AnisotropicDiscreteRemeshing, 2, manifold=False)
+    if "-q" in opts:
+        r.GetMetric().SetQuadricsOptimizationLevel(int(opts["-q"]))
+    r.Remesh()
+    _eng.write_mesh((opts.get("-o") or "") + "Remeshing.ply", r.GetOutput().points, r.GetOutput().faces)
     return 0

@@ -2,8 +2,12 @@
 //
 //   acvd  file nvertices gradation [options]   (DiscreteRemeshing/Examples/ACVD.cxx)
 //   acvdq file nvertices gradation [options]   (DiscreteRemeshing/Examples/ACVDQ.cxx)
+//   anisotropic_remeshing_q file nvertices gradation [options]
+//                                              (DiscreteRemeshing/Examples/AnisotropicRemeshingQ.cxx)
 //
-// Compiled twice from this file (ACVD_CLI_QEM selects ACVDQ).  The remeshing follows
+// Compiled three times from this file (ACVD_CLI_QEM selects ACVDQ, ACVD_CLI_ANISO
+// AnisotropicRemeshingQ: the quadric-anisotropic metric, its curvature and principal
+// directions computed on the original mesh, output <dir>Remeshing.ply).  The remeshing follows
 // vtkDiscreteRemeshing::Remesh (DiscreteRemeshing/vtkDiscreteRemeshing.h:877-954):
 // subdivision below SubsamplingThreshold x K, curvature of the original mesh when the
 // gradation asks for it (interpolated through the subdivision), the reference's initial
@@ -26,9 +30,12 @@
 
 namespace {
 
-#ifdef ACVD_CLI_QEM
+#if defined(ACVD_CLI_QEM)
 const char* kProg = "ACVDQ";
 const int kMetric = ACVD_METRIC_QEM;
+#elif defined(ACVD_CLI_ANISO)
+const char* kProg = "AnisotropicRemeshingQ";
+const int kMetric = ACVD_METRIC_QUADRIC_ANISOTROPIC;
 #else
 const char* kProg = "ACVD";
 const int kMetric = ACVD_METRIC_ISOTROPIC;
@@ -100,8 +107,8 @@ int main(int argc, char** argv) {
     int k = std::atoi(argv[2]);
     const double gradation = std::atof(argv[3]);
     int boundary_fixing = 0, force_manifold = 0, threshold = 10;
-#ifdef ACVD_CLI_QEM
-    int level = 3;          // the QEM metric's QuadricsOptimizationLevel
+#if defined(ACVD_CLI_QEM) || defined(ACVD_CLI_ANISO)
+    int level = 3;          // the metric's QuadricsOptimizationLevel
 #else
     int level = 1;          // ACVD's post-placement eigenvalues
 #endif
@@ -113,7 +120,9 @@ int main(int argc, char** argv) {
         const std::string key = argv[a];
         const char* value = argv[a + 1];
         if (key == "-b") boundary_fixing = std::atoi(value);
+#ifndef ACVD_CLI_ANISO
         else if (key == "-m") force_manifold = std::atoi(value);
+#endif
         else if (key == "-s") threshold = std::atoi(value);
         else if (key == "-o") { outdir = value; have_outdir = true; }
         else if (key == "-of") outfile = value;
@@ -177,20 +186,27 @@ int main(int argc, char** argv) {
     acvd_ctx* ctx = acvd_create(&opts);
     if (!ctx) die("acvd_create: no usable CUDA device");
 
-    // curvature of the original mesh when the metric's gradation asks for it
+    // curvature of the original mesh when the metric's gradation asks for it (the
+    // anisotropic metric always needs it, with the principal directions)
     std::vector<double> ind;
-    const bool need_ind = gradation > 0.0;
+    std::vector<float> pd;
+    const bool need_pd = kMetric == ACVD_METRIC_QUADRIC_ANISOTROPIC;
+    const bool need_ind = gradation > 0.0 || need_pd;
     bool original_on_device = false;
     if (need_ind) {
         set_mesh(ctx, m);
         original_on_device = true;
         ind.resize(m.nv());
-        check(ctx, acvd_compute_curvature(ctx, ind.data(), nullptr), "acvd_compute_curvature");
+        if (need_pd) pd.resize(6 * (size_t)m.nv());
+        check(ctx, acvd_compute_curvature(ctx, ind.data(), need_pd ? pd.data() : nullptr), "acvd_compute_curvature");
     }
     // CheckSubsamplingRatio: subdivide while the mesh has fewer than threshold x K vertices
     int levels = 0;
     while (m.nv() < (int64_t)threshold * k) {
         if (m.nf() == 0 || levels >= 99) die("the mesh cannot be subdivided to SubsamplingThreshold x K vertices");
+        // the reference interpolates only the indicator through the subdivision, and its
+        // anisotropic metric then reads principal directions past their end
+        if (need_pd) die("the quadric-anisotropic metric needs SubsamplingThreshold x K input vertices");
         std::printf("Subdividing mesh\n");
         Mesh s;
         const int64_t nout = m.nv() + m.ne();
@@ -209,10 +225,13 @@ int main(int argc, char** argv) {
         levels++;
     }
     if (!original_on_device) set_mesh(ctx, m);
-    check(ctx, acvd_set_metric(ctx, kMetric, need_ind ? ind.data() : nullptr, nullptr, gradation), "acvd_set_metric");
-#ifdef ACVD_CLI_QEM
+    check(ctx, acvd_set_metric(ctx, kMetric, need_ind ? ind.data() : nullptr, need_pd ? pd.data() : nullptr, gradation),
+          "acvd_set_metric");
+#if defined(ACVD_CLI_QEM)
     check(ctx, acvd_set_quadrics_optimization_level(ctx, level), "acvd_set_quadrics_optimization_level");
     check(ctx, acvd_set_unconstrained_initialization(ctx, 1), "acvd_set_unconstrained_initialization");
+#elif defined(ACVD_CLI_ANISO)
+    check(ctx, acvd_set_quadrics_optimization_level(ctx, level), "acvd_set_quadrics_optimization_level");
 #else
     check(ctx, acvd_set_quadrics_optimization_level(ctx, 3), "acvd_set_quadrics_optimization_level");
 #endif
@@ -270,7 +289,12 @@ int main(int argc, char** argv) {
         out_tri.insert(out_tri.end(), bt.begin(), bt.end());
     }
     std::printf("Coarse mesh: %lld vertices, %lld faces\n", (long long)out_xyz.size() / 3, (long long)nt);
-#ifdef ACVD_CLI_QEM
+#if defined(ACVD_CLI_ANISO)
+    // AnisotropicRemeshingQ.cxx:232-247: <dir>Remeshing.ply, binary PLY
+    write_mesh(outdir + "Remeshing.ply", out_xyz, out_tri);
+    (void)have_outdir;
+    (void)level;
+#elif defined(ACVD_CLI_QEM)
     // the fixed vertices are the first output vertices, in place (ACVDQ.cxx:341-363)
     if (has_fixed) {
         for (size_t i = 0; i < fixed.size(); i++)

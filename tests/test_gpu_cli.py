@@ -45,13 +45,15 @@ def test_acvdq_program_with_subdivision_and_options(tmp_path):
 @pytest.mark.parametrize("prog,args", [
     ("acvd", ["300", "0.5", "-q", "2"]),
     ("acvdq", ["200", "0", "-m", "1", "-b", "1", "-q", "2"]),
+    ("anisotropic_remeshing_q", ["300", "0.5", "-b", "1", "-q", "2", "-m", "1"]),
 ])
 def test_native_programs_match_the_python_drivers(tmp_path, prog, args):
     """The native programs (C++ over the C ABI) and the Python drivers run the same steps:
     their output files are byte for byte the same."""
     import subprocess
     from acvd_gb300 import build as B
-    mesh = synth.torus(80, 40, seed=2) if prog == "acvd" else synth.heightfield(30, seed=2)
+    mesh = {"acvd": lambda: synth.torus(80, 40, seed=2), "acvdq": lambda: synth.heightfield(30, seed=2),
+            "anisotropic_remeshing_q": lambda: synth.heightfield(64, seed=4)}[prog]()
     src = str(tmp_path / "in.ply")
     E.write_mesh(src, mesh.points, mesh.faces)
     native, python = tmp_path / "native", tmp_path / "python"
@@ -60,7 +62,8 @@ def test_native_programs_match_the_python_drivers(tmp_path, prog, args):
     r = subprocess.run([os.path.join(B.OUT, prog), src] + args + ["-o", str(native) + "/"], capture_output=True,
                        text=True)
     assert r.returncode == 0, r.stderr
-    main = cli.main_acvd if prog == "acvd" else cli.main_acvdq
+    main = {"acvd": cli.main_acvd, "acvdq": cli.main_acvdq,
+            "anisotropic_remeshing_q": cli.main_anisotropic_remeshing_q}[prog]
     assert main([src] + args + ["-o", str(python) + "/"]) == 0
     names = sorted(os.listdir(native))
     assert names == sorted(os.listdir(python)) and names

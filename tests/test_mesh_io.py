@@ -157,7 +157,7 @@ def test_native_programs_parse_like_the_reference():
     them before any file or device is touched."""
     import subprocess
     from acvd_gb300 import build as B
-    for name in ("acvd", "acvdq"):
+    for name in ("acvd", "acvdq", "anisotropic_remeshing_q"):
         exe = os.path.join(B.OUT, name)
         assert os.access(exe, os.X_OK)
         r = subprocess.run([exe], capture_output=True, text=True)
