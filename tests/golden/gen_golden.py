@@ -7,9 +7,13 @@ $ACVD_REFERENCE_ROOT).  For each small case below this script stores the inputs
 outputs: the initial sampling, the converged labels, global energy, per-cluster
 sizes / centroids / energies, the accumulators of a fixed assignment and its
 quadric post-placement (the ACVD driver's last step) at levels 1 and 3, and the
-reference's curvature indicator / principal directions of the mesh.
+reference's curvature indicator / principal directions of the mesh.  The fixtures
+under fixed_vertices/ hold runs with fixed vertices as ACVDQ sets them
+(SetFixedClusters, and the QEM clusters' AnchorItem) and a CleanClustering with fixed
+vertices.
 
-    python tests/golden/gen_golden.py
+    python tests/golden/gen_golden.py           # every fixture
+    python tests/golden/gen_golden.py fixed     # the fixed-vertex fixtures only
 """
 import os
 import sys
@@ -31,6 +35,50 @@ CASES = [
     ("qem_torus48x24_k100_g0", "qem", lambda: synth.torus(48, 24, seed=3), 100, 0.0, 0, None),
     ("aniso_heightfield40_k100_g15", "aniso", lambda: synth.heightfield(40, seed=0), 100, 1.5, 0, None),
 ]
+
+
+FIXED_CASES = [
+    # name, metric, mesh builder, K (fixed vertices included), gradation, unconstrained_init, fixed count
+    ("qem_torus64x32_k212_fixed12_g15", "qem", lambda: synth.torus(64, 32, seed=0), 212, 1.5, 1, 12),
+    ("iso_icosphere4_k130_fixed10", "iso", lambda: synth.icosphere(4, seed=1), 130, 0.0, 0, 10),
+]
+
+
+def fixed_ids(n, count, seed):
+    return np.sort(np.random.default_rng(seed).choice(n, size=count, replace=False)).astype(np.int32)
+
+
+def main_fixed():
+    O.build(ref=True)
+    out_dir = os.path.join(os.path.dirname(os.path.abspath(__file__)), "fixed_vertices")
+    os.makedirs(out_dir, exist_ok=True)
+    for name, metric, mk, k, grad, uinit, nfix in FIXED_CASES:
+        m = mk()
+        ind = m.indicator if grad > 0 else None
+        fixed = fixed_ids(m.n_points, nfix, k)
+        r = O.Ref(metric, m.points, m.faces, k, grad, ind, None, unconstrained_init=uinit)
+        r.set_fixed(fixed)
+        if metric == "qem":
+            r.set_anchors(fixed)
+        r.init(None)
+        lab_init = r.labels()
+        r.run()
+        cl = r.clusters()
+        # CleanClustering alone on a scattered assignment, the fixed vertices last in their clusters
+        lab_r = np.random.default_rng(3).integers(0, k, size=m.n_points).astype(np.int32)
+        fixed_c = np.array([int(np.flatnonzero(lab_r == c)[-1]) for c in range(nfix)], dtype=np.int32)
+        c = O.Ref(metric, m.points, m.faces, k, grad, ind, None)
+        c.set_fixed(fixed_c)
+        c.init(lab_r)
+        n_split = c.clean()
+        d = dict(points=m.points, faces=m.faces, k=k, gradation=grad, unconstrained_init=uinit, metric=metric,
+                 fixed=fixed, labels_init=lab_init, labels=r.labels(), energy=r.global_energy(),
+                 size=cl["size"], centroid=cl["centroid"], cluster_energy=cl["energy"],
+                 clean_labels_in=lab_r, clean_fixed=fixed_c, clean_labels_out=c.labels(), clean_split=n_split)
+        if ind is not None:
+            d["indicator"] = ind
+        np.savez_compressed(os.path.join(out_dir, name + ".npz"), **d)
+        print(f"{name}: N={m.n_points} K={k} fixed={nfix} E={d['energy']:.12g}")
 
 
 def main():
@@ -80,4 +128,6 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] != ["fixed"]:
+        main()
+    main_fixed()

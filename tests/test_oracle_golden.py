@@ -72,3 +72,42 @@ def test_curvature_matches_reference(oracle_lib, path):
     ind, pd = oracle_lib.Port(str(g["metric"]), g["points"], g["faces"], int(g["k"]), 0.0).curvature()
     np.testing.assert_array_equal(ind, g["curv_indicator"])
     np.testing.assert_array_equal(pd, g["curv_dirs"])
+
+
+FIXED = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "fixed_vertices", "*.npz")))
+
+
+@pytest.mark.parametrize("path", FIXED, ids=[os.path.basename(p)[:-4] for p in FIXED])
+def test_fixed_vertices_match_reference(oracle_lib, path):
+    """Fixed vertices as ACVDQ sets them (SetFixedClusters, and the QEM clusters'
+    AnchorItem): the reference's initial sampling, converged run and cluster records, and
+    its CleanClustering of a scattered assignment with fixed vertices; the host library's
+    sampling with fixed vertices gives the same labels."""
+    import acvd_gb300
+    g = _load(path)
+    metric = str(g["metric"])
+    fixed = g["fixed"]
+    p = _port(oracle_lib, g)
+    p.set_fixed(fixed)
+    if metric == "qem":
+        p.set_anchors(fixed)
+    p.init(None)
+    np.testing.assert_array_equal(p.labels(), g["labels_init"])
+    p.run()
+    np.testing.assert_array_equal(p.labels(), g["labels"])
+    assert p.global_energy() == float(g["energy"])
+    cl = p.clusters()
+    np.testing.assert_array_equal(cl["size"], g["size"])
+    np.testing.assert_array_equal(cl["centroid"], g["centroid"])
+    np.testing.assert_array_equal(cl["energy"], g["cluster_energy"])
+    # the host library's sampling
+    row, col, _ = acvd_gb300.build_topology(g["points"].shape[0], g["faces"])
+    w = acvd_gb300.vertex_weights(metric, g["points"], g["faces"], g.get("indicator"), float(g["gradation"]))
+    np.testing.assert_array_equal(acvd_gb300.initial_sampling(row, col, w, int(g["k"]), fixed=fixed),
+                                  g["labels_init"])
+    # CleanClustering with fixed vertices
+    c = oracle_lib.Port(metric, g["points"], g["faces"], int(g["k"]), float(g["gradation"]), g.get("indicator"))
+    c.set_fixed(g["clean_fixed"])
+    c.init(g["clean_labels_in"])
+    assert c.clean() == int(g["clean_split"])
+    np.testing.assert_array_equal(c.labels(), g["clean_labels_out"])
