@@ -16,13 +16,16 @@ Options are "-key value" pairs as in the reference:
               ACVDQ, AnisotropicRemeshingQ: the metric's QuadricsOptimizationLevel (default 3)
     -d 0      display (only 0: there is no graphics stack)
     -np n     threads of the reference's threaded engine (accepted, unused)
+    -l ratio  split the edges longer than ratio x the mean edge length first
+              (vtkSurface::SplitLongEdges)
     -fv file  ACVDQ: vertex ids (whitespace separated) that stay output vertices
     -ft file  ACVDQ: face ids whose three vertices stay output vertices
 
-Options of the reference that need parts this package does not build -- -l (long-edge
-splitting), -w (energy log), -cd/-cmin/-cmax/-cf (custom density image), -p (pooling)
--- stop with an error rather than being ignored.  Other keys are ignored, as the
-reference programs ignore them.
+-l, -fv and -ft act on the mesh in the order given, as the reference's argument loop
+does.  Options of the reference that need parts this package does not build -- -w
+(energy log), -cd/-cmin/-cmax/-cf (custom density image), -p (pooling) -- stop with an
+error rather than being ignored.  Other keys are ignored, as the reference programs
+ignore them.
 
 Outputs follow the reference: ACVD writes <dir>smooth_<name> before the post-placement
 and <dir>/<name> after it, in the format the name's extension selects; ACVDQ writes
@@ -41,7 +44,6 @@ from .remesh import (AnisotropicDiscreteRemeshing, IsotropicDiscreteRemeshing, Q
                      QuadricPostPlacement, Surface)
 
 _UNBUILT = {
-    "-l": "long-edge splitting (vtkSurface::SplitLongEdges)",
     "-w": "the global energy log (which the reference's ACVD / ACVDQ write through an uninitialised "
           "timer, vtkUniformClustering.h:1384-1395)",
     "-cd": "custom density images",
@@ -77,10 +79,33 @@ def _parse(argv: list[str], prog: str):
     return opts
 
 
-def _remesh(opts, cls, console: int, manifold: bool = True):
+def _mesh_options(opts, mesh: Surface, fixed_vertices: bool):
+    """-l, -fv and -ft in the order given (ACVD.cxx:151-155, ACVDQ.cxx:192-280): a split
+    replaces the mesh, -ft maps face ids of the mesh as it is at that point."""
+    fixed = None
+    for key, value in opts.get("_order", []):
+        if key == "-l":
+            print(f"Splitting edges longer than {float(value)} times the average edge length")
+            pts, tri = _eng.split_long_edges(mesh.points, mesh.faces, float(value))
+            mesh = Surface(pts, tri)
+        elif key == "-fv" and fixed_vertices:
+            fixed = np.asarray(_read_ids(value), dtype=np.int32)
+        elif key == "-ft" and fixed_vertices:
+            faces = _read_ids(value)
+            mark = np.zeros(mesh.GetNumberOfPoints(), dtype=bool)
+            for f in faces:
+                mark[mesh.faces[f]] = True
+            fixed = np.nonzero(mark)[0].astype(np.int32)
+            print(f"Added {len(faces)} constraints on triangles")
+    return mesh, fixed
+
+
+def _remesh(opts, cls, console: int, manifold: bool = True, fixed_vertices: bool = False):
     mesh = Surface.CreateFromFile(opts["file"])
     mesh.DisplayMeshProperties()
+    mesh, fixed = _mesh_options(opts, mesh, fixed_vertices)
     r = cls()
+    r._cli_fixed = fixed
     r.SetForceManifold(int(opts.get("-m", 0)) if manifold else 0)
     r.SetBoundaryFixing(int(opts.get("-b", 0)))
     r.SetInput(mesh)
@@ -127,19 +152,8 @@ def _read_ids(path: str) -> list[int]:
 
 
 def _fixed_vertices(opts, mesh: Surface):
-    """-fv / -ft (ACVDQ.cxx:246-280): the last of them given wins."""
-    fixed = None
-    for key, value in opts.get("_order", []):
-        if key == "-fv":
-            fixed = _read_ids(value)
-        elif key == "-ft":
-            faces = _read_ids(value)
-            mark = np.zeros(mesh.GetNumberOfPoints(), dtype=bool)
-            for f in faces:
-                mark[mesh.faces[f]] = True
-            fixed = [int(v) for v in np.nonzero(mark)[0]]
-            print(f"Added {len(faces)} constraints on triangles")
-    return None if fixed is None else np.asarray(fixed, dtype=np.int32)
+    """-fv / -ft (ACVDQ.cxx:246-280): the last of them given wins; None without either."""
+    return _mesh_options({"_order": [kv for kv in opts.get("_order", []) if kv[0] != "-l"]}, mesh, True)[1]
 
 
 def main_acvdq(argv: list[str] | None = None) -> int:
@@ -148,12 +162,12 @@ def main_acvdq(argv: list[str] | None = None) -> int:
     are the first output vertices, anchored in place (:327-363)."""
     argv = sys.argv[1:] if argv is None else argv
     opts = _parse(argv, "ACVDQ")
-    r = _remesh(opts, QIsotropicDiscreteRemeshing, 2)
+    r = _remesh(opts, QIsotropicDiscreteRemeshing, 2, fixed_vertices=True)
     if "-q" in opts:
         r.GetMetric().SetQuadricsOptimizationLevel(int(opts["-q"]))
     r.SetUnconstrainedInitialization(1)
     mesh = r.GetInput()
-    fixed = _fixed_vertices(opts, mesh)
+    fixed = r._cli_fixed
     if fixed is not None:
         r.SetFixedClusters(fixed)
         r.SetNumberOfClusters(opts["n"] + len(fixed))

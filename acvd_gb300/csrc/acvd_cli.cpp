@@ -24,6 +24,7 @@
 #include <cstring>
 #include <fstream>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/acvd_gpu.h"
@@ -114,7 +115,8 @@ int main(int argc, char** argv) {
 #endif
     std::string outdir, outfile = "simplification.ply";
     bool have_outdir = false;
-    std::string fixed_key, fixed_file;   // the last -fv / -ft given (ACVDQ)
+    // -l, -fv, -ft act on the mesh in the order given (the reference's argument loop)
+    std::vector<std::pair<std::string, std::string>> mesh_ops;
     for (int a = 4; a < argc; a += 2) {
         if (a + 1 >= argc) die(std::string("option ") + argv[a] + " without a value");
         const std::string key = argv[a];
@@ -130,14 +132,15 @@ int main(int argc, char** argv) {
         else if (key == "-np") {}
         else if (key == "-d") {
             if (std::atoi(value) != 0) die("display needs a graphics stack; only -d 0 is available");
-        } else if (key == "-l" || key == "-w" || key == "-cd" || key == "-cmin" || key == "-cmax" || key == "-cf" ||
-                   key == "-p") {
+        } else if (key == "-w" || key == "-cd" || key == "-cmin" || key == "-cmax" || key == "-cf" || key == "-p") {
             die("option " + key + " needs a part this build does not have");
+        } else if (key == "-l") {
+            if (!(std::atof(value) > 0.0)) die("-l needs a positive ratio");
+            mesh_ops.emplace_back(key, value);
         }
 #ifdef ACVD_CLI_QEM
         else if (key == "-fv" || key == "-ft") {
-            fixed_key = key;
-            fixed_file = value;
+            mesh_ops.emplace_back(key, value);
         }
 #endif
     }
@@ -157,23 +160,42 @@ int main(int argc, char** argv) {
     topology(m);
     std::printf("load : %s\nMesh with %lld vertices, %lld faces, %lld edges\n", file, (long long)m.nv(),
                 (long long)m.nf(), (long long)m.ne());
-    // fixed vertices: -fv lists vertex ids, -ft face ids whose vertices are fixed
+    // -l splits long edges (vtkSurface::SplitLongEdges); fixed vertices: -fv lists vertex
+    // ids, -ft face ids whose vertices are fixed; the last of -fv / -ft wins
     std::vector<int32_t> fixed;
-    const bool has_fixed = !fixed_key.empty();
-    const std::vector<double> input_xyz = has_fixed ? m.xyz : std::vector<double>();
-    if (fixed_key == "-fv") {
-        fixed = read_ids(fixed_file.c_str());
-    } else if (fixed_key == "-ft") {
-        const std::vector<int32_t> faces = read_ids(fixed_file.c_str());
-        std::vector<char> mark(m.nv(), 0);
-        for (int32_t f : faces) {
-            if (f < 0 || f >= m.nf()) die("-ft: face id " + std::to_string(f) + " outside the mesh");
-            for (int q = 0; q < 3; q++) mark[m.tri[3 * (int64_t)f + q]] = 1;
+    bool has_fixed = false;
+    for (const auto& op : mesh_ops) {
+        if (op.first == "-l") {
+            const double ratio = std::atof(op.second.c_str());
+            std::printf("Splitting edges longer than %g times the average edge length\n", ratio);
+            double* xyz = nullptr;
+            int32_t* tri = nullptr;
+            int64_t nv = 0, nf = 0;
+            check(nullptr, acvd_split_long_edges(m.nv(), m.xyz.data(), m.nf(), m.tri.data(), ratio, &xyz, &nv, &tri, &nf),
+                  "acvd_split_long_edges");
+            m.xyz.assign(xyz, xyz + 3 * nv);
+            m.tri.assign(tri, tri + 3 * nf);
+            acvd_free(xyz);
+            acvd_free(tri);
+            topology(m);
+        } else if (op.first == "-fv") {
+            fixed = read_ids(op.second.c_str());
+            has_fixed = true;
+        } else {
+            const std::vector<int32_t> faces = read_ids(op.second.c_str());
+            std::vector<char> mark(m.nv(), 0);
+            for (int32_t f : faces) {
+                if (f < 0 || f >= m.nf()) die("-ft: face id " + std::to_string(f) + " outside the mesh");
+                for (int q = 0; q < 3; q++) mark[m.tri[3 * (int64_t)f + q]] = 1;
+            }
+            fixed.clear();
+            for (int64_t v = 0; v < m.nv(); v++)
+                if (mark[v]) fixed.push_back((int32_t)v);
+            std::printf("Added %d constraints on triangles\n", (int)faces.size());
+            has_fixed = true;
         }
-        for (int64_t v = 0; v < m.nv(); v++)
-            if (mark[v]) fixed.push_back((int32_t)v);
-        std::printf("Added %d constraints on triangles\n", (int)faces.size());
     }
+    const std::vector<double> input_xyz = has_fixed ? m.xyz : std::vector<double>();
     if (has_fixed) {
         for (int32_t v : fixed)
             if (v < 0 || v >= m.nv()) die("fixed vertex id " + std::to_string(v) + " outside the mesh");

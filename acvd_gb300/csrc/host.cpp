@@ -3,11 +3,14 @@
 // weights and the default initial sampling.  These run before
 // MinimizeEnergy() in the reference too (Init / BuildMetric / InitSamples,
 // Common/vtkUniformClustering.h:1363,1124) and are not part of the GPU hot path.
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <cstdlib>
 #include <cstring>
 #include <queue>
 #include <random>
+#include <unordered_map>
 #include <vector>
 
 #include "../../include/acvd_gpu.h"
@@ -247,6 +250,172 @@ int acvd_initial_sampling_fixed(int64_t n_vertices, const int32_t* csr_row, cons
         remaining--;
         labels[item] = remaining + offset;
     }
+    return ACVD_OK;
+}
+
+
+// vtkSurface::SplitLongEdges (Common/vtkSurface.cxx:444-603) on the host.  The threshold
+// is ratio x the mean edge length of the input; passes repeat until no edge is longer.
+// A pass gives every edge longer than the threshold (and with a face) a midpoint vertex,
+// appended in edge-id order and stored as float (vtkPoints), then splits each face with
+// the reference's case table (Split2 / Split3 / four-way, :378-441, :524-582).  The
+// reference's dynamic edge table decides the edge ids of later passes: a face's deletion
+// frees, in the face's edge order, the edges left without a face into a FIFO that the
+// next new edges draw from (vtkSurfaceBase.cxx:560-609, 1166-1221), and the first face
+// of a split takes the deleted face's slot (:1223-1320).  That bookkeeping is simulated
+// here, so vertices and faces come out in the reference's order.  The faces are taken
+// as consistently oriented (the splits keep orientation; the reference's closing
+// CheckNormals then changes nothing).
+int acvd_split_long_edges(int64_t n_vertices, const double* xyz, int64_t n_faces, const int32_t* tri, double ratio,
+                          double** out_xyz, int64_t* out_nv, int32_t** out_tri, int64_t* out_nf) {
+    if (n_vertices <= 0 || n_faces < 0 || !xyz || (n_faces && !tri) || !out_xyz || !out_nv || !out_tri || !out_nf ||
+        !(ratio > 0.0))
+        return ACVD_ERR_ARG;
+    *out_xyz = nullptr;
+    *out_tri = nullptr;
+    for (int64_t i = 0; i < 3 * n_faces; i++)
+        if (tri[i] < 0 || tri[i] >= n_vertices) return ACVD_ERR_ARG;
+    for (int64_t f = 0; f < n_faces; f++)
+        if (tri[3 * f] == tri[3 * f + 1] || tri[3 * f + 1] == tri[3 * f + 2] || tri[3 * f] == tri[3 * f + 2])
+            return ACVD_ERR_ARG;
+    std::vector<double> pts(xyz, xyz + 3 * n_vertices);
+    std::vector<int32_t> faces(tri, tri + 3 * n_faces);
+    struct DynEdge {
+        int32_t a, b;
+        int nf;
+        bool active;
+    };
+    std::vector<DynEdge> edges;
+    std::unordered_map<uint64_t, int32_t> index;   // active edges by vertex pair
+    std::queue<int32_t> freed;
+    auto key = [](int32_t a, int32_t b) {
+        const uint32_t lo = (uint32_t)std::min(a, b), hi = (uint32_t)std::max(a, b);
+        return ((uint64_t)hi << 32) | lo;
+    };
+    auto add_edge = [&](int32_t a, int32_t b) {
+        auto it = index.find(key(a, b));
+        if (it != index.end()) {
+            edges[it->second].nf++;
+            return;
+        }
+        int32_t e;
+        if (freed.empty()) {
+            e = (int32_t)edges.size();
+            edges.push_back({});
+        } else {
+            e = freed.front();
+            freed.pop();
+        }
+        edges[e] = {a, b, 1, true};
+        index[key(a, b)] = e;
+    };
+    auto add_face_edges = [&](const int32_t* f) {
+        for (int j = 0; j < 3; j++) add_edge(f[j], f[(j + 1) % 3]);
+    };
+    auto delete_face_edges = [&](const int32_t* f) {
+        for (int j = 0; j < 3; j++) {
+            auto it = index.find(key(f[j], f[(j + 1) % 3]));
+            DynEdge& e = edges[it->second];
+            if (--e.nf == 0) {
+                e.active = false;
+                freed.push(it->second);
+                index.erase(it);
+            }
+        }
+    };
+    auto edge_of = [&](int32_t a, int32_t b) { return index.at(key(a, b)); };
+    for (int64_t f = 0; f < n_faces; f++) add_face_edges(&faces[3 * f]);
+    auto length = [&](int32_t a, int32_t b) {
+        const double dx = pts[3 * (size_t)a] - pts[3 * (size_t)b], dy = pts[3 * (size_t)a + 1] - pts[3 * (size_t)b + 1],
+                     dz = pts[3 * (size_t)a + 2] - pts[3 * (size_t)b + 2];
+        return std::sqrt(dx * dx + dy * dy + dz * dz);
+    };
+    double threshold = 0.0;
+    for (const DynEdge& e : edges) threshold += length(e.a, e.b);
+    threshold = edges.empty() ? 0.0 : ratio * threshold / (double)edges.size();
+    for (bool split = !edges.empty(); split;) {
+        split = false;
+        std::vector<int32_t> mid(edges.size(), -1);
+        for (size_t e = 0; e < edges.size(); e++) {
+            if (!edges[e].active || length(edges[e].a, edges[e].b) <= threshold) continue;
+            for (int c = 0; c < 3; c++)
+                pts.push_back((double)(float)(0.5 * (pts[3 * (size_t)edges[e].a + c] + pts[3 * (size_t)edges[e].b + c])));
+            mid[e] = (int32_t)(pts.size() / 3 - 1);
+        }
+        const size_t ncells = faces.size() / 3;
+        for (size_t i = 0; i < ncells; i++) {
+            const int32_t v1 = faces[3 * i], v2 = faces[3 * i + 1], v3 = faces[3 * i + 2];
+            const int32_t v12 = mid[edge_of(v1, v2)], v13 = mid[edge_of(v1, v3)], v23 = mid[edge_of(v2, v3)];
+            int32_t out[4][3];
+            int n = 0;
+            auto put = [&](int32_t a, int32_t b, int32_t c) {
+                out[n][0] = a;
+                out[n][1] = b;
+                out[n][2] = c;
+                n++;
+            };
+            // Split2(f, a, b, c, ab): (a, ab, c), (ab, b, c)
+            auto split2 = [&](int32_t a, int32_t b, int32_t c, int32_t ab) {
+                put(a, ab, c);
+                put(ab, b, c);
+            };
+            // Split3(f, a, b, c, ab, ac): (a, ab, ac), (ab, b, c), (c, ac, ab)
+            auto split3 = [&](int32_t a, int32_t b, int32_t c, int32_t ab, int32_t ac) {
+                put(a, ab, ac);
+                put(ab, b, c);
+                put(c, ac, ab);
+            };
+            if (v12 < 0) {
+                if (v13 < 0) {
+                    if (v23 >= 0) split2(v2, v3, v1, v23);
+                } else if (v23 < 0) {
+                    split2(v3, v1, v2, v13);
+                } else {
+                    split3(v3, v1, v2, v13, v23);
+                }
+            } else if (v13 < 0) {
+                if (v23 < 0) split2(v1, v2, v3, v12);
+                else split3(v2, v3, v1, v23, v12);
+            } else if (v23 < 0) {
+                split3(v1, v2, v3, v12, v13);
+            } else {
+                put(v1, v12, v13);
+                put(v12, v2, v23);
+                put(v23, v3, v13);
+                put(v12, v23, v13);
+            }
+            if (n == 0) continue;
+            split = true;
+            delete_face_edges(&faces[3 * i]);
+            for (int k = 0; k < n; k++) {
+                int32_t* dst;
+                if (k == 0) {
+                    dst = &faces[3 * i];   // the deleted face's slot
+                } else {
+                    faces.resize(faces.size() + 3);
+                    dst = &faces[faces.size() - 3];
+                }
+                dst[0] = out[k][0];
+                dst[1] = out[k][1];
+                dst[2] = out[k][2];
+                add_face_edges(dst);
+            }
+        }
+        if (pts.size() / 3 > (size_t)INT32_MAX / 2) return ACVD_ERR_UNSUPPORTED;
+    }
+    *out_xyz = (double*)std::malloc(pts.size() * sizeof(double));
+    *out_tri = (int32_t*)std::malloc(std::max<size_t>(faces.size(), 1) * sizeof(int32_t));
+    if (!*out_xyz || !*out_tri) {
+        std::free(*out_xyz);
+        std::free(*out_tri);
+        *out_xyz = nullptr;
+        *out_tri = nullptr;
+        return ACVD_ERR_ARG;
+    }
+    std::memcpy(*out_xyz, pts.data(), pts.size() * sizeof(double));
+    std::memcpy(*out_tri, faces.data(), faces.size() * sizeof(int32_t));
+    *out_nv = (int64_t)pts.size() / 3;
+    *out_nf = (int64_t)faces.size() / 3;
     return ACVD_OK;
 }
 

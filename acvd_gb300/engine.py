@@ -79,6 +79,10 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         "acvd_initial_sampling": (ctypes.c_int, [_i64, _P, _P, _P, ctypes.c_int32, _P]),
         "acvd_initial_sampling_fixed": (ctypes.c_int, [_i64, _P, _P, _P, ctypes.c_int32, ctypes.c_int32, _P, _P]),
         "acvd_set_fixed_clusters": (ctypes.c_int, [_P, ctypes.c_int32, _P]),
+        "acvd_split_long_edges": (ctypes.c_int, [_i64, _P, _i64, _P, ctypes.c_double,
+                                                 ctypes.POINTER(ctypes.POINTER(ctypes.c_double)),
+                                                 ctypes.POINTER(_i64), ctypes.POINTER(ctypes.POINTER(ctypes.c_int32)),
+                                                 ctypes.POINTER(_i64)]),
         "acvd_set_anchor_items": (ctypes.c_int, [_P, ctypes.c_int32, _P]),
         "acvd_clean_clustering": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int32)]),
         "acvd_set_mesh": (ctypes.c_int, [_P, _i64, _P, _i64, _P, _P, _P, _i64, _P]),
@@ -198,6 +202,27 @@ def vertex_weights(metric: str, points: np.ndarray, faces: np.ndarray, indicator
     _check(lib.acvd_vertex_weights(METRICS[metric], pts.shape[0], _ptr(pts), tri.shape[0], _ptr(tri), None, None,
                                    None, _ptr(ind), float(gradation), _ptr(w)), what="acvd_vertex_weights")
     return w
+
+
+def split_long_edges(points: np.ndarray, faces: np.ndarray, ratio: float):
+    """vtkSurface::SplitLongEdges: (points, faces) with every edge at most ratio x the
+    input's mean edge length; vertices keep their ids, new ones are appended."""
+    lib = load()
+    pts = np.ascontiguousarray(points, dtype=np.float64)
+    tri = np.ascontiguousarray(faces, dtype=np.int32)
+    xp = ctypes.POINTER(ctypes.c_double)()
+    tp = ctypes.POINTER(ctypes.c_int32)()
+    nv, nf = _i64(0), _i64(0)
+    _check(lib.acvd_split_long_edges(pts.shape[0], _ptr(pts), tri.shape[0], _ptr(tri), float(ratio), ctypes.byref(xp),
+                                     ctypes.byref(nv), ctypes.byref(tp), ctypes.byref(nf)),
+           what="acvd_split_long_edges")
+    try:
+        out_p = np.ctypeslib.as_array(xp, shape=(nv.value * 3,)).reshape(-1, 3).copy()
+        out_t = np.ctypeslib.as_array(tp, shape=(max(nf.value, 1) * 3,))[: nf.value * 3].reshape(-1, 3).copy()
+    finally:
+        lib.acvd_free(ctypes.cast(xp, ctypes.c_void_p))
+        lib.acvd_free(ctypes.cast(tp, ctypes.c_void_p))
+    return out_p, out_t
 
 
 def initial_sampling(row: np.ndarray, col: np.ndarray, weights: np.ndarray, k: int,

@@ -129,6 +129,18 @@ int acvd_initial_sampling_fixed(int64_t n_vertices, const int32_t* csr_row, cons
                                 int32_t* labels);
 
 /*
+ * vtkSurface::SplitLongEdges (Common/vtkSurface.cxx:444-603), host only: edges longer
+ * than ratio x the mean edge length are split at their midpoints (stored as floats),
+ * pass after pass until none is longer.  Vertices keep their ids, new ones are
+ * appended in the reference's order, faces keep the reference's slots (a split face's
+ * first part in its slot, the others appended); faces must be consistently oriented.
+ * *out_xyz (3 out_nv doubles) and *out_tri (3 out_nf int32) are allocated with malloc;
+ * release them with acvd_free.
+ */
+int acvd_split_long_edges(int64_t n_vertices, const double* xyz, int64_t n_faces, const int32_t* tri, double ratio,
+                          double** out_xyz, int64_t* out_nv, int32_t** out_tri, int64_t* out_nf);
+
+/*
  * Mesh upload (SetInput, vtkSurfaceClustering.h:179-211): coordinates, triangles
  * and the ring CSR / edge list from acvd_build_topology (or the caller's own
  * vtkSurface, exported in the same order).

@@ -46,6 +46,7 @@ def test_acvdq_program_with_subdivision_and_options(tmp_path):
     ("acvd", ["300", "0.5", "-q", "2"]),
     ("acvdq", ["200", "0", "-m", "1", "-b", "1", "-q", "2"]),
     ("anisotropic_remeshing_q", ["300", "0.5", "-b", "1", "-q", "2", "-m", "1"]),
+    ("acvd", ["300", "0.5", "-l", "0.9", "-q", "1"]),
 ])
 def test_native_programs_match_the_python_drivers(tmp_path, prog, args):
     """The native programs (C++ over the C ABI) and the Python drivers run the same steps:

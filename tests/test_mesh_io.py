@@ -128,7 +128,7 @@ def test_errors(tmp_path):
 def test_cli_rejects_unbuilt_options():
     from acvd_gb300 import cli
     with pytest.raises(SystemExit):
-        cli.main_acvd(["x.ply", "100", "0", "-l", "2"])
+        cli.main_acvd(["x.ply", "100", "0", "-w", "1"])
     with pytest.raises(SystemExit):
         cli.main_acvdq(["x.ply", "100", "0", "-d", "1"])
     with pytest.raises(SystemExit):
@@ -183,3 +183,63 @@ def test_checkpoint_files_round_trip(tmp_path):
     np.testing.assert_array_equal(r2.InitialClustering, lab)
     np.testing.assert_array_equal(r2.LoadCurvature(str(tmp_path / "curvature.dat")), ind)
     np.testing.assert_array_equal(r2.Indicator, ind)
+
+
+def test_split_long_edges_follows_the_reference_order():
+    """vtkSurface::SplitLongEdges worked by hand on one triangle (edges 4, sqrt(17), 1;
+    threshold = their mean): edges 0 and 1 get midpoints 3 and 4 in edge order, and the
+    face splits by the reference's Split3(f, v2, v3, v1, v23, v12) case, its first part in
+    the face's slot."""
+    pts = np.array([[0, 0, 0], [4, 0, 0], [0, 1, 0]], dtype=np.float64)
+    p, t = E.split_long_edges(pts, np.array([[0, 1, 2]], dtype=np.int32), 1.0)
+    np.testing.assert_array_equal(p, [[0, 0, 0], [4, 0, 0], [0, 1, 0], [2, 0, 0], [2, 0.5, 0]])
+    np.testing.assert_array_equal(t, [[1, 4, 3], [4, 2, 0], [0, 3, 4]])
+
+
+def _edges(tri):
+    e = np.sort(np.concatenate([tri[:, [0, 1]], tri[:, [1, 2]], tri[:, [2, 0]]]), axis=1)
+    u, cnt = np.unique(e, axis=0, return_counts=True)
+    return u, cnt
+
+
+def _area(p, t):
+    return 0.5 * np.linalg.norm(np.cross(p[t[:, 1]] - p[t[:, 0]], p[t[:, 2]] - p[t[:, 0]]), axis=1).sum()
+
+
+@pytest.mark.parametrize("ratio", [0.6, 1.0, 1.5])
+def test_split_long_edges_properties(ratio):
+    m = synth.torus(20, 6, seed=3)              # long edges around the tube's length
+    pts = m.points.astype(np.float32).astype(np.float64)
+    e0, _ = _edges(m.faces)
+    mean = np.linalg.norm(pts[e0[:, 0]] - pts[e0[:, 1]], axis=1).mean()
+    p, t = E.split_long_edges(pts, m.faces, ratio)
+    np.testing.assert_array_equal(p[: pts.shape[0]], pts)          # vertices keep their ids
+    np.testing.assert_array_equal(p, p.astype(np.float32))         # midpoints stored as floats
+    e, cnt = _edges(t)
+    assert np.all(cnt == 2)                                        # still closed and manifold
+    assert np.linalg.norm(p[e[:, 0]] - p[e[:, 1]], axis=1).max() <= ratio * mean
+    assert p.shape[0] - t.shape[0] // 2 == pts.shape[0] - m.faces.shape[0] // 2   # Euler: V - F/2 kept
+    assert abs(_area(p, t) - _area(pts, m.faces)) < 1e-5 * _area(pts, m.faces)
+    if ratio < 1.5:
+        assert p.shape[0] > pts.shape[0]
+    elif np.linalg.norm(pts[e0[:, 0]] - pts[e0[:, 1]], axis=1).max() <= ratio * mean:
+        np.testing.assert_array_equal(t, m.faces)                  # nothing to split: unchanged
+    # orientation kept: every interior edge is used once in each direction
+    d = np.concatenate([t[:, [0, 1]], t[:, [1, 2]], t[:, [2, 0]]])
+    assert len({tuple(x) for x in d.tolist()}) == d.shape[0]
+
+
+def test_split_long_edges_option_order(tmp_path):
+    """-l before -ft: the face ids refer to the split mesh (the reference's argument loop)."""
+    from acvd_gb300 import cli
+    pts = np.array([[0, 0, 0], [4, 0, 0], [0, 1, 0]], dtype=np.float64)
+    mesh = acvd_gb300.Surface(pts, np.array([[0, 1, 2]], dtype=np.int32))
+    (tmp_path / "f.txt").write_text("2\n")
+    opts = cli._parse(["m.ply", "3", "0", "-l", "1", "-ft", str(tmp_path / "f.txt")], "ACVDQ")
+    out, fixed = cli._mesh_options(opts, mesh, True)
+    assert out.GetNumberOfPoints() == 5
+    np.testing.assert_array_equal(fixed, [0, 3, 4])               # face 2 of the split mesh: (0, 3, 4)
+    opts = cli._parse(["m.ply", "3", "0", "-ft", str(tmp_path / "f.txt"), "-l", "1"], "ACVDQ")
+    with pytest.raises(IndexError):                                # face 2 does not exist before the split
+        cli._mesh_options(opts, mesh, True)
+
