@@ -18,13 +18,15 @@ Options are "-key value" pairs as in the reference:
     -np n     threads of the reference's threaded engine (accepted, unused)
     -l ratio  split the edges longer than ratio x the mean edge length first
               (vtkSurface::SplitLongEdges)
+    -cd file  ACVD, ACVDQ: MetaImage volume whose values replace the curvature indicator
+    -cmax v, -cmin v, -cf v
+              its mapping max(cmax - value * cf, cmin) (defaults 1, 0.1, 0.001)
     -fv file  ACVDQ: vertex ids (whitespace separated) that stay output vertices
     -ft file  ACVDQ: face ids whose three vertices stay output vertices
 
 -l, -fv and -ft act on the mesh in the order given, as the reference's argument loop
 does.  Options of the reference that need parts this package does not build -- -w
-(energy log), -cd/-cmin/-cmax/-cf (custom density image), -p (pooling) -- stop with an
-error rather than being ignored.  Other keys are ignored, as the reference programs
+(energy log), -p (pooling) -- stop with an error rather than being ignored.  Other keys are ignored, as the reference programs
 ignore them.
 
 Outputs follow the reference: ACVD writes <dir>smooth_<name> before the post-placement
@@ -46,10 +48,6 @@ from .remesh import (AnisotropicDiscreteRemeshing, IsotropicDiscreteRemeshing, Q
 _UNBUILT = {
     "-w": "the global energy log (which the reference's ACVD / ACVDQ write through an uninitialised "
           "timer, vtkUniformClustering.h:1384-1395)",
-    "-cd": "custom density images",
-    "-cmin": "custom density images",
-    "-cmax": "custom density images",
-    "-cf": "custom density images",
     "-p": "pooling (the threaded engine)",
 }
 
@@ -100,7 +98,7 @@ def _mesh_options(opts, mesh: Surface, fixed_vertices: bool):
     return mesh, fixed
 
 
-def _remesh(opts, cls, console: int, manifold: bool = True, fixed_vertices: bool = False):
+def _remesh(opts, cls, console: int, manifold: bool = True, fixed_vertices: bool = False, density: bool = True):
     mesh = Surface.CreateFromFile(opts["file"])
     mesh.DisplayMeshProperties()
     mesh, fixed = _mesh_options(opts, mesh, fixed_vertices)
@@ -113,6 +111,15 @@ def _remesh(opts, cls, console: int, manifold: bool = True, fixed_vertices: bool
     r.SetConsoleOutput(console)
     r.SetSubsamplingThreshold(int(opts.get("-s", 10)))
     r.GetMetric().SetGradation(opts["gradation"])
+    if density:
+        if "-cd" in opts:
+            r.SetInputDensityFile(opts["-cd"])
+        if "-cmax" in opts:
+            r.SetMaxCustomDensity(float(opts["-cmax"]))
+        if "-cmin" in opts:
+            r.SetMinCustomDensity(float(opts["-cmin"]))
+        if "-cf" in opts:
+            r.SetCustomDensityMultiplicationFactor(float(opts["-cf"]))
     return r
 
 
@@ -198,7 +205,7 @@ def main_anisotropic_remeshing_q(argv: list[str] | None = None) -> int:
     <dir>Remeshing.ply."""
     argv = sys.argv[1:] if argv is None else argv
     opts = _parse(argv, "AnisotropicRemeshingQ")
-    r = _remesh(opts, AnisotropicDiscreteRemeshing, 2, manifold=False)
+    r = _remesh(opts, AnisotropicDiscreteRemeshing, 2, manifold=False, density=False)
     if "-q" in opts:
         r.GetMetric().SetQuadricsOptimizationLevel(int(opts["-q"]))
     r.Remesh()

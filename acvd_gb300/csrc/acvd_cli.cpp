@@ -115,6 +115,9 @@ int main(int argc, char** argv) {
 #endif
     std::string outdir, outfile = "simplification.ply";
     bool have_outdir = false;
+    // custom density (vtkDiscreteRemeshing.h:603-640, defaults :1203-1206)
+    std::string density_file;
+    double density_max = 1.0, density_min = 0.1, density_factor = 0.001;
     // -l, -fv, -ft act on the mesh in the order given (the reference's argument loop)
     std::vector<std::pair<std::string, std::string>> mesh_ops;
     for (int a = 4; a < argc; a += 2) {
@@ -132,12 +135,18 @@ int main(int argc, char** argv) {
         else if (key == "-np") {}
         else if (key == "-d") {
             if (std::atoi(value) != 0) die("display needs a graphics stack; only -d 0 is available");
-        } else if (key == "-w" || key == "-cd" || key == "-cmin" || key == "-cmax" || key == "-cf" || key == "-p") {
+        } else if (key == "-w" || key == "-p") {
             die("option " + key + " needs a part this build does not have");
         } else if (key == "-l") {
             if (!(std::atof(value) > 0.0)) die("-l needs a positive ratio");
             mesh_ops.emplace_back(key, value);
         }
+#ifndef ACVD_CLI_ANISO
+        else if (key == "-cd") density_file = value;
+        else if (key == "-cmax") density_max = std::atof(value);
+        else if (key == "-cmin") density_min = std::atof(value);
+        else if (key == "-cf") density_factor = std::atof(value);
+#endif
 #ifdef ACVD_CLI_QEM
         else if (key == "-fv" || key == "-ft") {
             mesh_ops.emplace_back(key, value);
@@ -220,7 +229,12 @@ int main(int argc, char** argv) {
         original_on_device = true;
         ind.resize(m.nv());
         if (need_pd) pd.resize(6 * (size_t)m.nv());
-        check(ctx, acvd_compute_curvature(ctx, ind.data(), need_pd ? pd.data() : nullptr), "acvd_compute_curvature");
+        if (!density_file.empty() && !need_pd)
+            check(nullptr, acvd_density_indicator(density_file.c_str(), m.nv(), m.xyz.data(), density_max, density_min,
+                                                  density_factor, ind.data()),
+                  "the custom density");
+        else
+            check(ctx, acvd_compute_curvature(ctx, ind.data(), need_pd ? pd.data() : nullptr), "acvd_compute_curvature");
     }
     // CheckSubsamplingRatio: subdivide while the mesh has fewer than threshold x K vertices
     int levels = 0;

@@ -1060,6 +1060,132 @@ int read_vtp(const std::string& s, MeshData& m) {
     return check_faces(m);
 }
 
+// ---------------------------------------------------------------- MetaImage density
+// The custom density of vtkDiscreteRemeshing::SamplingPreProcessing
+// (DiscreteRemeshing/vtkDiscreteRemeshing.h:603-640): a scalar volume read from a
+// MetaImage file (.mhd header with its data file, or .mha with the data inline; raw or
+// zlib-compressed), sampled at each vertex in the voxel whose cell holds it
+// (vtkImageData::ComputeStructuredCoordinates: i = floor((x - origin) / spacing), the last
+// cell at the upper face; outside the volume the value is 0), and mapped to
+// max(max_density - value * factor, min_density).  Written from MetaIO's published header
+// keys: NDims, DimSize, ElementSpacing, Offset / Origin / Position, ElementType,
+// ElementNumberOfChannels, ElementByteOrderMSB / BinaryDataByteOrderMSB,
+// CompressedData, HeaderSize and ElementDataFile (LOCAL or a file name).
+int read_metaimage(const std::string& path, std::vector<int64_t>& dim, std::vector<double>& origin,
+                   std::vector<double>& spacing, std::vector<double>& values) {
+    std::string buf;
+    if (!read_all(path.c_str(), buf)) return io_fail(ACVD_ERR_ARG, "cannot read " + path);
+    std::map<std::string, std::string> kv;
+    size_t pos = 0, data_at = std::string::npos;
+    while (pos < buf.size()) {
+        const size_t eol = buf.find('\n', pos);
+        const size_t end = eol == std::string::npos ? buf.size() : eol;
+        std::string line = buf.substr(pos, end - pos);
+        pos = end + 1;
+        const size_t eq = line.find('=');
+        if (eq == std::string::npos) continue;
+        auto trim = [](std::string s) {
+            const size_t a = s.find_first_not_of(" \t\r"), b = s.find_last_not_of(" \t\r");
+            return a == std::string::npos ? std::string() : s.substr(a, b - a + 1);
+        };
+        const std::string key = trim(line.substr(0, eq)), val = trim(line.substr(eq + 1));
+        kv[key] = val;
+        if (key == "ElementDataFile") {
+            data_at = pos;
+            break;
+        }
+    }
+    if (data_at == std::string::npos) return io_fail(ACVD_ERR_ARG, "MetaImage: no ElementDataFile in " + path);
+    auto get = [&](const char* k) { auto it = kv.find(k); return it == kv.end() ? std::string() : it->second; };
+    auto numbers = [](const std::string& s) {
+        std::vector<double> v;
+        std::istringstream in(s);
+        double x;
+        while (in >> x) v.push_back(x);
+        return v;
+    };
+    const int nd = std::atoi(get("NDims").c_str());
+    if (nd < 1 || nd > 3) return io_fail(ACVD_ERR_UNSUPPORTED, "MetaImage: NDims must be 1 to 3");
+    const std::vector<double> ds = numbers(get("DimSize"));
+    if ((int)ds.size() < nd) return io_fail(ACVD_ERR_ARG, "MetaImage: DimSize");
+    dim.assign(3, 1);
+    origin.assign(3, 0.0);
+    spacing.assign(3, 1.0);
+    for (int i = 0; i < nd; i++) {
+        if (!(ds[i] >= 1)) return io_fail(ACVD_ERR_ARG, "MetaImage: DimSize");
+        dim[i] = (int64_t)ds[i];
+    }
+    std::vector<double> sp = numbers(get("ElementSpacing"));
+    if (sp.empty()) sp = numbers(get("ElementSize"));
+    for (int i = 0; i < nd && i < (int)sp.size(); i++) spacing[i] = sp[i];
+    std::vector<double> org = numbers(get("Offset"));
+    if (org.empty()) org = numbers(get("Origin"));
+    if (org.empty()) org = numbers(get("Position"));
+    for (int i = 0; i < nd && i < (int)org.size(); i++) origin[i] = org[i];
+    const std::string et = get("ElementType");
+    int size = 0;
+    bool is_float = false, is_signed = true;
+    if (et == "MET_CHAR") size = 1;
+    else if (et == "MET_UCHAR") { size = 1; is_signed = false; }
+    else if (et == "MET_SHORT") size = 2;
+    else if (et == "MET_USHORT") { size = 2; is_signed = false; }
+    else if (et == "MET_INT" || et == "MET_LONG") size = 4;
+    else if (et == "MET_UINT" || et == "MET_ULONG") { size = 4; is_signed = false; }
+    else if (et == "MET_LONG_LONG") size = 8;
+    else if (et == "MET_ULONG_LONG") { size = 8; is_signed = false; }
+    else if (et == "MET_FLOAT") { size = 4; is_float = true; }
+    else if (et == "MET_DOUBLE") { size = 8; is_float = true; }
+    else return io_fail(ACVD_ERR_UNSUPPORTED, "MetaImage: ElementType " + et);
+    const int channels = std::max(1, std::atoi(get("ElementNumberOfChannels").c_str()));
+    std::string msb = get("ElementByteOrderMSB");
+    if (msb.empty()) msb = get("BinaryDataByteOrderMSB");
+    const bool little = !(msb == "True" || msb == "true" || msb == "1");
+    const std::string cd = get("CompressedData");
+    const bool compressed = cd == "True" || cd == "true" || cd == "1";
+    const size_t count = (size_t)(dim[0] * dim[1] * dim[2]);
+    const size_t nbytes = count * (size_t)channels * (size_t)size;
+    std::string file = get("ElementDataFile"), data;
+    const char* p = nullptr;
+    size_t avail = 0;
+    if (file == "LOCAL") {
+        p = buf.data() + data_at;
+        avail = buf.size() - data_at;
+    } else {
+        if (file.find("%") != std::string::npos || file == "LIST")
+            return io_fail(ACVD_ERR_UNSUPPORTED, "MetaImage: lists of data files are not read");
+        const size_t slash = path.find_last_of('/');
+        if (file[0] != '/' && slash != std::string::npos) file = path.substr(0, slash + 1) + file;
+        if (!read_all(file.c_str(), data)) return io_fail(ACVD_ERR_ARG, "cannot read " + file);
+        const long long hs = std::atoll(get("HeaderSize").c_str());
+        size_t skip = 0;
+        if (hs > 0) skip = (size_t)hs;
+        else if (hs == -1 && !compressed && data.size() >= nbytes) skip = data.size() - nbytes;   // data at the end
+        if (skip > data.size()) return io_fail(ACVD_ERR_ARG, "MetaImage: HeaderSize past the data");
+        p = data.data() + skip;
+        avail = data.size() - skip;
+    }
+    std::string raw;
+    if (compressed) {
+        if (!zlib_inflate((const unsigned char*)p, avail, nbytes, raw))
+            return io_fail(ACVD_ERR_ARG, "MetaImage: corrupt compressed data");
+    } else {
+        if (avail < nbytes) return io_fail(ACVD_ERR_ARG, "MetaImage: data shorter than DimSize says");
+        raw.assign(p, nbytes);
+    }
+    values.resize(count);
+    const unsigned char* q = (const unsigned char*)raw.data();
+    for (size_t i = 0; i < count; i++, q += (size_t)channels * size) {   // first component
+        double v;
+        if (is_float) v = size == 4 ? (double)load_scalar<float>(q, little) : load_scalar<double>(q, little);
+        else if (size == 1) v = is_signed ? (double)(int8_t)q[0] : (double)q[0];
+        else if (size == 2) v = is_signed ? (double)load_scalar<int16_t>(q, little) : (double)load_scalar<uint16_t>(q, little);
+        else if (size == 4) v = is_signed ? (double)load_scalar<int32_t>(q, little) : (double)load_scalar<uint32_t>(q, little);
+        else v = is_signed ? (double)load_scalar<int64_t>(q, little) : (double)load_scalar<uint64_t>(q, little);
+        values[i] = v;
+    }
+    return ACVD_OK;
+}
+
 // ---------------------------------------------------------------- writers
 void fmt_double(std::string& out, double v) {
     char b[40];
@@ -1220,6 +1346,41 @@ int acvd_read_mesh(const char* path, double** xyz, int64_t* n_vertices, int32_t*
     std::memcpy(*tri, m.tri.data(), m.tri.size() * sizeof(int32_t));
     *n_vertices = (int64_t)m.xyz.size() / 3;
     *n_faces = (int64_t)m.tri.size() / 3;
+    return ACVD_OK;
+}
+
+int acvd_density_indicator(const char* image_path, int64_t n_vertices, const double* xyz, double max_density,
+                           double min_density, double factor, double* indicator) {
+    if (!image_path || n_vertices < 0 || (n_vertices && (!xyz || !indicator)))
+        return io_fail(ACVD_ERR_ARG, "null or negative argument");
+    const std::string name = lower(image_path);
+    if (name.find(".mnc") != std::string::npos)
+        return io_fail(ACVD_ERR_UNSUPPORTED, "MINC density images are not read (MetaImage only)");
+    std::vector<int64_t> dim;
+    std::vector<double> origin, spacing, values;
+    if (int rc = read_metaimage(image_path, dim, origin, spacing, values)) return rc;
+    for (int64_t i = 0; i < n_vertices; i++) {
+        int64_t ijk[3];
+        bool inside = true;
+        for (int c = 0; c < 3; c++) {
+            const double d = (xyz[3 * i + c] - origin[c]) / spacing[c];
+            if (dim[c] == 1) {
+                ijk[c] = 0;
+                inside = inside && d == 0.0;
+                continue;
+            }
+            if (!(d >= 0.0 && d <= (double)(dim[c] - 1))) {
+                inside = false;
+                ijk[c] = 0;
+                continue;
+            }
+            ijk[c] = std::min((int64_t)std::floor(d), dim[c] - 2);   // the last cell at the upper face
+        }
+        const double v = inside ? values[(size_t)((ijk[2] * dim[1] + ijk[1]) * dim[0] + ijk[0])] : 0.0;
+        double ind = max_density - v * factor;
+        if (ind < min_density) ind = min_density;
+        indicator[i] = ind;
+    }
     return ACVD_OK;
 }
 

@@ -79,6 +79,8 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         "acvd_initial_sampling": (ctypes.c_int, [_i64, _P, _P, _P, ctypes.c_int32, _P]),
         "acvd_initial_sampling_fixed": (ctypes.c_int, [_i64, _P, _P, _P, ctypes.c_int32, ctypes.c_int32, _P, _P]),
         "acvd_set_fixed_clusters": (ctypes.c_int, [_P, ctypes.c_int32, _P]),
+        "acvd_density_indicator": (ctypes.c_int, [ctypes.c_char_p, _i64, _P, ctypes.c_double, ctypes.c_double,
+                                                  ctypes.c_double, _P]),
         "acvd_split_long_edges": (ctypes.c_int, [_i64, _P, _i64, _P, ctypes.c_double,
                                                  ctypes.POINTER(ctypes.POINTER(ctypes.c_double)),
                                                  ctypes.POINTER(_i64), ctypes.POINTER(ctypes.POINTER(ctypes.c_int32)),
@@ -202,6 +204,20 @@ def vertex_weights(metric: str, points: np.ndarray, faces: np.ndarray, indicator
     _check(lib.acvd_vertex_weights(METRICS[metric], pts.shape[0], _ptr(pts), tri.shape[0], _ptr(tri), None, None,
                                    None, _ptr(ind), float(gradation), _ptr(w)), what="acvd_vertex_weights")
     return w
+
+
+def density_indicator(image_path: str, points: np.ndarray, max_density: float = 1.0, min_density: float = 0.1,
+                      factor: float = 0.001) -> np.ndarray:
+    """The custom-density indicator of a MetaImage volume at the points
+    (vtkDiscreteRemeshing's InputDensityFile): max(max - value * factor, min)."""
+    lib = load()
+    pts = np.ascontiguousarray(points, dtype=np.float64)
+    out = np.empty(pts.shape[0], dtype=np.float64)
+    code = lib.acvd_density_indicator(os.fsencode(image_path), pts.shape[0], _ptr(pts), float(max_density),
+                                      float(min_density), float(factor), _ptr(out))
+    if code != ACVD_OK:
+        raise AcvdError(code, (lib.acvd_io_last_error() or b"").decode())
+    return out
 
 
 def split_long_edges(points: np.ndarray, faces: np.ndarray, ratio: float):

@@ -124,6 +124,11 @@ class _DiscreteRemeshing:
         self._engine = None
         self._constrained_request = None
         self.FixedClusters = None         # SetFixedClusters (vtkUniformClustering.h:134)
+        # custom density (vtkDiscreteRemeshing.h:80-83, defaults :1203-1206)
+        self.InputDensityFile = None
+        self.MaxCustomDensity = 1.0
+        self.MinCustomDensity = 0.1
+        self.CustomDensityMultiplicationFactor = 0.001
         self._anchors = {}                # QEM Cluster::AnchorItem, by cluster
 
     @classmethod
@@ -171,6 +176,21 @@ class _DiscreteRemeshing:
     def SetBoundaryFixing(self, on: int):
         """Close the coarse mesh along the input's boundary (FixMeshBoundaries)."""
         self.BoundaryFixing = int(on)
+
+    def SetInputDensityFile(self, path):
+        """A MetaImage volume whose values replace the curvature indicator: at each vertex
+        max(MaxCustomDensity - value * CustomDensityMultiplicationFactor, MinCustomDensity)
+        (vtkDiscreteRemeshing.h:603-640)."""
+        self.InputDensityFile = path
+
+    def SetMaxCustomDensity(self, v: float):
+        self.MaxCustomDensity = float(v)
+
+    def SetMinCustomDensity(self, v: float):
+        self.MinCustomDensity = float(v)
+
+    def SetCustomDensityMultiplicationFactor(self, v: float):
+        self.CustomDensityMultiplicationFactor = float(v)
 
     def SetFixedClusters(self, vertex_ids):
         """Cluster c < len(vertex_ids) is the cluster of vertex vertex_ids[c]: the initial
@@ -248,6 +268,11 @@ class _DiscreteRemeshing:
         # SetCurvatureInfo gave it
         need_pd = self._metric_name == "aniso"
         on_device = None
+        if self._needs_indicator() and self.Indicator is None and self.InputDensityFile and not need_pd:
+            # the custom density replaces the curvature (vtkDiscreteRemeshing.h:603-640)
+            src = self.OriginalInput if self.OriginalInput is not None else self.Input
+            self.Indicator = _eng.density_indicator(self.InputDensityFile, src.points, self.MaxCustomDensity,
+                                                    self.MinCustomDensity, self.CustomDensityMultiplicationFactor)
         if (self._needs_indicator() and self.Indicator is None) or (need_pd and self.PrincipalDirections is None):
             src = self.OriginalInput if self.OriginalInput is not None else self.Input
             row, col, ev = src.topology()

@@ -434,6 +434,18 @@ int acvd_check_wait_limit(acvd_ctx* ctx, int64_t max_spins, int32_t* gave_up);
  * and reports through its error macros).
  */
 int acvd_read_mesh(const char* path, double** xyz, int64_t* n_vertices, int32_t** tri, int64_t* n_faces);
+
+/*
+ * Custom density (vtkDiscreteRemeshing::SamplingPreProcessing with an InputDensityFile,
+ * DiscreteRemeshing/vtkDiscreteRemeshing.h:603-640; the drivers' -cd / -cmax / -cmin /
+ * -cf, defaults 1, 0.1, 0.001): the curvature indicator replaced, at each vertex, by
+ * max(max_density - value * factor, min_density), value being the volume's voxel at the
+ * cell holding the vertex (floor((x - origin) / spacing), the last cell at the upper
+ * face; 0 outside the volume).  Host only.  The volume is a MetaImage file (.mhd with its
+ * data file, or .mha; raw or zlib-compressed); MINC (.mnc) is ACVD_ERR_UNSUPPORTED.
+ */
+int acvd_density_indicator(const char* image_path, int64_t n_vertices, const double* xyz, double max_density,
+                           double min_density, double factor, double* indicator);
 int acvd_write_mesh(const char* path, const double* xyz, int64_t n_vertices, const int32_t* tri, int64_t n_faces);
 void acvd_free(void* p);
 const char* acvd_io_last_error(void);

@@ -47,6 +47,7 @@ def test_acvdq_program_with_subdivision_and_options(tmp_path):
     ("acvdq", ["200", "0", "-m", "1", "-b", "1", "-q", "2"]),
     ("anisotropic_remeshing_q", ["300", "0.5", "-b", "1", "-q", "2", "-m", "1"]),
     ("acvd", ["300", "0.5", "-l", "0.9", "-q", "1"]),
+    ("acvdq", ["200", "1.5", "-cd", "DENSITY", "-cmax", "2", "-cmin", "0.2", "-cf", "0.01"]),
 ])
 def test_native_programs_match_the_python_drivers(tmp_path, prog, args):
     """The native programs (C++ over the C ABI) and the Python drivers run the same steps:
@@ -57,6 +58,16 @@ def test_native_programs_match_the_python_drivers(tmp_path, prog, args):
             "anisotropic_remeshing_q": lambda: synth.heightfield(64, seed=4)}[prog]()
     src = str(tmp_path / "in.ply")
     E.write_mesh(src, mesh.points, mesh.faces)
+    if "DENSITY" in args:   # a volume over the mesh's bounding box
+        vol = np.arange(8 * 8 * 8, dtype=np.float32) % 97
+        lo = mesh.points.min(axis=0) - 0.01
+        sp = (mesh.points.max(axis=0) + 0.01 - lo) / 7
+        (tmp_path / "d.raw").write_bytes(vol.tobytes())
+        (tmp_path / "d.mhd").write_text("ObjectType = Image\nNDims = 3\nDimSize = 8 8 8\n"
+                                        f"ElementSpacing = {sp[0]!r} {sp[1]!r} {sp[2]!r}\n"
+                                        f"Offset = {lo[0]!r} {lo[1]!r} {lo[2]!r}\n"
+                                        "ElementType = MET_FLOAT\nElementDataFile = d.raw\n")
+        args = [str(tmp_path / "d.mhd") if a == "DENSITY" else a for a in args]
     native, python = tmp_path / "native", tmp_path / "python"
     native.mkdir()
     python.mkdir()

@@ -180,3 +180,36 @@ def test_fixed_argument_errors():
     with pytest.raises(acvd_gb300.AcvdError):
         e.set_fixed_clusters(np.arange(5, dtype=np.int32))       # more fixed vertices than clusters
     e.close()
+
+
+@pytest.mark.parametrize("schedule", ["host_loop", "persistent"])
+def test_fixed_vertices_same_under_every_schedule(oracle_lib, schedule, monkeypatch):
+    """The anchored clusters run through the same device functions whatever drives the
+    sweeps: the device-side loop (default), the host loop and the persistent kernel give
+    bitwise the same clustering and energy."""
+    m = synth.torus(96, 48, seed=2)
+    k, nfix = 316, 16
+    fixed = _fixed_ids(m.n_points, nfix, 300)
+    row, col, ev = acvd_gb300.build_topology(m.n_points, m.faces)
+    w = acvd_gb300.vertex_weights("qem", m.points, m.faces, m.indicator, 1.5)
+    lab0 = acvd_gb300.initial_sampling(row, col, w, k, fixed=fixed)
+    out = []
+    for variant in ("default", schedule):
+        if variant == "host_loop":
+            monkeypatch.setenv("ACVD_HOST_LOOP", "1")
+        else:
+            monkeypatch.delenv("ACVD_HOST_LOOP", raising=False)
+        e = acvd_gb300.Engine(persistent=(variant == "persistent"))
+        e.set_mesh(m.points, m.faces, row, col, ev)
+        e.set_metric("qem", m.indicator, None, 1.5)
+        e.set_unconstrained_initialization(1)
+        e.set_labels(k, lab0)
+        e.set_fixed_clusters(fixed)
+        e.set_anchor_items(fixed)
+        st = e.minimize()
+        out.append((e.labels(), st))
+        e.close()
+    (lab_a, st_a), (lab_b, st_b) = out
+    np.testing.assert_array_equal(lab_a, lab_b)
+    np.testing.assert_array_equal(lab_a[fixed], np.arange(nfix))
+    assert st_a["energy"] == st_b["energy"] and st_a["sweeps"] == st_b["sweeps"]

@@ -162,8 +162,8 @@ def test_native_programs_parse_like_the_reference():
         assert os.access(exe, os.X_OK)
         r = subprocess.run([exe], capture_output=True, text=True)
         assert r.returncode == 0 and "Usage" in r.stdout
-        r = subprocess.run([exe, "missing.ply", "100", "0", "-cd", "density.mhd"], capture_output=True, text=True)
-        assert r.returncode == 1 and "-cd" in r.stderr
+        r = subprocess.run([exe, "missing.ply", "100", "0", "-w", "1"], capture_output=True, text=True)
+        assert r.returncode == 1 and "-w" in r.stderr
 
 
 def test_checkpoint_files_round_trip(tmp_path):
@@ -242,4 +242,44 @@ def test_split_long_edges_option_order(tmp_path):
     opts = cli._parse(["m.ply", "3", "0", "-ft", str(tmp_path / "f.txt"), "-l", "1"], "ACVDQ")
     with pytest.raises(IndexError):                                # face 2 does not exist before the split
         cli._mesh_options(opts, mesh, True)
+
+
+def _density_volume(tmp_path, kind):
+    """A 7 x 5 x 4 float volume, origin (-1.5, -1, -0.8), spacing (0.5, 0.5, 0.6)."""
+    import zlib
+    dims = (7, 5, 4)
+    vol = np.arange(np.prod(dims), dtype=np.float32).reshape(dims[::-1]) * 10.0   # z, y, x
+    head = ("ObjectType = Image\nNDims = 3\nDimSize = 7 5 4\nElementSpacing = 0.5 0.5 0.6\n"
+            "Offset = -1.5 -1 -0.8\nElementNumberOfChannels = 1\n")
+    if kind == "mhd_raw":
+        (tmp_path / "d.raw").write_bytes(vol.astype(">f4").tobytes())
+        (tmp_path / "d.mhd").write_text(head + "ElementType = MET_FLOAT\nElementByteOrderMSB = True\n"
+                                        "ElementDataFile = d.raw\n")
+        return str(tmp_path / "d.mhd"), vol
+    data = zlib.compress(vol.astype(np.uint16).tobytes())
+    (tmp_path / "d.mha").write_bytes((head + "ElementType = MET_USHORT\nCompressedData = True\n"
+                                      f"CompressedDataSize = {len(data)}\nElementDataFile = LOCAL\n").encode() + data)
+    return str(tmp_path / "d.mha"), vol.astype(np.uint16).astype(np.float64)
+
+
+@pytest.mark.parametrize("kind", ["mhd_raw", "mha_zlib"])
+def test_custom_density_indicator(tmp_path, kind):
+    """vtkDiscreteRemeshing's InputDensityFile: the voxel at the cell holding each vertex
+    (the last cell at the upper face, 0 outside), mapped to max(cmax - value * cf, cmin)."""
+    path, vol = _density_volume(tmp_path, kind)
+    origin, spacing, dims = np.array([-1.5, -1, -0.8]), np.array([0.5, 0.5, 0.6]), np.array([7, 5, 4])
+    rng = np.random.default_rng(0)
+    pts = rng.uniform(origin - 0.3, origin + spacing * (dims - 1) + 0.3, size=(400, 3))
+    pts[0] = origin + spacing * (dims - 1)          # the upper corner: last cell
+    pts[1] = origin                                  # the lower corner
+    got = E.density_indicator(path, pts, 60.0, 0.5, 0.25)
+    d = (pts - origin) / spacing
+    inside = np.all((d >= 0) & (d <= dims - 1), axis=1)
+    ijk = np.minimum(np.floor(d).astype(int), dims - 2)
+    val = np.where(inside, vol[ijk[:, 2].clip(0, 3), ijk[:, 1].clip(0, 4), ijk[:, 0].clip(0, 6)], 0.0)
+    want = np.maximum(60.0 - val * 0.25, 0.5)
+    np.testing.assert_array_equal(got, want)
+    assert inside.sum() > 100 and (~inside).sum() > 20
+    with pytest.raises(acvd_gb300.AcvdError):
+        E.density_indicator(str(tmp_path / "v.mnc"), pts)
 
