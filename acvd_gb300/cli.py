@@ -16,6 +16,7 @@ Options are "-key value" pairs as in the reference:
               ACVDQ, AnisotropicRemeshingQ: the metric's QuadricsOptimizationLevel (default 3)
     -d 0      display (only 0: there is no graphics stack)
     -np n     threads of the reference's threaded engine (accepted, unused)
+    -p n      its thread pooling ratio (accepted, unused)
     -l ratio  split the edges longer than ratio x the mean edge length first
               (vtkSurface::SplitLongEdges)
     -cd file  ACVD, ACVDQ: MetaImage volume whose values replace the curvature indicator
@@ -25,8 +26,8 @@ Options are "-key value" pairs as in the reference:
     -ft file  ACVDQ: face ids whose three vertices stay output vertices
 
 -l, -fv and -ft act on the mesh in the order given, as the reference's argument loop
-does.  Options of the reference that need parts this package does not build -- -w
-(energy log), -p (pooling) -- stop with an error rather than being ignored.  Other keys are ignored, as the reference programs
+does.  The option of the reference that needs a part this package does not build,
+-w (energy log), stops with an error rather than being ignored.  Other keys are ignored, as the reference programs
 ignore them.
 
 Outputs follow the reference: ACVD writes <dir>smooth_<name> before the post-placement
@@ -48,7 +49,6 @@ from .remesh import (AnisotropicDiscreteRemeshing, IsotropicDiscreteRemeshing, Q
 _UNBUILT = {
     "-w": "the global energy log (which the reference's ACVD / ACVDQ write through an uninitialised "
           "timer, vtkUniformClustering.h:1384-1395)",
-    "-p": "pooling (the threaded engine)",
 }
 
 

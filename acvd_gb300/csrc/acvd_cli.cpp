@@ -132,10 +132,10 @@ int main(int argc, char** argv) {
         else if (key == "-o") { outdir = value; have_outdir = true; }
         else if (key == "-of") outfile = value;
         else if (key == "-q") level = std::atoi(value);
-        else if (key == "-np") {}
+        else if (key == "-np" || key == "-p") {}   // the threaded CPU engine's threads / pooling
         else if (key == "-d") {
             if (std::atoi(value) != 0) die("display needs a graphics stack; only -d 0 is available");
-        } else if (key == "-w" || key == "-p") {
+        } else if (key == "-w") {
             die("option " + key + " needs a part this build does not have");
         } else if (key == "-l") {
             if (!(std::atof(value) > 0.0)) die("-l needs a positive ratio");
