@@ -1,0 +1,261 @@
+"""Schedule autotuner for the clustering engine.
+
+The engine can run the minimisation (the seam of vtkUniformClustering::MinimizeEnergy,
+Common/vtkUniformClustering.h:725-830) under several sweep schedules. Which one is fastest
+depends on the mesh size, the cluster count, the metric and the GPU. The tuner times
+converged solves of the caller's own problem under each candidate, keeps the fastest
+acceptable one, and caches the choice in a JSON file keyed by device, metric and size class.
+
+Two families of candidates:
+
+* exact schedules give the default schedule's clustering bit for bit, so a tuned run never
+  changes a result:
+    - ``graphs``: per-phase kernels, sweeps between convergence events looped on the device
+      inside one CUDA graph (the default);
+    - ``host_loop``: the same kernels, one graph launch per sweep decided on the host;
+    - ``persistent``: one cooperative kernel per phase with grid barriers.
+  A candidate of this family whose labels differ from the default's is rejected, since that
+  would mean a broken guarantee rather than a faster schedule.
+* approximate schedules (opt-in) reach a different deterministic clustering:
+    - ``exact_sweeps``: no relaxed multi-move sweeps, claim-based sweeps only;
+    - ``match2``: two claim / commit rounds per colour step.
+  One of them is accepted only when every item is assigned and its energy is within
+  ``energy_rel_tol`` (default 1e-3, the 0.1 % bar against the reference's converged energy)
+  of the default schedule's energy on the same input.
+
+The schedules' switches are the engine's own (the ``persistent`` option of ``acvd_opts`` and the
+``ACVD_HOST_LOOP`` / ``ACVD_RELAXED`` / ``ACVD_MATCH_ROUNDS`` environment switches). The engine reads
+the last two when a context is created and ``ACVD_HOST_LOOP`` when it minimises, so
+``ScheduledEngine`` sets them only around those calls and puts the environment back afterwards.
+"""
+from __future__ import annotations
+
+import contextlib
+import dataclasses
+import hashlib
+import json
+import math
+import os
+import statistics
+import tempfile
+from typing import Callable
+
+import numpy as np
+
+from .engine import AcvdError, Engine, build_topology
+
+
+@dataclasses.dataclass(frozen=True)
+class Schedule:
+    name: str
+    persistent: bool = False
+    host_loop: bool = False
+    relaxed: bool = True
+    match_rounds: int = 1
+    exact: bool = True   # same clustering as the default schedule, bit for bit
+
+    def create_env(self) -> dict:
+        """Switches the engine reads in acvd_create (None = unset)."""
+        return {"ACVD_RELAXED": None if self.relaxed else "0",
+                "ACVD_MATCH_ROUNDS": None if self.match_rounds == 1 else str(int(self.match_rounds))}
+
+    def run_env(self) -> dict:
+        """Switches the engine reads in acvd_minimize."""
+        return {"ACVD_HOST_LOOP": "1" if self.host_loop else None}
+
+
+DEFAULT = Schedule("graphs")
+EXACT_SCHEDULES = (DEFAULT, Schedule("host_loop", host_loop=True), Schedule("persistent", persistent=True))
+APPROX_SCHEDULES = (Schedule("exact_sweeps", relaxed=False, exact=False),
+                    Schedule("match2", match_rounds=2, exact=False))
+BY_NAME = {s.name: s for s in EXACT_SCHEDULES + APPROX_SCHEDULES}
+
+
+@contextlib.contextmanager
+def environ(values: dict):
+    """Sets (or, for None, removes) environment variables, and restores them on exit."""
+    saved = {k: os.environ.get(k) for k in values}
+    try:
+        for k, v in values.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
+        yield
+    finally:
+        for k, v in saved.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
+
+
+class ScheduledEngine(Engine):
+    """An Engine whose context is created, and whose minimisations run, under a schedule."""
+
+    def __init__(self, schedule: Schedule = DEFAULT, **kw):
+        self.schedule = schedule
+        with environ(schedule.create_env()):
+            super().__init__(persistent=schedule.persistent, **kw)
+
+    def minimize(self) -> dict:
+        with environ(self.schedule.run_env()):
+            return super().minimize()
+
+
+def size_class(n_items: int, k: int) -> str:
+    """Problems within a factor of about 1.4 in items and clusters share a tuned schedule."""
+    return "n2^%d_k2^%d" % (round(math.log2(max(int(n_items), 1))), round(math.log2(max(int(k), 1))))
+
+
+def labels_digest(labels: np.ndarray) -> str:
+    return hashlib.sha256(np.ascontiguousarray(labels, dtype=np.int32).tobytes()).hexdigest()
+
+
+@dataclasses.dataclass
+class Trial:
+    schedule: str
+    ms: float | None = None          # median device time of the timed solves
+    energy: float | None = None
+    accepted: bool = False
+    reason: str = ""
+
+
+class Autotuner:
+    """Chooses a schedule per key by measurement and caches the choice.
+
+    ``measure(schedule)`` runs one problem under ``schedule`` and returns a dict with
+    ``ms`` (a list of timed solves, device milliseconds), ``energy``, ``unassigned`` and
+    ``digest`` (labels_digest of the final clustering); it may raise AcvdError, which
+    rejects that candidate. The default schedule is always measured first: it is the
+    yardstick for the others, and a failure there is raised to the caller.
+    """
+
+    def __init__(self, cache_path: str | None = None, include_approximate: bool = False,
+                 energy_rel_tol: float = 1e-3, candidates=None):
+        self.cache_path = cache_path
+        self.energy_rel_tol = float(energy_rel_tol)
+        if candidates is None:
+            candidates = EXACT_SCHEDULES + (APPROX_SCHEDULES if include_approximate else ())
+        names = [s.name for s in candidates]
+        if DEFAULT.name not in names:
+            candidates = (DEFAULT,) + tuple(candidates)
+        self.candidates = tuple(sorted(candidates, key=lambda s: s.name != DEFAULT.name))
+        self.cache = self._load()
+
+    def _load(self) -> dict:
+        if not self.cache_path or not os.path.exists(self.cache_path):
+            return {}
+        with open(self.cache_path) as f:
+            data = json.load(f)
+        return data if isinstance(data, dict) else {}
+
+    def _save(self) -> None:
+        if not self.cache_path:
+            return
+        d = os.path.dirname(os.path.abspath(self.cache_path))
+        os.makedirs(d, exist_ok=True)
+        fd, tmp = tempfile.mkstemp(dir=d, prefix=".autotune-", suffix=".json")
+        with os.fdopen(fd, "w") as f:
+            json.dump(self.cache, f, indent=1, sort_keys=True)
+        os.replace(tmp, self.cache_path)
+
+    def lookup(self, key: str) -> Schedule | None:
+        entry = self.cache.get(key)
+        if entry is None:
+            return None
+        return BY_NAME.get(entry.get("schedule"))
+
+    def tune(self, key: str, measure: Callable[[Schedule], dict], retune: bool = False) -> tuple[Schedule, dict]:
+        """Returns (chosen schedule, report). A cached key is not measured again unless retune."""
+        if not retune:
+            hit = self.lookup(key)
+            if hit is not None:
+                return hit, dict(self.cache[key], cached=True)
+        trials: list[Trial] = []
+        base = None
+        for s in self.candidates:
+            t = Trial(s.name)
+            try:
+                r = measure(s)
+            except AcvdError as err:
+                if s.name == DEFAULT.name:
+                    raise
+                t.reason = "error: %s" % err
+                trials.append(t)
+                continue
+            t.ms = float(statistics.median(r["ms"]))
+            t.energy = float(r["energy"])
+            if s.name == DEFAULT.name:
+                base = r
+                t.accepted = True
+            elif r.get("unassigned", 0):
+                t.reason = "%d items unassigned" % r["unassigned"]
+            elif s.exact and r["digest"] != base["digest"]:
+                t.reason = "clustering differs from the default schedule's"
+            elif not s.exact and abs(t.energy - base["energy"]) > self.energy_rel_tol * abs(base["energy"]):
+                t.reason = "energy %.9g outside %.1e of %.9g" % (t.energy, self.energy_rel_tol, base["energy"])
+            else:
+                t.accepted = True
+            trials.append(t)
+        best = min((t for t in trials if t.accepted), key=lambda t: t.ms)
+        report = {"schedule": best.schedule, "ms": best.ms,
+                  "trials": [dataclasses.asdict(t) for t in trials]}
+        self.cache[key] = report
+        self._save()
+        return BY_NAME[best.schedule], dict(report, cached=False)
+
+
+def device_name(device: int = 0) -> str:
+    try:
+        import torch
+        if torch.cuda.is_available():
+            return torch.cuda.get_device_name(device)
+    except Exception:  # torch absent or without CUDA: the ordinal still keys the cache
+        pass
+    return "cuda:%d" % device
+
+
+def problem_key(metric: str, n_items: int, k: int, device: int = 0) -> str:
+    return "%s|%s|%s" % (device_name(device), metric, size_class(n_items, k))
+
+
+def solve_measure(points, faces, metric: str, k: int, labels, indicator=None, principal_dirs=None,
+                  gradation: float = 0.0, level: int = 3, unconstrained_init: int = 0,
+                  repeats: int = 3, device: int = 0, topology=None) -> Callable[[Schedule], dict]:
+    """A measure() for Autotuner.tune: one context per schedule, one untimed solve (graph
+    instantiation, first-touch), then ``repeats`` converged solves from the same initial
+    clustering (acvd_rewind), each timed on the device by the engine's own CUDA events."""
+    row, col, ev = topology if topology is not None else build_topology(np.asarray(points).shape[0], faces)
+    lab0 = np.ascontiguousarray(labels, dtype=np.int32)
+
+    def measure(s: Schedule) -> dict:
+        with ScheduledEngine(s, device=device) as e:
+            e.set_mesh(points, faces, row, col, ev)
+            e.set_metric(metric, indicator, principal_dirs, gradation)
+            e.set_level(level)
+            e.set_unconstrained_initialization(unconstrained_init)
+            e.set_labels(k, lab0)
+            e.minimize()
+            ms = []
+            for _ in range(max(1, int(repeats))):
+                e.rewind()
+                st = e.minimize()
+                ms.append(st["device_ms"])
+            return {"ms": ms, "energy": st["energy"], "unassigned": st["unassigned"],
+                    "digest": labels_digest(e.labels())}
+
+    return measure
+
+
+def default_cache_path() -> str:
+    base = os.environ.get("XDG_CACHE_HOME") or os.path.join(os.path.expanduser("~"), ".cache")
+    return os.path.join(base, "acvd_gb300", "autotune.json")
+
+
+def tune_problem(points, faces, metric: str, k: int, labels, tuner: Autotuner | None = None,
+                 retune: bool = False, **kw) -> tuple[Schedule, dict]:
+    """Tunes (or looks up) the schedule for one problem; keywords go to solve_measure."""
+    tuner = tuner if tuner is not None else Autotuner(default_cache_path())
+    key = problem_key(metric, np.asarray(points).shape[0], k, kw.get("device", 0))
+    return tuner.tune(key, solve_measure(points, faces, metric, k, labels, **kw), retune=retune)
