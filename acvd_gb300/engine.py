@@ -272,7 +272,8 @@ class Engine:
     DEFAULT_MAX_LOOPS = 20000
 
     def __init__(self, device: int = 0, use_graphs: bool = True, kernel_timing: bool = False,
-                 max_loops: int | None = DEFAULT_MAX_LOOPS, persistent: bool = False):
+                 max_loops: int | None = DEFAULT_MAX_LOOPS, persistent: bool = False,
+                 max_convergences: int | None = None):
         lib = load()
         o = Opts()
         lib.acvd_default_opts(ctypes.byref(o))
@@ -282,6 +283,8 @@ class Engine:
         o.kernel_timing = 1 if kernel_timing else 0
         if max_loops is not None:
             o.max_loops = int(max_loops)
+        if max_convergences is not None:
+            o.max_convergences = int(max_convergences)
         self._lib = lib
         self.ctx = lib.acvd_create(ctypes.byref(o))
         if not self.ctx:

@@ -74,6 +74,16 @@ class Surface:
               f"{self.GetNumberOfEdges()} edges")
 
 
+def initial_identity_sampling(n_items: int, k: int) -> np.ndarray:
+    """Initial sampling type -1 (vtkUniformClustering.h:1139-1157): item i seeds cluster i
+    for i < K, every other item is unassigned (label K)."""
+    if not 0 < k <= n_items:
+        raise _eng.AcvdError(1, "initial sampling type -1 needs 0 < NumberOfClusters <= items")
+    lab = np.full(n_items, k, dtype=np.int32)
+    lab[:k] = np.arange(k, dtype=np.int32)
+    return lab
+
+
 class _Metric:
     def __init__(self, owner):
         self._o = owner
@@ -111,6 +121,8 @@ class _DiscreteRemeshing:
         self.Display = 0
         self.MaxNumberOfLoops = 5000000
         self.InitialClustering = None
+        self.InitialSamplingType = 1        # vtkUniformClustering.h:108, default :1409
+        self.MaxNumberOfConvergences = 1000000000   # :99, default :1406
         self._resume = False              # LoadClustering: take the clustering as computed
         self.ForceManifold = False
         self.BoundaryFixing = 0          # the constructor's value (vtkDiscreteRemeshing.h:1192)
@@ -158,7 +170,53 @@ class _DiscreteRemeshing:
         self.UnconstrainedInitialization = int(on)
 
     def SetInitialClustering(self, labels):
+        """Start from these labels (NumberOfClusters = unassigned); like the reference, this
+        also selects initial sampling type 2 (vtkUniformClustering.h:337-342)."""
         self.InitialClustering = np.ascontiguousarray(labels, dtype=np.int32)
+        self.InitialSamplingType = 2
+
+    def SetInitialSamplingType(self, t: int):
+        """InitSamples (vtkUniformClustering.h:1124-1175): 1 = weighted region growing from a
+        seeded shuffle (the default), 2 = the labels of SetInitialClustering, -1 = item i seeds
+        cluster i. Type 0 draws seeds from VTK's vtkMath::Random sequence, which is not
+        restated here (VTK is not pinned), and is refused."""
+        t = int(t)
+        if t == 0:
+            raise _eng.AcvdError(5, "initial sampling type 0 draws from VTK's vtkMath::Random sequence, "
+                                    "which is not available; use type 1, 2 or -1")
+        if t not in (-1, 1, 2):
+            raise _eng.AcvdError(1, "initial sampling type must be -1, 0, 1 or 2")
+        self.InitialSamplingType = t
+
+    def SetMaxNumberOfConvergences(self, n: int):
+        """Convergence events after which the minimisation stops (:99, :773-824)."""
+        self.MaxNumberOfConvergences = int(n)
+        if self._engine is not None:   # the cap is a context option: the next Remesh makes a new context
+            self._engine.close()
+            self._engine = None
+
+    def SetMinimizeUsingEnergy(self, on):
+        """Only the energy-driven loop (ProcessOneLoop, the reference's default, :1416) is
+        built; the distance-driven ProcessOneLoopWithDistances (:1002-) is not."""
+        if not on:
+            raise _eng.AcvdError(5, "only energy minimisation (MinimizeUsingEnergy on) is available")
+
+    def SetWriteToGlobalEnergyLog(self, on: int):
+        """The per-loop energy log (ComputeAndSaveEnergy, :123, :1386-) is not written:
+        only 0 is accepted; the final energy is in Stats['energy']."""
+        if on:
+            raise _eng.AcvdError(5, "the global energy log is not available; read Stats['energy']")
+
+    def GetNumberOfItems(self) -> int:
+        return 0 if self.Input is None else self.Input.GetNumberOfPoints()
+
+    def GetClusterSize(self, c: int) -> int:
+        """Items in cluster c of the current clustering (ClustersSizes, :132)."""
+        if self.Clustering is None:
+            raise _eng.AcvdError(1, "no clustering yet: call Remesh or ProcessClustering first")
+        if not 0 <= int(c) < self.NumberOfClusters:
+            raise IndexError("cluster index outside [0, NumberOfClusters)")
+        return int(np.count_nonzero(np.asarray(self.Clustering) == int(c)))
 
     def SetConsoleOutput(self, v: int):
         self.ConsoleOutput = int(v)
@@ -261,7 +319,8 @@ class _DiscreteRemeshing:
         if k <= 0:
             raise _eng.AcvdError(1, "must set NumberOfClusters to more than zero")
         if self._engine is None:
-            self._engine = _eng.Engine(self._device, max_loops=self.MaxNumberOfLoops)
+            self._engine = _eng.Engine(self._device, max_loops=self.MaxNumberOfLoops,
+                                       max_convergences=self.MaxNumberOfConvergences)
         e = self._engine
         # SamplingPreProcessing (vtkDiscreteRemeshing.h:583-753): the curvature the
         # metric needs, computed here on the GPU on the original mesh unless
@@ -300,8 +359,12 @@ class _DiscreteRemeshing:
         e.set_metric(self._metric_name, ind, self.PrincipalDirections, self._metric.Gradation)
         e.set_level(self._metric.QuadricsOptimizationLevel)
         e.set_unconstrained_initialization(self.UnconstrainedInitialization)
-        if self.InitialClustering is not None:
+        if self.InitialSamplingType == 2:
+            if self.InitialClustering is None:
+                raise _eng.AcvdError(1, "initial sampling type 2 needs SetInitialClustering")
             lab = self.InitialClustering
+        elif self.InitialSamplingType == -1:
+            lab = initial_identity_sampling(n, k)
         else:
             w = _eng.vertex_weights(self._metric_name, self.Input.points, self.Input.faces, ind,
                                     self._metric.Gradation)

@@ -1,0 +1,70 @@
+"""Reference setters of the Python remesher that act before any solve: initial sampling
+type, convergence cap, energy-driven loop, energy log, cluster sizes (CPU only)."""
+import numpy as np
+import pytest
+
+import acvd_gb300
+from acvd_gb300 import remesh
+from acvd_gb300 import synth
+
+
+def _remesher(cls=acvd_gb300.IsotropicDiscreteRemeshing):
+    r = cls.New()
+    m = synth.icosphere(2, seed=0)
+    r.SetInput(acvd_gb300.Surface(m.points, m.faces))
+    r.SetNumberOfClusters(20)
+    return r
+
+
+def test_initial_sampling_types():
+    r = _remesher()
+    assert r.InitialSamplingType == 1                       # the reference's default
+    r.SetInitialClustering(np.zeros(r.GetNumberOfItems(), dtype=np.int32))
+    assert r.InitialSamplingType == 2                       # SetInitialClustering selects type 2
+    r.SetInitialSamplingType(-1)
+    assert r.InitialSamplingType == -1
+    with pytest.raises(acvd_gb300.AcvdError) as err:
+        r.SetInitialSamplingType(0)                         # vtkMath::Random's sequence: refused
+    assert err.value.code == 5
+    with pytest.raises(acvd_gb300.AcvdError):
+        r.SetInitialSamplingType(3)
+    assert r.InitialSamplingType == -1
+
+
+def test_identity_sampling():
+    np.testing.assert_array_equal(remesh.initial_identity_sampling(5, 3), [0, 1, 2, 3, 3])
+    np.testing.assert_array_equal(remesh.initial_identity_sampling(3, 3), [0, 1, 2])
+    for n, k in ((3, 4), (3, 0)):
+        with pytest.raises(acvd_gb300.AcvdError):
+            remesh.initial_identity_sampling(n, k)
+
+
+def test_loop_options_and_refusals():
+    r = _remesher(acvd_gb300.QIsotropicDiscreteRemeshing)
+    assert r.MaxNumberOfConvergences == 1000000000
+    r.SetMaxNumberOfConvergences(3)
+    assert r.MaxNumberOfConvergences == 3
+    r.SetMinimizeUsingEnergy(True)
+    r.SetWriteToGlobalEnergyLog(0)
+    for call in (lambda: r.SetMinimizeUsingEnergy(False), lambda: r.SetWriteToGlobalEnergyLog(1)):
+        with pytest.raises(acvd_gb300.AcvdError) as err:
+            call()
+        assert err.value.code == 5
+
+
+def test_cluster_sizes():
+    r = _remesher()
+    assert r.GetNumberOfItems() == 162
+    with pytest.raises(acvd_gb300.AcvdError):
+        r.GetClusterSize(0)
+    r.Clustering = np.repeat(np.arange(20, dtype=np.int32), 9)[:162]
+    assert [r.GetClusterSize(c) for c in (0, 17, 18, 19)] == [9, 9, 0, 0]
+    assert sum(r.GetClusterSize(c) for c in range(20)) == 162
+    with pytest.raises(IndexError):
+        r.GetClusterSize(20)
+    assert acvd_gb300.IsotropicDiscreteRemeshing.New().GetNumberOfItems() == 0
+
+
+def test_engine_takes_the_convergence_cap():
+    o = acvd_gb300.engine.Opts()
+    assert [f[0] for f in o._fields_].index("max_convergences") == 3
