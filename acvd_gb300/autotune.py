@@ -161,10 +161,22 @@ class Autotuner:
         os.replace(tmp, self.cache_path)
 
     def lookup(self, key: str) -> Schedule | None:
+        """The cached choice for key, if this tuner could have made it: a schedule outside
+        this tuner's candidates (an approximate one cached by an opt-in tuner, seen by a
+        default one) or an approximate one accepted under a looser energy tolerance than
+        this tuner's is a miss, so that a default tuner never returns a schedule that
+        changes the clustering."""
         entry = self.cache.get(key)
         if entry is None:
             return None
-        return BY_NAME.get(entry.get("schedule"))
+        s = BY_NAME.get(entry.get("schedule"))
+        if s is None or s not in self.candidates:
+            return None
+        if not s.exact:
+            tol = entry.get("energy_rel_tol")
+            if tol is None or float(tol) > self.energy_rel_tol:
+                return None
+        return s
 
     def tune(self, key: str, measure: Callable[[Schedule], dict], retune: bool = False) -> tuple[Schedule, dict]:
         """Returns (chosen schedule, report). A cached key is not measured again unless retune."""
@@ -199,7 +211,7 @@ class Autotuner:
                 t.accepted = True
             trials.append(t)
         best = min((t for t in trials if t.accepted), key=lambda t: t.ms)
-        report = {"schedule": best.schedule, "ms": best.ms,
+        report = {"schedule": best.schedule, "ms": best.ms, "energy_rel_tol": self.energy_rel_tol,
                   "trials": [dataclasses.asdict(t) for t in trials]}
         self.cache[key] = report
         self._save()

@@ -71,21 +71,48 @@ def build_batch(meshes, ks, metric: str = "qem", gradation: float = 0.0) -> Batc
                  k_total, metric, gradation, ind)
 
 
+def spec_items(spec) -> int:
+    """Vertex count of a batch mesh spec (kind, size parameters) without building it."""
+    kind, kw = spec
+    if kind == "icosphere":
+        return 10 * 4 ** kw["level"] + 2
+    if kind == "torus":
+        return kw["nu"] * kw["nv"]
+    return kw["n"] * kw["n"]
+
+
+def spec_faces(spec) -> int:
+    """Triangle count of a batch mesh spec without building it."""
+    kind, kw = spec
+    if kind == "icosphere":
+        return 20 * 4 ** kw["level"]
+    if kind == "torus":
+        return 2 * kw["nu"] * kw["nv"]
+    return 2 * (kw["n"] - 1) ** 2
+
+
+def mesh_from_spec(spec, with_curvature: bool):
+    kind, kw = spec
+    if kind == "icosphere":
+        return synth.icosphere(kw["level"], seed=kw["seed"], with_curvature=with_curvature)
+    if kind == "torus":
+        return synth.torus(kw["nu"], kw["nv"], seed=kw["seed"], with_curvature=with_curvature)
+    return synth.heightfield(kw["n"], seed=kw["seed"], with_curvature=with_curvature)
+
+
+def batch_from_specs(specs, metric: str = "qem", gradation: float = 0.0, items_per_cluster: int = 20) -> Batch:
+    """The batch of the given mesh specs, K = vertices / items_per_cluster per mesh."""
+    curv = gradation != 0.0 or metric == "aniso"
+    meshes = [mesh_from_spec(s, curv) for s in specs]
+    ks = [max(1, m.n_points // items_per_cluster) for m in meshes]
+    return build_batch(meshes, ks, metric, gradation)
+
+
 def synthetic_batch(n_meshes: int = 256, seed: int = 0, lo: int = 2000, hi: int = 500000,
                     items_per_cluster: int = 20, metric: str = "qem", gradation: float = 0.0) -> Batch:
     """The batched workload: generator type uniform over icosphere / torus / heightfield,
     vertex count log-uniform in [lo, hi], K = vertices / 20 per mesh."""
-    meshes = []
-    for kind, kw in synth.batch_specs(n_meshes, seed, lo, hi):
-        curv = gradation != 0.0 or metric == "aniso"
-        if kind == "icosphere":
-            meshes.append(synth.icosphere(kw["level"], seed=kw["seed"], with_curvature=curv))
-        elif kind == "torus":
-            meshes.append(synth.torus(kw["nu"], kw["nv"], seed=kw["seed"], with_curvature=curv))
-        else:
-            meshes.append(synth.heightfield(kw["n"], seed=kw["seed"], with_curvature=curv))
-    ks = [max(1, m.n_points // items_per_cluster) for m in meshes]
-    return build_batch(meshes, ks, metric, gradation)
+    return batch_from_specs(synth.batch_specs(n_meshes, seed, lo, hi), metric, gradation, items_per_cluster)
 
 
 def run_on_gpu(b: Batch, engine: "_eng.Engine | None" = None, unconstrained_init: int = 1):

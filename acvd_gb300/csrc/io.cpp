@@ -1111,10 +1111,17 @@ int read_metaimage(const std::string& path, std::vector<int64_t>& dim, std::vect
     dim.assign(3, 1);
     origin.assign(3, 0.0);
     spacing.assign(3, 1.0);
+    // each extent and the voxel count are bounded (2^31 per axis, 2^36 voxels) so
+    // that the byte count below cannot wrap
+    constexpr double kMaxExtent = 2147483648.0;
+    constexpr uint64_t kMaxVoxels = 1ull << 36;
     for (int i = 0; i < nd; i++) {
-        if (!(ds[i] >= 1)) return io_fail(ACVD_ERR_ARG, "MetaImage: DimSize");
+        if (!(ds[i] >= 1 && ds[i] <= kMaxExtent)) return io_fail(ACVD_ERR_ARG, "MetaImage: DimSize");
         dim[i] = (int64_t)ds[i];
     }
+    if ((uint64_t)dim[0] * (uint64_t)dim[1] > kMaxVoxels ||
+        (uint64_t)dim[0] * (uint64_t)dim[1] * (uint64_t)dim[2] > kMaxVoxels)
+        return io_fail(ACVD_ERR_ARG, "MetaImage: DimSize too large");
     std::vector<double> sp = numbers(get("ElementSpacing"));
     if (sp.empty()) sp = numbers(get("ElementSize"));
     for (int i = 0; i < nd && i < (int)sp.size(); i++) spacing[i] = sp[i];
@@ -1136,7 +1143,9 @@ int read_metaimage(const std::string& path, std::vector<int64_t>& dim, std::vect
     else if (et == "MET_FLOAT") { size = 4; is_float = true; }
     else if (et == "MET_DOUBLE") { size = 8; is_float = true; }
     else return io_fail(ACVD_ERR_UNSUPPORTED, "MetaImage: ElementType " + et);
-    const int channels = std::max(1, std::atoi(get("ElementNumberOfChannels").c_str()));
+    const long long channels_in = std::atoll(get("ElementNumberOfChannels").c_str());
+    if (channels_in > 1024) return io_fail(ACVD_ERR_ARG, "MetaImage: ElementNumberOfChannels too large");
+    const int channels = (int)std::max(1LL, channels_in);
     std::string msb = get("ElementByteOrderMSB");
     if (msb.empty()) msb = get("BinaryDataByteOrderMSB");
     const bool little = !(msb == "True" || msb == "true" || msb == "1");

@@ -85,7 +85,8 @@ __global__ void __launch_bounds__(kNaThreads) na_compact_kernel(const int32_t* _
     if (blockIdx.x == gridDim.x - 1 && tid == kNaThreads - 1) *count = at + pair;
 }
 
-// Per-device address of the scratch array, looked up once with that device current.
+// Per-device address of the scratch array, looked up once with that device current
+// and kept for the process (stale after a cudaDeviceReset of that device).
 int na_scratch(uint32_t** out) {
     int dev = -1;
     if (cudaGetDevice(&dev) != cudaSuccess) return ACVD_ERR_CUDA;

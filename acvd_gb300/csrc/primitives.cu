@@ -38,8 +38,10 @@ __device__ __forceinline__ uint32_t warp_incl_scan(uint32_t v, int lane) {
     return v;
 }
 
-__global__ void __launch_bounds__(kScanThreads) scan_tile_kernel(const uint32_t* __restrict__ in,
-                                                                 uint32_t* __restrict__ out, int64_t n,
+// `in` and `out` may be the same array (in-place scans): each thread reads its
+// own pair before the block's first barrier and writes it after the last, so
+// neither pointer is declared __restrict__.
+__global__ void __launch_bounds__(kScanThreads) scan_tile_kernel(const uint32_t* in, uint32_t* out, int64_t n,
                                                                  uint32_t* __restrict__ block_sums) {
     __shared__ uint32_t wsum[32];
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;

@@ -17,6 +17,7 @@ shard); rank 0 prints one JSON line.
 from __future__ import annotations
 
 import argparse
+import hashlib
 import json
 import math
 import os
@@ -619,6 +620,8 @@ def make_workload(name):
 
 
 def initial_labels(m, metric, ind, grad, k, init=None):
+    """The GPU arm's initial clustering: the library's host port of the reference's
+    ComputeInitialRandomSampling (or the seeded single-item seeds)."""
     import acvd_gb300
     from acvd_gb300 import synth
     row, col, ev = acvd_gb300.build_topology(m.n_points, m.faces)
@@ -626,6 +629,13 @@ def initial_labels(m, metric, ind, grad, k, init=None):
         return synth.seed_labels(m.n_points, k, seed=0), (row, col, ev)
     w = acvd_gb300.vertex_weights(metric, m.points, m.faces, ind, grad)
     return acvd_gb300.initial_sampling(row, col, w, k), (row, col, ev)
+
+
+def reference_seeds(m, w):
+    """The CPU side's initial-clustering input: the seeded single-item seeds of the
+    seeded workload, else None (the oracle runs the reference's own sampling)."""
+    from acvd_gb300 import synth    # numpy only: the CUDA library is not loaded
+    return synth.seed_labels(m.n_points, w["k"], seed=0) if w.get("init") == "seeds" else None
 
 
 class ClockSampler:
@@ -677,14 +687,18 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows), "samples_under_load": len(loaded)}
 
 
-def cpu_reference_run(m, ind, pd, w, lab0):
-    """The oracle's restatement of the reference's sequential MinimizeEnergy."""
+def cpu_reference_run(m, ind, pd, w, seeds):
+    """The oracle's restatement of the reference's sequential MinimizeEnergy, started
+    from the reference's own initial sampling (or the given seeds).  Nothing of the
+    CUDA library runs here.  Returns the solver, the minimisation's seconds and the
+    initial clustering."""
     from oracle import oracle
     oracle.build(ref=False)
     p = oracle.Port(w["metric"], m.points, m.faces, w["k"], w["gradation"], ind, pd, unconstrained_init=w["uinit"])
-    p.init(lab0)
+    p.init(seeds)
+    lab_init = p.labels()
     secs = p.run()
-    return p, secs
+    return p, secs, lab_init
 
 
 def evaluated_energy(w, points, faces, k, ind, pd, labels):
@@ -696,17 +710,118 @@ def evaluated_energy(w, points, faces, k, ind, pd, labels):
     return ev.global_energy(), ev
 
 
+FIXTURE_DIR = os.path.join(ROOT, "tests", "golden", "fullsize")
+L2_NOTE = "GPU arm: L2 flushed between timed steps (256 MB write)"
+EXTRA_STEPS = 5     # timed steps of the extra workloads of the default run
+
+
+def fullsize_fixture(name):
+    """The oracle's converged energy for a full-size workload from the reference's own
+    initial sampling, precomputed by tests/golden/gen_fullsize.py (the sequential CPU
+    solve is far longer than a bench run)."""
+    try:
+        with open(os.path.join(FIXTURE_DIR, name + ".json")) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return None
+
+
+def labels_sha(lab) -> str:
+    return hashlib.sha256(np.ascontiguousarray(lab, dtype=np.int32).tobytes()).hexdigest()
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def workload_config(name, desc, items, clusters, faces, ws, batch=False):
+    """The config block both arms print for a workload (identical keys and values)."""
+    par = "single"
+    if ws > 1:
+        par = f"meshes sharded over {ws} ranks" if batch else f"{ws} replicas"
+    return {"workload": name, "description": desc, "items": int(items), "clusters": int(clusters),
+            "faces": int(faces), "parallelism": par, "l2": L2_NOTE}
+
+
 def _port_job(args):
+    """Reference-arm worker: one sequential converged solve of the workload from the
+    reference's own initial sampling (oracle only)."""
     name, = args
     m, ind, pd, w = make_workload(name)
-    lab0, _ = initial_labels(m, w["metric"], ind, w["gradation"], w["k"], w.get("init"))
-    p, secs = cpu_reference_run(m, ind, pd, w, lab0)
+    p, secs, _ = cpu_reference_run(m, ind, pd, w, reference_seeds(m, w))
     return m.n_points, secs, p.global_energy()
+
+
+def _batch_port_job(a):
+    """Reference-arm worker for the batch: one mesh, one sequential converged solve."""
+    spec, metric, grad, uinit, ipc = a
+    from acvd_gb300 import batch as B
+    from oracle import oracle
+    m = B.mesh_from_spec(spec, grad != 0.0 or metric == "aniso")
+    k = max(1, m.n_points // ipc)
+    use_ind = grad != 0.0 if metric == "aniso" else grad > 0.0
+    p = oracle.Port(metric, m.points, m.faces, k, grad, m.indicator if use_ind else None, None,
+                    unconstrained_init=uinit)
+    p.init(None)
+    secs = p.run()
+    return m.n_points, secs
+
+
+def run_batch_reference_arm(args):
+    """CPU arm of the batch: one mesh per host core at a time, as the reference's
+    VolumeAnalysis hands one label to each thread (VolumeAnalysis.cxx:153).  Each step
+    solves a bounded sample of the batch (every 16th mesh); the step time is the sum of
+    the sample's solve times over the cores (a perfect packing of the meshes on the
+    cores, which favours the CPU)."""
+    ws, rank, _ = _dist()
+    if rank != 0:
+        return
+    import multiprocessing as mp
+    from acvd_gb300 import batch as B
+    from acvd_gb300 import synth
+    from oracle import oracle
+    oracle.build(ref=False)
+    w = BATCH_WORKLOADS[args.workload]
+    cores = os.cpu_count() or 1
+    specs = synth.batch_specs(w["n_meshes"] * ws, w["seed"])
+    sample = list(range(0, len(specs), w["cpu_every"]))
+    jobs = sorted(((specs[i], w["metric"], w["gradation"], w["uinit"], 20) for i in sample),
+                  key=lambda j: -B.spec_items(j[0]))
+    times = []
+    with mp.get_context("spawn").Pool(cores) as pool:
+        for step in range(args.warmup + args.steps):
+            res = pool.map(_batch_port_job, jobs, chunksize=1)
+            if step >= args.warmup:
+                times.append(sum(r[1] for r in res) / cores)
+    ms = 1000.0 * statistics.mean(times)
+    value = len(sample) / (ms / 1000.0)
+    items = sum(B.spec_items(s) for s in specs)
+    faces = sum(B.spec_faces(s) for s in specs)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "meshes/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": workload_config(args.workload, w["desc"], items, sum(max(1, B.spec_items(s) // 20)
+                                                                            for s in specs), faces, ws, batch=True),
+            "cpu_baseline": {"value": value, "unit": "meshes/s", "cores": cores, "kind": "port",
+                             "sample": f"every {w['cpu_every']}th mesh ({len(sample)} meshes) per step, one mesh "
+                                       f"per core at a time, sequential reference algorithm restated in C++; "
+                                       f"step time = summed solve time / {cores} cores"},
+            "e2e": {"value": value, "unit": "meshes/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
 
 
 def run_reference_arm(args):
     """CPU arm: the reference algorithm (oracle restatement, sequential per mesh);
-    every host core solves its own copy of the workload, so the whole CPU is used."""
+    every host core solves its own copy of the workload, so the whole CPU is used.
+    The initial clustering is the reference's own sampling, run by the oracle: the
+    CUDA library is never loaded on this arm."""
+    if args.workload in BATCH_WORKLOADS:
+        run_batch_reference_arm(args)
+        return
     ws, rank, _ = _dist()
     if rank != 0:
         return
@@ -714,7 +829,6 @@ def run_reference_arm(args):
     cores = os.cpu_count() or 1
     ctx = mp.get_context("spawn")
     m, ind, pd, w = make_workload(args.workload)
-    # build once before forking workers
     from oracle import oracle
     oracle.build(ref=False)
     times = []
@@ -733,11 +847,12 @@ def run_reference_arm(args):
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "items/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": args.workload, "description": w["desc"], "items": n, "clusters": w["k"],
-                       "copies_per_step": cores},
+            "config": workload_config(args.workload, w["desc"], n, w["k"], m.n_faces, ws),
+            "copies_per_step": cores,
             "cpu_baseline": {"value": value, "unit": "items/s", "cores": cores, "kind": "port",
                              "sample": f"{cores} concurrent full solves of the workload (one per core), "
-                                       f"sequential reference algorithm restated in C++"},
+                                       f"sequential reference algorithm restated in C++, from the reference's "
+                                       f"own initial sampling"},
             "e2e": {"value": value, "unit": "items/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "energy": energies[-1] if energies else None}
     print(json.dumps(line), flush=True)
@@ -798,21 +913,50 @@ def roofline_kernel(persistent, tot_t):
     return "eval_kernel", tot_t["eval_ms"], tot_t["eval_launches"]
 
 
-def run_batch_arm(args):
-    """Batched workload: every mesh of the batch in one packed CSR, one minimisation."""
+def roofline_block(persistent, tot_t, workload):
+    """The dominant kernel's roofline from the instrumented pass, and its DRAM traffic
+    per launch from the committed ncu summary (profiles/eval_traffic.json)."""
+    peaks = load_peaks()
+    peak = peaks.get("hbm_gbs", 6800.0)
+    kname, kms, klaunch = roofline_kernel(persistent, tot_t)
+    achieved = (tot_t["eval_bytes"] / 1e9) / (kms / 1000.0) if kms > 0 else None
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "eval_traffic.json")
+    if os.path.exists(tpath):
+        try:
+            with open(tpath) as f:
+                traffic = json.load(f).get(workload)
+        except ValueError:
+            traffic = None
+    return {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": (achieved / peak) if achieved else None,
+            "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if "hbm_gbs" in peaks else "fallback",
+            "traffic": traffic, "launches": klaunch,
+            "algorithmic_bytes_per_launch": tot_t["eval_bytes"] / max(1, klaunch),
+            "avg_launch_us": 1000.0 * kms / max(1, klaunch),
+            "timing": "CUDA events around each launch, in a second pass of the same steps "
+                      "(the headline pass carries no events)"}
+
+
+def batch_line(args, name, steps, warmup, e2e_on, cpu_on):
+    """Batched workload: the rank's share of the meshes (balanced by items) in one packed
+    CSR, one minimisation per step.  At N ranks the batch holds N x 256 meshes (the
+    first 256 are the single-GPU batch), so the work per GPU stays fixed.  Per-mesh
+    labels and energies are gathered on rank 0 after the timed steps.  Returns the
+    JSON line on rank 0, None elsewhere."""
     import torch
     from acvd_gb300 import batch as B
     from acvd_gb300 import engine as E
+    from acvd_gb300 import shards
+    from acvd_gb300 import synth
 
-    ws, rank, local = _dist()
-    if ws > 1:
-        torch.cuda.set_device(local)
-        replicas.init("nccl")
-    device = local
-    torch.cuda.set_device(device)
-    w = BATCH_WORKLOADS[args.workload]
+    ws, rank, device = _dist()
+    w = BATCH_WORKLOADS[name]
+    specs = synth.batch_specs(w["n_meshes"] * ws, w["seed"])
+    parts = shards.balanced_partition([B.spec_items(s) for s in specs], ws)
+    mine = parts[rank]
     t0 = time.perf_counter()
-    b = B.synthetic_batch(w["n_meshes"], w["seed"], metric=w["metric"], gradation=w["gradation"])
+    b = B.batch_from_specs([specs[i] for i in mine], w["metric"], w["gradation"])
     gen_s = time.perf_counter() - t0
     persistent = args.schedule == "persistent"
     row, col, ev = E.build_topology(b.n_points, b.faces)
@@ -830,17 +974,18 @@ def run_batch_arm(args):
     # pass 1 (the headline): no instrumentation; pass 2: events around the evaluation kernels
     eng = make_engine(False)
     with ClockSampler(device) as clk:
-        step_ms, tot, st = run_steps(torch, eng, args.steps, args.warmup, device, ws, flush)
+        step_ms, tot, st = run_steps(torch, eng, steps, warmup, device, ws, flush)
     engt = make_engine(True)
-    _, tot_t, _ = run_steps(torch, engt, args.steps, 1, device, ws, flush)
+    _, tot_t, _ = run_steps(torch, engt, steps, 1, device, ws, flush)
     engt.close()
     ms = statistics.mean(step_ms)
-    ms = replicas.max_over_ranks(ms, device=f"cuda:{device}")   # the slowest replica
-    value = ws * b.n_mesh / (ms / 1000.0)
+    ms = replicas.max_over_ranks(ms, device=f"cuda:{device}")   # the slowest rank
+    value = len(specs) / (ms / 1000.0)
     packed = eng.labels()
     mesh_e = eng.mesh_energies()
+    eng.close()
     e2e = None
-    if not args.no_e2e:
+    if e2e_on:
         h2d = (b.points.nbytes + b.faces.nbytes + row.nbytes + col.nbytes + ev.nbytes + b.labels0.nbytes +
                (b.indicator.nbytes if b.indicator is not None else 0))
         e2e_ms = []
@@ -853,7 +998,7 @@ def run_batch_arm(args):
         h_ind = pinned(torch, None if b.indicator is None else c(b.indicator, dtype=np.float64))
         h_lab0 = pinned(torch, c(b.labels0, dtype=np.int32))
         out = pinned(torch, c(b.labels0, dtype=np.int32))
-        for _ in range(max(1, args.steps)):
+        for _ in range(max(1, steps)):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             eng2.set_mesh(h_pts, h_faces, h_row, h_col, h_ev)
@@ -867,85 +1012,101 @@ def run_batch_arm(args):
             e2e_ms.append(1000.0 * (time.perf_counter() - t0))
         eng2.close()
         assert np.array_equal(out, packed), "end-to-end batch run differs from the resident run"
-        e2e = {"value": ws * b.n_mesh / (statistics.mean(e2e_ms) / 1000.0), "unit": "meshes/s",
+        e2e_t = replicas.max_over_ranks(statistics.mean(e2e_ms), device=f"cuda:{device}")
+        e2e = {"value": len(specs) / (e2e_t / 1000.0), "unit": "meshes/s",
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(b.labels0.nbytes),
-               "ms_per_step": statistics.mean(e2e_ms)}
+               "ms_per_step": e2e_t}
+    # per-mesh results of this rank, gathered on rank 0 (after the timed steps)
+    lab_m = shards.split_packed(packed, b.v_off, b.k_off, b.ks)
+    lab0_m = shards.split_packed(b.labels0, b.v_off, b.k_off, b.ks)
+    local = {g: (lab_m[j], float(mesh_e[j]), labels_sha(lab0_m[j])) for j, g in enumerate(mine)}
+    results = shards.gather_meshes(local, len(specs), rank, ws)
+    loads = shards.part_loads([B.spec_items(s) for s in specs], parts)
     replicas.barrier()
     if rank != 0:
-        return
-    cpu = None
+        return None
     energy = {}
-    if not args.no_cpu_baseline:
+    fx = fullsize_fixture(name)
+    if fx is not None:
+        # every mesh of the fixture's batch: the GPU clustering evaluated by the oracle
+        # against the oracle's own converged solve from the reference's sampling
+        t0 = time.perf_counter()
+        worst, n_ok, n_conn, n_init, n_chk = -1e300, 0, 0, 0, 0
+        for g, ref in enumerate(fx["meshes"][:len(specs)]):
+            m = B.mesh_from_spec(specs[g], False)
+            lab, _, sha0 = results[g]
+            e_gpu, chk = evaluated_energy(w, m.points, m.faces, ref["clusters"], None, None, lab)
+            rel = (e_gpu - ref["reference_energy"]) / abs(ref["reference_energy"])
+            worst = max(worst, rel)
+            n_ok += rel <= 1e-3
+            n_conn += chk.clean() == 0
+            n_init += sha0 == ref["labels0_sha256"]
+            n_chk += 1
+        energy = {"meshes_checked": n_chk, "worst_rel_diff_vs_reference": worst,
+                  "meshes_within_0.1pct": n_ok, "within_0.1pct": bool(n_ok == n_chk),
+                  "meshes_all_clusters_connected": n_conn, "all_clusters_connected": bool(n_conn == n_chk),
+                  "meshes_initial_clustering_identical_to_reference": n_init,
+                  "reference": "tests/golden/fullsize/" + name + ".json (oracle converged solve per mesh from the "
+                               "reference's own initial sampling)",
+                  "check_s": time.perf_counter() - t0}
+    cpu = None
+    if cpu_on:
         from oracle import oracle
         oracle.build(ref=False)
         secs = 0.0
-        worst = -1e300
         n_items = 0
-        sample = list(range(0, b.n_mesh, w["cpu_every"]))
-        for m in sample:
-            mesh = b.meshes[m]
-            k = int(b.ks[m])
-            p = oracle.Port(w["metric"], mesh.points, mesh.faces, k, w["gradation"], unconstrained_init=w["uinit"])
-            p.init(b.mesh_labels(b.labels0, m))
+        sample = list(range(0, w["n_meshes"], w["cpu_every"]))
+        for g in sample:
+            m = B.mesh_from_spec(specs[g], False)
+            k = max(1, m.n_points // 20)
+            p = oracle.Port(w["metric"], m.points, m.faces, k, w["gradation"], unconstrained_init=w["uinit"])
+            p.init(None)
             secs += p.run()
-            e_ref, _ = evaluated_energy(w, mesh.points, mesh.faces, k, None, None, p.labels())
-            e_gpu, _ = evaluated_energy(w, mesh.points, mesh.faces, k, None, None, b.mesh_labels(packed, m))
-            worst = max(worst, (e_gpu - e_ref) / abs(e_ref))
-            n_items += mesh.n_points
+            n_items += m.n_points
         cpu = {"value": len(sample) / secs, "unit": "meshes/s", "cores": 1, "kind": "port",
                "sample": f"every {w['cpu_every']}th mesh of the batch ({len(sample)} meshes, {n_items} vertices), "
-                         f"sequential converged solves ({secs:.2f} s)"}
-        energy = {"meshes_checked": len(sample), "worst_rel_diff_vs_reference": worst,
-                  "within_0.1pct": bool(worst <= 1e-3)}
-    peaks = {}
-    try:
-        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-    except (OSError, ValueError):
-        pass
-    peak = peaks.get("hbm_gbs", 6800.0)
-    kname, kms, klaunch = roofline_kernel(persistent, tot_t)
-    achieved = (tot_t["eval_bytes"] / 1e9) / (kms / 1000.0) if kms > 0 else None
-    line = {
-        "metric": METRIC, "value": value, "unit": "meshes/s", "n_gpus": ws, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": args.workload, "description": w["desc"], "meshes": b.n_mesh, "items": b.n_points,
-                   "clusters": b.k_total, "faces": int(b.faces.shape[0]), "generation_s": gen_s,
-                   "parallelism": "replicas" if ws > 1 else "single", "l2": "flushed between timed steps (256 MB write)",
-                   "schedule": args.schedule},
-        "roofline": {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": (achieved / peak) if achieved else None,
-                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if "hbm_gbs" in peaks else "fallback",
-                     "traffic": None, "launches": klaunch,
-                     "algorithmic_bytes_per_launch": tot_t["eval_bytes"] / max(1, klaunch),
-                     "avg_launch_us": 1000.0 * kms / max(1, klaunch),
-                     "timing": "CUDA events around each launch, in a second pass of the same steps "
-                               "(the headline pass carries no events)"},
+                         f"sequential converged solves from the reference's own sampling ({secs:.2f} s)"}
+    cfg = workload_config(name, w["desc"], sum(B.spec_items(s) for s in specs),
+                          sum(max(1, B.spec_items(s) // 20) for s in specs),
+                          sum(B.spec_faces(s) for s in specs), ws, batch=True)
+    return {
+        "metric": METRIC, "value": value, "unit": "meshes/s", "n_gpus": ws, "steps": steps,
+        "warmup": warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": cfg,
+        "schedule": args.schedule, "meshes_per_rank": [len(p) for p in parts], "items_per_rank": loads,
+        "generation_s": gen_s,
+        "roofline": roofline_block(persistent, tot_t, name),
         "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(tot["kernel_launches"]),
-        "sweeps_per_step": tot["sweeps"] / max(1, args.steps),
-        "relaxed_sweeps_per_step": tot["relaxed_sweeps"] / max(1, args.steps),
-        "items_per_s": ws * b.n_points / (ms / 1000.0),
-        "energy": energy, "mesh_energy_total": float(np.sum(mesh_e)), "clocks": clk.summary(),
+        "sweeps_per_step": tot["sweeps"] / max(1, steps),
+        "relaxed_sweeps_per_step": tot["relaxed_sweeps"] / max(1, steps),
+        "items_per_s": cfg["items"] / (ms / 1000.0),
+        "energy": energy, "mesh_energy_total_rank0": float(np.sum(mesh_e)), "clocks": clk.summary(),
     }
-    print(json.dumps(line), flush=True)
 
 
-def run_gpu_arm(args):
+def run_batch_arm(args):
     import torch
-    import acvd_gb300
+    ws, rank, local = _dist()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        replicas.init("nccl")
+    line = batch_line(args, args.workload, args.steps, args.warmup, not args.no_e2e, not args.no_cpu_baseline)
+    if line is not None:
+        print(json.dumps(line), flush=True)
+
+
+def clustering_line(args, name, steps, warmup, e2e_on, cpu_on):
+    """One single-mesh clustering workload on this rank's GPU: the headline pass, the
+    instrumented pass (roofline), the end-to-end pass through the C ABI from pinned
+    host buffers, and on rank 0 the checks against the oracle.  Returns the JSON line
+    on rank 0, None elsewhere."""
+    import torch
     from acvd_gb300 import engine as E
 
-    ws, rank, local = _dist()
-    if ws > 1:
-        torch.cuda.set_device(local)
-        replicas.init("nccl")
-    device = local
-    torch.cuda.set_device(device)
-
-    m, ind, pd, w = make_workload(args.workload)
+    ws, rank, device = _dist()
+    m, ind, pd, w = make_workload(name)
     lab0, (row, col, ev) = initial_labels(m, w["metric"], ind, w["gradation"], w["k"], w.get("init"))
     n = m.n_points
-
     persistent = args.schedule == "persistent"
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=f"cuda:{device}")
 
@@ -960,22 +1121,23 @@ def run_gpu_arm(args):
     # pass 1 (the headline): no instrumentation inside the sweeps
     eng = make_engine(False)
     with ClockSampler(device) as clk:
-        step_ms, tot, st = run_steps(torch, eng, args.steps, args.warmup, device, ws, flush)
+        step_ms, tot, st = run_steps(torch, eng, steps, warmup, device, ws, flush)
     ms = statistics.mean(step_ms)
+    lab = eng.labels()
+    eng.close()
     # pass 2 (the roofline): the same steps with CUDA events around every evaluation
     # kernel (event nodes inside the sweep graph; on the persistent schedule the
     # events bracket each persistent launch)
     engt = make_engine(True)
-    _, tot_t, _ = run_steps(torch, engt, args.steps, 1, device, ws, flush)
+    _, tot_t, _ = run_steps(torch, engt, steps, 1, device, ws, flush)
     engt.close()
     ms = replicas.max_over_ranks(ms, device=f"cuda:{device}")   # the slowest replica
     value = ws * n / (ms / 1000.0)
-    lab = eng.labels()
     gpu_energy_fp64 = st["energy"]
 
     # end to end through the C ABI with host buffers (copies inside the timed region)
     e2e = None
-    if not args.no_e2e:
+    if e2e_on:
         h2d = (m.points.nbytes + m.faces.astype(np.int32).nbytes + row.nbytes + col.nbytes + ev.nbytes +
                (ind.nbytes if ind is not None else 0) + (pd.nbytes if pd is not None else 0) + lab0.nbytes)
         d2h = lab0.nbytes
@@ -990,7 +1152,7 @@ def run_gpu_arm(args):
         h_pd = pinned(torch, None if pd is None else c(pd, dtype=np.float32))
         h_lab0 = pinned(torch, c(lab0, dtype=np.int32))
         out = pinned(torch, c(lab0, dtype=np.int32))
-        for it in range(max(1, args.steps)):
+        for it in range(max(1, steps)):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             eng2.set_mesh(h_pts, h_faces, h_row, h_col, h_ev)
@@ -1003,87 +1165,106 @@ def run_gpu_arm(args):
             e2e_ms.append(1000.0 * (time.perf_counter() - t0))
         eng2.close()
         assert np.array_equal(out, lab), "end-to-end run differs from the resident run"
-        e2e_val = ws * n / (statistics.mean(e2e_ms) / 1000.0)
-        e2e = {"value": e2e_val, "unit": "items/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-               "ms_per_step": statistics.mean(e2e_ms)}
+        e2e_t = replicas.max_over_ranks(statistics.mean(e2e_ms), device=f"cuda:{device}")
+        e2e = {"value": ws * n / (e2e_t / 1000.0), "unit": "items/s", "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_t}
 
     replicas.barrier()
     if rank != 0:
-        return
+        return None
 
-    # CPU reference run (same workload, same initial clustering) and energy check
+    # the CPU side: a sequential converged solve from the reference's own initial
+    # sampling (oracle only), or the precomputed fixture where that solve is out of budget
     cpu = None
-    energy = {}
-    if not args.no_cpu_baseline and w.get("cpu_sample"):
-        # bounded sample of the same workload (same generator, same items per cluster)
-        smp = dict(w)
-        smp.update(mesh=w["cpu_sample"]["mesh"], k=w["cpu_sample"]["k"])
-        from acvd_gb300 import synth
-        ms_ = synth.make(w["kind"], **smp["mesh"])
-        ind_s = ms_.indicator if ind is not None else None
-        pd_s = ms_.principal_dirs if pd is not None else None
-        lab_s, _ = initial_labels(ms_, w["metric"], ind_s, w["gradation"], smp["k"])
-        p, secs = cpu_reference_run(ms_, ind_s, pd_s, smp, lab_s)
-        cpu = {"value": ms_.n_points / secs, "unit": "items/s", "cores": 1, "kind": "port",
-               "sample": f"{w['kind']} {smp['mesh']} with K={smp['k']} (same items per cluster), one sequential "
-                         f"converged solve ({secs:.2f} s)"}
-        energy = {"note": "the full-size CPU solve is outside the bench budget; energy parity at this size "
-                          "is covered by the parity tests at smaller sizes",
-                  "gpu_energy_fp64_device": gpu_energy_fp64}
-    elif not args.no_cpu_baseline:
-        p, secs = cpu_reference_run(m, ind, pd, w, lab0)
+    fx = fullsize_fixture(name)
+    seeds = reference_seeds(m, w)
+    e_ref, ref_src, init_same = None, None, None
+    if w.get("cpu_sample"):
+        if cpu_on:
+            # bounded sample of the same workload (same generator, same items per cluster)
+            smp = dict(w)
+            smp.update(mesh=w["cpu_sample"]["mesh"], k=w["cpu_sample"]["k"])
+            from acvd_gb300 import synth
+            ms_ = synth.make(w["kind"], **smp["mesh"])
+            ind_s = ms_.indicator if ind is not None else None
+            pd_s = ms_.principal_dirs if pd is not None else None
+            _, secs, _ = cpu_reference_run(ms_, ind_s, pd_s, smp, None)
+            cpu = {"value": ms_.n_points / secs, "unit": "items/s", "cores": 1, "kind": "port",
+                   "sample": f"{w['kind']} {smp['mesh']} with K={smp['k']} (same items per cluster), one "
+                             f"sequential converged solve from the reference's own sampling ({secs:.2f} s)"}
+    elif cpu_on or fx is None:
+        p, secs, lab_init = cpu_reference_run(m, ind, pd, w, seeds)
+        init_same = bool(np.array_equal(lab_init, lab0))
         e_ref, _ = evaluated_energy(w, m.points, m.faces, w["k"], ind, pd, p.labels())
+        ref_src = "CPU solve in this run (oracle, from the reference's own initial sampling)"
+        if cpu_on:
+            cpu = {"value": n / secs, "unit": "items/s", "cores": 1, "kind": "port",
+                   "sample": f"full workload, one sequential converged solve ({secs:.2f} s)"}
+    if e_ref is None and fx is not None:
+        e_ref = fx["reference_energy"]
+        init_same = labels_sha(lab0) == fx["labels0_sha256"] if seeds is None else None
+        ref_src = ("tests/golden/fullsize/" + name + ".json (oracle converged solve from the reference's own "
+                   "initial sampling, precomputed)")
+    energy = {"gpu_energy_fp64_device": gpu_energy_fp64}
+    if e_ref is not None:
+        t0 = time.perf_counter()
         e_gpu, chk = evaluated_energy(w, m.points, m.faces, w["k"], ind, pd, lab)
         connected = chk.clean() == 0
-        cpu = {"value": n / secs, "unit": "items/s", "cores": 1, "kind": "port",
-               "sample": f"full workload, one sequential converged solve ({secs:.2f} s)"}
-        energy = {"reference_energy": e_ref, "gpu_energy_reference_arithmetic": e_gpu,
-                  "gpu_energy_fp64_device": gpu_energy_fp64,
-                  "rel_diff": (e_gpu - e_ref) / abs(e_ref), "within_0.1pct": bool(e_gpu <= e_ref + 1e-3 * abs(e_ref)),
-                  "all_clusters_connected": bool(connected)}
-
-    peaks = {}
-    try:
-        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-    except (OSError, ValueError):
-        pass
-    peak = peaks.get("hbm_gbs", 6800.0)
-    kname, kms, klaunch = roofline_kernel(persistent, tot_t)
-    achieved = (tot_t["eval_bytes"] / 1e9) / (kms / 1000.0) if kms > 0 else None
-    traffic = None
-    tpath = os.path.join(ROOT, "profiles", "eval_traffic.json")
-    if os.path.exists(tpath):
-        try:
-            traffic = json.load(open(tpath)).get(args.workload)
-        except ValueError:
-            traffic = None
-    line = {
-        "metric": METRIC, "value": value, "unit": "items/s", "n_gpus": ws, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        energy.update({
+            "reference_energy": e_ref, "reference_source": ref_src,
+            "gpu_energy_reference_arithmetic": e_gpu,
+            "rel_diff": (e_gpu - e_ref) / abs(e_ref),
+            "within_0.1pct": bool(e_gpu <= e_ref + 1e-3 * abs(e_ref)),
+            "all_clusters_connected": bool(connected),
+            "all_items_assigned": bool(np.all(lab < w["k"])),
+            "initial_clustering_identical_to_reference": init_same,
+            # the device's FP32-item / compensated-sum energy of the same clustering against
+            # the FP64 evaluation
+            "device_vs_fp64_rel_err": abs(gpu_energy_fp64 - e_gpu) / abs(e_gpu),
+            "check_s": time.perf_counter() - t0})
+    return {
+        "metric": METRIC, "value": value, "unit": "items/s", "n_gpus": ws, "steps": steps,
+        "warmup": warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": args.workload, "description": w["desc"], "items": n, "clusters": w["k"],
-                   "faces": m.n_faces, "parallelism": "replicas" if ws > 1 else "single",
-                   "l2": "flushed between timed steps (256 MB write)", "schedule": args.schedule},
-        "roofline": {"bound": "hbm", "kernel": kname, "achieved": achieved,
-                     "peak": peak, "unit": "GB/s", "frac": (achieved / peak) if achieved else None,
-                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if "hbm_gbs" in peaks else "fallback",
-                     "traffic": traffic, "launches": klaunch,
-                     "algorithmic_bytes_per_launch": tot_t["eval_bytes"] / max(1, klaunch),
-                     "avg_launch_us": 1000.0 * kms / max(1, klaunch),
-                     "timing": "CUDA events around each launch, in a second pass of the same steps "
-                               "(the headline pass carries no events)"},
+        "config": workload_config(name, w["desc"], n, w["k"], m.n_faces, ws),
+        "schedule": args.schedule,
+        "roofline": roofline_block(persistent, tot_t, name),
         "cpu_baseline": cpu,
         "e2e": e2e,
         "gpu_launches": int(tot["kernel_launches"]),
-        "sweeps_per_step": tot["sweeps"] / max(1, args.steps),
-        "moves_per_step": tot["moves"] / max(1, args.steps),
+        "sweeps_per_step": tot["sweeps"] / max(1, steps),
+        "moves_per_step": tot["moves"] / max(1, steps),
         "hit_loop_cap": bool(tot["hit_loop_cap"]),
-        "reverted_per_step": tot["reverted"] / max(1, args.steps),
-        "relaxed_sweeps_per_step": tot["relaxed_sweeps"] / max(1, args.steps),
+        "reverted_per_step": tot["reverted"] / max(1, steps),
+        "relaxed_sweeps_per_step": tot["relaxed_sweeps"] / max(1, steps),
         "energy": energy,
         "clocks": clk.summary(),
     }
-    print(json.dumps(line), flush=True)
+
+
+DEFAULT_WORKLOAD = "torus_1024x512_qem"
+# the default run adds the configurations the HBM roofline is judged on (single GPU only)
+EXTRA_WORKLOADS = ("heightfield_4096_aniso", "batch_256_qem")
+
+
+def run_gpu_arm(args):
+    import torch
+    ws, rank, local = _dist()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        replicas.init("nccl")
+    line = clustering_line(args, args.workload, args.steps, args.warmup, not args.no_e2e, not args.no_cpu_baseline)
+    if args.workload == DEFAULT_WORKLOAD and ws == 1 and not args.no_extra:
+        extra = {}
+        xs = min(args.steps, EXTRA_STEPS)
+        for name in EXTRA_WORKLOADS:
+            if name in BATCH_WORKLOADS:
+                extra[name] = batch_line(args, name, xs, 3, not args.no_e2e, False)
+            else:
+                extra[name] = clustering_line(args, name, xs, 3, not args.no_e2e, False)
+        line["extra_workloads"] = extra
+    if line is not None:
+        print(json.dumps(line), flush=True)
 
 
 def solve_once(args):
@@ -1119,6 +1300,8 @@ def main():
                     sorted(CURVATURE_WORKLOADS) + sorted(SUBDIVISION_WORKLOADS) + sorted(MANIFOLD_WORKLOADS))
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="default workload only: skip the heightfield 4096^2 and batch lines added to it")
     ap.add_argument("--solve-once", action="store_true",
                     help="set up and run one converged solve of a clustering workload, untimed (for ncu)")
     args = ap.parse_args()

@@ -261,14 +261,19 @@ int acvd_get_boundary_edges(acvd_ctx* ctx, int32_t* ids, int64_t* count);
 /*
  * The boundary edges of acvd_get_boundary_edges with no device allocation.  It
  * has no counterpart in the reference; it serves callers that hold the edge
- * table and the labels on the device already and must not allocate.
+ * table and the labels on the device already and must not allocate: a caller
+ * that enqueues it inside its own stream-ordered loop, where the cudaFree of
+ * acvd_get_boundary_edges would synchronise the whole device, or one whose
+ * device memory is held by a caching allocator, where a cudaMalloc can fail.
  * Inputs are DEVICE arrays on the current device: d_edge_v[2 n_edges] (edge
  * endpoints, reference edge numbering), d_labels[nV]; outputs d_ids[n_edges]
  * (boundary edge ids, increasing) and d_count[1].  Enqueued on `stream` (a
  * cudaStream_t; NULL = the default stream) and returns without waiting.
  * Scratch is a fixed 256 KiB device array per device: no cudaMalloc, no
- * cudaFree.  The first call on a device looks that array up (set-up); make it
- * before any stream capture.  Calls on one device share the array, so calls
+ * cudaFree.  The first call on a device looks that array's address up (set-up)
+ * and keeps it for the process; make it before any stream capture.  After a
+ * cudaDeviceReset of that device the kept address is stale: do not call this
+ * entry point again in that process.  Calls on one device share the array, so calls
  * that overlap in time (other streams, other threads) race: serialise them.
  * n_edges above ACVD_NOALLOC_MAX_EDGES returns ACVD_ERR_UNSUPPORTED with
  * nothing enqueued.

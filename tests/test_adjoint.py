@@ -1,7 +1,8 @@
 """GPU adjoint against the FP64 references (needs a GB300).
 
 Fixed clustering of a bumped torus with densities U[0.5, 2] as the indicator
-(gradation 1, weights = area * rho):
+(gradation 1, weights = area * rho), at 128x64 with K = 600 and at the adjoint
+workload's full size (512x512, 262,144 items, K = 10,000):
   * the energy equals the oracle's evaluation of the clustering (1e-10 relative);
   * gradients of  E + sum_k G_k . c_k  match the FP64 torch reference for every
     coordinate and density (1e-6 of the largest component);
@@ -19,10 +20,13 @@ from acvd_gb300.adjoint import ClusteringEnergy, cluster_energies, reference_ene
 pytestmark = pytest.mark.gpu
 
 
-@pytest.fixture(scope="module")
-def setup(oracle_lib):
-    m = synth.torus(128, 64, seed=5)
-    k = 600
+SIZES = {"torus128x64_k600": (128, 64, 5, 600), "torus512x512_k10000": (512, 512, 0, 10000)}
+
+
+@pytest.fixture(scope="module", params=sorted(SIZES))
+def setup(oracle_lib, request):
+    nu, nv, seed, k = SIZES[request.param]
+    m = synth.torus(nu, nv, seed=seed)
     rho = np.random.default_rng(3).uniform(0.5, 2.0, m.n_points)
     p = oracle_lib.Port("qem", m.points, m.faces, k, 1.0, rho, unconstrained_init=1)
     p.init(None)

@@ -65,6 +65,24 @@ def test_approximate_schedules_opt_in_and_energy_bar():
     assert "outside" in trial["exact_sweeps"]["reason"]
 
 
+def test_cached_approximate_choice_not_returned_to_a_default_tuner(tmp_path):
+    path = str(tmp_path / "tune.json")
+    times = {"graphs": [3.0], "host_loop": [3.5], "persistent": [3.2], "exact_sweeps": [2.5], "match2": [1.0]}
+    measure, _ = _fake(times, digests={"exact_sweeps": "x", "match2": "y"})
+    s, _ = at.Autotuner(path, include_approximate=True).tune("k", measure)
+    assert s.name == "match2"
+    # a default (exact-only) tuner on the same file must not answer with match2
+    measure2, calls2 = _fake(times)
+    s2, rep2 = at.Autotuner(path).tune("k", measure2)
+    assert s2.exact and not rep2["cached"] and calls2 == ["graphs", "host_loop", "persistent"]
+    # an opt-in tuner with a tighter tolerance than the cached choice's measures again
+    at.Autotuner(path, include_approximate=True).tune("k2", _fake(times, digests={"match2": "y"})[0])
+    tight = at.Autotuner(path, include_approximate=True, energy_rel_tol=1e-4)
+    assert tight.lookup("k2") is None
+    # the same tolerance answers from the cache
+    assert at.Autotuner(path, include_approximate=True).lookup("k2").name == "match2"
+
+
 def test_unassigned_items_and_errors_reject_a_candidate():
     measure, _ = _fake({"graphs": [3.0], "host_loop": [1.0], "persistent": [2.0]},
                        unassigned={"host_loop": 5}, fail=("persistent",))

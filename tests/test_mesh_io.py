@@ -283,3 +283,18 @@ def test_custom_density_indicator(tmp_path, kind):
     with pytest.raises(acvd_gb300.AcvdError):
         E.density_indicator(str(tmp_path / "v.mnc"), pts)
 
+
+
+@pytest.mark.parametrize("header", [
+    "DimSize = 4294967296 4294967296 16\n",                        # 2^68 voxels: the byte count would wrap
+    "DimSize = 7 5 4\nElementNumberOfChannels = 4611686018427387904\n",   # channels x size would wrap
+    "DimSize = 100000 100000 100000\n",                             # above the voxel cap
+])
+def test_oversized_density_volume_is_refused(tmp_path, header):
+    """DimSize / ElementNumberOfChannels whose byte count would overflow are refused
+    before any data is read (ACVD_ERR_ARG), not wrapped into a short read."""
+    (tmp_path / "big.mha").write_bytes((
+        "ObjectType = Image\nNDims = 3\n" + header + "ElementType = MET_UCHAR\nElementDataFile = LOCAL\n").encode()
+        + bytes(64))
+    with pytest.raises(acvd_gb300.AcvdError):
+        E.density_indicator(str(tmp_path / "big.mha"), np.zeros((3, 3)))

@@ -68,3 +68,34 @@ def test_cluster_sizes():
 def test_engine_takes_the_convergence_cap():
     o = acvd_gb300.engine.Opts()
     assert [f[0] for f in o._fields_].index("max_convergences") == 3
+
+
+@pytest.mark.gpu
+def test_identity_sampling_solves_and_cap_stops_the_loop(oracle_lib):
+    """Type -1 (item i seeds cluster i, the rest unassigned,
+    Common/vtkUniformClustering.h:1139-1157) through a whole Remesh(): hole filling
+    assigns every item and the clusters come out connected; and
+    SetMaxNumberOfConvergences(1) ends a real solve at its first convergence."""
+    m = synth.icosphere(3, seed=4)
+    k = 40
+    r = acvd_gb300.IsotropicDiscreteRemeshing.New()
+    r.SetInput(acvd_gb300.Surface(m.points, m.faces))
+    r.SetNumberOfClusters(k)
+    r.SetInitialSamplingType(-1)
+    r.Remesh()
+    lab = np.asarray(r.GetClustering())
+    assert np.all(lab < k)
+    ev = oracle_lib.Port("iso", m.points, m.faces, k)
+    ev.evaluate(lab, 1)
+    assert ev.clean() == 0
+    capped = acvd_gb300.QIsotropicDiscreteRemeshing.New()
+    capped.SetInput(acvd_gb300.Surface(m.points, m.faces))
+    capped.SetNumberOfClusters(k)
+    capped.SetMaxNumberOfConvergences(1)
+    capped.Remesh()
+    assert capped.Stats["convergences"] == 1
+    free = acvd_gb300.QIsotropicDiscreteRemeshing.New()
+    free.SetInput(acvd_gb300.Surface(m.points, m.faces))
+    free.SetNumberOfClusters(k)
+    free.Remesh()
+    assert free.Stats["convergences"] > 1
