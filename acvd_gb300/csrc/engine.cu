@@ -1,6 +1,7 @@
 // Host orchestration of the GPU clustering (the MinimizeEnergy() seam) and the
 // C ABI declared in include/acvd_gpu.h.
 #include <algorithm>
+#include <cmath>
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
@@ -1135,6 +1136,40 @@ static int energy_total(acvd_ctx* ctx, double* out) {
     return ACVD_OK;
 }
 
+// Algorithmic bytes of the evaluation kernels from the device counters: per visited
+// item its boundary flag; per screened item its 8-slot ring, label and evaluation
+// sweep; per ring slot the neighbour's label; per cached screen its cache entry, label,
+// evaluation sweep and up to 3 cluster stamps; per boundary item its record, its
+// cluster's record and size; per destination cluster its record; per proposal the
+// candidate slots and two claim words.
+static int64_t eval_bytes_of(const acvd_ctx* ctx, const unsigned long long* c) {
+    const int64_t R = ctx->metric == kIso ? 16 : (ctx->metric == kQEM ? 40 : 64);
+    const int64_t C = 16 * (int64_t)ev_stride(ctx->metric);
+    return 1 * (int64_t)c[kCntVisited] + 40 * (int64_t)c[kCntScreened] + 36 * (int64_t)c[kCntCached] +
+           4 * (int64_t)c[kCntSlots] + (R + C + 4) * (int64_t)c[kCntBoundary] + C * (int64_t)c[kCntTargets] +
+           24 * (int64_t)c[kCntCand];
+}
+
+// the per-sweep log's snapshot of the cumulative counters
+struct SweepCounters {
+    unsigned long long c[kNumCounters] = {};
+    void take(const acvd_ctx* ctx) {
+        for (int q = 0; q < kNumCounters; q++) c[q] = ctx->h_counters[q];
+    }
+    long long d(const SweepCounters& o, int q) const { return (long long)(c[q] - o.c[q]); }
+    int64_t eval_bytes(const acvd_ctx* ctx) const { return eval_bytes_of(ctx, c); }
+};
+
+struct SweepLogFile {
+    FILE* f = nullptr;
+    explicit SweepLogFile(const char* path) {
+        if (path && *path) f = std::fopen(path, "a");
+    }
+    ~SweepLogFile() {
+        if (f) std::fclose(f);
+    }
+};
+
 extern "C" int acvd_minimize(acvd_ctx* ctx, acvd_stats* stats) {
     if (!ctx) return ACVD_ERR_ARG;
     if (!ctx->ready_mesh || !ctx->ready_metric || !ctx->ready_labels)
@@ -1142,7 +1177,12 @@ extern "C" int acvd_minimize(acvd_ctx* ctx, acvd_stats* stats) {
     CK(cudaSetDevice(ctx->opts.device));
     acvd_stats local;
     std::memset(&local, 0, sizeof local);
-    const bool timing = ctx->opts.kernel_timing != 0;
+    // ACVD_SWEEP_LOG=<path>: one JSON line per sweep and per convergence event is
+    // appended to the file (the sweeps run from the host, with CUDA events around
+    // every evaluation kernel); an observation mode, the clustering is unchanged
+    const char* log_path = std::getenv("ACVD_SWEEP_LOG");
+    SweepLogFile slog(log_path);
+    const bool timing = ctx->opts.kernel_timing != 0 || slog.f != nullptr;
     // ProcessClustering: the unconstrained first phase of the QEM metric (:683-688)
     ctx->flags.constrained = (ctx->metric == kQEM && ctx->unconstrained) ? 0 : 1;
     ctx->flags.connexity = 0;
@@ -1204,6 +1244,15 @@ extern "C" int acvd_minimize(acvd_ctx* ctx, acvd_stats* stats) {
         // graph-looped sweeps unless per-sweep events or the per-sweep trace are wanted
         const bool device_loop = !persistent && !timing && !trace && ctx->opts.use_graphs &&
                                  std::getenv("ACVD_HOST_LOOP") == nullptr;
+        if (slog.f && persistent) {
+            status = fail(ctx, ACVD_ERR_UNSUPPORTED, "ACVD_SWEEP_LOG needs the per-phase schedule");
+            break;
+        }
+        SweepCounters prev_ctr;
+        if (slog.f) {
+            if ((r = sync_counters(ctx))) { status = r; break; }
+            prev_ctr.take(ctx);
+        }
         for (;;) {
             int64_t mods = 0;
             const bool relaxed = relaxed_ok && !ctx->flags.connexity;
@@ -1263,10 +1312,12 @@ extern "C" int acvd_minimize(acvd_ctx* ctx, acvd_stats* stats) {
                 e_prev = hl.e_prev;
                 mods = hl.last_moves;
             } else {
+            const double eval_ms0 = local.eval_ms;
+            const auto t_sweep = std::chrono::steady_clock::now();
             if ((r = run_sweep(ctx, timing, relaxed, &local.eval_ms, &local.eval_launches, &mods))) { status = r; break; }
+            double e_now = 0.0;
             if (relaxed) {
                 local.relaxed_sweeps++;
-                double e_now = 0.0;
                 if ((r = energy_total(ctx, &e_now))) { status = r; break; }
                 if (have_prev && !(e_now < e_prev)) relaxed_ok = false;
                 e_prev = e_now;
@@ -1274,6 +1325,29 @@ extern "C" int acvd_minimize(acvd_ctx* ctx, acvd_stats* stats) {
             }
             sweeps++;
             local.moves += mods;
+            if (slog.f) {
+                const double sweep_ms =
+                    std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_sweep).count();
+                if (!relaxed && (r = energy_total(ctx, &e_now))) { status = r; break; }
+                SweepCounters now_ctr;
+                now_ctr.take(ctx);
+                const double ems = local.eval_ms - eval_ms0;
+                const int64_t bytes = now_ctr.eval_bytes(ctx) - prev_ctr.eval_bytes(ctx);
+                std::fprintf(slog.f,
+                             "{\"sweep\": %d, \"mode\": \"%s\", \"moves\": %lld, \"candidates\": %lld, "
+                             "\"boundary_items\": %lld, \"targets\": %lld, \"visited\": %lld, \"screened\": %lld, "
+                             "\"cached\": %lld, \"reverted\": %lld, \"energy\": %.17g, \"eval_ms\": %.6f, "
+                             "\"eval_bytes\": %lld, \"eval_gbs\": %.3f, \"sweep_ms\": %.6f, \"constrained\": %d, "
+                             "\"connexity\": %d, \"convergences\": %d}\n",
+                             sweeps, relaxed ? "relaxed" : "exact", (long long)mods,
+                             now_ctr.d(prev_ctr, kCntCand), now_ctr.d(prev_ctr, kCntBoundary),
+                             now_ctr.d(prev_ctr, kCntTargets), now_ctr.d(prev_ctr, kCntVisited),
+                             now_ctr.d(prev_ctr, kCntScreened), now_ctr.d(prev_ctr, kCntCached),
+                             now_ctr.d(prev_ctr, kCntReverted), e_now, ems, (long long)bytes,
+                             ems > 0 ? bytes / (ems * 1e6) : 0.0, sweep_ms, ctx->flags.constrained,
+                             ctx->flags.connexity, convergences);
+                prev_ctr = now_ctr;
+            }
             }
             if (trace && !persistent && !device_loop) {
                 const auto now = std::chrono::steady_clock::now();
@@ -1297,6 +1371,18 @@ extern "C" int acvd_minimize(acvd_ctx* ctx, acvd_stats* stats) {
                 if (convergences >= 1 && !ctx->flags.connexity) {
                     ctx->flags.connexity = 1;
                     flags_changed = true;
+                }
+                if (slog.f) {
+                    // the incrementally tracked energy (FP32 items, double-float records)
+                    // against a full FP64 recompute of the same clustering
+                    double e_tracked = 0.0, e_fp64 = 0.0;
+                    if ((r = energy_total(ctx, &e_tracked)) || (r = recompute(ctx)) ||
+                        (r = energy_total(ctx, &e_fp64))) { status = r; break; }
+                    std::fprintf(slog.f,
+                                 "{\"event\": \"convergence\", \"sweep\": %d, \"convergence\": %d, "
+                                 "\"energy_tracked\": %.17g, \"energy_fp64\": %.17g, \"rel_err\": %.6g}\n",
+                                 sweeps, convergences + 1, e_tracked, e_fp64,
+                                 e_fp64 != 0.0 ? std::fabs(e_tracked - e_fp64) / std::fabs(e_fp64) : 0.0);
                 }
                 if (flags_changed && (r = upload_flags(ctx))) { status = r; break; }
                 convergences++;
@@ -1343,20 +1429,7 @@ extern "C" int acvd_minimize(acvd_ctx* ctx, acvd_stats* stats) {
         status = fail(ctx, ACVD_ERR_DEVICE_CHECK,
                       std::to_string(ctx->h_counters[kCntError]) + " device-side index checks failed");
     local.reverted = (int64_t)ctx->h_counters[kCntReverted];
-    {
-        // algorithmic bytes of the evaluation kernels: per visited item its boundary
-        // flag; per screened item its 8-slot ring, label and evaluation sweep; per
-        // ring slot the neighbour's label; per cached screen its cache entry, label,
-        // evaluation sweep and up to 3 cluster stamps; per
-        // boundary item its record, its cluster's record and size; per destination
-        // cluster its record; per proposal the candidate slots and two claim words
-        const int64_t R = ctx->metric == kIso ? 16 : (ctx->metric == kQEM ? 40 : 64);
-        const int64_t C = 16 * (int64_t)ev_stride(ctx->metric);
-        const int64_t screened = (int64_t)ctx->h_counters[kCntScreened];
-        const int64_t cached = (int64_t)ctx->h_counters[kCntCached];
-        local.eval_bytes = 1 * local.visited + 40 * screened + 36 * cached + 4 * local.slots +
-                           (R + C + 4) * local.boundary_items + C * local.targets + 24 * local.candidates;
-    }
+    local.eval_bytes = eval_bytes_of(ctx, ctx->h_counters);
     if (status == ACVD_OK) {
         double et = 0.0;
         int rr = acvd_get_clusters(ctx, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, &et);

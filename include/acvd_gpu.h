@@ -235,6 +235,14 @@ int acvd_clean_clustering(acvd_ctx* ctx, int32_t* n_disconnected);
  * reference's stopping rule holds (0 moves in a sweep and 0 disconnected
  * clusters), with its early-convergence, unconstrained->constrained and
  * connectivity phases.  stats may be NULL.
+ * Per-sweep log (the reference's SetWriteToGlobalEnergyLog, Common/vtkUniformClustering.h:
+ * 1384-1395, as JSON lines): with the environment variable ACVD_SWEEP_LOG set to a file
+ * path, every sweep appends {sweep, mode, moves, candidates, boundary_items, targets,
+ * visited, screened, cached, reverted, energy (FP64 sum of the tracked cluster energies),
+ * eval_ms (CUDA events around the evaluation kernels), eval_bytes, eval_gbs, sweep_ms,
+ * constrained, connexity, convergences}, and every convergence event appends
+ * {event, sweep, convergence, energy_tracked, energy_fp64 (a full FP64 recompute of the
+ * same labels), rel_err}.  The sweeps then run from the host; the clustering is the same.
  */
 int acvd_minimize(acvd_ctx* ctx, acvd_stats* stats);
 
