@@ -286,9 +286,14 @@ ACVD_DEV bool ring_connected_pref(const DevState& st, int p0, int p1, int L, con
 // (one work item per thread): the best destination, the acceptance margin, the
 // proposal and its claims.  Unassigned items and items with more than kMaxTgt
 // destinations run the whole test in B2.
+//
+// List mode (entries != nullptr): the tile's items are entries[0 .. n_entries), the
+// colour-list positions a screen_kernel pass forwarded (see below); they were
+// counted as visited there.
 template <int M>
 ACVD_DEV void eval_tile(const DevState& st, int item0, int64_t count, int color,
-                        int* cand_dest, unsigned* cand_prio, int claims, int64_t tile) {
+                        int* cand_dest, unsigned* cand_prio, int claims, int64_t tile,
+                        const int* entries = nullptr, int n_entries = 0) {
     __shared__ int s_idx[256];                 // work item -> colour-list position
     __shared__ int s_tgt[256][kMaxTgt];        // work item -> destination clusters (ring order)
     __shared__ float s_val[256][kMaxTgt + 1];  // energy parts: [j] add to s_tgt[j], [kMaxTgt] remove
@@ -307,8 +312,9 @@ ACVD_DEV void eval_tile(const DevState& st, int item0, int64_t count, int color,
     }
     __syncthreads();
     const int epoch = color * kRounds;   // claim epoch of this step's first matching round
-    const int64_t idx_t = tile * 256 + threadIdx.x;
-    const bool in = idx_t < count;
+    const bool listed = entries != nullptr;
+    const bool in = listed ? (int)threadIdx.x < n_entries : tile * 256 + threadIdx.x < count;
+    const int64_t idx_t = listed ? (in ? (int64_t)entries[threadIdx.x] : 0) : tile * 256 + threadIdx.x;
     const SweepState sw = *st.sweep;
     const RunFlags fl = *st.flags;
     unsigned n_slots = 0, n_bnd = 0, n_tgt = 0, n_cand = 0, n_scr = 0, n_cached = 0;
@@ -597,7 +603,8 @@ ACVD_DEV void eval_tile(const DevState& st, int item0, int64_t count, int color,
         __shared__ unsigned s_wc[8], s_base, s_cnt[8][kNC];
         const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
         const unsigned bal = __ballot_sync(kFull, my_cand >= 0);
-        const unsigned v[kNC] = {in ? 1u : 0u, n_scr - n_cached, n_cached, n_slots, n_bnd, n_tgt, n_cand};
+        const unsigned v[kNC] = {(in && !listed) ? 1u : 0u, n_scr - n_cached, n_cached, n_slots, n_bnd, n_tgt,
+                                 n_cand};
 #pragma unroll
         for (int c = 0; c < kNC; c++) {
             const unsigned t = __reduce_add_sync(kFull, v[c]);
@@ -643,6 +650,136 @@ template <int M>
 __global__ void __launch_bounds__(256, EvalMinBlocks<M>::value) eval_kernel(DevState st, int item0, int64_t count,
                                                       int color, int* cand_dest, unsigned* cand_prio, int claims) {
     eval_tile<M>(st, item0, count, color, cand_dest, cand_prio, claims, blockIdx.x);
+}
+
+// ---------------------------------------------------------------------------
+// Split evaluation of a large colour class: screen_kernel streams the class and
+// settles every item whose screen decides it does nothing -- interior items
+// (boundary flag 0) and cached screens whose clusters did not change since the
+// item's last evaluation, or that cannot move -- exactly as eval_tile's cached
+// path would; the other items (full screens, fresh movable cached screens) are
+// appended to a work list that eval_list_kernel runs through eval_tile.  Each item
+// takes the same decisions as in the fused kernel, so the clustering is the same
+// bit for bit; the screen pass is a plain stream at high occupancy with several
+// items' loads in flight per thread, where the fused kernel's per-tile barriers
+// and energy-test registers left the cached screens latency-bound.
+//
+// Work-list layout: kWorkStripes stripes, block b of the screen pass appends to
+// stripe b % kWorkStripes (one atomic per block, spread over the stripes' counters);
+// stripe s holds its entries at work[s * cap ...], cap = work_cap(count).
+// ---------------------------------------------------------------------------
+constexpr int kScreenItems = kScreenTile / 256;   // items per thread
+
+template <int M>
+__global__ void __launch_bounds__(256, 6) screen_kernel(DevState st, int item0, int64_t count, int color, int* work,
+                                                     unsigned* work_count) {
+    __shared__ int s_list[kScreenTile];
+    __shared__ unsigned s_n, s_base, s_cnt[8][3];
+    if (threadIdx.x == 0) s_n = 0u;
+    const SweepState sw = *st.sweep;
+    const RunFlags fl = *st.flags;
+    const int64_t base = (int64_t)blockIdx.x * kScreenTile + threadIdx.x;
+    unsigned char bf[kScreenItems];
+    int L[kScreenItems], ev_i[kScreenItems];
+    int4 c[kScreenItems];
+    // every item's flag, then every cached item's screen inputs, before any is used
+#pragma unroll
+    for (int u = 0; u < kScreenItems; u++) {
+        const int64_t idx = base + u * 256;
+        bf[u] = idx < count ? st.bflag[item0 + idx] : (unsigned char)0;
+    }
+#pragma unroll
+    for (int u = 0; u < kScreenItems; u++) {
+        if (bf[u] == 2) {
+            const int i = item0 + (int)(base + u * 256);
+            L[u] = st.label[i];
+            ev_i[u] = st.evald[i];
+            c[u] = st.tcache[i];
+        } else {
+            L[u] = 0;
+            ev_i[u] = 0;
+            c[u] = make_int4(0, 0, 0, 0);
+        }
+    }
+    unsigned n_visit = 0, n_cached = 0, n_bnd = 0;
+    bool fwd[kScreenItems];
+#pragma unroll
+    for (int u = 0; u < kScreenItems; u++) {
+        const int64_t idx = base + u * 256;
+        n_visit += idx < count ? 1u : 0u;
+        fwd[u] = bf[u] == 1;
+        if (bf[u] != 2 || !ACVD_VALID(st, L[u] >= 0 && L[u] <= st.k)) continue;
+        const int n = c[u].w & 3;
+        const bool conn_known = (c[u].w & 4) != 0, conn_ok = (c[u].w & 8) != 0;
+        const bool may_move = st.size[L[u]] > 1 && !(st.frozen && st.frozen[L[u]]);
+        if (fl.connexity && may_move && !conn_known) {
+            fwd[u] = true;   // the connectivity test is not cached: a full screen
+            continue;
+        }
+        const int tg[3] = {c[u].x, c[u].y, c[u].z};
+        bool fresh = ev_i[u] <= sw.floor || st.stamp[L[u]] >= ev_i[u];
+#pragma unroll
+        for (int q = 0; q < 3; q++)
+            if (q < n && st.stamp[tg[q]] >= ev_i[u]) fresh = true;
+        if (fresh && may_move && (!fl.connexity || conn_ok)) {
+            fwd[u] = true;   // an energy test to run: the work list
+            continue;
+        }
+        n_cached++;
+        if (fresh) {
+            n_bnd++;
+            st.evald[item0 + (int)idx] = sw.sweep;   // evaluated: nothing it may do
+        }
+    }
+    __syncthreads();   // s_n initialised
+#pragma unroll
+    for (int u = 0; u < kScreenItems; u++)
+        if (fwd[u]) s_list[atomicAdd(&s_n, 1u)] = (int)(base + u * 256);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const unsigned v[3] = {n_visit, n_cached, n_bnd};
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+        const unsigned t = __reduce_add_sync(kFull, v[q]);
+        if (lane == 0) s_cnt[wid][q] = t;
+    }
+    __syncthreads();
+    const int stripe = (int)(blockIdx.x % kWorkStripes);
+    if (threadIdx.x == 0) s_base = s_n ? atomicAdd(&work_count[color * kWorkStripes + stripe], s_n) : 0u;
+    if (threadIdx.x >= 32 && threadIdx.x < 35) {
+        const int q = threadIdx.x - 32;
+        const int which = q == 0 ? kCntVisited : (q == 1 ? kCntCached : kCntBoundary);
+        unsigned t = 0;
+        for (int w = 0; w < 8; w++) t += s_cnt[w][q];
+        if (t) atomicAdd(ctr(st.counters, which), (unsigned long long)t);
+    }
+    __syncthreads();
+    int* out = work + stripe * work_cap(count) + s_base;
+    for (unsigned j = threadIdx.x; j < s_n; j += 256) out[j] = s_list[j];
+}
+
+// The work list of a screen_kernel pass through eval_tile, 256 entries per tile,
+// grid-stride over (stripe, tile) pairs.
+template <int M>
+__global__ void __launch_bounds__(256, EvalMinBlocks<M>::value) eval_list_kernel(DevState st, int item0, int64_t count,
+                                                                              int color, int* cand_dest,
+                                                                              unsigned* cand_prio, int claims,
+                                                                              const int* work,
+                                                                              const unsigned* work_count) {
+    __shared__ unsigned s_cnt[kWorkStripes];
+    if (threadIdx.x < kWorkStripes) s_cnt[threadIdx.x] = work_count[color * kWorkStripes + threadIdx.x];
+    __syncthreads();
+    unsigned mx = 0;
+    for (int q = 0; q < kWorkStripes; q++) mx = max(mx, s_cnt[q]);
+    const int64_t per = (mx + 255) / 256;   // tiles of the fullest stripe
+    const int64_t cap = work_cap(count);
+    for (int64_t t = blockIdx.x; t < per * kWorkStripes; t += gridDim.x) {
+        const int q = (int)(t % kWorkStripes);
+        const int64_t j = t / kWorkStripes;
+        const int64_t have = (int64_t)s_cnt[q] - j * 256;
+        if (have <= 0) continue;   // block-uniform
+        eval_tile<M>(st, item0, count, color, cand_dest, cand_prio, claims, t, work + q * cap + j * 256,
+                     have < 256 ? (int)have : 256);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -1130,6 +1267,8 @@ __global__ void begin_sweep_kernel(DevState st, int ncolors, int reset_claims) {
     if (blockIdx.x == 0) {
         if (t == 0) st.sweep->sweep += 1;
         if (t < ncolors) st.cand_count[t] = 0u;
+        if (st.work_count)
+            for (int j = t; j < ncolors * kWorkStripes; j += blockDim.x) st.work_count[j] = 0u;
         if (t < kStripes) st.counters[t * kNumCounters + kCntMoves] = 0ull;   // this sweep's moves
     }
     if (reset_claims)
@@ -1692,11 +1831,32 @@ static inline unsigned nblk(int64_t n, int b = 256) { return (unsigned)((n + b -
         else KERNEL<kAniso><<<grid, block, 0, stream>>>(__VA_ARGS__);                     \
     } while (0)
 
+static int64_t sm_count();
+
+// Blocks per SM of eval_list_kernel (its grid strides over the work list).
+static int eval_list_blocks_per_sm(int metric) {
+    int nb = 0;
+    cudaError_t e;
+    if (metric == kIso) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, eval_list_kernel<kIso>, 256, 0);
+    else if (metric == kQEM) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, eval_list_kernel<kQEM>, 256, 0);
+    else e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, eval_list_kernel<kAniso>, 256, 0);
+    return (e == cudaSuccess && nb > 0) ? nb : 1;
+}
+
 cudaError_t launch_eval(int metric, const DevState& st, int item0, int64_t count, int color,
-                        int* cand_dest, unsigned* cand_prio, bool claims, cudaStream_t s) {
+                        int* cand_dest, unsigned* cand_prio, bool claims, bool split, cudaStream_t s) {
     if (count == 0) return cudaSuccess;
-    ACVD_DISPATCH(metric, eval_kernel, nblk(count), 256, s, st, item0, count, color, cand_dest, cand_prio,
-                  claims ? 1 : 0);
+    if (!split) {
+        ACVD_DISPATCH(metric, eval_kernel, nblk(count), 256, s, st, item0, count, color, cand_dest, cand_prio,
+                      claims ? 1 : 0);
+        return cudaGetLastError();
+    }
+    ACVD_DISPATCH(metric, screen_kernel, nblk(count, kScreenTile), 256, s, st, item0, count, color, st.work,
+                  st.work_count);
+    const int64_t tiles = kWorkStripes * (work_cap(count) / 256);
+    const unsigned grid = (unsigned)std::min<int64_t>(tiles, sm_count() * eval_list_blocks_per_sm(metric));
+    ACVD_DISPATCH(metric, eval_list_kernel, grid, 256, s, st, item0, count, color, cand_dest, cand_prio,
+                  claims ? 1 : 0, (const int*)st.work, (const unsigned*)st.work_count);
     return cudaGetLastError();
 }
 

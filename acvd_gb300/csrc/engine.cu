@@ -56,6 +56,11 @@ struct acvd_ctx {
     int ncolors = 0;
     std::vector<int64_t> color_off;
     DBuf<int> color_items, cand_dest, cand_list;
+    // split evaluation of large colour classes (screen pass + work list)
+    DBuf<int> work;
+    DBuf<unsigned> work_count;
+    int64_t split_min = 0;
+    bool has_work = false;
     // internal item order: colour classes contiguous (perm: item -> original
     // vertex id, inv: original vertex id -> item); faces and edges in item ids
     DBuf<int> perm, inv, tri_int, edge_int, label_orig;
@@ -203,6 +208,8 @@ struct acvd_ctx {
         st.anchor_xyz = has_anchor ? anchor_xyz.p : nullptr;
         st.nfixed = (int)h_fixed.size();
         st.fixed = h_fixed.empty() ? nullptr : fixed_item.p;
+        st.work = has_work ? work.p : nullptr;
+        st.work_count = has_work ? work_count.p : nullptr;
         return st;
     }
     cudaGraphExec_t relaxed_exec = nullptr;
@@ -282,13 +289,51 @@ static cudaError_t zero_counter(acvd_ctx* ctx, int which) {
 // ---------------------------------------------------------------------------
 // setup
 // ---------------------------------------------------------------------------
-static int setup_colors(acvd_ctx* ctx) {
+// Colour classes from this size on run the split evaluation: about four waves of
+// the fused evaluation kernel's blocks on a 152-SM GB300.  Smaller classes (the
+// 1024 x 512 torus has about 120,000 items per class) are latency-bound, and a
+// second kernel per colour step would cost more than it saves.
+constexpr int64_t kDefaultSplitMin = 600000;
+
+// Greedy colouring in vertex order on the host: each vertex takes the smallest
+// colour unused by its lower-numbered neighbours.  On meshes stored in a spatially
+// coherent order (grids, scans) it gives 4 balanced classes where the device's
+// hashed Jones-Plassmann colouring gives 6-7 with a few tiny ones.  Returns the
+// largest colour, or -1 when a vertex would need a 65th colour.
+static int greedy_colors_host(const int32_t* row, const int32_t* col, int64_t n, std::vector<int>& color) {
+    color.assign(n, -1);
+    int maxc = 0;
+    for (int64_t v = 0; v < n; v++) {
+        unsigned long long used = 0ull;
+        for (int p = row[v]; p < row[v + 1]; p++) {
+            const int c = color[col[p]];
+            if (c >= 0) used |= 1ull << c;
+        }
+        if (used == ~0ull) return -1;
+        const int c = __builtin_ctzll(~used);
+        color[v] = c;
+        maxc = std::max(maxc, c);
+    }
+    return maxc;
+}
+
+static int setup_colors(acvd_ctx* ctx, const int32_t* h_row, const int32_t* h_col) {
     const int64_t n = ctx->nV;
     CK(ctx->wk_int.resize(n));
     CK(cudaMemsetAsync(ctx->wk_int.p, 0xff, n * sizeof(int), ctx->s));   // color = -1
     CK(ctx->dtmp.resize(2));
     int* d_maxc = (int*)ctx->dtmp.p;
     CK(cudaMemsetAsync(d_maxc, 0, sizeof(int), ctx->s));
+    // ACVD_COLORING=order: the host greedy colouring in vertex order instead
+    const char* how = std::getenv("ACVD_COLORING");
+    if (how && std::strcmp(how, "order") == 0) {
+        std::vector<int> hc;
+        const int mc = greedy_colors_host(h_row, h_col, n, hc);
+        if (mc < 0) return fail(ctx, ACVD_ERR_UNSUPPORTED, "more than 64 colours needed (vertex valence too high)");
+        CK(cudaMemcpyAsync(ctx->wk_int.p, hc.data(), n * sizeof(int), cudaMemcpyHostToDevice, ctx->s));
+        CK(cudaMemcpyAsync(d_maxc, &mc, sizeof(int), cudaMemcpyHostToDevice, ctx->s));
+        CK(cudaStreamSynchronize(ctx->s));
+    }
     // rounds in groups of four between host checks (a round after the last one
     // finds every item coloured and does nothing); the count left is the last
     // round's number of items still waiting for a neighbour
@@ -367,6 +412,24 @@ static int setup_colors(acvd_ctx* ctx) {
     }
     ctx->nclasses = (int)ctx->sweep_off.size() - 1;
     CK(cudaStreamSynchronize(ctx->s));
+    // classes of at least split_min items run the split evaluation (screen pass +
+    // work list); ACVD_SPLIT_MIN overrides the threshold (0 = never split)
+    {
+        ctx->split_min = kDefaultSplitMin;
+        if (const char* e = std::getenv("ACVD_SPLIT_MIN")) ctx->split_min = std::atoll(e);
+        int64_t wmax = 0;
+        for (int c = 0; c < ctx->nclasses; c++) {
+            const int64_t cnt = ctx->sweep_off[c + 1] - ctx->sweep_off[c];
+            if (ctx->split_min > 0 && cnt >= ctx->split_min)
+                wmax = std::max<int64_t>(wmax, kWorkStripes * work_cap(cnt));
+        }
+        if (wmax > 0) {
+            CK(ctx->work.resize(wmax));
+            CK(ctx->work_count.resize(64 * kWorkStripes));
+            CK(cudaMemsetAsync(ctx->work_count.p, 0, 64 * kWorkStripes * sizeof(unsigned), ctx->s));
+        }
+        ctx->has_work = wmax > 0;
+    }
     CK(ctx->cand_dest.resize(mx));
     CK(ctx->cand_prio.resize(mx));
     CK(ctx->cand_list.resize(mx));
@@ -487,7 +550,7 @@ int acvd_set_mesh(acvd_ctx* ctx, int64_t n_vertices, const double* xyz, int64_t 
         CK(launch_segment_offsets(k1.p, 3 * n_faces, (uint32_t)n_vertices, ctx->vf_row.p, ctx->s));
     }
     // colouring on the input rings, then the items in internal order
-    int r = setup_colors(ctx);
+    int r = setup_colors(ctx, csr_row, csr_col);
     if (r) return r;
     int* d_maxdeg = nullptr;
     CK(ctx->dtmp.resize(2));
@@ -890,7 +953,9 @@ static int enqueue_sweep(acvd_ctx* ctx, bool timing, bool relaxed) {
         if (cnt == 0) continue;
         // cudaEventRecordExternal makes the records real graph nodes when captured
         if (timing) CK(cudaEventRecordWithFlags(ctx->ev_eval[2 * c], ctx->s, cudaEventRecordExternal));
-        CK(launch_eval(ctx->metric, st, item0, cnt, c, ctx->cand_dest.p, ctx->cand_prio.p, !relaxed, ctx->s));
+        const bool split = ctx->has_work && ctx->split_min > 0 && cnt >= ctx->split_min;
+        CK(launch_eval(ctx->metric, st, item0, cnt, c, ctx->cand_dest.p, ctx->cand_prio.p, !relaxed, split, ctx->s));
+        if (split) kernels++;
         if (timing) CK(cudaEventRecordWithFlags(ctx->ev_eval[2 * c + 1], ctx->s, cudaEventRecordExternal));
         if (relaxed) {
             CK(launch_relaxed_step(ctx->metric, st, item0, cnt, c, ctx->cand_dest.p, ctx->s));

@@ -103,6 +103,16 @@ struct SweepState {
     int floor;
 };
 
+// Work list of the split evaluation (screen_kernel -> eval_list_kernel): stripes
+// and the items one screen block covers; stripe s of a class of `count` items holds
+// its entries at [s * work_cap(count), (s + 1) * work_cap(count)).
+constexpr int kWorkStripes = 16;
+constexpr int kScreenTile = 1024;
+__host__ __device__ inline int64_t work_cap(int64_t count) {
+    const int64_t nb = (count + kScreenTile - 1) / kScreenTile;
+    return ((nb + kWorkStripes - 1) / kWorkStripes) * kScreenTile;
+}
+
 struct DevState {
     int64_t n;        // items
     int k;            // clusters; label k = null (unassigned)
@@ -165,6 +175,11 @@ struct DevState {
     // holds item fixed[c]; cleaning keeps the component that contains it
     const int* fixed;
     int nfixed;
+    // split evaluation of large colour classes: the work list (kWorkStripes stripes
+    // of work_cap(class size) entries) and its per-(class, stripe) counts; null when
+    // no class is split
+    int* work = nullptr;
+    unsigned* work_count = nullptr;
 };
 
 // Persistent sweep kernel: the loop that runs colour sweeps back to back on the
@@ -276,7 +291,7 @@ cudaError_t launch_relaxed_step(int metric, const DevState& st, int item0, int64
                                 const int* cand_dest, cudaStream_t s);
 cudaError_t launch_fx_scale(int metric, const DevState& st, unsigned* maxbits, cudaStream_t s);
 cudaError_t launch_eval(int metric, const DevState& st, int item0, int64_t count, int color,
-                        int* cand_dest, unsigned* cand_prio, bool claims, cudaStream_t s);
+                        int* cand_dest, unsigned* cand_prio, bool claims, bool split, cudaStream_t s);
 cudaError_t launch_apply(int metric, const DevState& st, int item0, int64_t count, int color, int round,
                          int* cand_dest, const unsigned* cand_prio, cudaStream_t s);
 cudaError_t launch_reclaim(const DevState& st, int item0, int64_t count, int color, int round,

@@ -449,3 +449,38 @@ def test_subdivide_device_matches_host_call():
     bad[5, 1] = nv + 7                         # a vertex that does not exist
     assert run(bad) == 1
     e.close()
+
+
+@pytest.mark.parametrize("case", RUNS, ids=[c[0] for c in RUNS])
+def test_split_evaluation_matches_fused_kernel(oracle_lib, case, monkeypatch):
+    """The split evaluation (a screen pass over the colour class that settles the
+    items with nothing to do, then the evaluation over the forwarded work list) takes
+    every item's decision as the fused evaluation kernel does: forced on every class
+    of a small mesh, the clustering, energy and counts equal the fused run's."""
+    name, metric, mk, k, grad, uinit, seeds = case
+    m = mk()
+    ind = m.indicator if (grad > 0 or metric == "aniso") else None
+    pd = m.principal_dirs if metric == "aniso" else None
+    init = synth.seed_labels(m.n_points, k, seed=11) if seeds else None
+    ref = oracle_lib.Port(metric, m.points, m.faces, k, grad, ind, pd, unconstrained_init=uinit)
+    ref.init(init)
+    lab0 = ref.labels()
+    row, col, ev = acvd_gb300.build_topology(m.n_points, m.faces)
+    out = []
+    for split_min in ("1", "0"):          # every class split / none split
+        monkeypatch.setenv("ACVD_SPLIT_MIN", split_min)
+        e = acvd_gb300.Engine()
+        e.set_mesh(m.points, m.faces, row, col, ev)
+        e.set_metric(metric, ind, pd, grad)
+        e.set_unconstrained_initialization(uinit)
+        e.set_labels(k, lab0)
+        st = e.minimize()
+        out.append((e.labels(), st))
+        e.close()
+    (lab_s, st_s), (lab_f, st_f) = out
+    np.testing.assert_array_equal(lab_s, lab_f)
+    assert st_s["energy"] == st_f["energy"]
+    for key in ("sweeps", "moves", "relaxed_sweeps", "convergences", "candidates", "reverted", "boundary_items",
+                "targets", "visited"):
+        assert st_s[key] == st_f[key], (key, st_s[key], st_f[key])
+    assert st_s["kernel_launches"] > st_f["kernel_launches"]
