@@ -13,20 +13,34 @@ Two families of candidates:
     - ``graphs``: per-phase kernels, sweeps between convergence events looped on the device
       inside one CUDA graph (the default);
     - ``host_loop``: the same kernels, one graph launch per sweep decided on the host;
-    - ``persistent``: one cooperative kernel per phase with grid barriers.
+    - ``persistent``: one cooperative kernel per phase with grid barriers;
+    - ``fused``: the launch shape of the evaluation -- every colour class through the one
+      fused evaluation kernel, where the default splits large classes into a screen pass
+      and an evaluation over the forwarded work list.
   A candidate of this family whose labels differ from the default's is rejected, since that
   would mean a broken guarantee rather than a faster schedule.
 * approximate schedules (opt-in) reach a different deterministic clustering:
     - ``exact_sweeps``: no relaxed multi-move sweeps, claim-based sweeps only;
-    - ``match2``: two claim / commit rounds per colour step.
+    - ``match2``: two claim / commit rounds per colour step;
+    - ``order_colors``: the colour classes of a greedy colouring in vertex order (4 balanced
+      classes on grid-like meshes, against the hashed Jones-Plassmann colouring's 6-7 with
+      a few nearly empty ones): fewer colour steps per sweep;
+    - ``squeeze_colors``: the Jones-Plassmann colouring with its highest classes emptied
+      where a local recolouring allows it.
   One of them is accepted only when every item is assigned and its energy is within
   ``energy_rel_tol`` (default 1e-3, the 0.1 % bar against the reference's converged energy)
   of the default schedule's energy on the same input.
 
+The objective is the median device time of a converged solve (``solve``), or that plus the
+wall time of the engine's set-up for the problem (``end_to_end``: the host colourings cost
+set-up time that a one-off solve pays).
+
 The schedules' switches are the engine's own (the ``persistent`` option of ``acvd_opts`` and the
-``ACVD_HOST_LOOP`` / ``ACVD_RELAXED`` / ``ACVD_MATCH_ROUNDS`` environment switches). The engine reads
-the last two when a context is created and ``ACVD_HOST_LOOP`` when it minimises, so
-``ScheduledEngine`` sets them only around those calls and puts the environment back afterwards.
+``ACVD_HOST_LOOP`` / ``ACVD_RELAXED`` / ``ACVD_MATCH_ROUNDS`` / ``ACVD_COLORING`` /
+``ACVD_SPLIT_MIN`` environment switches). The engine reads ``ACVD_RELAXED`` and
+``ACVD_MATCH_ROUNDS`` when a context is created, ``ACVD_COLORING`` and ``ACVD_SPLIT_MIN`` when it
+takes a mesh and ``ACVD_HOST_LOOP`` when it minimises, so ``ScheduledEngine`` sets them only
+around those calls and puts the environment back afterwards.
 """
 from __future__ import annotations
 
@@ -38,6 +52,7 @@ import math
 import os
 import statistics
 import tempfile
+import time
 from typing import Callable
 
 import numpy as np
@@ -52,6 +67,8 @@ class Schedule:
     host_loop: bool = False
     relaxed: bool = True
     match_rounds: int = 1
+    coloring: str = "jp"           # jp (device Jones-Plassmann) | order | squeeze
+    split_min: int | None = None   # None: the engine's threshold; 0: never split
     exact: bool = True   # same clustering as the default schedule, bit for bit
 
     def create_env(self) -> dict:
@@ -59,15 +76,23 @@ class Schedule:
         return {"ACVD_RELAXED": None if self.relaxed else "0",
                 "ACVD_MATCH_ROUNDS": None if self.match_rounds == 1 else str(int(self.match_rounds))}
 
+    def mesh_env(self) -> dict:
+        """Switches the engine reads in acvd_set_mesh."""
+        return {"ACVD_COLORING": None if self.coloring == "jp" else self.coloring,
+                "ACVD_SPLIT_MIN": None if self.split_min is None else str(int(self.split_min))}
+
     def run_env(self) -> dict:
         """Switches the engine reads in acvd_minimize."""
         return {"ACVD_HOST_LOOP": "1" if self.host_loop else None}
 
 
 DEFAULT = Schedule("graphs")
-EXACT_SCHEDULES = (DEFAULT, Schedule("host_loop", host_loop=True), Schedule("persistent", persistent=True))
+EXACT_SCHEDULES = (DEFAULT, Schedule("host_loop", host_loop=True), Schedule("persistent", persistent=True),
+                   Schedule("fused", split_min=0))
 APPROX_SCHEDULES = (Schedule("exact_sweeps", relaxed=False, exact=False),
-                    Schedule("match2", match_rounds=2, exact=False))
+                    Schedule("match2", match_rounds=2, exact=False),
+                    Schedule("order_colors", coloring="order", exact=False),
+                    Schedule("squeeze_colors", coloring="squeeze", exact=False))
 BY_NAME = {s.name: s for s in EXACT_SCHEDULES + APPROX_SCHEDULES}
 
 
@@ -98,6 +123,10 @@ class ScheduledEngine(Engine):
         with environ(schedule.create_env()):
             super().__init__(persistent=schedule.persistent, **kw)
 
+    def set_mesh(self, *a, **kw):
+        with environ(self.schedule.mesh_env()):
+            return super().set_mesh(*a, **kw)
+
     def minimize(self) -> dict:
         with environ(self.schedule.run_env()):
             return super().minimize()
@@ -116,6 +145,8 @@ def labels_digest(labels: np.ndarray) -> str:
 class Trial:
     schedule: str
     ms: float | None = None          # median device time of the timed solves
+    setup_ms: float = 0.0            # wall time of the engine's set-up for the problem
+    score: float | None = None       # what the objective minimises
     energy: float | None = None
     accepted: bool = False
     reason: str = ""
@@ -132,8 +163,11 @@ class Autotuner:
     """
 
     def __init__(self, cache_path: str | None = None, include_approximate: bool = False,
-                 energy_rel_tol: float = 1e-3, candidates=None):
+                 energy_rel_tol: float = 1e-3, candidates=None, objective: str = "solve"):
+        if objective not in ("solve", "end_to_end"):
+            raise ValueError("objective is 'solve' or 'end_to_end'")
         self.cache_path = cache_path
+        self.objective = objective
         self.energy_rel_tol = float(energy_rel_tol)
         if candidates is None:
             candidates = EXACT_SCHEDULES + (APPROX_SCHEDULES if include_approximate else ())
@@ -176,6 +210,8 @@ class Autotuner:
             tol = entry.get("energy_rel_tol")
             if tol is None or float(tol) > self.energy_rel_tol:
                 return None
+        if entry.get("objective", "solve") != self.objective:
+            return None
         return s
 
     def tune(self, key: str, measure: Callable[[Schedule], dict], retune: bool = False) -> tuple[Schedule, dict]:
@@ -197,6 +233,8 @@ class Autotuner:
                 trials.append(t)
                 continue
             t.ms = float(statistics.median(r["ms"]))
+            t.setup_ms = float(r.get("setup_ms", 0.0))
+            t.score = t.ms + (t.setup_ms if self.objective == "end_to_end" else 0.0)
             t.energy = float(r["energy"])
             if s.name == DEFAULT.name:
                 base = r
@@ -210,8 +248,9 @@ class Autotuner:
             else:
                 t.accepted = True
             trials.append(t)
-        best = min((t for t in trials if t.accepted), key=lambda t: t.ms)
-        report = {"schedule": best.schedule, "ms": best.ms, "energy_rel_tol": self.energy_rel_tol,
+        best = min((t for t in trials if t.accepted), key=lambda t: t.score)
+        report = {"schedule": best.schedule, "ms": best.ms, "score": best.score,
+                  "energy_rel_tol": self.energy_rel_tol, "objective": self.objective,
                   "trials": [dataclasses.asdict(t) for t in trials]}
         self.cache[key] = report
         self._save()
@@ -234,27 +273,33 @@ def problem_key(metric: str, n_items: int, k: int, device: int = 0) -> str:
 
 def solve_measure(points, faces, metric: str, k: int, labels, indicator=None, principal_dirs=None,
                   gradation: float = 0.0, level: int = 3, unconstrained_init: int = 0,
-                  repeats: int = 3, device: int = 0, topology=None) -> Callable[[Schedule], dict]:
-    """A measure() for Autotuner.tune: one context per schedule, one untimed solve (graph
-    instantiation, first-touch), then ``repeats`` converged solves from the same initial
-    clustering (acvd_rewind), each timed on the device by the engine's own CUDA events."""
+                  repeats: int = 3, device: int = 0, topology=None, batch=None) -> Callable[[Schedule], dict]:
+    """A measure() for Autotuner.tune: one context per schedule, its set-up for the problem
+    timed on the wall clock, one untimed solve (graph instantiation, first-touch), then
+    ``repeats`` converged solves from the same initial clustering (acvd_rewind), each timed
+    on the device by the engine's own CUDA events.  batch: (v_off, k_off) of a packed batch
+    (acvd_set_batch)."""
     row, col, ev = topology if topology is not None else build_topology(np.asarray(points).shape[0], faces)
     lab0 = np.ascontiguousarray(labels, dtype=np.int32)
 
     def measure(s: Schedule) -> dict:
         with ScheduledEngine(s, device=device) as e:
+            t0 = time.perf_counter()
             e.set_mesh(points, faces, row, col, ev)
+            if batch is not None:
+                e.set_batch(*batch)
             e.set_metric(metric, indicator, principal_dirs, gradation)
             e.set_level(level)
             e.set_unconstrained_initialization(unconstrained_init)
             e.set_labels(k, lab0)
+            setup_ms = 1000.0 * (time.perf_counter() - t0)
             e.minimize()
             ms = []
             for _ in range(max(1, int(repeats))):
                 e.rewind()
                 st = e.minimize()
                 ms.append(st["device_ms"])
-            return {"ms": ms, "energy": st["energy"], "unassigned": st["unassigned"],
+            return {"ms": ms, "setup_ms": setup_ms, "energy": st["energy"], "unassigned": st["unassigned"],
                     "digest": labels_digest(e.labels())}
 
     return measure

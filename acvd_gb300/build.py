@@ -17,6 +17,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libacvd_gb300.so")
+# the plain float32 form: cluster.cu compiled with ACVD_PLAIN_FP32 (uncompensated
+# cluster sums), linked with the other objects into a second library
+LIB_PLAIN = os.path.join(OUT, "libacvd_gb300_plain.so")
+PLAIN_SOURCE = "cluster.cu"
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 CU_SOURCES = ["primitives.cu", "topology.cu", "cluster.cu", "adjoint.cu", "engine.cu", "noalloc.cu", "curvature.cu", "subdivide.cu",
               "manifold.cu"]
@@ -61,6 +65,11 @@ def build(verbose: bool = False, force: bool = False) -> str:
         if force or _stale(obj, [src] + headers):
             jobs.append([nvcc, ARCH, "-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off",
                          "-diag-suppress", "128"] + CU_FILE_FLAGS.get(f, []) + extra + ["-c", src, "-o", obj])
+    plain_obj = os.path.join(OUT, "cluster_plain.cu.o")
+    src = os.path.join(SRC, PLAIN_SOURCE)
+    if force or _stale(plain_obj, [src] + headers):
+        jobs.append([nvcc, ARCH, "-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off",
+                     "-diag-suppress", "128", "-DACVD_PLAIN_FP32"] + extra + ["-c", src, "-o", plain_obj])
     for f in CXX_SOURCES:
         src = os.path.join(SRC, f)
         obj = os.path.join(OUT, f + ".o")
@@ -87,9 +96,11 @@ def build(verbose: bool = False, force: bool = False) -> str:
 
     with concurrent.futures.ThreadPoolExecutor(max_workers=max(1, len(jobs))) as ex:
         list(ex.map(run, jobs))
-    relinked = force or bool(jobs) or not os.path.exists(LIB)
+    relinked = force or bool(jobs) or not os.path.exists(LIB) or not os.path.exists(LIB_PLAIN)
     if relinked:
         run([nvcc, ARCH, "-shared", "-o", LIB] + objs + ["-lcudart"])
+        plain_objs = [plain_obj if o.endswith(os.sep + PLAIN_SOURCE + ".o") else o for o in objs]
+        run([nvcc, ARCH, "-shared", "-o", LIB_PLAIN] + plain_objs + ["-lcudart"])
     for name in CLI_PROGRAMS:
         exe = os.path.join(OUT, name)
         if relinked or name in cli_jobs or not os.path.exists(exe):

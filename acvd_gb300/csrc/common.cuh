@@ -20,6 +20,24 @@ struct df { float hi, lo; };
 
 ACVD_DEV df df_make(float x) { return {x, 0.0f}; }
 
+#ifdef ACVD_PLAIN_FP32
+// The plain form (a second build of the clustering kernels, libacvd_gb300_plain):
+// every double-float operation keeps only its rounded float32 leading part, so
+// cluster sums, incremental records and relaxed-step folds are plain float32
+// arithmetic.  It exists to measure what the compensation buys.
+ACVD_DEV df df_add(df x, df y) { return {__fadd_rn(x.hi, y.hi), 0.0f}; }
+ACVD_DEV df df_add_f(df x, float y) { return {__fadd_rn(x.hi, y), 0.0f}; }
+ACVD_DEV df df_neg(df x) { return {-x.hi, 0.0f}; }
+ACVD_DEV df two_prod(float a, float b) { return {__fmul_rn(a, b), 0.0f}; }
+ACVD_DEV double df_to_d(df x) { return (double)x.hi; }
+ACVD_DEV df df_renorm(float s, float e) { return {__fadd_rn(s, e), 0.0f}; }
+ACVD_DEV df df_sub(df x, df y) { return {__fsub_rn(x.hi, y.hi), 0.0f}; }
+ACVD_DEV df df_mul(df x, df y) { return {__fmul_rn(x.hi, y.hi), 0.0f}; }
+ACVD_DEV df df_mul_f(df x, float y) { return {__fmul_rn(x.hi, y), 0.0f}; }
+ACVD_DEV df df_div(df x, df y) { return {__fdiv_rn(x.hi, y.hi), 0.0f}; }
+ACVD_DEV df df_from_d(double v) { return {__double2float_rn(v), 0.0f}; }
+#else
+
 ACVD_DEV void two_sum(float a, float b, float& s, float& e) {
     s = __fadd_rn(a, b);
     const float bb = __fsub_rn(s, a);
@@ -101,6 +119,7 @@ ACVD_DEV df df_from_d(double v) {
     const float l = __double2float_rn(v - (double)h);
     return {h, l};
 }
+#endif  // ACVD_PLAIN_FP32
 
 // ---------------------------------------------------------------------------
 // Claim words: [8-bit epoch (descending)][30-bit priority][26-bit item slot].

@@ -317,6 +317,46 @@ static int greedy_colors_host(const int32_t* row, const int32_t* col, int64_t n,
     return maxc;
 }
 
+// Empties the highest colour class where it can: each of its items takes a free
+// colour below it, or swaps with its only neighbour u of some colour a when u can
+// take another free colour below the top (u -> b, item -> a).  Sequential in item
+// order, so deterministic.  Returns the new largest colour.
+static int squeeze_top_color(const int32_t* row, const int32_t* col, std::vector<int>& color, int maxc) {
+    const int64_t n = (int64_t)color.size();
+    while (maxc > 0) {
+        const int top = maxc;
+        bool emptied = true;
+        for (int64_t v = 0; v < n; v++) {
+            if (color[v] != top) continue;
+            unsigned long long used = 0ull;
+            for (int p = row[v]; p < row[v + 1]; p++) used |= 1ull << color[col[p]];
+            const unsigned long long below = (1ull << top) - 1ull;
+            if (~used & below) {
+                color[v] = __builtin_ctzll(~used & below);
+                continue;
+            }
+            bool done = false;
+            for (int a = 0; a < top && !done; a++) {
+                int u = -1, cnt = 0;
+                for (int p = row[v]; p < row[v + 1]; p++)
+                    if (color[col[p]] == a) { u = col[p]; cnt++; }
+                if (cnt != 1) continue;
+                unsigned long long uu = 1ull << a;
+                for (int p = row[u]; p < row[u + 1]; p++) uu |= 1ull << color[col[p]];
+                if (~uu & below) {
+                    color[u] = __builtin_ctzll(~uu & below);
+                    color[v] = a;
+                    done = true;
+                }
+            }
+            if (!done) emptied = false;
+        }
+        if (!emptied) break;
+        maxc = top - 1;
+    }
+    return maxc;
+}
+
 static int setup_colors(acvd_ctx* ctx, const int32_t* h_row, const int32_t* h_col) {
     const int64_t n = ctx->nV;
     CK(ctx->wk_int.resize(n));
@@ -352,6 +392,12 @@ static int setup_colors(acvd_ctx* ctx, const int32_t* h_row, const int32_t* h_co
     int maxc = 0;
     CK(cudaMemcpy(&maxc, d_maxc, sizeof(int), cudaMemcpyDeviceToHost));
     if (maxc >= 64) return fail(ctx, ACVD_ERR_UNSUPPORTED, "more than 64 colours needed (vertex valence too high)");
+    if (how && std::strcmp(how, "squeeze") == 0 && maxc > 0) {
+        std::vector<int> hc(n);
+        CK(cudaMemcpy(hc.data(), ctx->wk_int.p, n * sizeof(int), cudaMemcpyDeviceToHost));
+        maxc = squeeze_top_color(h_row, h_col, hc, maxc);
+        CK(cudaMemcpy(ctx->wk_int.p, hc.data(), n * sizeof(int), cudaMemcpyHostToDevice));
+    }
     ctx->ncolors = maxc + 1;
     // colour classes: stable sort of items by colour (items ascending inside a class)
     CK(ctx->wk_a.resize(n));

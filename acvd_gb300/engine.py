@@ -58,16 +58,24 @@ def lib_path() -> str:
     return _build.LIB
 
 
-def load(build_if_missing: bool = True) -> ctypes.CDLL:
-    """Loads libacvd_gb300.so (building it first when it is absent)."""
-    global _LIB
-    if _LIB is not None:
+_LIB_PLAIN = None
+
+
+def load(build_if_missing: bool = True, plain: bool = False) -> ctypes.CDLL:
+    """Loads libacvd_gb300.so (building it first when it is absent).  plain=True loads
+    libacvd_gb300_plain.so instead: the same C ABI, with the clustering kernels built
+    with plain float32 cluster sums (no compensation), for accuracy comparisons."""
+    global _LIB, _LIB_PLAIN
+    if plain and _LIB_PLAIN is not None:
+        return _LIB_PLAIN
+    if not plain and _LIB is not None:
         return _LIB
-    if not os.path.exists(_build.LIB):
+    path = _build.LIB_PLAIN if plain else _build.LIB
+    if not os.path.exists(path):
         if not build_if_missing:
-            raise RuntimeError(f"CUDA library not built: {_build.LIB}")
+            raise RuntimeError(f"CUDA library not built: {path}")
         _build.build()
-    lib = ctypes.CDLL(_build.LIB)
+    lib = ctypes.CDLL(path)
     sig = {
         "acvd_default_opts": (None, [ctypes.POINTER(Opts)]),
         "acvd_create": (_P, [ctypes.POINTER(Opts)]),
@@ -125,7 +133,10 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         fn = getattr(lib, name)
         fn.restype = res
         fn.argtypes = args
-    _LIB = lib
+    if plain:
+        _LIB_PLAIN = lib
+    else:
+        _LIB = lib
     return lib
 
 
@@ -273,8 +284,8 @@ class Engine:
 
     def __init__(self, device: int = 0, use_graphs: bool = True, kernel_timing: bool = False,
                  max_loops: int | None = DEFAULT_MAX_LOOPS, persistent: bool = False,
-                 max_convergences: int | None = None):
-        lib = load()
+                 max_convergences: int | None = None, plain: bool = False):
+        lib = load(plain=plain)
         o = Opts()
         lib.acvd_default_opts(ctypes.byref(o))
         o.device = device

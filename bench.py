@@ -938,6 +938,28 @@ def roofline_block(persistent, tot_t, workload):
                       "(the headline pass carries no events)"}
 
 
+def choose_schedule(args, metric, n, k, device, measure_kw):
+    """The schedule a line runs: 'tuned' (default) times the candidate schedules of the
+    project's autotuner on this very problem before the timed steps (a fresh tuning per
+    run, end-to-end objective: set-up plus converged solve; the approximate candidates
+    only within 1e-3 of the default schedule's energy), 'phases' is the default schedule,
+    'persistent' the persistent kernel.  Returns (schedule, tuning report or None)."""
+    import tempfile
+    from acvd_gb300 import autotune as AT
+    if args.schedule == "persistent":
+        return AT.BY_NAME["persistent"], None
+    if args.schedule == "phases":
+        return AT.DEFAULT, None
+    with tempfile.TemporaryDirectory() as td:
+        tuner = AT.Autotuner(os.path.join(td, "tune.json"), include_approximate=True, objective="end_to_end")
+        t0 = time.perf_counter()
+        sched, rep = tuner.tune(AT.problem_key(metric, n, k, device), AT.solve_measure(device=device, **measure_kw))
+        secs = time.perf_counter() - t0
+    trials = [{"schedule": t["schedule"], "solve_ms": t["ms"], "setup_ms": t["setup_ms"], "accepted": t["accepted"],
+               "reason": t["reason"]} for t in rep["trials"]]
+    return sched, {"chosen": sched.name, "objective": rep["objective"], "tuning_s": secs, "trials": trials}
+
+
 def batch_line(args, name, steps, warmup, e2e_on, cpu_on):
     """Batched workload: the rank's share of the meshes (balanced by items) in one packed
     CSR, one minimisation per step.  At N ranks the batch holds N x 256 meshes (the
@@ -958,12 +980,16 @@ def batch_line(args, name, steps, warmup, e2e_on, cpu_on):
     t0 = time.perf_counter()
     b = B.batch_from_specs([specs[i] for i in mine], w["metric"], w["gradation"])
     gen_s = time.perf_counter() - t0
-    persistent = args.schedule == "persistent"
+    from acvd_gb300 import autotune as AT
     row, col, ev = E.build_topology(b.n_points, b.faces)
+    sched, tuning = choose_schedule(args, w["metric"], b.n_points, b.k_total, device, dict(
+        points=b.points, faces=b.faces, metric=w["metric"], k=b.k_total, labels=b.labels0, indicator=b.indicator,
+        gradation=w["gradation"], unconstrained_init=w["uinit"], topology=(row, col, ev), batch=(b.v_off, b.k_off)))
+    persistent = sched.persistent
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=f"cuda:{device}")
 
     def make_engine(kernel_timing):
-        e = E.Engine(device=device, kernel_timing=kernel_timing, persistent=persistent)
+        e = AT.ScheduledEngine(sched, device=device, kernel_timing=kernel_timing)
         e.set_mesh(b.points, b.faces, row, col, ev)
         e.set_batch(b.v_off, b.k_off)
         e.set_metric(w["metric"], b.indicator, None, w["gradation"])
@@ -989,7 +1015,7 @@ def batch_line(args, name, steps, warmup, e2e_on, cpu_on):
         h2d = (b.points.nbytes + b.faces.nbytes + row.nbytes + col.nbytes + ev.nbytes + b.labels0.nbytes +
                (b.indicator.nbytes if b.indicator is not None else 0))
         e2e_ms = []
-        eng2 = E.Engine(device=device, persistent=persistent)
+        eng2 = AT.ScheduledEngine(sched, device=device)
         # the step's inputs and its output buffer in pinned host memory
         c = np.ascontiguousarray
         h_pts, h_faces, h_row, h_col, h_ev = (pinned(torch, a) for a in (
@@ -1073,7 +1099,7 @@ def batch_line(args, name, steps, warmup, e2e_on, cpu_on):
         "metric": METRIC, "value": value, "unit": "meshes/s", "n_gpus": ws, "steps": steps,
         "warmup": warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": cfg,
-        "schedule": args.schedule, "meshes_per_rank": [len(p) for p in parts], "items_per_rank": loads,
+        "schedule": sched.name, "tuning": tuning, "meshes_per_rank": [len(p) for p in parts], "items_per_rank": loads,
         "generation_s": gen_s,
         "roofline": roofline_block(persistent, tot_t, name),
         "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(tot["kernel_launches"]),
@@ -1107,11 +1133,15 @@ def clustering_line(args, name, steps, warmup, e2e_on, cpu_on):
     m, ind, pd, w = make_workload(name)
     lab0, (row, col, ev) = initial_labels(m, w["metric"], ind, w["gradation"], w["k"], w.get("init"))
     n = m.n_points
-    persistent = args.schedule == "persistent"
+    from acvd_gb300 import autotune as AT
+    sched, tuning = choose_schedule(args, w["metric"], n, w["k"], device, dict(
+        points=m.points, faces=m.faces, metric=w["metric"], k=w["k"], labels=lab0, indicator=ind,
+        principal_dirs=pd, gradation=w["gradation"], unconstrained_init=w["uinit"], topology=(row, col, ev)))
+    persistent = sched.persistent
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=f"cuda:{device}")
 
     def make_engine(kernel_timing):
-        e = E.Engine(device=device, kernel_timing=kernel_timing, persistent=persistent)
+        e = AT.ScheduledEngine(sched, device=device, kernel_timing=kernel_timing)
         e.set_mesh(m.points, m.faces, row, col, ev)
         e.set_metric(w["metric"], ind, pd, w["gradation"])
         e.set_unconstrained_initialization(w["uinit"])
@@ -1142,7 +1172,7 @@ def clustering_line(args, name, steps, warmup, e2e_on, cpu_on):
                (ind.nbytes if ind is not None else 0) + (pd.nbytes if pd is not None else 0) + lab0.nbytes)
         d2h = lab0.nbytes
         e2e_ms = []
-        eng2 = E.Engine(device=device, persistent=persistent)
+        eng2 = AT.ScheduledEngine(sched, device=device)
         # the step's inputs and its output buffer in pinned host memory
         c = np.ascontiguousarray
         h_pts, h_faces, h_row, h_col, h_ev = (pinned(torch, a) for a in (
@@ -1227,7 +1257,7 @@ def clustering_line(args, name, steps, warmup, e2e_on, cpu_on):
         "warmup": warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": workload_config(name, w["desc"], n, w["k"], m.n_faces, ws),
-        "schedule": args.schedule,
+        "schedule": sched.name, "tuning": tuning,
         "roofline": roofline_block(persistent, tot_t, name),
         "cpu_baseline": cpu,
         "e2e": e2e,
@@ -1240,6 +1270,75 @@ def clustering_line(args, name, steps, warmup, e2e_on, cpu_on):
         "energy": energy,
         "clocks": clk.summary(),
     }
+
+
+def plain_form_block(args, steps, warmup):
+    """The plain float32 form (libacvd_gb300_plain: uncompensated cluster sums) beside
+    the compensated one: the torus workload solved with each library from the same
+    initial clustering (time, converged energy against the reference, the device
+    energy's error against the FP64 evaluation of the same clustering), and the 256
+    meshes of the batch solved one at a time with the plain form (summed device time)
+    beside their single batched solve."""
+    import torch
+    from acvd_gb300 import batch as B
+    from acvd_gb300 import engine as E
+    from acvd_gb300 import synth
+    _, _, device = _dist()
+    name = DEFAULT_WORKLOAD
+    m, ind, pd, w = make_workload(name)
+    lab0, (row, col, ev) = initial_labels(m, w["metric"], ind, w["gradation"], w["k"], w.get("init"))
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=f"cuda:{device}")
+    fx = fullsize_fixture(name)
+    out = {}
+    for form in ("plain", "compensated"):
+        e = E.Engine(device=device, plain=form == "plain")
+        e.set_mesh(m.points, m.faces, row, col, ev)
+        e.set_metric(w["metric"], ind, pd, w["gradation"])
+        e.set_unconstrained_initialization(w["uinit"])
+        e.set_labels(w["k"], lab0)
+        step_ms, tot, st = run_steps(torch, e, steps, warmup, device, 1, flush)
+        lab = e.labels()
+        e.close()
+        e_gpu, chk = evaluated_energy(w, m.points, m.faces, w["k"], ind, pd, lab)
+        rec = {"ms_per_step": statistics.mean(step_ms), "sweeps_per_step": tot["sweeps"] / max(1, steps),
+               "reverted_per_step": tot["reverted"] / max(1, steps),
+               "gpu_energy_reference_arithmetic": e_gpu, "gpu_energy_device": st["energy"],
+               "device_vs_fp64_rel_err": abs(st["energy"] - e_gpu) / abs(e_gpu),
+               "all_clusters_connected": bool(chk.clean() == 0)}
+        if fx is not None:
+            rec["rel_diff_vs_reference"] = (e_gpu - fx["reference_energy"]) / abs(fx["reference_energy"])
+            rec["within_0.1pct"] = bool(rec["rel_diff_vs_reference"] <= 1e-3)
+        out[f"{name}_{form}"] = rec
+    # the batch's meshes one at a time with the plain form
+    bw = BATCH_WORKLOADS["batch_256_qem"]
+    specs = synth.batch_specs(bw["n_meshes"], bw["seed"])
+    total_ms, worst = 0.0, -1e300
+    bfx = fullsize_fixture("batch_256_qem")
+    for g, spec in enumerate(specs):
+        mesh = B.mesh_from_spec(spec, False)
+        k = max(1, mesh.n_points // 20)
+        r, c_, ev_ = E.build_topology(mesh.n_points, mesh.faces)
+        wts = E.vertex_weights(bw["metric"], mesh.points, mesh.faces, None, bw["gradation"])
+        l0 = E.initial_sampling(r, c_, wts, k)
+        e = E.Engine(device=device, plain=True)
+        e.set_mesh(mesh.points, mesh.faces, r, c_, ev_)
+        e.set_metric(bw["metric"], None, None, bw["gradation"])
+        e.set_unconstrained_initialization(bw["uinit"])
+        e.set_labels(k, l0)
+        e.minimize()                       # untimed: graph instantiation
+        e.rewind()
+        st = e.minimize()
+        total_ms += st["device_ms"]
+        if bfx is not None:
+            e_m, _ = evaluated_energy(bw, mesh.points, mesh.faces, k, None, None, e.labels())
+            ref = bfx["meshes"][g]["reference_energy"]
+            worst = max(worst, (e_m - ref) / abs(ref))
+        e.close()
+    out["batch_256_qem_plain_one_at_a_time"] = {
+        "ms_total": total_ms, "meshes_per_s": len(specs) / (total_ms / 1000.0),
+        "worst_rel_diff_vs_reference": worst if bfx is not None else None,
+        "timing": "device time of one converged solve per mesh (engine CUDA events), summed"}
+    return out
 
 
 DEFAULT_WORKLOAD = "torus_1024x512_qem"
@@ -1263,6 +1362,7 @@ def run_gpu_arm(args):
             else:
                 extra[name] = clustering_line(args, name, xs, 3, not args.no_e2e, False)
         line["extra_workloads"] = extra
+        line["plain_form"] = plain_form_block(args, xs, 3)
     if line is not None:
         print(json.dumps(line), flush=True)
 
@@ -1292,9 +1392,10 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--schedule", default="phases", choices=["phases", "persistent"],
-                    help="sweep schedule: per-phase kernels in CUDA graphs, or one persistent "
-                         "cooperative kernel between convergence events")
+    ap.add_argument("--schedule", default="tuned", choices=["tuned", "phases", "persistent"],
+                    help="sweep schedule of the clustering workloads: chosen by the autotuner on the "
+                         "workload before the timed steps (default), the default per-phase kernels in "
+                         "CUDA graphs, or one persistent cooperative kernel between convergence events")
     ap.add_argument("--workload", default="torus_1024x512_qem",
                     choices=sorted(WORKLOADS) + sorted(BATCH_WORKLOADS) + sorted(ADJOINT_WORKLOADS) +
                     sorted(CURVATURE_WORKLOADS) + sorted(SUBDIVISION_WORKLOADS) + sorted(MANIFOLD_WORKLOADS))

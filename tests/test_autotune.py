@@ -9,14 +9,15 @@ from acvd_gb300 import autotune as at
 from acvd_gb300.engine import AcvdError
 
 
-def _fake(times, energies=None, digests=None, unassigned=None, fail=()):
+def _fake(times, energies=None, digests=None, unassigned=None, fail=(), setup=None):
     calls = []
 
     def measure(s):
         calls.append(s.name)
         if s.name in fail:
             raise AcvdError(4, "cooperative launch refused")
-        return {"ms": times[s.name], "energy": (energies or {}).get(s.name, -2.0),
+        return {"ms": times.get(s.name, [50.0]), "energy": (energies or {}).get(s.name, -2.0),
+                "setup_ms": (setup or {}).get(s.name, 0.0),
                 "digest": (digests or {}).get(s.name, "same"),
                 "unassigned": (unassigned or {}).get(s.name, 0)}
     return measure, calls
@@ -27,7 +28,7 @@ def test_fastest_exact_schedule_chosen_and_cached(tmp_path):
     measure, calls = _fake({"graphs": [3.0, 2.9, 3.1], "host_loop": [4.0, 4.1, 3.9], "persistent": [2.0, 2.2, 2.1]})
     s, rep = at.Autotuner(path).tune("gb300|qem|n2^19_k2^14", measure)
     assert s == at.BY_NAME["persistent"] and not rep["cached"]
-    assert calls == ["graphs", "host_loop", "persistent"]
+    assert calls == ["graphs", "host_loop", "persistent", "fused"]
     assert rep["ms"] == pytest.approx(2.1)
     with open(path) as f:
         assert json.load(f)["gb300|qem|n2^19_k2^14"]["schedule"] == "persistent"
@@ -38,7 +39,7 @@ def test_fastest_exact_schedule_chosen_and_cached(tmp_path):
     # retune measures again
     measure3, calls3 = _fake({"graphs": [1.0], "host_loop": [4.0], "persistent": [2.0]})
     s3, _ = at.Autotuner(path).tune("gb300|qem|n2^19_k2^14", measure3, retune=True)
-    assert s3 == at.DEFAULT and len(calls3) == 3
+    assert s3 == at.DEFAULT and len(calls3) == 4
 
 
 def test_exact_schedule_with_another_clustering_is_rejected():
@@ -74,7 +75,7 @@ def test_cached_approximate_choice_not_returned_to_a_default_tuner(tmp_path):
     # a default (exact-only) tuner on the same file must not answer with match2
     measure2, calls2 = _fake(times)
     s2, rep2 = at.Autotuner(path).tune("k", measure2)
-    assert s2.exact and not rep2["cached"] and calls2 == ["graphs", "host_loop", "persistent"]
+    assert s2.exact and not rep2["cached"] and calls2 == ["graphs", "host_loop", "persistent", "fused"]
     # an opt-in tuner with a tighter tolerance than the cached choice's measures again
     at.Autotuner(path, include_approximate=True).tune("k2", _fake(times, digests={"match2": "y"})[0])
     tight = at.Autotuner(path, include_approximate=True, energy_rel_tol=1e-4)
@@ -130,3 +131,20 @@ def test_size_class_groups_nearby_sizes():
     assert at.size_class(524288, 20000) == at.size_class(600000, 18000) == "n2^19_k2^14"
     assert at.size_class(10242, 1000) != at.size_class(524288, 1000)
     assert at.size_class(0, 0) == "n2^0_k2^0"
+
+
+def test_mesh_switches_and_end_to_end_objective():
+    # colouring and split threshold are read by acvd_set_mesh: scoped to set_mesh
+    assert at.BY_NAME["order_colors"].mesh_env() == {"ACVD_COLORING": "order", "ACVD_SPLIT_MIN": None}
+    assert at.BY_NAME["fused"].mesh_env() == {"ACVD_COLORING": None, "ACVD_SPLIT_MIN": "0"}
+    assert at.BY_NAME["fused"].exact and not at.BY_NAME["order_colors"].exact
+    times = {"graphs": [10.0], "host_loop": [12.0], "persistent": [12.0], "fused": [11.0], "order_colors": [8.0]}
+    setup = {"order_colors": 5.0, "graphs": 1.0, "fused": 1.0}
+    dig = {"order_colors": "o"}
+    s, _ = at.Autotuner(include_approximate=True).tune("k", _fake(times, digests=dig, setup=setup)[0])
+    assert s.name == "order_colors"          # fastest solve
+    s, rep = at.Autotuner(include_approximate=True, objective="end_to_end").tune(
+        "k", _fake(times, digests=dig, setup=setup)[0])
+    assert s.name == "graphs" and rep["score"] == 11.0   # 10 + 1 beats 8 + 5
+    with pytest.raises(ValueError):
+        at.Autotuner(objective="wall")

@@ -484,3 +484,33 @@ def test_split_evaluation_matches_fused_kernel(oracle_lib, case, monkeypatch):
                 "targets", "visited"):
         assert st_s[key] == st_f[key], (key, st_s[key], st_f[key])
     assert st_s["kernel_launches"] > st_f["kernel_launches"]
+
+
+def test_plain_fp32_form_runs_through_the_same_abi(oracle_lib):
+    """libacvd_gb300_plain (cluster sums in plain float32, no compensation) is the
+    comparison form of the benchmark: same C ABI, a connected clustering within the
+    0.1 % bar of the reference's converged energy on a small QEM torus."""
+    case = RUNS[2]
+    name, metric, mk, k, grad, uinit, seeds = case
+    m = mk()
+    ind = m.indicator
+    ref = oracle_lib.Port(metric, m.points, m.faces, k, grad, ind, unconstrained_init=uinit)
+    ref.init(None)
+    lab0 = ref.labels()
+    ref.run()
+    e_ref = _evaluated(oracle_lib, metric, m.points, m.faces, k, grad, ind, None, ref.labels())
+    row, col, ev = acvd_gb300.build_topology(m.n_points, m.faces)
+    e = acvd_gb300.Engine(plain=True)
+    assert e._lib._name.endswith("libacvd_gb300_plain.so")
+    e.set_mesh(m.points, m.faces, row, col, ev)
+    e.set_metric(metric, ind, None, grad)
+    e.set_unconstrained_initialization(uinit)
+    e.set_labels(k, lab0)
+    e.minimize()
+    lab = e.labels()
+    e.close()
+    assert np.all(lab < k)
+    chk = oracle_lib.Port(metric, m.points, m.faces, k, grad, ind)
+    chk.evaluate(lab, 1)
+    assert chk.global_energy() <= e_ref + REL_ENERGY * abs(e_ref)
+    assert chk.clean() == 0
