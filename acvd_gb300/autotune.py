@@ -275,23 +275,28 @@ def solve_measure(points, faces, metric: str, k: int, labels, indicator=None, pr
                   gradation: float = 0.0, level: int = 3, unconstrained_init: int = 0,
                   repeats: int = 3, device: int = 0, topology=None, batch=None) -> Callable[[Schedule], dict]:
     """A measure() for Autotuner.tune: one context per schedule, its set-up for the problem
-    timed on the wall clock, one untimed solve (graph instantiation, first-touch), then
+    done twice and the second (warm) one timed on the wall clock, one untimed solve (graph instantiation, first-touch), then
     ``repeats`` converged solves from the same initial clustering (acvd_rewind), each timed
     on the device by the engine's own CUDA events.  batch: (v_off, k_off) of a packed batch
     (acvd_set_batch)."""
     row, col, ev = topology if topology is not None else build_topology(np.asarray(points).shape[0], faces)
     lab0 = np.ascontiguousarray(labels, dtype=np.int32)
 
+    def setup(e):
+        e.set_mesh(points, faces, row, col, ev)
+        if batch is not None:
+            e.set_batch(*batch)
+        e.set_metric(metric, indicator, principal_dirs, gradation)
+        e.set_level(level)
+        e.set_unconstrained_initialization(unconstrained_init)
+        e.set_labels(k, lab0)
+
     def measure(s: Schedule) -> dict:
         with ScheduledEngine(s, device=device) as e:
+            # the first set-up pays the context's allocations; the second one is timed
+            setup(e)
             t0 = time.perf_counter()
-            e.set_mesh(points, faces, row, col, ev)
-            if batch is not None:
-                e.set_batch(*batch)
-            e.set_metric(metric, indicator, principal_dirs, gradation)
-            e.set_level(level)
-            e.set_unconstrained_initialization(unconstrained_init)
-            e.set_labels(k, lab0)
+            setup(e)
             setup_ms = 1000.0 * (time.perf_counter() - t0)
             e.minimize()
             ms = []
