@@ -20,7 +20,10 @@
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
+#include <memory>
+#include <mutex>
 #include <queue>
+#include <thread>
 #include <random>
 #include <type_traits>
 #include <vector>
@@ -306,6 +309,104 @@ struct EngineBase {
     int max_convergences = 1000000000;
     int max_loops = 5000000;
     std::queue<idt> queue;
+
+    // ACVDQP: the threaded engine vtkThreadedClustering (DiscreteRemeshing/
+    // vtkThreadedClustering.h), selected by threads > 0 as DOmultithread selects it
+    // (vtkSurfaceClustering.h:44-52).  The mesh is split into pool_size - 1 regions
+    // (the engine's own random sampling, holes filled); an edge belongs to its region
+    // when both ends lie in it, else to the serial process pool_size - 1.  Each loop,
+    // `threads` threads take regions longest-first from a priority queue and run the
+    // edge test under per-cluster locks; the main thread then runs the serial process.
+    int threads = 0;              // SetNumberOfThreads; 0 = the sequential engine
+    int pooling_ratio = 5;        // SetPoolingRatio (ctor :990-1012)
+    int pool_size = 0;            // PoolingRatio * NumberOfThreads + 1 (Init :749)
+    std::vector<int> edge_proc;   // EdgesProcess (ComputeEdgesLayout :806-888)
+    // ProcessesQueues1/2 (:752-759): queue [owner * pool_size + pusher]; a process only
+    // pushes into its own pusher column, so concurrent processes never share a queue
+    std::vector<std::queue<idt>> queues_a, queues_b;
+    std::vector<std::queue<idt>>* push_q = &queues_a;
+    std::vector<std::queue<idt>>* pop_q = &queues_b;
+    // vtkPriorityQueue as the reference uses it: the smallest priority pops first, an id
+    // already queued is not inserted again
+    struct RegionQueue {
+        std::vector<std::pair<double, int>> h;
+        void insert(double pr, int id) {
+            for (const auto& x : h)
+                if (x.second == id) return;
+            h.push_back({pr, id});
+            std::push_heap(h.begin(), h.end(), [](const auto& a, const auto& b) { return a.first > b.first; });
+        }
+        int pop() {
+            if (h.empty()) return -1;
+            std::pop_heap(h.begin(), h.end(), [](const auto& a, const auto& b) { return a.first > b.first; });
+            const int id = h.back().second;
+            h.pop_back();
+            return id;
+        }
+    };
+    RegionQueue pool_a, pool_b;
+    RegionQueue* pool1 = &pool_a;      // PoolQueue1 / PoolQueue2, swapped after each loop
+    RegionQueue* pool2 = &pool_b;
+    std::mutex pool_lock1, pool_lock2;   // PoolAllocationLock, PoolAllocationLock2
+    std::unique_ptr<std::mutex[]> cluster_locks;   // ClustersLocks (K + 1)
+    int n_cluster_locks = 0;
+    long long collisions = 0;          // NumberOfLockingCollisions (summed after a loop)
+
+    // labels read and written concurrently by the threads (the reference's races on
+    // Clustering, benign there), as relaxed atomics
+    int lab_get(idt i) const { return __atomic_load_n(&labels[i], __ATOMIC_RELAXED); }
+    void lab_set(idt i, int v) { __atomic_store_n(&labels[i], v, __ATOMIC_RELAXED); }
+
+    // Init's part of vtkThreadedClustering (:746-772) with ComputeEdgesLayout type 1
+    void threaded_init() {
+        pool_size = pooling_ratio * threads + 1;
+        std::vector<int> region(n_items());
+        random_sampling(region, pool_size - 1);
+        fill_holes_in(region);
+        edge_proc.assign(mesh.n_edges(), 0);
+        for (idt e = 0; e < mesh.n_edges(); e++) {
+            int c1 = region[mesh.ev1[e]];
+            if (c1 >= pool_size || c1 < 0) c1 = pool_size - 1;
+            if (region[mesh.ev2[e]] != c1) c1 = pool_size - 1;
+            edge_proc[e] = c1;
+        }
+        queues_a.assign((size_t)pool_size * pool_size, std::queue<idt>());
+        queues_b.assign((size_t)pool_size * pool_size, std::queue<idt>());
+        push_q = &queues_a;
+        pop_q = &queues_b;
+        pool_a.h.clear();
+        pool_b.h.clear();
+        pool1 = &pool_a;
+        pool2 = &pool_b;
+        collisions = 0;
+    }
+
+    // FillQueuesFromClustering of the threaded engine (:203-240)
+    void threaded_fill_queue() {
+        for (auto& q : *push_q)
+            while (!q.empty()) q.pop();
+        for (idt e = 0; e < mesh.n_edges(); e++)
+            if (labels[mesh.ev1[e]] != labels[mesh.ev2[e]])
+                (*push_q)[(size_t)edge_proc[e] * pool_size + edge_proc[e]].push(e);
+        for (int i = 0; i < pool_size - 1; i++) pool1->insert(i, i);
+    }
+
+    // AddEdgeToProcess / AddItemRingToProcess of the threaded engine (:125-131, :108-114)
+    void push_edge(idt e, int process) { (*push_q)[(size_t)edge_proc[e] * pool_size + process].push(e); }
+    void push_ring(idt item, int process) { for (idt e : mesh.ring[item]) push_edge(e, process); }
+
+    // ConnexityConstraintProblemLocal with the labels read as the threads see them
+    int connexity_problem_threaded(idt item, int cluster) const {
+        if (!connexity) return 0;
+        std::vector<idt> vl;
+        for (idt e : mesh.ring[item]) {
+            const idt v1 = mesh.ev1[e], v2 = mesh.ev2[e];
+            if (v1 != item && lab_get(v1) == cluster) vl.push_back(v1);
+            if (v2 != item && lab_get(v2) == cluster) vl.push_back(v2);
+        }
+        return connected_set(vl);
+    }
+
     // statistics of the last MinimizeEnergy
     int stat_convergences = 0;
     long long stat_moves = 0;
@@ -315,6 +416,7 @@ struct EngineBase {
     virtual void set_constrained(int c) = 0;
     virtual void recompute_statistics() = 0;
     virtual int process_one_loop() = 0;
+    virtual int threaded_loop() = 0;
     virtual double item_weight(idt i) const = 0;
     virtual double cluster_energy(int k) const = 0;
     virtual void cluster_accum(int k, double* S, double* W, double* Q, double* c) const = 0;
@@ -336,6 +438,12 @@ struct EngineBase {
             if (v1 != item && labels[v1] == cluster) vl.push_back(v1);
             if (v2 != item && labels[v2] == cluster) vl.push_back(v2);
         }
+        return connected_set(vl);
+    }
+
+    // 0 when the vertices of vl are connected through mesh edges among themselves
+    // (the BFS of ConnexityConstraintProblemLocal, vtkVerticesProcessing.h:199-235)
+    int connected_set(std::vector<idt>& vl) const {
         if (vl.empty()) return 0;
         const size_t total = vl.size();
         size_t visited = 1;
@@ -430,7 +538,10 @@ struct EngineBase {
     }
 
     // FillHolesInClustering (:552-633); returns the number of items left unassigned
-    int fill_holes() {
+    int fill_holes() { return fill_holes_in(labels); }
+    // the same on another array (the threaded engine's regions); the connectivity test
+    // reads the engine's own labels, as the reference's does
+    int fill_holes_in(std::vector<int>& labels) {
         std::queue<idt> q;
         for (idt e = 0; e < mesh.n_edges(); e++) {
             const idt i1 = mesh.ev1[e], i2 = mesh.ev2[e];
@@ -443,7 +554,7 @@ struct EngineBase {
             idt i1 = mesh.ev1[e], i2 = mesh.ev2[e];
             int c1 = labels[i1], c2 = labels[i2];
             if (c1 == K) { std::swap(i1, i2); c1 = c2; c2 = K; }
-            if (c1 != K && c2 == K && connexity_problem(i2, c2) == 0) {
+            if (c1 != K && c2 == K && this->connexity_problem(i2, c2) == 0) {
                 labels[i2] = c1;
                 add_ring_to(q, i2);
             }
@@ -475,25 +586,29 @@ struct EngineBase {
         rel_loops = 1;
         n_loops = 0;
         while (!queue.empty()) queue.pop();
+        if (threads > 0) threaded_init();
     }
 
     // ComputeInitialRandomSampling (:1178-1316): the fixed items take clusters
     // 0 .. F-1, the grown regions the labels above them
-    void initial_random_sampling() {
+    void initial_random_sampling() { random_sampling(labels, K); }
+    // the same into another array with n_regions regions (the threaded engine's thread
+    // regions, vtkThreadedClustering.h:851-858); unassigned items keep the label K
+    void random_sampling(std::vector<int>& labels, int n_regions) {
         const idt n = n_items();
         for (idt i = 0; i < n; i++) labels[i] = K;
         const int offset = (int)fixed.size();
         for (int o = 0; o < offset; o++) labels[fixed[o]] = o;
         std::vector<int> itm(n);
         idt remaining_items = n;
-        int remaining_regions = K - offset;
+        int remaining_regions = n_regions - offset;
         for (idt i = 0; i < n; i++) itm[i] = (int)i;
         std::mt19937 rng;
         rng.seed(0);
         for (idt i = n - 1; i > 0; --i) std::swap(itm[i], itm[rng() % n]);
         double sw = 0;
         for (idt i = 0; i < n; i++) sw += item_weight(i);
-        const double target = sw / (double)K;
+        const double target = sw / (double)n_regions;
         idt first = 0;
         std::queue<int> q;
         std::vector<idt> nb;
@@ -563,7 +678,7 @@ struct EngineBase {
     void minimize_energy() {
         auto t0 = std::chrono::steady_clock::now();
         fill_holes();
-        fill_queue();
+        if (threads > 0) threaded_fill_queue(); else fill_queue();
         recompute_statistics();
         set_all_modified();
         int convergences = 0;
@@ -571,7 +686,8 @@ struct EngineBase {
         for (int k = 0; k < K; k++) if (!frozen[k]) early += sizes[k];
         stat_moves = 0;
         while (true) {
-            const int mods = process_one_loop();
+            if (threads > 0) std::swap(push_q, pop_q);   // SwapQueues (:742, :743-747)
+            const int mods = threads > 0 ? threaded_loop() : process_one_loop();
             stat_moves += mods;
             n_loops++;
             if (rel_loops == 255) {
@@ -589,7 +705,7 @@ struct EngineBase {
                 if (n_loops >= max_loops) break;
                 if (convergences >= max_convergences) break;
                 recompute_statistics();
-                fill_queue();
+                if (threads > 0) threaded_fill_queue(); else fill_queue();
                 set_all_modified();
             }
         }
@@ -672,6 +788,131 @@ struct Engine : EngineBase {
             if (c >= 0 && c < K) metric.add(i, &clusters[c]);
         }
         for (auto& c : clusters) { metric.centroid(&c); metric.energy(&c); }
+    }
+
+    // ProcessOneLoop of the threaded engine (vtkThreadedClustering.h:663-693) with its
+    // thread body MyMainForClustering (:245-283)
+    int threaded_loop() override {
+        if (n_cluster_locks != K + 1) {
+            cluster_locks.reset(new std::mutex[K + 1]);
+            n_cluster_locks = K + 1;
+        }
+        std::vector<int> mods(threads + 1, 0);
+        std::vector<long long> coll(threads + 1, 0);
+        std::vector<std::thread> th;
+        for (int t = 0; t < threads; t++) {
+            th.emplace_back([this, t, &mods, &coll] {
+                while (true) {
+                    int process;
+                    {
+                        std::lock_guard<std::mutex> g(pool_lock1);
+                        process = pool1->pop();
+                    }
+                    if (process < 0) break;
+                    const auto t0 = std::chrono::steady_clock::now();
+                    execute_process(process, mods[t], coll[t]);
+                    const double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+                    std::lock_guard<std::mutex> g(pool_lock2);
+                    pool2->insert(-dt, process);
+                }
+            });
+        }
+        for (auto& x : th) x.join();
+        execute_process(pool_size - 1, mods[threads], coll[threads]);
+        std::swap(pool1, pool2);
+        int total = 0;
+        for (int t = 0; t <= threads; t++) {
+            total += mods[t];
+            collisions += coll[t];
+        }
+        return total;
+    }
+
+    // ExecuteProcess (vtkThreadedClustering.h:285-493): the process's pop queues, the
+    // sequential loop's edge test under the two clusters' locks
+    void execute_process(int process, int& mods, long long& coll) {
+        typename M::Cluster c21, c22, c31, c32;
+        auto lock = [&](int c) {
+            if (!cluster_locks[c].try_lock()) {
+                coll++;
+                cluster_locks[c].lock();
+            }
+        };
+        for (int cq = 0; cq < pool_size; cq++) {
+            std::queue<idt>& q = (*pop_q)[(size_t)process * pool_size + cq];
+            while (!q.empty()) {
+                const idt edge = q.front();
+                q.pop();
+                const idt i1 = mesh.ev1[edge], i2 = mesh.ev2[edge];
+                if (edges_last_loop[edge] == rel_loops || i2 < 0) continue;
+                edges_last_loop[edge] = rel_loops;
+                const int v1 = lab_get(i1), v2 = lab_get(i2);
+                if (v1 == v2) continue;
+                if (v1 < v2) { lock(v1); lock(v2); } else { lock(v2); lock(v1); }
+                if (v1 == K) {
+                    // I1 unassigned: joins I2's cluster (no modification stamp here, :344-354)
+                    typename M::Cluster* c2 = &clusters[v2];
+                    metric.add(i1, c2); metric.centroid(c2); metric.energy(c2);
+                    sizes[v2]++;
+                    push_ring(i1, process);
+                    lab_set(i1, v2);
+                    mods++;
+                } else if (v2 == K) {
+                    typename M::Cluster* c1 = &clusters[v1];
+                    metric.add(i2, c1); metric.centroid(c1); metric.energy(c1);
+                    sizes[v1]++;
+                    push_ring(i2, process);
+                    lab_set(i2, v1);
+                    mods++;
+                } else {
+                    int result = 1;
+                    typename M::Cluster* c1 = &clusters[v1];
+                    typename M::Cluster* c2 = &clusters[v2];
+                    if ((last_mod[v1] >= n_loops - 1 || last_mod[v2] >= n_loops - 1) && !frozen[v1] && !frozen[v2]) {
+                        double try1, try2, try3;
+                        try1 = c1->E + c2->E;
+                        if (sizes[v1] == 1 || connexity_problem_threaded(i1, v1) == 1) try2 = 100000000.0;
+                        else {
+                            c21 = *c1; c22 = *c2;
+                            metric.sub(i1, &c21); metric.add(i1, &c22);
+                            metric.centroid(&c21); metric.centroid(&c22);
+                            metric.energy(&c21); metric.energy(&c22);
+                            try2 = c21.E + c22.E;
+                        }
+                        if (sizes[v2] == 1 || connexity_problem_threaded(i2, v2) == 1) try3 = 1000000000.0;
+                        else {
+                            c31 = *c1; c32 = *c2;
+                            metric.sub(i2, &c32); metric.add(i2, &c31);
+                            metric.centroid(&c31); metric.centroid(&c32);
+                            metric.energy(&c31); metric.energy(&c32);
+                            try3 = c31.E + c32.E;
+                        }
+                        if (try1 <= try2 && try1 <= try3) result = 1;
+                        else if (try2 < try1 && try2 < try3) result = 2;
+                        else result = 3;
+                    }
+                    if (result == 1) {
+                        push_edge(edge, process);
+                    } else if (result == 2) {
+                        lab_set(i1, v2);
+                        sizes[v2]++; sizes[v1]--;
+                        *c1 = c21; *c2 = c22;
+                        push_ring(i1, process);
+                        mods++;
+                        last_mod[v1] = n_loops; last_mod[v2] = n_loops;
+                    } else {
+                        lab_set(i2, v1);
+                        sizes[v1]++; sizes[v2]--;
+                        *c1 = c31; *c2 = c32;
+                        push_ring(i2, process);
+                        mods++;
+                        last_mod[v1] = n_loops; last_mod[v2] = n_loops;
+                    }
+                }
+                cluster_locks[v1].unlock();
+                cluster_locks[v2].unlock();
+            }
+        }
     }
 
     int process_one_loop() override {   // (:833-995)
@@ -809,6 +1050,8 @@ int port_set_option(void* hp, const char* name, double value) {
     else if (!std::strcmp(name, "max_loops")) e->max_loops = (int)value;
     else if (!std::strcmp(name, "max_convergences")) e->max_convergences = (int)value;
     else if (!std::strcmp(name, "connexity")) e->connexity = (int)value;
+    else if (!std::strcmp(name, "threads")) h->eng->threads = (int)value;
+    else if (!std::strcmp(name, "pooling_ratio")) h->eng->pooling_ratio = (int)value;
     else if (!std::strcmp(name, "level")) {
         if (h->metric == 1) static_cast<Engine<QEMMetric>*>(e)->metric.level = (int)value;
         else if (h->metric == 2) static_cast<Engine<AnisoMetric>*>(e)->metric.level = (int)value;

@@ -21,6 +21,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_LIB = os.path.join(HERE, "_build", "libacvd_port.so")
 REF_LIB = os.path.join(HERE, "_ref", "libacvdref.so")
+REF_MT_LIB = os.path.join(HERE, "_ref", "libacvdref_mt.so")
 REF_ROOT = os.environ.get("ACVD_REFERENCE_ROOT", "/root/reference")
 
 METRICS = {"iso": 0, "qem": 1, "aniso": 2}
@@ -338,6 +339,26 @@ class Ref(_Base):
 
     def loops(self) -> int:
         return int(self._lib.ref_loops(self.h))
+
+
+class RefThreaded(_Base):
+    """The reference built with DOmultithread: vtkThreadedClustering (ACVDQP's
+    engine) under the same driver.  Options "threads" and "pooling_ratio"."""
+    _prefix = "refmt_"
+    _libpath = REF_MT_LIB
+    _lib = None
+
+    @classmethod
+    def _extra(cls, lib):
+        lib.refmt_loops.argtypes = [_P]
+        lib.refmt_loops.restype = ctypes.c_int
+
+    def loops(self) -> int:
+        return int(self._lib.refmt_loops(self.h))
+
+
+def ref_threaded_available() -> bool:
+    return os.path.exists(REF_MT_LIB)
 
 
 def subdivide(points: np.ndarray, faces: np.ndarray, indicator: np.ndarray | None = None, timing: list | None = None):

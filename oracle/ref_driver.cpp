@@ -121,6 +121,10 @@ struct Ref : RefBase {
         else if (!std::strcmp(name, "max_loops")) p->SetMaxNumberOfLoops((int)v);
         else if (!std::strcmp(name, "max_convergences")) p->SetMaxNumberOfConvergences((int)v);
         else if (!std::strcmp(name, "connexity")) p->ConnexityConstraint = (int)v;
+#ifdef DOmultithread
+        else if (!std::strcmp(name, "threads")) p->SetNumberOfThreads((int)v);
+        else if (!std::strcmp(name, "pooling_ratio")) p->SetPoolingRatio((int)v);
+#endif
         else if (!std::strcmp(name, "constrained")) p->GetMetric()->SetConstrainedClustering((int)v);
         else if (!std::strcmp(name, "level")) {
             if constexpr (!std::is_same<M, vtkIsotropicMetricForClustering>::value)
@@ -228,33 +232,42 @@ struct Ref : RefBase {
     }
 };
 
+// Built twice: as is (prefix ref_, the sequential engine) and with DOmultithread,
+// the reference's own switch that makes vtkSurfaceClustering derive from
+// vtkThreadedClustering (ACVDQP), plus ACVD_REF_THREADED for the prefix refmt_.
+#ifdef ACVD_REF_THREADED
+#define REF_FN(x) refmt_##x
+#else
+#define REF_FN(x) ref_##x
+#endif
+
 extern "C" {
 
-void* ref_create(int metric, long long nV, const double* pts, long long nF, const int* tri,
+void* REF_FN(create)(int metric, long long nV, const double* pts, long long nF, const int* tri,
                  const double* indicator, const float* pdirs, double gradation, int K) {
     if (metric == 0) return new Ref<vtkIsotropicMetricForClustering>(nV, pts, nF, tri, indicator, pdirs, gradation, K);
     if (metric == 1) return new Ref<vtkQEMetricForClustering>(nV, pts, nF, tri, indicator, pdirs, gradation, K);
     return new Ref<vtkQuadricAnisotropicMetricForClustering>(nV, pts, nF, tri, indicator, pdirs, gradation, K);
 }
-void ref_destroy(void* h) { delete (RefBase*)h; }
-int ref_set_option(void* h, const char* name, double v) { ((RefBase*)h)->set_option(name, v); return 0; }
-void ref_init(void* h, const int* initial) { ((RefBase*)h)->init(initial); }
-double ref_run(void* h) { return ((RefBase*)h)->run(); }
-double ref_process(void* h, const int* initial) { return ((RefBase*)h)->process(initial); }
-void ref_get_labels(void* h, int* out) { ((RefBase*)h)->get_labels(out); }
-void ref_set_labels(void* h, const int* lab) { ((RefBase*)h)->set_labels(lab); }
-void ref_evaluate(void* h, const int* lab, int constrained) { ((RefBase*)h)->evaluate(lab, constrained); }
-double ref_global_energy(void* h) { return ((RefBase*)h)->global_energy(); }
-void ref_get_clusters(void* h, double* S, double* W, double* Q, double* C, double* E, int* sz) {
+void REF_FN(destroy)(void* h) { delete (RefBase*)h; }
+int REF_FN(set_option)(void* h, const char* name, double v) { ((RefBase*)h)->set_option(name, v); return 0; }
+void REF_FN(init)(void* h, const int* initial) { ((RefBase*)h)->init(initial); }
+double REF_FN(run)(void* h) { return ((RefBase*)h)->run(); }
+double REF_FN(process)(void* h, const int* initial) { return ((RefBase*)h)->process(initial); }
+void REF_FN(get_labels)(void* h, int* out) { ((RefBase*)h)->get_labels(out); }
+void REF_FN(set_labels)(void* h, const int* lab) { ((RefBase*)h)->set_labels(lab); }
+void REF_FN(evaluate)(void* h, const int* lab, int constrained) { ((RefBase*)h)->evaluate(lab, constrained); }
+double REF_FN(global_energy)(void* h) { return ((RefBase*)h)->global_energy(); }
+void REF_FN(get_clusters)(void* h, double* S, double* W, double* Q, double* C, double* E, int* sz) {
     ((RefBase*)h)->get_clusters(S, W, Q, C, E, sz);
 }
-int ref_clean(void* h) { return ((RefBase*)h)->clean(); }
-int ref_fill_holes(void* h) { return ((RefBase*)h)->fill(); }
-int ref_loops(void* h) { return ((RefBase*)h)->loops(); }
-void ref_post_placement(void* h, int level, double* out) { ((RefBase*)h)->post_placement(level, out); }
-void ref_set_fixed(void* h, int n, const int* ids) { ((RefBase*)h)->set_fixed(n, ids); }
-int ref_set_anchors(void* h, int n, const int* anchors) { return ((RefBase*)h)->set_anchors(n, anchors); }
-void ref_curvature(void* h, double* indicator, float* principal_dirs) {
+int REF_FN(clean)(void* h) { return ((RefBase*)h)->clean(); }
+int REF_FN(fill_holes)(void* h) { return ((RefBase*)h)->fill(); }
+int REF_FN(loops)(void* h) { return ((RefBase*)h)->loops(); }
+void REF_FN(post_placement)(void* h, int level, double* out) { ((RefBase*)h)->post_placement(level, out); }
+void REF_FN(set_fixed)(void* h, int n, const int* ids) { ((RefBase*)h)->set_fixed(n, ids); }
+int REF_FN(set_anchors)(void* h, int n, const int* anchors) { return ((RefBase*)h)->set_anchors(n, anchors); }
+void REF_FN(curvature)(void* h, double* indicator, float* principal_dirs) {
     ((RefBase*)h)->curvature(indicator, principal_dirs);
 }
 

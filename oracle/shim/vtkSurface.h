@@ -42,6 +42,13 @@ public:
     }
     void GetEdgeVertices(vtkIdType e, vtkIdType& v1, vtkIdType& v2) { v1 = M.ev1[e]; v2 = M.ev2[e]; }
     void GetEdgeFaces(vtkIdType e, vtkIdType& f1, vtkIdType& f2) { f1 = M.poly1[e]; f2 = M.poly2[e]; }
+    // the faces of an edge as a list (the face-clustering branch of GetEdgeItemsSure,
+    // compiled in the threaded engine, never run for vertex clustering)
+    void GetEdgeFaces(vtkIdType e, vtkIdList* out) {
+        out->Reset();
+        if (M.poly1[e] >= 0) out->InsertNextId(M.poly1[e]);
+        if (M.poly2[e] >= 0) out->InsertNextId(M.poly2[e]);
+    }
     void GetVertexNeighbourEdges(vtkIdType v, vtkIdType& n, vtkIdType*& e) {
         n = (vtkIdType)Ring[v].size(); e = Ring[v].data();
     }

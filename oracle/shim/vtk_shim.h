@@ -316,7 +316,14 @@ class vtkPriorityQueue : public vtkObject {
 public:
     static vtkPriorityQueue* New() { return new vtkPriorityQueue; }
     void Allocate(vtkIdType n, vtkIdType = 1000) { H.reserve(n); }
-    void Insert(double priority, vtkIdType id) { H.push_back({priority, id}); std::push_heap(H.begin(), H.end(), cmp); }
+    // an id already in the queue is not inserted again (the threaded engine re-inserts
+    // every region at each FillQueuesFromClustering)
+    void Insert(double priority, vtkIdType id) {
+        for (const auto& h : H)
+            if (h.second == id) return;
+        H.push_back({priority, id});
+        std::push_heap(H.begin(), H.end(), cmp);
+    }
     vtkIdType Pop(vtkIdType = 0) {
         if (H.empty()) return -1;
         std::pop_heap(H.begin(), H.end(), cmp);
