@@ -1,5 +1,6 @@
 """Gradients of the clustering energy and of the placed cluster vertices for a
-fixed clustering, as a torch.autograd.Function over acvd_adjoint (C ABI).
+fixed clustering: a libtorch torch::autograd::Function (csrc/adjoint_torch.cpp) over
+acvd_adjoint_on_stream (C ABI).
 
     E, C = ClusteringEnergy.apply(xyz, rho, engine, gradation)
     (E * 1.0 + (C * target).sum()).backward()   # -> xyz.grad, rho.grad
@@ -15,6 +16,8 @@ plain torch (CPU autograd) used by the tests.
 """
 from __future__ import annotations
 
+import ctypes
+
 import torch
 
 from . import engine as _eng
@@ -24,36 +27,32 @@ def _ptr(t):
     return None if t is None else int(t.data_ptr())
 
 
-class ClusteringEnergy(torch.autograd.Function):
-    @staticmethod
-    def forward(ctx, xyz, rho, engine: "_eng.Engine", gradation: float):
-        x64 = xyz.detach().to(torch.float64).contiguous()
-        r64 = None if rho is None else rho.detach().to(torch.float64).contiguous()
-        cent = torch.empty((engine.k, 3), dtype=torch.float64, device=xyz.device)
-        torch.cuda.current_stream(xyz.device).synchronize()
-        e = engine.adjoint_raw(_ptr(x64), _ptr(r64), gradation, 0.0, None, _ptr(cent), None, None)
-        ctx.engine = engine
-        ctx.gradation = gradation
-        ctx.has_rho = rho is not None
-        ctx.save_for_backward(x64, r64 if r64 is not None else torch.empty(0, dtype=torch.float64,
-                                                                           device=xyz.device))
-        ctx.dtypes = (xyz.dtype, None if rho is None else rho.dtype)
-        return torch.tensor(e, dtype=torch.float64, device=xyz.device), cent
+_EXT = None
+
+
+def _extension():
+    """The libtorch extension (csrc/adjoint_torch.cpp), bound to the C ABI of the
+    library instance this package loaded."""
+    global _EXT
+    if _EXT is None:
+        from . import build as _build
+        mod = _build.load_torch_extension()
+        lib = _eng.load()
+        mod.bind(ctypes.cast(lib.acvd_adjoint_on_stream, ctypes.c_void_p).value,
+                 ctypes.cast(lib.acvd_last_error, ctypes.c_void_p).value)
+        _EXT = mod
+    return _EXT
+
+
+class ClusteringEnergy:
+    """E, C = ClusteringEnergy.apply(xyz, rho, engine, gradation): the libtorch
+    torch::autograd::Function of csrc/adjoint_torch.cpp (forward and backward on
+    torch's current stream through acvd_adjoint_on_stream, no host waits)."""
 
     @staticmethod
-    def backward(ctx, g_energy, g_cent):
-        x64, r64 = ctx.saved_tensors
-        r64 = r64 if ctx.has_rho else None
-        engine = ctx.engine
-        gE = 0.0 if g_energy is None else float(g_energy.item())
-        gC = None if g_cent is None else g_cent.detach().to(torch.float64).contiguous()
-        gx = torch.empty_like(x64)
-        gr = torch.empty_like(r64) if r64 is not None else None
-        torch.cuda.current_stream(x64.device).synchronize()
-        engine.adjoint_raw(_ptr(x64), _ptr(r64), ctx.gradation, gE, _ptr(gC), None, _ptr(gx), _ptr(gr))
-        gx = gx.to(ctx.dtypes[0])
-        gr = None if gr is None else gr.to(ctx.dtypes[1])
-        return gx, gr, None, None
+    def apply(xyz, rho, engine: "_eng.Engine", gradation: float):
+        E, C = _extension().clustering_energy(xyz, rho, int(engine.ctx), float(gradation), int(engine.k))
+        return E, C
 
 
 def cluster_energies(engine: "_eng.Engine", xyz, rho, gradation: float):

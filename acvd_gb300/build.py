@@ -32,6 +32,21 @@ CXX_SOURCES = ["host.cpp", "io.cpp"]
 CLI_PROGRAMS = {"acvd": [], "acvdq": ["-DACVD_CLI_QEM"], "anisotropic_remeshing_q": ["-DACVD_CLI_ANISO"]}
 
 
+# the libtorch autograd function over acvd_adjoint_on_stream (csrc/adjoint_torch.cpp),
+# compiled by torch.utils.cpp_extension into _build/torch_ext
+TORCH_EXT_NAME = "acvd_adjoint_torch"
+TORCH_EXT_DIR = os.path.join(OUT, "torch_ext")
+
+
+def load_torch_extension(verbose: bool = False):
+    """Builds (when stale) and imports the libtorch extension module."""
+    from torch.utils import cpp_extension
+    os.makedirs(TORCH_EXT_DIR, exist_ok=True)
+    return cpp_extension.load(name=TORCH_EXT_NAME, sources=[os.path.join(SRC, "adjoint_torch.cpp")],
+                              extra_cflags=["-O2", "-std=c++17"], with_cuda=True, build_directory=TORCH_EXT_DIR,
+                              verbose=verbose)
+
+
 def _nvcc() -> str:
     for cand in (shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
         if cand and os.path.exists(cand):
@@ -94,8 +109,10 @@ def build(verbose: bool = False, force: bool = False) -> str:
             jobs.append(["g++", "-O2", "-std=c++17", "-ffp-contract=off"] + defs + ["-c", cli_src, "-o", obj])
             cli_jobs.append(name)
 
-    with concurrent.futures.ThreadPoolExecutor(max_workers=max(1, len(jobs))) as ex:
+    with concurrent.futures.ThreadPoolExecutor(max_workers=max(1, len(jobs)) + 1) as ex:
+        torch_ext = ex.submit(load_torch_extension, verbose)   # in parallel with the nvcc jobs
         list(ex.map(run, jobs))
+        torch_ext.result()
     relinked = force or bool(jobs) or not os.path.exists(LIB) or not os.path.exists(LIB_PLAIN)
     if relinked:
         run([nvcc, ARCH, "-shared", "-o", LIB] + objs + ["-lcudart"])

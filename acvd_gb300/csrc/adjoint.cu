@@ -97,10 +97,12 @@ ACVD_DEV void smul(const double a[6], const double v[3], double o[3]) {
 }
 
 // per cluster: placement, energy, and the cotangents of S, W, A, b
-__global__ void adj_cluster(AdjState a, int metric, int level, double thr, double gE, const double* __restrict__ gC,
-                            double* __restrict__ cent) {
+// gE: the cotangent of the total energy, read from dgE (device) when that is given
+__global__ void adj_cluster(AdjState a, int metric, int level, double thr, double gE_host, const double* dgE,
+                            const double* __restrict__ gC, double* __restrict__ cent) {
     const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= a.k) return;
+    const double gE = dgE ? *dgE : gE_host;
     double* r0 = a.cl + k * kClStride;
     const double S[3] = {r0[0], r0[1], r0[2]};
     const double W = r0[3];
@@ -288,15 +290,16 @@ __global__ void adj_vertex_bwd(AdjState a, double* __restrict__ gx, double* __re
 static inline unsigned nb(int64_t n, int b = 256) { return (unsigned)((n + b - 1) / b); }
 
 cudaError_t adjoint_run(const AdjState& a, int metric, int level, double thr, double ratio, double gE,
-                        const double* gC, const uint32_t* sorted, const uint32_t* off, const uint32_t* cnt,
-                        double* wsum, double* cent, double* gx, double* grho, cudaStream_t s, Scratch& scratch) {
+                        const double* dgE, const double* gC, const uint32_t* sorted, const uint32_t* off,
+                        const uint32_t* cnt, double* wsum, double* cent, double* gx, double* grho, cudaStream_t s,
+                        Scratch& scratch) {
     adj_face_fwd<<<nb(a.nf), 256, 0, s>>>(a);
     adj_vertex_fwd<<<nb(a.nv), 256, 0, s>>>(a);
     cudaError_t e = sum_f64(a.vw, a.nv, wsum, scratch, s);
     if (e != cudaSuccess) return e;
     adj_clamp<<<nb(a.nv), 256, 0, s>>>(a, wsum, ratio);
     adj_cluster_sums<<<nb((int64_t)a.k * 32), 256, 0, s>>>(a, sorted, off, cnt);
-    adj_cluster<<<nb(a.k, 128), 128, 0, s>>>(a, metric, level, thr, gE, gC, cent);
+    adj_cluster<<<nb(a.k, 128), 128, 0, s>>>(a, metric, level, thr, gE, dgE, gC, cent);
     g_launches += 6;
     if (gx) {
         adj_face_bwd<<<nb(a.nf), 256, 0, s>>>(a);

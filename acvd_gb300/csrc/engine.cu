@@ -56,6 +56,8 @@ struct acvd_ctx {
     int ncolors = 0;
     std::vector<int64_t> color_off;
     DBuf<int> color_items, cand_dest, cand_list;
+    // acvd_adjoint_on_stream: orders the context's stream after the caller's and back
+    cudaEvent_t adj_ev_in = nullptr, adj_ev_out = nullptr;
     // split evaluation of large colour classes (screen pass + work list)
     DBuf<int> work;
     DBuf<unsigned> work_count;
@@ -528,6 +530,8 @@ void acvd_destroy(acvd_ctx* ctx) {
     ctx->drop_graph();
     ctx->drop_events();
     if (ctx->h_raw) cudaFreeHost(ctx->h_raw);
+    if (ctx->adj_ev_in) cudaEventDestroy(ctx->adj_ev_in);
+    if (ctx->adj_ev_out) cudaEventDestroy(ctx->adj_ev_out);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     if (ctx->s) cudaStreamDestroy(ctx->s);
@@ -2155,17 +2159,17 @@ extern "C" int acvd_get_dual_mesh(acvd_ctx* ctx, int32_t* tris, int64_t* n_tris)
 // ---------------------------------------------------------------------------
 namespace acvd {
 cudaError_t adjoint_run(const AdjState& a, int metric, int level, double thr, double ratio, double gE,
-                        const double* gC, const uint32_t* sorted, const uint32_t* off, const uint32_t* cnt,
-                        double* wsum, double* cent, double* gx, double* grho, cudaStream_t s, Scratch& scratch);
+                        const double* dgE, const double* gC, const uint32_t* sorted, const uint32_t* off,
+                        const uint32_t* cnt, double* wsum, double* cent, double* gx, double* grho, cudaStream_t s,
+                        Scratch& scratch);
 }  // namespace acvd
 
-extern "C" int acvd_adjoint(acvd_ctx* ctx, const double* xyz, const double* rho, double gradation, double g_energy,
-                            const double* g_centroids, double* energy, double* cluster_energies, double* centroids,
-                            double* grad_xyz, double* grad_rho) {
-    if (!ctx) return ACVD_ERR_ARG;
-    if (!ctx->ready_metric || !ctx->ready_labels) return fail(ctx, ACVD_ERR_ARG, "acvd_adjoint needs metric and labels");
-    if (!xyz) return fail(ctx, ACVD_ERR_ARG, "acvd_adjoint: positions required");
-    if (ctx->metric == kAniso) return fail(ctx, ACVD_ERR_UNSUPPORTED, "adjoint of the anisotropic metric not built");
+// The adjoint's work on the context's stream.  g_energy / d_g_energy: the total
+// energy's cotangent as a host value or a device scalar (d_g_energy wins when given);
+// energy: host output, d_energy: device output.  No host synchronisation.
+static int adjoint_enqueue(acvd_ctx* ctx, const double* xyz, const double* rho, double gradation, double g_energy,
+                           const double* d_g_energy, const double* g_centroids, double* energy, double* d_energy,
+                           double* cluster_energies, double* centroids, double* grad_xyz, double* grad_rho) {
     CK(cudaSetDevice(ctx->opts.device));
     const int64_t nv = ctx->nV, nf = ctx->nF;
     const int K = ctx->K;
@@ -2192,14 +2196,58 @@ extern "C" int acvd_adjoint(acvd_ctx* ctx, const double* xyz, const double* rho,
     a.vf_face = ctx->vf_face.p;
     CK(ctx->dtmp.resize(4));
     const double ratio = ctx->metric == kQEM ? 10000.0 : 100000.0;
-    CK(adjoint_run(a, ctx->metric, ctx->level, 1e-3, ratio, g_energy, g_centroids, ctx->wk_b.p, ctx->wk_off.p,
-                   ctx->wk_cnt.p, ctx->dtmp.p, centroids, grad_xyz, grad_rho, ctx->s, ctx->scratch));
-    if (energy) {
+    CK(adjoint_run(a, ctx->metric, ctx->level, 1e-3, ratio, g_energy, d_g_energy, g_centroids, ctx->wk_b.p,
+                   ctx->wk_off.p, ctx->wk_cnt.p, ctx->dtmp.p, centroids, grad_xyz, grad_rho, ctx->s, ctx->scratch));
+    if (energy || d_energy) {
         CK(sum_f64(a.ek, K, ctx->dtmp.p + 1, ctx->scratch, ctx->s));
-        CK(cudaMemcpyAsync(energy, ctx->dtmp.p + 1, sizeof(double), cudaMemcpyDeviceToHost, ctx->s));
+        if (d_energy) CK(cudaMemcpyAsync(d_energy, ctx->dtmp.p + 1, sizeof(double), cudaMemcpyDeviceToDevice, ctx->s));
+        if (energy) CK(cudaMemcpyAsync(energy, ctx->dtmp.p + 1, sizeof(double), cudaMemcpyDeviceToHost, ctx->s));
     }
     if (cluster_energies)
         CK(cudaMemcpyAsync(cluster_energies, a.ek, K * sizeof(double), cudaMemcpyDeviceToDevice, ctx->s));
+    return ACVD_OK;
+}
+
+static int adjoint_check(acvd_ctx* ctx, const double* xyz) {
+    if (!ctx) return ACVD_ERR_ARG;
+    if (!ctx->ready_metric || !ctx->ready_labels) return fail(ctx, ACVD_ERR_ARG, "acvd_adjoint needs metric and labels");
+    if (!xyz) return fail(ctx, ACVD_ERR_ARG, "acvd_adjoint: positions required");
+    if (ctx->metric == kAniso) return fail(ctx, ACVD_ERR_UNSUPPORTED, "adjoint of the anisotropic metric not built");
+    return ACVD_OK;
+}
+
+extern "C" int acvd_adjoint(acvd_ctx* ctx, const double* xyz, const double* rho, double gradation, double g_energy,
+                            const double* g_centroids, double* energy, double* cluster_energies, double* centroids,
+                            double* grad_xyz, double* grad_rho) {
+    int r = adjoint_check(ctx, xyz);
+    if (r) return r;
+    r = adjoint_enqueue(ctx, xyz, rho, gradation, g_energy, nullptr, g_centroids, energy, nullptr, cluster_energies,
+                        centroids, grad_xyz, grad_rho);
+    if (r) return r;
     CK(cudaStreamSynchronize(ctx->s));
+    return ACVD_OK;
+}
+
+extern "C" int acvd_adjoint_on_stream(acvd_ctx* ctx, void* stream, const double* xyz, const double* rho,
+                                      double gradation, const double* d_g_energy, const double* g_centroids,
+                                      double* d_energy, double* cluster_energies, double* centroids,
+                                      double* grad_xyz, double* grad_rho) {
+    int r = adjoint_check(ctx, xyz);
+    if (r) return r;
+    CK(cudaSetDevice(ctx->opts.device));
+    if (!ctx->adj_ev_in) {
+        CK(cudaEventCreateWithFlags(&ctx->adj_ev_in, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&ctx->adj_ev_out, cudaEventDisableTiming));
+    }
+    cudaStream_t caller = (cudaStream_t)stream;
+    // the caller's earlier work (the inputs) before the context's; the caller's later
+    // work after the outputs -- ordering on the device, no host wait
+    CK(cudaEventRecord(ctx->adj_ev_in, caller));
+    CK(cudaStreamWaitEvent(ctx->s, ctx->adj_ev_in, 0));
+    r = adjoint_enqueue(ctx, xyz, rho, gradation, 0.0, d_g_energy, g_centroids, nullptr, d_energy, cluster_energies,
+                        centroids, grad_xyz, grad_rho);
+    if (r) return r;
+    CK(cudaEventRecord(ctx->adj_ev_out, ctx->s));
+    CK(cudaStreamWaitEvent(caller, ctx->adj_ev_out, 0));
     return ACVD_OK;
 }

@@ -104,6 +104,7 @@ def load(build_if_missing: bool = True, plain: bool = False) -> ctypes.CDLL:
         "acvd_rewind": (ctypes.c_int, [_P]),
         "acvd_set_batch": (ctypes.c_int, [_P, ctypes.c_int, _P, _P]),
         "acvd_adjoint": (ctypes.c_int, [_P, _P, _P, ctypes.c_double, ctypes.c_double, _P, _P, _P, _P, _P, _P]),
+        "acvd_adjoint_on_stream": (ctypes.c_int, [_P, _P, _P, _P, ctypes.c_double, _P, _P, _P, _P, _P, _P, _P]),
         "acvd_get_mesh_energies": (ctypes.c_int, [_P, _P]),
         "acvd_get_labels": (ctypes.c_int, [_P, _P]),
         "acvd_get_clusters": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P, _P]),

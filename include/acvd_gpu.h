@@ -417,6 +417,20 @@ int acvd_adjoint(acvd_ctx* ctx, const double* xyz, const double* rho, double gra
                  const double* g_centroids, double* energy, double* cluster_energies, double* centroids,
                  double* grad_xyz, double* grad_rho);
 
+/*
+ * acvd_adjoint ordered on the caller's CUDA stream (a cudaStream_t), with no host
+ * synchronisation: the work waits on the device for what the caller enqueued on
+ * `stream` before the call, and the caller's later work on `stream` waits for the
+ * outputs.  The energy's cotangent d_g_energy and the energy d_energy are DEVICE
+ * scalars (either may be NULL: cotangent 0, energy not returned).  This is what an
+ * autograd function inside a training loop calls (acvd_gb300/csrc/adjoint_torch.cpp:
+ * torch::autograd::Function on torch's current stream).  It has no counterpart in
+ * the reference, whose clustering has no gradients.
+ */
+int acvd_adjoint_on_stream(acvd_ctx* ctx, void* stream, const double* xyz, const double* rho, double gradation,
+                           const double* d_g_energy, const double* g_centroids, double* d_energy,
+                           double* cluster_energies, double* centroids, double* grad_xyz, double* grad_rho);
+
 /* The CUDA stream (cudaStream_t) the context launches on. */
 void* acvd_stream(acvd_ctx* ctx);
 
