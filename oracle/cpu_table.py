@@ -24,7 +24,8 @@ import sys
 import time
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-sys.path.insert(0, os.path.dirname(HERE))
+# run as a script, this directory would shadow the oracle package: the repository root instead
+sys.path[0] = os.path.dirname(HERE)
 
 import numpy as np  # noqa: E402
 
