@@ -668,74 +668,103 @@ __global__ void __launch_bounds__(256, EvalMinBlocks<M>::value) eval_kernel(DevS
 // stripe b % kWorkStripes (one atomic per block, spread over the stripes' counters);
 // stripe s holds its entries at work[s * cap ...], cap = work_cap(count).
 // ---------------------------------------------------------------------------
-constexpr int kScreenItems = kScreenTile / 256;   // items per thread
+constexpr int kScreenFlags = kScreenTile / 256;   // boundary flags each thread loads per tile
+constexpr int kScreenBatch = 4;                    // cached screens each thread resolves at once
 
+// Cached screen of item i: forward it (energy test to run, or its connectivity test is
+// not cached), or settle it here -- counted as cached, and when fresh but unable to
+// move marked evaluated -- exactly as eval_tile's cached path decides.
 template <int M>
-__global__ void __launch_bounds__(256, 6) screen_kernel(DevState st, int item0, int64_t count, int color, int* work,
-                                                     unsigned* work_count) {
-    __shared__ int s_list[kScreenTile];
-    __shared__ unsigned s_n, s_base, s_cnt[8][3];
-    if (threadIdx.x == 0) s_n = 0u;
+__global__ void __launch_bounds__(256, 4) screen_kernel(DevState st, int item0, int64_t count, int color, int* work,
+                                                        unsigned* work_count) {
+    __shared__ int s_cached[kScreenTile];   // tile positions with a cached screen
+    __shared__ int s_fwd[kScreenTile];      // tile positions forwarded to the work list
+    __shared__ unsigned s_nc, s_nf, s_base, s_cnt[8][3];
     const SweepState sw = *st.sweep;
     const RunFlags fl = *st.flags;
-    const int64_t base = (int64_t)blockIdx.x * kScreenTile + threadIdx.x;
-    unsigned char bf[kScreenItems];
-    int L[kScreenItems], ev_i[kScreenItems];
-    int4 c[kScreenItems];
-    // every item's flag, then every cached item's screen inputs, before any is used
-#pragma unroll
-    for (int u = 0; u < kScreenItems; u++) {
-        const int64_t idx = base + u * 256;
-        bf[u] = idx < count ? st.bflag[item0 + idx] : (unsigned char)0;
-    }
-#pragma unroll
-    for (int u = 0; u < kScreenItems; u++) {
-        if (bf[u] == 2) {
-            const int i = item0 + (int)(base + u * 256);
-            L[u] = st.label[i];
-            ev_i[u] = st.evald[i];
-            c[u] = st.tcache[i];
-        } else {
-            L[u] = 0;
-            ev_i[u] = 0;
-            c[u] = make_int4(0, 0, 0, 0);
-        }
-    }
-    unsigned n_visit = 0, n_cached = 0, n_bnd = 0;
-    bool fwd[kScreenItems];
-#pragma unroll
-    for (int u = 0; u < kScreenItems; u++) {
-        const int64_t idx = base + u * 256;
-        n_visit += idx < count ? 1u : 0u;
-        fwd[u] = bf[u] == 1;
-        if (bf[u] != 2 || !ACVD_VALID(st, L[u] >= 0 && L[u] <= st.k)) continue;
-        const int n = c[u].w & 3;
-        const bool conn_known = (c[u].w & 4) != 0, conn_ok = (c[u].w & 8) != 0;
-        const bool may_move = st.size[L[u]] > 1 && !(st.frozen && st.frozen[L[u]]);
-        if (fl.connexity && may_move && !conn_known) {
-            fwd[u] = true;   // the connectivity test is not cached: a full screen
-            continue;
-        }
-        const int tg[3] = {c[u].x, c[u].y, c[u].z};
-        bool fresh = ev_i[u] <= sw.floor || st.stamp[L[u]] >= ev_i[u];
-#pragma unroll
-        for (int q = 0; q < 3; q++)
-            if (q < n && st.stamp[tg[q]] >= ev_i[u]) fresh = true;
-        if (fresh && may_move && (!fl.connexity || conn_ok)) {
-            fwd[u] = true;   // an energy test to run: the work list
-            continue;
-        }
-        n_cached++;
-        if (fresh) {
-            n_bnd++;
-            st.evald[item0 + (int)idx] = sw.sweep;   // evaluated: nothing it may do
-        }
-    }
-    __syncthreads();   // s_n initialised
-#pragma unroll
-    for (int u = 0; u < kScreenItems; u++)
-        if (fwd[u]) s_list[atomicAdd(&s_n, 1u)] = (int)(base + u * 256);
+    const int64_t cap = work_cap(count);
+    const int64_t ntiles = (count + kScreenTile - 1) / kScreenTile;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    unsigned n_visit = 0, n_cached = 0, n_bnd = 0;
+    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        if (threadIdx.x == 0) {
+            s_nc = 0u;
+            s_nf = 0u;
+        }
+        __syncthreads();
+        const int64_t t0 = tile * kScreenTile;
+        // stage 1: every flag of the tile in one burst (coalesced, kScreenFlags loads in
+        // flight per thread), then the cached items compacted, full screens forwarded
+        unsigned char bf[kScreenFlags];
+#pragma unroll
+        for (int u = 0; u < kScreenFlags; u++) {
+            const int64_t idx = t0 + u * 256 + threadIdx.x;
+            bf[u] = idx < count ? st.bflag[item0 + idx] : (unsigned char)0;
+            n_visit += idx < count ? 1u : 0u;
+        }
+#pragma unroll
+        for (int u = 0; u < kScreenFlags; u++) {
+            const int pos = u * 256 + (int)threadIdx.x;
+            if (bf[u] == 2) s_cached[atomicAdd(&s_nc, 1u)] = pos;
+            else if (bf[u] == 1) s_fwd[atomicAdd(&s_nf, 1u)] = pos;
+        }
+        __syncthreads();
+        // stage 2: the cached screens, kScreenBatch per thread with all their loads
+        // issued before any is used
+        const int nc = (int)s_nc;
+        for (int j0 = 0; j0 < nc; j0 += 256 * kScreenBatch) {
+            int pos[kScreenBatch], L[kScreenBatch], ev_i[kScreenBatch];
+            int4 c[kScreenBatch];
+#pragma unroll
+            for (int u = 0; u < kScreenBatch; u++) {
+                const int j = j0 + u * 256 + (int)threadIdx.x;
+                pos[u] = j < nc ? s_cached[j] : -1;
+                if (pos[u] >= 0) {
+                    const int i = item0 + (int)(t0 + pos[u]);
+                    L[u] = st.label[i];
+                    ev_i[u] = st.evald[i];
+                    c[u] = st.tcache[i];
+                } else {
+                    L[u] = 0;
+                    ev_i[u] = 0;
+                    c[u] = make_int4(0, 0, 0, 0);
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < kScreenBatch; u++) {
+                if (pos[u] < 0 || !ACVD_VALID(st, L[u] >= 0 && L[u] <= st.k)) continue;
+                const int n = c[u].w & 3;
+                const bool conn_known = (c[u].w & 4) != 0, conn_ok = (c[u].w & 8) != 0;
+                const bool may_move = st.size[L[u]] > 1 && !(st.frozen && st.frozen[L[u]]);
+                bool fwd = fl.connexity && may_move && !conn_known;   // connectivity not cached: full screen
+                if (!fwd) {
+                    const int tg[3] = {c[u].x, c[u].y, c[u].z};
+                    bool fresh = ev_i[u] <= sw.floor || st.stamp[L[u]] >= ev_i[u];
+#pragma unroll
+                    for (int q = 0; q < 3; q++)
+                        if (q < n && st.stamp[tg[q]] >= ev_i[u]) fresh = true;
+                    if (fresh && may_move && (!fl.connexity || conn_ok)) {
+                        fwd = true;   // an energy test to run
+                    } else {
+                        n_cached++;
+                        if (fresh) {
+                            n_bnd++;
+                            st.evald[item0 + (int)(t0 + pos[u])] = sw.sweep;   // nothing it may do
+                        }
+                    }
+                }
+                if (fwd) s_fwd[atomicAdd(&s_nf, 1u)] = pos[u];
+            }
+        }
+        __syncthreads();
+        // the tile's forwarded items: one atomic per tile, on the stripe's counter
+        const int stripe = (int)(tile % kWorkStripes);
+        if (threadIdx.x == 0) s_base = s_nf ? atomicAdd(&work_count[color * kWorkStripes + stripe], s_nf) : 0u;
+        __syncthreads();
+        int* out = work + stripe * cap + s_base;
+        const int nf = (int)s_nf;
+        for (int j = threadIdx.x; j < nf; j += 256) out[j] = (int)t0 + s_fwd[j];
+    }
     const unsigned v[3] = {n_visit, n_cached, n_bnd};
 #pragma unroll
     for (int q = 0; q < 3; q++) {
@@ -743,18 +772,13 @@ __global__ void __launch_bounds__(256, 6) screen_kernel(DevState st, int item0, 
         if (lane == 0) s_cnt[wid][q] = t;
     }
     __syncthreads();
-    const int stripe = (int)(blockIdx.x % kWorkStripes);
-    if (threadIdx.x == 0) s_base = s_n ? atomicAdd(&work_count[color * kWorkStripes + stripe], s_n) : 0u;
-    if (threadIdx.x >= 32 && threadIdx.x < 35) {
-        const int q = threadIdx.x - 32;
+    if (threadIdx.x < 3) {
+        const int q = threadIdx.x;
         const int which = q == 0 ? kCntVisited : (q == 1 ? kCntCached : kCntBoundary);
         unsigned t = 0;
         for (int w = 0; w < 8; w++) t += s_cnt[w][q];
         if (t) atomicAdd(ctr(st.counters, which), (unsigned long long)t);
     }
-    __syncthreads();
-    int* out = work + stripe * work_cap(count) + s_base;
-    for (unsigned j = threadIdx.x; j < s_n; j += 256) out[j] = s_list[j];
 }
 
 // The work list of a screen_kernel pass through eval_tile, 256 entries per tile,
@@ -1843,6 +1867,16 @@ static int eval_list_blocks_per_sm(int metric) {
     return (e == cudaSuccess && nb > 0) ? nb : 1;
 }
 
+// Blocks per SM of screen_kernel (its grid strides over the class's tiles).
+static int screen_blocks_per_sm(int metric) {
+    int nb = 0;
+    cudaError_t e;
+    if (metric == kIso) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, screen_kernel<kIso>, 256, 0);
+    else if (metric == kQEM) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, screen_kernel<kQEM>, 256, 0);
+    else e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, screen_kernel<kAniso>, 256, 0);
+    return (e == cudaSuccess && nb > 0) ? nb : 1;
+}
+
 cudaError_t launch_eval(int metric, const DevState& st, int item0, int64_t count, int color,
                         int* cand_dest, unsigned* cand_prio, bool claims, bool split, cudaStream_t s) {
     if (count == 0) return cudaSuccess;
@@ -1851,8 +1885,8 @@ cudaError_t launch_eval(int metric, const DevState& st, int item0, int64_t count
                       claims ? 1 : 0);
         return cudaGetLastError();
     }
-    ACVD_DISPATCH(metric, screen_kernel, nblk(count, kScreenTile), 256, s, st, item0, count, color, st.work,
-                  st.work_count);
+    const unsigned sgrid = (unsigned)std::min<int64_t>(nblk(count, kScreenTile), sm_count() * screen_blocks_per_sm(metric));
+    ACVD_DISPATCH(metric, screen_kernel, sgrid, 256, s, st, item0, count, color, st.work, st.work_count);
     const int64_t tiles = kWorkStripes * (work_cap(count) / 256);
     const unsigned grid = (unsigned)std::min<int64_t>(tiles, sm_count() * eval_list_blocks_per_sm(metric));
     ACVD_DISPATCH(metric, eval_list_kernel, grid, 256, s, st, item0, count, color, cand_dest, cand_prio,

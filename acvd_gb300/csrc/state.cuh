@@ -107,7 +107,7 @@ struct SweepState {
 // and the items one screen block covers; stripe s of a class of `count` items holds
 // its entries at [s * work_cap(count), (s + 1) * work_cap(count)).
 constexpr int kWorkStripes = 16;
-constexpr int kScreenTile = 1024;
+constexpr int kScreenTile = 4096;
 __host__ __device__ inline int64_t work_cap(int64_t count) {
     const int64_t nb = (count + kScreenTile - 1) / kScreenTile;
     return ((nb + kWorkStripes - 1) / kWorkStripes) * kScreenTile;
