@@ -233,62 +233,6 @@ ACVD_DEV void warp_count(unsigned long long* ctr, unsigned v) {
     if ((threadIdx.x & 31) == 0 && tot) atomicAdd(ctr, (unsigned long long)tot);
 }
 
-// item contribution j (the accumulate_item components) as a double-float: the
-// products w x, A x and T x are formed exactly (TwoProd) and summed compensated
-template <int M>
-ACVD_DEV df contrib_df(const ItemRec& it, int j) {
-    const int rowi[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
-    if (j < 3) return two_prod(it.w, it.x[j]);
-    if (j == 3) return df_make(it.w);
-    if (j < 10) return df_make(it.A[j - 4]);
-    if (j < 13) {
-        const int c = j - 10;
-        return df_add(df_add(two_prod(it.A[rowi[c][0]], it.x[0]), two_prod(it.A[rowi[c][1]], it.x[1])),
-                      two_prod(it.A[rowi[c][2]], it.x[2]));
-    }
-    if (j < 19) return df_make(it.T[j - 13]);
-    const int c = j - 19;
-    return df_add(df_add(two_prod(it.T[rowi[c][0]], it.x[0]), two_prod(it.T[rowi[c][1]], it.x[1])),
-                  two_prod(it.T[rowi[c][2]], it.x[2]));
-}
-
-// Fixed-point units of component q: the scale is a power of two 2^e held as two
-// float factors (x, y; inverses in z, w), so both conversions are exact scalings.
-ACVD_DEV long long to_fixed(df v, float4 p) {
-    const float h = __fmul_rn(__fmul_rn(v.hi, p.x), p.y);
-    const float l = __fmul_rn(__fmul_rn(v.lo, p.x), p.y);
-    return __float2ll_rn(h) + __float2ll_rn(l);
-}
-
-ACVD_DEV df from_fixed(long long d, float4 p) {
-    const float h = __ll2float_rn(d);
-    const float l = __ll2float_rn(d - __float2ll_rn(h));
-    return df_renorm(__fmul_rn(__fmul_rn(h, p.z), p.w), __fmul_rn(__fmul_rn(l, p.z), p.w));
-}
-
-// A relaxed step's commit of item i from cluster L (K: unassigned) to B: the label,
-// the ring's boundary flags, and the item's contributions summed per cluster in
-// exact fixed point (fx_finalize folds them into the accumulators and stamps the
-// touched clusters after the step).
-template <int M>
-ACVD_DEV void relaxed_commit_item(const DevState& st, int i, int L, int B) {
-    constexpr int NA = Layout<M>::acc;
-    ItemRec it;
-    load_item<M>(st, i, it);
-    st.label[i] = B;
-    mark_ring(st, i);
-    atomicAdd(&st.in_done[B], 1);
-    long long* dB = st.fx_delta + (int64_t)B * NA;
-    long long* dL = st.fx_delta + (int64_t)(L < st.k ? L : 0) * NA;
-    if (L < st.k) atomicAdd(&st.out_done[L], 1);
-#pragma unroll
-    for (int q = 0; q < NA; q++) {
-        const long long v = to_fixed(contrib_df<M>(it, q), st.fx_pow[q]);
-        atomicAdd((unsigned long long*)&dB[q], (unsigned long long)v);
-        if (L < st.k) atomicAdd((unsigned long long*)&dL[q], (unsigned long long)(-v));
-    }
-}
-
 // ---------------------------------------------------------------------------
 // eval: proposals for one colour class
 //
@@ -354,7 +298,6 @@ ACVD_DEV void eval_tile(const DevState& st, int item0, int64_t count, int color,
     __shared__ int s_tgt[256][kMaxTgt];        // work item -> destination clusters (ring order)
     __shared__ float s_val[256][kMaxTgt + 1];  // energy parts: [j] add to s_tgt[j], [kMaxTgt] remove
     __shared__ signed char s_nt[256];          // destinations; -1: the whole test runs in B2
-    __shared__ unsigned char s_same[256];       // work item's ring holds a member of its own cluster
     __shared__ unsigned short s_task[256 * kMaxTgt];   // add tasks: (work item << 4) | destination
     __shared__ unsigned char s_rem[256];                // work items whose remove part B1 computes
     __shared__ int s_scr[256];                 // flagged items of the tile (colour-list positions)
@@ -374,7 +317,7 @@ ACVD_DEV void eval_tile(const DevState& st, int item0, int64_t count, int color,
     const int64_t idx_t = listed ? (in ? (int64_t)entries[threadIdx.x] : 0) : tile * 256 + threadIdx.x;
     const SweepState sw = *st.sweep;
     const RunFlags fl = *st.flags;
-    unsigned n_slots = 0, n_bnd = 0, n_tgt = 0, n_cand = 0, n_scr = 0, n_cached = 0, n_move = 0;
+    unsigned n_slots = 0, n_bnd = 0, n_tgt = 0, n_cand = 0, n_scr = 0, n_cached = 0;
     // A0: only items that may lie on a boundary go on to the ring screen, packed
     // so that warps without one issue nothing: cached screens from the front of the
     // list, full screens from its back, so that a warp runs one kind
@@ -426,7 +369,6 @@ ACVD_DEV void eval_tile(const DevState& st, int item0, int64_t count, int color,
                     if (may_move && (!fl.connexity || conn_ok)) {
                         const int w = (int)atomicAdd(&s_nwork, 1u);
                         s_idx[w] = (int)idx;
-                        s_same[w] = (c.w & 16) ? 1 : 0;
                         int nt = 0;
 #pragma unroll
                         for (int q = 0; q < 3; q++)
@@ -456,17 +398,8 @@ ACVD_DEV void eval_tile(const DevState& st, int item0, int64_t count, int color,
 #pragma unroll
             for (int q = 0; q < kRingPref; q++) deg += lb[q] >= 0;
         }
-        unsigned valid = 0u;   // ring slots that hold a neighbour (the others are padding)
-#pragma unroll
-        for (int q = 0; q < kRingPref; q++) valid |= (lb[q] >= 0 ? 1u : 0u) << q;
 #pragma unroll
         for (int q = 0; q < kRingPref; q++) lb[q] = lb[q] >= 0 ? st.label[lb[q]] : L;
-        // a ring member of the item's own cluster: in another colour class, it stays
-        // put this step, so the cluster cannot be emptied by the item leaving it
-        bool same = false;
-#pragma unroll
-        for (int q = 0; q < kRingPref; q++)
-            if (((valid >> q) & 1u) && lb[q] == L) same = true;
         bool fresh = ev_i <= sw.floor || (L < st.k && st.stamp[L] >= ev_i);
         n_slots = (unsigned)deg;
         bool boundary = false;
@@ -485,8 +418,6 @@ ACVD_DEV void eval_tile(const DevState& st, int item0, int64_t count, int color,
                 if (B != L) {
                     boundary = true;
                     if (B < st.k && st.stamp[B] >= ev_i) fresh = true;
-                } else {
-                    same = true;
                 }
             }
         }
@@ -510,7 +441,7 @@ ACVD_DEV void eval_tile(const DevState& st, int item0, int64_t count, int color,
                 n++;
             }
             if (n <= 3) {
-                int meta = n | (same ? 16 : 0);
+                int meta = n;
                 if (fl.connexity && may_move) {
                     conn = ring_connected_pref(st, st.row[i], st.row[i] + deg, L, lb) ? 1 : 0;
                     meta |= 4 | (conn ? 8 : 0);
@@ -527,7 +458,6 @@ ACVD_DEV void eval_tile(const DevState& st, int item0, int64_t count, int color,
             if (movable) {
                 const int w = (int)atomicAdd(&s_nwork, 1u);
                 s_idx[w] = (int)idx;
-                s_same[w] = same ? 1 : 0;
                 int nt = 0;
                 bool all = L < st.k && deg <= kRingPref;
 #pragma unroll
@@ -649,22 +579,18 @@ ACVD_DEV void eval_tile(const DevState& st, int item0, int64_t count, int color,
             }
         }
         if (best >= 0) {
-            n_cand = 1;
-            st.evald[i] = -1;
+            cand_dest[widx] = best;
+            cand_prio[widx] = pr;
             if (claims) {
-                cand_dest[widx] = best;
-                cand_prio[widx] = pr;
                 const unsigned long long c = make_claim((unsigned)epoch, pr, (unsigned)widx);
                 if (L < st.k) atomicMin(&st.claim[L], c);
                 atomicMin(&st.claim[best], c);
-                my_cand = widx;
-            } else if (L >= st.k || s_same[w]) {
-                // relaxed step: every proposal commits now, except one whose cluster
-                // could be emptied (no ring member of its own cluster stays put); that
-                // item is evaluated again next sweep
-                relaxed_commit_item<M>(st, i, L, best);
-                n_move = 1;
+            } else if (L < st.k) {
+                atomicAdd(&st.out_cnt[L], 1);   // relaxed step: proposals leaving L
             }
+            n_cand = 1;
+            my_cand = widx;
+            st.evald[i] = -1;
         } else {
             st.evald[i] = sw.sweep;
         }
@@ -673,12 +599,12 @@ ACVD_DEV void eval_tile(const DevState& st, int item0, int64_t count, int color,
     // counters: one atomic per block and counter (tens of thousands of warps would
     // otherwise serialise on the class's count and the counter stripes)
     {
-        constexpr int kNC = 8;
+        constexpr int kNC = 7;
         __shared__ unsigned s_wc[8], s_base, s_cnt[8][kNC];
         const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
         const unsigned bal = __ballot_sync(kFull, my_cand >= 0);
         const unsigned v[kNC] = {(in && !listed) ? 1u : 0u, n_scr - n_cached, n_cached, n_slots, n_bnd, n_tgt,
-                                 n_cand, n_move};
+                                 n_cand};
 #pragma unroll
         for (int c = 0; c < kNC; c++) {
             const unsigned t = __reduce_add_sync(kFull, v[c]);
@@ -697,7 +623,7 @@ ACVD_DEV void eval_tile(const DevState& st, int item0, int64_t count, int color,
         } else if (threadIdx.x >= 32 && threadIdx.x < 32 + kNC) {
             const int c = threadIdx.x - 32;
             const int which[kNC] = {kCntVisited, kCntScreened, kCntCached, kCntSlots, kCntBoundary, kCntTargets,
-                                    kCntCand, kCntMoves};
+                                    kCntCand};
             unsigned t = 0;
             for (int w = 0; w < 8; w++) t += s_cnt[w][c];
             if (t) atomicAdd(ctr(st.counters, which[c]), (unsigned long long)t);
@@ -1205,28 +1131,99 @@ __global__ void reclaim_kernel(DevState st, int item0, int color, int round, int
 
 // ---------------------------------------------------------------------------
 // relaxed step (phases without the connectivity constraint): every proposal of
-// the colour class commits at once, in the evaluation's decision phase
-// (relaxed_commit_item), except one that could empty its cluster.  Items of one
-// colour are never adjacent, so a ring member of the item's own cluster stays put
-// during the step and proves that the cluster keeps a member.  Nothing the
-// evaluation reads changes during the step: cluster records, sizes and stamps are
-// updated by fx_finalize afterwards, and the labels and boundary flags a commit
-// writes belong to the item and its ring, which no other item of the class reads.
-// The committed moves' contributions are summed per cluster in 64-bit fixed point
-// -- exact, so the atomics' order does not matter -- and folded into the
-// compensated accumulators by fx_finalize.
+// the colour class commits at once, except that a cluster is never emptied.
+// Items of one colour are never adjacent.  The committed moves' contributions are
+// summed per cluster in 64-bit fixed point -- exact, so the atomics' order does
+// not matter -- and folded into the compensated accumulators by fx_finalize.
 // ---------------------------------------------------------------------------
+
+// item contribution j (the accumulate_item components) as a double-float: the
+// products w x, A x and T x are formed exactly (TwoProd) and summed compensated
+template <int M>
+ACVD_DEV df contrib_df(const ItemRec& it, int j) {
+    const int rowi[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
+    if (j < 3) return two_prod(it.w, it.x[j]);
+    if (j == 3) return df_make(it.w);
+    if (j < 10) return df_make(it.A[j - 4]);
+    if (j < 13) {
+        const int c = j - 10;
+        return df_add(df_add(two_prod(it.A[rowi[c][0]], it.x[0]), two_prod(it.A[rowi[c][1]], it.x[1])),
+                      two_prod(it.A[rowi[c][2]], it.x[2]));
+    }
+    if (j < 19) return df_make(it.T[j - 13]);
+    const int c = j - 19;
+    return df_add(df_add(two_prod(it.T[rowi[c][0]], it.x[0]), two_prod(it.T[rowi[c][1]], it.x[1])),
+                  two_prod(it.T[rowi[c][2]], it.x[2]));
+}
+
+// Fixed-point units of component q: the scale is a power of two 2^e held as two
+// float factors (x, y; inverses in z, w), so both conversions are exact scalings.
+ACVD_DEV long long to_fixed(df v, float4 p) {
+    const float h = __fmul_rn(__fmul_rn(v.hi, p.x), p.y);
+    const float l = __fmul_rn(__fmul_rn(v.lo, p.x), p.y);
+    return __float2ll_rn(h) + __float2ll_rn(l);
+}
+
+ACVD_DEV df from_fixed(long long d, float4 p) {
+    const float h = __ll2float_rn(d);
+    const float l = __ll2float_rn(d - __float2ll_rn(h));
+    return df_renorm(__fmul_rn(__fmul_rn(h, p.z), p.w), __fmul_rn(__fmul_rn(l, p.z), p.w));
+}
+
+template <int M>
+ACVD_DEV void relaxed_commit_range(const DevState& st, int item0, int color,
+                                   const int* cand_dest, unsigned gtid, unsigned gstride) {
+    constexpr int NA = Layout<M>::acc;
+    const unsigned n = st.cand_count[color];
+    unsigned won = 0;
+    const int now = st.sweep->sweep;
+    for (unsigned j = gtid; j < n; j += gstride) {
+        const int idx = st.cand_list[j];
+        const int i = item0 + (int)idx;
+        const int B = cand_dest[idx];
+        const int L = st.label[i];
+        if (!ACVD_VALID(st, B >= 0 && B < st.k && L >= 0 && L <= st.k)) continue;
+        // sizes are untouched until fx_finalize: a cluster whose every member would
+        // leave keeps them all
+        if (L < st.k && st.size[L] - st.out_cnt[L] < 1) continue;
+        won++;
+        ItemRec it;
+        load_item<M>(st, i, it);
+        st.label[i] = B;
+        mark_ring(st, i);
+        atomicAdd(&st.in_done[B], 1);
+        st.stamp[B] = now;
+        long long* dB = st.fx_delta + (int64_t)B * NA;
+        long long* dL = st.fx_delta + (int64_t)(L < st.k ? L : 0) * NA;
+        if (L < st.k) {
+            atomicAdd(&st.out_done[L], 1);
+            st.stamp[L] = now;
+        }
+#pragma unroll
+        for (int q = 0; q < NA; q++) {
+            const long long v = to_fixed(contrib_df<M>(it, q), st.fx_pow[q]);
+            atomicAdd((unsigned long long*)&dB[q], (unsigned long long)v);
+            if (L < st.k) atomicAdd((unsigned long long*)&dL[q], (unsigned long long)(-v));
+        }
+    }
+    warp_count(ctr(st.counters, kCntMoves), won);
+}
+
+template <int M>
+__global__ void relaxed_commit_kernel(DevState st, int item0, int color, const int* cand_dest) {
+    relaxed_commit_range<M>(st, item0, color, cand_dest, blockIdx.x * blockDim.x + threadIdx.x,
+                            gridDim.x * blockDim.x);
+}
 
 template <int M>
 ACVD_DEV void fx_finalize_range(const DevState& st, int64_t k0, int64_t kstride) {
     constexpr int NA = Layout<M>::acc;
-    const int now = st.sweep->sweep;
     for (int64_t k = k0; k < st.k; k += kstride) {
         const int in = st.in_done[k], out = st.out_done[k];
+        st.out_cnt[k] = 0;
         if (in == 0 && out == 0) continue;
         st.in_done[k] = 0;
         st.out_done[k] = 0;
-        st.stamp[k] = now;   // modified in this step (stamped after the step's evaluation)
         st.size[k] += in - out;
         df* a = st.acc + k * NA;
         long long* d = st.fx_delta + k * NA;
@@ -1411,6 +1408,8 @@ __global__ void __launch_bounds__(256, 2) sweep_run_kernel(SweepRun a) {
             if (!grid_barrier(a.bar)) return;
             if (lead) a.ls->eval_ns += global_ns() - t0;
             if (relaxed) {
+                relaxed_commit_range<M>(st, item0, c, a.cand_dest, gtid, gstride);
+                if (!grid_barrier(a.bar)) return;
                 fx_finalize_range<M>(st, gtid, gstride);
                 if (!grid_barrier(a.bar)) return;
             } else {
@@ -1926,6 +1925,7 @@ cudaError_t launch_reclaim(const DevState& st, int item0, int64_t count, int col
 cudaError_t launch_relaxed_step(int metric, const DevState& st, int item0, int64_t count, int color,
                                 const int* cand_dest, cudaStream_t s) {
     if (count == 0) return cudaSuccess;
+    ACVD_DISPATCH(metric, relaxed_commit_kernel, list_grid(count), 256, s, st, item0, color, cand_dest);
     ACVD_DISPATCH(metric, fx_finalize_kernel, nblk(st.k, 64), 64, s, st);   // small blocks: every SM gets some
     return cudaGetLastError();
 }

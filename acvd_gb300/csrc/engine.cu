@@ -107,7 +107,7 @@ struct acvd_ctx {
     // relaxed steps
     DBuf<long long> fx_delta;
     DBuf<float4> fx_pow;
-    DBuf<int> in_done, out_done;
+    DBuf<int> out_cnt, in_done, out_done;
     bool use_relaxed = true;       // ACVD_RELAXED=0 turns relaxed steps off
     DBuf<df> acc;
     DBuf<float4> ev;
@@ -197,6 +197,7 @@ struct acvd_ctx {
         st.cand_count = cand_count.p;
         st.fx_delta = fx_delta.p;
         st.fx_pow = fx_pow.p;
+        st.out_cnt = out_cnt.p;
         st.in_done = in_done.p;
         st.out_done = out_done.p;
         st.ring8 = ring8.p;
@@ -774,6 +775,7 @@ int acvd_set_labels(acvd_ctx* ctx, int32_t k, const int32_t* labels) {
     CK(ctx->size.resize(k + 1));
     CK(ctx->stamp.resize(k + 1));
     CK(ctx->fx_delta.resize((size_t)(k + 1) * acc_stride(kAniso)));
+    CK(ctx->out_cnt.resize(k + 1));
     CK(ctx->in_done.resize(k + 1));
     CK(ctx->out_done.resize(k + 1));
     CK(ctx->claim.resize(k + 1));
@@ -1007,7 +1009,7 @@ static int enqueue_sweep(acvd_ctx* ctx, bool timing, bool relaxed) {
         if (timing) CK(cudaEventRecordWithFlags(ctx->ev_eval[2 * c + 1], ctx->s, cudaEventRecordExternal));
         if (relaxed) {
             CK(launch_relaxed_step(ctx->metric, st, item0, cnt, c, ctx->cand_dest.p, ctx->s));
-            kernels += 2;
+            kernels += 3;
             continue;
         }
         CK(launch_apply(ctx->metric, st, item0, cnt, c, 0, ctx->cand_dest.p, ctx->cand_prio.p, ctx->s));
@@ -1319,6 +1321,7 @@ extern "C" int acvd_minimize(acvd_ctx* ctx, acvd_stats* stats) {
         }
         if ((r = set_sweep_state(ctx, 0, 0))) { status = r; break; }
         if (cudaMemsetAsync(ctx->fx_delta.p, 0, (size_t)(ctx->K + 1) * acc_stride(kAniso) * sizeof(long long), ctx->s) ||
+            cudaMemsetAsync(ctx->out_cnt.p, 0, (ctx->K + 1) * sizeof(int), ctx->s) ||
             cudaMemsetAsync(ctx->in_done.p, 0, (ctx->K + 1) * sizeof(int), ctx->s) ||
             cudaMemsetAsync(ctx->out_done.p, 0, (ctx->K + 1) * sizeof(int), ctx->s)) {
             status = fail(ctx, ACVD_ERR_CUDA, "memset of the relaxed-step arrays failed");

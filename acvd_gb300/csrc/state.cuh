@@ -142,6 +142,7 @@ struct DevState {
     long long* fx_delta;   // K x acc stride
     const float4* fx_pow;  // per accumulator component: fixed-point scale 2^e as two float factors
                            // (x, y) and their inverses (z, w)
+    int* out_cnt;          // proposals leaving the cluster in this step
     int* in_done;          // committed moves into the cluster
     int* out_done;         // committed moves out of the cluster
     // per item: 0 = certainly interior (every ring label equals its own), 1 = maybe
