@@ -622,11 +622,11 @@ ACVD_DEV void eval_tile(const DevState& st, int item0, int64_t count, int color,
             s_base = tot ? atomicAdd(&st.cand_count[color], tot) : 0u;
         } else if (threadIdx.x >= 32 && threadIdx.x < 32 + kNC) {
             const int c = threadIdx.x - 32;
-            const int which[kNC] = {kCntVisited, kCntScreened, kCntCached, kCntSlots, kCntBoundary, kCntTargets,
-                                    kCntCand};
+            const int which = c == 0 ? kCntVisited : c == 1 ? kCntScreened : c == 2 ? kCntCached
+                            : c == 3 ? kCntSlots : c == 4 ? kCntBoundary : c == 5 ? kCntTargets : kCntCand;
             unsigned t = 0;
             for (int w = 0; w < 8; w++) t += s_cnt[w][c];
-            if (t) atomicAdd(ctr(st.counters, which[c]), (unsigned long long)t);
+            if (t) atomicAdd(ctr(st.counters, which), (unsigned long long)t);
         }
         __syncthreads();
         if (my_cand >= 0) st.cand_list[s_base + s_wc[wid] + __popc(bal & ((1u << lane) - 1u))] = my_cand;
@@ -783,8 +783,19 @@ __global__ void __launch_bounds__(256, 4) screen_kernel(DevState st, int item0, 
 
 // The work list of a screen_kernel pass through eval_tile, 256 entries per tile,
 // grid-stride over (stripe, tile) pairs.
+// blocks per SM of the work-list evaluation: a persistent grid over the forwarded
+// items, where spills of the energy tests cost more than occupancy gains
+#ifndef ACVD_LIST_MINB
+#define ACVD_LIST_MINB 4
+#endif
+#ifndef ACVD_LIST_MINB_ANISO
+#define ACVD_LIST_MINB_ANISO 4
+#endif
+template <int M> struct ListMinBlocks { static constexpr int value = ACVD_LIST_MINB; };
+template <> struct ListMinBlocks<kAniso> { static constexpr int value = ACVD_LIST_MINB_ANISO; };
+
 template <int M>
-__global__ void __launch_bounds__(256, EvalMinBlocks<M>::value) eval_list_kernel(DevState st, int item0, int64_t count,
+__global__ void __launch_bounds__(256, ListMinBlocks<M>::value) eval_list_kernel(DevState st, int item0, int64_t count,
                                                                               int color, int* cand_dest,
                                                                               unsigned* cand_prio, int claims,
                                                                               const int* work,

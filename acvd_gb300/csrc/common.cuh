@@ -201,32 +201,52 @@ ACVD_DEV void jacobi_eig3(const T a6[6], T w[3], T V[3][3], int max_sweeps) {
 // decreasing |lambda|; at most `level` of them, and only those with
 // |lambda| / max|lambda| > thr, are inverted.  Returns pinv(A) r in d and the
 // rank deficiency.
+// One eigenpair: |lambda|, lambda, eigenvector.
+template <typename T>
+struct EigPair {
+    T a, w, v0, v1, v2;
+};
+
+// Swaps x and y when x.a < y.a (strictly), so that equal magnitudes keep their order.
+template <typename T>
+ACVD_DEV void eig_order(EigPair<T>& x, EigPair<T>& y) {
+    if (x.a < y.a) {
+        const EigPair<T> t = x;
+        x = y;
+        y = t;
+    }
+}
+
 template <typename T>
 ACVD_DEV int pinv_apply(const T a6[6], const T r[3], T d[3], int level, T thr, int max_sweeps) {
     T w[3], V[3][3];
     jacobi_eig3<T>(a6, w, V, max_sweeps);
-    T aw[3] = {fabs(w[0]), fabs(w[1]), fabs(w[2])};
-    const T mx = fmax(aw[0], fmax(aw[1], aw[2]));
+    // the eigenpairs in decreasing |lambda|, equal magnitudes in index order (a stable
+    // three-element sorting network on registers)
+    EigPair<T> e0 = {fabs(w[0]), w[0], V[0][0], V[1][0], V[2][0]};
+    EigPair<T> e1 = {fabs(w[1]), w[1], V[0][1], V[1][1], V[2][1]};
+    EigPair<T> e2 = {fabs(w[2]), w[2], V[0][2], V[1][2], V[2][2]};
+    eig_order(e0, e1);
+    eig_order(e1, e2);
+    eig_order(e0, e1);
+    const T mx = e0.a;
     d[0] = d[1] = d[2] = T(0);
     int used = 0, rank_def = 0;
-#pragma unroll
-    for (int it = 0; it < 3; it++) {
-        int im = 0;
-        if (aw[1] > aw[im]) im = 1;
-        if (aw[2] > aw[im]) im = 2;
-        const T lam = w[im];
-        const bool keep = (mx > T(0)) && (aw[im] > thr * mx) && (used < level);
+    auto take = [&](const EigPair<T>& e) {
+        const bool keep = (mx > T(0)) && (e.a > thr * mx) && (used < level);
         if (keep) {
-            const T proj = (V[0][im] * r[0] + V[1][im] * r[1] + V[2][im] * r[2]) / lam;
-            d[0] += proj * V[0][im];
-            d[1] += proj * V[1][im];
-            d[2] += proj * V[2][im];
+            const T proj = (e.v0 * r[0] + e.v1 * r[1] + e.v2 * r[2]) / e.w;
+            d[0] += proj * e.v0;
+            d[1] += proj * e.v1;
+            d[2] += proj * e.v2;
             used++;
         } else {
             rank_def++;
         }
-        aw[im] = T(-1);
-    }
+    };
+    take(e0);
+    take(e1);
+    take(e2);
     return rank_def;
 }
 
