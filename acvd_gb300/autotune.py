@@ -16,7 +16,10 @@ Two families of candidates:
     - ``persistent``: one cooperative kernel per phase with grid barriers;
     - ``fused``: the launch shape of the evaluation -- every colour class through the one
       fused evaluation kernel, where the default splits large classes into a screen pass
-      and an evaluation over the forwarded work list.
+      and an evaluation over the forwarded work list;
+    - ``blocks3`` / ``blocks4`` / ``blocks5``: the evaluation kernels compiled for 3, 4 or 5
+      blocks of 256 threads per SM (80, 64 or 48 registers per thread) instead of the
+      per-kernel defaults.
   A candidate of this family whose labels differ from the default's is rejected, since that
   would mean a broken guarantee rather than a faster schedule.
 * approximate schedules (opt-in) reach a different deterministic clustering:
@@ -36,9 +39,9 @@ wall time of the engine's set-up for the problem (``end_to_end``: the host colou
 set-up time that a one-off solve pays).
 
 The schedules' switches are the engine's own (the ``persistent`` option of ``acvd_opts`` and the
-``ACVD_HOST_LOOP`` / ``ACVD_RELAXED`` / ``ACVD_MATCH_ROUNDS`` / ``ACVD_COLORING`` /
-``ACVD_SPLIT_MIN`` environment switches). The engine reads ``ACVD_RELAXED`` and
-``ACVD_MATCH_ROUNDS`` when a context is created, ``ACVD_COLORING`` and ``ACVD_SPLIT_MIN`` when it
+``ACVD_HOST_LOOP`` / ``ACVD_RELAXED`` / ``ACVD_MATCH_ROUNDS`` / ``ACVD_EVAL_BLOCKS`` /
+``ACVD_COLORING`` / ``ACVD_SPLIT_MIN`` environment switches). The engine reads ``ACVD_RELAXED``,
+``ACVD_MATCH_ROUNDS`` and ``ACVD_EVAL_BLOCKS`` when a context is created, ``ACVD_COLORING`` and ``ACVD_SPLIT_MIN`` when it
 takes a mesh and ``ACVD_HOST_LOOP`` when it minimises, so ``ScheduledEngine`` sets them only
 around those calls and puts the environment back afterwards.
 """
@@ -69,12 +72,14 @@ class Schedule:
     match_rounds: int = 1
     coloring: str = "jp"           # jp (device Jones-Plassmann) | order | squeeze
     split_min: int | None = None   # None: the engine's threshold; 0: never split
+    eval_blocks: int | None = None  # evaluation kernels' blocks per SM (3, 4, 5); None: the defaults
     exact: bool = True   # same clustering as the default schedule, bit for bit
 
     def create_env(self) -> dict:
         """Switches the engine reads in acvd_create (None = unset)."""
         return {"ACVD_RELAXED": None if self.relaxed else "0",
-                "ACVD_MATCH_ROUNDS": None if self.match_rounds == 1 else str(int(self.match_rounds))}
+                "ACVD_MATCH_ROUNDS": None if self.match_rounds == 1 else str(int(self.match_rounds)),
+                "ACVD_EVAL_BLOCKS": None if self.eval_blocks is None else str(int(self.eval_blocks))}
 
     def mesh_env(self) -> dict:
         """Switches the engine reads in acvd_set_mesh."""
@@ -88,7 +93,8 @@ class Schedule:
 
 DEFAULT = Schedule("graphs")
 EXACT_SCHEDULES = (DEFAULT, Schedule("host_loop", host_loop=True), Schedule("persistent", persistent=True),
-                   Schedule("fused", split_min=0))
+                   Schedule("fused", split_min=0), Schedule("blocks3", eval_blocks=3),
+                   Schedule("blocks4", eval_blocks=4), Schedule("blocks5", eval_blocks=5))
 APPROX_SCHEDULES = (Schedule("exact_sweeps", relaxed=False, exact=False),
                     Schedule("match2", match_rounds=2, exact=False),
                     Schedule("order_colors", coloring="order", exact=False),

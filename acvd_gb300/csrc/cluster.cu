@@ -633,24 +633,23 @@ ACVD_DEV void eval_tile(const DevState& st, int item0, int64_t count, int color,
     }
 }
 
-// blocks per SM the evaluation kernel is compiled for (registers per thread
-// follow: 3 -> 80, 4 -> 64, 5 -> 48)
-#ifndef ACVD_EVAL_MINB
-#define ACVD_EVAL_MINB 4
-#endif
-// the quadric-anisotropic evaluation at 5 blocks per SM (48 registers, more spills):
-// faster on the 4096^2 heightfield (330 ms against 347 ms); 4 stays faster for QEM
-#ifndef ACVD_EVAL_MINB_ANISO
-#define ACVD_EVAL_MINB_ANISO 5
-#endif
-template <int M> struct EvalMinBlocks { static constexpr int value = ACVD_EVAL_MINB; };
-template <> struct EvalMinBlocks<kAniso> { static constexpr int value = ACVD_EVAL_MINB_ANISO; };
-
-template <int M>
-__global__ void __launch_bounds__(256, EvalMinBlocks<M>::value) eval_kernel(DevState st, int item0, int64_t count,
-                                                      int color, int* cand_dest, unsigned* cand_prio, int claims) {
+// The evaluation kernels are compiled for 3, 4 and 5 blocks of 256 threads per SM
+// (registers per thread follow: 3 -> 80, 4 -> 64, 5 -> 48): fewer blocks spill
+// less of the energy tests, more hide more latency, and which wins depends on the
+// metric and the workload.  launch_eval takes the count at run time (the context's
+// eval_blocks, ACVD_EVAL_BLOCKS; the autotuner times the choices); 0 selects the
+// defaults below, measured on GB300.
+template <int M, int B>
+__global__ void __launch_bounds__(256, B) eval_kernel(DevState st, int item0, int64_t count, int color,
+                                                      int* cand_dest, unsigned* cand_prio, int claims) {
     eval_tile<M>(st, item0, count, color, cand_dest, cand_prio, claims, blockIdx.x);
 }
+
+// default blocks per SM: the fused evaluation 4 (isotropic, QEM) and 5 (the
+// quadric-anisotropic metric: 330 ms against 347 ms on the 4096^2 heightfield when it
+// ran every class); the work-list evaluation 4 (222 ms against 232 at 3 and 241 at 5)
+constexpr int default_eval_blocks(int metric) { return metric == kAniso ? 5 : 4; }
+constexpr int kDefaultListBlocks = 4;
 
 // ---------------------------------------------------------------------------
 // Split evaluation of a large colour class: screen_kernel streams the class and
@@ -783,23 +782,10 @@ __global__ void __launch_bounds__(256, 4) screen_kernel(DevState st, int item0, 
 
 // The work list of a screen_kernel pass through eval_tile, 256 entries per tile,
 // grid-stride over (stripe, tile) pairs.
-// blocks per SM of the work-list evaluation: a persistent grid over the forwarded
-// items, where spills of the energy tests cost more than occupancy gains
-#ifndef ACVD_LIST_MINB
-#define ACVD_LIST_MINB 4
-#endif
-#ifndef ACVD_LIST_MINB_ANISO
-#define ACVD_LIST_MINB_ANISO 4
-#endif
-template <int M> struct ListMinBlocks { static constexpr int value = ACVD_LIST_MINB; };
-template <> struct ListMinBlocks<kAniso> { static constexpr int value = ACVD_LIST_MINB_ANISO; };
-
-template <int M>
-__global__ void __launch_bounds__(256, ListMinBlocks<M>::value) eval_list_kernel(DevState st, int item0, int64_t count,
-                                                                              int color, int* cand_dest,
-                                                                              unsigned* cand_prio, int claims,
-                                                                              const int* work,
-                                                                              const unsigned* work_count) {
+template <int M, int B>
+__global__ void __launch_bounds__(256, B) eval_list_kernel(DevState st, int item0, int64_t count, int color,
+                                                           int* cand_dest, unsigned* cand_prio, int claims,
+                                                           const int* work, const unsigned* work_count) {
     __shared__ unsigned s_cnt[kWorkStripes];
     if (threadIdx.x < kWorkStripes) s_cnt[threadIdx.x] = work_count[color * kWorkStripes + threadIdx.x];
     __syncthreads();
@@ -1868,14 +1854,42 @@ static inline unsigned nblk(int64_t n, int b = 256) { return (unsigned)((n + b -
 
 static int64_t sm_count();
 
-// Blocks per SM of eval_list_kernel (its grid strides over the work list).
-static int eval_list_blocks_per_sm(int metric) {
+// (metric, blocks per SM) -> the instantiation; blocks outside 3..5 take `dflt`
+#define ACVD_DISPATCH_B(metric, blocks, dflt, KERNEL, grid, block, stream, ...)                               \
+    do {                                                                                                    \
+        ++g_launches;                                                                                       \
+        const int b_ = ((blocks) >= 3 && (blocks) <= 5) ? (blocks) : (dflt);                                \
+        if ((metric) == kIso) {                                                                             \
+            if (b_ == 3) KERNEL<kIso, 3><<<grid, block, 0, stream>>>(__VA_ARGS__);                          \
+            else if (b_ == 4) KERNEL<kIso, 4><<<grid, block, 0, stream>>>(__VA_ARGS__);                     \
+            else KERNEL<kIso, 5><<<grid, block, 0, stream>>>(__VA_ARGS__);                                  \
+        } else if ((metric) == kQEM) {                                                                      \
+            if (b_ == 3) KERNEL<kQEM, 3><<<grid, block, 0, stream>>>(__VA_ARGS__);                          \
+            else if (b_ == 4) KERNEL<kQEM, 4><<<grid, block, 0, stream>>>(__VA_ARGS__);                     \
+            else KERNEL<kQEM, 5><<<grid, block, 0, stream>>>(__VA_ARGS__);                                  \
+        } else {                                                                                            \
+            if (b_ == 3) KERNEL<kAniso, 3><<<grid, block, 0, stream>>>(__VA_ARGS__);                        \
+            else if (b_ == 4) KERNEL<kAniso, 4><<<grid, block, 0, stream>>>(__VA_ARGS__);                   \
+            else KERNEL<kAniso, 5><<<grid, block, 0, stream>>>(__VA_ARGS__);                                \
+        }                                                                                                   \
+    } while (0)
+
+// Resident blocks per SM of an eval_list_kernel instantiation (its grid strides over
+// the work list).
+template <int M, int B>
+static int list_occupancy() {
     int nb = 0;
-    cudaError_t e;
-    if (metric == kIso) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, eval_list_kernel<kIso>, 256, 0);
-    else if (metric == kQEM) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, eval_list_kernel<kQEM>, 256, 0);
-    else e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, eval_list_kernel<kAniso>, 256, 0);
+    const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, eval_list_kernel<M, B>, 256, 0);
     return (e == cudaSuccess && nb > 0) ? nb : 1;
+}
+
+static int eval_list_blocks_per_sm(int metric, int blocks) {
+    const int b = (blocks >= 3 && blocks <= 5) ? blocks : kDefaultListBlocks;
+    if (metric == kIso)
+        return b == 3 ? list_occupancy<kIso, 3>() : b == 4 ? list_occupancy<kIso, 4>() : list_occupancy<kIso, 5>();
+    if (metric == kQEM)
+        return b == 3 ? list_occupancy<kQEM, 3>() : b == 4 ? list_occupancy<kQEM, 4>() : list_occupancy<kQEM, 5>();
+    return b == 3 ? list_occupancy<kAniso, 3>() : b == 4 ? list_occupancy<kAniso, 4>() : list_occupancy<kAniso, 5>();
 }
 
 // Blocks per SM of screen_kernel (its grid strides over the class's tiles).
@@ -1889,19 +1903,19 @@ static int screen_blocks_per_sm(int metric) {
 }
 
 cudaError_t launch_eval(int metric, const DevState& st, int item0, int64_t count, int color,
-                        int* cand_dest, unsigned* cand_prio, bool claims, bool split, cudaStream_t s) {
+                        int* cand_dest, unsigned* cand_prio, bool claims, bool split, int blocks, cudaStream_t s) {
     if (count == 0) return cudaSuccess;
     if (!split) {
-        ACVD_DISPATCH(metric, eval_kernel, nblk(count), 256, s, st, item0, count, color, cand_dest, cand_prio,
-                      claims ? 1 : 0);
+        ACVD_DISPATCH_B(metric, blocks, default_eval_blocks(metric), eval_kernel, nblk(count), 256, s, st, item0,
+                        count, color, cand_dest, cand_prio, claims ? 1 : 0);
         return cudaGetLastError();
     }
     const unsigned sgrid = (unsigned)std::min<int64_t>(nblk(count, kScreenTile), sm_count() * screen_blocks_per_sm(metric));
     ACVD_DISPATCH(metric, screen_kernel, sgrid, 256, s, st, item0, count, color, st.work, st.work_count);
     const int64_t tiles = kWorkStripes * (work_cap(count) / 256);
-    const unsigned grid = (unsigned)std::min<int64_t>(tiles, sm_count() * eval_list_blocks_per_sm(metric));
-    ACVD_DISPATCH(metric, eval_list_kernel, grid, 256, s, st, item0, count, color, cand_dest, cand_prio,
-                  claims ? 1 : 0, (const int*)st.work, (const unsigned*)st.work_count);
+    const unsigned grid = (unsigned)std::min<int64_t>(tiles, sm_count() * eval_list_blocks_per_sm(metric, blocks));
+    ACVD_DISPATCH_B(metric, blocks, kDefaultListBlocks, eval_list_kernel, grid, 256, s, st, item0, count, color,
+                    cand_dest, cand_prio, claims ? 1 : 0, (const int*)st.work, (const unsigned*)st.work_count);
     return cudaGetLastError();
 }
 

@@ -134,6 +134,7 @@ struct acvd_ctx {
     std::vector<cudaEvent_t> ev_eval;
     bool timing_broken = false;    // event timing unavailable on this device / driver
     int match_rounds = 1;          // claim/commit rounds per colour step (ACVD_MATCH_ROUNDS, up to kRounds)
+    int eval_blocks = 0;           // evaluation kernels' blocks per SM, 3..5 (ACVD_EVAL_BLOCKS; 0 = defaults)
     int64_t sweep_kernels = 0;     // kernels in the sweep last enqueued
     int64_t loop_relaxed_kernels = 0, loop_exact_kernels = 0;   // kernels per sweep of the graph loop
     int64_t exact_kernels = 0, relaxed_kernels = 0;
@@ -505,6 +506,7 @@ acvd_ctx* acvd_create(const acvd_opts* opts) {
     else acvd_default_opts(&ctx->opts);
     if (const char* c = std::getenv("ACVD_SWEEP_COLORS")) ctx->sweep_by_color = std::atoi(c) != 0;
     if (const char* c = std::getenv("ACVD_RELAXED")) ctx->use_relaxed = std::atoi(c) != 0;
+    if (const char* b = std::getenv("ACVD_EVAL_BLOCKS")) ctx->eval_blocks = std::atoi(b);
     if (const char* r = std::getenv("ACVD_MATCH_ROUNDS")) {
         const int v = std::atoi(r);
         if (v >= 1 && v <= kRounds) ctx->match_rounds = v;
@@ -1004,7 +1006,8 @@ static int enqueue_sweep(acvd_ctx* ctx, bool timing, bool relaxed) {
         // cudaEventRecordExternal makes the records real graph nodes when captured
         if (timing) CK(cudaEventRecordWithFlags(ctx->ev_eval[2 * c], ctx->s, cudaEventRecordExternal));
         const bool split = ctx->has_work && ctx->split_min > 0 && cnt >= ctx->split_min;
-        CK(launch_eval(ctx->metric, st, item0, cnt, c, ctx->cand_dest.p, ctx->cand_prio.p, !relaxed, split, ctx->s));
+        CK(launch_eval(ctx->metric, st, item0, cnt, c, ctx->cand_dest.p, ctx->cand_prio.p, !relaxed, split,
+                       ctx->eval_blocks, ctx->s));
         if (split) kernels++;
         if (timing) CK(cudaEventRecordWithFlags(ctx->ev_eval[2 * c + 1], ctx->s, cudaEventRecordExternal));
         if (relaxed) {

@@ -291,7 +291,7 @@ cudaError_t launch_relaxed_step(int metric, const DevState& st, int item0, int64
                                 const int* cand_dest, cudaStream_t s);
 cudaError_t launch_fx_scale(int metric, const DevState& st, unsigned* maxbits, cudaStream_t s);
 cudaError_t launch_eval(int metric, const DevState& st, int item0, int64_t count, int color,
-                        int* cand_dest, unsigned* cand_prio, bool claims, bool split, cudaStream_t s);
+                        int* cand_dest, unsigned* cand_prio, bool claims, bool split, int blocks, cudaStream_t s);
 cudaError_t launch_apply(int metric, const DevState& st, int item0, int64_t count, int color, int round,
                          int* cand_dest, const unsigned* cand_prio, cudaStream_t s);
 cudaError_t launch_reclaim(const DevState& st, int item0, int64_t count, int color, int round,

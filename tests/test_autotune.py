@@ -28,7 +28,7 @@ def test_fastest_exact_schedule_chosen_and_cached(tmp_path):
     measure, calls = _fake({"graphs": [3.0, 2.9, 3.1], "host_loop": [4.0, 4.1, 3.9], "persistent": [2.0, 2.2, 2.1]})
     s, rep = at.Autotuner(path).tune("gb300|qem|n2^19_k2^14", measure)
     assert s == at.BY_NAME["persistent"] and not rep["cached"]
-    assert calls == ["graphs", "host_loop", "persistent", "fused"]
+    assert calls == ["graphs", "host_loop", "persistent", "fused", "blocks3", "blocks4", "blocks5"]
     assert rep["ms"] == pytest.approx(2.1)
     with open(path) as f:
         assert json.load(f)["gb300|qem|n2^19_k2^14"]["schedule"] == "persistent"
@@ -39,7 +39,7 @@ def test_fastest_exact_schedule_chosen_and_cached(tmp_path):
     # retune measures again
     measure3, calls3 = _fake({"graphs": [1.0], "host_loop": [4.0], "persistent": [2.0]})
     s3, _ = at.Autotuner(path).tune("gb300|qem|n2^19_k2^14", measure3, retune=True)
-    assert s3 == at.DEFAULT and len(calls3) == 4
+    assert s3 == at.DEFAULT and len(calls3) == 7
 
 
 def test_exact_schedule_with_another_clustering_is_rejected():
@@ -75,7 +75,8 @@ def test_cached_approximate_choice_not_returned_to_a_default_tuner(tmp_path):
     # a default (exact-only) tuner on the same file must not answer with match2
     measure2, calls2 = _fake(times)
     s2, rep2 = at.Autotuner(path).tune("k", measure2)
-    assert s2.exact and not rep2["cached"] and calls2 == ["graphs", "host_loop", "persistent", "fused"]
+    assert s2.exact and not rep2["cached"] and calls2 == ["graphs", "host_loop", "persistent", "fused", "blocks3",
+                                                           "blocks4", "blocks5"]
     # an opt-in tuner with a tighter tolerance than the cached choice's measures again
     at.Autotuner(path, include_approximate=True).tune("k2", _fake(times, digests={"match2": "y"})[0])
     tight = at.Autotuner(path, include_approximate=True, energy_rel_tol=1e-4)
@@ -138,6 +139,7 @@ def test_mesh_switches_and_end_to_end_objective():
     assert at.BY_NAME["order_colors"].mesh_env() == {"ACVD_COLORING": "order", "ACVD_SPLIT_MIN": None}
     assert at.BY_NAME["fused"].mesh_env() == {"ACVD_COLORING": None, "ACVD_SPLIT_MIN": "0"}
     assert at.BY_NAME["fused"].exact and not at.BY_NAME["order_colors"].exact
+    assert at.BY_NAME["blocks3"].create_env()["ACVD_EVAL_BLOCKS"] == "3" and at.BY_NAME["blocks3"].exact
     times = {"graphs": [10.0], "host_loop": [12.0], "persistent": [12.0], "fused": [11.0], "order_colors": [8.0]}
     setup = {"order_colors": 5.0, "graphs": 1.0, "fused": 1.0}
     dig = {"order_colors": "o"}
