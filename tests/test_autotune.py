@@ -123,7 +123,7 @@ def test_schedule_switches_are_the_engines():
     assert at.DEFAULT.run_env() == {"ACVD_HOST_LOOP": None}
     assert at.BY_NAME["exact_sweeps"].create_env()["ACVD_RELAXED"] == "0"
     assert at.BY_NAME["match2"].create_env()["ACVD_MATCH_ROUNDS"] == "2"
-    assert at.DEFAULT.create_env() == {"ACVD_RELAXED": None, "ACVD_MATCH_ROUNDS": None}
+    assert at.DEFAULT.create_env() == {"ACVD_RELAXED": None, "ACVD_MATCH_ROUNDS": None, "ACVD_EVAL_BLOCKS": None}
     assert at.BY_NAME["persistent"].persistent and all(s.exact for s in at.EXACT_SCHEDULES)
     assert not any(s.exact for s in at.APPROX_SCHEDULES)
 
