@@ -969,6 +969,38 @@ def choose_schedule(args, metric, n, k, device, measure_kw):
     return sched, {"chosen": sched.name, "objective": rep["objective"], "tuning_s": secs, "trials": trials}
 
 
+def roofline_by_phase(make_engine, peak):
+    """The evaluation's roofline split by sweep kind, from one more converged solve with
+    the per-sweep log on (ACVD_SWEEP_LOG: CUDA events around every evaluation, the
+    host loop): relaxed sweeps (no connectivity constraint, many moves) and exact
+    sweeps (claims, the connectivity phase's long tail)."""
+    import tempfile
+    with tempfile.TemporaryDirectory() as td:
+        path = os.path.join(td, "sweeps.jsonl")
+        old = os.environ.get("ACVD_SWEEP_LOG")
+        os.environ["ACVD_SWEEP_LOG"] = path
+        try:
+            e = make_engine(False)
+            e.minimize()
+            e.close()
+        finally:
+            if old is None:
+                os.environ.pop("ACVD_SWEEP_LOG", None)
+            else:
+                os.environ["ACVD_SWEEP_LOG"] = old
+        with open(path) as f:
+            rows = [json.loads(line) for line in f if '"event"' not in line]
+    out = {}
+    for mode in ("relaxed", "exact"):
+        sel = [r for r in rows if r["mode"] == mode]
+        ms = sum(r["eval_ms"] for r in sel)
+        by = sum(r["eval_bytes"] for r in sel)
+        gbs = by / 1e6 / ms if ms > 0 else None
+        out[mode] = {"sweeps": len(sel), "eval_ms": ms, "algorithmic_bytes": by, "achieved_gbs": gbs,
+                     "frac": (gbs / peak) if gbs else None}
+    return out
+
+
 def batch_line(args, name, steps, warmup, e2e_on, cpu_on):
     """Batched workload: the rank's share of the meshes (balanced by items) in one packed
     CSR, one minimisation per step.  At N ranks the batch holds N x 256 meshes (the
@@ -1013,6 +1045,7 @@ def batch_line(args, name, steps, warmup, e2e_on, cpu_on):
     engt = make_engine(True)
     _, tot_t, _ = run_steps(torch, engt, steps, 1, device, ws, flush)
     engt.close()
+    by_phase = None if persistent else roofline_by_phase(make_engine, load_peaks().get("hbm_gbs", 6800.0))
     ms = statistics.mean(step_ms)
     ms = replicas.max_over_ranks(ms, device=f"cuda:{device}")   # the slowest rank
     value = len(specs) / (ms / 1000.0)
@@ -1110,7 +1143,7 @@ def batch_line(args, name, steps, warmup, e2e_on, cpu_on):
         "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": cfg,
         "schedule": sched.name, "tuning": tuning, "meshes_per_rank": [len(p) for p in parts], "items_per_rank": loads,
         "generation_s": gen_s,
-        "roofline": roofline_block(persistent, tot_t, name),
+        "roofline": dict(roofline_block(persistent, tot_t, name), by_sweep_kind=by_phase),
         "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(tot["kernel_launches"]),
         "sweeps_per_step": tot["sweeps"] / max(1, steps),
         "relaxed_sweeps_per_step": tot["relaxed_sweeps"] / max(1, steps),
@@ -1170,6 +1203,7 @@ def clustering_line(args, name, steps, warmup, e2e_on, cpu_on):
     engt = make_engine(True)
     _, tot_t, _ = run_steps(torch, engt, steps, 1, device, ws, flush)
     engt.close()
+    by_phase = None if persistent else roofline_by_phase(make_engine, load_peaks().get("hbm_gbs", 6800.0))
     ms = replicas.max_over_ranks(ms, device=f"cuda:{device}")   # the slowest replica
     value = ws * n / (ms / 1000.0)
     gpu_energy_fp64 = st["energy"]
@@ -1267,7 +1301,7 @@ def clustering_line(args, name, steps, warmup, e2e_on, cpu_on):
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": workload_config(name, w["desc"], n, w["k"], m.n_faces, ws),
         "schedule": sched.name, "tuning": tuning,
-        "roofline": roofline_block(persistent, tot_t, name),
+        "roofline": dict(roofline_block(persistent, tot_t, name), by_sweep_kind=by_phase),
         "cpu_baseline": cpu,
         "e2e": e2e,
         "gpu_launches": int(tot["kernel_launches"]),
