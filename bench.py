@@ -1411,10 +1411,21 @@ def run_gpu_arm(args):
 
 
 def solve_once(args):
-    """One engine set-up and one converged solve of a clustering workload, untimed: the
-    program that ncu captures are taken on (launch lists, per-launch DRAM traffic)."""
+    """One engine set-up and one converged solve of a clustering workload (or the batch),
+    untimed: the program that ncu captures are taken on (launch lists, per-launch DRAM
+    traffic)."""
     import acvd_gb300
     from acvd_gb300 import engine as E
+    if args.workload in BATCH_WORKLOADS:
+        from acvd_gb300 import batch as B
+        w = BATCH_WORKLOADS[args.workload]
+        b = B.synthetic_batch(w["n_meshes"], w["seed"], metric=w["metric"], gradation=w["gradation"])
+        e, st = B.run_on_gpu(b, unconstrained_init=w["uinit"])
+        e.close()
+        print(json.dumps({"workload": args.workload, "sweeps": st["sweeps"], "moves": st["moves"],
+                          "device_ms": st["device_ms"], "eval_bytes": st["eval_bytes"],
+                          "kernel_launches": st["kernel_launches"]}), flush=True)
+        return
     m, ind, pd, w = make_workload(args.workload)
     lab0, (row, col, ev) = initial_labels(m, w["metric"], ind, w["gradation"], w["k"], w.get("init"))
     e = E.Engine()
@@ -1450,8 +1461,8 @@ def main():
                     help="set up and run one converged solve of a clustering workload, untimed (for ncu)")
     args = ap.parse_args()
     if args.solve_once:
-        if args.workload not in WORKLOADS:
-            raise SystemExit("--solve-once takes a clustering workload")
+        if args.workload not in WORKLOADS and args.workload not in BATCH_WORKLOADS:
+            raise SystemExit("--solve-once takes a clustering or batch workload")
         solve_once(args)
         return
     if args.impl == "reference" and args.workload in SUBDIVISION_WORKLOADS:
