@@ -7,6 +7,8 @@
 #include <cstdlib>
 #include <chrono>
 #include <cstring>
+#include <functional>
+#include <future>
 #include <string>
 #include <vector>
 
@@ -302,13 +304,18 @@ constexpr int64_t kDefaultSplitMin = 600000;
 // colour unused by its lower-numbered neighbours.  On meshes stored in a spatially
 // coherent order (grids, scans) it gives 4 balanced classes where the device's
 // hashed Jones-Plassmann colouring gives 6-7 with a few tiny ones.  Returns the
-// largest colour, or -1 when a vertex would need a 65th colour.
-static int greedy_colors_host(const int32_t* row, const int32_t* col, int64_t n, std::vector<int>& color) {
+// largest colour, -1 when a vertex would need a 65th colour, -2 when the rings are
+// malformed (offsets outside [0, n_slots] or decreasing, ids outside [0, n)): it runs
+// beside the device's validation of the same arrays, so it checks them itself.
+static int greedy_colors_host(const int32_t* row, const int32_t* col, int64_t n, int64_t n_slots,
+                              std::vector<int>& color) {
     color.assign(n, -1);
     int maxc = 0;
     for (int64_t v = 0; v < n; v++) {
+        if (row[v] < 0 || row[v + 1] < row[v] || row[v + 1] > n_slots) return -2;
         unsigned long long used = 0ull;
         for (int p = row[v]; p < row[v + 1]; p++) {
+            if (col[p] < 0 || col[p] >= n) return -2;
             const int c = color[col[p]];
             if (c >= 0) used |= 1ull << c;
         }
@@ -360,42 +367,52 @@ static int squeeze_top_color(const int32_t* row, const int32_t* col, std::vector
     return maxc;
 }
 
-static int setup_colors(acvd_ctx* ctx, const int32_t* h_row, const int32_t* h_col) {
+// The colouring the next set-up uses: ACVD_COLORING=order (host greedy in vertex
+// order), squeeze (device colouring, then its top class emptied on the host), or the
+// device's hashed Jones-Plassmann colouring (unset or anything else).
+static const char* coloring_choice() {
+    const char* how = std::getenv("ACVD_COLORING");
+    return how ? how : "";
+}
+
+// host_colors: the host greedy colouring of the input rings (ACVD_COLORING=order),
+// started by acvd_set_mesh on a host thread before the device set-up and waited for
+// here; null for the device colouring.
+static int setup_colors(acvd_ctx* ctx, const int32_t* h_row, const int32_t* h_col, std::future<int>* host_colors,
+                        const std::vector<int>* host_color) {
     const int64_t n = ctx->nV;
     CK(ctx->wk_int.resize(n));
-    CK(cudaMemsetAsync(ctx->wk_int.p, 0xff, n * sizeof(int), ctx->s));   // color = -1
     CK(ctx->dtmp.resize(2));
     int* d_maxc = (int*)ctx->dtmp.p;
-    CK(cudaMemsetAsync(d_maxc, 0, sizeof(int), ctx->s));
-    // ACVD_COLORING=order: the host greedy colouring in vertex order instead
-    const char* how = std::getenv("ACVD_COLORING");
-    if (how && std::strcmp(how, "order") == 0) {
-        std::vector<int> hc;
-        const int mc = greedy_colors_host(h_row, h_col, n, hc);
-        if (mc < 0) return fail(ctx, ACVD_ERR_UNSUPPORTED, "more than 64 colours needed (vertex valence too high)");
-        CK(cudaMemcpyAsync(ctx->wk_int.p, hc.data(), n * sizeof(int), cudaMemcpyHostToDevice, ctx->s));
-        CK(cudaMemcpyAsync(d_maxc, &mc, sizeof(int), cudaMemcpyHostToDevice, ctx->s));
-        CK(cudaStreamSynchronize(ctx->s));
-    }
-    // rounds in groups of four between host checks (a round after the last one
-    // finds every item coloured and does nothing); the count left is the last
-    // round's number of items still waiting for a neighbour
-    int rounds = 0;
-    for (;;) {
-        for (int g = 0; g < 4; g++) {
-            CK(zero_counter(ctx, kCntChanged));
-            CK(launch_color_round(ctx->row.p, ctx->col.p, n, ctx->wk_int.p, ctx->counters.p + kCntChanged, d_maxc,
-                                  ctx->s));
-        }
-        int r = sync_counters(ctx);
-        if (r) return r;
-        if (ctx->h_counters[kCntChanged] == 0) break;
-        if ((rounds += 4) > 100000) return fail(ctx, ACVD_ERR_ITER_LIMIT, "graph colouring did not finish");
-    }
+    const char* how = coloring_choice();
     int maxc = 0;
-    CK(cudaMemcpy(&maxc, d_maxc, sizeof(int), cudaMemcpyDeviceToHost));
-    if (maxc >= 64) return fail(ctx, ACVD_ERR_UNSUPPORTED, "more than 64 colours needed (vertex valence too high)");
-    if (how && std::strcmp(how, "squeeze") == 0 && maxc > 0) {
+    if (host_colors) {
+        maxc = host_colors->get();
+        if (maxc == -2) return fail(ctx, ACVD_ERR_ARG, "acvd_set_mesh: malformed ring CSR");
+        if (maxc < 0) return fail(ctx, ACVD_ERR_UNSUPPORTED, "more than 64 colours needed (vertex valence too high)");
+        CK(cudaMemcpyAsync(ctx->wk_int.p, host_color->data(), n * sizeof(int), cudaMemcpyHostToDevice, ctx->s));
+    } else {
+        CK(cudaMemsetAsync(ctx->wk_int.p, 0xff, n * sizeof(int), ctx->s));   // color = -1
+        CK(cudaMemsetAsync(d_maxc, 0, sizeof(int), ctx->s));
+        // rounds in groups of four between host checks (a round after the last one
+        // finds every item coloured and does nothing); the count left is the last
+        // round's number of items still waiting for a neighbour
+        int rounds = 0;
+        for (;;) {
+            for (int g = 0; g < 4; g++) {
+                CK(zero_counter(ctx, kCntChanged));
+                CK(launch_color_round(ctx->row.p, ctx->col.p, n, ctx->wk_int.p, ctx->counters.p + kCntChanged,
+                                      d_maxc, ctx->s));
+            }
+            int r = sync_counters(ctx);
+            if (r) return r;
+            if (ctx->h_counters[kCntChanged] == 0) break;
+            if ((rounds += 4) > 100000) return fail(ctx, ACVD_ERR_ITER_LIMIT, "graph colouring did not finish");
+        }
+        CK(cudaMemcpy(&maxc, d_maxc, sizeof(int), cudaMemcpyDeviceToHost));
+        if (maxc >= 64) return fail(ctx, ACVD_ERR_UNSUPPORTED, "more than 64 colours needed (vertex valence too high)");
+    }
+    if (std::strcmp(how, "squeeze") == 0 && maxc > 0) {
         std::vector<int> hc(n);
         CK(cudaMemcpy(hc.data(), ctx->wk_int.p, n * sizeof(int), cudaMemcpyDeviceToHost));
         maxc = squeeze_top_color(h_row, h_col, hc, maxc);
@@ -552,6 +569,16 @@ int acvd_set_mesh(acvd_ctx* ctx, int64_t n_vertices, const double* xyz, int64_t 
     if (n_vertices >= (1ll << 26)) return fail(ctx, ACVD_ERR_UNSUPPORTED, "more than 2^26 vertices");
     if (csr_row[0] != 0 || csr_row[n_vertices] != 2 * n_edges)
         return fail(ctx, ACVD_ERR_ARG, "acvd_set_mesh: ring CSR does not hold 2 * n_edges entries");
+    // the host greedy colouring (ACVD_COLORING=order) reads only the host rings: it
+    // runs on a host thread while the copies, the validation and the vertex -> face
+    // sort run on the device (an early return below waits for it in the future's
+    // destructor, before host_color goes)
+    std::vector<int> host_color;
+    std::future<int> host_colors;
+    const bool host_order = std::strcmp(coloring_choice(), "order") == 0;
+    if (host_order)
+        host_colors = std::async(std::launch::async, greedy_colors_host, csr_row, csr_col, n_vertices,
+                                 2 * n_edges, std::ref(host_color));
     CK(cudaSetDevice(ctx->opts.device));
     ctx->drop_graph();
     ctx->ready_mesh = ctx->ready_metric = ctx->ready_labels = false;
@@ -602,7 +629,7 @@ int acvd_set_mesh(acvd_ctx* ctx, int64_t n_vertices, const double* xyz, int64_t 
         CK(launch_segment_offsets(k1.p, 3 * n_faces, (uint32_t)n_vertices, ctx->vf_row.p, ctx->s));
     }
     // colouring on the input rings, then the items in internal order
-    int r = setup_colors(ctx, csr_row, csr_col);
+    int r = setup_colors(ctx, csr_row, csr_col, host_order ? &host_colors : nullptr, &host_color);
     if (r) return r;
     int* d_maxdeg = nullptr;
     CK(ctx->dtmp.resize(2));
