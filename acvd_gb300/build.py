@@ -62,10 +62,9 @@ def _stale(obj: str, deps: list[str]) -> bool:
 
 
 def build(verbose: bool = False, force: bool = False) -> str:
-    """ACVD_NVCC_FLAGS (environment) adds nvcc flags, e.g. the tuning macros
-    -DACVD_EVAL_MINB=<blocks per SM of the evaluation kernel> (isotropic / QEM) and
-    -DACVD_EVAL_MINB_ANISO=<the same for the quadric-anisotropic metric>; pass force=True
-    (or --force) when they change."""
+    """ACVD_NVCC_FLAGS (environment) adds nvcc flags (e.g. -DACVD_DEVICE_CHECKS for the
+    self-checking build); pass force=True (or --force) when they change.  The evaluation
+    kernels' blocks per SM are a run-time choice (ACVD_EVAL_BLOCKS), not a build flag."""
     os.makedirs(OUT, exist_ok=True)
     nvcc = _nvcc()
     extra = os.environ.get("ACVD_NVCC_FLAGS", "").split()

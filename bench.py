@@ -922,25 +922,34 @@ def roofline_kernel(persistent, tot_t):
     return "eval_kernel", tot_t["eval_ms"], tot_t["eval_launches"]
 
 
-def roofline_block(persistent, tot_t, workload):
+def eval_traffic(workload, coloring):
+    """DRAM bytes per evaluation launch of a workload under a colouring, from the
+    committed ncu summaries (profiles/eval_traffic.json): (bytes, how measured), or
+    (None, None) where no capture covers that evaluation."""
+    tpath = os.path.join(ROOT, "profiles", "eval_traffic.json")
+    try:
+        with open(tpath) as f:
+            entry = json.load(f).get(workload, {}).get(coloring)
+    except (OSError, ValueError, AttributeError):
+        return None, None
+    if not entry:
+        return None, None
+    return entry.get("bytes_per_launch"), entry.get("how")
+
+
+def roofline_block(persistent, tot_t, workload, coloring="jp"):
     """The dominant kernel's roofline from the instrumented pass, and its DRAM traffic
-    per launch from the committed ncu summary (profiles/eval_traffic.json)."""
+    per launch from the committed ncu summary (profiles/eval_traffic.json) of the same
+    evaluation (workload and colouring)."""
     peaks = load_peaks()
     peak = peaks.get("hbm_gbs", 6800.0)
     kname, kms, klaunch = roofline_kernel(persistent, tot_t)
     achieved = (tot_t["eval_bytes"] / 1e9) / (kms / 1000.0) if kms > 0 else None
-    traffic = None
-    tpath = os.path.join(ROOT, "profiles", "eval_traffic.json")
-    if os.path.exists(tpath):
-        try:
-            with open(tpath) as f:
-                traffic = json.load(f).get(workload)
-        except ValueError:
-            traffic = None
+    traffic, how = (None, None) if persistent else eval_traffic(workload, coloring)
     return {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": (achieved / peak) if achieved else None,
             "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if "hbm_gbs" in peaks else "fallback",
-            "traffic": traffic, "launches": klaunch,
+            "traffic": traffic, "traffic_source": how, "launches": klaunch,
             "algorithmic_bytes_per_launch": tot_t["eval_bytes"] / max(1, klaunch),
             "avg_launch_us": 1000.0 * kms / max(1, klaunch),
             "timing": "CUDA events around each launch, in a second pass of the same steps "
@@ -1143,7 +1152,7 @@ def batch_line(args, name, steps, warmup, e2e_on, cpu_on):
         "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": cfg,
         "schedule": sched.name, "tuning": tuning, "meshes_per_rank": [len(p) for p in parts], "items_per_rank": loads,
         "generation_s": gen_s,
-        "roofline": dict(roofline_block(persistent, tot_t, name), by_sweep_kind=by_phase),
+        "roofline": dict(roofline_block(persistent, tot_t, name, sched.coloring), by_sweep_kind=by_phase),
         "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(tot["kernel_launches"]),
         "sweeps_per_step": tot["sweeps"] / max(1, steps),
         "relaxed_sweeps_per_step": tot["relaxed_sweeps"] / max(1, steps),
@@ -1301,7 +1310,7 @@ def clustering_line(args, name, steps, warmup, e2e_on, cpu_on):
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": workload_config(name, w["desc"], n, w["k"], m.n_faces, ws),
         "schedule": sched.name, "tuning": tuning,
-        "roofline": dict(roofline_block(persistent, tot_t, name), by_sweep_kind=by_phase),
+        "roofline": dict(roofline_block(persistent, tot_t, name, sched.coloring), by_sweep_kind=by_phase),
         "cpu_baseline": cpu,
         "e2e": e2e,
         "gpu_launches": int(tot["kernel_launches"]),
