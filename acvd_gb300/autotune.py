@@ -19,7 +19,10 @@ Two families of candidates:
       and an evaluation over the forwarded work list;
     - ``blocks3`` / ``blocks4`` / ``blocks5``: the evaluation kernels compiled for 3, 4 or 5
       blocks of 256 threads per SM (80, 64 or 48 registers per thread) instead of the
-      per-kernel defaults.
+      per-kernel defaults;
+    - ``threads128``: the evaluation kernels in blocks of 128 threads (8 per SM, 64
+      registers): a block waits at its tile's barriers, and smaller blocks let more of them
+      be in different phases.
   A candidate of this family whose labels differ from the default's is rejected, since that
   would mean a broken guarantee rather than a faster schedule.
 * approximate schedules (opt-in) reach a different deterministic clustering:
@@ -40,8 +43,9 @@ set-up time that a one-off solve pays).
 
 The schedules' switches are the engine's own (the ``persistent`` option of ``acvd_opts`` and the
 ``ACVD_HOST_LOOP`` / ``ACVD_RELAXED`` / ``ACVD_MATCH_ROUNDS`` / ``ACVD_EVAL_BLOCKS`` /
-``ACVD_COLORING`` / ``ACVD_SPLIT_MIN`` environment switches). The engine reads ``ACVD_RELAXED``,
-``ACVD_MATCH_ROUNDS`` and ``ACVD_EVAL_BLOCKS`` when a context is created, ``ACVD_COLORING`` and ``ACVD_SPLIT_MIN`` when it
+``ACVD_EVAL_THREADS`` / ``ACVD_COLORING`` / ``ACVD_SPLIT_MIN`` environment switches). The engine
+reads ``ACVD_RELAXED``, ``ACVD_MATCH_ROUNDS``, ``ACVD_EVAL_BLOCKS`` and ``ACVD_EVAL_THREADS``
+when a context is created, ``ACVD_COLORING`` and ``ACVD_SPLIT_MIN`` when it
 takes a mesh and ``ACVD_HOST_LOOP`` when it minimises, so ``ScheduledEngine`` sets them only
 around those calls and puts the environment back afterwards.
 """
@@ -73,13 +77,15 @@ class Schedule:
     coloring: str = "jp"           # jp (device Jones-Plassmann) | order | squeeze
     split_min: int | None = None   # None: the engine's threshold; 0: never split
     eval_blocks: int | None = None  # evaluation kernels' blocks per SM (3, 4, 5); None: the defaults
+    eval_threads: int | None = None  # evaluation kernels' threads per block (128); None: 256
     exact: bool = True   # same clustering as the default schedule, bit for bit
 
     def create_env(self) -> dict:
         """Switches the engine reads in acvd_create (None = unset)."""
         return {"ACVD_RELAXED": None if self.relaxed else "0",
                 "ACVD_MATCH_ROUNDS": None if self.match_rounds == 1 else str(int(self.match_rounds)),
-                "ACVD_EVAL_BLOCKS": None if self.eval_blocks is None else str(int(self.eval_blocks))}
+                "ACVD_EVAL_BLOCKS": None if self.eval_blocks is None else str(int(self.eval_blocks)),
+                "ACVD_EVAL_THREADS": None if self.eval_threads is None else str(int(self.eval_threads))}
 
     def mesh_env(self) -> dict:
         """Switches the engine reads in acvd_set_mesh."""
@@ -94,7 +100,8 @@ class Schedule:
 DEFAULT = Schedule("graphs")
 EXACT_SCHEDULES = (DEFAULT, Schedule("host_loop", host_loop=True), Schedule("persistent", persistent=True),
                    Schedule("fused", split_min=0), Schedule("blocks3", eval_blocks=3),
-                   Schedule("blocks4", eval_blocks=4), Schedule("blocks5", eval_blocks=5))
+                   Schedule("blocks4", eval_blocks=4), Schedule("blocks5", eval_blocks=5),
+                   Schedule("threads128", eval_threads=128))
 APPROX_SCHEDULES = (Schedule("exact_sweeps", relaxed=False, exact=False),
                     Schedule("match2", match_rounds=2, exact=False),
                     Schedule("order_colors", coloring="order", exact=False),

@@ -290,17 +290,25 @@ ACVD_DEV bool ring_connected_pref(const DevState& st, int p0, int p1, int L, con
 // List mode (entries != nullptr): the tile's items are entries[0 .. n_entries), the
 // colour-list positions a screen_kernel pass forwarded (see below); they were
 // counted as visited there.
-template <int M>
+// A new evaluation sweep for an item whose screen record c is valid (bflag 2): into
+// the record, or, beyond the sweeps a record holds, the item is screened in full next.
+ACVD_DEV void set_cached_ev(const DevState& st, int i, int4 c, int ev) {
+    if (ev < kCacheSweeps) st.tcache[i] = screen_with_ev(c, ev);
+    else st.bflag[i] = 1;
+}
+
+template <int M, int TB = 256>
 ACVD_DEV void eval_tile(const DevState& st, int item0, int64_t count, int color,
                         int* cand_dest, unsigned* cand_prio, int claims, int64_t tile,
                         const int* entries = nullptr, int n_entries = 0) {
-    __shared__ int s_idx[256];                 // work item -> colour-list position
-    __shared__ int s_tgt[256][kMaxTgt];        // work item -> destination clusters (ring order)
-    __shared__ float s_val[256][kMaxTgt + 1];  // energy parts: [j] add to s_tgt[j], [kMaxTgt] remove
-    __shared__ signed char s_nt[256];          // destinations; -1: the whole test runs in B2
-    __shared__ unsigned short s_task[256 * kMaxTgt];   // add tasks: (work item << 4) | destination
-    __shared__ unsigned char s_rem[256];                // work items whose remove part B1 computes
-    __shared__ int s_scr[256];                 // flagged items of the tile (colour-list positions)
+    __shared__ int s_idx[TB];                 // work item -> colour-list position
+    __shared__ int s_tgt[TB][kMaxTgt];        // work item -> destination clusters (ring order)
+    __shared__ float s_val[TB][kMaxTgt + 1];  // energy parts: [j] add to s_tgt[j], [kMaxTgt] remove
+    __shared__ signed char s_nt[TB];          // destinations; -1: the whole test runs in B2
+    __shared__ unsigned short s_task[TB * kMaxTgt];   // add tasks: (work item << 4) | destination
+    __shared__ unsigned char s_rem[TB];                // work items whose remove part B1 computes
+    __shared__ int s_scr[TB];                 // flagged items of the tile (colour-list positions)
+    __shared__ unsigned char s_rec[TB];       // work item -> its screen record is valid (bflag 2)
     __shared__ unsigned s_nwork, s_ntask, s_nrem, s_nscr, s_nfull;
     __syncthreads();                     // the previous tile is done with the shared arrays
     if (threadIdx.x == 0) {
@@ -313,8 +321,8 @@ ACVD_DEV void eval_tile(const DevState& st, int item0, int64_t count, int color,
     __syncthreads();
     const int epoch = color * kRounds;   // claim epoch of this step's first matching round
     const bool listed = entries != nullptr;
-    const bool in = listed ? (int)threadIdx.x < n_entries : tile * 256 + threadIdx.x < count;
-    const int64_t idx_t = listed ? (in ? (int64_t)entries[threadIdx.x] : 0) : tile * 256 + threadIdx.x;
+    const bool in = listed ? (int)threadIdx.x < n_entries : tile * TB + threadIdx.x < count;
+    const int64_t idx_t = listed ? (in ? (int64_t)entries[threadIdx.x] : 0) : tile * TB + threadIdx.x;
     const SweepState sw = *st.sweep;
     const RunFlags fl = *st.flags;
     unsigned n_slots = 0, n_bnd = 0, n_tgt = 0, n_cand = 0, n_scr = 0, n_cached = 0;
@@ -337,29 +345,33 @@ ACVD_DEV void eval_tile(const DevState& st, int item0, int64_t count, int color,
             unsigned base = 0;
             if (lane == 0) base = atomicAdd(&s_nfull, (unsigned)__popc(bal_f));
             base = __shfl_sync(kFull, base, 0);
-            if (bf == 1) s_scr[255 - (base + __popc(bal_f & below))] = (int)idx_t;
+            if (bf == 1) s_scr[TB - 1 - (base + __popc(bal_f & below))] = (int)idx_t;
         }
     }
     __syncthreads();
-    if (threadIdx.x < s_nscr || threadIdx.x >= 256u - s_nfull) {
+    if (threadIdx.x < s_nscr || threadIdx.x >= (unsigned)TB - s_nfull) {
         const int code = s_scr[threadIdx.x];
         const int64_t idx = code & ~kScrCached;
         const int i = item0 + (int)idx;
         n_scr = 1;
-        const int L = st.label[i];
-        const int ev_i = st.evald[i];
+        // a cached screen's record holds the item's cluster and evaluation sweep too
+        const bool cached = (code & kScrCached) != 0;
+        const int4 c = cached ? st.tcache[i] : make_int4(0, 0, 0, 0);
+        const Screen sc = unpack_screen(c);
+        const int L = cached ? sc.L : st.label[i];
+        int ev_i = cached ? sc.ev : st.evald[i];
+        if (cached) ACVD_VALID(st, L == st.label[i] && ev_i == st.evald[i]);
         bool screened = !ACVD_VALID(st, L >= 0 && L <= st.k);   // a bad label is skipped
-        if (code & kScrCached) {
+        if (cached && !screened) {
             // the ring kept its labels since the last full screen: its distinct
             // neighbour clusters and the connectivity test are in the cache
-            const int4 c = st.tcache[i];
-            const int n = c.w & 3;
-            const bool conn_known = (c.w & 4) != 0, conn_ok = (c.w & 8) != 0;
+            const int n = sc.n;
+            const bool conn_known = sc.conn_known, conn_ok = sc.conn_ok;
             const bool may_move = st.size[L] > 1 && !(st.frozen && st.frozen[L]);
             if (!(fl.connexity && may_move && !conn_known)) {
                 screened = true;
                 n_cached = 1;
-                const int tg[3] = {c.x, c.y, c.z};
+                const int tg[3] = {sc.t[0], sc.t[1], sc.t[2]};
                 bool fresh = ev_i <= sw.floor || st.stamp[L] >= ev_i;
 #pragma unroll
                 for (int q = 0; q < 3; q++)
@@ -369,6 +381,7 @@ ACVD_DEV void eval_tile(const DevState& st, int item0, int64_t count, int color,
                     if (may_move && (!fl.connexity || conn_ok)) {
                         const int w = (int)atomicAdd(&s_nwork, 1u);
                         s_idx[w] = (int)idx;
+                        s_rec[w] = 1;
                         int nt = 0;
 #pragma unroll
                         for (int q = 0; q < 3; q++)
@@ -382,6 +395,7 @@ ACVD_DEV void eval_tile(const DevState& st, int item0, int64_t count, int color,
                         }
                     } else {
                         st.evald[i] = sw.sweep;   // evaluated: nothing it may do
+                        set_cached_ev(st, i, c, sw.sweep);
                     }
                 }
             }
@@ -425,8 +439,11 @@ ACVD_DEV void eval_tile(const DevState& st, int item0, int64_t count, int color,
         const bool may_move = L < st.k && st.size[L] > 1 && !(st.frozen && st.frozen[L]);
         int conn = -1;   // the local connectivity test, evaluated at most once
         // cache a boundary screen of a ring of at most 8 with at most 3 neighbour
-        // clusters: they hold until a commit touches the ring (mark_ring)
-        if (boundary && !longer && L < st.k) {
+        // clusters: they hold until a commit touches the ring (mark_ring).  The record
+        // is written below, with the evaluation sweep this screen leaves.
+        bool cache_it = false;
+        int4 rec = make_int4(0, 0, 0, 0);
+        if (boundary && !longer && L < st.k && st.k <= kCacheClusters) {
             int tg[3] = {0, 0, 0};
             int n = 0;
 #pragma unroll
@@ -446,8 +463,8 @@ ACVD_DEV void eval_tile(const DevState& st, int item0, int64_t count, int color,
                     conn = ring_connected_pref(st, st.row[i], st.row[i] + deg, L, lb) ? 1 : 0;
                     meta |= 4 | (conn ? 8 : 0);
                 }
-                st.tcache[i] = make_int4(tg[0], tg[1], tg[2], meta);
-                st.bflag[i] = 2;
+                rec = pack_screen(L, tg[0], tg[1], tg[2], meta, 0);
+                cache_it = true;
             }
         }
         if (boundary && fresh) {
@@ -458,6 +475,7 @@ ACVD_DEV void eval_tile(const DevState& st, int item0, int64_t count, int color,
             if (movable) {
                 const int w = (int)atomicAdd(&s_nwork, 1u);
                 s_idx[w] = (int)idx;
+                s_rec[w] = cache_it ? 1 : 0;
                 int nt = 0;
                 bool all = L < st.k && deg <= kRingPref;
 #pragma unroll
@@ -487,6 +505,15 @@ ACVD_DEV void eval_tile(const DevState& st, int item0, int64_t count, int color,
                 }
             } else {
                 st.evald[i] = sw.sweep;   // evaluated: nothing it may do
+                ev_i = sw.sweep;
+            }
+        }
+        if (cache_it) {
+            if (ev_i < kCacheSweeps) {
+                st.tcache[i] = screen_with_ev(rec, ev_i);
+                st.bflag[i] = 2;
+            } else {
+                st.bflag[i] = 1;   // beyond the sweeps a record holds: screened in full
             }
         }
         }
@@ -495,7 +522,7 @@ ACVD_DEV void eval_tile(const DevState& st, int item0, int64_t count, int color,
     // B1: energy parts -- the remove parts first, then the add parts, so that a warp
     // runs one kind
     const unsigned nrem = s_nrem, ntask = nrem + s_ntask;
-    for (unsigned t = threadIdx.x; t < ntask; t += 256) {
+    for (unsigned t = threadIdx.x; t < ntask; t += TB) {
         const unsigned code = t < nrem ? ((unsigned)s_rem[t] << 4) | (unsigned)kTaskRemove : s_task[t - nrem];
         const int w = (int)(code >> 4), j = (int)(code & 15u);
         const int i = item0 + s_idx[w];
@@ -591,8 +618,10 @@ ACVD_DEV void eval_tile(const DevState& st, int item0, int64_t count, int color,
             n_cand = 1;
             my_cand = widx;
             st.evald[i] = -1;
+            if (s_rec[w]) set_cached_ev(st, i, st.tcache[i], -1);
         } else {
             st.evald[i] = sw.sweep;
+            if (s_rec[w]) set_cached_ev(st, i, st.tcache[i], sw.sweep);
         }
     }
     // block-aggregated append to the compact proposal list and block totals of the
@@ -600,7 +629,8 @@ ACVD_DEV void eval_tile(const DevState& st, int item0, int64_t count, int color,
     // otherwise serialise on the class's count and the counter stripes)
     {
         constexpr int kNC = 7;
-        __shared__ unsigned s_wc[8], s_base, s_cnt[8][kNC];
+        constexpr int kW = TB / 32;
+        __shared__ unsigned s_wc[kW], s_base, s_cnt[kW][kNC];
         const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
         const unsigned bal = __ballot_sync(kFull, my_cand >= 0);
         const unsigned v[kNC] = {(in && !listed) ? 1u : 0u, n_scr - n_cached, n_cached, n_slots, n_bnd, n_tgt,
@@ -614,7 +644,7 @@ ACVD_DEV void eval_tile(const DevState& st, int item0, int64_t count, int color,
         __syncthreads();
         if (threadIdx.x == 0) {
             unsigned tot = 0;
-            for (int w = 0; w < 8; w++) {
+            for (int w = 0; w < kW; w++) {
                 const unsigned c = s_wc[w];
                 s_wc[w] = tot;
                 tot += c;
@@ -625,7 +655,7 @@ ACVD_DEV void eval_tile(const DevState& st, int item0, int64_t count, int color,
             const int which = c == 0 ? kCntVisited : c == 1 ? kCntScreened : c == 2 ? kCntCached
                             : c == 3 ? kCntSlots : c == 4 ? kCntBoundary : c == 5 ? kCntTargets : kCntCand;
             unsigned t = 0;
-            for (int w = 0; w < 8; w++) t += s_cnt[w][c];
+            for (int w = 0; w < kW; w++) t += s_cnt[w][c];
             if (t) atomicAdd(ctr(st.counters, which), (unsigned long long)t);
         }
         __syncthreads();
@@ -639,10 +669,13 @@ ACVD_DEV void eval_tile(const DevState& st, int item0, int64_t count, int color,
 // metric and the workload.  launch_eval takes the count at run time (the context's
 // eval_blocks, ACVD_EVAL_BLOCKS; the autotuner times the choices); 0 selects the
 // defaults below, measured on GB300.
-template <int M, int B>
-__global__ void __launch_bounds__(256, B) eval_kernel(DevState st, int item0, int64_t count, int color,
-                                                      int* cand_dest, unsigned* cand_prio, int claims) {
-    eval_tile<M>(st, item0, count, color, cand_dest, cand_prio, claims, blockIdx.x);
+// TB: threads (and items) per block.  A block is the unit that waits at the tile's
+// barriers, so smaller blocks at the same threads per SM (B * 256 / TB blocks of TB)
+// let more of them be in different phases of their tiles.
+template <int M, int B, int TB = 256>
+__global__ void __launch_bounds__(TB, B * 256 / TB) eval_kernel(DevState st, int item0, int64_t count, int color,
+                                                                int* cand_dest, unsigned* cand_prio, int claims) {
+    eval_tile<M, TB>(st, item0, count, color, cand_dest, cand_prio, claims, blockIdx.x);
 }
 
 // default blocks per SM: the fused evaluation 4 (isotropic, QEM) and 5 (the
@@ -712,43 +745,41 @@ __global__ void __launch_bounds__(256, 4) screen_kernel(DevState st, int item0, 
         // issued before any is used
         const int nc = (int)s_nc;
         for (int j0 = 0; j0 < nc; j0 += 256 * kScreenBatch) {
-            int pos[kScreenBatch], L[kScreenBatch], ev_i[kScreenBatch];
+            // one 16-byte record per cached screen: cluster, targets, evaluation sweep
+            int pos[kScreenBatch];
             int4 c[kScreenBatch];
 #pragma unroll
             for (int u = 0; u < kScreenBatch; u++) {
                 const int j = j0 + u * 256 + (int)threadIdx.x;
                 pos[u] = j < nc ? s_cached[j] : -1;
-                if (pos[u] >= 0) {
-                    const int i = item0 + (int)(t0 + pos[u]);
-                    L[u] = st.label[i];
-                    ev_i[u] = st.evald[i];
-                    c[u] = st.tcache[i];
-                } else {
-                    L[u] = 0;
-                    ev_i[u] = 0;
-                    c[u] = make_int4(0, 0, 0, 0);
-                }
+                c[u] = pos[u] >= 0 ? st.tcache[item0 + (int)(t0 + pos[u])] : make_int4(0, 0, 0, 0);
             }
 #pragma unroll
             for (int u = 0; u < kScreenBatch; u++) {
-                if (pos[u] < 0 || !ACVD_VALID(st, L[u] >= 0 && L[u] <= st.k)) continue;
-                const int n = c[u].w & 3;
-                const bool conn_known = (c[u].w & 4) != 0, conn_ok = (c[u].w & 8) != 0;
-                const bool may_move = st.size[L[u]] > 1 && !(st.frozen && st.frozen[L[u]]);
-                bool fwd = fl.connexity && may_move && !conn_known;   // connectivity not cached: full screen
+                const Screen sc = unpack_screen(c[u]);
+                const int L = sc.L, ev_i = sc.ev;
+                if (pos[u] >= 0) {
+                    const int i = item0 + (int)(t0 + pos[u]);
+                    ACVD_VALID(st, L == st.label[i] && ev_i == st.evald[i]);
+                }
+                if (pos[u] < 0 || !ACVD_VALID(st, L >= 0 && L <= st.k)) continue;
+                const int n = sc.n;
+                const bool may_move = st.size[L] > 1 && !(st.frozen && st.frozen[L]);
+                bool fwd = fl.connexity && may_move && !sc.conn_known;   // connectivity not cached: full screen
                 if (!fwd) {
-                    const int tg[3] = {c[u].x, c[u].y, c[u].z};
-                    bool fresh = ev_i[u] <= sw.floor || st.stamp[L[u]] >= ev_i[u];
+                    bool fresh = ev_i <= sw.floor || st.stamp[L] >= ev_i;
 #pragma unroll
                     for (int q = 0; q < 3; q++)
-                        if (q < n && st.stamp[tg[q]] >= ev_i[u]) fresh = true;
-                    if (fresh && may_move && (!fl.connexity || conn_ok)) {
+                        if (q < n && st.stamp[sc.t[q]] >= ev_i) fresh = true;
+                    if (fresh && may_move && (!fl.connexity || sc.conn_ok)) {
                         fwd = true;   // an energy test to run
                     } else {
                         n_cached++;
                         if (fresh) {
                             n_bnd++;
-                            st.evald[item0 + (int)(t0 + pos[u])] = sw.sweep;   // nothing it may do
+                            const int i = item0 + (int)(t0 + pos[u]);
+                            st.evald[i] = sw.sweep;   // nothing it may do
+                            set_cached_ev(st, i, c[u], sw.sweep);
                         }
                     }
                 }
@@ -780,26 +811,27 @@ __global__ void __launch_bounds__(256, 4) screen_kernel(DevState st, int item0, 
     }
 }
 
-// The work list of a screen_kernel pass through eval_tile, 256 entries per tile,
+// The work list of a screen_kernel pass through eval_tile, TB entries per tile,
 // grid-stride over (stripe, tile) pairs.
-template <int M, int B>
-__global__ void __launch_bounds__(256, B) eval_list_kernel(DevState st, int item0, int64_t count, int color,
-                                                           int* cand_dest, unsigned* cand_prio, int claims,
-                                                           const int* work, const unsigned* work_count) {
+template <int M, int B, int TB = 256>
+__global__ void __launch_bounds__(TB, B * 256 / TB) eval_list_kernel(DevState st, int item0, int64_t count,
+                                                                     int color, int* cand_dest, unsigned* cand_prio,
+                                                                     int claims, const int* work,
+                                                                     const unsigned* work_count) {
     __shared__ unsigned s_cnt[kWorkStripes];
     if (threadIdx.x < kWorkStripes) s_cnt[threadIdx.x] = work_count[color * kWorkStripes + threadIdx.x];
     __syncthreads();
     unsigned mx = 0;
     for (int q = 0; q < kWorkStripes; q++) mx = max(mx, s_cnt[q]);
-    const int64_t per = (mx + 255) / 256;   // tiles of the fullest stripe
+    const int64_t per = (mx + TB - 1) / TB;   // tiles of the fullest stripe
     const int64_t cap = work_cap(count);
     for (int64_t t = blockIdx.x; t < per * kWorkStripes; t += gridDim.x) {
         const int q = (int)(t % kWorkStripes);
         const int64_t j = t / kWorkStripes;
-        const int64_t have = (int64_t)s_cnt[q] - j * 256;
+        const int64_t have = (int64_t)s_cnt[q] - j * TB;
         if (have <= 0) continue;   // block-uniform
-        eval_tile<M>(st, item0, count, color, cand_dest, cand_prio, claims, t, work + q * cap + j * 256,
-                     have < 256 ? (int)have : 256);
+        eval_tile<M, TB>(st, item0, count, color, cand_dest, cand_prio, claims, t, work + q * cap + j * TB,
+                         have < TB ? (int)have : TB);
     }
 }
 
@@ -1618,6 +1650,63 @@ __global__ void comp_step_kernel(DevState st, int* __restrict__ comp) {
     }
 }
 
+// The same components by union-find in one pass over the ring CSR (the result equals
+// the propagation's: every component ends as the smallest original id of its items).
+// parent[] links items; a root is linked only under a root of smaller original id, so
+// ids decrease along every chain and each set's root is its smallest-id item.  Concurrent
+// links race through atomicCAS on the root's slot; a failed CAS retries from the new
+// roots.  Finding a root halves the path (writes of an ancestor, benign under races).
+constexpr int kUnionTries = 1 << 16;   // retries of one link before the pass gives up
+
+__device__ __forceinline__ int uf_root(int* parent, int x) {
+    for (;;) {
+        const int p = parent[x];
+        if (p == x) return x;
+        const int g = parent[p];
+        if (g != p) parent[x] = g;
+        x = p;
+    }
+}
+
+__global__ void uf_init_kernel(DevState st, int* __restrict__ parent) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < st.n) parent[i] = (int)i;
+}
+
+__global__ void uf_link_kernel(DevState st, int* parent) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= st.n) return;
+    const int L = st.label[i];
+    if (L >= st.k) return;
+    unsigned gave_up = 0;
+    for (int p = st.row[i]; p < st.row[i + 1]; p++) {
+        const int j = st.col[p];
+        if (j <= (int)i || st.label[j] != L) continue;   // each same-cluster edge once
+        int a = uf_root(parent, (int)i), b = uf_root(parent, j);
+        int t = 0;
+        for (; t < kUnionTries && a != b; t++) {
+            if (st.orig[a] > st.orig[b]) {
+                const int x = a;
+                a = b;
+                b = x;
+            }
+            // b (larger original id) goes under a
+            const int old = atomicCAS(&parent[b], b, a);
+            if (old == b) break;
+            a = uf_root(parent, a);
+            b = uf_root(parent, old);
+        }
+        gave_up += t == kUnionTries;
+    }
+    if (gave_up) atomicAdd(ctr(st.counters, kCntChanged), (unsigned long long)gave_up);
+}
+
+__global__ void uf_flatten_kernel(DevState st, int* parent, int* __restrict__ comp) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= st.n) return;
+    comp[i] = st.label[i] < st.k ? st.orig[uf_root(parent, (int)i)] : -1;
+}
+
 __global__ void comp_size_kernel(DevState st, const int* __restrict__ comp, int* __restrict__ csize) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= st.n) return;
@@ -1874,6 +1963,30 @@ static int64_t sm_count();
         }                                                                                                   \
     } while (0)
 
+// metric -> the 128-thread instantiation with B = 4 (the threads per SM of four
+// 256-thread blocks)
+#define ACVD_DISPATCH_128(metric, KERNEL, grid, stream, ...)                                                    \
+    do {                                                                                                        \
+        ++g_launches;                                                                                           \
+        if ((metric) == kIso) KERNEL<kIso, 4, 128><<<grid, 128, 0, stream>>>(__VA_ARGS__);                      \
+        else if ((metric) == kQEM) KERNEL<kQEM, 4, 128><<<grid, 128, 0, stream>>>(__VA_ARGS__);                 \
+        else KERNEL<kAniso, 4, 128><<<grid, 128, 0, stream>>>(__VA_ARGS__);                                     \
+    } while (0)
+
+// Resident blocks per SM of the 128-thread eval_list_kernel instantiation
+template <int M>
+static int list_occupancy_128() {
+    int nb = 0;
+    const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, eval_list_kernel<M, 4, 128>, 128, 0);
+    return (e == cudaSuccess && nb > 0) ? nb : 1;
+}
+
+static int eval_list_blocks_per_sm_128(int metric) {
+    if (metric == kIso) return list_occupancy_128<kIso>();
+    if (metric == kQEM) return list_occupancy_128<kQEM>();
+    return list_occupancy_128<kAniso>();
+}
+
 // Resident blocks per SM of an eval_list_kernel instantiation (its grid strides over
 // the work list).
 template <int M, int B>
@@ -1903,8 +2016,25 @@ static int screen_blocks_per_sm(int metric) {
 }
 
 cudaError_t launch_eval(int metric, const DevState& st, int item0, int64_t count, int color,
-                        int* cand_dest, unsigned* cand_prio, bool claims, bool split, int blocks, cudaStream_t s) {
+                        int* cand_dest, unsigned* cand_prio, bool claims, bool split, int blocks, int threads,
+                        cudaStream_t s) {
     if (count == 0) return cudaSuccess;
+    if (threads == 128) {
+        // 128-thread blocks, as many threads per SM as four blocks of 256
+        if (!split) {
+            ACVD_DISPATCH_128(metric, eval_kernel, nblk(count, 128), s, st, item0, count, color, cand_dest,
+                              cand_prio, claims ? 1 : 0);
+            return cudaGetLastError();
+        }
+        const unsigned sgrid =
+            (unsigned)std::min<int64_t>(nblk(count, kScreenTile), sm_count() * screen_blocks_per_sm(metric));
+        ACVD_DISPATCH(metric, screen_kernel, sgrid, 256, s, st, item0, count, color, st.work, st.work_count);
+        const int64_t tiles = kWorkStripes * (work_cap(count) / 128);
+        const unsigned grid = (unsigned)std::min<int64_t>(tiles, sm_count() * eval_list_blocks_per_sm_128(metric));
+        ACVD_DISPATCH_128(metric, eval_list_kernel, grid, s, st, item0, count, color, cand_dest, cand_prio,
+                          claims ? 1 : 0, (const int*)st.work, (const unsigned*)st.work_count);
+        return cudaGetLastError();
+    }
     if (!split) {
         ACVD_DISPATCH_B(metric, blocks, default_eval_blocks(metric), eval_kernel, nblk(count), 256, s, st, item0,
                         count, color, cand_dest, cand_prio, claims ? 1 : 0);
@@ -2019,6 +2149,14 @@ cudaError_t launch_comp_init(const DevState& st, int* comp, cudaStream_t s) {
 cudaError_t launch_comp_step(const DevState& st, int* comp, cudaStream_t s) {
     ++g_launches;
     comp_step_kernel<<<nblk(st.n), 256, 0, s>>>(st, comp);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_comp_union(const DevState& st, int* comp, int* parent, cudaStream_t s) {
+    g_launches += 3;
+    uf_init_kernel<<<nblk(st.n), 256, 0, s>>>(st, parent);
+    uf_link_kernel<<<nblk(st.n), 256, 0, s>>>(st, parent);
+    uf_flatten_kernel<<<nblk(st.n), 256, 0, s>>>(st, parent, comp);
     return cudaGetLastError();
 }
 

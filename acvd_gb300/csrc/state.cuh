@@ -95,6 +95,53 @@ __device__ __forceinline__ unsigned long long* ctr(unsigned long long* counters,
 #define ACVD_VALID(st, cond) true
 #endif
 
+// Packed cached screen (16 bytes).  Cluster ids below 2^24 (kCacheClusters; a
+// clustering with more clusters never caches), e = evaluation sweep + 1 below 2^28
+// (0 for "never evaluated without a proposal"):
+//   x = L  | meta << 24 | (e >> 24) << 28      meta = count | 4 if the connectivity
+//   y = t0 | (e & 0xff) << 24                        test is known | 8 if it passed
+//   z = t1 | ((e >> 8) & 0xff) << 24
+//   w = t2 | ((e >> 16) & 0xff) << 24
+// Unused targets are 0.  The evaluation sweep is kept here as well as in evald, and
+// every write of evald for an item whose screen is cached writes both.
+constexpr int kCacheClusters = 1 << 24;
+constexpr int kCacheSweeps = (1 << 28) - 2;   // evaluation sweeps a record can hold
+struct Screen {
+    int L, t[3], n, ev;
+    bool conn_known, conn_ok;
+};
+__host__ __device__ inline int4 pack_screen(int L, int t0, int t1, int t2, int meta, int ev) {
+    const unsigned e = (unsigned)(ev + 1);
+    return make_int4((int)((unsigned)L | ((unsigned)meta << 24) | ((e >> 24) << 28)),
+                     (int)((unsigned)t0 | ((e & 0xffu) << 24)), (int)((unsigned)t1 | (((e >> 8) & 0xffu) << 24)),
+                     (int)((unsigned)t2 | (((e >> 16) & 0xffu) << 24)));
+}
+__host__ __device__ inline Screen unpack_screen(int4 c) {
+    const unsigned m = (1u << 24) - 1u;
+    const unsigned x = (unsigned)c.x, y = (unsigned)c.y, z = (unsigned)c.z, w = (unsigned)c.w;
+    Screen r;
+    r.L = (int)(x & m);
+    r.t[0] = (int)(y & m);
+    r.t[1] = (int)(z & m);
+    r.t[2] = (int)(w & m);
+    const unsigned meta = (x >> 24) & 15u;
+    r.n = (int)(meta & 3u);
+    r.conn_known = (meta & 4u) != 0;
+    r.conn_ok = (meta & 8u) != 0;
+    const unsigned e = (y >> 24) | ((z >> 24) << 8) | ((w >> 24) << 16) | ((x >> 28) << 24);
+    r.ev = (int)e - 1;
+    return r;
+}
+// the record with its evaluation sweep replaced
+__host__ __device__ inline int4 screen_with_ev(int4 c, int ev) {
+    const unsigned m = (1u << 24) - 1u;
+    const unsigned e = (unsigned)(ev + 1);
+    return make_int4((int)(((unsigned)c.x & ((1u << 28) - 1u)) | ((e >> 24) << 28)),
+                     (int)(((unsigned)c.y & m) | ((e & 0xffu) << 24)),
+                     (int)(((unsigned)c.z & m) | (((e >> 8) & 0xffu) << 24)),
+                     (int)(((unsigned)c.w & m) | (((e >> 16) & 0xffu) << 24)));
+}
+
 // Sweep bookkeeping on the device (one captured graph serves every sweep):
 // `sweep` counts sweeps, `floor` is the sweep after which every cluster counts as
 // modified (the reference's SetAllClustersToModified, vtkUniformClustering.h:717-722).
@@ -152,9 +199,10 @@ struct DevState {
     // edges in its queue and re-queues a moved item's ring
     // (vtkUniformClustering.h:858-872, 971, 985).
     unsigned char* bflag;
-    // per item with bflag 2: its distinct neighbour clusters (x, y, z; ring order) and
-    // w = count | 4 if the connectivity test is known | 8 if it passed.  Valid while
-    // no label in the ring changes.
+    // per item with bflag 2: its packed cached screen (pack_screen: its cluster, its
+    // distinct neighbour clusters in ring order, the connectivity bits and a copy of
+    // its evaluation sweep), 16 bytes so that a cached screen reads one record.
+    // Valid while no label in the ring changes.
     int4* tcache;
     // per item, the first 8 ring neighbours (two int4, ring order, -1 padded; slot
     // 7 = -2 when the ring is longer than 8, which then is read from row / col)
@@ -290,8 +338,11 @@ cudaError_t launch_loop_decide(LoopState* ls, const unsigned long long* counters
 cudaError_t launch_relaxed_step(int metric, const DevState& st, int item0, int64_t count, int color,
                                 const int* cand_dest, cudaStream_t s);
 cudaError_t launch_fx_scale(int metric, const DevState& st, unsigned* maxbits, cudaStream_t s);
+// blocks: 256-thread blocks per SM (3..5, else the defaults); threads: 128 for
+// 128-thread blocks at the threads per SM of four 256-thread blocks (else 256)
 cudaError_t launch_eval(int metric, const DevState& st, int item0, int64_t count, int color,
-                        int* cand_dest, unsigned* cand_prio, bool claims, bool split, int blocks, cudaStream_t s);
+                        int* cand_dest, unsigned* cand_prio, bool claims, bool split, int blocks, int threads,
+                        cudaStream_t s);
 cudaError_t launch_apply(int metric, const DevState& st, int item0, int64_t count, int color, int round,
                          int* cand_dest, const unsigned* cand_prio, cudaStream_t s);
 cudaError_t launch_reclaim(const DevState& st, int item0, int64_t count, int color, int round,
@@ -307,6 +358,9 @@ cudaError_t launch_reduce_clusters(int metric, const DevState& st, const uint32_
                                    const uint32_t* seg_off, const uint32_t* seg_cnt, cudaStream_t s);
 cudaError_t launch_comp_init(const DevState& st, int* comp, cudaStream_t s);
 cudaError_t launch_comp_step(const DevState& st, int* comp, cudaStream_t s);
+// the components in one union-find pass; kCntChanged counts links it gave up on
+// (then the propagation above runs instead)
+cudaError_t launch_comp_union(const DevState& st, int* comp, int* parent, cudaStream_t s);
 cudaError_t launch_comp_finish(const DevState& st, const int* comp, int* csize, unsigned long long* best,
                                int* multi, cudaStream_t s);
 cudaError_t launch_fill_color(const DevState& st, const int* items, int64_t count, cudaStream_t s);

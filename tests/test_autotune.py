@@ -28,7 +28,7 @@ def test_fastest_exact_schedule_chosen_and_cached(tmp_path):
     measure, calls = _fake({"graphs": [3.0, 2.9, 3.1], "host_loop": [4.0, 4.1, 3.9], "persistent": [2.0, 2.2, 2.1]})
     s, rep = at.Autotuner(path).tune("gb300|qem|n2^19_k2^14", measure)
     assert s == at.BY_NAME["persistent"] and not rep["cached"]
-    assert calls == ["graphs", "host_loop", "persistent", "fused", "blocks3", "blocks4", "blocks5"]
+    assert calls == ["graphs", "host_loop", "persistent", "fused", "blocks3", "blocks4", "blocks5", "threads128"]
     assert rep["ms"] == pytest.approx(2.1)
     with open(path) as f:
         assert json.load(f)["gb300|qem|n2^19_k2^14"]["schedule"] == "persistent"
@@ -39,7 +39,7 @@ def test_fastest_exact_schedule_chosen_and_cached(tmp_path):
     # retune measures again
     measure3, calls3 = _fake({"graphs": [1.0], "host_loop": [4.0], "persistent": [2.0]})
     s3, _ = at.Autotuner(path).tune("gb300|qem|n2^19_k2^14", measure3, retune=True)
-    assert s3 == at.DEFAULT and len(calls3) == 7
+    assert s3 == at.DEFAULT and len(calls3) == 8
 
 
 def test_exact_schedule_with_another_clustering_is_rejected():
@@ -76,7 +76,7 @@ def test_cached_approximate_choice_not_returned_to_a_default_tuner(tmp_path):
     measure2, calls2 = _fake(times)
     s2, rep2 = at.Autotuner(path).tune("k", measure2)
     assert s2.exact and not rep2["cached"] and calls2 == ["graphs", "host_loop", "persistent", "fused", "blocks3",
-                                                           "blocks4", "blocks5"]
+                                                           "blocks4", "blocks5", "threads128"]
     # an opt-in tuner with a tighter tolerance than the cached choice's measures again
     at.Autotuner(path, include_approximate=True).tune("k2", _fake(times, digests={"match2": "y"})[0])
     tight = at.Autotuner(path, include_approximate=True, energy_rel_tol=1e-4)
@@ -123,7 +123,8 @@ def test_schedule_switches_are_the_engines():
     assert at.DEFAULT.run_env() == {"ACVD_HOST_LOOP": None}
     assert at.BY_NAME["exact_sweeps"].create_env()["ACVD_RELAXED"] == "0"
     assert at.BY_NAME["match2"].create_env()["ACVD_MATCH_ROUNDS"] == "2"
-    assert at.DEFAULT.create_env() == {"ACVD_RELAXED": None, "ACVD_MATCH_ROUNDS": None, "ACVD_EVAL_BLOCKS": None}
+    assert at.DEFAULT.create_env() == {"ACVD_RELAXED": None, "ACVD_MATCH_ROUNDS": None, "ACVD_EVAL_BLOCKS": None,
+                                       "ACVD_EVAL_THREADS": None}
     assert at.BY_NAME["persistent"].persistent and all(s.exact for s in at.EXACT_SCHEDULES)
     assert not any(s.exact for s in at.APPROX_SCHEDULES)
 

@@ -21,7 +21,8 @@ def test_tuned_schedule_keeps_the_clustering(tmp_path):
     s, rep = at.tune_problem(m.points, m.faces, "qem", k, lab0, tuner=tuner, **kw)
     assert not rep["cached"]
     trials = {t["schedule"]: t for t in rep["trials"]}
-    assert set(trials) == {"graphs", "host_loop", "persistent", "fused", "blocks3", "blocks4", "blocks5"}
+    assert set(trials) == {"graphs", "host_loop", "persistent", "fused", "blocks3", "blocks4", "blocks5",
+                           "threads128"}
     assert trials["graphs"]["accepted"] and trials["graphs"]["ms"] > 0
     for t in trials.values():   # every exact schedule reaches the same clustering
         assert t["accepted"] or t["reason"].startswith("error"), t
