@@ -102,6 +102,7 @@ struct acvd_ctx {
     // clusters
     int K = 0;
     DBuf<int> label, size, stamp, evald;
+    DBuf<int> uf_parent;           // clean: union-find links
     DBuf<unsigned long long> claim;
     DBuf<SweepState> dsweep;
     // relaxed steps
@@ -137,6 +138,7 @@ struct acvd_ctx {
     bool timing_broken = false;    // event timing unavailable on this device / driver
     int match_rounds = 1;          // claim/commit rounds per colour step (ACVD_MATCH_ROUNDS, up to kRounds)
     int eval_blocks = 0;           // evaluation kernels' blocks per SM, 3..5 (ACVD_EVAL_BLOCKS; 0 = defaults)
+    int eval_threads = 256;        // their threads per block: 256, or 128 (ACVD_EVAL_THREADS)
     int64_t sweep_kernels = 0;     // kernels in the sweep last enqueued
     int64_t loop_relaxed_kernels = 0, loop_exact_kernels = 0;   // kernels per sweep of the graph loop
     int64_t exact_kernels = 0, relaxed_kernels = 0;
@@ -303,28 +305,25 @@ constexpr int64_t kDefaultSplitMin = 600000;
 // Greedy colouring in vertex order on the host: each vertex takes the smallest
 // colour unused by its lower-numbered neighbours.  On meshes stored in a spatially
 // coherent order (grids, scans) it gives 4 balanced classes where the device's
-// hashed Jones-Plassmann colouring gives 6-7 with a few tiny ones.  The rings have
-// passed the device's validation (ids in [0, n)).  The loop is a serial chain through
-// the previous vertex's colour: colours are bytes (zero until written) and a neighbour
-// counts only when its id is lower, with no branch, which makes it about a quarter
-// faster on a Grace core than testing for "not yet coloured".  Writes color[0..n) and
-// returns the largest colour, or -1 when a vertex would need a 65th colour.
+// hashed Jones-Plassmann colouring gives 6-7 with a few tiny ones.  Writes color[0..n)
+// (the context's pinned buffer: a byte-colour, branch-free form of the loop measured
+// slower inside the engine on a Grace core) and returns the largest colour, or -1
+// when a vertex would need a 65th colour.
 static int greedy_colors_host(const int32_t* row, const int32_t* col, int64_t n, int* color) {
-    std::vector<uint8_t> c8((size_t)n, 0);
-    unsigned maxc = 0;
+    std::fill(color, color + n, -1);
+    int maxc = 0;
     for (int64_t v = 0; v < n; v++) {
         unsigned long long used = 0ull;
         for (int p = row[v]; p < row[v + 1]; p++) {
-            const uint32_t u = (uint32_t)col[p];
-            used |= (unsigned long long)(u < (uint32_t)v) << (c8[u] & 63u);
+            const int c = color[col[p]];
+            if (c >= 0) used |= 1ull << c;
         }
         if (used == ~0ull) return -1;
-        const unsigned c = (unsigned)__builtin_ctzll(~used);
-        c8[v] = (uint8_t)c;
+        const int c = __builtin_ctzll(~used);
+        color[v] = c;
         maxc = std::max(maxc, c);
     }
-    for (int64_t v = 0; v < n; v++) color[v] = c8[v];
-    return (int)maxc;
+    return maxc;
 }
 
 // Empties the highest colour class where it can: each of its items takes a free
@@ -540,6 +539,10 @@ acvd_ctx* acvd_create(const acvd_opts* opts) {
     if (const char* c = std::getenv("ACVD_SWEEP_COLORS")) ctx->sweep_by_color = std::atoi(c) != 0;
     if (const char* c = std::getenv("ACVD_RELAXED")) ctx->use_relaxed = std::atoi(c) != 0;
     if (const char* b = std::getenv("ACVD_EVAL_BLOCKS")) ctx->eval_blocks = std::atoi(b);
+    if (const char* t = std::getenv("ACVD_EVAL_THREADS")) {
+        const int v = std::atoi(t);
+        ctx->eval_threads = v == 128 ? 128 : 256;
+    }
     if (const char* r = std::getenv("ACVD_MATCH_ROUNDS")) {
         const int v = std::atoi(r);
         if (v >= 1 && v <= kRounds) ctx->match_rounds = v;
@@ -994,15 +997,26 @@ static int clean(acvd_ctx* ctx, int* n_disconnected) {
     CK(ctx->csize.resize(n));
     CK(ctx->multi.resize(ctx->K + 1));
     CK(ctx->best.resize(ctx->K + 1));
-    CK(launch_comp_init(st, ctx->comp.p, ctx->s));
-    for (int it = 0;; it++) {
-        if (it > 100000) return fail(ctx, ACVD_ERR_ITER_LIMIT, "connected-component labelling did not converge");
-        CK(zero_counter(ctx, kCntChanged));
-        // several propagation steps between host checks
-        for (int j = 0; j < 4; j++) CK(launch_comp_step(st, ctx->comp.p, ctx->s));
+    // union-find in one pass; should a link give up (a bound, never met in practice),
+    // min-id propagation with pointer jumping gives the same components
+    CK(ctx->uf_parent.resize(n));
+    CK(zero_counter(ctx, kCntChanged));
+    CK(launch_comp_union(st, ctx->comp.p, ctx->uf_parent.p, ctx->s));
+    {
         int r = sync_counters(ctx);
         if (r) return r;
-        if (ctx->h_counters[kCntChanged] == 0) break;
+    }
+    if (ctx->h_counters[kCntChanged] != 0) {
+        CK(launch_comp_init(st, ctx->comp.p, ctx->s));
+        for (int it = 0;; it++) {
+            if (it > 100000) return fail(ctx, ACVD_ERR_ITER_LIMIT, "connected-component labelling did not converge");
+            CK(zero_counter(ctx, kCntChanged));
+            // several propagation steps between host checks
+            for (int j = 0; j < 4; j++) CK(launch_comp_step(st, ctx->comp.p, ctx->s));
+            int r = sync_counters(ctx);
+            if (r) return r;
+            if (ctx->h_counters[kCntChanged] == 0) break;
+        }
     }
     CK(cudaMemsetAsync(ctx->csize.p, 0, n * sizeof(int), ctx->s));
     CK(cudaMemsetAsync(ctx->best.p, 0, (ctx->K + 1) * sizeof(unsigned long long), ctx->s));
@@ -1041,7 +1055,7 @@ static int enqueue_sweep(acvd_ctx* ctx, bool timing, bool relaxed) {
         if (timing) CK(cudaEventRecordWithFlags(ctx->ev_eval[2 * c], ctx->s, cudaEventRecordExternal));
         const bool split = ctx->has_work && ctx->split_min > 0 && cnt >= ctx->split_min;
         CK(launch_eval(ctx->metric, st, item0, cnt, c, ctx->cand_dest.p, ctx->cand_prio.p, !relaxed, split,
-                       ctx->eval_blocks, ctx->s));
+                       ctx->eval_blocks, ctx->eval_threads, ctx->s));
         if (split) kernels++;
         if (timing) CK(cudaEventRecordWithFlags(ctx->ev_eval[2 * c + 1], ctx->s, cudaEventRecordExternal));
         if (relaxed) {
@@ -1290,14 +1304,14 @@ static int energy_total(acvd_ctx* ctx, double* out) {
 
 // Algorithmic bytes of the evaluation kernels from the device counters: per visited
 // item its boundary flag; per screened item its 8-slot ring, label and evaluation
-// sweep; per ring slot the neighbour's label; per cached screen its cache entry, label,
-// evaluation sweep and up to 3 cluster stamps; per boundary item its record, its
+// sweep; per ring slot the neighbour's label; per cached screen its 16-byte record
+// (cluster, targets, evaluation sweep) and up to 4 cluster stamps; per boundary item its record, its
 // cluster's record and size; per destination cluster its record; per proposal the
 // candidate slots and two claim words.
 static int64_t eval_bytes_of(const acvd_ctx* ctx, const unsigned long long* c) {
     const int64_t R = ctx->metric == kIso ? 16 : (ctx->metric == kQEM ? 40 : 64);
     const int64_t C = 16 * (int64_t)ev_stride(ctx->metric);
-    return 1 * (int64_t)c[kCntVisited] + 40 * (int64_t)c[kCntScreened] + 36 * (int64_t)c[kCntCached] +
+    return 1 * (int64_t)c[kCntVisited] + 40 * (int64_t)c[kCntScreened] + 32 * (int64_t)c[kCntCached] +
            4 * (int64_t)c[kCntSlots] + (R + C + 4) * (int64_t)c[kCntBoundary] + C * (int64_t)c[kCntTargets] +
            24 * (int64_t)c[kCntCand];
 }
