@@ -1630,8 +1630,11 @@ extern "C" int acvd_get_clusters(acvd_ctx* ctx, int32_t* sizes, double* S, doubl
     if (r) return r;
     const int K = ctx->K;
     const int as = acc_stride(ctx->metric);
-    std::vector<df> acc((size_t)K * as);
-    CK(cudaMemcpyAsync(acc.data(), ctx->acc.p, acc.size() * sizeof(df), cudaMemcpyDeviceToHost, ctx->s));
+    // the accumulators come back only when one of their views is asked for
+    const bool want_acc = S || W || quadric;
+    std::vector<df> acc(want_acc ? (size_t)K * as : 0);
+    if (want_acc)
+        CK(cudaMemcpyAsync(acc.data(), ctx->acc.p, acc.size() * sizeof(df), cudaMemcpyDeviceToHost, ctx->s));
     if (sizes) CK(cudaMemcpyAsync(sizes, ctx->size.p, K * sizeof(int), cudaMemcpyDeviceToHost, ctx->s));
     if (energy) CK(cudaMemcpyAsync(energy, ctx->energy.p, K * sizeof(double), cudaMemcpyDeviceToHost, ctx->s));
     if (energy_total) {
@@ -1647,7 +1650,7 @@ extern "C" int acvd_get_clusters(acvd_ctx* ctx, int32_t* sizes, double* S, doubl
         CK(cudaStreamSynchronize(ctx->s));
     }
     CK(cudaStreamSynchronize(ctx->s));
-    for (int k = 0; k < K; k++) {
+    for (int k = 0; want_acc && k < K; k++) {
         const df* a = acc.data() + (size_t)k * as;
         auto d = [](df x) { return (double)x.hi + (double)x.lo; };
         if (S) for (int j = 0; j < 3; j++) S[3 * k + j] = d(a[j]);
