@@ -1770,6 +1770,82 @@ __global__ void fill_color_kernel(DevState st, const int* __restrict__ items, in
     warp_count(ctr(st.counters, kCntAssigned), done);
 }
 
+// The same rounds over a list of the unassigned items: fill_collect_kernel lists them
+// per colour class (class c at list[off[c] ...], items being numbered by class); a
+// round then runs fill_list_kernel class after class over its list.  Items of one
+// class are never ring neighbours, so the order inside a class list does not matter
+// and the labels equal the full-class rounds'.
+__global__ void fill_collect_kernel(DevState st, const int64_t* __restrict__ off, int ncolors, int* __restrict__ list,
+                                    unsigned* __restrict__ cnt) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= st.n || st.label[i] < st.k) return;
+    int c = 0;
+    while (c + 1 < ncolors && off[c + 1] <= i) c++;
+    list[off[c] + atomicAdd(&cnt[c], 1u)] = (int)i;
+}
+
+__global__ void fill_list_kernel(DevState st, const int* __restrict__ list, const unsigned* __restrict__ cnt) {
+    const unsigned n = *cnt;
+    unsigned done = 0;
+    for (unsigned j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        const int i = list[j];
+        if (st.label[i] < st.k) continue;   // filled in an earlier round
+        const int p0 = st.row[i], p1 = st.row[i + 1];
+        int B = -1;
+        for (int p = p0; p < p1 && B < 0; p++) {
+            const int l = st.label[st.col[p]];
+            if (l < st.k) B = l;
+        }
+        if (B >= 0 && (!st.flags->connexity || ring_connected(st, p0, p1, st.k))) {
+            st.label[i] = B;
+            done++;
+        }
+    }
+    warp_count(ctr(st.counters, kCntAssigned), done);
+}
+
+// Every round over short lists in one block: the classes in order with a block barrier
+// between them (the items of one class read only labels of other classes), rounds until
+// one assigns nothing.  *err is set when the round bound runs out.
+constexpr int kFillRounds = 1 << 20;
+
+__global__ void __launch_bounds__(1024) fill_block_kernel(DevState st, const int* __restrict__ list,
+                                                          const int64_t* __restrict__ off, int ncolors,
+                                                          const unsigned* __restrict__ cnt, unsigned* err) {
+    __shared__ int s_changed;
+    unsigned done = 0;
+    int round = 0;
+    for (; round < kFillRounds; round++) {
+        if (threadIdx.x == 0) s_changed = 0;
+        __syncthreads();
+        for (int c = 0; c < ncolors; c++) {
+            const int* lc = list + off[c];
+            const unsigned n = cnt[c];
+            for (unsigned j = threadIdx.x; j < n; j += blockDim.x) {
+                const int i = lc[j];
+                if (st.label[i] < st.k) continue;
+                const int p0 = st.row[i], p1 = st.row[i + 1];
+                int B = -1;
+                for (int p = p0; p < p1 && B < 0; p++) {
+                    const int l = st.label[st.col[p]];
+                    if (l < st.k) B = l;
+                }
+                if (B >= 0 && (!st.flags->connexity || ring_connected(st, p0, p1, st.k))) {
+                    st.label[i] = B;
+                    done++;
+                    s_changed = 1;
+                }
+            }
+            __syncthreads();   // the next class reads this class's labels
+        }
+        const bool again = s_changed != 0;
+        __syncthreads();
+        if (!again) break;
+    }
+    if (round == kFillRounds && threadIdx.x == 0) *err = 1u;
+    warp_count(ctr(st.counters, kCntAssigned), done);
+}
+
 // ---------------------------------------------------------------------------
 // boundary edges, compaction, dual mesh
 // ---------------------------------------------------------------------------
@@ -2175,6 +2251,28 @@ cudaError_t launch_fill_color(const DevState& st, const int* items, int64_t coun
     if (count == 0) return cudaSuccess;
     ++g_launches;
     fill_color_kernel<<<nblk(count), 256, 0, s>>>(st, items, count);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fill_collect(const DevState& st, const int64_t* off, int ncolors, int* list, unsigned* cnt,
+                                cudaStream_t s) {
+    ++g_launches;
+    fill_collect_kernel<<<nblk(st.n), 256, 0, s>>>(st, off, ncolors, list, cnt);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fill_list(const DevState& st, const int* list, const unsigned* cnt, int64_t cap, cudaStream_t s) {
+    if (cap == 0) return cudaSuccess;
+    ++g_launches;
+    const unsigned grid = (unsigned)std::min<int64_t>(nblk(cap), 2 * sm_count());
+    fill_list_kernel<<<grid, 256, 0, s>>>(st, list, cnt);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fill_block(const DevState& st, const int* list, const int64_t* off, int ncolors,
+                              const unsigned* cnt, unsigned* err, cudaStream_t s) {
+    ++g_launches;
+    fill_block_kernel<<<1, 1024, 0, s>>>(st, list, off, ncolors, cnt, err);
     return cudaGetLastError();
 }
 

@@ -103,6 +103,9 @@ struct acvd_ctx {
     int K = 0;
     DBuf<int> label, size, stamp, evald;
     DBuf<int> uf_parent;           // clean: union-find links
+    DBuf<int> fill_list;           // hole filling: unassigned items per colour class
+    DBuf<unsigned> fill_cnt;
+    DBuf<int64_t> fill_off;
     DBuf<unsigned long long> claim;
     DBuf<SweepState> dsweep;
     // relaxed steps
@@ -961,32 +964,53 @@ static int recompute(acvd_ctx* ctx) {
     return ACVD_OK;
 }
 
+// FillHolesInClustering (Common/vtkUniformClustering.h:552-633): rounds of the colour
+// classes in order until no unassigned item can join a cluster.  The rounds run over
+// lists of the unassigned items, collected once: up to kFillBlockItems of them, every
+// round in one single-block launch; more, one launch per class and round with a host
+// check per round.  *unassigned: the items left (collected minus filled).
+constexpr int64_t kFillBlockItems = 65536;
+
 static int fill_holes(acvd_ctx* ctx, int* unassigned) {
     DevState st = ctx->state();
-    for (int round = 0;; round++) {
-        if (round > 1000000) return fail(ctx, ACVD_ERR_ITER_LIMIT, "hole filling did not finish");
+    const int nc = ctx->ncolors;
+    CK(ctx->fill_list.resize(ctx->nV));
+    CK(ctx->fill_cnt.resize(nc + 1));   // [nc]: the single-block pass's error flag
+    CK(ctx->fill_off.resize(nc + 1));
+    CK(cudaMemsetAsync(ctx->fill_cnt.p, 0, (nc + 1) * sizeof(unsigned), ctx->s));
+    CK(cudaMemcpyAsync(ctx->fill_off.p, ctx->color_off.data(), (nc + 1) * sizeof(int64_t), cudaMemcpyHostToDevice,
+                       ctx->s));
+    CK(launch_fill_collect(st, ctx->fill_off.p, nc, ctx->fill_list.p, ctx->fill_cnt.p, ctx->s));
+    std::vector<unsigned> cnt(nc);
+    CK(cudaMemcpyAsync(cnt.data(), ctx->fill_cnt.p, nc * sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->s));
+    CK(cudaStreamSynchronize(ctx->s));
+    int64_t total = 0;
+    for (int c = 0; c < nc; c++) total += cnt[c];
+    int64_t filled = 0;
+    if (total > 0 && total <= kFillBlockItems) {
         CK(zero_counter(ctx, kCntAssigned));
-        for (int c = 0; c < ctx->ncolors; c++)
-            CK(launch_fill_color(st, ctx->color_items.p + ctx->color_off[c], ctx->color_off[c + 1] - ctx->color_off[c],
-                                 ctx->s));
+        CK(launch_fill_block(st, ctx->fill_list.p, ctx->fill_off.p, nc, ctx->fill_cnt.p, ctx->fill_cnt.p + nc, ctx->s));
+        unsigned err = 0;
+        CK(cudaMemcpyAsync(&err, ctx->fill_cnt.p + nc, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->s));
         int r = sync_counters(ctx);
         if (r) return r;
-        if (ctx->h_counters[kCntAssigned] == 0) break;
+        if (err) return fail(ctx, ACVD_ERR_ITER_LIMIT, "hole filling did not finish");
+        filled = (int64_t)ctx->h_counters[kCntAssigned];
+    } else if (total > 0) {
+        for (int round = 0;; round++) {
+            if (round > 1000000) return fail(ctx, ACVD_ERR_ITER_LIMIT, "hole filling did not finish");
+            CK(zero_counter(ctx, kCntAssigned));
+            for (int c = 0; c < nc; c++)
+                if (cnt[c])
+                    CK(launch_fill_list(st, ctx->fill_list.p + ctx->color_off[c], ctx->fill_cnt.p + c, cnt[c],
+                                        ctx->s));
+            int r = sync_counters(ctx);
+            if (r) return r;
+            if (ctx->h_counters[kCntAssigned] == 0) break;
+            filled += (int64_t)ctx->h_counters[kCntAssigned];
+        }
     }
-    if (unassigned) {
-        // items still unassigned: count them with the boundary/compaction helpers' flag kernel
-        CK(ctx->wk_cnt.resize(ctx->K + 1));
-        CK(cudaMemsetAsync(ctx->wk_cnt.p, 0, (ctx->K + 1) * sizeof(uint32_t), ctx->s));
-        CK(ctx->wk_a.resize(ctx->nV));
-        CK(ctx->wk_b.resize(ctx->nV));
-        CK(launch_cluster_keys(st, ctx->wk_a.p, ctx->wk_b.p, ctx->wk_cnt.p, ctx->s));
-        std::vector<uint32_t> cnt(ctx->K);
-        CK(cudaMemcpyAsync(cnt.data(), ctx->wk_cnt.p, ctx->K * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->s));
-        CK(cudaStreamSynchronize(ctx->s));
-        int64_t assigned = 0;
-        for (int k = 0; k < ctx->K; k++) assigned += cnt[k];
-        *unassigned = (int)(ctx->nV - assigned);
-    }
+    if (unassigned) *unassigned = (int)(total - filled);
     return ACVD_OK;
 }
 
@@ -1597,8 +1621,10 @@ extern "C" int acvd_minimize(acvd_ctx* ctx, acvd_stats* stats) {
     local.reverted = (int64_t)ctx->h_counters[kCntReverted];
     local.eval_bytes = eval_bytes_of(ctx, ctx->h_counters);
     if (status == ACVD_OK) {
+        // every way out of the loop follows a convergence event, whose recompute left
+        // the per-cluster FP64 energies of the final labels in place
         double et = 0.0;
-        int rr = acvd_get_clusters(ctx, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, &et);
+        int rr = energy_total(ctx, &et);
         if (rr) return rr;
         local.energy = et;
     }

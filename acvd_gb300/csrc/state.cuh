@@ -364,6 +364,16 @@ cudaError_t launch_comp_union(const DevState& st, int* comp, int* parent, cudaSt
 cudaError_t launch_comp_finish(const DevState& st, const int* comp, int* csize, unsigned long long* best,
                                int* multi, cudaStream_t s);
 cudaError_t launch_fill_color(const DevState& st, const int* items, int64_t count, cudaStream_t s);
+// hole filling over lists of the unassigned items: collect them per colour class
+// (class c's list at list[off[c] ...], cnt[c] entries; off: ncolors + 1 class offsets
+// on the device), then one round of class c over its list (cap: the class size)
+cudaError_t launch_fill_collect(const DevState& st, const int64_t* off, int ncolors, int* list, unsigned* cnt,
+                                cudaStream_t s);
+cudaError_t launch_fill_list(const DevState& st, const int* list, const unsigned* cnt, int64_t cap, cudaStream_t s);
+// every round over the class lists in one block (short lists); *err = 1 if the round
+// bound ran out
+cudaError_t launch_fill_block(const DevState& st, const int* list, const int64_t* off, int ncolors,
+                              const unsigned* cnt, unsigned* err, cudaStream_t s);
 cudaError_t launch_boundary_edges(const int* edge_v, int64_t ne, const int* label, uint32_t* flags,
                                   cudaStream_t s);
 cudaError_t launch_compact(const uint32_t* flags, const uint32_t* pos, int64_t n, int* out, cudaStream_t s);
