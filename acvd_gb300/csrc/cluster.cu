@@ -1811,8 +1811,17 @@ constexpr int kFillRounds = 1 << 20;
 
 __global__ void __launch_bounds__(1024) fill_block_kernel(DevState st, const int* __restrict__ list,
                                                           const int64_t* __restrict__ off, int ncolors,
-                                                          const unsigned* __restrict__ cnt, unsigned* err) {
+                                                          const unsigned* __restrict__ cnt, unsigned* err,
+                                                          unsigned max_items) {
     __shared__ int s_changed;
+    // lists longer than max_items: *err = 2 and nothing done (the host runs the rounds
+    // one launch per class instead)
+    unsigned total = 0;
+    for (int c = 0; c < ncolors; c++) total += cnt[c];
+    if (total > max_items) {
+        if (threadIdx.x == 0) *err = 2u;
+        return;
+    }
     unsigned done = 0;
     int round = 0;
     for (; round < kFillRounds; round++) {
@@ -2270,9 +2279,9 @@ cudaError_t launch_fill_list(const DevState& st, const int* list, const unsigned
 }
 
 cudaError_t launch_fill_block(const DevState& st, const int* list, const int64_t* off, int ncolors,
-                              const unsigned* cnt, unsigned* err, cudaStream_t s) {
+                              const unsigned* cnt, unsigned* err, unsigned max_items, cudaStream_t s) {
     ++g_launches;
-    fill_block_kernel<<<1, 1024, 0, s>>>(st, list, off, ncolors, cnt, err);
+    fill_block_kernel<<<1, 1024, 0, s>>>(st, list, off, ncolors, cnt, err, max_items);
     return cudaGetLastError();
 }
 

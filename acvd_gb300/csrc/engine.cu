@@ -271,9 +271,10 @@ static int sync_counters(acvd_ctx* ctx) {
     return ACVD_OK;
 }
 
+// (a copy from pageable host memory returns once the source is staged, so neither this
+// nor set_sweep_state waits for the stream)
 static int upload_flags(acvd_ctx* ctx) {
     CK(cudaMemcpyAsync(ctx->dflags.p, &ctx->flags, sizeof(RunFlags), cudaMemcpyHostToDevice, ctx->s));
-    CK(cudaStreamSynchronize(ctx->s));
     return ACVD_OK;
 }
 
@@ -286,7 +287,6 @@ static int set_sweep_state(acvd_ctx* ctx, int sweep, int floor) {
     CK(ctx->bflag.resize(ctx->nV));
     CK(ctx->tcache.resize(ctx->nV));
     CK(cudaMemsetAsync(ctx->bflag.p, 1, ctx->nV, ctx->s));
-    CK(cudaStreamSynchronize(ctx->s));
     return ACVD_OK;
 }
 
@@ -981,22 +981,25 @@ static int fill_holes(acvd_ctx* ctx, int* unassigned) {
     CK(cudaMemcpyAsync(ctx->fill_off.p, ctx->color_off.data(), (nc + 1) * sizeof(int64_t), cudaMemcpyHostToDevice,
                        ctx->s));
     CK(launch_fill_collect(st, ctx->fill_off.p, nc, ctx->fill_list.p, ctx->fill_cnt.p, ctx->s));
-    std::vector<unsigned> cnt(nc);
-    CK(cudaMemcpyAsync(cnt.data(), ctx->fill_cnt.p, nc * sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->s));
-    CK(cudaStreamSynchronize(ctx->s));
-    int64_t total = 0;
-    for (int c = 0; c < nc; c++) total += cnt[c];
-    int64_t filled = 0;
-    if (total > 0 && total <= kFillBlockItems) {
-        CK(zero_counter(ctx, kCntAssigned));
-        CK(launch_fill_block(st, ctx->fill_list.p, ctx->fill_off.p, nc, ctx->fill_cnt.p, ctx->fill_cnt.p + nc, ctx->s));
-        unsigned err = 0;
-        CK(cudaMemcpyAsync(&err, ctx->fill_cnt.p + nc, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->s));
+    // the single-block pass, which declines lists longer than kFillBlockItems; the
+    // counts and its status come back with one host round trip
+    CK(zero_counter(ctx, kCntAssigned));
+    CK(launch_fill_block(st, ctx->fill_list.p, ctx->fill_off.p, nc, ctx->fill_cnt.p, ctx->fill_cnt.p + nc,
+                         (unsigned)kFillBlockItems, ctx->s));
+    std::vector<unsigned> cnt(nc + 1);
+    CK(cudaMemcpyAsync(cnt.data(), ctx->fill_cnt.p, (nc + 1) * sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->s));
+    {
         int r = sync_counters(ctx);
         if (r) return r;
-        if (err) return fail(ctx, ACVD_ERR_ITER_LIMIT, "hole filling did not finish");
+    }
+    int64_t total = 0;
+    for (int c = 0; c < nc; c++) total += cnt[c];
+    const unsigned status = cnt[nc];
+    int64_t filled = 0;
+    if (status == 1) return fail(ctx, ACVD_ERR_ITER_LIMIT, "hole filling did not finish");
+    if (status == 0) {
         filled = (int64_t)ctx->h_counters[kCntAssigned];
-    } else if (total > 0) {
+    } else {
         for (int round = 0;; round++) {
             if (round > 1000000) return fail(ctx, ACVD_ERR_ITER_LIMIT, "hole filling did not finish");
             CK(zero_counter(ctx, kCntAssigned));

@@ -370,10 +370,10 @@ cudaError_t launch_fill_color(const DevState& st, const int* items, int64_t coun
 cudaError_t launch_fill_collect(const DevState& st, const int64_t* off, int ncolors, int* list, unsigned* cnt,
                                 cudaStream_t s);
 cudaError_t launch_fill_list(const DevState& st, const int* list, const unsigned* cnt, int64_t cap, cudaStream_t s);
-// every round over the class lists in one block (short lists); *err = 1 if the round
-// bound ran out
+// every round over the class lists in one block when they hold at most max_items
+// items; *err = 1 if the round bound ran out, 2 if the lists were longer (nothing done)
 cudaError_t launch_fill_block(const DevState& st, const int* list, const int64_t* off, int ncolors,
-                              const unsigned* cnt, unsigned* err, cudaStream_t s);
+                              const unsigned* cnt, unsigned* err, unsigned max_items, cudaStream_t s);
 cudaError_t launch_boundary_edges(const int* edge_v, int64_t ne, const int* label, uint32_t* flags,
                                   cudaStream_t s);
 cudaError_t launch_compact(const uint32_t* flags, const uint32_t* pos, int64_t n, int* out, cudaStream_t s);
