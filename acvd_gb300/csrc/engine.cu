@@ -106,6 +106,7 @@ struct acvd_ctx {
     DBuf<int> fill_list;           // hole filling: unassigned items per colour class
     DBuf<unsigned> fill_cnt;
     DBuf<int64_t> fill_off;
+    int64_t fill_block_max = 65536;   // ACVD_FILL_BLOCK_MAX: longest lists the single-block fill takes
     DBuf<unsigned long long> claim;
     DBuf<SweepState> dsweep;
     // relaxed steps
@@ -542,6 +543,8 @@ acvd_ctx* acvd_create(const acvd_opts* opts) {
     if (const char* c = std::getenv("ACVD_SWEEP_COLORS")) ctx->sweep_by_color = std::atoi(c) != 0;
     if (const char* c = std::getenv("ACVD_RELAXED")) ctx->use_relaxed = std::atoi(c) != 0;
     if (const char* b = std::getenv("ACVD_EVAL_BLOCKS")) ctx->eval_blocks = std::atoi(b);
+    if (const char* f = std::getenv("ACVD_FILL_BLOCK_MAX"))
+        ctx->fill_block_max = std::max<int64_t>(0, std::min<int64_t>(std::atoll(f), 1ll << 30));
     if (const char* t = std::getenv("ACVD_EVAL_THREADS")) {
         const int v = std::atoi(t);
         ctx->eval_threads = v == 128 ? 128 : 256;
@@ -966,10 +969,10 @@ static int recompute(acvd_ctx* ctx) {
 
 // FillHolesInClustering (Common/vtkUniformClustering.h:552-633): rounds of the colour
 // classes in order until no unassigned item can join a cluster.  The rounds run over
-// lists of the unassigned items, collected once: up to kFillBlockItems of them, every
-// round in one single-block launch; more, one launch per class and round with a host
-// check per round.  *unassigned: the items left (collected minus filled).
-constexpr int64_t kFillBlockItems = 65536;
+// lists of the unassigned items, collected once: up to fill_block_max of them (65,536;
+// ACVD_FILL_BLOCK_MAX), every round in one single-block launch; more, one launch per
+// class and round with a host check per round.  Both give the same labels.
+// *unassigned: the items left (collected minus filled).
 
 static int fill_holes(acvd_ctx* ctx, int* unassigned) {
     DevState st = ctx->state();
@@ -981,11 +984,11 @@ static int fill_holes(acvd_ctx* ctx, int* unassigned) {
     CK(cudaMemcpyAsync(ctx->fill_off.p, ctx->color_off.data(), (nc + 1) * sizeof(int64_t), cudaMemcpyHostToDevice,
                        ctx->s));
     CK(launch_fill_collect(st, ctx->fill_off.p, nc, ctx->fill_list.p, ctx->fill_cnt.p, ctx->s));
-    // the single-block pass, which declines lists longer than kFillBlockItems; the
+    // the single-block pass, which declines lists longer than fill_block_max; the
     // counts and its status come back with one host round trip
     CK(zero_counter(ctx, kCntAssigned));
     CK(launch_fill_block(st, ctx->fill_list.p, ctx->fill_off.p, nc, ctx->fill_cnt.p, ctx->fill_cnt.p + nc,
-                         (unsigned)kFillBlockItems, ctx->s));
+                         (unsigned)ctx->fill_block_max, ctx->s));
     std::vector<unsigned> cnt(nc + 1);
     CK(cudaMemcpyAsync(cnt.data(), ctx->fill_cnt.p, (nc + 1) * sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->s));
     {

@@ -104,3 +104,30 @@ def test_identity_sampling_solves_and_cap_stops_the_loop(oracle_lib):
 
     assert qem(None) > 1
     assert qem(1) == 1
+
+
+@pytest.mark.gpu
+def test_hole_filling_paths_agree(monkeypatch):
+    """Hole filling (Common/vtkUniformClustering.h:552-633) over the unassigned items of
+    type -1 sampling (K seeds, every other item unassigned): all rounds in one
+    single-block launch, and one launch per colour class and round (ACVD_FILL_BLOCK_MAX=0,
+    read when a context is created), give the same labels after a whole solve."""
+    t = synth.torus(128, 64, seed=3)
+
+    def run(block_max):
+        if block_max is None:
+            monkeypatch.delenv("ACVD_FILL_BLOCK_MAX", raising=False)
+        else:
+            monkeypatch.setenv("ACVD_FILL_BLOCK_MAX", str(block_max))
+        r = acvd_gb300.QIsotropicDiscreteRemeshing.New()
+        r.SetInput(acvd_gb300.Surface(t.points, t.faces))
+        r.SetNumberOfClusters(300)
+        r.SetInitialSamplingType(-1)
+        r.Remesh()
+        return np.asarray(r.GetClustering()).copy(), r.Stats
+
+    lab_block, st_block = run(None)
+    lab_rounds, st_rounds = run(0)
+    assert np.all(lab_block < 300)
+    assert np.array_equal(lab_block, lab_rounds)
+    assert st_block["sweeps"] == st_rounds["sweeps"]
