@@ -1238,24 +1238,34 @@ def clustering_line(args, name, steps, warmup, e2e_on, cpu_on):
         h_pd = pinned(torch, None if pd is None else c(pd, dtype=np.float32))
         h_lab0 = pinned(torch, c(lab0, dtype=np.int32))
         out = pinned(torch, c(lab0, dtype=np.int32))
+        parts = {"set_mesh": [], "set_metric": [], "set_labels": [], "minimize": [], "labels": []}
         # untimed warm-up calls first (the engine's device buffers are allocated on the first)
         for it in range(warmup + max(1, steps)):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             eng2.set_mesh(h_pts, h_faces, h_row, h_col, h_ev)
+            t1 = time.perf_counter()
             eng2.set_metric(w["metric"], h_ind, h_pd, w["gradation"])
+            t2 = time.perf_counter()
             eng2.set_unconstrained_initialization(w["uinit"])
             eng2.set_labels(w["k"], h_lab0)
+            t3 = time.perf_counter()
             eng2.minimize()
+            t4 = time.perf_counter()
             eng2.labels(out=out)
             torch.cuda.synchronize()
+            t5 = time.perf_counter()
             if it >= warmup:
-                e2e_ms.append(1000.0 * (time.perf_counter() - t0))
+                e2e_ms.append(1000.0 * (t5 - t0))
+                for key, a, b_ in (("set_mesh", t0, t1), ("set_metric", t1, t2), ("set_labels", t2, t3),
+                                   ("minimize", t3, t4), ("labels", t4, t5)):
+                    parts[key].append(1000.0 * (b_ - a))
         eng2.close()
         assert np.array_equal(out, lab), "end-to-end run differs from the resident run"
         e2e_t = replicas.max_over_ranks(statistics.mean(e2e_ms), device=f"cuda:{device}")
         e2e = {"value": ws * n / (e2e_t / 1000.0), "unit": "items/s", "h2d_bytes_per_step": int(h2d),
-               "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_t, "warmup_calls": warmup}
+               "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_t, "warmup_calls": warmup,
+               "breakdown_ms": {k: statistics.mean(v) for k, v in parts.items()}}
 
     replicas.barrier()
     if rank != 0:
