@@ -1749,32 +1749,10 @@ __global__ void comp_reset_kernel(DevState st, const int* __restrict__ comp,
 // connected without it (the reference applies the same local test to the null
 // cluster, Common/vtkUniformClustering.h:606-607)
 // ---------------------------------------------------------------------------
-__global__ void fill_color_kernel(DevState st, const int* __restrict__ items, int64_t count) {
-    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    unsigned done = 0;
-    if (idx < count) {
-        const int i = items[idx];
-        if (st.label[i] >= st.k) {
-            const int p0 = st.row[i], p1 = st.row[i + 1];
-            int B = -1;
-            for (int p = p0; p < p1 && B < 0; p++) {
-                const int l = st.label[st.col[p]];
-                if (l < st.k) B = l;
-            }
-            if (B >= 0 && (!st.flags->connexity || ring_connected(st, p0, p1, st.k))) {
-                st.label[i] = B;
-                done = 1;
-            }
-        }
-    }
-    warp_count(ctr(st.counters, kCntAssigned), done);
-}
-
-// The same rounds over a list of the unassigned items: fill_collect_kernel lists them
+// The rounds run over lists of the unassigned items: fill_collect_kernel lists them
 // per colour class (class c at list[off[c] ...], items being numbered by class); a
-// round then runs fill_list_kernel class after class over its list.  Items of one
-// class are never ring neighbours, so the order inside a class list does not matter
-// and the labels equal the full-class rounds'.
+// round then runs the classes in order over their lists.  Items of one class are never
+// ring neighbours, so the order inside a class list does not matter.
 __global__ void fill_collect_kernel(DevState st, const int64_t* __restrict__ off, int ncolors, int* __restrict__ list,
                                     unsigned* __restrict__ cnt) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -2256,12 +2234,6 @@ cudaError_t launch_comp_finish(const DevState& st, const int* comp, int* csize, 
     return cudaGetLastError();
 }
 
-cudaError_t launch_fill_color(const DevState& st, const int* items, int64_t count, cudaStream_t s) {
-    if (count == 0) return cudaSuccess;
-    ++g_launches;
-    fill_color_kernel<<<nblk(count), 256, 0, s>>>(st, items, count);
-    return cudaGetLastError();
-}
 
 cudaError_t launch_fill_collect(const DevState& st, const int64_t* off, int ncolors, int* list, unsigned* cnt,
                                 cudaStream_t s) {

@@ -363,7 +363,6 @@ cudaError_t launch_comp_step(const DevState& st, int* comp, cudaStream_t s);
 cudaError_t launch_comp_union(const DevState& st, int* comp, int* parent, cudaStream_t s);
 cudaError_t launch_comp_finish(const DevState& st, const int* comp, int* csize, unsigned long long* best,
                                int* multi, cudaStream_t s);
-cudaError_t launch_fill_color(const DevState& st, const int* items, int64_t count, cudaStream_t s);
 // hole filling over lists of the unassigned items: collect them per colour class
 // (class c's list at list[off[c] ...], cnt[c] entries; off: ncolors + 1 class offsets
 // on the device), then one round of class c over its list (cap: the class size)
