@@ -32,9 +32,7 @@ Two families of candidates:
       classes on grid-like meshes, against the hashed Jones-Plassmann colouring's 6-7 with
       a few nearly empty ones): fewer colour steps per sweep;
     - ``squeeze_colors``: the Jones-Plassmann colouring with its highest classes emptied
-      where a local recolouring allows it;
-    - ``squeeze_tail``: the same, for top classes of at most 1,024 items only (the nearly
-      empty classes the hashed colouring leaves), at a fraction of the set-up time.
+      where a local recolouring allows it.
   One of them is accepted only when every item is assigned and its energy is within
   ``energy_rel_tol`` (default 1e-3, the 0.1 % bar against the reference's converged energy)
   of the default schedule's energy on the same input.
@@ -76,7 +74,7 @@ class Schedule:
     host_loop: bool = False
     relaxed: bool = True
     match_rounds: int = 1
-    coloring: str = "jp"           # jp (device Jones-Plassmann) | order | squeeze | squeeze_tail
+    coloring: str = "jp"           # jp (device Jones-Plassmann) | order | squeeze
     split_min: int | None = None   # None: the engine's threshold; 0: never split
     eval_blocks: int | None = None  # evaluation kernels' blocks per SM (3, 4, 5); None: the defaults
     eval_threads: int | None = None  # evaluation kernels' threads per block (128); None: 256
@@ -107,8 +105,7 @@ EXACT_SCHEDULES = (DEFAULT, Schedule("host_loop", host_loop=True), Schedule("per
 APPROX_SCHEDULES = (Schedule("exact_sweeps", relaxed=False, exact=False),
                     Schedule("match2", match_rounds=2, exact=False),
                     Schedule("order_colors", coloring="order", exact=False),
-                    Schedule("squeeze_colors", coloring="squeeze", exact=False),
-                    Schedule("squeeze_tail", coloring="squeeze_tail", exact=False))
+                    Schedule("squeeze_colors", coloring="squeeze", exact=False))
 BY_NAME = {s.name: s for s in EXACT_SCHEDULES + APPROX_SCHEDULES}
 
 

@@ -336,15 +336,13 @@ static int greedy_colors_host(const int32_t* row, const int32_t* col, int64_t n,
 // order, so deterministic; each pass visits only the items of the class it empties
 // (listed in item order by one scan), since recolouring touches no other item of
 // that class.  Returns the new largest colour.
-static int squeeze_top_color(const int32_t* row, const int32_t* col, int* color, int64_t n, int maxc,
-                             int64_t max_class = INT64_MAX) {
+static int squeeze_top_color(const int32_t* row, const int32_t* col, int* color, int64_t n, int maxc) {
     std::vector<int> top_items;
     while (maxc > 0) {
         const int top = maxc;
         top_items.clear();
         for (int64_t v = 0; v < n; v++)
             if (color[v] == top) top_items.push_back((int)v);
-        if ((int64_t)top_items.size() > max_class) break;   // only classes of at most max_class items
         bool emptied = true;
         for (const int v : top_items) {
             unsigned long long used = 0ull;
@@ -375,8 +373,6 @@ static int squeeze_top_color(const int32_t* row, const int32_t* col, int* color,
     }
     return maxc;
 }
-
-constexpr int64_t kSqueezeTail = 1024;   // squeeze_tail: largest class it empties
 
 // The context's pinned host array of n colours, through which the host colourings
 // reach the device.
@@ -431,17 +427,13 @@ static int setup_colors(acvd_ctx* ctx, const int32_t* h_row, const int32_t* h_co
         CK(cudaMemcpy(&maxc, d_maxc, sizeof(int), cudaMemcpyDeviceToHost));
         if (maxc >= 64) return fail(ctx, ACVD_ERR_UNSUPPORTED, "more than 64 colours needed (vertex valence too high)");
     }
-    // squeeze: every class it can empty from the top; squeeze_tail: only top classes of
-    // at most kSqueezeTail items (the nearly empty ones the hashed colouring leaves)
-    const bool squeeze_all = how && std::strcmp(how, "squeeze") == 0;
-    const bool squeeze_tail = how && std::strcmp(how, "squeeze_tail") == 0;
-    if ((squeeze_all || squeeze_tail) && maxc > 0) {
+    if (how && std::strcmp(how, "squeeze") == 0 && maxc > 0) {
         int* hc = nullptr;
         int r = host_color_buffer(ctx, n, &hc);
         if (r) return r;
         CK(cudaMemcpyAsync(hc, ctx->wk_int.p, n * sizeof(int), cudaMemcpyDeviceToHost, ctx->s));
         CK(cudaStreamSynchronize(ctx->s));
-        maxc = squeeze_top_color(h_row, h_col, hc, n, maxc, squeeze_tail ? kSqueezeTail : INT64_MAX);
+        maxc = squeeze_top_color(h_row, h_col, hc, n, maxc);
         CK(cudaMemcpyAsync(ctx->wk_int.p, hc, n * sizeof(int), cudaMemcpyHostToDevice, ctx->s));
         CK(cudaStreamSynchronize(ctx->s));
     }

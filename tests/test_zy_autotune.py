@@ -57,9 +57,9 @@ def test_approximate_colourings_within_the_energy_bar(tmp_path):
     kw = dict(indicator=m.indicator, gradation=1.5, level=3, unconstrained_init=1, repeats=2, topology=topo)
     s, rep = at.tune_problem(m.points, m.faces, "qem", k, lab0, tuner=tuner, **kw)
     trials = {t["schedule"]: t for t in rep["trials"]}
-    assert {"order_colors", "squeeze_colors", "squeeze_tail"} <= set(trials)
+    assert {"order_colors", "squeeze_colors"} <= set(trials)
     base = trials["graphs"]["energy"]
-    for name in ("order_colors", "squeeze_colors", "squeeze_tail"):
+    for name in ("order_colors", "squeeze_colors"):
         t = trials[name]
         assert t["accepted"] == (abs(t["energy"] - base) <= 1e-3 * abs(base)), t
     with at.ScheduledEngine(s) as e:
