@@ -58,11 +58,6 @@ struct acvd_ctx {
     DBuf<int> color_items, cand_dest, cand_list;
     // acvd_adjoint_on_stream: orders the context's stream after the caller's and back
     cudaEvent_t adj_ev_in = nullptr, adj_ev_out = nullptr;
-    // The bulk host <-> device copies of the set-up and of the labels go on their own
-    // stream, joined to s by events: on GB300, copies queued on the stream that has run
-    // the sweep graphs moved at 30-60 GB/s where a stream of their own moves 211 GB/s.
-    cudaStream_t s_copy = nullptr;
-    cudaEvent_t copy_ev_in = nullptr, copy_ev_out = nullptr;
     // split evaluation of large colour classes (screen pass + work list)
     DBuf<int> work;
     DBuf<unsigned> work_count;
@@ -581,9 +576,6 @@ void acvd_destroy(acvd_ctx* ctx) {
     if (ctx->h_raw) cudaFreeHost(ctx->h_raw);
     if (ctx->h_color) cudaFreeHost(ctx->h_color);
     if (ctx->adj_ev_in) cudaEventDestroy(ctx->adj_ev_in);
-    if (ctx->copy_ev_in) cudaEventDestroy(ctx->copy_ev_in);
-    if (ctx->copy_ev_out) cudaEventDestroy(ctx->copy_ev_out);
-    if (ctx->s_copy) cudaStreamDestroy(ctx->s_copy);
     if (ctx->adj_ev_out) cudaEventDestroy(ctx->adj_ev_out);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
@@ -594,25 +586,6 @@ void acvd_destroy(acvd_ctx* ctx) {
 const char* acvd_last_error(const acvd_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
 
 void* acvd_stream(acvd_ctx* ctx) { return ctx ? (void*)ctx->s : nullptr; }
-
-// copy_fork: the copy stream waits for the work queued on s so far; copies then go on
-// ctx->s_copy; copy_join: s waits for them.
-static int copy_fork(acvd_ctx* ctx) {
-    if (!ctx->s_copy) {
-        CK(cudaStreamCreateWithFlags(&ctx->s_copy, cudaStreamNonBlocking));
-        CK(cudaEventCreateWithFlags(&ctx->copy_ev_in, cudaEventDisableTiming));
-        CK(cudaEventCreateWithFlags(&ctx->copy_ev_out, cudaEventDisableTiming));
-    }
-    CK(cudaEventRecord(ctx->copy_ev_in, ctx->s));
-    CK(cudaStreamWaitEvent(ctx->s_copy, ctx->copy_ev_in, 0));
-    return ACVD_OK;
-}
-
-static int copy_join(acvd_ctx* ctx) {
-    CK(cudaEventRecord(ctx->copy_ev_out, ctx->s_copy));
-    CK(cudaStreamWaitEvent(ctx->s, ctx->copy_ev_out, 0));
-    return ACVD_OK;
-}
 
 int acvd_set_mesh(acvd_ctx* ctx, int64_t n_vertices, const double* xyz, int64_t n_faces, const int32_t* tri,
                   const int32_t* csr_row, const int32_t* csr_col, int64_t n_edges, const int32_t* edge_v) {
@@ -638,18 +611,11 @@ int acvd_set_mesh(acvd_ctx* ctx, int64_t n_vertices, const double* xyz, int64_t 
     CK(ctx->col.resize(2 * n_edges));
     CK(ctx->edge_v.resize(2 * n_edges));
     CK(ctx->adj.resize(2 * n_edges));
-    {
-        int r = copy_fork(ctx);
-        if (r) return r;
-        cudaStream_t cs = ctx->s_copy;
-        CK(cudaMemcpyAsync(ctx->xyz.p, xyz, 3 * n_vertices * sizeof(double), cudaMemcpyHostToDevice, cs));
-        CK(cudaMemcpyAsync(ctx->tri.p, tri, 3 * n_faces * sizeof(int), cudaMemcpyHostToDevice, cs));
-        CK(cudaMemcpyAsync(ctx->row.p, csr_row, (n_vertices + 1) * sizeof(int), cudaMemcpyHostToDevice, cs));
-        CK(cudaMemcpyAsync(ctx->col.p, csr_col, 2 * n_edges * sizeof(int), cudaMemcpyHostToDevice, cs));
-        CK(cudaMemcpyAsync(ctx->edge_v.p, edge_v, 2 * n_edges * sizeof(int), cudaMemcpyHostToDevice, cs));
-        r = copy_join(ctx);
-        if (r) return r;
-    }
+    CK(cudaMemcpyAsync(ctx->xyz.p, xyz, 3 * n_vertices * sizeof(double), cudaMemcpyHostToDevice, ctx->s));
+    CK(cudaMemcpyAsync(ctx->tri.p, tri, 3 * n_faces * sizeof(int), cudaMemcpyHostToDevice, ctx->s));
+    CK(cudaMemcpyAsync(ctx->row.p, csr_row, (n_vertices + 1) * sizeof(int), cudaMemcpyHostToDevice, ctx->s));
+    CK(cudaMemcpyAsync(ctx->col.p, csr_col, 2 * n_edges * sizeof(int), cudaMemcpyHostToDevice, ctx->s));
+    CK(cudaMemcpyAsync(ctx->edge_v.p, edge_v, 2 * n_edges * sizeof(int), cudaMemcpyHostToDevice, ctx->s));
     {
         // every id in range before any kernel indexes with it
         CK(ctx->dtmp.resize(2));
@@ -708,18 +674,13 @@ int acvd_set_metric(acvd_ctx* ctx, int metric, const double* indicator, const fl
     DBuf<double>&ind = ctx->setup.ind, &farea = ctx->setup.farea, &fnorm = ctx->setup.fnorm, &wd = ctx->setup.wd,
                 &varea = ctx->setup.varea, &wsum = ctx->setup.wsum;
     DBuf<float>& pd = ctx->setup.pd;
-    if (use_ind) CK(ind.resize(nv));
-    if (metric == kAniso) CK(pd.resize(6 * nv));
-    if (use_ind || metric == kAniso) {
-        int r = copy_fork(ctx);
-        if (r) return r;
-        if (use_ind)
-            CK(cudaMemcpyAsync(ind.p, indicator, nv * sizeof(double), cudaMemcpyHostToDevice, ctx->s_copy));
-        if (metric == kAniso)
-            CK(cudaMemcpyAsync(pd.p, principal_dirs, 6 * nv * sizeof(float), cudaMemcpyHostToDevice,
-                               ctx->s_copy));
-        r = copy_join(ctx);
-        if (r) return r;
+    if (use_ind) {
+        CK(ind.resize(nv));
+        CK(cudaMemcpyAsync(ind.p, indicator, nv * sizeof(double), cudaMemcpyHostToDevice, ctx->s));
+    }
+    if (metric == kAniso) {
+        CK(pd.resize(6 * nv));
+        CK(cudaMemcpyAsync(pd.p, principal_dirs, 6 * nv * sizeof(float), cudaMemcpyHostToDevice, ctx->s));
     }
     CK(farea.resize(nf));
     CK(fnorm.resize(3 * nf));
@@ -869,13 +830,7 @@ int acvd_set_labels(acvd_ctx* ctx, int32_t k, const int32_t* labels) {
     (void)ms;
     CK(ctx->label_init.resize(ctx->nV));
     CK(ctx->label_orig.resize(ctx->nV));
-    {
-        int r = copy_fork(ctx);
-        if (r) return r;
-        CK(cudaMemcpyAsync(ctx->label_orig.p, labels, ctx->nV * sizeof(int), cudaMemcpyHostToDevice, ctx->s_copy));
-        r = copy_join(ctx);
-        if (r) return r;
-    }
+    CK(cudaMemcpyAsync(ctx->label_orig.p, labels, ctx->nV * sizeof(int), cudaMemcpyHostToDevice, ctx->s));
     // the range check runs in the gather: a label outside [0, K] fails the call
     CK(ctx->dtmp.resize(2));
     unsigned* bad = (unsigned*)ctx->dtmp.p;
@@ -1689,10 +1644,8 @@ extern "C" int acvd_get_labels(acvd_ctx* ctx, int32_t* labels) {
     CK(cudaSetDevice(ctx->opts.device));
     CK(ctx->label_orig.resize(ctx->nV));
     CK(launch_gather_i32(ctx->label.p, ctx->inv.p, ctx->nV, ctx->label_orig.p, ctx->s));
-    int r = copy_fork(ctx);
-    if (r) return r;
-    CK(cudaMemcpyAsync(labels, ctx->label_orig.p, ctx->nV * sizeof(int), cudaMemcpyDeviceToHost, ctx->s_copy));
-    CK(cudaStreamSynchronize(ctx->s_copy));
+    CK(cudaMemcpyAsync(labels, ctx->label_orig.p, ctx->nV * sizeof(int), cudaMemcpyDeviceToHost, ctx->s));
+    CK(cudaStreamSynchronize(ctx->s));
     return ACVD_OK;
 }
 
