@@ -1656,7 +1656,6 @@ __global__ void comp_step_kernel(DevState st, int* __restrict__ comp) {
 // ids decrease along every chain and each set's root is its smallest-id item.  Concurrent
 // links race through atomicCAS on the root's slot; a failed CAS retries from the new
 // roots.  Finding a root halves the path (writes of an ancestor, benign under races).
-constexpr int kUnionTries = 1 << 16;   // retries of one link before the pass gives up
 
 __device__ __forceinline__ int uf_root(int* parent, int x) {
     for (;;) {
@@ -1673,7 +1672,7 @@ __global__ void uf_init_kernel(DevState st, int* __restrict__ parent) {
     if (i < st.n) parent[i] = (int)i;
 }
 
-__global__ void uf_link_kernel(DevState st, int* parent) {
+__global__ void uf_link_kernel(DevState st, int* parent, int tries) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= st.n) return;
     const int L = st.label[i];
@@ -1684,7 +1683,7 @@ __global__ void uf_link_kernel(DevState st, int* parent) {
         if (j <= (int)i || st.label[j] != L) continue;   // each same-cluster edge once
         int a = uf_root(parent, (int)i), b = uf_root(parent, j);
         int t = 0;
-        for (; t < kUnionTries && a != b; t++) {
+        for (; t < tries && a != b; t++) {
             if (st.orig[a] > st.orig[b]) {
                 const int x = a;
                 a = b;
@@ -1696,7 +1695,7 @@ __global__ void uf_link_kernel(DevState st, int* parent) {
             a = uf_root(parent, a);
             b = uf_root(parent, old);
         }
-        gave_up += t == kUnionTries;
+        gave_up += a != b && t == tries;
     }
     if (gave_up) atomicAdd(ctr(st.counters, kCntChanged), (unsigned long long)gave_up);
 }
@@ -2215,10 +2214,10 @@ cudaError_t launch_comp_step(const DevState& st, int* comp, cudaStream_t s) {
     return cudaGetLastError();
 }
 
-cudaError_t launch_comp_union(const DevState& st, int* comp, int* parent, cudaStream_t s) {
+cudaError_t launch_comp_union(const DevState& st, int* comp, int* parent, int tries, cudaStream_t s) {
     g_launches += 3;
     uf_init_kernel<<<nblk(st.n), 256, 0, s>>>(st, parent);
-    uf_link_kernel<<<nblk(st.n), 256, 0, s>>>(st, parent);
+    uf_link_kernel<<<nblk(st.n), 256, 0, s>>>(st, parent, tries);
     uf_flatten_kernel<<<nblk(st.n), 256, 0, s>>>(st, parent, comp);
     return cudaGetLastError();
 }

@@ -107,6 +107,7 @@ struct acvd_ctx {
     DBuf<unsigned> fill_cnt;
     DBuf<int64_t> fill_off;
     int64_t fill_block_max = 65536;   // ACVD_FILL_BLOCK_MAX: longest lists the single-block fill takes
+    int union_tries = 1 << 16;        // ACVD_UNION_TRIES: attempts per union-find link before the fallback
     DBuf<unsigned long long> claim;
     DBuf<SweepState> dsweep;
     // relaxed steps
@@ -543,6 +544,7 @@ acvd_ctx* acvd_create(const acvd_opts* opts) {
     if (const char* c = std::getenv("ACVD_SWEEP_COLORS")) ctx->sweep_by_color = std::atoi(c) != 0;
     if (const char* c = std::getenv("ACVD_RELAXED")) ctx->use_relaxed = std::atoi(c) != 0;
     if (const char* b = std::getenv("ACVD_EVAL_BLOCKS")) ctx->eval_blocks = std::atoi(b);
+    if (const char* u = std::getenv("ACVD_UNION_TRIES")) ctx->union_tries = std::max(0, std::atoi(u));
     if (const char* f = std::getenv("ACVD_FILL_BLOCK_MAX"))
         ctx->fill_block_max = std::max<int64_t>(0, std::min<int64_t>(std::atoll(f), 1ll << 30));
     if (const char* t = std::getenv("ACVD_EVAL_THREADS")) {
@@ -1027,11 +1029,12 @@ static int clean(acvd_ctx* ctx, int* n_disconnected) {
     CK(ctx->csize.resize(n));
     CK(ctx->multi.resize(ctx->K + 1));
     CK(ctx->best.resize(ctx->K + 1));
-    // union-find in one pass; should a link give up (a bound, never met in practice),
-    // min-id propagation with pointer jumping gives the same components
+    // union-find in one pass; should a link give up (after union_tries attempts, a bound
+    // never met in practice at the default), min-id propagation with pointer jumping
+    // gives the same components
     CK(ctx->uf_parent.resize(n));
     CK(zero_counter(ctx, kCntChanged));
-    CK(launch_comp_union(st, ctx->comp.p, ctx->uf_parent.p, ctx->s));
+    CK(launch_comp_union(st, ctx->comp.p, ctx->uf_parent.p, ctx->union_tries, ctx->s));
     {
         int r = sync_counters(ctx);
         if (r) return r;

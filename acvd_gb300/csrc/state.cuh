@@ -358,9 +358,9 @@ cudaError_t launch_reduce_clusters(int metric, const DevState& st, const uint32_
                                    const uint32_t* seg_off, const uint32_t* seg_cnt, cudaStream_t s);
 cudaError_t launch_comp_init(const DevState& st, int* comp, cudaStream_t s);
 cudaError_t launch_comp_step(const DevState& st, int* comp, cudaStream_t s);
-// the components in one union-find pass; kCntChanged counts links it gave up on
-// (then the propagation above runs instead)
-cudaError_t launch_comp_union(const DevState& st, int* comp, int* parent, cudaStream_t s);
+// the components in one union-find pass, at most `tries` attempts per link; kCntChanged
+// counts links it gave up on (then the propagation above runs instead)
+cudaError_t launch_comp_union(const DevState& st, int* comp, int* parent, int tries, cudaStream_t s);
 cudaError_t launch_comp_finish(const DevState& st, const int* comp, int* csize, unsigned long long* best,
                                int* multi, cudaStream_t s);
 // hole filling over lists of the unassigned items: collect them per colour class

@@ -140,8 +140,15 @@ def test_remesh_keeps_fixed_vertices():
     np.testing.assert_array_equal(r.GetClustering()[fixed], np.arange(len(fixed)))
 
 
+@pytest.mark.parametrize("union_tries", [None, 0])
 @pytest.mark.parametrize("with_fixed", [False, True])
-def test_clean_clustering_equals_oracle(oracle_lib, with_fixed):
+def test_clean_clustering_equals_oracle(oracle_lib, with_fixed, union_tries, monkeypatch):
+    # the components by union-find (default), and by the min-id propagation it falls back
+    # to when a link gives up (ACVD_UNION_TRIES=0, read when the engine is created)
+    if union_tries is None:
+        monkeypatch.delenv("ACVD_UNION_TRIES", raising=False)
+    else:
+        monkeypatch.setenv("ACVD_UNION_TRIES", str(union_tries))
     m = synth.icosphere(4, seed=3)
     rng = np.random.default_rng(5)
     k = 60
