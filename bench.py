@@ -1410,7 +1410,7 @@ def plain_form_block(args, steps, warmup):
 
 
 DEFAULT_WORKLOAD = "torus_1024x512_qem"
-# the default run adds the configurations the HBM roofline is judged on (single GPU only)
+# the default run adds the configurations whose evaluation is HBM-bound (single GPU only)
 EXTRA_WORKLOADS = ("heightfield_4096_aniso", "batch_256_qem")
 
 
