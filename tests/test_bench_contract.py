@@ -1,7 +1,8 @@
 """CPU checks of bench.py's reporting helpers: the per-launch DRAM traffic table
 (profiles/eval_traffic.json) is well formed and is looked up by workload and colouring,
-and the roofline block computes its fraction from the instrumented pass's bytes and
-event time against the measured copy bandwidth."""
+the roofline block computes its fraction from the instrumented pass's bytes and
+event time against the measured copy bandwidth, and the reference arm prints the
+contract's line without ever mapping the CUDA library."""
 import importlib.util
 import json
 import os
@@ -60,3 +61,35 @@ def test_roofline_block_fraction(bench):
     rp = bench.roofline_block(True, tot_p, "heightfield_4096_aniso", "jp")
     assert rp["kernel"] == "sweep_run_kernel" and rp["traffic"] is None
     assert rp["achieved"] == pytest.approx(1500.0)
+
+
+RUNNER = r"""
+import runpy, sys
+sys.argv = ["bench.py", "--impl", "reference", "--workload", "icosphere_l5_iso", "--steps", "2", "--warmup", "1"]
+runpy.run_path("bench.py", run_name="__main__")
+with open("/proc/self/maps") as f:
+    libs = sorted({l.split()[-1] for l in f if ".so" in l})
+print("MAPPED " + " ".join(libs))
+"""
+
+
+def test_reference_arm_line_and_no_cuda_library():
+    """The reference arm on a small workload: one JSON line with the contract's keys, a
+    cpu_baseline describing this run, an e2e block with no copies, a connected clustering
+    -- and the process never maps the CUDA library (the arm runs the oracle's threaded
+    restatement only)."""
+    import subprocess
+    r = subprocess.run([sys.executable, "-c", RUNNER], cwd=ROOT, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1, r.stdout
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["steps"] == 2 and d["warmup"] == 1
+    assert d["unit"] == "items/s" and d["higher_is_better"] is True and d["value"] > 0
+    assert d["config"]["workload"] == "icosphere_l5_iso"
+    cb = d["cpu_baseline"]
+    assert cb["value"] == d["value"] and cb["cores"] >= 1 and cb["kind"] in ("port", "reference") and cb["sample"]
+    assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    assert d["energy"]["all_clusters_connected"] is True
+    mapped = [l for l in r.stdout.splitlines() if l.startswith("MAPPED ")][0]
+    assert "libacvd_gb300" not in mapped, mapped
