@@ -142,6 +142,9 @@ class _DiscreteRemeshing:
         self.MinCustomDensity = 0.1
         self.CustomDensityMultiplicationFactor = 0.001
         self._anchors = {}                # QEM Cluster::AnchorItem, by cluster
+        self.EdgeOptimization = 0          # vtkDiscreteRemeshing.h:74, default :1193 (stored, never read)
+        self.OutputDirectory = None        # vtkUniformClustering.h:126, default :1412
+        self.FileLoadSaveOption = 0        # vtkDiscreteRemeshing.h:67
 
     @classmethod
     def New(cls, device: int = 0):
@@ -206,6 +209,48 @@ class _DiscreteRemeshing:
         only 0 is accepted; the final energy is in Stats['energy']."""
         if on:
             raise _eng.AcvdError(5, "the global energy log is not available; read Stats['energy']")
+
+    def SetComputeAndSaveEnergy(self, on: int):
+        """The setter behind SetWriteToGlobalEnergyLog (vtkUniformClustering.h:123, :307)."""
+        self.SetWriteToGlobalEnergyLog(on)
+
+    def SetEdgeOptimization(self, on: int):
+        """Stored as the reference stores it (vtkDiscreteRemeshing.h:74); nothing reads it."""
+        self.EdgeOptimization = int(on)
+
+    def SetOutputDirectory(self, path):
+        """Stored (vtkUniformClustering.h:126).  The reference uses it only to name the
+        global energy log (:670-675), which is not written here."""
+        self.OutputDirectory = None if path is None else str(path)
+
+    def SetFileLoadSaveOption(self, on: int):
+        """The reference's FileLoadSaveOption asks on standard input whether to compute the
+        curvature and the clustering or load them from curvature.dat / clustering.dat
+        (vtkDiscreteRemeshing.h:591-700, :885-932).  The interactive prompts are not kept:
+        0 is accepted; the files are read and written by SaveCurvature / LoadCurvature /
+        SaveClustering / LoadClustering."""
+        if on:
+            raise _eng.AcvdError(5, "FileLoadSaveOption's prompts are not available; use SaveClustering / "
+                                    "LoadClustering / SaveCurvature / LoadCurvature")
+        self.FileLoadSaveOption = 0
+
+    def FixClusteringToVoronoi(self):
+        """A no-op, as in the reference, whose body is commented out
+        (vtkDiscreteRemeshing.h:386-423)."""
+
+    def GetDualItemNeighbourClusters(self, face: int) -> list:
+        """The distinct clusters of a dual item -- an input face when the items are vertices
+        -- in the order of its vertices, unassigned vertices left out
+        (vtkDiscreteRemeshing.h:956-1000, ClusteringType 1)."""
+        if self.Clustering is None or self.Input is None:
+            raise _eng.AcvdError(1, "no clustering")
+        k = self.NumberOfClusters
+        out = []
+        for v in self.Input.faces[int(face)]:
+            c = int(self.Clustering[int(v)])
+            if c < k and c not in out:
+                out.append(c)
+        return out
 
     def GetNumberOfItems(self) -> int:
         return 0 if self.Input is None else self.Input.GetNumberOfPoints()
@@ -410,7 +455,7 @@ class _DiscreteRemeshing:
         e = self._engine
         passes = 0
         while True:
-            n = e.force_manifold_step()
+            n = self.DetectNonManifoldOutputVertices()
             if n == 0:
                 break
             if self.ConsoleOutput:
@@ -425,6 +470,14 @@ class _DiscreteRemeshing:
         self.NumberOfManifoldPasses = passes
         self.NumberOfClusters = e.k
         self.Clustering = e.labels()
+
+    def DetectNonManifoldOutputVertices(self) -> int:
+        """One detection pass of the ForceManifold loop (vtkDiscreteRemeshing.h:166-383) on
+        the current clustering: the issues found, with the reference's side effects (the
+        new clusters, the frozen set) applied to the context."""
+        if self._engine is None:
+            raise _eng.AcvdError(1, "no clustering: call ProcessClustering or Remesh first")
+        return self._engine.force_manifold_step()
 
     def FixMeshBoundaries(self) -> bool:
         """FixMeshBoundaries (vtkDiscreteRemeshing.h:426-579): appends the boundary

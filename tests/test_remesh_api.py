@@ -1,5 +1,6 @@
 """Reference setters of the Python remesher that act before any solve: initial sampling
-type, convergence cap, energy-driven loop, energy log, cluster sizes (CPU only)."""
+type, convergence cap, energy-driven loop, energy log, the remaining stored or refused
+options, cluster sizes and a dual item's clusters (CPU), and two solves on the GPU."""
 import numpy as np
 import pytest
 
@@ -63,6 +64,51 @@ def test_cluster_sizes():
     with pytest.raises(IndexError):
         r.GetClusterSize(20)
     assert acvd_gb300.IsotropicDiscreteRemeshing.New().GetNumberOfItems() == 0
+
+
+def test_remaining_reference_setters():
+    """SetEdgeOptimization and SetOutputDirectory are stored (nothing on the path reads
+    them); SetComputeAndSaveEnergy is SetWriteToGlobalEnergyLog; SetFileLoadSaveOption's
+    interactive prompts are refused; FixClusteringToVoronoi is the reference's no-op."""
+    r = _remesher()
+    assert r.EdgeOptimization == 0 and r.OutputDirectory is None and r.FileLoadSaveOption == 0
+    r.SetEdgeOptimization(1)
+    r.SetOutputDirectory("/tmp/out")
+    r.SetComputeAndSaveEnergy(0)
+    r.SetFileLoadSaveOption(0)
+    assert r.EdgeOptimization == 1 and r.OutputDirectory == "/tmp/out"
+    for call in (lambda: r.SetComputeAndSaveEnergy(1), lambda: r.SetFileLoadSaveOption(1)):
+        with pytest.raises(acvd_gb300.AcvdError) as err:
+            call()
+        assert err.value.code == 5
+    r.Clustering = np.arange(162, dtype=np.int32) % 20
+    before = r.Clustering.copy()
+    assert r.FixClusteringToVoronoi() is None
+    np.testing.assert_array_equal(r.Clustering, before)
+
+
+def test_dual_item_neighbour_clusters():
+    """A face's distinct clusters in its vertex order, unassigned vertices left out
+    (vtkDiscreteRemeshing.h:956-1000)."""
+    r = _remesher()
+    with pytest.raises(acvd_gb300.AcvdError):
+        r.GetDualItemNeighbourClusters(0)
+    faces = r.Input.faces
+    lab = np.full(162, 20, dtype=np.int32)          # all unassigned
+    a, b, c = (int(v) for v in faces[5])
+    lab[a], lab[b], lab[c] = 7, 3, 7
+    r.Clustering = lab
+    assert r.GetDualItemNeighbourClusters(5) == [7, 3]
+    lab[b] = 20
+    assert r.GetDualItemNeighbourClusters(5) == [7]
+    lab[a] = lab[c] = 20
+    assert r.GetDualItemNeighbourClusters(5) == []
+
+
+def test_manifold_detection_needs_a_clustering():
+    r = _remesher()
+    with pytest.raises(acvd_gb300.AcvdError):
+        r.DetectNonManifoldOutputVertices()
 
 
 def test_engine_takes_the_convergence_cap():
